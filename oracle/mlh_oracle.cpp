@@ -1,0 +1,880 @@
+// TEST INFRASTRUCTURE (oracle).  Not part of the product: only tests/, the
+// smoke check and bench.py's CPU baseline load this library, as the checker.
+//
+// A plain, serial CPU restatement of one MFV (meshless finite volume) step of
+// the reference demonstrator, jammartin/meshlessHydro.  Every stage follows the
+// reference method it names, with the same floating-point expression order, so
+// that on identical inputs it reproduces the reference's numbers (bit for bit
+// where the reference's own arithmetic is used; see the notes on the matrix
+// inverse and on the Riemann solver).
+//
+// Stage order: demonstrator/src/MeshlessScheme.cpp:39-253.
+//
+// Differences from the reference, all deliberate:
+//  * Matrix inverse: closed-form adjugate / determinant instead of LAPACK
+//    dgetrf_+dgetri_ (demonstrator/src/Helper.cpp:7-18).  Agrees to rounding.
+//  * Exact Riemann solver: own restatement of Toro ch. 4 (riemann_exact.hpp);
+//    the reference's third-party RiemannSolver.hpp is not in its tree.
+//  * Periodic images: the reference builds explicit ghost copies and searches
+//    them by brute force (Particles.cpp:2113-2260, 2D only).  This restatement
+//    finds the same images through the wrapped cell stencil and orders them by
+//    parent index, which is the reference's ghost order (ghosts are created in
+//    parent order, one image of a parent at most lies within h when every
+//    periodic axis has >= 3 cells).  It extends that arithmetic per axis to 3D.
+//  * In 3D with FIRST_ORDER_QUAD_POINT the reference reads an uninitialised
+//    xjxi[2] in the pairwise limiter (Particles.cpp:1498-1539, 1623-1631); this
+//    restatement uses z_j - z_i.
+//  * Errors set bits in the returned status instead of calling exit().
+#include "mlh_oracle.h"
+#include "riemann_exact.hpp"
+
+#include <algorithm>
+#include <cfloat>
+#include <climits>
+#include <cmath>
+#include <cstdint>
+#include <cstring>
+#include <limits>
+#include <string>
+#include <vector>
+
+namespace {
+
+enum Status {
+    ST_OK = 0,
+    ST_NEG_PRESSURE = 1 << 1,
+    ST_NEG_DENSITY = 1 << 2,
+    ST_NEG_MASS = 1 << 3,
+    ST_NEG_ENERGY = 1 << 4,
+    ST_NEWTON = 1 << 5,
+    ST_VACUUM = 1 << 6,
+    ST_GRID = 1 << 7,
+    ST_NO_NEIGHBOUR = 1 << 8,
+};
+
+const unsigned IMG_SHIFT = 29;
+const unsigned IDX_MASK = (1u << IMG_SHIFT) - 1u;
+
+// abs() as the reference binds it.  With only <cmath>/<iostream> visible, the
+// unqualified abs(double) at Particles.cpp:1416-1417, 1748-1749, 1754, 1759
+// resolves to int ::abs(int): the double is truncated (x86 cvttsd2si gives
+// INT_MIN for NaN and out-of-range values, and abs(INT_MIN) stays INT_MIN).
+inline double ref_abs(double x, int int_abs) {
+    if (!int_abs) return std::fabs(x);
+    int t;
+    if (!(x > -2147483649.0 && x < 2147483648.0)) t = INT_MIN;
+    else t = (int)x;
+    if (t == INT_MIN) return (double)INT_MIN;
+    return (double)(t < 0 ? -t : t);
+}
+
+template <int D>
+struct Sim {
+    orc_config c;
+    int N;
+    double h;
+    std::vector<double> X[3], V[3], m, u, rho, P, omega;
+    // gradients in the reference's call order: rho, vx, vy, (vz), P
+    std::vector<double> G[5];          // [field][i*3+alpha]
+    std::vector<double> Graw[5];       // unlimited copies (for tests)
+    std::vector<double> B;             // inverse of E_i, D*D per particle
+    // neighbour lists: real neighbours first (grid stencil order), then
+    // periodic images ordered by parent index
+    std::vector<int> off, noi, noiImg;
+    std::vector<uint32_t> nb;
+    std::vector<int> rev;              // slot of i in the neighbour's list
+    std::vector<double> psi, Aij, WL, WR, vFrame, F;
+    std::vector<double> mF, vF, eF;
+    std::vector<int> newtonIters;
+    double dt = 0.;
+    double lo[3], hi[3];
+    int cells[3];
+    double cellSize[3];
+    std::vector<int> cellOf;
+    std::vector<std::vector<int>> grid;
+    unsigned status = 0;
+    long riemannSolves = 0, newtonTotal = 0;
+
+    // --- Kernel::cubicSpline, demonstrator/src/Particles.cpp:7-24
+    double kernel(double r) const {
+        double h2 = h / 2.;
+        double sigma = (D == 2) ? 10. / (7. * M_PI * h2 * h2) : 1. / (M_PI * h2 * h2 * h2);
+        double q = r / h2;
+        if (0. <= q && q <= 1.) return sigma * (1. - 3. / 2. * q * q * (1. - q / 2.));
+        else if (1. < q && q < 2.) return sigma / 4. * std::pow(2. - q, 3.);
+        return 0.;
+    }
+
+    // field accessor in gradient order
+    const std::vector<double> &field(int f) const {
+        if (f == 0) return rho;
+        if (f == D + 1) return P;
+        return V[f - 1];
+    }
+    int nfields() const { return D + 2; }
+
+    // image coordinate of a particle coordinate along axis a, ghost rule of
+    // Particles.cpp:2123-2142 (returns false when the particle has no image)
+    bool image(int a, double xa, double &out) const {
+        if (xa <= lo[a] + h) { out = hi[a] + (xa - lo[a]); return true; }
+        else if (hi[a] - h < xa) { out = lo[a] - (hi[a] - xa); return true; }
+        return false;
+    }
+    // coordinates of neighbour entry e (index + image bits)
+    void coords(uint32_t e, double *xj) const {
+        int j = (int)(e & IDX_MASK);
+        for (int a = 0; a < D; ++a) {
+            xj[a] = X[a][j];
+            if (e & (1u << (IMG_SHIFT + a))) image(a, X[a][j], xj[a]);
+        }
+    }
+
+    // --- Particles::getDomainLimits, Particles.cpp:228-267 (else-if and
+    // numeric_limits<double>::min() kept)
+    void domainLimits() {
+        for (int a = 0; a < D; ++a) { lo[a] = std::numeric_limits<double>::max(); hi[a] = std::numeric_limits<double>::min(); }
+        for (int i = 0; i < N; ++i)
+            for (int a = 0; a < D; ++a) {
+                if (X[a][i] < lo[a]) lo[a] = X[a][i];
+                else if (X[a][i] > hi[a]) hi[a] = X[a][i];
+            }
+    }
+
+    // --- Domain::createGrid, demonstrator/src/Domain.cpp:9-54
+    void createGrid() {
+        long total = 1;
+        for (int a = 0; a < D; ++a) {
+            cells[a] = (int)std::floor((hi[a] - lo[a]) / h);
+            if (cells[a] < 1) { status |= ST_GRID; cells[a] = 1; }
+            total *= cells[a];
+        }
+        for (int a = 0; a < D; ++a) cellSize[a] = (hi[a] - lo[a]) / (double)cells[a];
+        if (c.periodic)
+            for (int a = 0; a < D; ++a) if (cells[a] < 3) status |= ST_GRID;
+        grid.assign(total, std::vector<int>());
+    }
+
+    // --- Particles::assignParticlesAndCells, Particles.cpp:270-322
+    void assign() {
+        for (auto &g : grid) g.clear();
+        cellOf.assign(N, 0);
+        for (int i = 0; i < N; ++i) {
+            int fl[3] = {0, 0, 0};
+            for (int a = 0; a < D; ++a) {
+                fl[a] = (int)std::floor((X[a][i] - lo[a]) / cellSize[a]);
+                if (fl[a] == cells[a]) fl[a] -= 1;
+                if (fl[a] < 0 || fl[a] >= cells[a]) { status |= ST_GRID; fl[a] = fl[a] < 0 ? 0 : cells[a] - 1; }
+            }
+            int ic = fl[0] + fl[1] * cells[0] + (D == 3 ? fl[2] * cells[0] * cells[1] : 0);
+            grid[ic].push_back(i);
+            cellOf[i] = ic;
+        }
+    }
+
+    // --- Particles::gridNNS (Particles.cpp:324-365) with the stencil of
+    // Domain::getNeighborCells (Domain.cpp:83-118), plus the periodic images
+    // (Particles::ghostNNS, Particles.cpp:2237-2260) found through wrapped cells.
+    void nns() {
+        const double hSqr = h * h;
+        off.assign(N + 1, 0);
+        noi.assign(N, 0);
+        noiImg.assign(N, 0);
+        std::vector<std::vector<uint32_t>> lists(N);
+        for (int i = 0; i < N; ++i) {
+            int ic = cellOf[i];
+            int ix = ic % cells[0];
+            int iy = (ic / cells[0]) % cells[1];
+            int iz = D == 3 ? ic / (cells[0] * cells[1]) : 0;
+            std::vector<uint32_t> real, img;
+            for (int k = ix - 1; k <= ix + 1; ++k)
+                for (int l = iy - 1; l <= iy + 1; ++l)
+                    for (int mm = (D == 3 ? iz - 1 : 0); mm <= (D == 3 ? iz + 1 : 0); ++mm) {
+                        int cc[3] = {k, l, mm};
+                        unsigned wrap = 0;
+                        bool skip = false;
+                        for (int a = 0; a < D; ++a) {
+                            if (cc[a] < 0 || cc[a] >= cells[a]) {
+                                if (!c.periodic) { skip = true; break; }
+                                cc[a] = cc[a] < 0 ? cc[a] + cells[a] : cc[a] - cells[a];
+                                wrap |= 1u << a;
+                            }
+                        }
+                        if (skip) continue;
+                        int cell = cc[0] + cc[1] * cells[0] + (D == 3 ? cc[2] * cells[0] * cells[1] : 0);
+                        for (int j : grid[cell]) {
+                            if (!wrap) {
+                                if (j == i) continue;
+                                double dSqr = (X[0][j] - X[0][i]) * (X[0][j] - X[0][i])
+                                            + (X[1][j] - X[1][i]) * (X[1][j] - X[1][i]);
+                                if (D == 3) dSqr += (X[2][j] - X[2][i]) * (X[2][j] - X[2][i]);
+                                if (dSqr < hSqr) real.push_back((uint32_t)j);
+                            } else {
+                                double xj[3];
+                                bool ok = true;
+                                for (int a = 0; a < D; ++a) {
+                                    xj[a] = X[a][j];
+                                    if (wrap & (1u << a)) ok = ok && image(a, X[a][j], xj[a]);
+                                }
+                                if (!ok) continue;
+                                double dSqr = (xj[0] - X[0][i]) * (xj[0] - X[0][i])
+                                            + (xj[1] - X[1][i]) * (xj[1] - X[1][i]);
+                                if (D == 3) dSqr += (xj[2] - X[2][i]) * (xj[2] - X[2][i]);
+                                if (dSqr < hSqr) img.push_back((uint32_t)j | (wrap << IMG_SHIFT));
+                            }
+                        }
+                    }
+            std::sort(img.begin(), img.end(), [](uint32_t a, uint32_t b) { return (a & IDX_MASK) < (b & IDX_MASK); });
+            if (real.empty() && img.empty()) status |= ST_NO_NEIGHBOUR;
+            noi[i] = (int)real.size();
+            noiImg[i] = (int)img.size();
+            lists[i] = real;
+            lists[i].insert(lists[i].end(), img.begin(), img.end());
+            off[i + 1] = off[i] + (int)lists[i].size();
+        }
+        nb.resize(off[N]);
+        for (int i = 0; i < N; ++i) std::copy(lists[i].begin(), lists[i].end(), nb.begin() + off[i]);
+        // reverse slots: position of i in the list of its neighbour (for
+        // images: the first image entry of the parent whose parent is i,
+        // Particles.cpp:2514-2516)
+        rev.assign(off[N], -1);
+        for (int i = 0; i < N; ++i)
+            for (int s = off[i]; s < off[i + 1]; ++s) {
+                int j = (int)(nb[s] & IDX_MASK);
+                bool isImg = (s - off[i]) >= noi[i];
+                int b = isImg ? off[j] + noi[j] : off[j];
+                int e = isImg ? off[j + 1] : off[j] + noi[j];
+                for (int t = b; t < e; ++t)
+                    if ((int)(nb[t] & IDX_MASK) == i) { rev[s] = t; break; }
+            }
+    }
+
+    double dist(int i, int s) const {
+        double xj[3];
+        coords(nb[s], xj);
+        double dSqr = (X[0][i] - xj[0]) * (X[0][i] - xj[0]) + (X[1][i] - xj[1]) * (X[1][i] - xj[1]);
+        if (D == 3) dSqr += (X[2][i] - xj[2]) * (X[2][i] - xj[2]);
+        return std::sqrt(dSqr);
+    }
+
+    // --- Particles::compDensity/compOmega, Particles.cpp:1151-1184 and the
+    // image part 2262-2290
+    void density() {
+        omega.assign(N, 0.);
+        for (int i = 0; i < N; ++i) {
+            double omg = 0.;
+            for (int s = off[i]; s < off[i] + noi[i]; ++s) omg += kernel(dist(i, s));
+            omega[i] = omg + kernel(0.);
+            rho[i] = m[i] * omega[i];
+            if (rho[i] <= 0.) status |= ST_NEG_DENSITY;
+        }
+        if (c.periodic)
+            for (int i = 0; i < N; ++i) {
+                double omg = omega[i];
+                for (int s = off[i] + noi[i]; s < off[i + 1]; ++s) omg += kernel(dist(i, s));
+                omega[i] = omg;
+                rho[i] = m[i] * omega[i];
+            }
+    }
+
+    // --- Particles::compPressure, Particles.cpp:1272-1288
+    void pressure() {
+        for (int i = 0; i < N; ++i) {
+            P[i] = (c.gamma - 1.) * rho[i] * u[i];
+            if (P[i] <= 0.) status |= ST_NEG_PRESSURE;
+        }
+    }
+
+    static double dot(const double *a, const double *b) {
+        double r = 0.;
+        for (int k = 0; k < D; ++k) r += a[k] * b[k];
+        return r;
+    }
+
+    // --- Particles::compGlobalTimestep, Particles.cpp:1446-1485 (real
+    // neighbours only, v_sig starting at numeric_limits<double>::min())
+    double globalTimestep() {
+        double dt_ = std::numeric_limits<double>::max();
+        for (int i = 0; i < N; ++i) {
+            double vSig = std::numeric_limits<double>::min();
+            double ci = std::sqrt(c.gamma * P[i] / rho[i]);
+            for (int s = off[i]; s < off[i] + noi[i]; ++s) {
+                int j = (int)(nb[s] & IDX_MASK);
+                double cj = std::sqrt(c.gamma * P[j] / rho[j]);
+                double xij[3], vij[3];
+                for (int a = 0; a < D; ++a) { xij[a] = X[a][i] - X[a][j]; vij[a] = V[a][i] - V[a][j]; }
+                double vijxij = dot(vij, xij) / std::sqrt(dot(xij, xij));
+                vijxij = vijxij < 0. ? vijxij : 0.;
+                double vSig_i = ci + cj - vijxij;
+                vSig = vSig_i > vSig ? vSig_i : vSig;
+            }
+            double dti = c.cfl * h / vSig;
+            dt_ = dti < dt_ ? dti : dt_;
+        }
+        return dt_;
+    }
+
+    // closed-form inverse (replaces Helper::inverseMatrix, Helper.cpp:7-18)
+    static void invert(double *A) {
+        if (D == 2) {
+            double a = A[0], b = A[1], cc = A[2], d = A[3];
+            double det = a * d - b * cc;
+            double id = 1. / det;
+            A[0] = d * id; A[1] = -b * id; A[2] = -cc * id; A[3] = a * id;
+        } else {
+            double a00 = A[0], a01 = A[1], a02 = A[2], a10 = A[3], a11 = A[4], a12 = A[5], a20 = A[6], a21 = A[7], a22 = A[8];
+            double c00 = a11 * a22 - a12 * a21;
+            double c01 = a12 * a20 - a10 * a22;
+            double c02 = a10 * a21 - a11 * a20;
+            double det = a00 * c00 + a01 * c01 + a02 * c02;
+            double id = 1. / det;
+            A[0] = c00 * id;
+            A[1] = (a02 * a21 - a01 * a22) * id;
+            A[2] = (a01 * a12 - a02 * a11) * id;
+            A[3] = c01 * id;
+            A[4] = (a00 * a22 - a02 * a20) * id;
+            A[5] = (a02 * a10 - a00 * a12) * id;
+            A[6] = c02 * id;
+            A[7] = (a01 * a20 - a00 * a21) * id;
+            A[8] = (a00 * a11 - a01 * a10) * id;
+        }
+    }
+
+    // --- Particles::compPsijTilde, Particles.cpp:1186-1254 / 2292-2455
+    void psijTilde() {
+        B.assign((size_t)N * D * D, 0.);
+        psi.assign((size_t)off[N] * 3, 0.);
+        for (int i = 0; i < N; ++i) {
+            double Bi[9] = {0};
+            double xi[3];
+            for (int a = 0; a < D; ++a) xi[a] = X[a][i];
+            for (int s = off[i]; s < off[i + 1]; ++s) {
+                double r = dist(i, s);
+                double psij_xi = kernel(r) / omega[i];
+                double xj[3];
+                coords(nb[s], xj);
+                for (int al = 0; al < D; ++al)
+                    for (int be = 0; be < D; ++be)
+                        Bi[D * al + be] += (xj[al] - xi[al]) * (xj[be] - xi[be]) * psij_xi;
+            }
+            invert(Bi);
+            for (int k = 0; k < D * D; ++k) B[(size_t)i * D * D + k] = Bi[k];
+            for (int s = off[i]; s < off[i + 1]; ++s) {
+                double r = dist(i, s);
+                double psij_xi = kernel(r) / omega[i];
+                double xj[3];
+                coords(nb[s], xj);
+                for (int al = 0; al < D; ++al) {
+                    double p = 0.;
+                    for (int be = 0; be < D; ++be) p += Bi[D * al + be] * (xj[be] - xi[be]) * psij_xi;
+                    psi[(size_t)s * 3 + al] = p;
+                }
+            }
+        }
+    }
+
+    // --- Particles::gradient, Particles.cpp:1257-1270 / 2457-2502
+    void gradients() {
+        for (int f = 0; f < nfields(); ++f) {
+            const std::vector<double> &fv = field(f);
+            G[f].assign((size_t)N * 3, 0.);
+            for (int i = 0; i < N; ++i)
+                for (int s = off[i]; s < off[i + 1]; ++s) {
+                    int j = (int)(nb[s] & IDX_MASK);
+                    for (int a = 0; a < D; ++a) G[f][(size_t)i * 3 + a] += (fv[j] - fv[i]) * psi[(size_t)s * 3 + a];
+                }
+            Graw[f] = G[f];
+        }
+    }
+
+    // --- Particles::slopeLimiter, Particles.cpp:1313-1444
+    void slopeLimiter() {
+        for (int f = 0; f < nfields(); ++f) {
+            const std::vector<double> &fv = field(f);
+            for (int i = 0; i < N; ++i) {
+                double psiMaxNgb = std::numeric_limits<double>::min();
+                double psiMinNgb = std::numeric_limits<double>::max();
+                double psiMaxMid = std::numeric_limits<double>::min();
+                double psiMinMid = std::numeric_limits<double>::max();
+                double *g = &G[f][(size_t)i * 3];
+                for (int s = off[i]; s < off[i + 1]; ++s) {
+                    int j = (int)(nb[s] & IDX_MASK);
+                    double xj[3], xij[3], xijxi[3];
+                    coords(nb[s], xj);
+                    for (int a = 0; a < D; ++a) {
+                        if (c.first_order_quad_point) xij[a] = (X[a][i] + xj[a]) / 2.;
+                        else xij[a] = X[a][i] + h / 4. * (xj[a] - X[a][i]);
+                        xijxi[a] = xij[a] - X[a][i];
+                    }
+                    if (psiMaxNgb < fv[j]) psiMaxNgb = fv[j];
+                    if (psiMinNgb > fv[j]) psiMinNgb = fv[j];
+                    double fij = fv[i] + dot(g, xijxi);
+                    if (psiMaxMid < fij) psiMaxMid = fij;
+                    if (psiMinMid > fij) psiMinMid = fij;
+                }
+                double alphaMax = ref_abs((psiMaxNgb - fv[i]) / (psiMaxMid - fv[i]), c.int_abs);
+                double alphaMin = ref_abs((fv[i] - psiMinNgb) / (fv[i] - psiMinMid), c.int_abs);
+                if (alphaMin <= alphaMax && c.beta * alphaMin < 1.) {
+                    for (int a = 0; a < D; ++a) g[a] *= alphaMin;
+                } else if (alphaMax <= alphaMin && c.beta * alphaMax < 1.) {
+                    for (int a = 0; a < D; ++a) g[a] *= alphaMax;
+                }
+            }
+        }
+    }
+
+    // --- Particles::compEffectiveFace, Particles.cpp:1290-1311 / 2504-2531
+    void effectiveFace() {
+        Aij.assign((size_t)off[N] * 3, 0.);
+        for (int i = 0; i < N; ++i)
+            for (int s = off[i]; s < off[i + 1]; ++s) {
+                int j = (int)(nb[s] & IDX_MASK);
+                int t = rev[s];
+                for (int a = 0; a < D; ++a)
+                    Aij[(size_t)s * 3 + a] = 1. / omega[i] * psi[(size_t)s * 3 + a] - 1. / omega[j] * psi[(size_t)t * 3 + a];
+            }
+    }
+
+    // --- Particles::pairwiseLimiter, Particles.cpp:1735-1785
+    double pairwiseLimiter(double phi0, double phi_i, double phi_j, double xijxi_abs, double xjxi_abs) const {
+        double phi_ = phi_i;
+        double phi_ij = phi_i + xijxi_abs / xjxi_abs * (phi_j - phi_i);
+        double phiMin, phiMax;
+        if (phi_i < phi_j) { phiMin = phi_i; phiMax = phi_j; }
+        else { phiMin = phi_j; phiMax = phi_i; }
+        double delta1 = c.psi1 * ref_abs(phi_i - phi_j, c.int_abs);
+        double delta2 = c.psi2 * ref_abs(phi_i - phi_j, c.int_abs);
+        double phiMinus, phiPlus;
+        if ((phiMax + delta1 >= 0. && phiMax >= 0.) || (phiMax + delta1 < 0. && phiMax < 0.)) phiPlus = phiMax + delta1;
+        else phiPlus = phiMax / (1. + delta1 / ref_abs(phiMax, c.int_abs));
+        if ((phiMin - delta1 >= 0. && phiMin >= 0.) || (phiMin - delta1 < 0. && phiMin < 0.)) phiMinus = phiMin - delta1;
+        else phiMinus = phiMin / (1. + delta1 / ref_abs(phiMin, c.int_abs));
+        if (phi_i < phi_j) {
+            double minPhiD2 = (phi_ij + delta2 < phi0) ? phi_ij + delta2 : phi0;
+            phi_ = phiMinus > minPhiD2 ? phiMinus : minPhiD2;
+        } else if (phi_i > phi_j) {
+            double maxPhiD2 = (phi_ij - delta2 > phi0) ? phi_ij - delta2 : phi0;
+            phi_ = phiPlus < maxPhiD2 ? phiPlus : maxPhiD2;
+        }
+        return phi_;
+    }
+
+    // --- Particles::compRiemannStatesLR, Particles.cpp:1488-1733 (real) and
+    // 2533-2683 (images: no pairwise limiter unless image_pairwise_limiter)
+    void riemannStatesLR() {
+        const int NV = D + 2;
+        WL.assign((size_t)off[N] * NV, 0.);
+        WR.assign((size_t)off[N] * NV, 0.);
+        vFrame.assign((size_t)off[N] * 3, 0.);
+        const std::vector<double> &rG = G[0], &vxG = G[1], &vyG = G[2], &vzG = G[3], &PG = G[D + 1];
+        const double gamma = c.gamma;
+        for (int i = 0; i < N; ++i)
+            for (int s = off[i]; s < off[i + 1]; ++s) {
+                int j = (int)(nb[s] & IDX_MASK);
+                bool isImg = (s - off[i]) >= noi[i];
+                double xj[3], xij[3], xijxi[3], xjxi[3], xijxj[3];
+                coords(nb[s], xj);
+                for (int a = 0; a < D; ++a) {
+                    xjxi[a] = xj[a] - X[a][i];
+                    if (c.first_order_quad_point) {
+                        xij[a] = (X[a][i] + xj[a]) / 2.;
+                        xijxj[a] = .5 * (X[a][i] - xj[a]);
+                        xijxi[a] = .5 * (xj[a] - X[a][i]);
+                    } else {
+                        xij[a] = X[a][i] + h / 4. * xjxi[a];
+                        xijxi[a] = xij[a] - X[a][i];
+                        xijxj[a] = xij[a] - xj[a];
+                    }
+                }
+                double *vf = &vFrame[(size_t)s * 3];
+                if (!c.move_particles) { for (int a = 0; a < D; ++a) vf[a] = 0.; }
+                else if (c.first_order_quad_point) { for (int a = 0; a < D; ++a) vf[a] = (V[a][i] + V[a][j]) / 2.; }
+                else {
+                    double dotProd = dot(xijxi, xjxi);
+                    double dSqr = dot(xjxi, xjxi);
+                    for (int a = 0; a < D; ++a) vf[a] = V[a][i] + (V[a][j] - V[a][i]) * dotProd / dSqr;
+                }
+                double *R = &WR[(size_t)s * NV], *L = &WL[(size_t)s * NV];
+                R[0] = rho[i]; L[0] = rho[j];
+                R[1] = P[i]; L[1] = P[j];
+                for (int a = 0; a < D; ++a) { R[2 + a] = V[a][i] - vf[a]; L[2 + a] = V[a][j] - vf[a]; }
+                double Rb[5], Lb[5];
+                for (int nu = 0; nu < NV; ++nu) { Rb[nu] = R[nu]; Lb[nu] = L[nu]; }
+                const double *gi, *gj;
+                size_t I = (size_t)i * 3, J = (size_t)j * 3;
+                R[0] += dot(&rG[I], xijxi); L[0] += dot(&rG[J], xijxj);
+                R[1] += dot(&PG[I], xijxi); L[1] += dot(&PG[J], xijxj);
+                R[2] += dot(&vxG[I], xijxi); L[2] += dot(&vxG[J], xijxj);
+                R[3] += dot(&vyG[I], xijxi); L[3] += dot(&vyG[J], xijxj);
+                if (D == 3) { R[4] += dot(&vzG[I], xijxi); L[4] += dot(&vzG[J], xijxj); }
+                (void)gi; (void)gj;
+                if (c.pairwise_limiter && (!isImg || c.image_pairwise_limiter)) {
+                    double xijxi_abs = 0., xijxj_abs = 0., xjxi_abs = 0.;
+                    for (int a = 0; a < D; ++a) {
+                        xijxi_abs += xijxi[a] * xijxi[a];
+                        xijxj_abs += xijxj[a] * xijxj[a];
+                        xjxi_abs += xjxi[a] * xjxi[a];
+                    }
+                    xijxi_abs = std::sqrt(xijxi_abs);
+                    xijxj_abs = std::sqrt(xijxj_abs);
+                    xjxi_abs = std::sqrt(xjxi_abs);
+                    for (int nu = 0; nu < NV; ++nu) {
+                        R[nu] = pairwiseLimiter(R[nu], Rb[nu], Lb[nu], xijxi_abs, xjxi_abs);
+                        L[nu] = pairwiseLimiter(L[nu], Lb[nu], Rb[nu], xijxj_abs, xjxi_abs);
+                    }
+                }
+                double viDiv = vxG[I + 0] + vyG[I + 1];
+                double vjDiv = vxG[J + 0] + vyG[J + 1];
+                if (D == 3) { viDiv += vzG[I + 2]; vjDiv += vzG[J + 2]; }
+                double vxi = V[0][i], vyi = V[1][i], vxj = V[0][j], vyj = V[1][j];
+                R[0] -= dt / 2. * (rho[i] * viDiv + (vxi - vf[0]) * rG[I + 0] + (vyi - vf[1]) * rG[I + 1]);
+                L[0] -= dt / 2. * (rho[j] * vjDiv + (vxj - vf[0]) * rG[J + 0] + (vyj - vf[1]) * rG[J + 1]);
+                R[1] -= dt / 2. * (gamma * P[i] * viDiv + (vxi - vf[0]) * PG[I + 0] + (vyi - vf[1]) * PG[I + 1]);
+                L[1] -= dt / 2. * (gamma * P[j] * vjDiv + (vxj - vf[0]) * PG[J + 0] + (vyj - vf[1]) * PG[J + 1]);
+                R[2] -= dt / 2. * (PG[I + 0] / rho[i] + (vxi - vf[0]) * vxG[I + 0] + (vyi - vf[1]) * vxG[I + 1]);
+                L[2] -= dt / 2. * (PG[J + 0] / rho[j] + (vxj - vf[0]) * vxG[J + 0] + (vyj - vf[1]) * vxG[J + 1]);
+                R[3] -= dt / 2. * (PG[I + 1] / rho[i] + (vxi - vf[0]) * vyG[I + 0] + (vyi - vf[1]) * vyG[I + 1]);
+                L[3] -= dt / 2. * (PG[J + 1] / rho[j] + (vxj - vf[0]) * vyG[J + 0] + (vyj - vf[1]) * vyG[J + 1]);
+                if (D == 3) {
+                    double vzi = V[2][i], vzj = V[2][j];
+                    R[0] -= dt / 2. * (vzi - vf[2]) * rG[I + 2];
+                    L[0] -= dt / 2. * (vzj - vf[2]) * rG[J + 2];
+                    R[1] -= dt / 2. * (vzi - vf[2]) * PG[I + 2];
+                    L[1] -= dt / 2. * (vzj - vf[2]) * PG[J + 2];
+                    // Particles.cpp:1717,1719 use vz[i] on the j side
+                    R[2] -= dt / 2. * (vzi - vf[2]) * vxG[I + 2];
+                    L[2] -= dt / 2. * (vzi - vf[2]) * vxG[J + 2];
+                    R[3] -= dt / 2. * (vzi - vf[2]) * vyG[I + 2];
+                    L[3] -= dt / 2. * (vzi - vf[2]) * vyG[J + 2];
+                    R[4] -= dt / 2. * (PG[I + 2] / rho[i] + (vxi - vf[0]) * vzG[I + 0] + (vyi - vf[1]) * vzG[I + 1] + (vzi - vf[2]) * vzG[I + 2]);
+                    L[4] -= dt / 2. * (PG[J + 2] / rho[j] + (vxj - vf[0]) * vzG[J + 0] + (vyj - vf[1]) * vzG[J + 1] + (vzj - vf[2]) * vzG[J + 2]);
+                }
+            }
+    }
+
+    // --- Helper::rotationMatrix2D/3D, demonstrator/src/Helper.cpp:39-77
+    static void rot2(const double *a, const double *b, double *L) {
+        L[0] = a[0] * b[0] + a[1] * b[1];
+        L[1] = -(a[0] * b[1] - a[1] * b[0]);
+        L[2] = -L[1];
+        L[3] = L[0];
+    }
+    static void rot3(const double *a, const double *b, double *L) {
+        double v[3];
+        v[0] = a[1] * b[2] - a[2] * b[1];
+        v[1] = a[2] * b[0] - a[0] * b[2];
+        v[2] = a[0] * b[1] - a[1] * b[0];
+        double cosAB = dot(a, b);
+        double n = 1. / (1. + cosAB);
+        L[0] = 1. - n * (v[2] * v[2] + v[1] * v[1]);
+        L[1] = -v[2] + n * v[0] * v[1];
+        L[2] = v[1] + n * v[0] * v[2];
+        L[3] = v[2] + n * v[0] * v[1];
+        L[4] = 1. - n * (v[2] * v[2] + v[0] * v[0]);
+        L[5] = -v[0] + n * v[1] * v[2];
+        L[6] = -v[1] + n * v[0] * v[2];
+        L[7] = v[0] + n * v[1] * v[2];
+        L[8] = 1. - n * (v[1] * v[1] + v[0] * v[0]);
+    }
+
+    // --- Riemann::Riemann + Riemann::exact + rotateAndProjectFluxes2D/3D,
+    // demonstrator/src/Riemann.cpp:7-229.  wi = state of the list owner i
+    // (the reference's WijR, which the constructor receives as WL), wj = state
+    // of neighbour j; i is the LEFT state of the 1D problem.
+    void riemann(double *wi, double *wj, const double *vfr, const double *A, double *Fo, const orc::ExactRiemann &rs) {
+        const double unitX[3] = {1., 0., 0.};
+        double AN = std::sqrt(dot(A, A));
+        double hatA[3];
+        for (int a = 0; a < D; ++a) hatA[a] = 1. / AN * A[a];
+        double Lam[9];
+        if (D == 2) {
+            rot2(hatA, unitX, Lam);
+            double bR[2] = {wj[2], wj[3]}, bL[2] = {wi[2], wi[3]};
+            wj[2] = Lam[0] * bR[0] + Lam[1] * bR[1];
+            wj[3] = Lam[2] * bR[0] + Lam[3] * bR[1];
+            wi[2] = Lam[0] * bL[0] + Lam[1] * bL[1];
+            wi[3] = Lam[2] * bL[0] + Lam[3] * bL[1];
+        } else {
+            rot3(hatA, unitX, Lam);
+            double bR[3] = {wj[2], wj[3], wj[4]}, bL[3] = {wi[2], wi[3], wi[4]};
+            wj[2] = Lam[0] * bR[0] + Lam[1] * bR[1] + Lam[2] * bR[2];
+            wj[3] = Lam[3] * bR[0] + Lam[4] * bR[1] + Lam[5] * bR[2];
+            wj[4] = Lam[6] * bR[0] + Lam[7] * bR[1] + Lam[8] * bR[2];
+            wi[2] = Lam[0] * bL[0] + Lam[1] * bL[1] + Lam[2] * bL[2];
+            wi[3] = Lam[3] * bL[0] + Lam[4] * bL[1] + Lam[5] * bL[2];
+            wi[4] = Lam[6] * bL[0] + Lam[7] * bL[1] + Lam[8] * bL[2];
+        }
+        double rhoSol, vSol[3] = {0., 0., 0.}, PSol;
+        int iters = 0;
+        int flag = rs.solve(wi[0], wi[2], wi[1], wj[0], wj[2], wj[1], rhoSol, vSol[0], PSol, &iters);
+        ++riemannSolves;
+        if (iters < 0) status |= ST_NEWTON; else newtonTotal += iters;
+        newtonIters.push_back(iters);
+        if (flag == 1) { for (int a = 1; a < D; ++a) vSol[a] = wj[2 + a]; }
+        else if (flag == -1) { for (int a = 1; a < D; ++a) vSol[a] = wi[2 + a]; }
+        else status |= ST_VACUUM;
+        const double gamma = c.gamma;
+        double LI[9];
+        if (D == 2) {
+            rot2(unitX, hatA, LI);
+            double b[2] = {vSol[0], vSol[1]};
+            vSol[0] = LI[0] * b[0] + LI[1] * b[1];
+            vSol[1] = LI[2] * b[0] + LI[3] * b[1];
+            Fo[0] = A[0] * rhoSol * vSol[0] + A[1] * rhoSol * vSol[1];
+            double vLab[2] = {vSol[0] + vfr[0], vSol[1] + vfr[1]};
+            if (c.meshless_finite_mass) { vSol[0] = 0.; vSol[1] = 0.; }
+            Fo[2] = A[0] * (rhoSol * vLab[0] * vSol[0] + PSol) + A[1] * rhoSol * vLab[0] * vSol[1];
+            Fo[3] = A[0] * rhoSol * vLab[1] * vSol[0] + A[1] * (rhoSol * vLab[1] * vSol[1] + PSol);
+            Fo[1] = A[0] * (vSol[0] * (PSol / (gamma - 1.) + rhoSol * .5 * dot(vLab, vLab)) + PSol * vLab[0])
+                  + A[1] * (vSol[1] * (PSol / (gamma - 1.) + rhoSol * .5 * dot(vLab, vLab)) + PSol * vLab[1]);
+        } else {
+            rot3(unitX, hatA, LI);
+            double b[3] = {vSol[0], vSol[1], vSol[2]};
+            vSol[0] = LI[0] * b[0] + LI[1] * b[1] + LI[2] * b[2];
+            vSol[1] = LI[3] * b[0] + LI[4] * b[1] + LI[5] * b[2];
+            vSol[2] = LI[6] * b[0] + LI[7] * b[1] + LI[8] * b[2];
+            Fo[0] = A[0] * rhoSol * vSol[0] + A[1] * rhoSol * vSol[1] + A[2] * rhoSol * vSol[2];
+            double vLab[3] = {vSol[0] + vfr[0], vSol[1] + vfr[1], vSol[2] + vfr[2]};
+            if (c.meshless_finite_mass) { vSol[0] = 0.; vSol[1] = 0.; vSol[2] = 0.; }
+            Fo[2] = A[0] * (rhoSol * vLab[0] * vSol[0] + PSol) + A[1] * rhoSol * vLab[0] * vSol[1] + A[2] * rhoSol * vLab[0] * vSol[2];
+            Fo[3] = A[0] * rhoSol * vLab[1] * vSol[0] + A[1] * (rhoSol * vLab[1] * vSol[1] + PSol) + A[2] * rhoSol * vLab[1] * vSol[2];
+            Fo[4] = A[0] * rhoSol * vLab[2] * vSol[0] + A[1] * rhoSol * vLab[2] * vSol[1] + A[2] * (rhoSol * vLab[2] * vSol[2] + PSol);
+            Fo[1] = A[0] * (vSol[0] * (PSol / (gamma - 1.) + rhoSol * .5 * dot(vLab, vLab)) + PSol * vLab[0])
+                  + A[1] * (vSol[1] * (PSol / (gamma - 1.) + rhoSol * .5 * dot(vLab, vLab)) + PSol * vLab[1])
+                  + A[2] * (vSol[2] * (PSol / (gamma - 1.) + rhoSol * .5 * dot(vLab, vLab)) + PSol * vLab[2]);
+        }
+    }
+
+    // --- Particles::solveRiemannProblems, Particles.cpp:1787-1911: the face is
+    // solved from the side of the lower (parent) index; the other side copies
+    // -F (ENFORCE_FLUX_SYM).
+    void solveRiemannProblems() {
+        const int NV = D + 2;
+        F.assign((size_t)off[N] * NV, 0.);
+        newtonIters.clear();
+        orc::ExactRiemann rs(c.gamma, c.riemann_tol, c.riemann_max_iter);
+        for (int i = 0; i < N; ++i)
+            for (int s = off[i]; s < off[i + 1]; ++s) {
+                int j = (int)(nb[s] & IDX_MASK);
+                double *R = &WR[(size_t)s * NV], *L = &WL[(size_t)s * NV];
+                if (R[1] < 0. || L[1] < 0.) status |= ST_NEG_PRESSURE;
+                if (j < i) {
+                    int t = rev[s];
+                    for (int d = 0; d < NV; ++d) F[(size_t)s * NV + d] = -F[(size_t)t * NV + d];
+                } else {
+                    double wi[5], wj[5];
+                    for (int d = 0; d < NV; ++d) { wi[d] = R[d]; wj[d] = L[d]; }
+                    riemann(wi, wj, &vFrame[(size_t)s * 3], &Aij[(size_t)s * 3], &F[(size_t)s * NV], rs);
+                }
+            }
+    }
+
+    // --- Particles::collectFluxes, Particles.cpp:1913-2011
+    void collectFluxes() {
+        const int NV = D + 2;
+        mF.assign(N, 0.); eF.assign(N, 0.); vF.assign((size_t)N * 3, 0.);
+        for (int i = 0; i < N; ++i)
+            for (int s = off[i]; s < off[i + 1]; ++s) {
+                const double *f = &F[(size_t)s * NV];
+                mF[i] += f[0];
+                vF[(size_t)i * 3 + 0] += f[2];
+                vF[(size_t)i * 3 + 1] += f[3];
+                if (D == 3) vF[(size_t)i * 3 + 2] += f[4];
+                eF[i] += f[1];
+            }
+    }
+
+    // --- Particles::updateStateAndPosition, Particles.cpp:2013-2110
+    void update() {
+        for (int i = 0; i < N; ++i) {
+            double vxi = V[0][i], vyi = V[1][i], vzi = D == 3 ? V[2][i] : 0.;
+            double Q[4];
+            if (D == 3) Q[0] = m[i] * (u[i] + .5 * (vxi * vxi + vyi * vyi + vzi * vzi));
+            else Q[0] = m[i] * (u[i] + .5 * (vxi * vxi + vyi * vyi));
+            Q[1] = m[i] * vxi;
+            Q[2] = m[i] * vyi;
+            if (D == 3) Q[3] = m[i] * vzi;
+            if (!c.meshless_finite_mass) m[i] -= dt * mF[i];
+            if (m[i] <= 0.) status |= ST_NEG_MASS;
+            for (int a = 0; a < D; ++a) {
+                Q[1 + a] -= dt * vF[(size_t)i * 3 + a];
+                V[a][i] = Q[1 + a] / m[i];
+            }
+            Q[0] -= dt * eF[i];
+            if (D == 3) u[i] = Q[0] / m[i] - .5 * (V[0][i] * V[0][i] + V[1][i] * V[1][i] + V[2][i] * V[2][i]);
+            else u[i] = Q[0] / m[i] - .5 * (V[0][i] * V[0][i] + V[1][i] * V[1][i]);
+            if (u[i] <= 0.) status |= ST_NEG_ENERGY;
+            if (c.move_particles) {
+                double vo[3] = {vxi, vyi, vzi};
+                for (int a = 0; a < D; ++a) X[a][i] += vo[a] * dt;
+                if (c.periodic)
+                    for (int a = 0; a < D; ++a) {
+                        if (X[a][i] < lo[a]) X[a][i] = hi[a] - (lo[a] - X[a][i]);
+                        else if (hi[a] <= X[a][i]) X[a][i] = lo[a] + (X[a][i] - hi[a]);
+                    }
+            }
+        }
+    }
+
+    // MeshlessScheme::run loop body, MeshlessScheme.cpp:39-253 (no dumps)
+    int step() {
+        status = 0;
+        riemannSolves = 0; newtonTotal = 0;
+        if (c.periodic) {
+            for (int a = 0; a < D; ++a) { lo[a] = c.box_lo[a]; hi[a] = c.box_hi[a]; }
+        } else {
+            domainLimits();
+        }
+        createGrid();
+        assign();
+        nns();
+        density();
+        pressure();
+        dt = c.adaptive_timestep ? globalTimestep() : c.time_step;
+        psijTilde();
+        gradients();
+        if (c.slope_limiting) slopeLimiter();
+        effectiveFace();
+        riemannStatesLR();
+        solveRiemannProblems();
+        collectFluxes();
+        update();
+        return (int)status;
+    }
+};
+
+struct Handle {
+    int dim;
+    void *sim;
+};
+
+template <int D>
+Sim<D> *make(const orc_config *cfg, int n, const double *x, const double *y, const double *z,
+             const double *vx, const double *vy, const double *vz, const double *m, const double *u) {
+    Sim<D> *s = new Sim<D>();
+    s->c = *cfg;
+    s->N = n;
+    s->h = cfg->kernel_size;
+    const double *xs[3] = {x, y, z}, *vs[3] = {vx, vy, vz};
+    for (int a = 0; a < 3; ++a) {
+        s->X[a].assign(n, 0.);
+        s->V[a].assign(n, 0.);
+        if (a < D) {
+            std::copy(xs[a], xs[a] + n, s->X[a].begin());
+            std::copy(vs[a], vs[a] + n, s->V[a].begin());
+        }
+    }
+    s->m.assign(m, m + n);
+    s->u.assign(u, u + n);
+    s->rho.assign(n, 0.);
+    s->P.assign(n, 0.);
+    return s;
+}
+
+template <int D>
+long sizeOf(Sim<D> *s, const std::string &nm) {
+    long N = s->N, S = s->off.empty() ? 0 : s->off[N];
+    if (nm == "x" || nm == "y" || nm == "z" || nm == "vx" || nm == "vy" || nm == "vz" || nm == "m" || nm == "u" ||
+        nm == "rho" || nm == "P" || nm == "omega" || nm == "noi" || nm == "noi_img" || nm == "mF" || nm == "eF")
+        return N;
+    if (nm == "off") return N + 1;
+    if (nm == "nnl" || nm == "rev" ) return S;
+    if (nm == "vF") return N * 3;
+    if (nm.compare(0, 4, "grad") == 0) return N * 3;
+    if (nm == "B") return N * D * D;
+    if (nm == "psi" || nm == "Aij" || nm == "vFrame") return S * 3;
+    if (nm == "WL" || nm == "WR" || nm == "F") return S * (D + 2);
+    if (nm == "dt" || nm == "grid" || nm == "stats") return nm == "grid" ? 9 : (nm == "stats" ? 2 : 1);
+    if (nm == "newton_iters") return (long)s->newtonIters.size();
+    return -1;
+}
+
+template <int D>
+int getArr(Sim<D> *s, const std::string &nm, void *out) {
+    double *o = (double *)out;
+    int *oi = (int *)out;
+    auto cp = [&](const std::vector<double> &v) { std::copy(v.begin(), v.end(), o); return 0; };
+    auto cpi = [&](const std::vector<int> &v) { std::copy(v.begin(), v.end(), oi); return 0; };
+    if (nm == "x") return cp(s->X[0]);
+    if (nm == "y") return cp(s->X[1]);
+    if (nm == "z") return cp(s->X[2]);
+    if (nm == "vx") return cp(s->V[0]);
+    if (nm == "vy") return cp(s->V[1]);
+    if (nm == "vz") return cp(s->V[2]);
+    if (nm == "m") return cp(s->m);
+    if (nm == "u") return cp(s->u);
+    if (nm == "rho") return cp(s->rho);
+    if (nm == "P") return cp(s->P);
+    if (nm == "omega") return cp(s->omega);
+    if (nm == "mF") return cp(s->mF);
+    if (nm == "eF") return cp(s->eF);
+    if (nm == "vF") return cp(s->vF);
+    if (nm == "B") return cp(s->B);
+    if (nm == "psi") return cp(s->psi);
+    if (nm == "Aij") return cp(s->Aij);
+    if (nm == "vFrame") return cp(s->vFrame);
+    if (nm == "WL") return cp(s->WL);
+    if (nm == "WR") return cp(s->WR);
+    if (nm == "F") return cp(s->F);
+    if (nm == "noi") return cpi(s->noi);
+    if (nm == "noi_img") return cpi(s->noiImg);
+    if (nm == "off") return cpi(s->off);
+    if (nm == "rev") return cpi(s->rev);
+    if (nm == "newton_iters") return cpi(s->newtonIters);
+    if (nm == "nnl") { std::copy(s->nb.begin(), s->nb.end(), (uint32_t *)out); return 0; }
+    if (nm == "dt") { o[0] = s->dt; return 0; }
+    if (nm == "stats") { o[0] = (double)s->riemannSolves; o[1] = (double)s->newtonTotal; return 0; }
+    if (nm == "grid") {
+        for (int a = 0; a < 3; ++a) { o[a] = a < D ? s->lo[a] : 0.; o[3 + a] = a < D ? s->hi[a] : 0.; o[6 + a] = a < D ? s->cells[a] : 0; }
+        return 0;
+    }
+    // gradients: "grad_<f>" limited, "gradraw_<f>" unlimited; f in
+    // rho, vx, vy, vz, P
+    static const char *names[5] = {"rho", "vx", "vy", "vz", "P"};
+    for (int k = 0; k < 5; ++k) {
+        int f = k;
+        if (D == 2) { if (k == 3) continue; if (k == 4) f = 3; }
+        if (nm == std::string("grad_") + names[k]) return cp(s->G[f]);
+        if (nm == std::string("gradraw_") + names[k]) return cp(s->Graw[f]);
+    }
+    return -1;
+}
+
+}  // namespace
+
+extern "C" {
+
+void *orc_create(const orc_config *cfg, int n, const double *x, const double *y, const double *z,
+                 const double *vx, const double *vy, const double *vz, const double *m, const double *u) {
+    Handle *hnd = new Handle();
+    hnd->dim = cfg->dim;
+    if (cfg->dim == 2) hnd->sim = make<2>(cfg, n, x, y, z, vx, vy, vz, m, u);
+    else hnd->sim = make<3>(cfg, n, x, y, z, vx, vy, vz, m, u);
+    return hnd;
+}
+
+int orc_step(void *ctx) {
+    Handle *hnd = (Handle *)ctx;
+    if (hnd->dim == 2) return ((Sim<2> *)hnd->sim)->step();
+    return ((Sim<3> *)hnd->sim)->step();
+}
+
+long orc_size(void *ctx, const char *name) {
+    Handle *hnd = (Handle *)ctx;
+    if (hnd->dim == 2) return sizeOf((Sim<2> *)hnd->sim, name);
+    return sizeOf((Sim<3> *)hnd->sim, name);
+}
+
+int orc_get(void *ctx, const char *name, void *out) {
+    Handle *hnd = (Handle *)ctx;
+    if (hnd->dim == 2) return getArr((Sim<2> *)hnd->sim, name, out);
+    return getArr((Sim<3> *)hnd->sim, name, out);
+}
+
+void orc_destroy(void *ctx) {
+    Handle *hnd = (Handle *)ctx;
+    if (hnd->dim == 2) delete (Sim<2> *)hnd->sim;
+    else delete (Sim<3> *)hnd->sim;
+    delete hnd;
+}
+
+}  // extern "C"

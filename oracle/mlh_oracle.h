@@ -1,0 +1,58 @@
+/* TEST INFRASTRUCTURE (oracle). Not part of the product.
+ *
+ * C interface of the CPU restatement of the reference's MFV timestep
+ * (jammartin/meshlessHydro, demonstrator/src/MeshlessScheme.cpp:39-253 and the
+ * Particles stage methods it calls).  Only tests/, the smoke check and
+ * bench.py's CPU baseline load this library, as the checker.
+ */
+#ifndef MLH_ORACLE_H
+#define MLH_ORACLE_H
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* Same field meaning as mlh_config in include/mlh.h (the compile-time
+ * switches of demonstrator/include/parameter.h:9-74 and the config.info keys
+ * of demonstrator/config.info:1-33), declared separately so that the oracle
+ * and the product share no code. */
+typedef struct orc_config {
+    int dim;
+    int periodic;
+    int adaptive_timestep;
+    int slope_limiting;
+    int pairwise_limiter;
+    int meshless_finite_mass;
+    int move_particles;
+    int first_order_quad_point;
+    int int_abs;
+    int image_pairwise_limiter;
+    int riemann_max_iter;
+    int max_neighbours;
+    double box_lo[3];
+    double box_hi[3];
+    double kernel_size;
+    double gamma;
+    double cfl;
+    double time_step;
+    double beta;
+    double psi1;
+    double psi2;
+    double riemann_tol;
+} orc_config;
+
+void *orc_create(const orc_config *cfg, int n,
+                 const double *x, const double *y, const double *z,
+                 const double *vx, const double *vy, const double *vz,
+                 const double *m, const double *u);
+/* One MFV step.  Returns 0, or a nonzero status (see the .cpp). */
+int orc_step(void *ctx);
+/* Number of elements of a named array (after the last step), -1 if unknown. */
+long orc_size(void *ctx, const char *name);
+/* Copy a named array into `out` (doubles, or int32 for integer arrays). */
+int orc_get(void *ctx, const char *name, void *out);
+void orc_destroy(void *ctx);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

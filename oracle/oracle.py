@@ -1,0 +1,157 @@
+"""TEST INFRASTRUCTURE (oracle): ctypes access to the CPU restatement
+(oracle/libmlh_oracle.so) and to the reference build (oracle/_ref/ref_*).
+
+Only tests/, the smoke check and bench.py's CPU baseline use this module, as
+the checker; the product never imports it.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+import struct
+import subprocess
+import tempfile
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB = os.path.join(HERE, "libmlh_oracle.so")
+REF_DIR = os.path.join(HERE, "_ref")
+
+_INT_FIELDS = ["dim", "periodic", "adaptive_timestep", "slope_limiting", "pairwise_limiter",
+               "meshless_finite_mass", "move_particles", "first_order_quad_point", "int_abs",
+               "image_pairwise_limiter", "riemann_max_iter", "max_neighbours"]
+_DBL_FIELDS = ["kernel_size", "gamma", "cfl", "time_step", "beta", "psi1", "psi2", "riemann_tol"]
+
+
+class OrcConfig(ctypes.Structure):
+    _fields_ = ([(f, ctypes.c_int) for f in _INT_FIELDS]
+                + [("box_lo", ctypes.c_double * 3), ("box_hi", ctypes.c_double * 3)]
+                + [(f, ctypes.c_double) for f in _DBL_FIELDS])
+
+
+INT_ARRAYS = {"noi", "noi_img", "off", "rev", "newton_iters", "nnl"}
+
+
+def build():
+    subprocess.run(["make", "-s", "-C", HERE], check=True)
+
+
+_lib = None
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB):
+            build()
+        L = ctypes.CDLL(LIB)
+        dp = ctypes.POINTER(ctypes.c_double)
+        L.orc_create.restype = ctypes.c_void_p
+        L.orc_create.argtypes = [ctypes.POINTER(OrcConfig), ctypes.c_int] + [dp] * 8
+        L.orc_step.restype = ctypes.c_int
+        L.orc_step.argtypes = [ctypes.c_void_p]
+        L.orc_size.restype = ctypes.c_long
+        L.orc_size.argtypes = [ctypes.c_void_p, ctypes.c_char_p]
+        L.orc_get.restype = ctypes.c_int
+        L.orc_get.argtypes = [ctypes.c_void_p, ctypes.c_char_p, ctypes.c_void_p]
+        L.orc_destroy.argtypes = [ctypes.c_void_p]
+        _lib = L
+    return _lib
+
+
+def _cfg_struct(cfg) -> OrcConfig:
+    s = OrcConfig()
+    for f in _INT_FIELDS:
+        setattr(s, f, int(getattr(cfg, f)))
+    for a in range(3):
+        s.box_lo[a] = float(cfg.box_lo[a])
+        s.box_hi[a] = float(cfg.box_hi[a])
+    for f in _DBL_FIELDS:
+        setattr(s, f, float(getattr(cfg, f)))
+    return s
+
+
+class Oracle:
+    """One simulation held by the CPU restatement."""
+
+    def __init__(self, cfg, pset):
+        self.L = lib()
+        self._arrays = [np.ascontiguousarray(a, dtype=np.float64) for a in pset.arrays()]
+        ptrs = [a.ctypes.data_as(ctypes.POINTER(ctypes.c_double)) for a in self._arrays]
+        self._cfg = _cfg_struct(cfg)
+        self.h = self.L.orc_create(ctypes.byref(self._cfg), pset.n, *ptrs)
+        self.dim = cfg.dim
+
+    def step(self) -> int:
+        return self.L.orc_step(self.h)
+
+    def get(self, name: str) -> np.ndarray:
+        n = self.L.orc_size(self.h, name.encode())
+        if n < 0:
+            raise KeyError(name)
+        if name in INT_ARRAYS:
+            out = np.empty(n, dtype=np.uint32 if name == "nnl" else np.int32)
+        else:
+            out = np.empty(n, dtype=np.float64)
+        if self.L.orc_get(self.h, name.encode(), out.ctypes.data) != 0:
+            raise KeyError(name)
+        return out
+
+    def state(self) -> dict:
+        names = ["x", "y", "vx", "vy", "m", "u"] + (["z", "vz"] if self.dim == 3 else [])
+        return {k: self.get(k) for k in names}
+
+    def close(self):
+        if self.h:
+            self.L.orc_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+# ---------------------------------------------------------------- reference build
+
+def read_dump(path: str) -> dict:
+    out = {}
+    with open(path, "rb") as f:
+        data = f.read()
+    p = 0
+    while p < len(data):
+        (ln,) = struct.unpack_from("<I", data, p); p += 4
+        name = data[p:p + ln].decode(); p += ln
+        t = data[p:p + 1].decode(); p += 1
+        (cnt,) = struct.unpack_from("<Q", data, p); p += 8
+        dt = np.float64 if t == "d" else np.int32
+        size = 8 if t == "d" else 4
+        out[name] = np.frombuffer(data, dtype=dt, count=cnt, offset=p).copy()
+        p += cnt * size
+    if "nnl" in out:
+        out["nnl"] = out["nnl"].view(np.uint32)
+    return out
+
+
+def ref_available(variant: str) -> bool:
+    return os.path.exists(os.path.join(REF_DIR, "ref_" + variant))
+
+
+def run_ref(variant: str, pset, nsteps: int, time_step: float = 0.005) -> dict:
+    """Run the reference's own code (oracle/_ref/ref_<variant>) for nsteps."""
+    exe = os.path.join(REF_DIR, "ref_" + variant)
+    with tempfile.TemporaryDirectory() as td:
+        fin = os.path.join(td, "in.bin")
+        fout = os.path.join(td, "out.bin")
+        with open(fin, "wb") as f:
+            f.write(struct.pack("<q", pset.n))
+            arrs = [pset.x, pset.y] + ([pset.z] if pset.dim == 3 else []) + \
+                   [pset.vx, pset.vy] + ([pset.vz] if pset.dim == 3 else []) + [pset.m, pset.u]
+            for a in arrs:
+                f.write(np.ascontiguousarray(a, dtype=np.float64).tobytes())
+        args = [exe, fin, fout, str(nsteps), repr(pset.kernel_size), repr(pset.gamma), repr(time_step)]
+        args += [repr(float(v)) for v in pset.box_lo] + [repr(float(v)) for v in pset.box_hi]
+        subprocess.run(args, check=True)
+        return read_dump(fout)

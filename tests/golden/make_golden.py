@@ -1,0 +1,99 @@
+"""Generate the golden fixtures of tests/golden/ from the reference's own code.
+
+Runs the reference demonstrator's MFV stages, compiled unmodified from the
+reference tree by oracle/build_ref.sh (oracle/_ref/ref_<variant>), on small
+seeded inputs and stores inputs and outputs as .npz files.  The reference tree
+is needed only here; the fixtures travel with the repository and pin the CPU
+restatement (oracle/) on any host.
+
+    python tests/golden/make_golden.py      # after: bash oracle/build_ref.sh
+
+Variants (abs binding, see oracle/build_ref.sh):
+  kh24_dbl      2D periodic Kelvin-Helmholtz, 24x24, fabs limiters
+  kh24_int      same, limiters with the int abs(int) binding
+  kh24pw_dbl    same set-up with PAIRWISE_LIMITER 1 (2D real faces)
+  sedov12np_dbl 3D non-periodic Sedov 12^3 without the pairwise limiter (the
+                reference's 3D pairwise limiter reads an uninitialised xjxi[2])
+  kh100_dbl     the 100x100 Kelvin-Helmholtz set-up: lists and state after
+                one step, state after ten steps
+"""
+import hashlib
+import os
+import sys
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(os.path.dirname(HERE))
+sys.path.insert(0, ROOT)
+sys.path.insert(0, os.path.join(ROOT, "oracle"))
+
+from meshlesshydro_gb300 import ic  # noqa: E402
+import oracle as O  # noqa: E402
+
+STAGE_KEYS = ["off", "noi", "noi_img", "nnl", "omega", "rho", "P", "dt", "grid",
+              "psi", "Aij", "vFrame", "WL", "WR", "F", "mF", "eF", "vF"]
+
+
+def inputs(p):
+    return {"in_x": p.x, "in_y": p.y, "in_z": p.z, "in_vx": p.vx, "in_vy": p.vy, "in_vz": p.vz,
+            "in_m": p.m, "in_u": p.u, "kernel_size": np.array(p.kernel_size),
+            "gamma": np.array(p.gamma), "box_lo": np.array(p.box_lo), "box_hi": np.array(p.box_hi),
+            "dim": np.array(p.dim)}
+
+
+SLOT_KEYS = {"psi": 1, "Aij": 1, "vFrame": 1, "WL": 2, "WR": 2, "F": 2}
+
+
+def full(name, variant, p, nsteps, slot_particles=64):
+    """Per-stage arrays of the first step; per-interaction arrays only for the
+    slots of the first `slot_particles` particles (keeps the files small)."""
+    r = O.run_ref(variant, p, nsteps)
+    d = inputs(p)
+    ns = int(r["off"][min(slot_particles, p.n)])
+    for k in STAGE_KEYS:
+        if k in SLOT_KEYS:
+            width = p.dim if SLOT_KEYS[k] == 1 else p.dim + 2
+            d[k] = r[k][: ns * width]
+        else:
+            d[k] = r[k]
+    d["slot_particles"] = np.array(min(slot_particles, p.n))
+    for k, v in r.items():
+        if k.startswith(("grad_", "gradraw_", "s1_", "out_")) or k == "dts":
+            d[k] = v
+    d["nsteps"] = np.array(nsteps)
+    np.savez_compressed(os.path.join(HERE, name + ".npz"), **d)
+    print("wrote", name, {k: v.shape for k, v in d.items() if hasattr(v, "shape") and v.size > 1})
+
+
+def summary(name, variant, p, nsteps):
+    r1 = O.run_ref(variant, p, 1)
+    rn = O.run_ref(variant, p, nsteps)
+    d = inputs(p)
+    for k in ["off", "noi", "noi_img", "dt", "grid"]:
+        d[k] = r1[k]
+    d["nnl_sha256"] = np.frombuffer(hashlib.sha256(r1["nnl"].tobytes()).digest(), dtype=np.uint8)
+    for k, v in r1.items():
+        if k.startswith("s1_"):
+            d[k] = v
+    for k, v in rn.items():
+        if k.startswith("out_") or k == "dts":
+            d[k] = v
+    d["nsteps"] = np.array(nsteps)
+    np.savez_compressed(os.path.join(HERE, name + ".npz"), **d)
+    print("wrote", name)
+
+
+def main():
+    kh24 = ic.kelvin_helmholtz(n_side=24, seed=3)
+    full("kh24_dbl", "kh_dbl", kh24, 5)
+    full("kh24_int", "kh_int", kh24, 5)
+    full("kh24pw_dbl", "khpw_dbl", kh24, 5)
+    sd12 = ic.sedov(n_side=12, seed=4, energy=0.05)
+    full("sedov12np_dbl", "sedovnopw_dbl", sd12, 1)
+    kh100 = ic.kelvin_helmholtz(n_side=100, seed=1)
+    summary("kh100_dbl", "kh_dbl", kh100, 10)
+
+
+if __name__ == "__main__":
+    main()
