@@ -1,0 +1,328 @@
+"""Throughput of the GB300 MFV step: particle-updates/s on one GB300.
+
+Default workload: the 3D Sedov blast on a jittered 128^3 lattice (2,097,152
+particles) in the periodic cube [-0.5, 0.5]^3, FP64 state, cubic spline with a
+mean of 32 neighbours (kernelSize 2.102 lattice spacings), CFL 0.25, BETA 1,
+pairwise limiter: the "plain GPU method at scale" configuration.  A step is one
+full MFV step (binning, neighbour search, density, dt, gradients, limiter,
+faces, exact Riemann solves, flux gather, kick/drift) over all particles.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl mlh|reference]
+                    [--workload sedov128|sedov64|kh100]
+
+Prints one JSON line.  --impl reference times the CPU restatement of the
+reference's serial code (the oracle; the reference itself cannot run on the
+GPU host) on a bounded sample of the same workload.
+"""
+from __future__ import annotations
+
+import argparse
+import ctypes
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+import numpy as np  # noqa: E402
+
+WORKLOADS = {
+    "sedov128": dict(kind="sedov", n_side=128, periodic=True),
+    "sedov64": dict(kind="sedov", n_side=64, periodic=True),
+    "kh100": dict(kind="kh", n_side=100),
+}
+METRIC = "particle-updates/s per MFV step on 1 GB300"
+LAUNCHES_PER_STEP = 18   # kernels launched by one mlh_step iteration (see csrc/mlh_kernels.cu)
+
+
+def make_workload(name: str, seed_offset: int = 0):
+    from meshlesshydro_gb300 import ic
+    from meshlesshydro_gb300.config import MFVConfig
+    w = WORKLOADS[name]
+    if w["kind"] == "sedov":
+        p = ic.sedov(n_side=w["n_side"], seed=2 + seed_offset)
+        return p, MFVConfig.sedov(p, periodic=w["periodic"])
+    p = ic.kelvin_helmholtz(n_side=w["n_side"], seed=1 + seed_offset)
+    return p, MFVConfig.kelvin_helmholtz(p)
+
+
+def dist_env():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index: int):
+        self.gpu = gpu_index
+        self.proc = None
+        self.lines = []
+        self.thread = None
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.gpu), f"--query-gpu={self.Q}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except (FileNotFoundError, OSError):
+            self.proc = None
+            return
+        self.thread = threading.Thread(target=self._read, daemon=True)
+        self.thread.start()
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        if self.thread:
+            self.thread.join(timeout=2)
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [x.strip() for x in ln.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                smax.append(float(parts[2]))
+            except ValueError:
+                continue
+            for k, v in zip(names, parts[5:9]):
+                if v.lower() == "active":
+                    reasons.add(k)
+        return {"sm_mhz": float(np.median(sm)) if sm else None,
+                "sm_max_mhz": float(max(smax)) if smax else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def measured_peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            return json.load(f), "measured"
+    except (OSError, ValueError):
+        return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0}, "fallback"
+
+
+def cpu_model():
+    try:
+        out = subprocess.run(["lscpu"], capture_output=True, text=True).stdout
+        for ln in out.splitlines():
+            if ln.startswith("Model name"):
+                return ln.split(":", 1)[1].strip()
+    except OSError:
+        pass
+    return "unknown"
+
+
+def cpu_baseline_sample(seconds_hint: float = 20.0):
+    """The oracle (serial CPU restatement of the reference) on a bounded sample:
+    whole MFV steps of the 32^3 Sedov lattice with the workload's particle
+    density and neighbour count (same per-particle work as 128^3)."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle
+    from meshlesshydro_gb300 import ic
+    from meshlesshydro_gb300.config import MFVConfig
+    oracle.build()
+    p = ic.sedov(n_side=32, seed=2)
+    cfg = MFVConfig.sedov(p, periodic=True)
+    o = oracle.Oracle(cfg, p)
+    o.step()  # warm-up
+    steps, t0 = 0, time.perf_counter()
+    while True:
+        o.step()
+        steps += 1
+        el = time.perf_counter() - t0
+        if el >= seconds_hint or steps >= 50:
+            break
+    return {"value": p.n * steps / el, "unit": "particle-updates/s", "cores": 1, "kind": "port",
+            "sample": f"{steps} MFV steps of the 32^3 periodic Sedov lattice ({p.n} particles, same h/dx and "
+                      f"~32 neighbours as the 128^3 workload), serial oracle, {el:.1f} s, host {cpu_model()}"}
+
+
+def run_reference(args):
+    ws, rank, _ = dist_env()
+    if rank != 0:
+        return 0
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle
+    from meshlesshydro_gb300 import ic
+    from meshlesshydro_gb300.config import MFVConfig
+    oracle.build()
+    w = WORKLOADS[args.workload]
+    # bounded sample: the 32^3 lattice for Sedov workloads, the full KH set-up
+    if w["kind"] == "sedov":
+        p = ic.sedov(n_side=32, seed=2)
+        cfg = MFVConfig.sedov(p, periodic=w["periodic"])
+        sample = f"32^3 periodic Sedov lattice ({p.n} particles; same h/dx as {args.workload}), one MFV step per step"
+    else:
+        p = ic.kelvin_helmholtz(n_side=w["n_side"], seed=1)
+        cfg = MFVConfig.kelvin_helmholtz(p)
+        sample = f"{args.workload} ({p.n} particles), one MFV step per step"
+    o = oracle.Oracle(cfg, p)
+    for _ in range(args.warmup):
+        o.step()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        o.step()
+    el = time.perf_counter() - t0
+    val = p.n * args.steps / el
+    line = {"metric": METRIC, "value": val, "unit": "particle-updates/s", "n_gpus": ws, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": 1e3 * el / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic", "impl": "reference",
+            "config": {"workload": args.workload, "sample": sample},
+            "cpu_baseline": {"value": val, "unit": "particle-updates/s", "cores": 1, "kind": "port",
+                             "sample": sample + f", host {cpu_model()}"},
+            "e2e": {"value": val, "unit": "particle-updates/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def run_mlh(args):
+    import torch
+    ws, rank, local = dist_env()
+    if ws > 1:
+        import torch.distributed as dist
+        torch.cuda.set_device(local)
+        dist.init_process_group("gloo")
+    else:
+        dist = None
+    from meshlesshydro_gb300 import build, runtime
+    build.build()
+    p, cfg = make_workload(args.workload, seed_offset=rank)
+    sim = runtime.Simulation(cfg, p)
+    sim.step(args.warmup)
+    sim.reset_kernel_times()
+    sim.set_kernel_timing(True)
+    if dist:
+        dist.barrier()
+    torch.cuda.synchronize()
+    clocks = ClockSampler(local)
+    clocks.start()
+    t0 = time.perf_counter()
+    st = sim.step(args.steps)
+    torch.cuda.synchronize()
+    wall = time.perf_counter() - t0
+    ck = clocks.stop()
+    sim.set_kernel_timing(False)
+    dev_s = st.device_ms / 1e3
+    t_max = dev_s
+    if dist:
+        t = torch.tensor([dev_s], dtype=torch.float64)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        t_max = float(t.item())
+    kt = sim.kernel_times()
+    faces_per_step = st.faces / max(st.steps, 1)
+    pairs_per_step = st.pair_interactions / max(st.steps, 1)
+
+    # end to end through the C ABI with host buffers: H2D of the state,
+    # one step, D2H of the state, every step (pinned host memory)
+    n = p.n
+    keys = ("x", "y", "z", "vx", "vy", "vz", "m", "u")
+    pinned = {k: torch.empty(n, dtype=torch.float64, pin_memory=True) for k in keys}
+    view = runtime.ParticlesView()
+    view.n = n
+    for k in keys:
+        setattr(view, k, ctypes.cast(pinned[k].data_ptr(), ctypes.POINTER(ctypes.c_double)))
+    L = sim.L
+    L.mlh_get_fields(sim.h, ctypes.byref(view))
+    e2e_steps = max(2, min(args.steps, 5))
+    used = 8 if cfg.dim == 3 else 6
+    t0 = time.perf_counter()
+    for _ in range(e2e_steps):
+        L.mlh_set_fields(sim.h, ctypes.byref(view))
+        sim.step(1)
+        L.mlh_get_fields(sim.h, ctypes.byref(view))
+    e2e_wall = time.perf_counter() - t0
+
+    if rank != 0:
+        if dist:
+            dist.barrier()
+        return 0
+    value = ws * n * st.steps / t_max
+    peaks, peak_kind = measured_peaks()
+    # dominant kernel and its roofline
+    dom = max(kt.items(), key=lambda kv: kv[1][1])
+    dom_name, (dom_launches, dom_ms) = dom
+    dom_avg_s = dom_ms / max(dom_launches, 1) / 1e3
+    fp64_peak = args.fp64_peak_tflops
+    flops_per_face = args.flops_per_face
+    achieved_tf = flops_per_face * faces_per_step / dom_avg_s / 1e12 if dom_name == "faces_riemann" else None
+    roofline = {"kernel": dom_name, "bound": "fp64", "unit": "TFLOP/s",
+                "achieved": achieved_tf, "peak": fp64_peak,
+                "frac": (achieved_tf / fp64_peak) if (achieved_tf and fp64_peak) else None,
+                "traffic": args.dom_traffic_bytes * faces_per_step if args.dom_traffic_bytes else None,
+                "peak_source": args.fp64_peak_source,
+                "flops_per_face": flops_per_face,
+                "units_per_launch": faces_per_step,
+                "avg_launch_ms": dom_avg_s * 1e3}
+    line = {"metric": METRIC, "value": value, "unit": "particle-updates/s", "n_gpus": ws, "steps": st.steps,
+            "warmup": args.warmup, "ms_per_step": 1e3 * t_max / st.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": args.workload, "particles_per_gpu": n, "dim": cfg.dim,
+                       "periodic": bool(cfg.periodic), "kernel_size": cfg.kernel_size,
+                       "pair_interactions_per_step": pairs_per_step, "faces_per_step": faces_per_step,
+                       "l2": "inputs larger than L2 (state + neighbour lists >> 129 MB)",
+                       "parallelism": f"replicas x{ws}"},
+            "pair_interactions_per_s": ws * pairs_per_step * st.steps / t_max,
+            "newton_iterations_per_face": st.newton_iterations / max(st.faces, 1),
+            "status": runtime.status_names(st.status),
+            "wall_s_timed": wall,
+            "gpu_launches": LAUNCHES_PER_STEP * st.steps,
+            "kernel_ms_per_step": {k: v[1] / max(v[0], 1) for k, v in kt.items()},
+            "roofline": roofline,
+            "clocks": ck,
+            "e2e": {"value": ws * n * e2e_steps / e2e_wall, "unit": "particle-updates/s",
+                    "h2d_bytes_per_step": used * 8 * n, "d2h_bytes_per_step": used * 8 * n,
+                    "steps": e2e_steps},
+            "peaks": {"source": peak_kind, "hbm_gbs": peaks.get("hbm_gbs")}}
+    if not args.no_cpu_baseline:
+        line["cpu_baseline"] = cpu_baseline_sample(args.cpu_seconds)
+    print(json.dumps(line), flush=True)
+    if dist:
+        dist.barrier()
+    return 0
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="mlh", choices=["mlh", "reference"])
+    ap.add_argument("--workload", default="sedov128", choices=sorted(WORKLOADS))
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--cpu-seconds", type=float, default=15.0)
+    # FP64 work per face and the FP64 peak (see profiles/): executed FP64
+    # flops per Riemann face from ncu instruction counts, peak from the
+    # FP64 FMA probe
+    ap.add_argument("--flops-per-face", type=float, default=0.0)
+    ap.add_argument("--fp64-peak-tflops", type=float, default=0.0)
+    ap.add_argument("--fp64-peak-source", default="")
+    ap.add_argument("--dom-traffic-bytes", type=float, default=0.0)
+    args = ap.parse_args()
+    if args.impl == "reference":
+        return run_reference(args)
+    return run_mlh(args)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

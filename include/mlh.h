@@ -1,0 +1,137 @@
+/*
+ * meshlesshydro-gb300: C ABI of the GB300 (sm_103a) MFV timestep.
+ *
+ * This is the boundary that replaces the body of one step of the reference's
+ * MeshlessScheme::run (jammartin/meshlessHydro, demonstrator/src/
+ * MeshlessScheme.cpp:39-253) and the Particles stage methods it calls.  All
+ * functions take plain pointers and sizes, return an int status (0 = OK,
+ * otherwise MLH_ERR_* bits), and never exit().  One context owns the device
+ * memory and one CUDA stream; calls on one context must be serialised.
+ */
+#ifndef MLH_H
+#define MLH_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define MLH_ABI_VERSION 1
+
+/* Status bits.  The reference exits instead (demonstrator/src/Particles.cpp:
+ * 348-352 exit(1) neighbour overflow, :2249-2253 exit(3), :1878-1881 exit(6)
+ * negative ghost-face pressure) or only warns. */
+enum mlh_status_bits {
+    MLH_OK = 0,
+    MLH_ERR_NGB_OVERFLOW = 1 << 0,   /* a particle has more neighbours than slots */
+    MLH_ERR_NEG_PRESSURE = 1 << 1,   /* P <= 0 or a face state with P < 0 */
+    MLH_ERR_NEG_DENSITY = 1 << 2,
+    MLH_ERR_NEG_MASS = 1 << 3,
+    MLH_ERR_NEG_ENERGY = 1 << 4,
+    MLH_ERR_NEWTON = 1 << 5,         /* Riemann Newton iteration did not converge */
+    MLH_ERR_VACUUM = 1 << 6,         /* vacuum generated in a Riemann problem */
+    MLH_ERR_GRID = 1 << 7,           /* particle outside the grid / < 3 periodic cells */
+    MLH_ERR_NO_NEIGHBOUR = 1 << 8,
+    MLH_ERR_ASYMMETRIC = 1 << 9,     /* a neighbour pair found from one side only */
+    MLH_ERR_NAN = 1 << 10,
+    MLH_ERR_TIMEOUT = 1 << 11,       /* a bounded device wait gave up */
+    MLH_ERR_INVALID = 1 << 20,       /* bad argument */
+    MLH_ERR_CUDA = 1 << 21,          /* CUDA runtime error (message: mlh_last_error) */
+    MLH_ERR_NO_DEVICE = 1 << 22,
+    MLH_ERR_CAPACITY = 1 << 23       /* a size above a fixed maximum */
+};
+
+/* Run-time form of the reference's settings: the compile-time switches of
+ * demonstrator/include/parameter.h:9-74 and the config.info keys read in
+ * demonstrator/src/main.cpp:55-85. */
+typedef struct mlh_config {
+    int dim;                    /* DIM: 2 or 3 */
+    int periodic;               /* PERIODIC_BOUNDARIES */
+    int adaptive_timestep;      /* ADAPTIVE_TIMESTEP */
+    int slope_limiting;         /* SLOPE_LIMITING */
+    int pairwise_limiter;       /* PAIRWISE_LIMITER */
+    int meshless_finite_mass;   /* MESHLESS_FINITE_MASS */
+    int move_particles;         /* MOVE_PARTICLES */
+    int first_order_quad_point; /* FIRST_ORDER_QUAD_POINT */
+    int int_abs;                /* limiters use int abs(int) (see DESIGN) */
+    int image_pairwise_limiter; /* pairwise limiter also on periodic-image faces */
+    int riemann_max_iter;       /* Newton iteration cap */
+    int max_neighbours;         /* slots per particle; 0 = automatic */
+    double box_lo[3];           /* periodicBoxLimits lowerX/Y/Z */
+    double box_hi[3];           /* periodicBoxLimits upperX/Y/Z */
+    double kernel_size;         /* kernelSize (support radius h) */
+    double gamma;               /* gamma */
+    double cfl;                 /* CFL */
+    double time_step;           /* timeStep: dt when !adaptive_timestep */
+    double beta;                /* BETA */
+    double psi1;                /* PSI_1 */
+    double psi2;                /* PSI_2 */
+    double riemann_tol;         /* relative Newton tolerance on p* */
+} mlh_config;
+
+/* Caller-owned host arrays (structure of arrays, float64), the fields of the
+ * reference's Particles class (demonstrator/include/Particles.h:33-38) that
+ * InitialDistribution fills (demonstrator/src/InitialDistribution.cpp:32-59).
+ * z and vz are ignored in 2D and may be NULL there. */
+typedef struct mlh_particles_view {
+    int n;
+    double *x, *y, *z;
+    double *vx, *vy, *vz;
+    double *m, *u;
+} mlh_particles_view;
+
+typedef struct mlh_step_stats {
+    int steps;                       /* steps completed by this call */
+    unsigned int status;             /* accumulated MLH_ERR_* bits */
+    double dt;                       /* dt of the last step */
+    double time;                     /* simulation time after the call */
+    long long pair_interactions;     /* directed neighbour slots, summed over steps */
+    long long faces;                 /* Riemann problems solved, summed */
+    long long newton_iterations;     /* summed over faces and steps */
+    double device_ms;                /* device time of the call (CUDA events) */
+} mlh_step_stats;
+
+typedef struct mlh_ctx mlh_ctx;
+
+int mlh_abi_version(void);
+const char *mlh_last_error(void);
+
+/* Particles(N) + InitialDistribution::getAllParticles + MeshlessScheme ctor
+ * (demonstrator/src/MeshlessScheme.cpp:8-19): copies the initial state to the
+ * device and allocates all per-particle and per-interaction buffers. */
+int mlh_create(const mlh_config *cfg, const mlh_particles_view *init, mlh_ctx **out);
+void mlh_destroy(mlh_ctx *ctx);
+
+/* Host <-> device copies of the state (x, v, m, u). */
+int mlh_set_fields(mlh_ctx *ctx, const mlh_particles_view *src);
+int mlh_get_fields(mlh_ctx *ctx, mlh_particles_view *dst);
+
+/* `nsteps` MFV steps (MeshlessScheme.cpp:39-253: bin, neighbour search,
+ * density, pressure, dt, gradients, limiter, faces, reconstruction, Riemann,
+ * flux gather, kick/drift).  `dt_max` > 0 clamps dt (the dump-time clamp of
+ * MeshlessScheme.cpp:98-101); pass 0 for none.  stats may be NULL. */
+int mlh_step(mlh_ctx *ctx, int nsteps, double dt_max, mlh_step_stats *stats);
+
+/* Copy a named per-step array of the last step to host memory, for parity
+ * checks (the arrays the reference keeps as Particles members):
+ *   int32 : "off" (N+1), "noi", "noi_img" (N), "nnl" (uint32 index|image bits,
+ *           real neighbours first in the reference's order, then images by
+ *           parent index), "face_of" (per slot)
+ *   double: "omega", "rho", "P" (N); "grad_rho", "grad_vx", "grad_vy",
+ *           "grad_vz", "grad_P" (N*3, limited); "B" (N*dim*dim); "dt" (1);
+ *           "grid" (9: lo[3], hi[3], cells[3]); "F" (per slot, dim+2, the
+ *           flux of each interaction as the reference's Fij); "mF", "eF" (N),
+ *           "vF" (N*3).
+ * `count` receives the number of elements; `out` may be NULL to query it. */
+int mlh_stage_array(mlh_ctx *ctx, const char *name, void *out, long long capacity, long long *count);
+
+/* Per-kernel device times: when enabled, every launch of the step is
+ * bracketed by CUDA events on the context's stream.  mlh_kernel_times fills
+ * up to `max` entries (name, launches, total ms) and returns the count. */
+int mlh_set_kernel_timing(mlh_ctx *ctx, int enable);
+int mlh_kernel_times(mlh_ctx *ctx, const char **names, long long *launches, double *total_ms, int max);
+void mlh_reset_kernel_times(mlh_ctx *ctx);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* MLH_H */

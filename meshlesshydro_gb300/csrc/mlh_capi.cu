@@ -1,0 +1,527 @@
+// C ABI of the MFV step (include/mlh.h): context, device memory, copies,
+// step driver with capacity retries, parity dumps and kernel timing.
+#include "../../include/mlh.h"
+#include "mlh_kernels.h"
+
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+using namespace mlh;
+
+namespace {
+
+thread_local std::string g_last_error;
+
+int cuda_fail(cudaError_t e, const char *what) {
+    g_last_error = std::string(what) + ": " + cudaGetErrorString(e);
+    return MLH_ERR_CUDA;
+}
+
+#define CK(call)                                          \
+    do {                                                  \
+        cudaError_t e_ = (call);                          \
+        if (e_ != cudaSuccess) return cuda_fail(e_, #call); \
+    } while (0)
+
+template <class T>
+cudaError_t dalloc(T **p, size_t count) {
+    *p = nullptr;
+    if (count == 0) count = 1;
+    return cudaMalloc((void **)p, sizeof(T) * count);
+}
+
+}  // namespace
+
+struct mlh_ctx {
+    mlh_config cfg;
+    Params p;
+    int n = 0;
+    int device = 0;
+    int sm_count = 152;
+    cudaStream_t stream = nullptr;
+    cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+    // state
+    double *x = nullptr, *y = nullptr, *z = nullptr, *vx = nullptr, *vy = nullptr, *vz = nullptr, *m = nullptr, *u = nullptr;
+    float4 *posf = nullptr;
+    // grid
+    GridInfo *grid = nullptr;
+    double *boundsPart = nullptr;
+    int *cell = nullptr, *cellCount = nullptr, *cellStart = nullptr, *cellFill = nullptr, *cellList = nullptr;
+    // neighbours (capacity K slots per particle)
+    uint32_t *nbr = nullptr;
+    double *rr = nullptr, *ww = nullptr;
+    int *noi = nullptr, *noiImg = nullptr, *faceCnt = nullptr, *faceOff = nullptr, *faceOf = nullptr;
+    FaceRef *faces = nullptr;
+    double *Fface = nullptr;
+    Prim *prim = nullptr;
+    Geo *geo = nullptr;
+    Grad *grad = nullptr, *gradRaw = nullptr;
+    double *fluxSums = nullptr;
+    // scalars
+    unsigned *status = nullptr;
+    unsigned long long *dtbits = nullptr, *newtonSum = nullptr;
+    double *dt = nullptr, *simTime = nullptr;
+    int *stepsDone = nullptr;
+    int *scanTiles = nullptr, *scanTotal = nullptr;
+    bool debug_arrays = true;
+    // kernel timing
+    bool timing = false;
+    std::vector<cudaEvent_t> tev;   // pairs, in launch order
+    std::vector<int> tid;
+    double kt_ms[KT_COUNT] = {0};
+    long long kt_launches[KT_COUNT] = {0};
+};
+
+namespace {
+
+void free_neighbour_buffers(mlh_ctx *c) {
+    cudaFree(c->nbr); cudaFree(c->rr); cudaFree(c->ww); cudaFree(c->faceOf); cudaFree(c->faces); cudaFree(c->Fface);
+    c->nbr = nullptr; c->rr = nullptr; c->ww = nullptr; c->faceOf = nullptr; c->faces = nullptr; c->Fface = nullptr;
+}
+
+int alloc_neighbour_buffers(mlh_ctx *c) {
+    size_t slots = (size_t)c->n * c->p.K;
+    size_t faces = slots / 2 + (size_t)c->n + 16;
+    CK(dalloc(&c->nbr, slots));
+    CK(dalloc(&c->rr, slots));
+    CK(dalloc(&c->ww, slots));
+    CK(dalloc(&c->faceOf, slots));
+    CK(dalloc(&c->faces, faces));
+    CK(dalloc(&c->Fface, faces * 6));
+    return 0;
+}
+
+void free_cell_buffers(mlh_ctx *c) {
+    cudaFree(c->cellCount); cudaFree(c->cellStart); cudaFree(c->cellFill);
+    c->cellCount = c->cellStart = c->cellFill = nullptr;
+}
+
+int alloc_cell_buffers(mlh_ctx *c) {
+    size_t nc = (size_t)c->p.ncells_cap + 1;
+    CK(dalloc(&c->cellCount, nc));
+    CK(dalloc(&c->cellStart, nc + 1));
+    CK(dalloc(&c->cellFill, nc));
+    return 0;
+}
+
+long long estimate_cells(const mlh_config &cfg, const mlh_particles_view *v) {
+    double lo[3], hi[3];
+    const double *X[3] = {v->x, v->y, v->z};
+    long long total = 1;
+    for (int a = 0; a < cfg.dim; ++a) {
+        if (cfg.periodic) { lo[a] = cfg.box_lo[a]; hi[a] = cfg.box_hi[a]; }
+        else {
+            lo[a] = hi[a] = X[a][0];
+            for (int i = 1; i < v->n; ++i) { lo[a] = std::fmin(lo[a], X[a][i]); hi[a] = std::fmax(hi[a], X[a][i]); }
+        }
+        double c = std::floor((hi[a] - lo[a]) / cfg.kernel_size);
+        long long ci = c >= 1. ? (long long)c : 1;
+        if (!cfg.periodic) ci = ci + ci / 4 + 4;   // room for an expanding bounding box
+        total *= ci;
+    }
+    return total;
+}
+
+void timer_cb(void *vc, int id, int phase) {
+    mlh_ctx *c = (mlh_ctx *)vc;
+    cudaEvent_t e;
+    cudaEventCreate(&e);
+    cudaEventRecord(e, c->stream);
+    c->tev.push_back(e);
+    if (phase == 0) c->tid.push_back(id);
+}
+
+void collect_timers(mlh_ctx *c) {
+    for (size_t k = 0; k + 1 < c->tev.size(); k += 2) {
+        float ms = 0.f;
+        cudaEventElapsedTime(&ms, c->tev[k], c->tev[k + 1]);
+        int id = c->tid[k / 2];
+        c->kt_ms[id] += ms;
+        c->kt_launches[id] += 1;
+    }
+    for (auto e : c->tev) cudaEventDestroy(e);
+    c->tev.clear();
+    c->tid.clear();
+}
+
+StepArgs make_args(mlh_ctx *c, double dt_max) {
+    StepArgs a;
+    std::memset(&a, 0, sizeof(a));
+    a.p = c->p;
+    a.stream = c->stream;
+    a.face_blocks = c->sm_count * 8;
+    a.dt_max = dt_max;
+    a.x = c->x; a.y = c->y; a.z = c->z; a.vx = c->vx; a.vy = c->vy; a.vz = c->vz; a.m = c->m; a.u = c->u;
+    a.posf = c->posf;
+    a.grid = c->grid; a.boundsPart = c->boundsPart;
+    a.cell = c->cell; a.cellCount = c->cellCount; a.cellStart = c->cellStart; a.cellFill = c->cellFill;
+    a.cellList = c->cellList;
+    a.nbr = c->nbr; a.rr = c->rr; a.ww = c->ww;
+    a.noi = c->noi; a.noiImg = c->noiImg; a.faceCnt = c->faceCnt; a.faceOff = c->faceOff; a.faceOf = c->faceOf;
+    a.faces = c->faces;
+    a.prim = c->prim; a.geo = c->geo; a.grad = c->grad; a.gradRaw = c->debug_arrays ? c->gradRaw : nullptr;
+    a.Fface = c->Fface; a.fluxSums = c->debug_arrays ? c->fluxSums : nullptr;
+    a.status = c->status; a.dtbits = c->dtbits; a.newtonSum = c->newtonSum;
+    a.dt = c->dt; a.simTime = c->simTime; a.stepsDone = c->stepsDone;
+    a.scanTiles = c->scanTiles; a.scanTotal = c->scanTotal;
+    a.timer = c->timing ? timer_cb : nullptr;
+    a.timer_ctx = c;
+    return a;
+}
+
+void fill_params(mlh_ctx *c) {
+    const mlh_config &f = c->cfg;
+    Params &p = c->p;
+    p.n = c->n;
+    p.dim = f.dim;
+    p.periodic = f.periodic;
+    p.adaptive = f.adaptive_timestep;
+    p.slope = f.slope_limiting;
+    p.pairwise = f.pairwise_limiter;
+    p.mfm = f.meshless_finite_mass;
+    p.move = f.move_particles;
+    p.foqp = f.first_order_quad_point;
+    p.int_abs = f.int_abs;
+    p.img_pw = f.image_pairwise_limiter;
+    p.rmaxit = f.riemann_max_iter > 0 ? f.riemann_max_iter : 100;
+    p.h = f.kernel_size;
+    p.hsq = f.kernel_size * f.kernel_size;
+    p.h2 = f.kernel_size / 2.;
+    // Kernel::cubicSpline normalisation, demonstrator/src/Particles.cpp:10-15
+    const double h2 = p.h2;
+    p.sigma = f.dim == 2 ? 10. / (7. * M_PI * h2 * h2) : 1. / (M_PI * h2 * h2 * h2);
+    p.w0 = p.sigma * (1. - 3. / 2. * 0. * 0. * (1. - 0. / 2.));
+    p.gamma = f.gamma;
+    p.cfl_h = f.cfl * f.kernel_size;
+    p.beta = f.beta;
+    p.psi1 = f.psi1;
+    p.psi2 = f.psi2;
+    p.rtol = f.riemann_tol > 0. ? f.riemann_tol : 1e-10;
+    p.time_step = f.time_step;
+    for (int a = 0; a < 3; ++a) { p.box_lo[a] = f.box_lo[a]; p.box_hi[a] = f.box_hi[a]; }
+    // single-precision pre-filter bound: positions rounded to float move a
+    // distance of ~1e-7 relative to the box; 1e-3 relative on h^2 is ample
+    p.hsq_f = (float)(p.hsq * (1. + 1e-3));
+}
+
+int upload(mlh_ctx *c, const mlh_particles_view *v) {
+    size_t b = sizeof(double) * (size_t)c->n;
+    CK(cudaMemcpyAsync(c->x, v->x, b, cudaMemcpyHostToDevice, c->stream));
+    CK(cudaMemcpyAsync(c->y, v->y, b, cudaMemcpyHostToDevice, c->stream));
+    CK(cudaMemcpyAsync(c->vx, v->vx, b, cudaMemcpyHostToDevice, c->stream));
+    CK(cudaMemcpyAsync(c->vy, v->vy, b, cudaMemcpyHostToDevice, c->stream));
+    if (c->cfg.dim == 3) {
+        CK(cudaMemcpyAsync(c->z, v->z, b, cudaMemcpyHostToDevice, c->stream));
+        CK(cudaMemcpyAsync(c->vz, v->vz, b, cudaMemcpyHostToDevice, c->stream));
+    } else {
+        CK(cudaMemsetAsync(c->z, 0, b, c->stream));
+        CK(cudaMemsetAsync(c->vz, 0, b, c->stream));
+    }
+    CK(cudaMemcpyAsync(c->m, v->m, b, cudaMemcpyHostToDevice, c->stream));
+    CK(cudaMemcpyAsync(c->u, v->u, b, cudaMemcpyHostToDevice, c->stream));
+    pack_posf(c->x, c->y, c->z, c->n, c->cfg.dim, c->posf, c->stream);
+    CK(cudaGetLastError());
+    return 0;
+}
+
+}  // namespace
+
+extern "C" {
+
+int mlh_abi_version(void) { return MLH_ABI_VERSION; }
+const char *mlh_last_error(void) { return g_last_error.c_str(); }
+
+int mlh_create(const mlh_config *cfg, const mlh_particles_view *init, mlh_ctx **out) {
+    if (!cfg || !init || !out) { g_last_error = "null argument"; return MLH_ERR_INVALID; }
+    *out = nullptr;
+    if ((cfg->dim != 2 && cfg->dim != 3) || init->n < 1 || !(cfg->kernel_size > 0.) || !init->x || !init->y ||
+        !init->vx || !init->vy || !init->m || !init->u || (cfg->dim == 3 && (!init->z || !init->vz))) {
+        g_last_error = "invalid configuration or particle view";
+        return MLH_ERR_INVALID;
+    }
+    if (init->n > (int)IDX_MASK) { g_last_error = "too many particles"; return MLH_ERR_CAPACITY; }
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) { g_last_error = "no CUDA device"; return MLH_ERR_NO_DEVICE; }
+    mlh_ctx *c = new mlh_ctx();
+    c->cfg = *cfg;
+    c->n = init->n;
+    cudaGetDevice(&c->device);
+    cudaDeviceGetAttribute(&c->sm_count, cudaDevAttrMultiProcessorCount, c->device);
+    fill_params(c);
+    c->p.K = cfg->max_neighbours > 0 ? cfg->max_neighbours : (cfg->dim == 2 ? 40 : 64);
+    long long nc = estimate_cells(*cfg, init);
+    if (nc > (1ll << 30)) { delete c; g_last_error = "grid too large"; return MLH_ERR_CAPACITY; }
+    c->p.ncells_cap = (int)nc;
+    int rc = 0;
+    auto fail = [&](int r) { mlh_destroy(c); return r; };
+    if (cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking) != cudaSuccess) return fail(cuda_fail(cudaGetLastError(), "stream"));
+    cudaEventCreate(&c->ev0);
+    cudaEventCreate(&c->ev1);
+    size_t n = (size_t)c->n;
+#define A(ptr, cnt) if (dalloc(&c->ptr, cnt) != cudaSuccess) return fail(cuda_fail(cudaGetLastError(), "cudaMalloc " #ptr))
+    A(x, n); A(y, n); A(z, n); A(vx, n); A(vy, n); A(vz, n); A(m, n); A(u, n);
+    A(posf, n);
+    A(grid, 1); A(boundsPart, 304 * 6);
+    A(cell, n); A(cellList, n);
+    A(noi, n); A(noiImg, n); A(faceCnt, n); A(faceOff, n + 1);
+    A(prim, n); A(geo, n); A(grad, n); A(gradRaw, n); A(fluxSums, n * 5);
+    A(status, 1); A(dtbits, 1); A(newtonSum, 1); A(dt, 1); A(simTime, 1); A(stepsDone, 1);
+    A(scanTiles, n / 4096 + 1024); A(scanTotal, 1);
+#undef A
+    if ((rc = alloc_cell_buffers(c))) return fail(rc);
+    if ((rc = alloc_neighbour_buffers(c))) return fail(rc);
+    cudaMemsetAsync(c->status, 0, sizeof(unsigned), c->stream);
+    cudaMemsetAsync(c->simTime, 0, sizeof(double), c->stream);
+    cudaMemsetAsync(c->newtonSum, 0, sizeof(unsigned long long), c->stream);
+    cudaMemsetAsync(c->stepsDone, 0, sizeof(int), c->stream);
+    if ((rc = upload(c, init))) return fail(rc);
+    if (cudaStreamSynchronize(c->stream) != cudaSuccess) return fail(cuda_fail(cudaGetLastError(), "create sync"));
+    *out = c;
+    return 0;
+}
+
+void mlh_destroy(mlh_ctx *c) {
+    if (!c) return;
+    if (c->stream) cudaStreamSynchronize(c->stream);
+    void *ptrs[] = {c->x, c->y, c->z, c->vx, c->vy, c->vz, c->m, c->u, c->posf, c->grid, c->boundsPart, c->cell,
+                    c->cellList, c->noi, c->noiImg, c->faceCnt, c->faceOff, c->prim, c->geo, c->grad, c->gradRaw,
+                    c->fluxSums, c->status, c->dtbits, c->newtonSum, c->dt, c->simTime, c->stepsDone, c->scanTiles,
+                    c->scanTotal};
+    for (void *q : ptrs) if (q) cudaFree(q);
+    free_cell_buffers(c);
+    free_neighbour_buffers(c);
+    for (auto e : c->tev) cudaEventDestroy(e);
+    if (c->ev0) cudaEventDestroy(c->ev0);
+    if (c->ev1) cudaEventDestroy(c->ev1);
+    if (c->stream) cudaStreamDestroy(c->stream);
+    delete c;
+}
+
+int mlh_set_fields(mlh_ctx *c, const mlh_particles_view *v) {
+    if (!c || !v || v->n != c->n) { g_last_error = "size mismatch"; return MLH_ERR_INVALID; }
+    int rc = upload(c, v);
+    if (rc) return rc;
+    return 0;
+}
+
+int mlh_get_fields(mlh_ctx *c, mlh_particles_view *v) {
+    if (!c || !v || v->n != c->n) { g_last_error = "size mismatch"; return MLH_ERR_INVALID; }
+    size_t b = sizeof(double) * (size_t)c->n;
+    double *src[8] = {c->x, c->y, c->z, c->vx, c->vy, c->vz, c->m, c->u};
+    double *dst[8] = {v->x, v->y, v->z, v->vx, v->vy, v->vz, v->m, v->u};
+    for (int k = 0; k < 8; ++k) {
+        if (c->cfg.dim == 2 && (k == 2 || k == 5)) continue;
+        if (!dst[k]) continue;
+        CK(cudaMemcpyAsync(dst[k], src[k], b, cudaMemcpyDeviceToHost, c->stream));
+    }
+    CK(cudaStreamSynchronize(c->stream));
+    return 0;
+}
+
+int mlh_step(mlh_ctx *c, int nsteps, double dt_max, mlh_step_stats *stats) {
+    if (!c || nsteps < 0) { g_last_error = "invalid argument"; return MLH_ERR_INVALID; }
+    unsigned accumulated = 0;
+    long long pairs = 0, faces = 0;
+    unsigned long long newton = 0;
+    double dev_ms = 0.;
+    int done_total = 0;
+    int remaining = nsteps;
+    int retries = 0;
+    while (remaining > 0) {
+        CK(cudaMemsetAsync(c->status, 0, sizeof(unsigned), c->stream));
+        CK(cudaMemsetAsync(c->stepsDone, 0, sizeof(int), c->stream));
+        CK(cudaMemsetAsync(c->newtonSum, 0, sizeof(unsigned long long), c->stream));
+        CK(cudaEventRecord(c->ev0, c->stream));
+        StepArgs a = make_args(c, dt_max);
+        for (int k = 0; k < remaining; ++k) step(a);
+        CK(cudaEventRecord(c->ev1, c->stream));
+        CK(cudaGetLastError());
+        CK(cudaStreamSynchronize(c->stream));
+        float ms = 0.f;
+        cudaEventElapsedTime(&ms, c->ev0, c->ev1);
+        dev_ms += ms;
+        if (c->timing) collect_timers(c);
+        unsigned st = 0;
+        int done = 0;
+        unsigned long long nsum = 0;
+        CK(cudaMemcpy(&st, c->status, sizeof(unsigned), cudaMemcpyDeviceToHost));
+        CK(cudaMemcpy(&done, c->stepsDone, sizeof(int), cudaMemcpyDeviceToHost));
+        CK(cudaMemcpy(&nsum, c->newtonSum, sizeof(unsigned long long), cudaMemcpyDeviceToHost));
+        newton += nsum;
+        done_total += done;
+        remaining -= done;
+        // per-step interaction counts of the last step
+        int ftot = 0;
+        CK(cudaMemcpy(&ftot, c->faceOff + c->n, sizeof(int), cudaMemcpyDeviceToHost));
+        faces += (long long)ftot * done;
+        pairs += 2ll * ftot * done;
+        if (st & (MLH_ERR_NGB_OVERFLOW | ST_CAPACITY)) {
+            if (++retries > 8) { accumulated |= st; g_last_error = "capacity retries exhausted"; break; }
+            if (st & MLH_ERR_NGB_OVERFLOW) {
+                free_neighbour_buffers(c);
+                c->p.K = c->p.K + c->p.K / 2;
+                int rc = alloc_neighbour_buffers(c);
+                if (rc) return rc;
+            }
+            if (st & ST_CAPACITY) {
+                free_cell_buffers(c);
+                c->p.ncells_cap = c->p.ncells_cap * 2;
+                int rc = alloc_cell_buffers(c);
+                if (rc) return rc;
+            }
+            continue;
+        }
+        accumulated |= st;
+        if (done == 0) break;
+    }
+    if (stats) {
+        stats->steps = done_total;
+        stats->status = accumulated;
+        cudaMemcpy(&stats->dt, c->dt, sizeof(double), cudaMemcpyDeviceToHost);
+        cudaMemcpy(&stats->time, c->simTime, sizeof(double), cudaMemcpyDeviceToHost);
+        stats->pair_interactions = pairs;
+        stats->faces = faces;
+        stats->newton_iterations = (long long)newton;
+        stats->device_ms = dev_ms;
+    }
+    return (int)(accumulated & ~(unsigned)MLH_ERR_NGB_OVERFLOW & ~ST_CAPACITY) ? (int)accumulated : 0;
+}
+
+int mlh_stage_array(mlh_ctx *c, const char *name, void *out, long long capacity, long long *count) {
+    if (!c || !name) return MLH_ERR_INVALID;
+    const std::string nm(name);
+    const int n = c->n, K = c->p.K, D = c->cfg.dim;
+    std::vector<int> noi(n), noiImg(n);
+    auto need_lists = [&]() -> int {
+        CK(cudaMemcpy(noi.data(), c->noi, sizeof(int) * n, cudaMemcpyDeviceToHost));
+        CK(cudaMemcpy(noiImg.data(), c->noiImg, sizeof(int) * n, cudaMemcpyDeviceToHost));
+        return 0;
+    };
+    CK(cudaStreamSynchronize(c->stream));
+    auto put = [&](const void *src, size_t elems, size_t esize) -> int {
+        if (count) *count = (long long)elems;
+        if (!out) return 0;
+        if ((long long)elems > capacity) { g_last_error = "capacity too small"; return MLH_ERR_INVALID; }
+        std::memcpy(out, src, elems * esize);
+        return 0;
+    };
+    if (nm == "noi" || nm == "noi_img" || nm == "off") {
+        if (int rc = need_lists()) return rc;
+        if (nm == "noi") return put(noi.data(), n, 4);
+        if (nm == "noi_img") return put(noiImg.data(), n, 4);
+        std::vector<int> off(n + 1, 0);
+        for (int i = 0; i < n; ++i) off[i + 1] = off[i] + noi[i] + noiImg[i];
+        return put(off.data(), n + 1, 4);
+    }
+    if (nm == "nnl" || nm == "face_of" || nm == "F") {
+        if (int rc = need_lists()) return rc;
+        std::vector<uint32_t> nb((size_t)n * K);
+        std::vector<int> fo((size_t)n * K);
+        CK(cudaMemcpy(nb.data(), c->nbr, sizeof(uint32_t) * nb.size(), cudaMemcpyDeviceToHost));
+        CK(cudaMemcpy(fo.data(), c->faceOf, sizeof(int) * fo.size(), cudaMemcpyDeviceToHost));
+        if (nm == "nnl" || nm == "face_of") {
+            std::vector<uint32_t> o;
+            for (int i = 0; i < n; ++i)
+                for (int s = 0; s < noi[i] + noiImg[i]; ++s)
+                    o.push_back(nm == "nnl" ? nb[(size_t)i * K + s] : (uint32_t)fo[(size_t)i * K + s]);
+            return put(o.data(), o.size(), 4);
+        }
+        int ftot = 0;
+        CK(cudaMemcpy(&ftot, c->faceOff + n, sizeof(int), cudaMemcpyDeviceToHost));
+        std::vector<double> F((size_t)ftot * 6 + 6);
+        CK(cudaMemcpy(F.data(), c->Fface, sizeof(double) * (size_t)ftot * 6, cudaMemcpyDeviceToHost));
+        std::vector<double> o;
+        const int NV = D + 2;
+        for (int i = 0; i < n; ++i)
+            for (int s = 0; s < noi[i] + noiImg[i]; ++s) {
+                int f = fo[(size_t)i * K + s];
+                double sg = f > 0 ? 1. : -1.;
+                int id = (f > 0 ? f : -f) - 1;
+                for (int k = 0; k < NV; ++k) o.push_back(f == 0 ? 0. : sg * F[(size_t)id * 6 + k]);
+            }
+        return put(o.data(), o.size(), 8);
+    }
+    if (nm == "omega" || nm == "rho" || nm == "P" || nm == "c" || nm == "B") {
+        std::vector<Prim> pr(n);
+        std::vector<Geo> ge(n);
+        CK(cudaMemcpy(pr.data(), c->prim, sizeof(Prim) * n, cudaMemcpyDeviceToHost));
+        CK(cudaMemcpy(ge.data(), c->geo, sizeof(Geo) * n, cudaMemcpyDeviceToHost));
+        std::vector<double> o;
+        for (int i = 0; i < n; ++i) {
+            if (nm == "omega") o.push_back(ge[i].omega);
+            else if (nm == "rho") o.push_back(pr[i].rho);
+            else if (nm == "P") o.push_back(pr[i].P);
+            else if (nm == "c") o.push_back(ge[i].c);
+            else for (int k = 0; k < D * D; ++k) o.push_back(ge[i].B[k]);
+        }
+        return put(o.data(), o.size(), 8);
+    }
+    if (nm.compare(0, 5, "grad_") == 0 || nm.compare(0, 8, "gradraw_") == 0) {
+        const bool raw = nm.compare(0, 8, "gradraw_") == 0;
+        const std::string f = nm.substr(raw ? 8 : 5);
+        int blk = f == "rho" ? 0 : f == "vx" ? 1 : f == "vy" ? 2 : f == "vz" ? 3 : f == "P" ? 4 : -1;
+        if (blk < 0 || (raw && !c->debug_arrays)) return MLH_ERR_INVALID;
+        std::vector<Grad> g(n);
+        CK(cudaMemcpy(g.data(), raw ? c->gradRaw : c->grad, sizeof(Grad) * n, cudaMemcpyDeviceToHost));
+        std::vector<double> o((size_t)n * 3);
+        for (int i = 0; i < n; ++i)
+            for (int a = 0; a < 3; ++a) o[(size_t)i * 3 + a] = g[i].g[blk * 3 + a];
+        return put(o.data(), o.size(), 8);
+    }
+    if (nm == "mF" || nm == "eF" || nm == "vF") {
+        std::vector<double> fs((size_t)n * 5);
+        CK(cudaMemcpy(fs.data(), c->fluxSums, sizeof(double) * fs.size(), cudaMemcpyDeviceToHost));
+        std::vector<double> o;
+        for (int i = 0; i < n; ++i) {
+            if (nm == "mF") o.push_back(fs[(size_t)i * 5]);
+            else if (nm == "eF") o.push_back(fs[(size_t)i * 5 + 1]);
+            else for (int a = 0; a < 3; ++a) o.push_back(fs[(size_t)i * 5 + 2 + a]);
+        }
+        return put(o.data(), o.size(), 8);
+    }
+    if (nm == "dt") {
+        double d;
+        CK(cudaMemcpy(&d, c->dt, sizeof(double), cudaMemcpyDeviceToHost));
+        return put(&d, 1, 8);
+    }
+    if (nm == "grid") {
+        GridInfo g;
+        CK(cudaMemcpy(&g, c->grid, sizeof(GridInfo), cudaMemcpyDeviceToHost));
+        double o[9];
+        for (int a = 0; a < 3; ++a) {
+            o[a] = a < D ? g.lo[a] : 0.;
+            o[3 + a] = a < D ? g.hi[a] : 0.;
+            o[6 + a] = a < D ? g.cells[a] : 0.;
+        }
+        return put(o, 9, 8);
+    }
+    g_last_error = "unknown array " + nm;
+    return MLH_ERR_INVALID;
+}
+
+int mlh_set_kernel_timing(mlh_ctx *c, int enable) {
+    if (!c) return MLH_ERR_INVALID;
+    c->timing = enable != 0;
+    return 0;
+}
+
+int mlh_kernel_times(mlh_ctx *c, const char **names, long long *launches, double *total_ms, int max) {
+    if (!c) return -1;
+    int k = 0;
+    for (int id = 0; id < KT_COUNT && k < max; ++id, ++k) {
+        if (names) names[k] = kernel_timer_name(id);
+        if (launches) launches[k] = c->kt_launches[id];
+        if (total_ms) total_ms[k] = c->kt_ms[id];
+    }
+    return k;
+}
+
+void mlh_reset_kernel_times(mlh_ctx *c) {
+    if (!c) return;
+    for (int id = 0; id < KT_COUNT; ++id) { c->kt_ms[id] = 0.; c->kt_launches[id] = 0; }
+}
+
+}  // extern "C"

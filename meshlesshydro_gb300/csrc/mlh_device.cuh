@@ -1,0 +1,108 @@
+// Device-side definitions shared by the MFV kernels (sm_103a).
+//
+// Physics and arithmetic follow the reference demonstrator
+// (jammartin/meshlessHydro, demonstrator/src/Particles.cpp, Riemann.cpp,
+// Helper.cpp); each function cites the lines it restates.
+#pragma once
+#include <cstdint>
+#include <cuda_runtime.h>
+
+namespace mlh {
+
+constexpr unsigned IMG_SHIFT = 29;
+constexpr unsigned IDX_MASK = (1u << IMG_SHIFT) - 1u;
+constexpr double DBL_MIN_ = 2.2250738585072014e-308;   // numeric_limits<double>::min()
+constexpr double DBL_MAX_ = 1.7976931348623157e+308;   // numeric_limits<double>::max()
+
+// status bits (mirror MLH_ERR_* of include/mlh.h)
+enum : unsigned {
+    ST_NGB_OVERFLOW = 1u << 0,
+    ST_NEG_PRESSURE = 1u << 1,
+    ST_NEG_DENSITY = 1u << 2,
+    ST_NEG_MASS = 1u << 3,
+    ST_NEG_ENERGY = 1u << 4,
+    ST_NEWTON = 1u << 5,
+    ST_VACUUM = 1u << 6,
+    ST_GRID = 1u << 7,
+    ST_NO_NEIGHBOUR = 1u << 8,
+    ST_ASYMMETRIC = 1u << 9,
+    ST_NAN = 1u << 10,
+    ST_TIMEOUT = 1u << 11,
+    ST_CAPACITY = 1u << 23,   // a fixed-size device buffer was too small
+};
+
+// Uniform search grid (Domain::createGrid, demonstrator/src/Domain.cpp:9-54).
+struct GridInfo {
+    double lo[3], hi[3], cs[3];
+    int cells[3];
+    int ncells;
+};
+
+// Everything a kernel needs to know about the run, passed by value.
+struct Params {
+    int n, dim, periodic, adaptive, slope, pairwise, mfm, move, foqp, int_abs, img_pw, rmaxit;
+    int K;                 // neighbour slots per particle
+    int ncells_cap;
+    double h, hsq, h2, sigma, w0, gamma, cfl_h, beta, psi1, psi2, rtol, time_step;
+    double box_lo[3], box_hi[3];
+    float hsq_f;           // conservative single-precision bound for the pre-filter
+};
+
+// Per-particle records (array of structures: one particle's values sit in
+// one or two 64-byte sectors for the random-access neighbour loops).
+struct Prim {       // positions, primitive state of this step
+    double x, y, z, rho, vx, vy, vz, P;
+};
+struct Grad {       // limited gradients: rho, vx, vy, vz, P (x,y,z each) + pad
+    double g[16];
+};
+struct Geo {        // E_i^{-1}, 1/omega_i, omega_i, sound speed
+    double B[9];
+    double V, omega, c;
+};
+struct FaceRef {    // canonical face: owner i, slot index, reverse slot (images)
+    int i, slot, rslot, pad;
+};
+
+// Kernel::cubicSpline, demonstrator/src/Particles.cpp:7-24.  sigma is
+// precomputed on the host with the reference's expression; pow(2-q, 3.) is
+// written as a product.
+__device__ __forceinline__ double kernelW(double r, const Params &p) {
+    double q = r / p.h2;
+    if (0. <= q && q <= 1.) return p.sigma * (1. - 3. / 2. * q * q * (1. - q / 2.));
+    if (1. < q && q < 2.) { double t = 2. - q; return p.sigma / 4. * (t * t * t); }
+    return 0.;
+}
+
+// Ghost image coordinate, Particles.cpp:2123-2142.
+__device__ __forceinline__ bool in_band(double xa, double lo, double hi, double h) {
+    return xa <= lo + h || hi - h < xa;
+}
+__device__ __forceinline__ double image_coord(double xa, double lo, double hi, double h) {
+    if (xa <= lo + h) return hi + (xa - lo);
+    return lo - (hi - xa);
+}
+
+// abs() as bound by the reference's limiter code (fabs, or int abs(int) with
+// x86 conversion semantics: NaN / out of range -> INT_MIN, abs(INT_MIN) = INT_MIN).
+__device__ __forceinline__ double ref_abs(double x, int int_abs) {
+    if (!int_abs) return fabs(x);
+    if (!(x > -2147483649.0 && x < 2147483648.0)) return -2147483648.0;
+    int t = (int)x;
+    if (t == (int)0x80000000) return -2147483648.0;
+    return (double)(t < 0 ? -t : t);
+}
+
+template <int D>
+__device__ __forceinline__ double dotD(const double *a, const double *b) {
+    double r = 0.;
+#pragma unroll
+    for (int k = 0; k < D; ++k) r += a[k] * b[k];
+    return r;
+}
+
+__device__ __forceinline__ void flag(unsigned *status, unsigned bits) {
+    atomicOr(status, bits);
+}
+
+}  // namespace mlh

@@ -1,0 +1,1158 @@
+// MFV timestep kernels for GB300 (sm_103a), FP64 state.
+//
+// One step = the stage sequence of the reference's MeshlessScheme::run
+// (jammartin/meshlessHydro, demonstrator/src/MeshlessScheme.cpp:39-253):
+//   bounds + grid        Particles::getDomainLimits / Domain::createGrid
+//   bin                  Particles::assignParticlesAndCells
+//   neighbour search     Particles::gridNNS + ghostNNS (images via wrapped cells)
+//   density, pressure    Particles::compDensity / compPressure
+//   dt                   Particles::compGlobalTimestep
+//   E^-1, gradients,     Particles::compPsijTilde / gradient / slopeLimiter
+//   limiter
+//   faces                compEffectiveFace + compRiemannStatesLR +
+//                        solveRiemannProblems (one thread per canonical face)
+//   gather + kick/drift  collectFluxes + updateStateAndPosition
+//
+// Determinism: no floating-point atomics.  Every per-particle sum runs over the
+// neighbour list in the reference's order; each face flux is computed once,
+// from the side of the lower particle index, and gathered with sign.
+#include "mlh_device.cuh"
+#include "mlh_riemann.cuh"
+#include "mlh_kernels.h"
+
+#include <cfloat>
+
+namespace mlh {
+
+// ------------------------------------------------------------------ helpers
+
+__device__ __forceinline__ double atomic_min_pos_double(unsigned long long *addr, double v) {
+    // positive doubles order like their bit patterns
+    return (double)atomicMin(addr, (unsigned long long)__double_as_longlong(v));
+}
+
+template <typename T>
+__device__ __forceinline__ T warp_reduce_sum(T v) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    return v;
+}
+
+// ------------------------------------------------------------------ scan
+
+// Exclusive scan of int counts in three launches (tile reduce, scan of tile
+// sums in one block, tile scan).  Tile = 1024 threads x 4 items.
+constexpr int SCAN_T = 1024, SCAN_I = 4, SCAN_TILE = SCAN_T * SCAN_I;
+
+__device__ __forceinline__ int block_exclusive_scan(int v, int *smem, int &total) {
+    int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    int x = v;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        int y = __shfl_up_sync(0xffffffffu, x, o);
+        if (lane >= o) x += y;
+    }
+    if (lane == 31) smem[w] = x;
+    __syncthreads();
+    if (w == 0) {
+        int s = (lane < (int)(blockDim.x >> 5)) ? smem[lane] : 0;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            int y = __shfl_up_sync(0xffffffffu, s, o);
+            if (lane >= o) s += y;
+        }
+        smem[lane] = s;
+    }
+    __syncthreads();
+    int base = w > 0 ? smem[w - 1] : 0;
+    total = smem[(blockDim.x >> 5) - 1];
+    __syncthreads();
+    return base + x - v;
+}
+
+__global__ void k_scan_reduce(const int *__restrict__ in, int n, int *__restrict__ tile_sums) {
+    __shared__ int smem[32];
+    long long base = (long long)blockIdx.x * SCAN_TILE;
+    int s = 0;
+    for (int k = 0; k < SCAN_I; ++k) {
+        long long idx = base + (long long)k * SCAN_T + threadIdx.x;
+        if (idx < n) s += in[idx];
+    }
+    s = warp_reduce_sum(s);
+    if ((threadIdx.x & 31) == 0) smem[threadIdx.x >> 5] = s;
+    __syncthreads();
+    if (threadIdx.x < 32) {
+        int v = threadIdx.x < (blockDim.x >> 5) ? smem[threadIdx.x] : 0;
+        v = warp_reduce_sum(v);
+        if (threadIdx.x == 0) tile_sums[blockIdx.x] = v;
+    }
+}
+
+__global__ void k_scan_tiles(int *__restrict__ tile_sums, int ntiles, int *__restrict__ total_out) {
+    __shared__ int smem[32];
+    int carry = 0;
+    for (int b = 0; b < ntiles; b += SCAN_T) {
+        int idx = b + threadIdx.x;
+        int v = idx < ntiles ? tile_sums[idx] : 0;
+        int tot;
+        int ex = block_exclusive_scan(v, smem, tot);
+        if (idx < ntiles) tile_sums[idx] = carry + ex;
+        carry += tot;
+    }
+    if (threadIdx.x == 0) *total_out = carry;
+}
+
+__global__ void k_scan_apply(const int *__restrict__ in, int n, const int *__restrict__ tile_offsets,
+                             int *__restrict__ out, const int *__restrict__ total, int write_total_at_n) {
+    __shared__ int smem[32];
+    long long base = (long long)blockIdx.x * SCAN_TILE;
+    long long idx0 = base + (long long)threadIdx.x * SCAN_I;
+    int v[SCAN_I];
+    int loc = 0;
+#pragma unroll
+    for (int k = 0; k < SCAN_I; ++k) {
+        long long idx = idx0 + k;
+        v[k] = idx < n ? in[idx] : 0;
+        loc += v[k];
+    }
+    int tot;
+    int ex = block_exclusive_scan(loc, smem, tot) + tile_offsets[blockIdx.x];
+#pragma unroll
+    for (int k = 0; k < SCAN_I; ++k) {
+        long long idx = idx0 + k;
+        if (idx < n) out[idx] = ex;
+        ex += v[k];
+    }
+    if (write_total_at_n && blockIdx.x == 0 && threadIdx.x == 0) out[n] = *total;
+}
+
+void exclusive_scan(const int *in, int n, int *out, int *tile_buf, int *total, cudaStream_t s) {
+    int ntiles = (n + SCAN_TILE - 1) / SCAN_TILE;
+    if (ntiles < 1) ntiles = 1;
+    k_scan_reduce<<<ntiles, SCAN_T, 0, s>>>(in, n, tile_buf);
+    k_scan_tiles<<<1, SCAN_T, 0, s>>>(tile_buf, ntiles, total);
+    k_scan_apply<<<ntiles, SCAN_T, 0, s>>>(in, n, tile_buf, out, total, 1);
+}
+
+// ------------------------------------------------------------------ bounds + grid
+
+// Particles::getDomainLimits (Particles.cpp:228-267): lo = min over all
+// particles; because of `else if` and numeric_limits<double>::min(), hi = the
+// max over i >= 1 of the x_i that are not below the running minimum of
+// x_0..x_{i-1}, or DBL_MIN.  The partial pass computes min over all i and max
+// over i >= 1; the final pass falls back to the sequential rule whenever x_0 is
+// above every other particle (the only case where the two differ).
+constexpr int BOUNDS_BLOCKS = 304, BOUNDS_T = 256;
+
+template <int D>
+__global__ void k_bounds_partial(const double *__restrict__ x, const double *__restrict__ y,
+                                 const double *__restrict__ z, int n, double *__restrict__ part) {
+    __shared__ double smin[3][BOUNDS_T / 32], smax[3][BOUNDS_T / 32];
+    const double *X[3] = {x, y, z};
+    double mn[3], mx[3];
+    for (int a = 0; a < 3; ++a) { mn[a] = DBL_MAX_; mx[a] = -DBL_MAX_; }
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+#pragma unroll
+        for (int a = 0; a < D; ++a) {
+            double v = X[a][i];
+            mn[a] = fmin(mn[a], v);
+            if (i >= 1) mx[a] = fmax(mx[a], v);
+        }
+    }
+#pragma unroll
+    for (int a = 0; a < D; ++a) {
+        for (int o = 16; o > 0; o >>= 1) {
+            mn[a] = fmin(mn[a], __shfl_xor_sync(0xffffffffu, mn[a], o));
+            mx[a] = fmax(mx[a], __shfl_xor_sync(0xffffffffu, mx[a], o));
+        }
+        if ((threadIdx.x & 31) == 0) { smin[a][threadIdx.x >> 5] = mn[a]; smax[a][threadIdx.x >> 5] = mx[a]; }
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        for (int a = 0; a < D; ++a) {
+            double a0 = DBL_MAX_, a1 = -DBL_MAX_;
+            for (int w = 0; w < BOUNDS_T / 32; ++w) { a0 = fmin(a0, smin[a][w]); a1 = fmax(a1, smax[a][w]); }
+            part[(blockIdx.x * 3 + a) * 2 + 0] = a0;
+            part[(blockIdx.x * 3 + a) * 2 + 1] = a1;
+        }
+    }
+}
+
+// Final pass + Domain::createGrid (Domain.cpp:9-54).  For periodic runs the
+// bounds are the configured box.
+template <int D>
+__global__ void k_bounds_final(const double *__restrict__ x, const double *__restrict__ y,
+                               const double *__restrict__ z, const double *__restrict__ part, int nparts,
+                               Params p, GridInfo *__restrict__ grid, unsigned *__restrict__ status) {
+    if (threadIdx.x != 0) return;
+    const double *X[3] = {x, y, z};
+    GridInfo g;
+    for (int a = 0; a < 3; ++a) { g.lo[a] = 0.; g.hi[a] = 0.; g.cs[a] = 1.; g.cells[a] = 1; }
+    for (int a = 0; a < D; ++a) {
+        if (p.periodic) { g.lo[a] = p.box_lo[a]; g.hi[a] = p.box_hi[a]; continue; }
+        double mn = DBL_MAX_, mx1 = -DBL_MAX_;
+        for (int b = 0; b < nparts; ++b) { mn = fmin(mn, part[(b * 3 + a) * 2]); mx1 = fmax(mx1, part[(b * 3 + a) * 2 + 1]); }
+        double x0 = X[a][0];
+        double hi;
+        if (p.n < 2 || !(mx1 >= x0)) {
+            // sequential rule of the reference
+            double lo_s = DBL_MAX_, hi_s = DBL_MIN_;
+            for (int i = 0; i < p.n; ++i) {
+                double v = X[a][i];
+                if (v < lo_s) lo_s = v;
+                else if (v > hi_s) hi_s = v;
+            }
+            hi = hi_s;
+        } else {
+            hi = mx1 > DBL_MIN_ ? mx1 : DBL_MIN_;
+        }
+        g.lo[a] = mn;
+        g.hi[a] = hi;
+    }
+    long long total = 1;
+    for (int a = 0; a < D; ++a) {
+        double c = floor((g.hi[a] - g.lo[a]) / p.h);
+        int ci = (c >= 1. && c < 2147483647.) ? (int)c : 1;
+        if (!(c >= 1.)) flag(status, ST_GRID);
+        if (p.periodic && ci < 3) flag(status, ST_GRID);
+        g.cells[a] = ci;
+        total *= ci;
+    }
+    for (int a = 0; a < D; ++a) g.cs[a] = (g.hi[a] - g.lo[a]) / (double)g.cells[a];
+    if (total > p.ncells_cap) { flag(status, ST_CAPACITY); total = p.ncells_cap; }
+    g.ncells = (int)total;
+    *grid = g;
+}
+
+// Particles::assignParticlesAndCells (Particles.cpp:270-322).
+template <int D>
+__global__ void k_assign(const double *__restrict__ x, const double *__restrict__ y, const double *__restrict__ z,
+                         int n, const GridInfo *__restrict__ gridp, int *__restrict__ cell,
+                         int *__restrict__ cellCount, unsigned *__restrict__ status) {
+    const GridInfo g = *gridp;
+    const double *X[3] = {x, y, z};
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        int fl[3] = {0, 0, 0};
+        bool bad = false;
+#pragma unroll
+        for (int a = 0; a < D; ++a) {
+            double f = floor((X[a][i] - g.lo[a]) / g.cs[a]);
+            int fi = (f > -1e9 && f < 1e9) ? (int)f : -1;
+            if (fi == g.cells[a]) fi -= 1;
+            if (fi < 0 || fi >= g.cells[a]) { bad = true; fi = fi < 0 ? 0 : g.cells[a] - 1; }
+            fl[a] = fi;
+        }
+        if (bad) flag(status, ST_GRID);
+        int c = fl[0] + fl[1] * g.cells[0] + (D == 3 ? fl[2] * g.cells[0] * g.cells[1] : 0);
+        if (c >= g.ncells) { c = g.ncells - 1; flag(status, ST_GRID); }
+        cell[i] = c;
+        atomicAdd(&cellCount[c], 1);
+    }
+}
+
+__global__ void k_fill_cells(const int *__restrict__ cell, int n, const int *__restrict__ cellStart,
+                             int *__restrict__ cellFill, int *__restrict__ cellList) {
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        int c = cell[i];
+        int pos = atomicAdd(&cellFill[c], 1);
+        cellList[cellStart[c] + pos] = i;
+    }
+}
+
+// Members of a cell in ascending particle index: the order in which
+// assignParticlesAndCells pushes them (Particles.cpp:319).
+__global__ void k_sort_cells(const GridInfo *__restrict__ gridp, const int *__restrict__ cellStart,
+                             int *__restrict__ cellList) {
+    int nc = gridp->ncells;
+    for (int c = blockIdx.x * blockDim.x + threadIdx.x; c < nc; c += gridDim.x * blockDim.x) {
+        int b = cellStart[c], e = cellStart[c + 1];
+        for (int k = b + 1; k < e; ++k) {
+            int v = cellList[k];
+            int t = k - 1;
+            while (t >= b && cellList[t] > v) { cellList[t + 1] = cellList[t]; --t; }
+            cellList[t + 1] = v;
+        }
+    }
+}
+
+// ------------------------------------------------------------------ neighbour search
+
+// Particles::gridNNS (Particles.cpp:324-365) over the 3^D stencil of
+// Domain::getNeighborCells (Domain.cpp:83-118, x outer, z inner), and the
+// periodic images of Particles::ghostNNS (Particles.cpp:2237-2260) through
+// wrapped stencil cells, appended after the real neighbours in parent order.
+// A single-precision test with a conservative bound rejects most candidates;
+// the accepted ones are tested in FP64 exactly as the reference does
+// (d^2 = (dx*dx + dy*dy) + dz*dz < h*h, no fused multiply-add).
+// Then Particles::compDensity/compOmega (Particles.cpp:1151-1184, 2262-2290)
+// and compPressure (:1272-1288) for the particle.
+template <int D>
+__global__ void __launch_bounds__(128) k_neighbours(
+    Params p, const GridInfo *__restrict__ gridp, const double *__restrict__ x, const double *__restrict__ y,
+    const double *__restrict__ z, const float4 *__restrict__ posf, const double *__restrict__ vx,
+    const double *__restrict__ vy, const double *__restrict__ vz, const double *__restrict__ m,
+    const double *__restrict__ u, const int *__restrict__ cell, const int *__restrict__ cellStart,
+    const int *__restrict__ cellList, uint32_t *__restrict__ nbr, double *__restrict__ rr,
+    double *__restrict__ ww, int *__restrict__ noi, int *__restrict__ noiImg, int *__restrict__ faceCnt,
+    Prim *__restrict__ prim, Geo *__restrict__ geo, unsigned *__restrict__ status) {
+    const GridInfo g = *gridp;
+    const double *X[3] = {x, y, z};
+    const int K = p.K;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < p.n; i += gridDim.x * blockDim.x) {
+        double xi[3] = {0., 0., 0.};
+#pragma unroll
+        for (int a = 0; a < D; ++a) xi[a] = X[a][i];
+        const float4 fi = posf[i];
+        const int ic = cell[i];
+        const int ix = ic % g.cells[0];
+        const int iy = (ic / g.cells[0]) % g.cells[1];
+        const int iz = D == 3 ? ic / (g.cells[0] * g.cells[1]) : 0;
+        const size_t base = (size_t)i * K;
+        int nr = 0, ni = 0;
+        bool overflow = false;
+        for (int k = ix - 1; k <= ix + 1; ++k)
+            for (int l = iy - 1; l <= iy + 1; ++l)
+                for (int mm = (D == 3 ? iz - 1 : 0); mm <= (D == 3 ? iz + 1 : 0); ++mm) {
+                    int cc[3] = {k, l, mm};
+                    unsigned wrap = 0;
+                    bool skip = false;
+#pragma unroll
+                    for (int a = 0; a < D; ++a) {
+                        if (cc[a] < 0 || cc[a] >= g.cells[a]) {
+                            if (!p.periodic) skip = true;
+                            cc[a] = cc[a] < 0 ? cc[a] + g.cells[a] : cc[a] - g.cells[a];
+                            wrap |= 1u << a;
+                        }
+                    }
+                    if (skip) continue;
+                    int c = cc[0] + cc[1] * g.cells[0] + (D == 3 ? cc[2] * g.cells[0] * g.cells[1] : 0);
+                    int b = cellStart[c], e = cellStart[c + 1];
+                    for (int t = b; t < e; ++t) {
+                        int j = cellList[t];
+                        if (!wrap) {
+                            if (j == i) continue;
+                            float4 fj = posf[j];
+                            float dx = fj.x - fi.x, dy = fj.y - fi.y, dz = fj.z - fi.z;
+                            float d2f = dx * dx + dy * dy + (D == 3 ? dz * dz : 0.f);
+                            if (d2f > p.hsq_f) continue;
+                            double ex = __dsub_rn(X[0][j], xi[0]), ey = __dsub_rn(X[1][j], xi[1]);
+                            double d2 = __dadd_rn(__dmul_rn(ex, ex), __dmul_rn(ey, ey));
+                            if (D == 3) { double ez = __dsub_rn(X[2][j], xi[2]); d2 = __dadd_rn(d2, __dmul_rn(ez, ez)); }
+                            if (d2 < p.hsq) {
+                                if (nr + ni < K) {
+                                    nbr[base + nr] = (uint32_t)j;
+                                    rr[base + nr] = sqrt(d2);
+                                } else overflow = true;
+                                ++nr;
+                            }
+                        } else {
+                            double xj[3];
+                            bool ok = true;
+#pragma unroll
+                            for (int a = 0; a < D; ++a) {
+                                xj[a] = X[a][j];
+                                if (wrap & (1u << a)) {
+                                    if (in_band(xj[a], g.lo[a], g.hi[a], p.h)) xj[a] = image_coord(xj[a], g.lo[a], g.hi[a], p.h);
+                                    else ok = false;
+                                }
+                            }
+                            if (!ok) continue;
+                            double ex = __dsub_rn(xj[0], xi[0]), ey = __dsub_rn(xj[1], xi[1]);
+                            double d2 = __dadd_rn(__dmul_rn(ex, ex), __dmul_rn(ey, ey));
+                            if (D == 3) { double ez = __dsub_rn(xj[2], xi[2]); d2 = __dadd_rn(d2, __dmul_rn(ez, ez)); }
+                            if (d2 < p.hsq) {
+                                if (nr + ni < K) {
+                                    // images grow downwards from the end of the slot range
+                                    nbr[base + K - 1 - ni] = (uint32_t)j | (wrap << IMG_SHIFT);
+                                    rr[base + K - 1 - ni] = sqrt(d2);
+                                } else overflow = true;
+                                ++ni;
+                            }
+                        }
+                    }
+                }
+        if (overflow || nr + ni > K) {
+            flag(status, ST_NGB_OVERFLOW);
+            if (nr > K) nr = K;
+            ni = K - nr < ni ? K - nr : ni;
+        }
+        // move images behind the real neighbours, ordered by parent index
+        for (int q = 0; q < ni; ++q) {
+            uint32_t e = nbr[base + K - 1 - q];
+            double r = rr[base + K - 1 - q];
+            int t = nr + q - 1;
+            // insertion into [nr, nr+q)
+            while (t >= nr && (nbr[base + t] & IDX_MASK) > (e & IDX_MASK)) {
+                nbr[base + t + 1] = nbr[base + t];
+                rr[base + t + 1] = rr[base + t];
+                --t;
+            }
+            nbr[base + t + 1] = e;
+            rr[base + t + 1] = r;
+        }
+        const int tot = nr + ni;
+        if (tot == 0) flag(status, ST_NO_NEIGHBOUR);
+        int fc = 0;
+        for (int s = 0; s < tot; ++s) {
+            ww[base + s] = kernelW(rr[base + s], p);
+            if ((int)(nbr[base + s] & IDX_MASK) > i) ++fc;
+        }
+        // omega = (sum over real neighbours) + W(0), then + images
+        double omega = 0.;
+        {
+            double o2 = 0.;
+            for (int s = 0; s < nr; ++s) o2 += ww[base + s];
+            omega = o2 + p.w0;
+            for (int s = nr; s < tot; ++s) omega += ww[base + s];
+        }
+        const double rho = m[i] * omega;
+        const double P = (p.gamma - 1.) * rho * u[i];
+        if (rho <= 0.) flag(status, ST_NEG_DENSITY);
+        if (P <= 0.) flag(status, ST_NEG_PRESSURE);
+        noi[i] = nr;
+        noiImg[i] = ni;
+        faceCnt[i] = fc;
+        Prim pr;
+        pr.x = xi[0]; pr.y = xi[1]; pr.z = xi[2];
+        pr.rho = rho; pr.P = P;
+        pr.vx = vx[i]; pr.vy = vy[i]; pr.vz = D == 3 ? vz[i] : 0.;
+        prim[i] = pr;
+        geo[i].omega = omega;
+        geo[i].V = 1. / omega;
+        geo[i].c = sqrt(p.gamma * P / rho);
+    }
+}
+
+// ------------------------------------------------------------------ dt
+
+// Particles::compGlobalTimestep (Particles.cpp:1446-1485): real neighbours
+// only, v_sig starting at numeric_limits<double>::min().  The minimum over
+// particles is order independent, so an atomicMin on the bit pattern of the
+// (positive) per-particle dt is deterministic.
+template <int D>
+__global__ void __launch_bounds__(256) k_timestep(Params p, const Prim *__restrict__ prim, const Geo *__restrict__ geo,
+                                                  const uint32_t *__restrict__ nbr, const double *__restrict__ rr,
+                                                  const int *__restrict__ noi, unsigned long long *__restrict__ dtbits) {
+    double best = DBL_MAX_;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < p.n; i += gridDim.x * blockDim.x) {
+        const Prim pi = prim[i];
+        const double ci = geo[i].c;
+        double vSig = DBL_MIN_;
+        const size_t base = (size_t)i * p.K;
+        const int nr = noi[i];
+        for (int s = 0; s < nr; ++s) {
+            const int j = (int)(nbr[base + s] & IDX_MASK);
+            const Prim pj = prim[j];
+            const double cj = geo[j].c;
+            double xij[3] = {pi.x - pj.x, pi.y - pj.y, pi.z - pj.z};
+            double vij[3] = {pi.vx - pj.vx, pi.vy - pj.vy, pi.vz - pj.vz};
+            double vijxij = dotD<D>(vij, xij) / rr[base + s];
+            vijxij = vijxij < 0. ? vijxij : 0.;
+            double vs = ci + cj - vijxij;
+            vSig = vs > vSig ? vs : vSig;
+        }
+        double dti = p.cfl_h / vSig;
+        best = dti < best ? dti : best;
+    }
+    for (int o = 16; o > 0; o >>= 1) best = fmin(best, __shfl_xor_sync(0xffffffffu, best, o));
+    if ((threadIdx.x & 31) == 0 && best < DBL_MAX_) atomic_min_pos_double(dtbits, best);
+}
+
+__global__ void k_dt_final(Params p, const unsigned long long *__restrict__ dtbits, double dt_max,
+                           double *__restrict__ dt_out) {
+    double dt = p.adaptive ? __longlong_as_double((long long)*dtbits) : p.time_step;
+    if (dt_max > 0. && dt > dt_max) dt = dt_max;
+    *dt_out = dt;
+}
+
+// ------------------------------------------------------------------ gradients
+
+// Particles::compPsijTilde (Particles.cpp:1186-1254, 2292-2455): E_i =
+// sum_j (x_j - x_i)(x_j - x_i)^T W_ij / omega_i, B_i = E_i^-1 (closed form);
+// Particles::gradient (:1257-1270, 2457-2502) for rho, vx, vy, (vz), P with
+// psi~_j(x_i) = B_i (x_j - x_i) W_ij / omega_i; Particles::slopeLimiter
+// (:1313-1444) with the face midpoint x_ij = (x_i + x_j)/2.
+template <int D>
+__device__ __forceinline__ void neighbour_pos(uint32_t e, const Prim &pj, const GridInfo &g, double h, double *xj) {
+    xj[0] = pj.x; xj[1] = pj.y; if (D == 3) xj[2] = pj.z;
+    if (e >> IMG_SHIFT) {
+#pragma unroll
+        for (int a = 0; a < D; ++a)
+            if (e & (1u << (IMG_SHIFT + a))) xj[a] = image_coord(xj[a], g.lo[a], g.hi[a], h);
+    }
+}
+
+template <int D>
+__device__ __forceinline__ void invert_closed_form(double *A) {
+    if (D == 2) {
+        double a = A[0], b = A[1], c = A[2], d = A[3];
+        double det = a * d - b * c;
+        double id = 1. / det;
+        A[0] = d * id; A[1] = -b * id; A[2] = -c * id; A[3] = a * id;
+    } else {
+        double a00 = A[0], a01 = A[1], a02 = A[2], a10 = A[3], a11 = A[4], a12 = A[5], a20 = A[6], a21 = A[7], a22 = A[8];
+        double c00 = a11 * a22 - a12 * a21;
+        double c01 = a12 * a20 - a10 * a22;
+        double c02 = a10 * a21 - a11 * a20;
+        double det = a00 * c00 + a01 * c01 + a02 * c02;
+        double id = 1. / det;
+        A[0] = c00 * id;
+        A[1] = (a02 * a21 - a01 * a22) * id;
+        A[2] = (a01 * a12 - a02 * a11) * id;
+        A[3] = c01 * id;
+        A[4] = (a00 * a22 - a02 * a20) * id;
+        A[5] = (a02 * a10 - a00 * a12) * id;
+        A[6] = c02 * id;
+        A[7] = (a01 * a20 - a00 * a21) * id;
+        A[8] = (a00 * a11 - a01 * a10) * id;
+    }
+}
+
+template <int D>
+__device__ __forceinline__ double field_of(const Prim &q, int f) {
+    // gradient order of MeshlessScheme.cpp:114-120: rho, vx, vy, (vz), P
+    if (f == 0) return q.rho;
+    if (f == 1) return q.vx;
+    if (f == 2) return q.vy;
+    if (D == 3 && f == 3) return q.vz;
+    return q.P;
+}
+
+template <int D>
+__global__ void __launch_bounds__(128) k_gradients(Params p, const GridInfo *__restrict__ gridp,
+                                                   const Prim *__restrict__ prim, Geo *__restrict__ geo,
+                                                   const uint32_t *__restrict__ nbr, const double *__restrict__ ww,
+                                                   const int *__restrict__ noi, const int *__restrict__ noiImg,
+                                                   Grad *__restrict__ grad, Grad *__restrict__ gradRaw) {
+    constexpr int NF = D + 2;
+    const GridInfo g = *gridp;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < p.n; i += gridDim.x * blockDim.x) {
+        const Prim pi = prim[i];
+        const double xi[3] = {pi.x, pi.y, pi.z};
+        const double Vi = geo[i].V;
+        const size_t base = (size_t)i * p.K;
+        const int tot = noi[i] + noiImg[i];
+        double E[9] = {0., 0., 0., 0., 0., 0., 0., 0., 0.};
+        for (int s = 0; s < tot; ++s) {
+            const uint32_t e = nbr[base + s];
+            const Prim pj = prim[e & IDX_MASK];
+            double xj[3];
+            neighbour_pos<D>(e, pj, g, p.h, xj);
+            const double psij = ww[base + s] * Vi;
+            double d[3];
+#pragma unroll
+            for (int a = 0; a < D; ++a) d[a] = xj[a] - xi[a];
+#pragma unroll
+            for (int a = 0; a < D; ++a)
+#pragma unroll
+                for (int b = a; b < D; ++b) E[D * a + b] += d[a] * d[b] * psij;
+        }
+#pragma unroll
+        for (int a = 0; a < D; ++a)
+#pragma unroll
+            for (int b = 0; b < a; ++b) E[D * a + b] = E[D * b + a];
+        invert_closed_form<D>(E);
+        double gr[NF][3];
+        double fi[NF];
+#pragma unroll
+        for (int f = 0; f < NF; ++f) { fi[f] = field_of<D>(pi, f); gr[f][0] = gr[f][1] = gr[f][2] = 0.; }
+        for (int s = 0; s < tot; ++s) {
+            const uint32_t e = nbr[base + s];
+            const Prim pj = prim[e & IDX_MASK];
+            double xj[3];
+            neighbour_pos<D>(e, pj, g, p.h, xj);
+            const double psij = ww[base + s] * Vi;
+            double d[3], ps[3];
+#pragma unroll
+            for (int a = 0; a < D; ++a) d[a] = xj[a] - xi[a];
+#pragma unroll
+            for (int a = 0; a < D; ++a) {
+                double t = 0.;
+#pragma unroll
+                for (int b = 0; b < D; ++b) t += E[D * a + b] * d[b] * psij;
+                ps[a] = t;
+            }
+#pragma unroll
+            for (int f = 0; f < NF; ++f) {
+                const double df = field_of<D>(pj, f) - fi[f];
+#pragma unroll
+                for (int a = 0; a < D; ++a) gr[f][a] += df * ps[a];
+            }
+        }
+        if (gradRaw) {
+            Grad graw;
+            for (int k = 0; k < 16; ++k) graw.g[k] = 0.;
+#pragma unroll
+            for (int f = 0; f < NF; ++f) {
+                int slot = (f == NF - 1) ? 4 : f;
+#pragma unroll
+                for (int a = 0; a < D; ++a) graw.g[slot * 3 + a] = gr[f][a];
+            }
+            gradRaw[i] = graw;
+        }
+        if (p.slope) {
+            double mxN[NF], mnN[NF], mxM[NF], mnM[NF];
+#pragma unroll
+            for (int f = 0; f < NF; ++f) { mxN[f] = DBL_MIN_; mnN[f] = DBL_MAX_; mxM[f] = DBL_MIN_; mnM[f] = DBL_MAX_; }
+            for (int s = 0; s < tot; ++s) {
+                const uint32_t e = nbr[base + s];
+                const Prim pj = prim[e & IDX_MASK];
+                double xj[3], xijxi[3];
+                neighbour_pos<D>(e, pj, g, p.h, xj);
+#pragma unroll
+                for (int a = 0; a < D; ++a) {
+                    double xij = p.foqp ? (xi[a] + xj[a]) / 2. : xi[a] + p.h / 4. * (xj[a] - xi[a]);
+                    xijxi[a] = xij - xi[a];
+                }
+#pragma unroll
+                for (int f = 0; f < NF; ++f) {
+                    const double fj = field_of<D>(pj, f);
+                    if (mxN[f] < fj) mxN[f] = fj;
+                    if (mnN[f] > fj) mnN[f] = fj;
+                    const double fij = fi[f] + dotD<D>(gr[f], xijxi);
+                    if (mxM[f] < fij) mxM[f] = fij;
+                    if (mnM[f] > fij) mnM[f] = fij;
+                }
+            }
+#pragma unroll
+            for (int f = 0; f < NF; ++f) {
+                double aMax = ref_abs((mxN[f] - fi[f]) / (mxM[f] - fi[f]), p.int_abs);
+                double aMin = ref_abs((fi[f] - mnN[f]) / (fi[f] - mnM[f]), p.int_abs);
+                if (aMin <= aMax && p.beta * aMin < 1.) {
+#pragma unroll
+                    for (int a = 0; a < D; ++a) gr[f][a] *= aMin;
+                } else if (aMax <= aMin && p.beta * aMax < 1.) {
+#pragma unroll
+                    for (int a = 0; a < D; ++a) gr[f][a] *= aMax;
+                }
+            }
+        }
+        Grad go;
+#pragma unroll
+        for (int k = 0; k < 16; ++k) go.g[k] = 0.;
+#pragma unroll
+        for (int f = 0; f < NF; ++f) {
+            int slot = (f == NF - 1) ? 4 : f;   // P always at slot 4
+#pragma unroll
+            for (int a = 0; a < D; ++a) go.g[slot * 3 + a] = gr[f][a];
+        }
+        grad[i] = go;
+#pragma unroll
+        for (int k = 0; k < D * D; ++k) geo[i].B[k] = E[k];
+    }
+}
+
+// ------------------------------------------------------------------ face links
+
+// Canonical faces: slot s of particle i with neighbour (or image parent)
+// j > i, the side on which Particles::solveRiemannProblems computes the flux
+// (Particles.cpp:1838-1858, 1886-1897).  Slot -> face id (+1 canonical, -1
+// copied with the opposite sign), face -> (i, slot, reverse slot).  The
+// reverse slot of a non-canonical slot is the first entry of j's list (real
+// part or image part) that refers to i, as in the reference's searches.
+__global__ void __launch_bounds__(128) k_link(Params p, const uint32_t *__restrict__ nbr, const int *__restrict__ noi,
+                                              const int *__restrict__ noiImg, const int *__restrict__ faceOff,
+                                              int *__restrict__ faceOf, FaceRef *__restrict__ faces,
+                                              unsigned *__restrict__ status) {
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < p.n; i += gridDim.x * blockDim.x) {
+        const size_t base = (size_t)i * p.K;
+        const int nr = noi[i], tot = nr + noiImg[i];
+        int rank = 0;
+        for (int s = 0; s < tot; ++s) {
+            const uint32_t e = nbr[base + s];
+            const int j = (int)(e & IDX_MASK);
+            const bool img = s >= nr;
+            // search j's list (matching part) for i
+            const size_t jb = (size_t)j * p.K;
+            const int jnr = noi[j];
+            const int b = img ? jnr : 0, en = img ? jnr + noiImg[j] : jnr;
+            int found = -1, crank = 0;
+            const bool canon = j > i;
+            if (!canon || img) {
+                for (int t = b; t < en; ++t) {
+                    const uint32_t f = nbr[jb + t];
+                    const int q = (int)(f & IDX_MASK);
+                    if (q == i) { found = t; break; }
+                }
+            }
+            if (canon) {
+                const int fid = faceOff[i] + rank;
+                ++rank;
+                faceOf[base + s] = fid + 1;
+                FaceRef fr;
+                fr.i = i; fr.slot = s; fr.rslot = img ? found : -1; fr.pad = 0;
+                if (img && found < 0) flag(status, ST_ASYMMETRIC);
+                faces[fid] = fr;
+            } else {
+                if (found < 0) { flag(status, ST_ASYMMETRIC); faceOf[base + s] = 0; continue; }
+                // rank of slot `found` among j's canonical slots
+                for (int t = 0; t < found; ++t)
+                    if ((int)(nbr[jb + t] & IDX_MASK) > j) ++crank;
+                faceOf[base + s] = -(faceOff[j] + crank + 1);
+            }
+        }
+    }
+}
+
+// ------------------------------------------------------------------ faces
+
+// Particles::pairwiseLimiter, Particles.cpp:1735-1785.
+__device__ __forceinline__ double pairwise_limiter(const Params &p, double phi0, double phi_i, double phi_j,
+                                                   double xijxi_abs, double xjxi_abs) {
+    double phi_ = phi_i;
+    double phi_ij = phi_i + xijxi_abs / xjxi_abs * (phi_j - phi_i);
+    double phiMin, phiMax;
+    if (phi_i < phi_j) { phiMin = phi_i; phiMax = phi_j; }
+    else { phiMin = phi_j; phiMax = phi_i; }
+    double ad = ref_abs(phi_i - phi_j, p.int_abs);
+    double delta1 = p.psi1 * ad;
+    double delta2 = p.psi2 * ad;
+    double phiMinus, phiPlus;
+    if ((phiMax + delta1 >= 0. && phiMax >= 0.) || (phiMax + delta1 < 0. && phiMax < 0.)) phiPlus = phiMax + delta1;
+    else phiPlus = phiMax / (1. + delta1 / ref_abs(phiMax, p.int_abs));
+    if ((phiMin - delta1 >= 0. && phiMin >= 0.) || (phiMin - delta1 < 0. && phiMin < 0.)) phiMinus = phiMin - delta1;
+    else phiMinus = phiMin / (1. + delta1 / ref_abs(phiMin, p.int_abs));
+    if (phi_i < phi_j) {
+        double minPhiD2 = (phi_ij + delta2 < phi0) ? phi_ij + delta2 : phi0;
+        phi_ = phiMinus > minPhiD2 ? phiMinus : minPhiD2;
+    } else if (phi_i > phi_j) {
+        double maxPhiD2 = (phi_ij - delta2 > phi0) ? phi_ij - delta2 : phi0;
+        phi_ = phiPlus < maxPhiD2 ? phiPlus : maxPhiD2;
+    }
+    return phi_;
+}
+
+// Helper::rotationMatrix2D/3D, demonstrator/src/Helper.cpp:39-77.
+__device__ __forceinline__ void rot2(const double *a, const double *b, double *L) {
+    L[0] = a[0] * b[0] + a[1] * b[1];
+    L[1] = -(a[0] * b[1] - a[1] * b[0]);
+    L[2] = -L[1];
+    L[3] = L[0];
+}
+__device__ __forceinline__ void rot3(const double *a, const double *b, double *L) {
+    double v0 = a[1] * b[2] - a[2] * b[1];
+    double v1 = a[2] * b[0] - a[0] * b[2];
+    double v2 = a[0] * b[1] - a[1] * b[0];
+    double cosAB = ((0. + a[0] * b[0]) + a[1] * b[1]) + a[2] * b[2];
+    double n = 1. / (1. + cosAB);
+    L[0] = 1. - n * (v2 * v2 + v1 * v1);
+    L[1] = -v2 + n * v0 * v1;
+    L[2] = v1 + n * v0 * v2;
+    L[3] = v2 + n * v0 * v1;
+    L[4] = 1. - n * (v2 * v2 + v0 * v0);
+    L[5] = -v0 + n * v1 * v2;
+    L[6] = -v1 + n * v0 * v2;
+    L[7] = v0 + n * v1 * v2;
+    L[8] = 1. - n * (v1 * v1 + v0 * v0);
+}
+
+// One canonical face (i < j): effective face A_ij (compEffectiveFace,
+// Particles.cpp:1290-1311, 2504-2531) from B_i and B_j; boosted, reconstructed,
+// optionally pairwise-limited and half-step-predicted states
+// (compRiemannStatesLR, :1488-1733 / 2533-2683, including the vz[i] of
+// :1717,1719); rotation to the face frame, exact solve with i as the left
+// state, rotation back and projection on A_ij (Riemann::Riemann/exact/
+// rotateAndProjectFluxes2D/3D, demonstrator/src/Riemann.cpp:7-229).
+// Output slot order: [mass, energy, px, py, pz].
+template <int D>
+__global__ void __launch_bounds__(128) k_faces(Params p, const GridInfo *__restrict__ gridp,
+                                               const Prim *__restrict__ prim, const Geo *__restrict__ geo,
+                                               const Grad *__restrict__ grad, const uint32_t *__restrict__ nbr,
+                                               const double *__restrict__ ww, const int *__restrict__ faceTotal,
+                                               const FaceRef *__restrict__ faces, const double *__restrict__ dtp,
+                                               double *__restrict__ Fface, unsigned long long *__restrict__ newtonSum,
+                                               unsigned *__restrict__ status) {
+    constexpr int NV = D + 2;
+    const GridInfo g = *gridp;
+    const int nf = *faceTotal;
+    const double dt = *dtp;
+    const RiemannConsts rc = make_riemann_consts(p.gamma, p.rtol, p.rmaxit);
+    const double gamma = p.gamma;
+    unsigned long long iters_local = 0;
+    unsigned st_local = 0;
+    for (int f = blockIdx.x * blockDim.x + threadIdx.x; f < nf; f += gridDim.x * blockDim.x) {
+        const FaceRef fr = faces[f];
+        const int i = fr.i;
+        const size_t si = (size_t)i * p.K + fr.slot;
+        const uint32_t e = nbr[si];
+        const int j = (int)(e & IDX_MASK);
+        const bool img = (e >> IMG_SHIFT) != 0;
+        const Prim pi = prim[i], pj = prim[j];
+        const Geo gi = geo[i], gj = geo[j];
+        double xi[3] = {pi.x, pi.y, pi.z}, xj[3];
+        neighbour_pos<D>(e, pj, g, p.h, xj);
+        // reverse geometry: position of i as seen from j, and W from j's slot
+        double xir[3] = {pi.x, pi.y, pi.z};
+        double wij = ww[si], wji = wij;
+        if (img) {
+            if (fr.rslot >= 0) {
+                const size_t sj = (size_t)j * p.K + fr.rslot;
+                neighbour_pos<D>(nbr[sj], pi, g, p.h, xir);
+                wji = ww[sj];
+            } else {
+                wji = 0.;
+            }
+        }
+        // --- effective face
+        double A[3];
+        {
+            const double psi_i = wij * gi.V, psi_j = wji * gj.V;
+            double dij[3], dji[3];
+#pragma unroll
+            for (int a = 0; a < D; ++a) { dij[a] = xj[a] - xi[a]; dji[a] = xir[a] - xj[a]; }
+#pragma unroll
+            for (int a = 0; a < D; ++a) {
+                double t1 = 0., t2 = 0.;
+#pragma unroll
+                for (int b = 0; b < D; ++b) {
+                    t1 += gi.B[D * a + b] * dij[b] * psi_i;
+                    t2 += gj.B[D * a + b] * dji[b] * psi_j;
+                }
+                A[a] = gi.V * t1 - gj.V * t2;
+            }
+        }
+        // --- states at the face
+        double xijxi[3], xjxi[3], xijxj[3];
+#pragma unroll
+        for (int a = 0; a < D; ++a) {
+            xjxi[a] = xj[a] - xi[a];
+            if (p.foqp) {
+                xijxj[a] = .5 * (xi[a] - xj[a]);
+                xijxi[a] = .5 * (xj[a] - xi[a]);
+            } else {
+                double xij = xi[a] + p.h / 4. * xjxi[a];
+                xijxi[a] = xij - xi[a];
+                xijxj[a] = xij - xj[a];
+            }
+        }
+        const double vi[3] = {pi.vx, pi.vy, pi.vz}, vj[3] = {pj.vx, pj.vy, pj.vz};
+        double vf[3] = {0., 0., 0.};
+        if (p.move) {
+            if (p.foqp) {
+#pragma unroll
+                for (int a = 0; a < D; ++a) vf[a] = (vi[a] + vj[a]) / 2.;
+            } else {
+                double dotProd = dotD<D>(xijxi, xjxi);
+                double dSqr = dotD<D>(xjxi, xjxi);
+#pragma unroll
+                for (int a = 0; a < D; ++a) vf[a] = vi[a] + (vj[a] - vi[a]) * dotProd / dSqr;
+            }
+        }
+        const double *Gi = grad[i].g, *Gj = grad[j].g;
+        // gradient blocks: 0 rho, 1 vx, 2 vy, 3 vz, 4 P
+        double R[5], L[5];
+        R[0] = pi.rho; L[0] = pj.rho;
+        R[1] = pi.P; L[1] = pj.P;
+#pragma unroll
+        for (int a = 0; a < D; ++a) { R[2 + a] = vi[a] - vf[a]; L[2 + a] = vj[a] - vf[a]; }
+        double Rb[5], Lb[5];
+#pragma unroll
+        for (int k = 0; k < NV; ++k) { Rb[k] = R[k]; Lb[k] = L[k]; }
+        R[0] += dotD<D>(Gi + 0, xijxi); L[0] += dotD<D>(Gj + 0, xijxj);
+        R[1] += dotD<D>(Gi + 12, xijxi); L[1] += dotD<D>(Gj + 12, xijxj);
+        R[2] += dotD<D>(Gi + 3, xijxi); L[2] += dotD<D>(Gj + 3, xijxj);
+        R[3] += dotD<D>(Gi + 6, xijxi); L[3] += dotD<D>(Gj + 6, xijxj);
+        if (D == 3) { R[4] += dotD<D>(Gi + 9, xijxi); L[4] += dotD<D>(Gj + 9, xijxj); }
+        if (p.pairwise && (!img || p.img_pw)) {
+            double xijxi_abs = 0., xijxj_abs = 0., xjxi_abs = 0.;
+#pragma unroll
+            for (int a = 0; a < D; ++a) {
+                xijxi_abs += xijxi[a] * xijxi[a];
+                xijxj_abs += xijxj[a] * xijxj[a];
+                xjxi_abs += xjxi[a] * xjxi[a];
+            }
+            xijxi_abs = sqrt(xijxi_abs);
+            xijxj_abs = sqrt(xijxj_abs);
+            xjxi_abs = sqrt(xjxi_abs);
+#pragma unroll
+            for (int k = 0; k < NV; ++k) {
+                R[k] = pairwise_limiter(p, R[k], Rb[k], Lb[k], xijxi_abs, xjxi_abs);
+                L[k] = pairwise_limiter(p, L[k], Lb[k], Rb[k], xijxj_abs, xjxi_abs);
+            }
+        }
+        {
+            double viDiv = Gi[3 + 0] + Gi[6 + 1];
+            double vjDiv = Gj[3 + 0] + Gj[6 + 1];
+            if (D == 3) { viDiv += Gi[9 + 2]; vjDiv += Gj[9 + 2]; }
+            const double hdt = dt / 2.;
+            const double ui0 = vi[0] - vf[0], ui1 = vi[1] - vf[1], uj0 = vj[0] - vf[0], uj1 = vj[1] - vf[1];
+            R[0] -= hdt * (pi.rho * viDiv + ui0 * Gi[0] + ui1 * Gi[1]);
+            L[0] -= hdt * (pj.rho * vjDiv + uj0 * Gj[0] + uj1 * Gj[1]);
+            R[1] -= hdt * (gamma * pi.P * viDiv + ui0 * Gi[12] + ui1 * Gi[13]);
+            L[1] -= hdt * (gamma * pj.P * vjDiv + uj0 * Gj[12] + uj1 * Gj[13]);
+            R[2] -= hdt * (Gi[12] / pi.rho + ui0 * Gi[3] + ui1 * Gi[4]);
+            L[2] -= hdt * (Gj[12] / pj.rho + uj0 * Gj[3] + uj1 * Gj[4]);
+            R[3] -= hdt * (Gi[13] / pi.rho + ui0 * Gi[6] + ui1 * Gi[7]);
+            L[3] -= hdt * (Gj[13] / pj.rho + uj0 * Gj[6] + uj1 * Gj[7]);
+            if (D == 3) {
+                const double ui2 = vi[2] - vf[2], uj2 = vj[2] - vf[2];
+                R[0] -= hdt * ui2 * Gi[2];
+                L[0] -= hdt * uj2 * Gj[2];
+                R[1] -= hdt * ui2 * Gi[14];
+                L[1] -= hdt * uj2 * Gj[14];
+                // the reference uses vz[i] on the j side here (Particles.cpp:1717,1719)
+                R[2] -= hdt * ui2 * Gi[5];
+                L[2] -= hdt * ui2 * Gj[5];
+                R[3] -= hdt * ui2 * Gi[8];
+                L[3] -= hdt * ui2 * Gj[8];
+                R[4] -= hdt * (Gi[14] / pi.rho + ui0 * Gi[9] + ui1 * Gi[10] + ui2 * Gi[11]);
+                L[4] -= hdt * (Gj[14] / pj.rho + uj0 * Gj[9] + uj1 * Gj[10] + uj2 * Gj[11]);
+            }
+        }
+        if (R[1] < 0. || L[1] < 0.) st_local |= ST_NEG_PRESSURE;
+        // --- Riemann problem in the face frame (i left, j right)
+        const double unitX[3] = {1., 0., 0.};
+        double AN = sqrt(dotD<D>(A, A));
+        double hatA[3] = {0., 0., 0.};
+#pragma unroll
+        for (int a = 0; a < D; ++a) hatA[a] = 1. / AN * A[a];
+        double Lam[9];
+        if (D == 2) {
+            rot2(hatA, unitX, Lam);
+            double bR0 = L[2], bR1 = L[3], bL0 = R[2], bL1 = R[3];
+            L[2] = Lam[0] * bR0 + Lam[1] * bR1;
+            L[3] = Lam[2] * bR0 + Lam[3] * bR1;
+            R[2] = Lam[0] * bL0 + Lam[1] * bL1;
+            R[3] = Lam[2] * bL0 + Lam[3] * bL1;
+        } else {
+            rot3(hatA, unitX, Lam);
+            double bR0 = L[2], bR1 = L[3], bR2 = L[4], bL0 = R[2], bL1 = R[3], bL2 = R[4];
+            L[2] = Lam[0] * bR0 + Lam[1] * bR1 + Lam[2] * bR2;
+            L[3] = Lam[3] * bR0 + Lam[4] * bR1 + Lam[5] * bR2;
+            L[4] = Lam[6] * bR0 + Lam[7] * bR1 + Lam[8] * bR2;
+            R[2] = Lam[0] * bL0 + Lam[1] * bL1 + Lam[2] * bL2;
+            R[3] = Lam[3] * bL0 + Lam[4] * bL1 + Lam[5] * bL2;
+            R[4] = Lam[6] * bL0 + Lam[7] * bL1 + Lam[8] * bL2;
+        }
+        RiemannResult rs = riemann_exact(rc, R[0], R[2], R[1], L[0], L[2], L[1]);
+        if (rs.iters < 0) st_local |= ST_NEWTON;
+        else iters_local += (unsigned long long)rs.iters;
+        double vSol[3] = {rs.u, 0., 0.};
+        if (rs.flag == 1) { for (int a = 1; a < D; ++a) vSol[a] = L[2 + a]; }
+        else if (rs.flag == -1) { for (int a = 1; a < D; ++a) vSol[a] = R[2 + a]; }
+        else st_local |= ST_VACUUM;
+        const double rhoSol = rs.rho, PSol = rs.p;
+        double Fo[5];
+        if (D == 2) {
+            double LI[4];
+            rot2(unitX, hatA, LI);
+            double b0 = vSol[0], b1 = vSol[1];
+            vSol[0] = LI[0] * b0 + LI[1] * b1;
+            vSol[1] = LI[2] * b0 + LI[3] * b1;
+            Fo[0] = A[0] * rhoSol * vSol[0] + A[1] * rhoSol * vSol[1];
+            double vLab[2] = {vSol[0] + vf[0], vSol[1] + vf[1]};
+            if (p.mfm) { vSol[0] = 0.; vSol[1] = 0.; }
+            Fo[2] = A[0] * (rhoSol * vLab[0] * vSol[0] + PSol) + A[1] * rhoSol * vLab[0] * vSol[1];
+            Fo[3] = A[0] * rhoSol * vLab[1] * vSol[0] + A[1] * (rhoSol * vLab[1] * vSol[1] + PSol);
+            const double ek = rhoSol * .5 * (vLab[0] * vLab[0] + vLab[1] * vLab[1]);
+            const double pe = PSol / (gamma - 1.);
+            Fo[1] = A[0] * (vSol[0] * (pe + ek) + PSol * vLab[0]) + A[1] * (vSol[1] * (pe + ek) + PSol * vLab[1]);
+            Fo[4] = 0.;
+        } else {
+            double LI[9];
+            rot3(unitX, hatA, LI);
+            double b0 = vSol[0], b1 = vSol[1], b2 = vSol[2];
+            vSol[0] = LI[0] * b0 + LI[1] * b1 + LI[2] * b2;
+            vSol[1] = LI[3] * b0 + LI[4] * b1 + LI[5] * b2;
+            vSol[2] = LI[6] * b0 + LI[7] * b1 + LI[8] * b2;
+            Fo[0] = A[0] * rhoSol * vSol[0] + A[1] * rhoSol * vSol[1] + A[2] * rhoSol * vSol[2];
+            double vLab[3] = {vSol[0] + vf[0], vSol[1] + vf[1], vSol[2] + vf[2]};
+            if (p.mfm) { vSol[0] = 0.; vSol[1] = 0.; vSol[2] = 0.; }
+            Fo[2] = A[0] * (rhoSol * vLab[0] * vSol[0] + PSol) + A[1] * rhoSol * vLab[0] * vSol[1] + A[2] * rhoSol * vLab[0] * vSol[2];
+            Fo[3] = A[0] * rhoSol * vLab[1] * vSol[0] + A[1] * (rhoSol * vLab[1] * vSol[1] + PSol) + A[2] * rhoSol * vLab[1] * vSol[2];
+            Fo[4] = A[0] * rhoSol * vLab[2] * vSol[0] + A[1] * rhoSol * vLab[2] * vSol[1] + A[2] * (rhoSol * vLab[2] * vSol[2] + PSol);
+            const double ek = rhoSol * .5 * ((vLab[0] * vLab[0] + vLab[1] * vLab[1]) + vLab[2] * vLab[2]);
+            const double pe = PSol / (gamma - 1.);
+            Fo[1] = A[0] * (vSol[0] * (pe + ek) + PSol * vLab[0]) + A[1] * (vSol[1] * (pe + ek) + PSol * vLab[1])
+                  + A[2] * (vSol[2] * (pe + ek) + PSol * vLab[2]);
+        }
+        double2 *dst = reinterpret_cast<double2 *>(Fface + (size_t)f * 6);
+        dst[0] = make_double2(Fo[0], Fo[1]);
+        dst[1] = make_double2(Fo[2], Fo[3]);
+        dst[2] = make_double2(Fo[4], 0.);
+    }
+    // block-level accumulation of the counters
+    for (int o = 16; o > 0; o >>= 1) {
+        iters_local += __shfl_xor_sync(0xffffffffu, iters_local, o);
+        st_local |= __shfl_xor_sync(0xffffffffu, st_local, o);
+    }
+    if ((threadIdx.x & 31) == 0) {
+        if (iters_local) atomicAdd(newtonSum, iters_local);
+        if (st_local) flag(status, st_local);
+    }
+}
+
+// ------------------------------------------------------------------ gather + update
+
+// Particles::collectFluxes (Particles.cpp:1913-2011) in slot order, then
+// Particles::updateStateAndPosition (:2013-2110).  The update is skipped when
+// the neighbour search overflowed, so that the host can retry the step with
+// more slots.
+template <int D>
+__global__ void __launch_bounds__(128) k_update(Params p, const GridInfo *__restrict__ gridp, const int *__restrict__ noi,
+                                                const int *__restrict__ noiImg, const int *__restrict__ faceOf,
+                                                const double *__restrict__ Fface, const double *__restrict__ dtp,
+                                                double *__restrict__ x, double *__restrict__ y, double *__restrict__ z,
+                                                double *__restrict__ vx, double *__restrict__ vy, double *__restrict__ vz,
+                                                double *__restrict__ m, double *__restrict__ u, float4 *__restrict__ posf,
+                                                double *__restrict__ fluxSums, double *__restrict__ simTime,
+                                                int *__restrict__ stepsDone, unsigned *__restrict__ status) {
+    const unsigned st0 = *status;
+    if (st0 & (ST_NGB_OVERFLOW | ST_CAPACITY)) return;
+    const GridInfo g = *gridp;
+    const double dt = *dtp;
+    double *X[3] = {x, y, z};
+    double *Vv[3] = {vx, vy, vz};
+    unsigned st_local = 0;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < p.n; i += gridDim.x * blockDim.x) {
+        const size_t base = (size_t)i * p.K;
+        const int tot = noi[i] + noiImg[i];
+        double mF = 0., eF = 0., vF[3] = {0., 0., 0.};
+        for (int s = 0; s < tot; ++s) {
+            const int fo = faceOf[base + s];
+            if (fo == 0) continue;
+            const double2 *src = reinterpret_cast<const double2 *>(Fface + (size_t)((fo > 0 ? fo : -fo) - 1) * 6);
+            const double2 a = src[0], b = src[1], c = src[2];
+            if (fo > 0) {
+                mF += a.x; vF[0] += b.x; vF[1] += b.y; if (D == 3) vF[2] += c.x; eF += a.y;
+            } else {
+                mF += -a.x; vF[0] += -b.x; vF[1] += -b.y; if (D == 3) vF[2] += -c.x; eF += -a.y;
+            }
+        }
+        if (fluxSums) {
+            fluxSums[(size_t)i * 5 + 0] = mF;
+            fluxSums[(size_t)i * 5 + 1] = eF;
+            fluxSums[(size_t)i * 5 + 2] = vF[0];
+            fluxSums[(size_t)i * 5 + 3] = vF[1];
+            fluxSums[(size_t)i * 5 + 4] = vF[2];
+        }
+        double mi = m[i], ui = u[i];
+        double vo[3] = {vx[i], vy[i], D == 3 ? vz[i] : 0.};
+        double Q0 = D == 3 ? mi * (ui + .5 * (vo[0] * vo[0] + vo[1] * vo[1] + vo[2] * vo[2]))
+                           : mi * (ui + .5 * (vo[0] * vo[0] + vo[1] * vo[1]));
+        double Qv[3] = {mi * vo[0], mi * vo[1], mi * vo[2]};
+        if (!p.mfm) mi -= dt * mF;
+        if (mi <= 0.) st_local |= ST_NEG_MASS;
+        double vn[3];
+#pragma unroll
+        for (int a = 0; a < D; ++a) { Qv[a] -= dt * vF[a]; vn[a] = Qv[a] / mi; }
+        Q0 -= dt * eF;
+        double un = D == 3 ? Q0 / mi - .5 * (vn[0] * vn[0] + vn[1] * vn[1] + vn[2] * vn[2])
+                           : Q0 / mi - .5 * (vn[0] * vn[0] + vn[1] * vn[1]);
+        if (un <= 0.) st_local |= ST_NEG_ENERGY;
+        if (!(un == un) || !(mi == mi)) st_local |= ST_NAN;
+        m[i] = mi;
+        u[i] = un;
+#pragma unroll
+        for (int a = 0; a < D; ++a) Vv[a][i] = vn[a];
+        double xn[3] = {0., 0., 0.};
+#pragma unroll
+        for (int a = 0; a < D; ++a) {
+            double xa = X[a][i];
+            if (p.move) {
+                xa += vo[a] * dt;
+                if (p.periodic) {
+                    if (xa < g.lo[a]) xa = g.hi[a] - (g.lo[a] - xa);
+                    else if (g.hi[a] <= xa) xa = g.lo[a] + (xa - g.hi[a]);
+                }
+                X[a][i] = xa;
+            }
+            xn[a] = xa;
+        }
+        posf[i] = make_float4((float)xn[0], (float)xn[1], (float)xn[2], 0.f);
+    }
+    for (int o = 16; o > 0; o >>= 1) st_local |= __shfl_xor_sync(0xffffffffu, st_local, o);
+    if ((threadIdx.x & 31) == 0 && st_local) flag(status, st_local);
+    if (blockIdx.x == 0 && threadIdx.x == 0) {
+        *simTime += dt;
+        *stepsDone += 1;
+    }
+}
+
+template <int D>
+__global__ void k_pack_posf(const double *__restrict__ x, const double *__restrict__ y, const double *__restrict__ z,
+                            int n, float4 *__restrict__ posf) {
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+        posf[i] = make_float4((float)x[i], (float)y[i], D == 3 ? (float)z[i] : 0.f, 0.f);
+}
+
+// ------------------------------------------------------------------ launchers
+
+template <int D>
+void launch_step(StepArgs &a) {
+    const Params &p = a.p;
+    cudaStream_t s = a.stream;
+    const int T = 128;
+    const int blocksN = (p.n + T - 1) / T;
+    auto tick = [&](int id) { if (a.timer) a.timer(a.timer_ctx, id, 0); };
+    auto tock = [&](int id) { if (a.timer) a.timer(a.timer_ctx, id, 1); };
+
+    tick(KT_GRID);
+    k_bounds_partial<D><<<BOUNDS_BLOCKS, BOUNDS_T, 0, s>>>(a.x, a.y, a.z, p.n, a.boundsPart);
+    k_bounds_final<D><<<1, 32, 0, s>>>(a.x, a.y, a.z, a.boundsPart, BOUNDS_BLOCKS, p, a.grid, a.status);
+    cudaMemsetAsync(a.cellCount, 0, sizeof(int) * (size_t)(p.ncells_cap + 1), s);
+    cudaMemsetAsync(a.cellFill, 0, sizeof(int) * (size_t)(p.ncells_cap + 1), s);
+    k_assign<D><<<blocksN, T, 0, s>>>(a.x, a.y, a.z, p.n, a.grid, a.cell, a.cellCount, a.status);
+    exclusive_scan(a.cellCount, p.ncells_cap, a.cellStart, a.scanTiles, a.scanTotal, s);
+    k_fill_cells<<<blocksN, T, 0, s>>>(a.cell, p.n, a.cellStart, a.cellFill, a.cellList);
+    k_sort_cells<<<(p.ncells_cap + T - 1) / T, T, 0, s>>>(a.grid, a.cellStart, a.cellList);
+    tock(KT_GRID);
+
+    tick(KT_NNS);
+    k_neighbours<D><<<blocksN, T, 0, s>>>(p, a.grid, a.x, a.y, a.z, a.posf, a.vx, a.vy, a.vz, a.m, a.u, a.cell,
+                                          a.cellStart, a.cellList, a.nbr, a.rr, a.ww, a.noi, a.noiImg, a.faceCnt,
+                                          a.prim, a.geo, a.status);
+    tock(KT_NNS);
+
+    tick(KT_DT);
+    cudaMemsetAsync(a.dtbits, 0xff, sizeof(unsigned long long), s);
+    k_timestep<D><<<(p.n + 255) / 256, 256, 0, s>>>(p, a.prim, a.geo, a.nbr, a.rr, a.noi, a.dtbits);
+    k_dt_final<<<1, 1, 0, s>>>(p, a.dtbits, a.dt_max, a.dt);
+    tock(KT_DT);
+
+    tick(KT_GRAD);
+    k_gradients<D><<<blocksN, T, 0, s>>>(p, a.grid, a.prim, a.geo, a.nbr, a.ww, a.noi, a.noiImg, a.grad, a.gradRaw);
+    tock(KT_GRAD);
+
+    tick(KT_LINK);
+    exclusive_scan(a.faceCnt, p.n, a.faceOff, a.scanTiles, a.scanTotal, s);
+    k_link<<<blocksN, T, 0, s>>>(p, a.nbr, a.noi, a.noiImg, a.faceOff, a.faceOf, a.faces, a.status);
+    tock(KT_LINK);
+
+    tick(KT_FACES);
+    k_faces<D><<<a.face_blocks, T, 0, s>>>(p, a.grid, a.prim, a.geo, a.grad, a.nbr, a.ww, a.faceOff + p.n, a.faces,
+                                          a.dt, a.Fface, a.newtonSum, a.status);
+    tock(KT_FACES);
+
+    tick(KT_UPDATE);
+    k_update<D><<<blocksN, T, 0, s>>>(p, a.grid, a.noi, a.noiImg, a.faceOf, a.Fface, a.dt, a.x, a.y, a.z, a.vx, a.vy,
+                                      a.vz, a.m, a.u, a.posf, a.fluxSums, a.simTime, a.stepsDone, a.status);
+    tock(KT_UPDATE);
+}
+
+void step(StepArgs &a) {
+    if (a.p.dim == 2) launch_step<2>(a);
+    else launch_step<3>(a);
+}
+
+void pack_posf(const double *x, const double *y, const double *z, int n, int dim, float4 *posf, cudaStream_t s) {
+    int blocks = (n + 255) / 256;
+    if (blocks < 1) blocks = 1;
+    if (dim == 2) k_pack_posf<2><<<blocks, 256, 0, s>>>(x, y, z, n, posf);
+    else k_pack_posf<3><<<blocks, 256, 0, s>>>(x, y, z, n, posf);
+}
+
+const char *kernel_timer_name(int id) {
+    switch (id) {
+        case KT_GRID: return "grid_bin";
+        case KT_NNS: return "neighbours_density";
+        case KT_DT: return "timestep";
+        case KT_GRAD: return "gradients_limiter";
+        case KT_LINK: return "face_links";
+        case KT_FACES: return "faces_riemann";
+        case KT_UPDATE: return "gather_update";
+    }
+    return "?";
+}
+
+}  // namespace mlh

@@ -1,0 +1,51 @@
+// Host-visible interface of the step kernels (mlh_kernels.cu).
+#pragma once
+#include <cstdint>
+#include <cuda_runtime.h>
+
+#include "mlh_device.cuh"
+
+namespace mlh {
+
+enum KernelTimerId { KT_GRID = 0, KT_NNS, KT_DT, KT_GRAD, KT_LINK, KT_FACES, KT_UPDATE, KT_COUNT };
+
+// Device pointers and settings of one step.
+struct StepArgs {
+    Params p;
+    cudaStream_t stream;
+    int face_blocks;
+    double dt_max;
+    // state (structure of arrays)
+    double *x, *y, *z, *vx, *vy, *vz, *m, *u;
+    float4 *posf;
+    // grid
+    GridInfo *grid;
+    double *boundsPart;
+    int *cell, *cellCount, *cellStart, *cellFill, *cellList;
+    // neighbours
+    uint32_t *nbr;
+    double *rr, *ww;
+    int *noi, *noiImg, *faceCnt, *faceOff, *faceOf;
+    FaceRef *faces;
+    // per particle
+    Prim *prim;
+    Geo *geo;
+    Grad *grad, *gradRaw;
+    double *Fface, *fluxSums;
+    // scalars
+    unsigned *status;
+    unsigned long long *dtbits, *newtonSum;
+    double *dt, *simTime;
+    int *stepsDone;
+    int *scanTiles, *scanTotal;
+    // optional per-kernel timer callback (phase 0 = before, 1 = after)
+    void (*timer)(void *, int, int);
+    void *timer_ctx;
+};
+
+void step(StepArgs &a);
+void pack_posf(const double *x, const double *y, const double *z, int n, int dim, float4 *posf, cudaStream_t s);
+void exclusive_scan(const int *in, int n, int *out, int *tile_buf, int *total, cudaStream_t s);
+const char *kernel_timer_name(int id);
+
+}  // namespace mlh

@@ -1,0 +1,180 @@
+"""ctypes binding of the C ABI in include/mlh.h (libmlh.so).
+
+`Simulation` is the Python face of one mlh context: the reference's
+MeshlessScheme driving one Particles set (demonstrator/src/MeshlessScheme.cpp:8-19
+for construction, :39-253 for a step).  There is no CPU fallback: loading
+fails loudly when the CUDA library is missing or no GPU is visible.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+
+import numpy as np
+
+from .config import CConfig, MFVConfig, to_struct
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "libmlh.so")
+
+ERR_BITS = {
+    0: "NGB_OVERFLOW", 1: "NEG_PRESSURE", 2: "NEG_DENSITY", 3: "NEG_MASS", 4: "NEG_ENERGY",
+    5: "NEWTON", 6: "VACUUM", 7: "GRID", 8: "NO_NEIGHBOUR", 9: "ASYMMETRIC", 10: "NAN",
+    11: "TIMEOUT", 20: "INVALID", 21: "CUDA", 22: "NO_DEVICE", 23: "CAPACITY",
+}
+
+
+def status_names(st: int):
+    return [name for bit, name in ERR_BITS.items() if st & (1 << bit)]
+
+
+class MLHError(RuntimeError):
+    def __init__(self, status: int, where: str, msg: str = ""):
+        super().__init__(f"{where}: status {status:#x} {status_names(status)} {msg}")
+        self.status = status
+
+
+class ParticlesView(ctypes.Structure):
+    _fields_ = [("n", ctypes.c_int)] + [(k, ctypes.POINTER(ctypes.c_double))
+                                         for k in ("x", "y", "z", "vx", "vy", "vz", "m", "u")]
+
+
+class StepStats(ctypes.Structure):
+    _fields_ = [("steps", ctypes.c_int), ("status", ctypes.c_uint), ("dt", ctypes.c_double),
+                ("time", ctypes.c_double), ("pair_interactions", ctypes.c_longlong),
+                ("faces", ctypes.c_longlong), ("newton_iterations", ctypes.c_longlong),
+                ("device_ms", ctypes.c_double)]
+
+
+EXPORTS = ["mlh_abi_version", "mlh_last_error", "mlh_create", "mlh_destroy", "mlh_set_fields",
+           "mlh_get_fields", "mlh_step", "mlh_stage_array", "mlh_set_kernel_timing",
+           "mlh_kernel_times", "mlh_reset_kernel_times"]
+
+_lib = None
+
+
+def load(path: str = LIB_PATH):
+    """Load libmlh.so and declare the C ABI.  Raises if it is missing."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(path):
+        raise RuntimeError(f"{path} is missing: build it with meshlesshydro_gb300.build.build()")
+    L = ctypes.CDLL(path)
+    vp = ctypes.c_void_p
+    L.mlh_abi_version.restype = ctypes.c_int
+    L.mlh_last_error.restype = ctypes.c_char_p
+    L.mlh_create.argtypes = [ctypes.POINTER(CConfig), ctypes.POINTER(ParticlesView), ctypes.POINTER(vp)]
+    L.mlh_create.restype = ctypes.c_int
+    L.mlh_destroy.argtypes = [vp]
+    L.mlh_set_fields.argtypes = [vp, ctypes.POINTER(ParticlesView)]
+    L.mlh_set_fields.restype = ctypes.c_int
+    L.mlh_get_fields.argtypes = [vp, ctypes.POINTER(ParticlesView)]
+    L.mlh_get_fields.restype = ctypes.c_int
+    L.mlh_step.argtypes = [vp, ctypes.c_int, ctypes.c_double, ctypes.POINTER(StepStats)]
+    L.mlh_step.restype = ctypes.c_int
+    L.mlh_stage_array.argtypes = [vp, ctypes.c_char_p, vp, ctypes.c_longlong, ctypes.POINTER(ctypes.c_longlong)]
+    L.mlh_stage_array.restype = ctypes.c_int
+    L.mlh_set_kernel_timing.argtypes = [vp, ctypes.c_int]
+    L.mlh_set_kernel_timing.restype = ctypes.c_int
+    L.mlh_kernel_times.argtypes = [vp, ctypes.POINTER(ctypes.c_char_p), ctypes.POINTER(ctypes.c_longlong),
+                                   ctypes.POINTER(ctypes.c_double), ctypes.c_int]
+    L.mlh_kernel_times.restype = ctypes.c_int
+    L.mlh_reset_kernel_times.argtypes = [vp]
+    _lib = L
+    return L
+
+
+INT_ARRAYS = {"noi", "noi_img", "off", "nnl", "face_of"}
+
+
+class HostState:
+    """Pinned-free host SoA buffers matching mlh_particles_view."""
+
+    def __init__(self, pset=None, n=None, dim=None):
+        if pset is not None:
+            self.n, self.dim = pset.n, pset.dim
+            self.arrays = {k: np.ascontiguousarray(a, dtype=np.float64).copy()
+                           for k, a in zip(("x", "y", "z", "vx", "vy", "vz", "m", "u"), pset.arrays())}
+        else:
+            self.n, self.dim = n, dim
+            self.arrays = {k: np.zeros(n) for k in ("x", "y", "z", "vx", "vy", "vz", "m", "u")}
+        self.view = ParticlesView()
+        self.view.n = self.n
+        for k, a in self.arrays.items():
+            setattr(self.view, k, a.ctypes.data_as(ctypes.POINTER(ctypes.c_double)))
+
+
+class Simulation:
+    """One MFV simulation on the GPU through the C ABI."""
+
+    def __init__(self, cfg: MFVConfig, pset):
+        self.L = load()
+        self.cfg = cfg
+        self._cfg = to_struct(cfg)
+        self.host = HostState(pset)
+        self.n = pset.n
+        self.dim = cfg.dim
+        h = ctypes.c_void_p()
+        st = self.L.mlh_create(ctypes.byref(self._cfg), ctypes.byref(self.host.view), ctypes.byref(h))
+        if st != 0:
+            raise MLHError(st, "mlh_create", self.L.mlh_last_error().decode())
+        self.h = h
+
+    def step(self, nsteps: int = 1, dt_max: float = 0.0, check: bool = True) -> StepStats:
+        stats = StepStats()
+        st = self.L.mlh_step(self.h, nsteps, dt_max, ctypes.byref(stats))
+        if check and st != 0:
+            raise MLHError(st, "mlh_step", self.L.mlh_last_error().decode())
+        return stats
+
+    def get_state(self) -> dict:
+        st = self.L.mlh_get_fields(self.h, ctypes.byref(self.host.view))
+        if st != 0:
+            raise MLHError(st, "mlh_get_fields", self.L.mlh_last_error().decode())
+        keys = ("x", "y", "vx", "vy", "m", "u") + (("z", "vz") if self.dim == 3 else ())
+        return {k: self.host.arrays[k].copy() for k in keys}
+
+    def set_state(self, pset):
+        self.host = HostState(pset)
+        st = self.L.mlh_set_fields(self.h, ctypes.byref(self.host.view))
+        if st != 0:
+            raise MLHError(st, "mlh_set_fields", self.L.mlh_last_error().decode())
+
+    def get(self, name: str) -> np.ndarray:
+        cnt = ctypes.c_longlong()
+        st = self.L.mlh_stage_array(self.h, name.encode(), None, 0, ctypes.byref(cnt))
+        if st != 0:
+            raise MLHError(st, f"mlh_stage_array({name})", self.L.mlh_last_error().decode())
+        dt = np.uint32 if name in ("nnl",) else (np.int32 if name in INT_ARRAYS else np.float64)
+        out = np.empty(cnt.value, dtype=dt)
+        st = self.L.mlh_stage_array(self.h, name.encode(), out.ctypes.data_as(ctypes.c_void_p), cnt.value,
+                                    ctypes.byref(cnt))
+        if st != 0:
+            raise MLHError(st, f"mlh_stage_array({name})", self.L.mlh_last_error().decode())
+        return out
+
+    def set_kernel_timing(self, on: bool):
+        self.L.mlh_set_kernel_timing(self.h, 1 if on else 0)
+
+    def reset_kernel_times(self):
+        self.L.mlh_reset_kernel_times(self.h)
+
+    def kernel_times(self) -> dict:
+        k = 16
+        names = (ctypes.c_char_p * k)()
+        launches = (ctypes.c_longlong * k)()
+        ms = (ctypes.c_double * k)()
+        cnt = self.L.mlh_kernel_times(self.h, names, launches, ms, k)
+        return {names[i].decode(): (int(launches[i]), float(ms[i])) for i in range(cnt)}
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.L.mlh_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

@@ -1,0 +1,45 @@
+"""The C-ABI library loads and exports every symbol include/mlh.h declares
+(no compute calls: this runs without a GPU)."""
+import os
+import re
+
+from meshlesshydro_gb300 import build, runtime
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def declared_functions():
+    text = open(os.path.join(ROOT, "include", "mlh.h")).read()
+    return sorted(set(re.findall(r"\b(mlh_[a-z_]+)\s*\(", text)))
+
+
+def test_header_and_exports_agree():
+    build.build()
+    L = runtime.load()
+    names = declared_functions()
+    assert len(names) >= 10
+    for n in names:
+        assert hasattr(L, n), n
+    assert set(names) == set(runtime.EXPORTS)
+    assert L.mlh_abi_version() == 1
+
+
+def test_create_without_gpu_fails_cleanly():
+    import ctypes
+    from meshlesshydro_gb300 import ic
+    from meshlesshydro_gb300.config import MFVConfig, to_struct
+    L = runtime.load()
+    p = ic.kelvin_helmholtz(n_side=8, seed=1)
+    hs = runtime.HostState(p)
+    cfg = to_struct(MFVConfig.kelvin_helmholtz(p))
+    h = ctypes.c_void_p()
+    import torch
+    st = L.mlh_create(ctypes.byref(cfg), ctypes.byref(hs.view), ctypes.byref(h))
+    if not torch.cuda.is_available():
+        assert st == (1 << 22)  # MLH_ERR_NO_DEVICE
+    else:
+        assert st == 0
+        L.mlh_destroy(h)
+    # invalid arguments are rejected before touching the device
+    cfg.dim = 4
+    assert L.mlh_create(ctypes.byref(cfg), ctypes.byref(hs.view), ctypes.byref(h)) == (1 << 20)

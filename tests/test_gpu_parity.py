@@ -1,0 +1,178 @@
+"""GPU parity: the CUDA MFV step (libmlh.so, through the C ABI) against the
+CPU oracle on identical seeded inputs.
+
+Bar: neighbour lists bit-exact (indices, order, image flags); every per-step
+field within FIELD_RTOL = 1e-12 normwise relative error (max |a-b| / max |b|).
+The oracle itself is pinned to the reference's own code by
+tests/test_oracle_golden.py.
+"""
+import numpy as np
+import pytest
+
+from meshlesshydro_gb300 import ic
+from meshlesshydro_gb300.config import MFVConfig
+from helpers import FIELD_RTOL, assert_close, normwise
+
+pytestmark = pytest.mark.gpu
+
+
+def _sim(cfg, p):
+    from meshlesshydro_gb300 import build, runtime
+    build.build()
+    return runtime.Simulation(cfg, p)
+
+
+def cases():
+    kh24 = ic.kelvin_helmholtz(n_side=24, seed=3)
+    kh100 = ic.kelvin_helmholtz(n_side=100, seed=1)
+    sd12 = ic.sedov(n_side=12, seed=4, energy=0.05)
+    sd16 = ic.sedov(n_side=16, seed=5)
+    return {
+        "kh24": (kh24, MFVConfig.kelvin_helmholtz(kh24)),
+        "kh24_int_abs": (kh24, MFVConfig.kelvin_helmholtz(kh24, int_abs=True)),
+        "kh24_pairwise": (kh24, MFVConfig.kelvin_helmholtz(kh24, pairwise_limiter=True)),
+        "kh100": (kh100, MFVConfig.kelvin_helmholtz(kh100)),
+        "sedov12_nonperiodic_nopw": (sd12, MFVConfig.sedov(sd12, periodic=False, pairwise_limiter=False)),
+        "sedov16_nonperiodic": (sd16, MFVConfig.sedov(sd16, periodic=False)),
+        "sedov16_periodic": (sd16, MFVConfig.sedov(sd16, periodic=True)),
+        "sedov16_periodic_int_abs": (sd16, MFVConfig.sedov(sd16, periodic=True, int_abs=True)),
+    }
+
+
+CASES = cases()
+
+
+@pytest.mark.parametrize("name", sorted(CASES))
+def test_one_step_stagewise(oracle_mod, name):
+    p, cfg = CASES[name]
+    o = oracle_mod.Oracle(cfg, p)
+    assert o.step() == 0
+    g = _sim(cfg, p)
+    stats = g.step(1)
+    assert stats.steps == 1
+    # neighbour search: bit-exact
+    for k in ("off", "noi", "noi_img"):
+        np.testing.assert_array_equal(g.get(k), o.get(k), err_msg=k)
+    np.testing.assert_array_equal(g.get("nnl"), o.get("nnl"))
+    np.testing.assert_array_equal(g.get("grid"), o.get("grid"))
+    for k in ("omega", "rho", "P", "dt"):
+        assert_close(g.get(k), o.get(k), what=k)
+    fields = ["rho", "vx", "vy"] + (["vz"] if cfg.dim == 3 else []) + ["P"]
+    for f in fields:
+        assert_close(g.get("gradraw_" + f), o.get("gradraw_" + f), what="gradraw_" + f)
+        assert_close(g.get("grad_" + f), o.get("grad_" + f), what="grad_" + f)
+    assert_close(g.get("B"), o.get("B"), what="B")
+    # per-interaction fluxes with the reference's sign convention
+    assert_close(g.get("F"), o.get("F"), what="F")
+    assert_close(g.get("mF"), o.get("mF"), what="mF")
+    assert_close(g.get("eF"), o.get("eF"), what="eF")
+    assert_close(g.get("vF").reshape(-1, 3)[:, :cfg.dim], o.get("vF").reshape(-1, 3)[:, :cfg.dim], what="vF")
+    gs = g.get_state()
+    for k, v in o.state().items():
+        assert_close(gs[k], v, what="state " + k)
+    assert stats.faces == int(o.get("stats")[0])
+
+
+def test_flux_antisymmetry_bitwise():
+    """Particles::checkFluxSymmetry (Particles.cpp:2888-2976): F_ji = -F_ij exactly."""
+    p, cfg = CASES["sedov16_periodic"]
+    g = _sim(cfg, p)
+    g.step(1)
+    off = g.get("off")
+    nnl = g.get("nnl")
+    noi = g.get("noi")
+    F = g.get("F").reshape(-1, cfg.dim + 2)
+    idx = nnl & ((1 << 29) - 1)
+    n = p.n
+    checked = 0
+    for i in range(0, n, 7):
+        for s in range(off[i], off[i + 1]):
+            j = int(idx[s])
+            img = (s - off[i]) >= noi[i]
+            lo, hi = (off[j] + noi[j], off[j + 1]) if img else (off[j], off[j] + noi[j])
+            t = lo + int(np.nonzero(idx[lo:hi] == i)[0][0])
+            assert np.array_equal(F[s], -F[t])
+            checked += 1
+    assert checked > 1000
+
+
+def _totals(st, dim):
+    m = st["m"]
+    v = [st["vx"], st["vy"]] + ([st["vz"]] if dim == 3 else [])
+    E = m * (st["u"] + 0.5 * sum(c * c for c in v))
+    import math
+    return {"mass": math.fsum(m), "energy": math.fsum(E),
+            **{f"p{a}": math.fsum(m * c) for a, c in zip("xyz", v)},
+            "pscale": math.fsum(m * np.sqrt(sum(c * c for c in v)))}
+
+
+@pytest.mark.parametrize("name", ["kh100", "sedov16_periodic"])
+def test_conservation(name):
+    """Mass and energy to 1e-13 relative per step; momentum relative to sum m|v|."""
+    p, cfg = CASES[name]
+    g = _sim(cfg, p)
+    t0 = _totals(g.get_state(), cfg.dim)
+    for _ in range(10):
+        g.step(1)
+        t1 = _totals(g.get_state(), cfg.dim)
+        assert abs(t1["mass"] - t0["mass"]) <= 1e-13 * abs(t0["mass"])
+        assert abs(t1["energy"] - t0["energy"]) <= 1e-13 * abs(t0["energy"])
+        for a in "xyz"[:cfg.dim]:
+            assert abs(t1["p" + a] - t0["p" + a]) <= 1e-13 * max(t0["pscale"], 1e-300) + 1e-18
+        t0 = t1
+
+
+def test_deterministic_bitwise():
+    p, cfg = CASES["sedov16_periodic"]
+    a = _sim(cfg, p)
+    b = _sim(cfg, p)
+    a.step(3)
+    b.step(3)
+    sa, sb = a.get_state(), b.get_state()
+    for k in sa:
+        assert np.array_equal(sa[k], sb[k]), k
+
+
+def test_neighbour_overflow_retry(oracle_mod):
+    """Too few slots: the step detects the overflow, grows the slots and
+    repeats (the reference exits, Particles.cpp:348-352)."""
+    p, cfg = CASES["kh24"]
+    from dataclasses import replace
+    g = _sim(replace(cfg, max_neighbours=6), p)
+    g.step(2)
+    o = oracle_mod.Oracle(cfg, p)
+    o.step(); o.step()
+    np.testing.assert_array_equal(g.get("nnl"), o.get("nnl"))
+    gs = g.get_state()
+    for k, v in o.state().items():
+        assert_close(gs[k], v, rtol=1e-11, what=k)
+
+
+def test_negative_pressure_reported():
+    """A negative internal energy gives P < 0: the status word reports it
+    (the reference only warns, Particles.cpp:1284-1286)."""
+    p, cfg = CASES["kh24"]
+    q = p.copy()
+    q.u[5] = -1.0
+    from meshlesshydro_gb300 import runtime
+    g = _sim(cfg, q)
+    st = g.step(1, check=False)
+    assert st.status & (1 << 1)
+
+
+@pytest.mark.parametrize("name,nsteps,rtol", [("kh100", 100, 1e-8), ("sedov16_periodic", 30, 1e-8),
+                                              ("sedov16_nonperiodic", 60, 1e-8)])
+def test_multistep_density_l1(oracle_mod, name, nsteps, rtol):
+    """Density after many steps: L1 relative difference to the oracle."""
+    p, cfg = CASES[name]
+    o = oracle_mod.Oracle(cfg, p)
+    g = _sim(cfg, p)
+    for _ in range(nsteps):
+        assert o.step() == 0
+    g.step(nsteps)
+    # density of the final state: one more density evaluation on both sides
+    o.step()
+    g.step(1)
+    ro, rg = o.get("rho"), g.get("rho")
+    l1 = np.sum(np.abs(rg - ro)) / np.sum(np.abs(ro))
+    assert l1 <= rtol, f"L1 {l1:.3e}"
