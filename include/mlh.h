@@ -131,6 +131,12 @@ int mlh_set_kernel_timing(mlh_ctx *ctx, int enable);
 int mlh_kernel_times(mlh_ctx *ctx, const char **names, long long *launches, double *total_ms, int max);
 void mlh_reset_kernel_times(mlh_ctx *ctx);
 
+/* FP64 fused multiply-add throughput of the current device (TFLOP/s, an FMA
+ * counts as two operations), measured for about `seconds`: the denominator
+ * of the FP64 roofline.  No counterpart in the reference (it has no GPU
+ * code); used by bench.py. */
+int mlh_probe_fp64_tflops(double seconds, double *tflops);
+
 #ifdef __cplusplus
 }
 #endif

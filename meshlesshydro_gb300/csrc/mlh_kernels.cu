@@ -376,19 +376,28 @@ __global__ void __launch_bounds__(128) k_neighbours(
             if (nr > K) nr = K;
             ni = K - nr < ni ? K - nr : ni;
         }
-        // move images behind the real neighbours, ordered by parent index
-        for (int q = 0; q < ni; ++q) {
-            uint32_t e = nbr[base + K - 1 - q];
-            double r = rr[base + K - 1 - q];
-            int t = nr + q - 1;
-            // insertion into [nr, nr+q)
-            while (t >= nr && (nbr[base + t] & IDX_MASK) > (e & IDX_MASK)) {
-                nbr[base + t + 1] = nbr[base + t];
-                rr[base + t + 1] = rr[base + t];
-                --t;
+        // images sit in [K - ni, K) in reverse discovery order: sort them there
+        // by parent index, then move the block down behind the real neighbours
+        // (destination below source, so a forward copy is safe)
+        {
+            const int b0 = K - ni;
+            for (int k = b0 + 1; k < K; ++k) {
+                const uint32_t e = nbr[base + k];
+                const double r = rr[base + k];
+                int t = k - 1;
+                while (t >= b0 && (nbr[base + t] & IDX_MASK) > (e & IDX_MASK)) {
+                    nbr[base + t + 1] = nbr[base + t];
+                    rr[base + t + 1] = rr[base + t];
+                    --t;
+                }
+                nbr[base + t + 1] = e;
+                rr[base + t + 1] = r;
             }
-            nbr[base + t + 1] = e;
-            rr[base + t + 1] = r;
+            if (b0 != nr)
+                for (int t = 0; t < ni; ++t) {
+                    nbr[base + nr + t] = nbr[base + b0 + t];
+                    rr[base + nr + t] = rr[base + b0 + t];
+                }
         }
         const int tot = nr + ni;
         if (tot == 0) flag(status, ST_NO_NEIGHBOUR);
@@ -798,8 +807,11 @@ __global__ void __launch_bounds__(128) k_faces(Params p, const GridInfo *__restr
         {
             const double psi_i = wij * gi.V, psi_j = wji * gj.V;
             double dij[3], dji[3];
+            // psi~_i(x_j) is formed in j's own frame: image of i minus the
+            // real position of j (Particles.cpp:2428-2453 for ghosts)
+            const double xjr[3] = {pj.x, pj.y, pj.z};
 #pragma unroll
-            for (int a = 0; a < D; ++a) { dij[a] = xj[a] - xi[a]; dji[a] = xir[a] - xj[a]; }
+            for (int a = 0; a < D; ++a) { dij[a] = xj[a] - xi[a]; dji[a] = xir[a] - xjr[a]; }
 #pragma unroll
             for (int a = 0; a < D; ++a) {
                 double t1 = 0., t2 = 0.;

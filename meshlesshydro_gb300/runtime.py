@@ -48,7 +48,7 @@ class StepStats(ctypes.Structure):
 
 EXPORTS = ["mlh_abi_version", "mlh_last_error", "mlh_create", "mlh_destroy", "mlh_set_fields",
            "mlh_get_fields", "mlh_step", "mlh_stage_array", "mlh_set_kernel_timing",
-           "mlh_kernel_times", "mlh_reset_kernel_times"]
+           "mlh_kernel_times", "mlh_reset_kernel_times", "mlh_probe_fp64_tflops"]
 
 _lib = None
 
@@ -81,6 +81,8 @@ def load(path: str = LIB_PATH):
                                    ctypes.POINTER(ctypes.c_double), ctypes.c_int]
     L.mlh_kernel_times.restype = ctypes.c_int
     L.mlh_reset_kernel_times.argtypes = [vp]
+    L.mlh_probe_fp64_tflops.argtypes = [ctypes.c_double, ctypes.POINTER(ctypes.c_double)]
+    L.mlh_probe_fp64_tflops.restype = ctypes.c_int
     _lib = L
     return L
 
@@ -103,6 +105,16 @@ class HostState:
         self.view.n = self.n
         for k, a in self.arrays.items():
             setattr(self.view, k, a.ctypes.data_as(ctypes.POINTER(ctypes.c_double)))
+
+
+def probe_fp64_tflops(seconds: float = 0.5) -> float:
+    """FP64 FMA throughput of the current GPU in TFLOP/s (mlh_probe_fp64_tflops)."""
+    L = load()
+    out = ctypes.c_double()
+    st = L.mlh_probe_fp64_tflops(seconds, ctypes.byref(out))
+    if st != 0:
+        raise MLHError(st, "mlh_probe_fp64_tflops", L.mlh_last_error().decode())
+    return out.value
 
 
 class Simulation:

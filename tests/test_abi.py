@@ -10,7 +10,7 @@ ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 
 def declared_functions():
     text = open(os.path.join(ROOT, "include", "mlh.h")).read()
-    return sorted(set(re.findall(r"\b(mlh_[a-z_]+)\s*\(", text)))
+    return sorted(set(re.findall(r"\b(mlh_[a-z_0-9]+)\s*\(", text)))
 
 
 def test_header_and_exports_agree():
