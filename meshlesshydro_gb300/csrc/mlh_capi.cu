@@ -2,6 +2,7 @@
 // step driver with capacity retries, parity dumps and kernel timing.
 #include "../../include/mlh.h"
 #include "mlh_kernels.h"
+#include "mlh_riemann.cuh"
 
 #include <cmath>
 #include <cstdio>
@@ -52,7 +53,8 @@ struct mlh_ctx {
     int *cell = nullptr, *cellCount = nullptr, *cellStart = nullptr, *cellFill = nullptr, *cellList = nullptr;
     // neighbours (capacity K slots per particle)
     uint32_t *nbr = nullptr;
-    double *rr = nullptr, *ww = nullptr;
+    double *rr = nullptr, *ww = nullptr, *psi = nullptr;
+    size_t faces_cap = 0;
     int *noi = nullptr, *noiImg = nullptr, *faceCnt = nullptr, *faceOff = nullptr, *faceOf = nullptr;
     FaceRef *faces = nullptr;
     double *Fface = nullptr;
@@ -78,8 +80,10 @@ struct mlh_ctx {
 namespace {
 
 void free_neighbour_buffers(mlh_ctx *c) {
-    cudaFree(c->nbr); cudaFree(c->rr); cudaFree(c->ww); cudaFree(c->faceOf); cudaFree(c->faces); cudaFree(c->Fface);
-    c->nbr = nullptr; c->rr = nullptr; c->ww = nullptr; c->faceOf = nullptr; c->faces = nullptr; c->Fface = nullptr;
+    cudaFree(c->nbr); cudaFree(c->rr); cudaFree(c->ww); cudaFree(c->psi); cudaFree(c->faceOf); cudaFree(c->faces);
+    cudaFree(c->Fface);
+    c->nbr = nullptr; c->rr = nullptr; c->ww = nullptr; c->psi = nullptr; c->faceOf = nullptr; c->faces = nullptr;
+    c->Fface = nullptr;
 }
 
 int alloc_neighbour_buffers(mlh_ctx *c) {
@@ -88,6 +92,8 @@ int alloc_neighbour_buffers(mlh_ctx *c) {
     CK(dalloc(&c->nbr, slots));
     CK(dalloc(&c->rr, slots));
     CK(dalloc(&c->ww, slots));
+    CK(dalloc(&c->psi, slots * 3));
+    c->faces_cap = faces;
     CK(dalloc(&c->faceOf, slots));
     CK(dalloc(&c->faces, faces));
     CK(dalloc(&c->Fface, faces * 6));
@@ -153,13 +159,15 @@ StepArgs make_args(mlh_ctx *c, double dt_max) {
     a.p = c->p;
     a.stream = c->stream;
     a.face_blocks = c->sm_count * 8;
+    a.faces_cap = c->faces_cap;
+    a.root5 = make_riemann_consts(c->p.gamma, c->p.rtol, c->p.rmaxit).root5;
     a.dt_max = dt_max;
     a.x = c->x; a.y = c->y; a.z = c->z; a.vx = c->vx; a.vy = c->vy; a.vz = c->vz; a.m = c->m; a.u = c->u;
     a.posf = c->posf;
     a.grid = c->grid; a.boundsPart = c->boundsPart;
     a.cell = c->cell; a.cellCount = c->cellCount; a.cellStart = c->cellStart; a.cellFill = c->cellFill;
     a.cellList = c->cellList;
-    a.nbr = c->nbr; a.rr = c->rr; a.ww = c->ww;
+    a.nbr = c->nbr; a.rr = c->rr; a.ww = c->ww; a.psi = c->psi;
     a.noi = c->noi; a.noiImg = c->noiImg; a.faceCnt = c->faceCnt; a.faceOff = c->faceOff; a.faceOf = c->faceOf;
     a.faces = c->faces;
     a.prim = c->prim; a.geo = c->geo; a.grad = c->grad; a.gradRaw = c->debug_arrays ? c->gradRaw : nullptr;

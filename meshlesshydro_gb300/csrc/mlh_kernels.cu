@@ -455,8 +455,10 @@ __global__ void __launch_bounds__(256) k_timestep(Params p, const Prim *__restri
             const double cj = geo[j].c;
             double xij[3] = {pi.x - pj.x, pi.y - pj.y, pi.z - pj.z};
             double vij[3] = {pi.vx - pj.vx, pi.vy - pj.vy, pi.vz - pj.vz};
-            double vijxij = dotD<D>(vij, xij) / rr[base + s];
-            vijxij = vijxij < 0. ? vijxij : 0.;
+            // min(0, v_ij . x_ij / r): the quotient is needed only when the
+            // dot product is negative (same value and sign as the reference's)
+            const double dv = dotD<D>(vij, xij);
+            const double vijxij = dv < 0. ? dv / rr[base + s] : 0.;
             double vs = ci + cj - vijxij;
             vSig = vs > vSig ? vs : vSig;
         }
@@ -532,7 +534,8 @@ __global__ void __launch_bounds__(128) k_gradients(Params p, const GridInfo *__r
                                                    const Prim *__restrict__ prim, Geo *__restrict__ geo,
                                                    const uint32_t *__restrict__ nbr, const double *__restrict__ ww,
                                                    const int *__restrict__ noi, const int *__restrict__ noiImg,
-                                                   Grad *__restrict__ grad, Grad *__restrict__ gradRaw) {
+                                                   Grad *__restrict__ grad, Grad *__restrict__ gradRaw,
+                                                   double *__restrict__ psiOut) {
     constexpr int NF = D + 2;
     const GridInfo g = *gridp;
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < p.n; i += gridDim.x * blockDim.x) {
@@ -581,6 +584,10 @@ __global__ void __launch_bounds__(128) k_gradients(Params p, const GridInfo *__r
                 for (int b = 0; b < D; ++b) t += E[D * a + b] * d[b] * psij;
                 ps[a] = t;
             }
+            // psi~_j(x_i) of this slot, reused by the face kernel for A_ij
+            double *po = psiOut + (base + s) * 3;
+#pragma unroll
+            for (int a = 0; a < D; ++a) po[a] = ps[a];
 #pragma unroll
             for (int f = 0; f < NF; ++f) {
                 const double df = field_of<D>(pj, f) - fi[f];
@@ -663,6 +670,8 @@ __global__ void __launch_bounds__(128) k_link(Params p, const uint32_t *__restri
                                               const int *__restrict__ noiImg, const int *__restrict__ faceOff,
                                               int *__restrict__ faceOf, FaceRef *__restrict__ faces,
                                               unsigned *__restrict__ status) {
+    // faces[] was set to -1: the owner writes (i, slot), the slot on the other
+    // side writes rslot, so each field has exactly one writer
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < p.n; i += gridDim.x * blockDim.x) {
         const size_t base = (size_t)i * p.K;
         const int nr = noi[i], tot = nr + noiImg[i];
@@ -670,35 +679,30 @@ __global__ void __launch_bounds__(128) k_link(Params p, const uint32_t *__restri
         for (int s = 0; s < tot; ++s) {
             const uint32_t e = nbr[base + s];
             const int j = (int)(e & IDX_MASK);
-            const bool img = s >= nr;
-            // search j's list (matching part) for i
-            const size_t jb = (size_t)j * p.K;
-            const int jnr = noi[j];
-            const int b = img ? jnr : 0, en = img ? jnr + noiImg[j] : jnr;
-            int found = -1, crank = 0;
-            const bool canon = j > i;
-            if (!canon || img) {
-                for (int t = b; t < en; ++t) {
-                    const uint32_t f = nbr[jb + t];
-                    const int q = (int)(f & IDX_MASK);
-                    if (q == i) { found = t; break; }
-                }
-            }
-            if (canon) {
+            if (j > i) {
                 const int fid = faceOff[i] + rank;
                 ++rank;
                 faceOf[base + s] = fid + 1;
-                FaceRef fr;
-                fr.i = i; fr.slot = s; fr.rslot = img ? found : -1; fr.pad = 0;
-                if (img && found < 0) flag(status, ST_ASYMMETRIC);
-                faces[fid] = fr;
-            } else {
-                if (found < 0) { flag(status, ST_ASYMMETRIC); faceOf[base + s] = 0; continue; }
-                // rank of slot `found` among j's canonical slots
-                for (int t = 0; t < found; ++t)
-                    if ((int)(nbr[jb + t] & IDX_MASK) > j) ++crank;
-                faceOf[base + s] = -(faceOff[j] + crank + 1);
+                faces[fid].i = i;
+                faces[fid].slot = s;
+                continue;
             }
+            // search j's list (real part or image part) for i
+            const bool img = s >= nr;
+            const size_t jb = (size_t)j * p.K;
+            const int jnr = noi[j];
+            const int b = img ? jnr : 0, en = img ? jnr + noiImg[j] : jnr;
+            int found = -1;
+            for (int t = b; t < en; ++t)
+                if ((int)(nbr[jb + t] & IDX_MASK) == i) { found = t; break; }
+            if (found < 0) { flag(status, ST_ASYMMETRIC); faceOf[base + s] = 0; continue; }
+            // rank of slot `found` among j's canonical slots
+            int crank = 0;
+            for (int t = 0; t < found; ++t)
+                if ((int)(nbr[jb + t] & IDX_MASK) > j) ++crank;
+            const int fid = faceOff[j] + crank;
+            faceOf[base + s] = -(fid + 1);
+            faces[fid].rslot = s;
         }
     }
 }
@@ -755,19 +759,22 @@ __device__ __forceinline__ void rot3(const double *a, const double *b, double *L
     L[8] = 1. - n * (v1 * v1 + v0 * v0);
 }
 
-// One canonical face (i < j): effective face A_ij (compEffectiveFace,
-// Particles.cpp:1290-1311, 2504-2531) from B_i and B_j; boosted, reconstructed,
-// optionally pairwise-limited and half-step-predicted states
-// (compRiemannStatesLR, :1488-1733 / 2533-2683, including the vz[i] of
-// :1717,1719); rotation to the face frame, exact solve with i as the left
-// state, rotation back and projection on A_ij (Riemann::Riemann/exact/
-// rotateAndProjectFluxes2D/3D, demonstrator/src/Riemann.cpp:7-229).
-// Output slot order: [mass, energy, px, py, pz].
-template <int D>
+// One canonical face (i < j): effective face A_ij = psi~_j(x_i)/omega_i -
+// psi~_i(x_j)/omega_j from the psi~ of both slots (compEffectiveFace,
+// Particles.cpp:1290-1311, 2504-2531); boosted, reconstructed, optionally
+// pairwise-limited and half-step-predicted states (compRiemannStatesLR,
+// :1488-1733 / 2533-2683, including the vz[i] of :1717,1719); rotation to the
+// face frame, exact solve with i as the left state, rotation back and
+// projection on A_ij (Riemann::Riemann/exact/rotateAndProjectFluxes2D/3D,
+// demonstrator/src/Riemann.cpp:7-229).  The back rotation of
+// Helper::rotationMatrix2D/3D(unitX, hatA) is the transpose of the forward
+// one, bit for bit, so it is not recomputed.  Output slot order:
+// [mass, energy, px, py, pz].
+template <int D, bool ROOT5>
 __global__ void __launch_bounds__(128) k_faces(Params p, const GridInfo *__restrict__ gridp,
                                                const Prim *__restrict__ prim, const Geo *__restrict__ geo,
                                                const Grad *__restrict__ grad, const uint32_t *__restrict__ nbr,
-                                               const double *__restrict__ ww, const int *__restrict__ faceTotal,
+                                               const double *__restrict__ psi, const int *__restrict__ faceTotal,
                                                const FaceRef *__restrict__ faces, const double *__restrict__ dtp,
                                                double *__restrict__ Fface, unsigned long long *__restrict__ newtonSum,
                                                unsigned *__restrict__ status) {
@@ -787,40 +794,21 @@ __global__ void __launch_bounds__(128) k_faces(Params p, const GridInfo *__restr
         const int j = (int)(e & IDX_MASK);
         const bool img = (e >> IMG_SHIFT) != 0;
         const Prim pi = prim[i], pj = prim[j];
-        const Geo gi = geo[i], gj = geo[j];
+        const double Vi = geo[i].V, Vj = geo[j].V;
         double xi[3] = {pi.x, pi.y, pi.z}, xj[3];
         neighbour_pos<D>(e, pj, g, p.h, xj);
-        // reverse geometry: position of i as seen from j, and W from j's slot
-        double xir[3] = {pi.x, pi.y, pi.z};
-        double wij = ww[si], wji = wij;
-        if (img) {
-            if (fr.rslot >= 0) {
-                const size_t sj = (size_t)j * p.K + fr.rslot;
-                neighbour_pos<D>(nbr[sj], pi, g, p.h, xir);
-                wji = ww[sj];
-            } else {
-                wji = 0.;
-            }
-        }
         // --- effective face
-        double A[3];
+        double A[3] = {0., 0., 0.};
         {
-            const double psi_i = wij * gi.V, psi_j = wji * gj.V;
-            double dij[3], dji[3];
-            // psi~_i(x_j) is formed in j's own frame: image of i minus the
-            // real position of j (Particles.cpp:2428-2453 for ghosts)
-            const double xjr[3] = {pj.x, pj.y, pj.z};
+            const double *ps_i = psi + si * 3;
+            if (fr.rslot >= 0) {
+                const double *ps_j = psi + ((size_t)j * p.K + fr.rslot) * 3;
 #pragma unroll
-            for (int a = 0; a < D; ++a) { dij[a] = xj[a] - xi[a]; dji[a] = xir[a] - xjr[a]; }
+                for (int a = 0; a < D; ++a) A[a] = Vi * ps_i[a] - Vj * ps_j[a];
+            } else {
+                st_local |= ST_ASYMMETRIC;
 #pragma unroll
-            for (int a = 0; a < D; ++a) {
-                double t1 = 0., t2 = 0.;
-#pragma unroll
-                for (int b = 0; b < D; ++b) {
-                    t1 += gi.B[D * a + b] * dij[b] * psi_i;
-                    t2 += gj.B[D * a + b] * dji[b] * psi_j;
-                }
-                A[a] = gi.V * t1 - gj.V * t2;
+                for (int a = 0; a < D; ++a) A[a] = Vi * ps_i[a];
             }
         }
         // --- states at the face
@@ -851,7 +839,7 @@ __global__ void __launch_bounds__(128) k_faces(Params p, const GridInfo *__restr
             }
         }
         const double *Gi = grad[i].g, *Gj = grad[j].g;
-        // gradient blocks: 0 rho, 1 vx, 2 vy, 3 vz, 4 P
+        // gradient blocks: 0 rho, 3 vx, 6 vy, 9 vz, 12 P
         double R[5], L[5];
         R[0] = pi.rho; L[0] = pj.rho;
         R[1] = pi.P; L[1] = pj.P;
@@ -887,15 +875,16 @@ __global__ void __launch_bounds__(128) k_faces(Params p, const GridInfo *__restr
             double vjDiv = Gj[3 + 0] + Gj[6 + 1];
             if (D == 3) { viDiv += Gi[9 + 2]; vjDiv += Gj[9 + 2]; }
             const double hdt = dt / 2.;
+            const double iri = 1. / pi.rho, irj = 1. / pj.rho;
             const double ui0 = vi[0] - vf[0], ui1 = vi[1] - vf[1], uj0 = vj[0] - vf[0], uj1 = vj[1] - vf[1];
             R[0] -= hdt * (pi.rho * viDiv + ui0 * Gi[0] + ui1 * Gi[1]);
             L[0] -= hdt * (pj.rho * vjDiv + uj0 * Gj[0] + uj1 * Gj[1]);
             R[1] -= hdt * (gamma * pi.P * viDiv + ui0 * Gi[12] + ui1 * Gi[13]);
             L[1] -= hdt * (gamma * pj.P * vjDiv + uj0 * Gj[12] + uj1 * Gj[13]);
-            R[2] -= hdt * (Gi[12] / pi.rho + ui0 * Gi[3] + ui1 * Gi[4]);
-            L[2] -= hdt * (Gj[12] / pj.rho + uj0 * Gj[3] + uj1 * Gj[4]);
-            R[3] -= hdt * (Gi[13] / pi.rho + ui0 * Gi[6] + ui1 * Gi[7]);
-            L[3] -= hdt * (Gj[13] / pj.rho + uj0 * Gj[6] + uj1 * Gj[7]);
+            R[2] -= hdt * (Gi[12] * iri + ui0 * Gi[3] + ui1 * Gi[4]);
+            L[2] -= hdt * (Gj[12] * irj + uj0 * Gj[3] + uj1 * Gj[4]);
+            R[3] -= hdt * (Gi[13] * iri + ui0 * Gi[6] + ui1 * Gi[7]);
+            L[3] -= hdt * (Gj[13] * irj + uj0 * Gj[6] + uj1 * Gj[7]);
             if (D == 3) {
                 const double ui2 = vi[2] - vf[2], uj2 = vj[2] - vf[2];
                 R[0] -= hdt * ui2 * Gi[2];
@@ -907,8 +896,8 @@ __global__ void __launch_bounds__(128) k_faces(Params p, const GridInfo *__restr
                 L[2] -= hdt * ui2 * Gj[5];
                 R[3] -= hdt * ui2 * Gi[8];
                 L[3] -= hdt * ui2 * Gj[8];
-                R[4] -= hdt * (Gi[14] / pi.rho + ui0 * Gi[9] + ui1 * Gi[10] + ui2 * Gi[11]);
-                L[4] -= hdt * (Gj[14] / pj.rho + uj0 * Gj[9] + uj1 * Gj[10] + uj2 * Gj[11]);
+                R[4] -= hdt * (Gi[14] * iri + ui0 * Gi[9] + ui1 * Gi[10] + ui2 * Gi[11]);
+                L[4] -= hdt * (Gj[14] * irj + uj0 * Gj[9] + uj1 * Gj[10] + uj2 * Gj[11]);
             }
         }
         if (R[1] < 0. || L[1] < 0.) st_local |= ST_NEG_PRESSURE;
@@ -916,8 +905,9 @@ __global__ void __launch_bounds__(128) k_faces(Params p, const GridInfo *__restr
         const double unitX[3] = {1., 0., 0.};
         double AN = sqrt(dotD<D>(A, A));
         double hatA[3] = {0., 0., 0.};
+        const double iAN = 1. / AN;
 #pragma unroll
-        for (int a = 0; a < D; ++a) hatA[a] = 1. / AN * A[a];
+        for (int a = 0; a < D; ++a) hatA[a] = iAN * A[a];
         double Lam[9];
         if (D == 2) {
             rot2(hatA, unitX, Lam);
@@ -936,7 +926,8 @@ __global__ void __launch_bounds__(128) k_faces(Params p, const GridInfo *__restr
             R[3] = Lam[3] * bL0 + Lam[4] * bL1 + Lam[5] * bL2;
             R[4] = Lam[6] * bL0 + Lam[7] * bL1 + Lam[8] * bL2;
         }
-        RiemannResult rs = riemann_exact(rc, R[0], R[2], R[1], L[0], L[2], L[1]);
+        RiemannResult rs = ROOT5 ? riemann_exact5(rc, R[0], R[2], R[1], L[0], L[2], L[1])
+                                 : riemann_exact(rc, R[0], R[2], R[1], L[0], L[2], L[1]);
         if (rs.iters < 0) st_local |= ST_NEWTON;
         else iters_local += (unsigned long long)rs.iters;
         double vSol[3] = {rs.u, 0., 0.};
@@ -944,29 +935,26 @@ __global__ void __launch_bounds__(128) k_faces(Params p, const GridInfo *__restr
         else if (rs.flag == -1) { for (int a = 1; a < D; ++a) vSol[a] = R[2 + a]; }
         else st_local |= ST_VACUUM;
         const double rhoSol = rs.rho, PSol = rs.p;
+        const double pe = PSol * rc.inv_gm1;
         double Fo[5];
         if (D == 2) {
-            double LI[4];
-            rot2(unitX, hatA, LI);
+            // back rotation = transpose of Lam
             double b0 = vSol[0], b1 = vSol[1];
-            vSol[0] = LI[0] * b0 + LI[1] * b1;
-            vSol[1] = LI[2] * b0 + LI[3] * b1;
+            vSol[0] = Lam[0] * b0 + Lam[2] * b1;
+            vSol[1] = Lam[1] * b0 + Lam[3] * b1;
             Fo[0] = A[0] * rhoSol * vSol[0] + A[1] * rhoSol * vSol[1];
             double vLab[2] = {vSol[0] + vf[0], vSol[1] + vf[1]};
             if (p.mfm) { vSol[0] = 0.; vSol[1] = 0.; }
             Fo[2] = A[0] * (rhoSol * vLab[0] * vSol[0] + PSol) + A[1] * rhoSol * vLab[0] * vSol[1];
             Fo[3] = A[0] * rhoSol * vLab[1] * vSol[0] + A[1] * (rhoSol * vLab[1] * vSol[1] + PSol);
             const double ek = rhoSol * .5 * (vLab[0] * vLab[0] + vLab[1] * vLab[1]);
-            const double pe = PSol / (gamma - 1.);
             Fo[1] = A[0] * (vSol[0] * (pe + ek) + PSol * vLab[0]) + A[1] * (vSol[1] * (pe + ek) + PSol * vLab[1]);
             Fo[4] = 0.;
         } else {
-            double LI[9];
-            rot3(unitX, hatA, LI);
             double b0 = vSol[0], b1 = vSol[1], b2 = vSol[2];
-            vSol[0] = LI[0] * b0 + LI[1] * b1 + LI[2] * b2;
-            vSol[1] = LI[3] * b0 + LI[4] * b1 + LI[5] * b2;
-            vSol[2] = LI[6] * b0 + LI[7] * b1 + LI[8] * b2;
+            vSol[0] = Lam[0] * b0 + Lam[3] * b1 + Lam[6] * b2;
+            vSol[1] = Lam[1] * b0 + Lam[4] * b1 + Lam[7] * b2;
+            vSol[2] = Lam[2] * b0 + Lam[5] * b1 + Lam[8] * b2;
             Fo[0] = A[0] * rhoSol * vSol[0] + A[1] * rhoSol * vSol[1] + A[2] * rhoSol * vSol[2];
             double vLab[3] = {vSol[0] + vf[0], vSol[1] + vf[1], vSol[2] + vf[2]};
             if (p.mfm) { vSol[0] = 0.; vSol[1] = 0.; vSol[2] = 0.; }
@@ -974,7 +962,6 @@ __global__ void __launch_bounds__(128) k_faces(Params p, const GridInfo *__restr
             Fo[3] = A[0] * rhoSol * vLab[1] * vSol[0] + A[1] * (rhoSol * vLab[1] * vSol[1] + PSol) + A[2] * rhoSol * vLab[1] * vSol[2];
             Fo[4] = A[0] * rhoSol * vLab[2] * vSol[0] + A[1] * rhoSol * vLab[2] * vSol[1] + A[2] * (rhoSol * vLab[2] * vSol[2] + PSol);
             const double ek = rhoSol * .5 * ((vLab[0] * vLab[0] + vLab[1] * vLab[1]) + vLab[2] * vLab[2]);
-            const double pe = PSol / (gamma - 1.);
             Fo[1] = A[0] * (vSol[0] * (pe + ek) + PSol * vLab[0]) + A[1] * (vSol[1] * (pe + ek) + PSol * vLab[1])
                   + A[2] * (vSol[2] * (pe + ek) + PSol * vLab[2]);
         }
@@ -1123,17 +1110,23 @@ void launch_step(StepArgs &a) {
     tock(KT_DT);
 
     tick(KT_GRAD);
-    k_gradients<D><<<blocksN, T, 0, s>>>(p, a.grid, a.prim, a.geo, a.nbr, a.ww, a.noi, a.noiImg, a.grad, a.gradRaw);
+    k_gradients<D><<<blocksN, T, 0, s>>>(p, a.grid, a.prim, a.geo, a.nbr, a.ww, a.noi, a.noiImg, a.grad, a.gradRaw,
+                                         a.psi);
     tock(KT_GRAD);
 
     tick(KT_LINK);
     exclusive_scan(a.faceCnt, p.n, a.faceOff, a.scanTiles, a.scanTotal, s);
+    cudaMemsetAsync(a.faces, 0xff, sizeof(FaceRef) * a.faces_cap, s);
     k_link<<<blocksN, T, 0, s>>>(p, a.nbr, a.noi, a.noiImg, a.faceOff, a.faceOf, a.faces, a.status);
     tock(KT_LINK);
 
     tick(KT_FACES);
-    k_faces<D><<<a.face_blocks, T, 0, s>>>(p, a.grid, a.prim, a.geo, a.grad, a.nbr, a.ww, a.faceOff + p.n, a.faces,
-                                          a.dt, a.Fface, a.newtonSum, a.status);
+    if (a.root5)
+        k_faces<D, true><<<a.face_blocks, T, 0, s>>>(p, a.grid, a.prim, a.geo, a.grad, a.nbr, a.psi, a.faceOff + p.n,
+                                                     a.faces, a.dt, a.Fface, a.newtonSum, a.status);
+    else
+        k_faces<D, false><<<a.face_blocks, T, 0, s>>>(p, a.grid, a.prim, a.geo, a.grad, a.nbr, a.psi, a.faceOff + p.n,
+                                                      a.faces, a.dt, a.Fface, a.newtonSum, a.status);
     tock(KT_FACES);
 
     tick(KT_UPDATE);

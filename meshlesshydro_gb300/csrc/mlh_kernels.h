@@ -14,6 +14,8 @@ struct StepArgs {
     Params p;
     cudaStream_t stream;
     int face_blocks;
+    int root5;              // gamma = 5/3 fast path of the Riemann solver
+    size_t faces_cap;
     double dt_max;
     // state (structure of arrays)
     double *x, *y, *z, *vx, *vy, *vz, *m, *u;
@@ -24,7 +26,7 @@ struct StepArgs {
     int *cell, *cellCount, *cellStart, *cellFill, *cellList;
     // neighbours
     uint32_t *nbr;
-    double *rr, *ww;
+    double *rr, *ww, *psi;
     int *noi, *noiImg, *faceCnt, *faceOff, *faceOf;
     FaceRef *faces;
     // per particle

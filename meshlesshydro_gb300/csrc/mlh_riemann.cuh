@@ -13,8 +13,11 @@
 namespace mlh {
 
 struct RiemannConsts {
-    double gamma, g1, g2, g3, g4, g5, g6, g7, inv_gamma, tol;
+    double gamma, g1, g2, g3, g4, g5, g6, g7, inv_gamma, inv_gm1, tol;
     int max_iter;
+    // gamma = 5/3: g1 = 1/5, g3 = 5, g4 = 3 and 1/gamma = 3 g1, so every
+    // power in the solver is a fifth root or an integer power
+    int root5;
 };
 
 __host__ __device__ inline RiemannConsts make_riemann_consts(double gamma, double tol, int max_iter) {
@@ -28,8 +31,10 @@ __host__ __device__ inline RiemannConsts make_riemann_consts(double gamma, doubl
     c.g6 = (gamma - 1.) / (gamma + 1.);
     c.g7 = (gamma - 1.) / 2.;
     c.inv_gamma = 1. / gamma;
+    c.inv_gm1 = 1. / (gamma - 1.);
     c.tol = tol;
     c.max_iter = max_iter;
+    c.root5 = (fabs(1. / c.g1 - 5.) < 1e-12 && fabs(c.g4 - 3.) < 1e-12) ? 1 : 0;
     return c;
 }
 
@@ -151,6 +156,187 @@ __device__ inline RiemannResult riemann_exact(const RiemannConsts &c, double rho
         res.flag = 1;
     }
     res.rho = rho; res.u = u; res.p = p;
+    return res;
+}
+
+// ---------------------------------------------------------------- fast path
+
+// x^(-1/5): single-precision seed (relative error ~1e-7) refined by two
+// Newton steps y <- y + y (1 - x y^5) / 5, whose error contracts as 3 e^2, so
+// the result is within a few ulp of the correctly rounded value.  Values
+// outside the float range go through pow.
+__device__ __forceinline__ double rroot5(double x) {
+    if (!(x > 1e-30 && x < 1e30)) return pow(x, -0.2);
+    float xf = (float)x;
+    double y = (double)exp2f(-0.2f * __log2f(xf));
+#pragma unroll
+    for (int k = 0; k < 2; ++k) {
+        double y2 = y * y;
+        double y5 = y2 * y2 * y;
+        double r = fma(-x, y5, 1.);
+        y = fma(y * 0.2, r, y);
+    }
+    return y;
+}
+// x^(1/5) = x * (x^(-1/5))^4
+__device__ __forceinline__ double root5(double x) {
+    double y = rroot5(x);
+    double y2 = y * y;
+    return x * (y2 * y2);
+}
+
+struct RiemannSide {
+    double rho, u, p, c, invp, C, ak, bk, g4c;
+};
+
+__device__ __forceinline__ RiemannSide make_side(const RiemannConsts &k, double rho, double u, double p) {
+    RiemannSide s;
+    s.rho = rho; s.u = u; s.p = p;
+    s.c = sqrt(k.gamma * p / rho);
+    s.invp = 1. / p;
+    s.C = p / (rho * s.c);       // f' = (p/pK)^g1 * pK / (p rhoK cK)
+    s.ak = k.g5 / rho;
+    s.bk = k.g6 * p;
+    s.g4c = k.g4 * s.c;
+    return s;
+}
+
+// f_K, f_K' at p (1/p given); q = (p/pK)^g1 on the rarefaction branch
+__device__ __forceinline__ void pressure_fn5(const RiemannSide &s, double p, double invp, double &f, double &fd,
+                                             double &q, bool &rare) {
+    if (p <= s.p) {
+        q = root5(p * s.invp);
+        f = s.g4c * (q - 1.);
+        fd = q * s.C * invp;
+        rare = true;
+    } else {
+        double t = 1. / (s.bk + p);
+        double qrt = sqrt(s.ak * t);
+        f = (p - s.p) * qrt;
+        fd = (1. - .5 * (p - s.p) * t) * qrt;
+        q = 0.;
+        rare = false;
+    }
+}
+
+// Same solution as riemann_exact for gamma = 5/3 with cheaper arithmetic:
+// fifth roots instead of pow, integer powers for g3, g4 and 1/gamma, one
+// reciprocal of p per Newton step, and f_K(p*) from the last Newton
+// evaluation plus its derivative times the final (<= tol relative) step,
+// which differs from re-evaluating f at p* by O(tol^2) relative.
+__device__ inline RiemannResult riemann_exact5(const RiemannConsts &k, double rhoL, double uL, double pL,
+                                               double rhoR, double uR, double pR, double guess = -1.) {
+    RiemannResult res;
+    const RiemannSide L = make_side(k, rhoL, uL, pL), R = make_side(k, rhoR, uR, pR);
+    if (k.g4 * (L.c + R.c) <= uR - uL) {
+        res.rho = 0.; res.u = 0.; res.p = 0.; res.flag = 0; res.iters = 0;
+        return res;
+    }
+    const double du = uR - uL;
+    const double pfloor = 1e-12 * (pL > pR ? pL : pR);
+    double p0;
+    bool tried_guess = guess > 0.;
+    if (tried_guess) p0 = guess;
+    else {
+        double num = L.c + R.c - k.g7 * du;
+        double den = L.c * rroot5(pL) + R.c * rroot5(pR);
+        double t = num / den;
+        double t2 = t * t;
+        p0 = t2 * t2 * t;
+    }
+    double p, fLs = 0., fRs = 0., qLs = -1., qRs = -1.;
+    int iters = -1, extra = 0;
+    for (int attempt = 0; attempt < 2 && iters < 0; ++attempt) {
+        if (attempt == 1) {
+            if (!tried_guess) break;
+            extra = k.max_iter;
+            double num = L.c + R.c - k.g7 * du;
+            double den = L.c * rroot5(pL) + R.c * rroot5(pR);
+            double t = num / den;
+            double t2 = t * t;
+            p0 = t2 * t2 * t;
+        }
+        p = p0 > pfloor ? p0 : pfloor;
+        for (int it = 1; it <= k.max_iter; ++it) {
+            double invp = 1. / p;
+            double fL, fdL, qL, fR, fdR, qR;
+            bool rL, rR;
+            pressure_fn5(L, p, invp, fL, fdL, qL, rL);
+            pressure_fn5(R, p, invp, fR, fdR, qR, rR);
+            double pnew = p - (fL + fR + du) / (fdL + fdR);
+            if (!(pnew > 0.)) pnew = pfloor;
+            double dp = pnew - p;
+            if (2. * fabs(dp) <= k.tol * (pnew + p)) {
+                fLs = fL + fdL * dp;
+                fRs = fR + fdR * dp;
+                double rel = dp * invp;
+                qLs = rL ? qL + qL * (k.g1 * rel) : -1.;
+                qRs = rR ? qR + qR * (k.g1 * rel) : -1.;
+                p = pnew;
+                iters = it;
+                break;
+            }
+            p = pnew;
+        }
+    }
+    const double pstar = p;
+    if (iters < 0) {
+        double invp = 1. / pstar, fdL, fdR, qL, qR;
+        bool rL, rR;
+        pressure_fn5(L, pstar, invp, fLs, fdL, qL, rL);
+        pressure_fn5(R, pstar, invp, fRs, fdR, qR, rR);
+        qLs = rL ? qL : -1.;
+        qRs = rR ? qR : -1.;
+        res.iters = -1;
+    } else {
+        res.iters = iters + extra;
+    }
+    const double ustar = .5 * (uL + uR) + .5 * (fRs - fLs);
+    double rho, u, pp;
+    if (0. <= ustar) {
+        if (pstar <= pL) {
+            double shl = uL - L.c;
+            if (0. <= shl) { rho = rhoL; u = uL; pp = pL; }
+            else {
+                double q = qLs >= 0. ? qLs : root5(pstar * L.invp);
+                double stl = ustar - L.c * q;
+                if (0. > stl) { rho = rhoL * (q * q * q); u = ustar; pp = pstar; }
+                else {
+                    double cf = k.g5 * (L.c + k.g7 * uL);
+                    double r = cf / L.c, r3 = r * r * r;
+                    u = cf; rho = rhoL * r3; pp = pL * (r3 * r * r);
+                }
+            }
+        } else {
+            double pml = pstar * L.invp;
+            double sl = uL - L.c * sqrt(k.g2 * pml + k.g1);
+            if (0. <= sl) { rho = rhoL; u = uL; pp = pL; }
+            else { rho = rhoL * (pml + k.g6) / (pml * k.g6 + 1.); u = ustar; pp = pstar; }
+        }
+        res.flag = -1;
+    } else {
+        if (pstar > pR) {
+            double pmr = pstar * R.invp;
+            double sr = uR + R.c * sqrt(k.g2 * pmr + k.g1);
+            if (0. >= sr) { rho = rhoR; u = uR; pp = pR; }
+            else { rho = rhoR * (pmr + k.g6) / (pmr * k.g6 + 1.); u = ustar; pp = pstar; }
+        } else {
+            double shr = uR + R.c;
+            if (0. >= shr) { rho = rhoR; u = uR; pp = pR; }
+            else {
+                double q = qRs >= 0. ? qRs : root5(pstar * R.invp);
+                double str = ustar + R.c * q;
+                if (0. <= str) { rho = rhoR * (q * q * q); u = ustar; pp = pstar; }
+                else {
+                    double cf = k.g5 * (R.c - k.g7 * uR);
+                    double r = cf / R.c, r3 = r * r * r;
+                    u = -cf; rho = rhoR * r3; pp = pR * (r3 * r * r);
+                }
+            }
+        }
+        res.flag = 1;
+    }
+    res.rho = rho; res.u = u; res.p = pp;
     return res;
 }
 
