@@ -710,10 +710,11 @@ __global__ void __launch_bounds__(128) k_link(Params p, const uint32_t *__restri
 // ------------------------------------------------------------------ faces
 
 // Particles::pairwiseLimiter, Particles.cpp:1735-1785.
+// `ratio` = |x_ij - x_i| / |x_j - x_i|.
 __device__ __forceinline__ double pairwise_limiter(const Params &p, double phi0, double phi_i, double phi_j,
-                                                   double xijxi_abs, double xjxi_abs) {
+                                                   double ratio) {
     double phi_ = phi_i;
-    double phi_ij = phi_i + xijxi_abs / xjxi_abs * (phi_j - phi_i);
+    double phi_ij = phi_i + ratio * (phi_j - phi_i);
     double phiMin, phiMax;
     if (phi_i < phi_j) { phiMin = phi_i; phiMax = phi_j; }
     else { phiMin = phi_j; phiMax = phi_i; }
@@ -854,20 +855,28 @@ __global__ void __launch_bounds__(128) k_faces(Params p, const GridInfo *__restr
         R[3] += dotD<D>(Gi + 6, xijxi); L[3] += dotD<D>(Gj + 6, xijxj);
         if (D == 3) { R[4] += dotD<D>(Gi + 9, xijxi); L[4] += dotD<D>(Gj + 9, xijxj); }
         if (p.pairwise && (!img || p.img_pw)) {
-            double xijxi_abs = 0., xijxj_abs = 0., xjxi_abs = 0.;
+            double ri, rj;   // |x_ij - x_i| / |x_j - x_i| and |x_ij - x_j| / |x_j - x_i|
+            if (p.foqp) {
+                // x_ij - x_i = (x_j - x_i) / 2 exactly, so both norms are
+                // exactly half of |x_j - x_i| (scaling by 1/2 and 1/4 is exact)
+                // and both quotients are exactly 0.5
+                ri = .5; rj = .5;
+            } else {
+                double xijxi_abs = 0., xijxj_abs = 0., xjxi_abs = 0.;
 #pragma unroll
-            for (int a = 0; a < D; ++a) {
-                xijxi_abs += xijxi[a] * xijxi[a];
-                xijxj_abs += xijxj[a] * xijxj[a];
-                xjxi_abs += xjxi[a] * xjxi[a];
+                for (int a = 0; a < D; ++a) {
+                    xijxi_abs += xijxi[a] * xijxi[a];
+                    xijxj_abs += xijxj[a] * xijxj[a];
+                    xjxi_abs += xjxi[a] * xjxi[a];
+                }
+                xjxi_abs = sqrt(xjxi_abs);
+                ri = sqrt(xijxi_abs) / xjxi_abs;
+                rj = sqrt(xijxj_abs) / xjxi_abs;
             }
-            xijxi_abs = sqrt(xijxi_abs);
-            xijxj_abs = sqrt(xijxj_abs);
-            xjxi_abs = sqrt(xjxi_abs);
 #pragma unroll
             for (int k = 0; k < NV; ++k) {
-                R[k] = pairwise_limiter(p, R[k], Rb[k], Lb[k], xijxi_abs, xjxi_abs);
-                L[k] = pairwise_limiter(p, L[k], Lb[k], Rb[k], xijxj_abs, xjxi_abs);
+                R[k] = pairwise_limiter(p, R[k], Rb[k], Lb[k], ri);
+                L[k] = pairwise_limiter(p, L[k], Lb[k], Rb[k], rj);
             }
         }
         {

@@ -192,10 +192,11 @@ struct RiemannSide {
 __device__ __forceinline__ RiemannSide make_side(const RiemannConsts &k, double rho, double u, double p) {
     RiemannSide s;
     s.rho = rho; s.u = u; s.p = p;
-    s.c = sqrt(k.gamma * p / rho);
+    const double irho = 1. / rho;
+    s.c = sqrt(k.gamma * p * irho);
     s.invp = 1. / p;
-    s.C = p / (rho * s.c);       // f' = (p/pK)^g1 * pK / (p rhoK cK)
-    s.ak = k.g5 / rho;
+    s.C = s.c * k.inv_gamma;     // pK / (rhoK cK) = cK / gamma: f' = (p/pK)^g1 C / p
+    s.ak = k.g5 * irho;
     s.bk = k.g6 * p;
     s.g4c = k.g4 * s.c;
     return s;
