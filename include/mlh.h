@@ -137,6 +137,31 @@ void mlh_reset_kernel_times(mlh_ctx *ctx);
  * code); used by bench.py. */
 int mlh_probe_fp64_tflops(double seconds, double *tflops);
 
+/* Largest particle count mlh_grid_bounds_noalloc accepts (29-bit indices). */
+#define MLH_NOALLOC_MAX_PARTICLES ((1 << 29) - 1)
+
+/* Search grid of one step computed without allocating any memory: for
+ * callers that cannot call cudaMalloc (code running during CUDA graph
+ * capture, frameworks that own all device memory through their own pool, loops
+ * that must not allocate after start-up).  No counterpart in the reference:
+ * it computes what Particles::getDomainLimits + Domain::createGrid compute at
+ * the start of a non-periodic step (the box itself when `periodic`), as
+ * mlh_step does, from caller-owned device arrays x, y (, z) of n particles.
+ * Writes 9 doubles to the device buffer grid_out: lo[3], hi[3], cells[3]
+ * (unused axes 0).  box_lo/box_hi are host arrays, read only when periodic.
+ * stream: a cudaStream_t, or NULL for the default stream; the call waits for
+ * it to finish.
+ * Scratch: a fixed 16 KiB static device array that every GPU loading the
+ * library keeps until exit; its device address is looked up on the first
+ * call on each device, so make that first call before any stream capture.
+ * Every call shares the same scratch: calls that overlap on the GPU (from
+ * several host threads or streams at once) race and must be serialised by
+ * the caller.  n > MLH_NOALLOC_MAX_PARTICLES returns MLH_ERR_CAPACITY
+ * (message in mlh_last_error()). */
+int mlh_grid_bounds_noalloc(int dim, int periodic, int n, const double *x, const double *y, const double *z,
+                            const double *box_lo, const double *box_hi, double kernel_size, double *grid_out,
+                            void *stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -36,6 +36,11 @@ cudaError_t dalloc(T **p, size_t count) {
 
 }  // namespace
 
+namespace mlh {
+// message for mlh_last_error from other translation units of the library
+void set_last_error(const char *msg) { g_last_error = msg ? msg : ""; }
+}  // namespace mlh
+
 struct mlh_ctx {
     mlh_config cfg;
     Params p;

@@ -142,7 +142,7 @@ void exclusive_scan(const int *in, int n, int *out, int *tile_buf, int *total, c
 // x_0..x_{i-1}, or DBL_MIN.  The partial pass computes min over all i and max
 // over i >= 1; the final pass falls back to the sequential rule whenever x_0 is
 // above every other particle (the only case where the two differ).
-constexpr int BOUNDS_BLOCKS = 304, BOUNDS_T = 256;
+constexpr int BOUNDS_T = 256;
 
 template <int D>
 __global__ void k_bounds_partial(const double *__restrict__ x, const double *__restrict__ y,
@@ -1142,6 +1142,17 @@ void launch_step(StepArgs &a) {
     k_update<D><<<blocksN, T, 0, s>>>(p, a.grid, a.noi, a.noiImg, a.faceOf, a.Fface, a.dt, a.x, a.y, a.z, a.vx, a.vy,
                                       a.vz, a.m, a.u, a.posf, a.fluxSums, a.simTime, a.stepsDone, a.status);
     tock(KT_UPDATE);
+}
+
+void launch_grid_bounds(const double *x, const double *y, const double *z, const Params &p, double *partials,
+                        GridInfo *grid, unsigned *status, cudaStream_t s) {
+    if (p.dim == 2) {
+        k_bounds_partial<2><<<BOUNDS_BLOCKS, BOUNDS_T, 0, s>>>(x, y, z, p.n, partials);
+        k_bounds_final<2><<<1, 32, 0, s>>>(x, y, z, partials, BOUNDS_BLOCKS, p, grid, status);
+    } else {
+        k_bounds_partial<3><<<BOUNDS_BLOCKS, BOUNDS_T, 0, s>>>(x, y, z, p.n, partials);
+        k_bounds_final<3><<<1, 32, 0, s>>>(x, y, z, partials, BOUNDS_BLOCKS, p, grid, status);
+    }
 }
 
 void step(StepArgs &a) {

@@ -45,9 +45,17 @@ struct StepArgs {
     void *timer_ctx;
 };
 
+// blocks of the bounding-box reduction; its scratch holds 6 doubles per block
+constexpr int BOUNDS_BLOCKS = 304;
+
 void step(StepArgs &a);
+// Particles::getDomainLimits + Domain::createGrid alone: per-block partial
+// minima/maxima in `partials` (BOUNDS_BLOCKS * 6 doubles), result in `grid`.
+void launch_grid_bounds(const double *x, const double *y, const double *z, const Params &p, double *partials,
+                        GridInfo *grid, unsigned *status, cudaStream_t s);
 void pack_posf(const double *x, const double *y, const double *z, int n, int dim, float4 *posf, cudaStream_t s);
 void exclusive_scan(const int *in, int n, int *out, int *tile_buf, int *total, cudaStream_t s);
 const char *kernel_timer_name(int id);
+void set_last_error(const char *msg);
 
 }  // namespace mlh

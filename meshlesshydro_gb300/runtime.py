@@ -48,7 +48,8 @@ class StepStats(ctypes.Structure):
 
 EXPORTS = ["mlh_abi_version", "mlh_last_error", "mlh_create", "mlh_destroy", "mlh_set_fields",
            "mlh_get_fields", "mlh_step", "mlh_stage_array", "mlh_set_kernel_timing",
-           "mlh_kernel_times", "mlh_reset_kernel_times", "mlh_probe_fp64_tflops"]
+           "mlh_kernel_times", "mlh_reset_kernel_times", "mlh_probe_fp64_tflops",
+           "mlh_grid_bounds_noalloc"]
 
 _lib = None
 
@@ -83,6 +84,11 @@ def load(path: str = LIB_PATH):
     L.mlh_reset_kernel_times.argtypes = [vp]
     L.mlh_probe_fp64_tflops.argtypes = [ctypes.c_double, ctypes.POINTER(ctypes.c_double)]
     L.mlh_probe_fp64_tflops.restype = ctypes.c_int
+    dp = ctypes.c_void_p
+    L.mlh_grid_bounds_noalloc.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_int, dp, dp, dp,
+                                          ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_double),
+                                          ctypes.c_double, dp, dp]
+    L.mlh_grid_bounds_noalloc.restype = ctypes.c_int
     _lib = L
     return L
 
