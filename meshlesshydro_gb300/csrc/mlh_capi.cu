@@ -164,7 +164,9 @@ StepArgs make_args(mlh_ctx *c, double dt_max) {
     a.p = c->p;
     a.stream = c->stream;
     a.face_blocks = c->sm_count * 8;
+    a.sm_count = c->sm_count;
     a.faces_cap = c->faces_cap;
+    a.p.faces_cap = c->faces_cap > 0x7fffffff ? 0x7fffffff : (int)c->faces_cap;
     a.root5 = make_riemann_consts(c->p.gamma, c->p.rtol, c->p.rmaxit).root5;
     a.dt_max = dt_max;
     a.x = c->x; a.y = c->y; a.z = c->z; a.vx = c->vx; a.vy = c->vy; a.vz = c->vz; a.m = c->m; a.u = c->u;

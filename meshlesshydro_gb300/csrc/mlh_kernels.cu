@@ -281,13 +281,38 @@ __global__ void k_sort_cells(const GridInfo *__restrict__ gridp, const int *__re
 // Domain::getNeighborCells (Domain.cpp:83-118, x outer, z inner), and the
 // periodic images of Particles::ghostNNS (Particles.cpp:2237-2260) through
 // wrapped stencil cells, appended after the real neighbours in parent order.
-// A single-precision test with a conservative bound rejects most candidates;
-// the accepted ones are tested in FP64 exactly as the reference does
-// (d^2 = (dx*dx + dy*dy) + dz*dz < h*h, no fused multiply-add).
 // Then Particles::compDensity/compOmega (Particles.cpp:1151-1184, 2262-2290)
 // and compPressure (:1272-1288) for the particle.
+//
+// One warp per particle.  Phase 1: the lanes walk the concatenated member
+// lists of the stencil cells and reject candidates with a single-precision
+// distance test against a bound slightly above h^2; the survivors are
+// compacted with a ballot into a per-warp shared list, keeping the stencil
+// order.  Phase 2: the lanes take the survivors 32 at a time and apply the
+// reference's FP64 test exactly (d^2 = (dx*dx + dy*dy) + dz*dz < h*h, no fused
+// multiply-add), compute r and W(r), and append real neighbours (in order) to
+// the slot list and images to a shared list, which is then placed behind the
+// real neighbours sorted by parent index.
+constexpr int NNS_WARPS = 8;
+
+struct NnsCells {
+    int excl[27], start[27];
+    unsigned wrap[27];
+    int shift[27][3];   // stencil offset of a wrapped axis (-1 or +1), else 0
+};
+
+// shared memory of k_neighbours: NNS_WARPS NnsCells, then per warp the
+// candidate list (K + 32 uint32), image r and W (K doubles each) and image
+// entries (K uint32), each rounded up to 16 bytes
+__host__ __device__ constexpr size_t nns_cells_bytes() {
+    return (sizeof(NnsCells) * NNS_WARPS + 15) / 16 * 16;
+}
+__host__ __device__ constexpr size_t nns_warp_bytes(int K) {
+    return ((size_t)(K + 32) * 4 + 15) / 16 * 16 + (size_t)K * 16 + ((size_t)K * 4 + 15) / 16 * 16;
+}
+
 template <int D>
-__global__ void __launch_bounds__(128) k_neighbours(
+__global__ void __launch_bounds__(NNS_WARPS * 32) k_neighbours(
     Params p, const GridInfo *__restrict__ gridp, const double *__restrict__ x, const double *__restrict__ y,
     const double *__restrict__ z, const float4 *__restrict__ posf, const double *__restrict__ vx,
     const double *__restrict__ vy, const double *__restrict__ vz, const double *__restrict__ m,
@@ -295,141 +320,216 @@ __global__ void __launch_bounds__(128) k_neighbours(
     const int *__restrict__ cellList, uint32_t *__restrict__ nbr, double *__restrict__ rr,
     double *__restrict__ ww, int *__restrict__ noi, int *__restrict__ noiImg, int *__restrict__ faceCnt,
     Prim *__restrict__ prim, Geo *__restrict__ geo, unsigned *__restrict__ status) {
+    constexpr int NC = D == 3 ? 27 : 9;
+    const int K = p.K;
+    const int CAP = K + 32;
+    extern __shared__ __align__(16) unsigned char nns_smem[];
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const unsigned lt_mask = (1u << lane) - 1u;
+    // per-warp shared areas; every sub-array starts on a 16-byte boundary
+    // whatever K is (see nns_warp_bytes)
+    NnsCells *cs = reinterpret_cast<NnsCells *>(nns_smem) + warp;
+    const size_t cand_bytes = ((size_t)CAP * 4 + 15) / 16 * 16;
+    unsigned char *wbase = nns_smem + nns_cells_bytes() + (size_t)warp * nns_warp_bytes(K);
+    uint32_t *cand = reinterpret_cast<uint32_t *>(wbase);
+    double *imgR = reinterpret_cast<double *>(wbase + cand_bytes);
+    double *imgW = imgR + K;
+    uint32_t *imgE = reinterpret_cast<uint32_t *>(imgW + K);
+
     const GridInfo g = *gridp;
     const double *X[3] = {x, y, z};
-    const int K = p.K;
-    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < p.n; i += gridDim.x * blockDim.x) {
-        double xi[3] = {0., 0., 0.};
+    float Lf[3];
 #pragma unroll
-        for (int a = 0; a < D; ++a) xi[a] = X[a][i];
-        const float4 fi = posf[i];
+    for (int a = 0; a < 3; ++a) Lf[a] = (float)(g.hi[a] - g.lo[a]);
+    const int gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int nw = (gridDim.x * blockDim.x) >> 5;
+    for (int i = gw; i < p.n; i += nw) {
         const int ic = cell[i];
         const int ix = ic % g.cells[0];
         const int iy = (ic / g.cells[0]) % g.cells[1];
         const int iz = D == 3 ? ic / (g.cells[0] * g.cells[1]) : 0;
-        const size_t base = (size_t)i * K;
-        int nr = 0, ni = 0;
-        bool overflow = false;
-        for (int k = ix - 1; k <= ix + 1; ++k)
-            for (int l = iy - 1; l <= iy + 1; ++l)
-                for (int mm = (D == 3 ? iz - 1 : 0); mm <= (D == 3 ? iz + 1 : 0); ++mm) {
-                    int cc[3] = {k, l, mm};
-                    unsigned wrap = 0;
-                    bool skip = false;
+        // --- stencil cells in the reference's order, lane k holds cell k
+        int cnt = 0, start = 0;
+        unsigned wrap = 0;
+        int sh[3] = {0, 0, 0};
+        if (lane < NC) {
+            int off[3] = {D == 3 ? lane / 9 - 1 : lane / 3 - 1, D == 3 ? (lane / 3) % 3 - 1 : lane % 3 - 1,
+                          D == 3 ? lane % 3 - 1 : 0};
+            int cc[3] = {ix + off[0], iy + off[1], iz + off[2]};
+            bool skip = false;
 #pragma unroll
-                    for (int a = 0; a < D; ++a) {
-                        if (cc[a] < 0 || cc[a] >= g.cells[a]) {
-                            if (!p.periodic) skip = true;
-                            cc[a] = cc[a] < 0 ? cc[a] + g.cells[a] : cc[a] - g.cells[a];
-                            wrap |= 1u << a;
-                        }
-                    }
-                    if (skip) continue;
-                    int c = cc[0] + cc[1] * g.cells[0] + (D == 3 ? cc[2] * g.cells[0] * g.cells[1] : 0);
-                    int b = cellStart[c], e = cellStart[c + 1];
-                    for (int t = b; t < e; ++t) {
-                        int j = cellList[t];
-                        if (!wrap) {
-                            if (j == i) continue;
-                            float4 fj = posf[j];
-                            float dx = fj.x - fi.x, dy = fj.y - fi.y, dz = fj.z - fi.z;
-                            float d2f = dx * dx + dy * dy + (D == 3 ? dz * dz : 0.f);
-                            if (d2f > p.hsq_f) continue;
-                            double ex = __dsub_rn(X[0][j], xi[0]), ey = __dsub_rn(X[1][j], xi[1]);
-                            double d2 = __dadd_rn(__dmul_rn(ex, ex), __dmul_rn(ey, ey));
-                            if (D == 3) { double ez = __dsub_rn(X[2][j], xi[2]); d2 = __dadd_rn(d2, __dmul_rn(ez, ez)); }
-                            if (d2 < p.hsq) {
-                                if (nr + ni < K) {
-                                    nbr[base + nr] = (uint32_t)j;
-                                    rr[base + nr] = sqrt(d2);
-                                } else overflow = true;
-                                ++nr;
-                            }
-                        } else {
-                            double xj[3];
-                            bool ok = true;
-#pragma unroll
-                            for (int a = 0; a < D; ++a) {
-                                xj[a] = X[a][j];
-                                if (wrap & (1u << a)) {
-                                    if (in_band(xj[a], g.lo[a], g.hi[a], p.h)) xj[a] = image_coord(xj[a], g.lo[a], g.hi[a], p.h);
-                                    else ok = false;
-                                }
-                            }
-                            if (!ok) continue;
-                            double ex = __dsub_rn(xj[0], xi[0]), ey = __dsub_rn(xj[1], xi[1]);
-                            double d2 = __dadd_rn(__dmul_rn(ex, ex), __dmul_rn(ey, ey));
-                            if (D == 3) { double ez = __dsub_rn(xj[2], xi[2]); d2 = __dadd_rn(d2, __dmul_rn(ez, ez)); }
-                            if (d2 < p.hsq) {
-                                if (nr + ni < K) {
-                                    // images grow downwards from the end of the slot range
-                                    nbr[base + K - 1 - ni] = (uint32_t)j | (wrap << IMG_SHIFT);
-                                    rr[base + K - 1 - ni] = sqrt(d2);
-                                } else overflow = true;
-                                ++ni;
-                            }
-                        }
-                    }
+            for (int a = 0; a < D; ++a) {
+                if (cc[a] < 0 || cc[a] >= g.cells[a]) {
+                    if (!p.periodic) skip = true;
+                    cc[a] = cc[a] < 0 ? cc[a] + g.cells[a] : cc[a] - g.cells[a];
+                    wrap |= 1u << a;
+                    sh[a] = off[a];
                 }
-        if (overflow || nr + ni > K) {
-            flag(status, ST_NGB_OVERFLOW);
-            if (nr > K) nr = K;
-            ni = K - nr < ni ? K - nr : ni;
-        }
-        // images sit in [K - ni, K) in reverse discovery order: sort them there
-        // by parent index, then move the block down behind the real neighbours
-        // (destination below source, so a forward copy is safe)
-        {
-            const int b0 = K - ni;
-            for (int k = b0 + 1; k < K; ++k) {
-                const uint32_t e = nbr[base + k];
-                const double r = rr[base + k];
-                int t = k - 1;
-                while (t >= b0 && (nbr[base + t] & IDX_MASK) > (e & IDX_MASK)) {
-                    nbr[base + t + 1] = nbr[base + t];
-                    rr[base + t + 1] = rr[base + t];
-                    --t;
-                }
-                nbr[base + t + 1] = e;
-                rr[base + t + 1] = r;
             }
-            if (b0 != nr)
-                for (int t = 0; t < ni; ++t) {
-                    nbr[base + nr + t] = nbr[base + b0 + t];
-                    rr[base + nr + t] = rr[base + b0 + t];
+            if (!skip) {
+                int c = cc[0] + cc[1] * g.cells[0] + (D == 3 ? cc[2] * g.cells[0] * g.cells[1] : 0);
+                start = cellStart[c];
+                cnt = cellStart[c + 1] - start;
+            }
+        }
+        int incl = cnt;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            int t = __shfl_up_sync(0xffffffffu, incl, o);
+            if (lane >= o) incl += t;
+        }
+        const int total = __shfl_sync(0xffffffffu, incl, 31);
+        if (lane < NC) {
+            cs->excl[lane] = incl - cnt;
+            cs->start[lane] = start;
+            cs->wrap[lane] = wrap;
+            cs->shift[lane][0] = sh[0]; cs->shift[lane][1] = sh[1]; cs->shift[lane][2] = sh[2];
+        }
+        __syncwarp();
+        const float4 fi = posf[i];
+        // --- phase 1: single-precision pre-filter, ordered compaction
+        int ncand = 0;
+        bool overflow = false;
+        for (int t0 = 0; t0 < total; t0 += 32) {
+            const int t = t0 + lane;
+            bool pass = false;
+            uint32_t ent = 0;
+            if (t < total) {
+                int k = 0;
+                for (int kk = 1; kk < NC; ++kk)
+                    if (cs->excl[kk] <= t) k = kk;
+                // empty cells share their offset with the next one: take the
+                // last cell whose range contains t
+                const int j = cellList[cs->start[k] + (t - cs->excl[k])];
+                const unsigned wr = cs->wrap[k];
+                if (wr || j != i) {
+                    float4 fj = posf[j];
+                    float dx = fj.x - fi.x, dy = fj.y - fi.y, dz = fj.z - fi.z;
+                    if (wr) {
+                        dx += (float)cs->shift[k][0] * Lf[0];
+                        dy += (float)cs->shift[k][1] * Lf[1];
+                        if (D == 3) dz += (float)cs->shift[k][2] * Lf[2];
+                    }
+                    float d2f = dx * dx + dy * dy + (D == 3 ? dz * dz : 0.f);
+                    pass = d2f <= p.hsq_f;
+                    ent = (uint32_t)j | (wr << IMG_SHIFT);
                 }
+            }
+            const unsigned bal = __ballot_sync(0xffffffffu, pass);
+            if (pass) {
+                const int pos = ncand + __popc(bal & lt_mask);
+                if (pos < CAP) cand[pos] = ent;
+            }
+            ncand += __popc(bal);
         }
-        const int tot = nr + ni;
-        if (tot == 0) flag(status, ST_NO_NEIGHBOUR);
-        int fc = 0;
-        for (int s = 0; s < tot; ++s) {
-            ww[base + s] = kernelW(rr[base + s], p);
-            if ((int)(nbr[base + s] & IDX_MASK) > i) ++fc;
+        if (ncand > CAP) { overflow = true; ncand = CAP; }
+        __syncwarp();
+        // --- phase 2: exact FP64 test, r, W
+        int nr = 0, ni = 0, fc = 0;
+        double wsumR = 0., wsumI = 0.;
+        const size_t base = (size_t)i * K;
+        double xi[3] = {0., 0., 0.};
+#pragma unroll
+        for (int a = 0; a < D; ++a) xi[a] = X[a][i];
+        for (int t0 = 0; t0 < ncand; t0 += 32) {
+            const int t = t0 + lane;
+            bool pass = false, img = false;
+            uint32_t e = 0;
+            double r = 0., w = 0.;
+            if (t < ncand) {
+                e = cand[t];
+                const int j = (int)(e & IDX_MASK);
+                const unsigned wr = e >> IMG_SHIFT;
+                img = wr != 0;
+                double xj[3];
+                bool ok = true;
+#pragma unroll
+                for (int a = 0; a < D; ++a) {
+                    xj[a] = X[a][j];
+                    if (wr & (1u << a)) {
+                        if (in_band(xj[a], g.lo[a], g.hi[a], p.h)) xj[a] = image_coord(xj[a], g.lo[a], g.hi[a], p.h);
+                        else ok = false;
+                    }
+                }
+                if (ok) {
+                    double ex = __dsub_rn(xj[0], xi[0]), ey = __dsub_rn(xj[1], xi[1]);
+                    double d2 = __dadd_rn(__dmul_rn(ex, ex), __dmul_rn(ey, ey));
+                    if (D == 3) { double ez = __dsub_rn(xj[2], xi[2]); d2 = __dadd_rn(d2, __dmul_rn(ez, ez)); }
+                    pass = d2 < p.hsq;
+                    if (pass) {
+                        r = sqrt(d2);
+                        w = kernelW(r, p);
+                    }
+                }
+            }
+            const unsigned balR = __ballot_sync(0xffffffffu, pass && !img);
+            const unsigned balI = __ballot_sync(0xffffffffu, pass && img);
+            if (pass && !img) {
+                const int pos = nr + __popc(balR & lt_mask);
+                if (pos < K) { nbr[base + pos] = e; rr[base + pos] = r; ww[base + pos] = w; }
+                wsumR += w;
+            }
+            if (pass && img) {
+                const int pos = ni + __popc(balI & lt_mask);
+                if (pos < K) { imgE[pos] = e; imgR[pos] = r; imgW[pos] = w; }
+                wsumI += w;
+            }
+            nr += __popc(balR);
+            ni += __popc(balI);
         }
-        // omega = (sum over real neighbours) + W(0), then + images
-        double omega = 0.;
-        {
-            double o2 = 0.;
-            for (int s = 0; s < nr; ++s) o2 += ww[base + s];
-            omega = o2 + p.w0;
-            for (int s = nr; s < tot; ++s) omega += ww[base + s];
+        if (nr + ni > K || overflow) {
+            overflow = true;
+            if (nr > K) nr = K;
+            if (ni > K - nr) ni = K - nr;
         }
-        const double rho = m[i] * omega;
-        const double P = (p.gamma - 1.) * rho * u[i];
-        if (rho <= 0.) flag(status, ST_NEG_DENSITY);
-        if (P <= 0.) flag(status, ST_NEG_PRESSURE);
-        noi[i] = nr;
-        noiImg[i] = ni;
-        faceCnt[i] = fc;
-        Prim pr;
-        pr.x = xi[0]; pr.y = xi[1]; pr.z = xi[2];
-        pr.rho = rho; pr.P = P;
-        pr.vx = vx[i]; pr.vy = vy[i]; pr.vz = D == 3 ? vz[i] : 0.;
-        prim[i] = pr;
-        geo[i].omega = omega;
-        geo[i].V = 1. / omega;
-        geo[i].c = sqrt(p.gamma * P / rho);
+        __syncwarp();
+        // --- images behind the real neighbours, ordered by parent index
+        for (int t = lane; t < ni; t += 32) {
+            const uint32_t e = imgE[t];
+            const uint32_t id = e & IDX_MASK;
+            int rank = 0;
+            for (int q = 0; q < ni; ++q) rank += (imgE[q] & IDX_MASK) < id;
+            nbr[base + nr + rank] = e;
+            rr[base + nr + rank] = imgR[t];
+            ww[base + nr + rank] = imgW[t];
+        }
+        __syncwarp();
+        // canonical faces among the stored slots (neighbour or parent > i);
+        // counted from the final list so that it matches k_link exactly
+        for (int t = lane; t < nr + ni; t += 32) fc += (int)(nbr[base + t] & IDX_MASK) > i;
+        // --- omega = (sum over real neighbours) + W(0) + (sum over images)
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+            wsumR += __shfl_xor_sync(0xffffffffu, wsumR, o);
+            wsumI += __shfl_xor_sync(0xffffffffu, wsumI, o);
+            fc += __shfl_xor_sync(0xffffffffu, fc, o);
+        }
+        if (lane == 0) {
+            if (overflow) flag(status, ST_NGB_OVERFLOW);
+            if (nr + ni == 0) flag(status, ST_NO_NEIGHBOUR);
+            const double omega = (wsumR + p.w0) + wsumI;
+            const double rho = m[i] * omega;
+            const double P = (p.gamma - 1.) * rho * u[i];
+            if (rho <= 0.) flag(status, ST_NEG_DENSITY);
+            if (P <= 0.) flag(status, ST_NEG_PRESSURE);
+            noi[i] = nr;
+            noiImg[i] = ni;
+            faceCnt[i] = fc;
+            Prim pr;
+            pr.x = xi[0]; pr.y = xi[1]; pr.z = xi[2];
+            pr.rho = rho; pr.P = P;
+            pr.vx = vx[i]; pr.vy = vy[i]; pr.vz = D == 3 ? vz[i] : 0.;
+            prim[i] = pr;
+            geo[i].omega = omega;
+            geo[i].V = 1. / omega;
+            geo[i].c = sqrt(p.gamma * P / rho);
+        }
+        __syncwarp();
     }
+}
+
+size_t nns_smem_bytes(int K) {
+    return nns_cells_bytes() + (size_t)NNS_WARPS * nns_warp_bytes(K);
 }
 
 // ------------------------------------------------------------------ dt
@@ -682,6 +782,7 @@ __global__ void __launch_bounds__(128) k_link(Params p, const uint32_t *__restri
             if (j > i) {
                 const int fid = faceOff[i] + rank;
                 ++rank;
+                if (fid >= p.faces_cap) { flag(status, ST_CAPACITY); faceOf[base + s] = 0; continue; }
                 faceOf[base + s] = fid + 1;
                 faces[fid].i = i;
                 faces[fid].slot = s;
@@ -701,6 +802,7 @@ __global__ void __launch_bounds__(128) k_link(Params p, const uint32_t *__restri
             for (int t = 0; t < found; ++t)
                 if ((int)(nbr[jb + t] & IDX_MASK) > j) ++crank;
             const int fid = faceOff[j] + crank;
+            if (fid >= p.faces_cap) { flag(status, ST_CAPACITY); faceOf[base + s] = 0; continue; }
             faceOf[base + s] = -(fid + 1);
             faces[fid].rslot = s;
         }
@@ -781,7 +883,7 @@ __global__ void __launch_bounds__(128) k_faces(Params p, const GridInfo *__restr
                                                unsigned *__restrict__ status) {
     constexpr int NV = D + 2;
     const GridInfo g = *gridp;
-    const int nf = *faceTotal;
+    const int nf = *faceTotal < p.faces_cap ? *faceTotal : p.faces_cap;
     const double dt = *dtp;
     const RiemannConsts rc = make_riemann_consts(p.gamma, p.rtol, p.rmaxit);
     const double gamma = p.gamma;
@@ -789,6 +891,7 @@ __global__ void __launch_bounds__(128) k_faces(Params p, const GridInfo *__restr
     unsigned st_local = 0;
     for (int f = blockIdx.x * blockDim.x + threadIdx.x; f < nf; f += gridDim.x * blockDim.x) {
         const FaceRef fr = faces[f];
+        if (fr.i < 0 || fr.slot < 0) { st_local |= ST_ASYMMETRIC; continue; }
         const int i = fr.i;
         const size_t si = (size_t)i * p.K + fr.slot;
         const uint32_t e = nbr[si];
@@ -1018,7 +1121,7 @@ __global__ void __launch_bounds__(128) k_update(Params p, const GridInfo *__rest
         double mF = 0., eF = 0., vF[3] = {0., 0., 0.};
         for (int s = 0; s < tot; ++s) {
             const int fo = faceOf[base + s];
-            if (fo == 0) continue;
+            if (fo == 0 || (fo > 0 ? fo : -fo) > p.faces_cap) continue;
             const double2 *src = reinterpret_cast<const double2 *>(Fface + (size_t)((fo > 0 ? fo : -fo) - 1) * 6);
             const double2 a = src[0], b = src[1], c = src[2];
             if (fo > 0) {
@@ -1107,9 +1210,16 @@ void launch_step(StepArgs &a) {
     tock(KT_GRID);
 
     tick(KT_NNS);
-    k_neighbours<D><<<blocksN, T, 0, s>>>(p, a.grid, a.x, a.y, a.z, a.posf, a.vx, a.vy, a.vz, a.m, a.u, a.cell,
-                                          a.cellStart, a.cellList, a.nbr, a.rr, a.ww, a.noi, a.noiImg, a.faceCnt,
-                                          a.prim, a.geo, a.status);
+    {
+        const int warps_total = a.sm_count * 64;   // grid-stride over particles, one warp each
+        const int blocks = (warps_total + NNS_WARPS - 1) / NNS_WARPS;
+        const size_t smem = nns_smem_bytes(p.K);
+        if (smem > 48 * 1024)
+            cudaFuncSetAttribute(k_neighbours<D>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        k_neighbours<D><<<blocks, NNS_WARPS * 32, smem, s>>>(
+            p, a.grid, a.x, a.y, a.z, a.posf, a.vx, a.vy, a.vz, a.m, a.u, a.cell, a.cellStart, a.cellList, a.nbr,
+            a.rr, a.ww, a.noi, a.noiImg, a.faceCnt, a.prim, a.geo, a.status);
+    }
     tock(KT_NNS);
 
     tick(KT_DT);

@@ -14,6 +14,7 @@ struct StepArgs {
     Params p;
     cudaStream_t stream;
     int face_blocks;
+    int sm_count;
     int root5;              // gamma = 5/3 fast path of the Riemann solver
     size_t faces_cap;
     double dt_max;
