@@ -38,6 +38,14 @@ WORKLOADS = {
 METRIC = "particle-updates/s per MFV step on 1 GB300"
 LAUNCHES_PER_STEP = 18   # kernels launched by one mlh_step iteration (see csrc/mlh_kernels.cu)
 
+# Per-face cost of the dominant kernel (k_faces, 3D, gamma = 5/3 path),
+# from one ncu --set full capture of the 64^3 periodic Sedov step
+# (profiles/sedov64_step_kernels.md): FP64 operations executed per face
+# (2 x DFMA + DADD + DMUL thread instructions / faces) and DRAM bytes
+# (read + write) per face.
+FACE_FP64_FLOPS = {3: 772.0}
+FACE_DRAM_BYTES = {3: 209.0}
+
 
 def make_workload(name: str, seed_offset: int = 0):
     from meshlesshydro_gb300 import ic
@@ -207,6 +215,7 @@ def run_mlh(args):
         dist = None
     from meshlesshydro_gb300 import build, runtime
     build.build()
+    fp64_peak = runtime.probe_fp64_tflops(0.5)
     p, cfg = make_workload(args.workload, seed_offset=rank)
     sim = runtime.Simulation(cfg, p)
     sim.step(args.warmup)
@@ -263,17 +272,20 @@ def run_mlh(args):
     dom = max(kt.items(), key=lambda kv: kv[1][1])
     dom_name, (dom_launches, dom_ms) = dom
     dom_avg_s = dom_ms / max(dom_launches, 1) / 1e3
-    fp64_peak = args.fp64_peak_tflops
-    flops_per_face = args.flops_per_face
-    achieved_tf = flops_per_face * faces_per_step / dom_avg_s / 1e12 if dom_name == "faces_riemann" else None
-    roofline = {"kernel": dom_name, "bound": "fp64", "unit": "TFLOP/s",
+    flops_per_face = FACE_FP64_FLOPS.get(cfg.dim)
+    bytes_per_face = FACE_DRAM_BYTES.get(cfg.dim)
+    achieved_tf = (flops_per_face * faces_per_step / dom_avg_s / 1e12
+                   if (dom_name == "faces_riemann" and flops_per_face) else None)
+    roofline = {"kernel": "k_faces (faces_riemann)" if dom_name == "faces_riemann" else dom_name,
+                "bound": "fp64", "unit": "TFLOP/s",
                 "achieved": achieved_tf, "peak": fp64_peak,
                 "frac": (achieved_tf / fp64_peak) if (achieved_tf and fp64_peak) else None,
-                "traffic": args.dom_traffic_bytes * faces_per_step if args.dom_traffic_bytes else None,
-                "peak_source": args.fp64_peak_source,
-                "flops_per_face": flops_per_face,
-                "units_per_launch": faces_per_step,
-                "avg_launch_ms": dom_avg_s * 1e3}
+                "traffic": bytes_per_face * faces_per_step if bytes_per_face else None,
+                "peak_source": "measured: FP64 FMA-chain probe (mlh_probe_fp64_tflops) on this GPU in this run",
+                "units": "canonical faces", "units_per_launch": faces_per_step,
+                "flops_per_unit": flops_per_face, "avg_launch_ms": dom_avg_s * 1e3,
+                "hbm_view": {"achieved_gbs": (bytes_per_face * faces_per_step / dom_avg_s / 1e9) if bytes_per_face else None,
+                             "peak_gbs": peaks.get("hbm_gbs"), "peak_source": peak_kind}}
     line = {"metric": METRIC, "value": value, "unit": "particle-updates/s", "n_gpus": ws, "steps": st.steps,
             "warmup": args.warmup, "ms_per_step": 1e3 * t_max / st.steps, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
@@ -311,13 +323,6 @@ def main():
     ap.add_argument("--workload", default="sedov128", choices=sorted(WORKLOADS))
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
-    # FP64 work per face and the FP64 peak (see profiles/): executed FP64
-    # flops per Riemann face from ncu instruction counts, peak from the
-    # FP64 FMA probe
-    ap.add_argument("--flops-per-face", type=float, default=0.0)
-    ap.add_argument("--fp64-peak-tflops", type=float, default=0.0)
-    ap.add_argument("--fp64-peak-source", default="")
-    ap.add_argument("--dom-traffic-bytes", type=float, default=0.0)
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference(args)
