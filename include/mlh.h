@@ -90,6 +90,15 @@ typedef struct mlh_step_stats {
     double device_ms;                /* device time of the call (CUDA events) */
 } mlh_step_stats;
 
+/* One simulation of an ensemble: its particle count (members are stored back
+ * to back in the particle view, in member order), kernelSize and periodic box. */
+typedef struct mlh_member {
+    int n;
+    double kernel_size;
+    double box_lo[3];
+    double box_hi[3];
+} mlh_member;
+
 typedef struct mlh_ctx mlh_ctx;
 
 int mlh_abi_version(void);
@@ -100,6 +109,21 @@ const char *mlh_last_error(void);
  * device and allocates all per-particle and per-interaction buffers. */
 int mlh_create(const mlh_config *cfg, const mlh_particles_view *init, mlh_ctx **out);
 void mlh_destroy(mlh_ctx *ctx);
+
+/* An ensemble of independent simulations of uneven sizes advanced together:
+ * every stage of a step runs once for all members (one launch per kernel),
+ * each member with its own kernelSize, box, grid and dt.  The settings of
+ * `cfg` other than kernel_size and the box apply to every member.  No
+ * counterpart in the reference (which runs one simulation per process);
+ * mlh_step then advances all members by one step each. */
+int mlh_ensemble_create(const mlh_config *cfg, int nmembers, const mlh_member *members,
+                        const mlh_particles_view *all, mlh_ctx **out);
+/* dt of the last step and simulation time of every member (host arrays of
+ * nmembers doubles, either may be NULL). */
+int mlh_member_times(mlh_ctx *ctx, double *dt, double *time, int nmembers);
+/* Graph mode: mlh_step captures one step into a CUDA graph (once, and again
+ * after a capacity change) and replays it; kernel timing bypasses it. */
+int mlh_set_graph_mode(mlh_ctx *ctx, int enable);
 
 /* Host <-> device copies of the state (x, v, m, u). */
 int mlh_set_fields(mlh_ctx *ctx, const mlh_particles_view *src);

@@ -52,8 +52,15 @@ struct mlh_ctx {
     // state
     double *x = nullptr, *y = nullptr, *z = nullptr, *vx = nullptr, *vy = nullptr, *vz = nullptr, *m = nullptr, *u = nullptr;
     float4 *posf = nullptr;
-    // grid
-    GridInfo *grid = nullptr;
+    // simulations held by the context (1, or an ensemble stored back to back)
+    int nmembers = 1;
+    int bpm = 1;
+    std::vector<Member> hmembers;
+    Member *members = nullptr;
+    int *memberOf = nullptr;
+    // grids (one per member)
+    GridInfo *grids = nullptr;
+    int *cellTotal = nullptr;
     double *boundsPart = nullptr;
     int *cell = nullptr, *cellCount = nullptr, *cellStart = nullptr, *cellFill = nullptr, *cellList = nullptr;
     // neighbours (capacity K slots per particle)
@@ -74,6 +81,10 @@ struct mlh_ctx {
     int *stepsDone = nullptr;
     int *scanTiles = nullptr, *scanTotal = nullptr;
     bool debug_arrays = true;
+    // CUDA graph of one step, replayed by mlh_step in graph mode
+    bool graph_mode = false;
+    cudaGraphExec_t graph_exec = nullptr;
+    double graph_dt_max = -1.;
     // kernel timing
     bool timing = false;
     std::vector<cudaEvent_t> tev;   // pairs, in launch order
@@ -118,22 +129,46 @@ int alloc_cell_buffers(mlh_ctx *c) {
     return 0;
 }
 
-long long estimate_cells(const mlh_config &cfg, const mlh_particles_view *v) {
+long long estimate_cells(const mlh_config &cfg, const mlh_particles_view *v, const Member &mb) {
     double lo[3], hi[3];
     const double *X[3] = {v->x, v->y, v->z};
     long long total = 1;
     for (int a = 0; a < cfg.dim; ++a) {
-        if (cfg.periodic) { lo[a] = cfg.box_lo[a]; hi[a] = cfg.box_hi[a]; }
+        if (cfg.periodic) { lo[a] = mb.box_lo[a]; hi[a] = mb.box_hi[a]; }
         else {
-            lo[a] = hi[a] = X[a][0];
-            for (int i = 1; i < v->n; ++i) { lo[a] = std::fmin(lo[a], X[a][i]); hi[a] = std::fmax(hi[a], X[a][i]); }
+            lo[a] = hi[a] = X[a][mb.first];
+            for (int i = mb.first + 1; i < mb.first + mb.count; ++i) {
+                lo[a] = std::fmin(lo[a], X[a][i]);
+                hi[a] = std::fmax(hi[a], X[a][i]);
+            }
         }
-        double c = std::floor((hi[a] - lo[a]) / cfg.kernel_size);
+        double c = std::floor((hi[a] - lo[a]) / mb.h);
         long long ci = c >= 1. ? (long long)c : 1;
         if (!cfg.periodic) ci = ci + ci / 4 + 4;   // room for an expanding bounding box
         total *= ci;
     }
     return total;
+}
+
+// Kernel::cubicSpline normalisation (demonstrator/src/Particles.cpp:10-15)
+// and the other per-simulation constants.
+Member make_member(const mlh_config &f, double h, const double *lo, const double *hi, int first, int count) {
+    Member m;
+    std::memset(&m, 0, sizeof(m));
+    m.h = h;
+    m.hsq = h * h;
+    m.h2 = h / 2.;
+    const double h2 = m.h2;
+    m.sigma = f.dim == 2 ? 10. / (7. * M_PI * h2 * h2) : 1. / (M_PI * h2 * h2 * h2);
+    m.w0 = m.sigma * (1. - 3. / 2. * 0. * 0. * (1. - 0. / 2.));
+    m.cfl_h = f.cfl * h;
+    // single-precision pre-filter bound: positions rounded to float move a
+    // distance of ~1e-7 relative to the box; 1e-3 relative on h^2 is ample
+    m.hsq_f = (float)(m.hsq * (1. + 1e-3));
+    for (int a = 0; a < 3; ++a) { m.box_lo[a] = lo[a]; m.box_hi[a] = hi[a]; }
+    m.first = first;
+    m.count = count;
+    return m;
 }
 
 void timer_cb(void *vc, int id, int phase) {
@@ -171,7 +206,9 @@ StepArgs make_args(mlh_ctx *c, double dt_max) {
     a.dt_max = dt_max;
     a.x = c->x; a.y = c->y; a.z = c->z; a.vx = c->vx; a.vy = c->vy; a.vz = c->vz; a.m = c->m; a.u = c->u;
     a.posf = c->posf;
-    a.grid = c->grid; a.boundsPart = c->boundsPart;
+    a.nmembers = c->nmembers; a.bpm = c->bpm;
+    a.members = c->members; a.memberOf = c->memberOf;
+    a.grids = c->grids; a.cellTotal = c->cellTotal; a.boundsPart = c->boundsPart;
     a.cell = c->cell; a.cellCount = c->cellCount; a.cellStart = c->cellStart; a.cellFill = c->cellFill;
     a.cellList = c->cellList;
     a.nbr = c->nbr; a.rr = c->rr; a.ww = c->ww; a.psi = c->psi;
@@ -249,25 +286,43 @@ extern "C" {
 int mlh_abi_version(void) { return MLH_ABI_VERSION; }
 const char *mlh_last_error(void) { return g_last_error.c_str(); }
 
-int mlh_create(const mlh_config *cfg, const mlh_particles_view *init, mlh_ctx **out) {
+static int create_impl(const mlh_config *cfg, int nmembers, const mlh_member *mdesc, const mlh_particles_view *init,
+                       mlh_ctx **out) {
     if (!cfg || !init || !out) { g_last_error = "null argument"; return MLH_ERR_INVALID; }
     *out = nullptr;
-    if ((cfg->dim != 2 && cfg->dim != 3) || init->n < 1 || !(cfg->kernel_size > 0.) || !init->x || !init->y ||
-        !init->vx || !init->vy || !init->m || !init->u || (cfg->dim == 3 && (!init->z || !init->vz))) {
+    if ((cfg->dim != 2 && cfg->dim != 3) || init->n < 1 || !init->x || !init->y || !init->vx || !init->vy ||
+        !init->m || !init->u || (cfg->dim == 3 && (!init->z || !init->vz)) || nmembers < 1) {
         g_last_error = "invalid configuration or particle view";
         return MLH_ERR_INVALID;
     }
     if (init->n > (int)IDX_MASK) { g_last_error = "too many particles"; return MLH_ERR_CAPACITY; }
+    std::vector<Member> mem;
+    {
+        int first = 0;
+        for (int k = 0; k < nmembers; ++k) {
+            const double h = mdesc ? mdesc[k].kernel_size : cfg->kernel_size;
+            const int cnt = mdesc ? mdesc[k].n : init->n;
+            if (!(h > 0.) || cnt < 1) { g_last_error = "invalid member"; return MLH_ERR_INVALID; }
+            const double *lo = mdesc ? mdesc[k].box_lo : cfg->box_lo, *hi = mdesc ? mdesc[k].box_hi : cfg->box_hi;
+            mem.push_back(make_member(*cfg, h, lo, hi, first, cnt));
+            first += cnt;
+        }
+        if (first != init->n) { g_last_error = "member sizes do not add up to n"; return MLH_ERR_INVALID; }
+    }
     int ndev = 0;
     if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) { g_last_error = "no CUDA device"; return MLH_ERR_NO_DEVICE; }
     mlh_ctx *c = new mlh_ctx();
     c->cfg = *cfg;
     c->n = init->n;
+    c->nmembers = nmembers;
+    c->hmembers = mem;
+    c->bpm = nmembers >= BOUNDS_BLOCKS ? 1 : (BOUNDS_BLOCKS + nmembers - 1) / nmembers;
     cudaGetDevice(&c->device);
     cudaDeviceGetAttribute(&c->sm_count, cudaDevAttrMultiProcessorCount, c->device);
     fill_params(c);
     c->p.K = cfg->max_neighbours > 0 ? cfg->max_neighbours : (cfg->dim == 2 ? 40 : 64);
-    long long nc = estimate_cells(*cfg, init);
+    long long nc = 0;
+    for (const Member &mb : mem) nc += estimate_cells(*cfg, init, mb);
     if (nc > (1ll << 30)) { delete c; g_last_error = "grid too large"; return MLH_ERR_CAPACITY; }
     c->p.ncells_cap = (int)nc;
     int rc = 0;
@@ -275,21 +330,32 @@ int mlh_create(const mlh_config *cfg, const mlh_particles_view *init, mlh_ctx **
     if (cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking) != cudaSuccess) return fail(cuda_fail(cudaGetLastError(), "stream"));
     cudaEventCreate(&c->ev0);
     cudaEventCreate(&c->ev1);
-    size_t n = (size_t)c->n;
+    size_t n = (size_t)c->n, nm = (size_t)nmembers;
 #define A(ptr, cnt) if (dalloc(&c->ptr, cnt) != cudaSuccess) return fail(cuda_fail(cudaGetLastError(), "cudaMalloc " #ptr))
     A(x, n); A(y, n); A(z, n); A(vx, n); A(vy, n); A(vz, n); A(m, n); A(u, n);
     A(posf, n);
-    A(grid, 1); A(boundsPart, 304 * 6);
+    A(members, nm); A(grids, nm); A(cellTotal, 1); A(boundsPart, nm * (size_t)c->bpm * 6);
+    if (nmembers > 1) A(memberOf, n);
     A(cell, n); A(cellList, n);
     A(noi, n); A(noiImg, n); A(faceCnt, n); A(faceOff, n + 1);
     A(prim, n); A(geo, n); A(grad, n); A(gradRaw, n); A(fluxSums, n * 5);
-    A(status, 1); A(dtbits, 1); A(newtonSum, 1); A(dt, 1); A(simTime, 1); A(stepsDone, 1);
+    A(status, 1); A(dtbits, nm); A(newtonSum, 1); A(dt, nm); A(simTime, nm); A(stepsDone, 1);
     A(scanTiles, n / 4096 + 1024); A(scanTotal, 1);
 #undef A
     if ((rc = alloc_cell_buffers(c))) return fail(rc);
     if ((rc = alloc_neighbour_buffers(c))) return fail(rc);
+    if (cudaMemcpyAsync(c->members, mem.data(), sizeof(Member) * nm, cudaMemcpyHostToDevice, c->stream) != cudaSuccess)
+        return fail(cuda_fail(cudaGetLastError(), "members"));
+    if (nmembers > 1) {
+        std::vector<int> mo(n);
+        for (int k = 0; k < nmembers; ++k)
+            for (int i = mem[k].first; i < mem[k].first + mem[k].count; ++i) mo[i] = k;
+        if (cudaMemcpy(c->memberOf, mo.data(), sizeof(int) * n, cudaMemcpyHostToDevice) != cudaSuccess)
+            return fail(cuda_fail(cudaGetLastError(), "memberOf"));
+    }
     cudaMemsetAsync(c->status, 0, sizeof(unsigned), c->stream);
-    cudaMemsetAsync(c->simTime, 0, sizeof(double), c->stream);
+    cudaMemsetAsync(c->simTime, 0, sizeof(double) * nm, c->stream);
+    cudaMemsetAsync(c->dt, 0, sizeof(double) * nm, c->stream);
     cudaMemsetAsync(c->newtonSum, 0, sizeof(unsigned long long), c->stream);
     cudaMemsetAsync(c->stepsDone, 0, sizeof(int), c->stream);
     if ((rc = upload(c, init))) return fail(rc);
@@ -298,13 +364,29 @@ int mlh_create(const mlh_config *cfg, const mlh_particles_view *init, mlh_ctx **
     return 0;
 }
 
+int mlh_create(const mlh_config *cfg, const mlh_particles_view *init, mlh_ctx **out) {
+    return create_impl(cfg, 1, nullptr, init, out);
+}
+
+int mlh_ensemble_create(const mlh_config *cfg, int nmembers, const mlh_member *members,
+                        const mlh_particles_view *all, mlh_ctx **out) {
+    if (!members || nmembers < 1) { g_last_error = "no members"; return MLH_ERR_INVALID; }
+    return create_impl(cfg, nmembers, members, all, out);
+}
+
+static void drop_graph(mlh_ctx *c) {
+    if (c->graph_exec) cudaGraphExecDestroy(c->graph_exec);
+    c->graph_exec = nullptr;
+}
+
 void mlh_destroy(mlh_ctx *c) {
     if (!c) return;
     if (c->stream) cudaStreamSynchronize(c->stream);
-    void *ptrs[] = {c->x, c->y, c->z, c->vx, c->vy, c->vz, c->m, c->u, c->posf, c->grid, c->boundsPart, c->cell,
-                    c->cellList, c->noi, c->noiImg, c->faceCnt, c->faceOff, c->prim, c->geo, c->grad, c->gradRaw,
-                    c->fluxSums, c->status, c->dtbits, c->newtonSum, c->dt, c->simTime, c->stepsDone, c->scanTiles,
-                    c->scanTotal};
+    drop_graph(c);
+    void *ptrs[] = {c->x, c->y, c->z, c->vx, c->vy, c->vz, c->m, c->u, c->posf, c->members, c->memberOf, c->grids,
+                    c->cellTotal, c->boundsPart, c->cell, c->cellList, c->noi, c->noiImg, c->faceCnt, c->faceOff,
+                    c->prim, c->geo, c->grad, c->gradRaw, c->fluxSums, c->status, c->dtbits, c->newtonSum, c->dt,
+                    c->simTime, c->stepsDone, c->scanTiles, c->scanTotal};
     for (void *q : ptrs) if (q) cudaFree(q);
     free_cell_buffers(c);
     free_neighbour_buffers(c);
@@ -336,6 +418,24 @@ int mlh_get_fields(mlh_ctx *c, mlh_particles_view *v) {
     return 0;
 }
 
+// One step into a CUDA graph on the context's stream (no host work inside the
+// step, so the captured launches are replayed as they are).
+static int capture_step(mlh_ctx *c, double dt_max) {
+    drop_graph(c);
+    StepArgs a = make_args(c, dt_max);
+    a.timer = nullptr;
+    cudaGraph_t g = nullptr;
+    CK(cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal));
+    step(a);
+    cudaError_t e = cudaStreamEndCapture(c->stream, &g);
+    if (e != cudaSuccess) return cuda_fail(e, "cudaStreamEndCapture");
+    e = cudaGraphInstantiate(&c->graph_exec, g, 0);
+    cudaGraphDestroy(g);
+    if (e != cudaSuccess) { c->graph_exec = nullptr; return cuda_fail(e, "cudaGraphInstantiate"); }
+    c->graph_dt_max = dt_max;
+    return 0;
+}
+
 int mlh_step(mlh_ctx *c, int nsteps, double dt_max, mlh_step_stats *stats) {
     if (!c || nsteps < 0) { g_last_error = "invalid argument"; return MLH_ERR_INVALID; }
     unsigned accumulated = 0;
@@ -346,12 +446,21 @@ int mlh_step(mlh_ctx *c, int nsteps, double dt_max, mlh_step_stats *stats) {
     int remaining = nsteps;
     int retries = 0;
     while (remaining > 0) {
+        const bool use_graph = c->graph_mode && !c->timing;
+        if (use_graph && (!c->graph_exec || c->graph_dt_max != dt_max)) {
+            int rc = capture_step(c, dt_max);
+            if (rc) return rc;
+        }
         CK(cudaMemsetAsync(c->status, 0, sizeof(unsigned), c->stream));
         CK(cudaMemsetAsync(c->stepsDone, 0, sizeof(int), c->stream));
         CK(cudaMemsetAsync(c->newtonSum, 0, sizeof(unsigned long long), c->stream));
         CK(cudaEventRecord(c->ev0, c->stream));
-        StepArgs a = make_args(c, dt_max);
-        for (int k = 0; k < remaining; ++k) step(a);
+        if (use_graph) {
+            for (int k = 0; k < remaining; ++k) CK(cudaGraphLaunch(c->graph_exec, c->stream));
+        } else {
+            StepArgs a = make_args(c, dt_max);
+            for (int k = 0; k < remaining; ++k) step(a);
+        }
         CK(cudaEventRecord(c->ev1, c->stream));
         CK(cudaGetLastError());
         CK(cudaStreamSynchronize(c->stream));
@@ -387,6 +496,7 @@ int mlh_step(mlh_ctx *c, int nsteps, double dt_max, mlh_step_stats *stats) {
                 int rc = alloc_cell_buffers(c);
                 if (rc) return rc;
             }
+            drop_graph(c);   // buffers changed
             continue;
         }
         accumulated |= st;
@@ -403,6 +513,21 @@ int mlh_step(mlh_ctx *c, int nsteps, double dt_max, mlh_step_stats *stats) {
         stats->device_ms = dev_ms;
     }
     return (int)(accumulated & ~(unsigned)MLH_ERR_NGB_OVERFLOW & ~ST_CAPACITY) ? (int)accumulated : 0;
+}
+
+int mlh_set_graph_mode(mlh_ctx *c, int enable) {
+    if (!c) return MLH_ERR_INVALID;
+    c->graph_mode = enable != 0;
+    if (!c->graph_mode) drop_graph(c);
+    return 0;
+}
+
+int mlh_member_times(mlh_ctx *c, double *dt, double *time, int nmembers) {
+    if (!c || nmembers != c->nmembers) { g_last_error = "member count mismatch"; return MLH_ERR_INVALID; }
+    CK(cudaStreamSynchronize(c->stream));
+    if (dt) CK(cudaMemcpy(dt, c->dt, sizeof(double) * nmembers, cudaMemcpyDeviceToHost));
+    if (time) CK(cudaMemcpy(time, c->simTime, sizeof(double) * nmembers, cudaMemcpyDeviceToHost));
+    return 0;
 }
 
 int mlh_stage_array(mlh_ctx *c, const char *name, void *out, long long capacity, long long *count) {
@@ -504,7 +629,7 @@ int mlh_stage_array(mlh_ctx *c, const char *name, void *out, long long capacity,
     }
     if (nm == "grid") {
         GridInfo g;
-        CK(cudaMemcpy(&g, c->grid, sizeof(GridInfo), cudaMemcpyDeviceToHost));
+        CK(cudaMemcpy(&g, c->grids, sizeof(GridInfo), cudaMemcpyDeviceToHost));
         double o[9];
         for (int a = 0; a < 3; ++a) {
             o[a] = a < D ? g.lo[a] : 0.;

@@ -31,11 +31,24 @@ enum : unsigned {
     ST_CAPACITY = 1u << 23,   // a fixed-size device buffer was too small
 };
 
-// Uniform search grid (Domain::createGrid, demonstrator/src/Domain.cpp:9-54).
+// Uniform search grid of one simulation (Domain::createGrid,
+// demonstrator/src/Domain.cpp:9-54); its cells are numbered from cell_base in
+// the concatenated cell array of all simulations of a context.
 struct GridInfo {
     double lo[3], hi[3], cs[3];
     int cells[3];
     int ncells;
+    int cell_base;
+};
+
+// One simulation of a context (a context holds one, or an ensemble of
+// independent simulations stored back to back): its kernel size and the
+// quantities derived from it, its periodic box and its particle range.
+struct Member {
+    double h, hsq, h2, sigma, w0, cfl_h;
+    double box_lo[3], box_hi[3];
+    float hsq_f;           // conservative single-precision bound for the pre-filter
+    int first, count;
 };
 
 // Everything a kernel needs to know about the run, passed by value.
@@ -68,10 +81,10 @@ struct FaceRef {    // canonical face: owner i, slot index, reverse slot (images
 // Kernel::cubicSpline, demonstrator/src/Particles.cpp:7-24.  sigma is
 // precomputed on the host with the reference's expression; pow(2-q, 3.) is
 // written as a product.
-__device__ __forceinline__ double kernelW(double r, const Params &p) {
-    double q = r / p.h2;
-    if (0. <= q && q <= 1.) return p.sigma * (1. - 3. / 2. * q * q * (1. - q / 2.));
-    if (1. < q && q < 2.) { double t = 2. - q; return p.sigma / 4. * (t * t * t); }
+__device__ __forceinline__ double kernelW(double r, const Member &mb) {
+    double q = r / mb.h2;
+    if (0. <= q && q <= 1.) return mb.sigma * (1. - 3. / 2. * q * q * (1. - q / 2.));
+    if (1. < q && q < 2.) { double t = 2. - q; return mb.sigma / 4. * (t * t * t); }
     return 0.;
 }
 

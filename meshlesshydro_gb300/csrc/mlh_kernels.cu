@@ -140,23 +140,30 @@ void exclusive_scan(const int *in, int n, int *out, int *tile_buf, int *total, c
 // particles; because of `else if` and numeric_limits<double>::min(), hi = the
 // max over i >= 1 of the x_i that are not below the running minimum of
 // x_0..x_{i-1}, or DBL_MIN.  The partial pass computes min over all i and max
-// over i >= 1; the final pass falls back to the sequential rule whenever x_0 is
-// above every other particle (the only case where the two differ).
+// over i >= 1 of each simulation's range (blocks_per_member blocks each); the
+// final pass falls back to the sequential rule whenever x_0 is above every
+// other particle (the only case where the two differ).
 constexpr int BOUNDS_T = 256;
 
 template <int D>
 __global__ void k_bounds_partial(const double *__restrict__ x, const double *__restrict__ y,
-                                 const double *__restrict__ z, int n, double *__restrict__ part) {
+                                 const double *__restrict__ z, Params p, const Member *__restrict__ members,
+                                 int bpm, double *__restrict__ part) {
     __shared__ double smin[3][BOUNDS_T / 32], smax[3][BOUNDS_T / 32];
+    const int mi = blockIdx.x / bpm, sub = blockIdx.x % bpm;
+    const Member mb = members[mi];
     const double *X[3] = {x, y, z};
     double mn[3], mx[3];
     for (int a = 0; a < 3; ++a) { mn[a] = DBL_MAX_; mx[a] = -DBL_MAX_; }
-    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    if (!p.periodic) {
+        const int end = mb.first + mb.count;
+        for (int i = mb.first + sub * blockDim.x + threadIdx.x; i < end; i += bpm * blockDim.x) {
 #pragma unroll
-        for (int a = 0; a < D; ++a) {
-            double v = X[a][i];
-            mn[a] = fmin(mn[a], v);
-            if (i >= 1) mx[a] = fmax(mx[a], v);
+            for (int a = 0; a < D; ++a) {
+                double v = X[a][i];
+                mn[a] = fmin(mn[a], v);
+                if (i >= mb.first + 1) mx[a] = fmax(mx[a], v);
+            }
         }
     }
 #pragma unroll
@@ -178,60 +185,79 @@ __global__ void k_bounds_partial(const double *__restrict__ x, const double *__r
     }
 }
 
-// Final pass + Domain::createGrid (Domain.cpp:9-54).  For periodic runs the
+// Final pass + Domain::createGrid (Domain.cpp:9-54) for every simulation,
+// then the cell numbering of the concatenated grids.  For periodic runs the
 // bounds are the configured box.
 template <int D>
 __global__ void k_bounds_final(const double *__restrict__ x, const double *__restrict__ y,
-                               const double *__restrict__ z, const double *__restrict__ part, int nparts,
-                               Params p, GridInfo *__restrict__ grid, unsigned *__restrict__ status) {
-    if (threadIdx.x != 0) return;
+                               const double *__restrict__ z, const double *__restrict__ part, int bpm, Params p,
+                               const Member *__restrict__ members, int nmembers, GridInfo *__restrict__ grids,
+                               int *__restrict__ cellTotal, unsigned *__restrict__ status) {
     const double *X[3] = {x, y, z};
-    GridInfo g;
-    for (int a = 0; a < 3; ++a) { g.lo[a] = 0.; g.hi[a] = 0.; g.cs[a] = 1.; g.cells[a] = 1; }
-    for (int a = 0; a < D; ++a) {
-        if (p.periodic) { g.lo[a] = p.box_lo[a]; g.hi[a] = p.box_hi[a]; continue; }
-        double mn = DBL_MAX_, mx1 = -DBL_MAX_;
-        for (int b = 0; b < nparts; ++b) { mn = fmin(mn, part[(b * 3 + a) * 2]); mx1 = fmax(mx1, part[(b * 3 + a) * 2 + 1]); }
-        double x0 = X[a][0];
-        double hi;
-        if (p.n < 2 || !(mx1 >= x0)) {
-            // sequential rule of the reference
-            double lo_s = DBL_MAX_, hi_s = DBL_MIN_;
-            for (int i = 0; i < p.n; ++i) {
-                double v = X[a][i];
-                if (v < lo_s) lo_s = v;
-                else if (v > hi_s) hi_s = v;
+    for (int mi = threadIdx.x; mi < nmembers; mi += blockDim.x) {
+        const Member mb = members[mi];
+        GridInfo g;
+        for (int a = 0; a < 3; ++a) { g.lo[a] = 0.; g.hi[a] = 0.; g.cs[a] = 1.; g.cells[a] = 1; }
+        for (int a = 0; a < D; ++a) {
+            if (p.periodic) { g.lo[a] = mb.box_lo[a]; g.hi[a] = mb.box_hi[a]; continue; }
+            double mn = DBL_MAX_, mx1 = -DBL_MAX_;
+            for (int b = mi * bpm; b < (mi + 1) * bpm; ++b) {
+                mn = fmin(mn, part[(b * 3 + a) * 2]);
+                mx1 = fmax(mx1, part[(b * 3 + a) * 2 + 1]);
             }
-            hi = hi_s;
-        } else {
-            hi = mx1 > DBL_MIN_ ? mx1 : DBL_MIN_;
+            const double x0 = X[a][mb.first];
+            double hi;
+            if (mb.count < 2 || !(mx1 >= x0)) {
+                // sequential rule of the reference
+                double lo_s = DBL_MAX_, hi_s = DBL_MIN_;
+                for (int i = mb.first; i < mb.first + mb.count; ++i) {
+                    double v = X[a][i];
+                    if (v < lo_s) lo_s = v;
+                    else if (v > hi_s) hi_s = v;
+                }
+                hi = hi_s;
+            } else {
+                hi = mx1 > DBL_MIN_ ? mx1 : DBL_MIN_;
+            }
+            g.lo[a] = mn;
+            g.hi[a] = hi;
         }
-        g.lo[a] = mn;
-        g.hi[a] = hi;
+        long long total = 1;
+        for (int a = 0; a < D; ++a) {
+            double c = floor((g.hi[a] - g.lo[a]) / mb.h);
+            int ci = (c >= 1. && c < 2147483647.) ? (int)c : 1;
+            if (!(c >= 1.)) flag(status, ST_GRID);
+            if (p.periodic && ci < 3) flag(status, ST_GRID);
+            g.cells[a] = ci;
+            total *= ci;
+        }
+        for (int a = 0; a < D; ++a) g.cs[a] = (g.hi[a] - g.lo[a]) / (double)g.cells[a];
+        if (total > p.ncells_cap) { flag(status, ST_CAPACITY); total = 1; }
+        g.ncells = (int)total;
+        g.cell_base = 0;
+        grids[mi] = g;
     }
-    long long total = 1;
-    for (int a = 0; a < D; ++a) {
-        double c = floor((g.hi[a] - g.lo[a]) / p.h);
-        int ci = (c >= 1. && c < 2147483647.) ? (int)c : 1;
-        if (!(c >= 1.)) flag(status, ST_GRID);
-        if (p.periodic && ci < 3) flag(status, ST_GRID);
-        g.cells[a] = ci;
-        total *= ci;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        long long base = 0;
+        for (int mi = 0; mi < nmembers; ++mi) {
+            int nc = grids[mi].ncells;
+            if (base + nc > p.ncells_cap) { flag(status, ST_CAPACITY); nc = 0; grids[mi].ncells = 0; }
+            grids[mi].cell_base = (int)base;
+            base += nc;
+        }
+        *cellTotal = (int)base;
     }
-    for (int a = 0; a < D; ++a) g.cs[a] = (g.hi[a] - g.lo[a]) / (double)g.cells[a];
-    if (total > p.ncells_cap) { flag(status, ST_CAPACITY); total = p.ncells_cap; }
-    g.ncells = (int)total;
-    *grid = g;
 }
 
 // Particles::assignParticlesAndCells (Particles.cpp:270-322).
 template <int D>
 __global__ void k_assign(const double *__restrict__ x, const double *__restrict__ y, const double *__restrict__ z,
-                         int n, const GridInfo *__restrict__ gridp, int *__restrict__ cell,
-                         int *__restrict__ cellCount, unsigned *__restrict__ status) {
-    const GridInfo g = *gridp;
+                         int n, const int *__restrict__ memberOf, const GridInfo *__restrict__ grids,
+                         int *__restrict__ cell, int *__restrict__ cellCount, unsigned *__restrict__ status) {
     const double *X[3] = {x, y, z};
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const GridInfo g = grids[memberOf ? memberOf[i] : 0];
         int fl[3] = {0, 0, 0};
         bool bad = false;
 #pragma unroll
@@ -244,7 +270,8 @@ __global__ void k_assign(const double *__restrict__ x, const double *__restrict_
         }
         if (bad) flag(status, ST_GRID);
         int c = fl[0] + fl[1] * g.cells[0] + (D == 3 ? fl[2] * g.cells[0] * g.cells[1] : 0);
-        if (c >= g.ncells) { c = g.ncells - 1; flag(status, ST_GRID); }
+        if (c >= g.ncells) { c = g.ncells > 0 ? g.ncells - 1 : 0; flag(status, ST_GRID); }
+        c += g.cell_base;
         cell[i] = c;
         atomicAdd(&cellCount[c], 1);
     }
@@ -261,9 +288,9 @@ __global__ void k_fill_cells(const int *__restrict__ cell, int n, const int *__r
 
 // Members of a cell in ascending particle index: the order in which
 // assignParticlesAndCells pushes them (Particles.cpp:319).
-__global__ void k_sort_cells(const GridInfo *__restrict__ gridp, const int *__restrict__ cellStart,
+__global__ void k_sort_cells(const int *__restrict__ cellTotal, const int *__restrict__ cellStart,
                              int *__restrict__ cellList) {
-    int nc = gridp->ncells;
+    const int nc = *cellTotal;
     for (int c = blockIdx.x * blockDim.x + threadIdx.x; c < nc; c += gridDim.x * blockDim.x) {
         int b = cellStart[c], e = cellStart[c + 1];
         for (int k = b + 1; k < e; ++k) {
@@ -313,7 +340,8 @@ __host__ __device__ constexpr size_t nns_warp_bytes(int K) {
 
 template <int D>
 __global__ void __launch_bounds__(NNS_WARPS * 32) k_neighbours(
-    Params p, const GridInfo *__restrict__ gridp, const double *__restrict__ x, const double *__restrict__ y,
+    Params p, const Member *__restrict__ members, const int *__restrict__ memberOf,
+    const GridInfo *__restrict__ grids, const double *__restrict__ x, const double *__restrict__ y,
     const double *__restrict__ z, const float4 *__restrict__ posf, const double *__restrict__ vx,
     const double *__restrict__ vy, const double *__restrict__ vz, const double *__restrict__ m,
     const double *__restrict__ u, const int *__restrict__ cell, const int *__restrict__ cellStart,
@@ -336,15 +364,17 @@ __global__ void __launch_bounds__(NNS_WARPS * 32) k_neighbours(
     double *imgW = imgR + K;
     uint32_t *imgE = reinterpret_cast<uint32_t *>(imgW + K);
 
-    const GridInfo g = *gridp;
     const double *X[3] = {x, y, z};
-    float Lf[3];
-#pragma unroll
-    for (int a = 0; a < 3; ++a) Lf[a] = (float)(g.hi[a] - g.lo[a]);
     const int gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const int nw = (gridDim.x * blockDim.x) >> 5;
     for (int i = gw; i < p.n; i += nw) {
-        const int ic = cell[i];
+        const int mi = memberOf ? memberOf[i] : 0;
+        const GridInfo g = grids[mi];
+        const Member mb = members[mi];
+        float Lf[3];
+#pragma unroll
+        for (int a = 0; a < 3; ++a) Lf[a] = (float)(g.hi[a] - g.lo[a]);
+        const int ic = cell[i] - g.cell_base;
         const int ix = ic % g.cells[0];
         const int iy = (ic / g.cells[0]) % g.cells[1];
         const int iz = D == 3 ? ic / (g.cells[0] * g.cells[1]) : 0;
@@ -367,7 +397,7 @@ __global__ void __launch_bounds__(NNS_WARPS * 32) k_neighbours(
                 }
             }
             if (!skip) {
-                int c = cc[0] + cc[1] * g.cells[0] + (D == 3 ? cc[2] * g.cells[0] * g.cells[1] : 0);
+                int c = g.cell_base + cc[0] + cc[1] * g.cells[0] + (D == 3 ? cc[2] * g.cells[0] * g.cells[1] : 0);
                 start = cellStart[c];
                 cnt = cellStart[c + 1] - start;
             }
@@ -411,7 +441,7 @@ __global__ void __launch_bounds__(NNS_WARPS * 32) k_neighbours(
                         if (D == 3) dz += (float)cs->shift[k][2] * Lf[2];
                     }
                     float d2f = dx * dx + dy * dy + (D == 3 ? dz * dz : 0.f);
-                    pass = d2f <= p.hsq_f;
+                    pass = d2f <= mb.hsq_f;
                     ent = (uint32_t)j | (wr << IMG_SHIFT);
                 }
             }
@@ -447,7 +477,7 @@ __global__ void __launch_bounds__(NNS_WARPS * 32) k_neighbours(
                 for (int a = 0; a < D; ++a) {
                     xj[a] = X[a][j];
                     if (wr & (1u << a)) {
-                        if (in_band(xj[a], g.lo[a], g.hi[a], p.h)) xj[a] = image_coord(xj[a], g.lo[a], g.hi[a], p.h);
+                        if (in_band(xj[a], g.lo[a], g.hi[a], mb.h)) xj[a] = image_coord(xj[a], g.lo[a], g.hi[a], mb.h);
                         else ok = false;
                     }
                 }
@@ -455,10 +485,10 @@ __global__ void __launch_bounds__(NNS_WARPS * 32) k_neighbours(
                     double ex = __dsub_rn(xj[0], xi[0]), ey = __dsub_rn(xj[1], xi[1]);
                     double d2 = __dadd_rn(__dmul_rn(ex, ex), __dmul_rn(ey, ey));
                     if (D == 3) { double ez = __dsub_rn(xj[2], xi[2]); d2 = __dadd_rn(d2, __dmul_rn(ez, ez)); }
-                    pass = d2 < p.hsq;
+                    pass = d2 < mb.hsq;
                     if (pass) {
                         r = sqrt(d2);
-                        w = kernelW(r, p);
+                        w = kernelW(r, mb);
                     }
                 }
             }
@@ -507,7 +537,7 @@ __global__ void __launch_bounds__(NNS_WARPS * 32) k_neighbours(
         if (lane == 0) {
             if (overflow) flag(status, ST_NGB_OVERFLOW);
             if (nr + ni == 0) flag(status, ST_NO_NEIGHBOUR);
-            const double omega = (wsumR + p.w0) + wsumI;
+            const double omega = (wsumR + mb.w0) + wsumI;
             const double rho = m[i] * omega;
             const double P = (p.gamma - 1.) * rho * u[i];
             if (rho <= 0.) flag(status, ST_NEG_DENSITY);
@@ -539,41 +569,62 @@ size_t nns_smem_bytes(int K) {
 // particles is order independent, so an atomicMin on the bit pattern of the
 // (positive) per-particle dt is deterministic.
 template <int D>
-__global__ void __launch_bounds__(256) k_timestep(Params p, const Prim *__restrict__ prim, const Geo *__restrict__ geo,
-                                                  const uint32_t *__restrict__ nbr, const double *__restrict__ rr,
-                                                  const int *__restrict__ noi, unsigned long long *__restrict__ dtbits) {
-    double best = DBL_MAX_;
-    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < p.n; i += gridDim.x * blockDim.x) {
-        const Prim pi = prim[i];
-        const double ci = geo[i].c;
-        double vSig = DBL_MIN_;
-        const size_t base = (size_t)i * p.K;
-        const int nr = noi[i];
-        for (int s = 0; s < nr; ++s) {
-            const int j = (int)(nbr[base + s] & IDX_MASK);
-            const Prim pj = prim[j];
-            const double cj = geo[j].c;
-            double xij[3] = {pi.x - pj.x, pi.y - pj.y, pi.z - pj.z};
-            double vij[3] = {pi.vx - pj.vx, pi.vy - pj.vy, pi.vz - pj.vz};
-            // min(0, v_ij . x_ij / r): the quotient is needed only when the
-            // dot product is negative (same value and sign as the reference's)
-            const double dv = dotD<D>(vij, xij);
-            const double vijxij = dv < 0. ? dv / rr[base + s] : 0.;
-            double vs = ci + cj - vijxij;
-            vSig = vs > vSig ? vs : vSig;
+__global__ void __launch_bounds__(256) k_timestep(Params p, const Member *__restrict__ members,
+                                                  const int *__restrict__ memberOf, const Prim *__restrict__ prim,
+                                                  const Geo *__restrict__ geo, const uint32_t *__restrict__ nbr,
+                                                  const double *__restrict__ rr, const int *__restrict__ noi,
+                                                  unsigned long long *__restrict__ dtbits) {
+    const int lane = threadIdx.x & 31;
+    // warp-uniform loop: every lane takes part in the reductions below
+    for (int i0 = (blockIdx.x * blockDim.x + threadIdx.x) & ~31; i0 < p.n; i0 += gridDim.x * blockDim.x) {
+        const int i = i0 + lane;
+        int mi = -1;
+        double dti = DBL_MAX_;
+        if (i < p.n) {
+            mi = memberOf ? memberOf[i] : 0;
+            const Prim pi = prim[i];
+            const double ci = geo[i].c;
+            double vSig = DBL_MIN_;
+            const size_t base = (size_t)i * p.K;
+            const int nr = noi[i];
+            for (int s = 0; s < nr; ++s) {
+                const int j = (int)(nbr[base + s] & IDX_MASK);
+                const Prim pj = prim[j];
+                const double cj = geo[j].c;
+                double xij[3] = {pi.x - pj.x, pi.y - pj.y, pi.z - pj.z};
+                double vij[3] = {pi.vx - pj.vx, pi.vy - pj.vy, pi.vz - pj.vz};
+                // min(0, v_ij . x_ij / r): the quotient is needed only when the
+                // dot product is negative (same value and sign as the reference's)
+                const double dv = dotD<D>(vij, xij);
+                const double vijxij = dv < 0. ? dv / rr[base + s] : 0.;
+                double vs = ci + cj - vijxij;
+                vSig = vs > vSig ? vs : vSig;
+            }
+            dti = members[mi].cfl_h / vSig;
         }
-        double dti = p.cfl_h / vSig;
-        best = dti < best ? dti : best;
+        // the minimum over particles does not depend on the order of the
+        // atomicMin calls: a warp inside one simulation (the common case)
+        // reduces first and issues one atomic; a warp that straddles two
+        // simulations issues one per lane
+        const int m0 = __shfl_sync(0xffffffffu, mi, 0);
+        if (__all_sync(0xffffffffu, mi == m0)) {
+            double best = dti;
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) best = fmin(best, __shfl_xor_sync(0xffffffffu, best, o));
+            if (lane == 0 && m0 >= 0 && best < DBL_MAX_) atomic_min_pos_double(dtbits + m0, best);
+        } else if (mi >= 0 && dti < DBL_MAX_) {
+            atomic_min_pos_double(dtbits + mi, dti);
+        }
     }
-    for (int o = 16; o > 0; o >>= 1) best = fmin(best, __shfl_xor_sync(0xffffffffu, best, o));
-    if ((threadIdx.x & 31) == 0 && best < DBL_MAX_) atomic_min_pos_double(dtbits, best);
 }
 
-__global__ void k_dt_final(Params p, const unsigned long long *__restrict__ dtbits, double dt_max,
+__global__ void k_dt_final(Params p, int nmembers, const unsigned long long *__restrict__ dtbits, double dt_max,
                            double *__restrict__ dt_out) {
-    double dt = p.adaptive ? __longlong_as_double((long long)*dtbits) : p.time_step;
-    if (dt_max > 0. && dt > dt_max) dt = dt_max;
-    *dt_out = dt;
+    for (int mi = blockIdx.x * blockDim.x + threadIdx.x; mi < nmembers; mi += gridDim.x * blockDim.x) {
+        double dt = p.adaptive ? __longlong_as_double((long long)dtbits[mi]) : p.time_step;
+        if (dt_max > 0. && dt > dt_max) dt = dt_max;
+        dt_out[mi] = dt;
+    }
 }
 
 // ------------------------------------------------------------------ gradients
@@ -630,15 +681,18 @@ __device__ __forceinline__ double field_of(const Prim &q, int f) {
 }
 
 template <int D>
-__global__ void __launch_bounds__(128) k_gradients(Params p, const GridInfo *__restrict__ gridp,
+__global__ void __launch_bounds__(128) k_gradients(Params p, const Member *__restrict__ members,
+                                                   const int *__restrict__ memberOf, const GridInfo *__restrict__ grids,
                                                    const Prim *__restrict__ prim, Geo *__restrict__ geo,
                                                    const uint32_t *__restrict__ nbr, const double *__restrict__ ww,
                                                    const int *__restrict__ noi, const int *__restrict__ noiImg,
                                                    Grad *__restrict__ grad, Grad *__restrict__ gradRaw,
                                                    double *__restrict__ psiOut) {
     constexpr int NF = D + 2;
-    const GridInfo g = *gridp;
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < p.n; i += gridDim.x * blockDim.x) {
+        const int mi = memberOf ? memberOf[i] : 0;
+        const GridInfo g = grids[mi];
+        const double h = members[mi].h;
         const Prim pi = prim[i];
         const double xi[3] = {pi.x, pi.y, pi.z};
         const double Vi = geo[i].V;
@@ -649,7 +703,7 @@ __global__ void __launch_bounds__(128) k_gradients(Params p, const GridInfo *__r
             const uint32_t e = nbr[base + s];
             const Prim pj = prim[e & IDX_MASK];
             double xj[3];
-            neighbour_pos<D>(e, pj, g, p.h, xj);
+            neighbour_pos<D>(e, pj, g, h, xj);
             const double psij = ww[base + s] * Vi;
             double d[3];
 #pragma unroll
@@ -672,7 +726,7 @@ __global__ void __launch_bounds__(128) k_gradients(Params p, const GridInfo *__r
             const uint32_t e = nbr[base + s];
             const Prim pj = prim[e & IDX_MASK];
             double xj[3];
-            neighbour_pos<D>(e, pj, g, p.h, xj);
+            neighbour_pos<D>(e, pj, g, h, xj);
             const double psij = ww[base + s] * Vi;
             double d[3], ps[3];
 #pragma unroll
@@ -714,10 +768,10 @@ __global__ void __launch_bounds__(128) k_gradients(Params p, const GridInfo *__r
                 const uint32_t e = nbr[base + s];
                 const Prim pj = prim[e & IDX_MASK];
                 double xj[3], xijxi[3];
-                neighbour_pos<D>(e, pj, g, p.h, xj);
+                neighbour_pos<D>(e, pj, g, h, xj);
 #pragma unroll
                 for (int a = 0; a < D; ++a) {
-                    double xij = p.foqp ? (xi[a] + xj[a]) / 2. : xi[a] + p.h / 4. * (xj[a] - xi[a]);
+                    double xij = p.foqp ? (xi[a] + xj[a]) / 2. : xi[a] + h / 4. * (xj[a] - xi[a]);
                     xijxi[a] = xij - xi[a];
                 }
 #pragma unroll
@@ -874,7 +928,8 @@ __device__ __forceinline__ void rot3(const double *a, const double *b, double *L
 // one, bit for bit, so it is not recomputed.  Output slot order:
 // [mass, energy, px, py, pz].
 template <int D, bool ROOT5>
-__global__ void __launch_bounds__(128) k_faces(Params p, const GridInfo *__restrict__ gridp,
+__global__ void __launch_bounds__(128) k_faces(Params p, const Member *__restrict__ members,
+                                               const int *__restrict__ memberOf, const GridInfo *__restrict__ grids,
                                                const Prim *__restrict__ prim, const Geo *__restrict__ geo,
                                                const Grad *__restrict__ grad, const uint32_t *__restrict__ nbr,
                                                const double *__restrict__ psi, const int *__restrict__ faceTotal,
@@ -882,9 +937,7 @@ __global__ void __launch_bounds__(128) k_faces(Params p, const GridInfo *__restr
                                                double *__restrict__ Fface, unsigned long long *__restrict__ newtonSum,
                                                unsigned *__restrict__ status) {
     constexpr int NV = D + 2;
-    const GridInfo g = *gridp;
     const int nf = *faceTotal < p.faces_cap ? *faceTotal : p.faces_cap;
-    const double dt = *dtp;
     const RiemannConsts rc = make_riemann_consts(p.gamma, p.rtol, p.rmaxit);
     const double gamma = p.gamma;
     unsigned long long iters_local = 0;
@@ -893,6 +946,9 @@ __global__ void __launch_bounds__(128) k_faces(Params p, const GridInfo *__restr
         const FaceRef fr = faces[f];
         if (fr.i < 0 || fr.slot < 0) { st_local |= ST_ASYMMETRIC; continue; }
         const int i = fr.i;
+        const int mi = memberOf ? memberOf[i] : 0;
+        const double dt = dtp[mi];
+        const double h = members[mi].h;
         const size_t si = (size_t)i * p.K + fr.slot;
         const uint32_t e = nbr[si];
         const int j = (int)(e & IDX_MASK);
@@ -900,7 +956,8 @@ __global__ void __launch_bounds__(128) k_faces(Params p, const GridInfo *__restr
         const Prim pi = prim[i], pj = prim[j];
         const double Vi = geo[i].V, Vj = geo[j].V;
         double xi[3] = {pi.x, pi.y, pi.z}, xj[3];
-        neighbour_pos<D>(e, pj, g, p.h, xj);
+        if (img) neighbour_pos<D>(e, pj, grids[mi], h, xj);
+        else { xj[0] = pj.x; xj[1] = pj.y; xj[2] = pj.z; }
         // --- effective face
         double A[3] = {0., 0., 0.};
         {
@@ -924,7 +981,7 @@ __global__ void __launch_bounds__(128) k_faces(Params p, const GridInfo *__restr
                 xijxj[a] = .5 * (xi[a] - xj[a]);
                 xijxi[a] = .5 * (xj[a] - xi[a]);
             } else {
-                double xij = xi[a] + p.h / 4. * xjxi[a];
+                double xij = xi[a] + h / 4. * xjxi[a];
                 xijxi[a] = xij - xi[a];
                 xijxj[a] = xij - xj[a];
             }
@@ -1100,22 +1157,22 @@ __global__ void __launch_bounds__(128) k_faces(Params p, const GridInfo *__restr
 // the neighbour search overflowed, so that the host can retry the step with
 // more slots.
 template <int D>
-__global__ void __launch_bounds__(128) k_update(Params p, const GridInfo *__restrict__ gridp, const int *__restrict__ noi,
+__global__ void __launch_bounds__(128) k_update(Params p, const int *__restrict__ memberOf,
+                                                const GridInfo *__restrict__ grids, const int *__restrict__ noi,
                                                 const int *__restrict__ noiImg, const int *__restrict__ faceOf,
                                                 const double *__restrict__ Fface, const double *__restrict__ dtp,
                                                 double *__restrict__ x, double *__restrict__ y, double *__restrict__ z,
                                                 double *__restrict__ vx, double *__restrict__ vy, double *__restrict__ vz,
                                                 double *__restrict__ m, double *__restrict__ u, float4 *__restrict__ posf,
-                                                double *__restrict__ fluxSums, double *__restrict__ simTime,
-                                                int *__restrict__ stepsDone, unsigned *__restrict__ status) {
+                                                double *__restrict__ fluxSums, unsigned *__restrict__ status) {
     const unsigned st0 = *status;
     if (st0 & (ST_NGB_OVERFLOW | ST_CAPACITY)) return;
-    const GridInfo g = *gridp;
-    const double dt = *dtp;
     double *X[3] = {x, y, z};
     double *Vv[3] = {vx, vy, vz};
     unsigned st_local = 0;
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < p.n; i += gridDim.x * blockDim.x) {
+        const int sim = memberOf ? memberOf[i] : 0;
+        const double dt = dtp[sim];
         const size_t base = (size_t)i * p.K;
         const int tot = noi[i] + noiImg[i];
         double mF = 0., eF = 0., vF[3] = {0., 0., 0.};
@@ -1163,8 +1220,9 @@ __global__ void __launch_bounds__(128) k_update(Params p, const GridInfo *__rest
             if (p.move) {
                 xa += vo[a] * dt;
                 if (p.periodic) {
-                    if (xa < g.lo[a]) xa = g.hi[a] - (g.lo[a] - xa);
-                    else if (g.hi[a] <= xa) xa = g.lo[a] + (xa - g.hi[a]);
+                    const double lo = grids[sim].lo[a], hi = grids[sim].hi[a];
+                    if (xa < lo) xa = hi - (lo - xa);
+                    else if (hi <= xa) xa = lo + (xa - hi);
                 }
                 X[a][i] = xa;
             }
@@ -1174,10 +1232,16 @@ __global__ void __launch_bounds__(128) k_update(Params p, const GridInfo *__rest
     }
     for (int o = 16; o > 0; o >>= 1) st_local |= __shfl_xor_sync(0xffffffffu, st_local, o);
     if ((threadIdx.x & 31) == 0 && st_local) flag(status, st_local);
-    if (blockIdx.x == 0 && threadIdx.x == 0) {
-        *simTime += dt;
-        *stepsDone += 1;
-    }
+}
+
+// Simulation time of every member and the count of completed steps (skipped,
+// like the update, when the step is to be repeated with more capacity).
+__global__ void k_advance_time(int nmembers, const double *__restrict__ dt, double *__restrict__ simTime,
+                               int *__restrict__ stepsDone, const unsigned *__restrict__ status) {
+    if (*status & (ST_NGB_OVERFLOW | ST_CAPACITY)) return;
+    for (int mi = blockIdx.x * blockDim.x + threadIdx.x; mi < nmembers; mi += gridDim.x * blockDim.x)
+        simTime[mi] += dt[mi];
+    if (blockIdx.x == 0 && threadIdx.x == 0) *stepsDone += 1;
 }
 
 template <int D>
@@ -1199,14 +1263,15 @@ void launch_step(StepArgs &a) {
     auto tock = [&](int id) { if (a.timer) a.timer(a.timer_ctx, id, 1); };
 
     tick(KT_GRID);
-    k_bounds_partial<D><<<BOUNDS_BLOCKS, BOUNDS_T, 0, s>>>(a.x, a.y, a.z, p.n, a.boundsPart);
-    k_bounds_final<D><<<1, 32, 0, s>>>(a.x, a.y, a.z, a.boundsPart, BOUNDS_BLOCKS, p, a.grid, a.status);
+    k_bounds_partial<D><<<a.nmembers * a.bpm, BOUNDS_T, 0, s>>>(a.x, a.y, a.z, p, a.members, a.bpm, a.boundsPart);
+    k_bounds_final<D><<<1, 256, 0, s>>>(a.x, a.y, a.z, a.boundsPart, a.bpm, p, a.members, a.nmembers, a.grids,
+                                        a.cellTotal, a.status);
     cudaMemsetAsync(a.cellCount, 0, sizeof(int) * (size_t)(p.ncells_cap + 1), s);
     cudaMemsetAsync(a.cellFill, 0, sizeof(int) * (size_t)(p.ncells_cap + 1), s);
-    k_assign<D><<<blocksN, T, 0, s>>>(a.x, a.y, a.z, p.n, a.grid, a.cell, a.cellCount, a.status);
+    k_assign<D><<<blocksN, T, 0, s>>>(a.x, a.y, a.z, p.n, a.memberOf, a.grids, a.cell, a.cellCount, a.status);
     exclusive_scan(a.cellCount, p.ncells_cap, a.cellStart, a.scanTiles, a.scanTotal, s);
     k_fill_cells<<<blocksN, T, 0, s>>>(a.cell, p.n, a.cellStart, a.cellFill, a.cellList);
-    k_sort_cells<<<(p.ncells_cap + T - 1) / T, T, 0, s>>>(a.grid, a.cellStart, a.cellList);
+    k_sort_cells<<<(p.ncells_cap + T - 1) / T, T, 0, s>>>(a.cellTotal, a.cellStart, a.cellList);
     tock(KT_GRID);
 
     tick(KT_NNS);
@@ -1217,20 +1282,21 @@ void launch_step(StepArgs &a) {
         if (smem > 48 * 1024)
             cudaFuncSetAttribute(k_neighbours<D>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
         k_neighbours<D><<<blocks, NNS_WARPS * 32, smem, s>>>(
-            p, a.grid, a.x, a.y, a.z, a.posf, a.vx, a.vy, a.vz, a.m, a.u, a.cell, a.cellStart, a.cellList, a.nbr,
-            a.rr, a.ww, a.noi, a.noiImg, a.faceCnt, a.prim, a.geo, a.status);
+            p, a.members, a.memberOf, a.grids, a.x, a.y, a.z, a.posf, a.vx, a.vy, a.vz, a.m, a.u, a.cell,
+            a.cellStart, a.cellList, a.nbr, a.rr, a.ww, a.noi, a.noiImg, a.faceCnt, a.prim, a.geo, a.status);
     }
     tock(KT_NNS);
 
     tick(KT_DT);
-    cudaMemsetAsync(a.dtbits, 0xff, sizeof(unsigned long long), s);
-    k_timestep<D><<<(p.n + 255) / 256, 256, 0, s>>>(p, a.prim, a.geo, a.nbr, a.rr, a.noi, a.dtbits);
-    k_dt_final<<<1, 1, 0, s>>>(p, a.dtbits, a.dt_max, a.dt);
+    cudaMemsetAsync(a.dtbits, 0xff, sizeof(unsigned long long) * (size_t)a.nmembers, s);
+    k_timestep<D><<<(p.n + 255) / 256, 256, 0, s>>>(p, a.members, a.memberOf, a.prim, a.geo, a.nbr, a.rr, a.noi,
+                                                    a.dtbits);
+    k_dt_final<<<(a.nmembers + 127) / 128, 128, 0, s>>>(p, a.nmembers, a.dtbits, a.dt_max, a.dt);
     tock(KT_DT);
 
     tick(KT_GRAD);
-    k_gradients<D><<<blocksN, T, 0, s>>>(p, a.grid, a.prim, a.geo, a.nbr, a.ww, a.noi, a.noiImg, a.grad, a.gradRaw,
-                                         a.psi);
+    k_gradients<D><<<blocksN, T, 0, s>>>(p, a.members, a.memberOf, a.grids, a.prim, a.geo, a.nbr, a.ww, a.noi,
+                                         a.noiImg, a.grad, a.gradRaw, a.psi);
     tock(KT_GRAD);
 
     tick(KT_LINK);
@@ -1241,27 +1307,32 @@ void launch_step(StepArgs &a) {
 
     tick(KT_FACES);
     if (a.root5)
-        k_faces<D, true><<<a.face_blocks, T, 0, s>>>(p, a.grid, a.prim, a.geo, a.grad, a.nbr, a.psi, a.faceOff + p.n,
-                                                     a.faces, a.dt, a.Fface, a.newtonSum, a.status);
+        k_faces<D, true><<<a.face_blocks, T, 0, s>>>(p, a.members, a.memberOf, a.grids, a.prim, a.geo, a.grad, a.nbr,
+                                                     a.psi, a.faceOff + p.n, a.faces, a.dt, a.Fface, a.newtonSum,
+                                                     a.status);
     else
-        k_faces<D, false><<<a.face_blocks, T, 0, s>>>(p, a.grid, a.prim, a.geo, a.grad, a.nbr, a.psi, a.faceOff + p.n,
-                                                      a.faces, a.dt, a.Fface, a.newtonSum, a.status);
+        k_faces<D, false><<<a.face_blocks, T, 0, s>>>(p, a.members, a.memberOf, a.grids, a.prim, a.geo, a.grad, a.nbr,
+                                                      a.psi, a.faceOff + p.n, a.faces, a.dt, a.Fface, a.newtonSum,
+                                                      a.status);
     tock(KT_FACES);
 
     tick(KT_UPDATE);
-    k_update<D><<<blocksN, T, 0, s>>>(p, a.grid, a.noi, a.noiImg, a.faceOf, a.Fface, a.dt, a.x, a.y, a.z, a.vx, a.vy,
-                                      a.vz, a.m, a.u, a.posf, a.fluxSums, a.simTime, a.stepsDone, a.status);
+    k_update<D><<<blocksN, T, 0, s>>>(p, a.memberOf, a.grids, a.noi, a.noiImg, a.faceOf, a.Fface, a.dt, a.x, a.y,
+                                      a.z, a.vx, a.vy, a.vz, a.m, a.u, a.posf, a.fluxSums, a.status);
+    k_advance_time<<<(a.nmembers + 127) / 128, 128, 0, s>>>(a.nmembers, a.dt, a.simTime, a.stepsDone, a.status);
     tock(KT_UPDATE);
 }
 
-void launch_grid_bounds(const double *x, const double *y, const double *z, const Params &p, double *partials,
-                        GridInfo *grid, unsigned *status, cudaStream_t s) {
+void launch_grid_bounds(const double *x, const double *y, const double *z, const Params &p,
+                        const Member *members, int nmembers, int bpm, double *partials, GridInfo *grids,
+                        int *cellTotal, unsigned *status, cudaStream_t s) {
+    const int blocks = nmembers * bpm;
     if (p.dim == 2) {
-        k_bounds_partial<2><<<BOUNDS_BLOCKS, BOUNDS_T, 0, s>>>(x, y, z, p.n, partials);
-        k_bounds_final<2><<<1, 32, 0, s>>>(x, y, z, partials, BOUNDS_BLOCKS, p, grid, status);
+        k_bounds_partial<2><<<blocks, BOUNDS_T, 0, s>>>(x, y, z, p, members, bpm, partials);
+        k_bounds_final<2><<<1, 256, 0, s>>>(x, y, z, partials, bpm, p, members, nmembers, grids, cellTotal, status);
     } else {
-        k_bounds_partial<3><<<BOUNDS_BLOCKS, BOUNDS_T, 0, s>>>(x, y, z, p.n, partials);
-        k_bounds_final<3><<<1, 32, 0, s>>>(x, y, z, partials, BOUNDS_BLOCKS, p, grid, status);
+        k_bounds_partial<3><<<blocks, BOUNDS_T, 0, s>>>(x, y, z, p, members, bpm, partials);
+        k_bounds_final<3><<<1, 256, 0, s>>>(x, y, z, partials, bpm, p, members, nmembers, grids, cellTotal, status);
     }
 }
 

@@ -21,8 +21,14 @@ struct StepArgs {
     // state (structure of arrays)
     double *x, *y, *z, *vx, *vy, *vz, *m, *u;
     float4 *posf;
-    // grid
-    GridInfo *grid;
+    // simulations (members) of the context
+    int nmembers;
+    int bpm;                   // bounding-box blocks per member
+    const Member *members;
+    const int *memberOf;       // per particle; nullptr when nmembers == 1
+    // grids, one per member
+    GridInfo *grids;
+    int *cellTotal;
     double *boundsPart;
     int *cell, *cellCount, *cellStart, *cellFill, *cellList;
     // neighbours
@@ -46,14 +52,17 @@ struct StepArgs {
     void *timer_ctx;
 };
 
-// blocks of the bounding-box reduction; its scratch holds 6 doubles per block
+// blocks of the bounding-box reduction of a single simulation; its scratch
+// holds 6 doubles per block
 constexpr int BOUNDS_BLOCKS = 304;
 
 void step(StepArgs &a);
 // Particles::getDomainLimits + Domain::createGrid alone: per-block partial
-// minima/maxima in `partials` (BOUNDS_BLOCKS * 6 doubles), result in `grid`.
-void launch_grid_bounds(const double *x, const double *y, const double *z, const Params &p, double *partials,
-                        GridInfo *grid, unsigned *status, cudaStream_t s);
+// minima/maxima in `partials` (nmembers * bpm * 6 doubles), one GridInfo per
+// member in `grids`, the concatenated cell count in `cellTotal`.
+void launch_grid_bounds(const double *x, const double *y, const double *z, const Params &p,
+                        const Member *members, int nmembers, int bpm, double *partials, GridInfo *grids,
+                        int *cellTotal, unsigned *status, cudaStream_t s);
 void pack_posf(const double *x, const double *y, const double *z, int n, int dim, float4 *posf, cudaStream_t s);
 void exclusive_scan(const int *in, int n, int *out, int *tile_buf, int *total, cudaStream_t s);
 const char *kernel_timer_name(int id);

@@ -23,12 +23,15 @@ namespace {
 
 // 16 KiB of scratch on every device that loads the library, kept until exit:
 // BOUNDS_BLOCKS * 6 doubles of per-block partials, then the GridInfo result,
-// then the status word.
+// the status word, the simulation's parameters and the cell count, each on a
+// 256-byte boundary.
 constexpr size_t SCRATCH_BYTES = 16384;
 constexpr size_t PARTIALS_BYTES = sizeof(double) * 6 * BOUNDS_BLOCKS;
 constexpr size_t GRID_OFFSET = (PARTIALS_BYTES + 255) / 256 * 256;
 constexpr size_t STATUS_OFFSET = GRID_OFFSET + (sizeof(GridInfo) + 255) / 256 * 256;
-static_assert(STATUS_OFFSET + sizeof(unsigned) <= SCRATCH_BYTES, "scratch too small");
+constexpr size_t MEMBER_OFFSET = STATUS_OFFSET + 256;
+constexpr size_t CELLS_OFFSET = MEMBER_OFFSET + (sizeof(Member) + 255) / 256 * 256;
+static_assert(CELLS_OFFSET + sizeof(int) <= SCRATCH_BYTES, "scratch too small");
 
 static __device__ __align__(256) unsigned char g_scratch[SCRATCH_BYTES];
 
@@ -61,6 +64,10 @@ int scratch_address(void **out) {
     return 0;
 }
 
+__global__ void k_set_member(Member m, Member *__restrict__ dst) {
+    if (threadIdx.x == 0 && blockIdx.x == 0) *dst = m;
+}
+
 __global__ void k_grid_to_doubles(const GridInfo *__restrict__ g, int dim, double *__restrict__ out) {
     if (threadIdx.x != 0 || blockIdx.x != 0) return;
     for (int a = 0; a < 3; ++a) {
@@ -90,6 +97,8 @@ extern "C" int mlh_grid_bounds_noalloc(int dim, int periodic, int n, const doubl
     double *partials = (double *)base;
     GridInfo *grid = (GridInfo *)((unsigned char *)base + GRID_OFFSET);
     unsigned *status = (unsigned *)((unsigned char *)base + STATUS_OFFSET);
+    Member *member = (Member *)((unsigned char *)base + MEMBER_OFFSET);
+    int *cellTotal = (int *)((unsigned char *)base + CELLS_OFFSET);
 
     Params p;
     std::memset(&p, 0, sizeof(p));
@@ -106,7 +115,14 @@ extern "C" int mlh_grid_bounds_noalloc(int dim, int periodic, int n, const doubl
     // the partials and the GridInfo are overwritten completely
     cudaError_t e = cudaMemsetAsync(status, 0, sizeof(unsigned), s);
     if (e != cudaSuccess) { g_error = std::string("cudaMemsetAsync: ") + cudaGetErrorString(e); return MLH_ERR_CUDA; }
-    launch_grid_bounds(x, y, dim == 3 ? z : x, p, partials, grid, status, s);
+    Member mb;
+    std::memset(&mb, 0, sizeof(mb));
+    mb.h = kernel_size;
+    mb.first = 0;
+    mb.count = n;
+    for (int a = 0; a < 3; ++a) { mb.box_lo[a] = p.box_lo[a]; mb.box_hi[a] = p.box_hi[a]; }
+    k_set_member<<<1, 1, 0, s>>>(mb, member);
+    launch_grid_bounds(x, y, dim == 3 ? z : x, p, member, 1, BOUNDS_BLOCKS, partials, grid, cellTotal, status, s);
     k_grid_to_doubles<<<1, 1, 0, s>>>(grid, dim, grid_out);
     unsigned st = 0;
     e = cudaMemcpyAsync(&st, status, sizeof(unsigned), cudaMemcpyDeviceToHost, s);

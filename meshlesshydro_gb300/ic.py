@@ -151,3 +151,27 @@ def sedov(n_side: int = 64, seed: int = 2, jitter: float = 0.05, energy: float =
                        (-0.5, -0.5, -0.5), (0.5, 0.5, 0.5), gamma,
                        {"setup": "sedov", "n_side": n_side, "seed": seed, "jitter": jitter,
                         "energy": energy, "p_background": p_background, "periodic": periodic})
+
+
+def concatenate(members) -> ParticleSet:
+    """The particle sets of an ensemble stored back to back (member order)."""
+    first = members[0]
+    cat = [np.concatenate([getattr(m, k) for m in members]) for k in ("x", "y", "z", "vx", "vy", "vz", "m", "u")]
+    return ParticleSet(first.dim, *cat, first.kernel_size, first.box_lo, first.box_hi, first.gamma,
+                       {"setup": "ensemble", "members": len(members)})
+
+
+def kh_ensemble(n_members: int = 256, seed: int = 7, n_min: int = 2500, n_max: int = 40000,
+                amp_min: float = 0.005, amp_max: float = 0.05):
+    """Uneven ensemble of 2D Kelvin-Helmholtz runs: particle counts drawn
+    log-uniformly in [n_min, n_max] (lattice side round(sqrt(N)), so N := side^2),
+    vy amplitude uniform in [amp_min, amp_max], kernelSize 2.5231 spacings each."""
+    rng = np.random.default_rng(seed)
+    logn = rng.uniform(math.log(n_min), math.log(n_max), n_members)
+    amps = rng.uniform(amp_min, amp_max, n_members)
+    out = []
+    for k in range(n_members):
+        side = int(round(math.sqrt(math.exp(logn[k]))))
+        out.append(kelvin_helmholtz(n_side=side, seed=seed * 100003 + k, amplitude=float(amps[k])))
+    return out
+

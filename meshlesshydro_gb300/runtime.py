@@ -34,6 +34,12 @@ class MLHError(RuntimeError):
         self.status = status
 
 
+class MemberDesc(ctypes.Structure):
+    """mlh_member: one simulation of an ensemble."""
+    _fields_ = [("n", ctypes.c_int), ("kernel_size", ctypes.c_double),
+                ("box_lo", ctypes.c_double * 3), ("box_hi", ctypes.c_double * 3)]
+
+
 class ParticlesView(ctypes.Structure):
     _fields_ = [("n", ctypes.c_int)] + [(k, ctypes.POINTER(ctypes.c_double))
                                          for k in ("x", "y", "z", "vx", "vy", "vz", "m", "u")]
@@ -49,7 +55,7 @@ class StepStats(ctypes.Structure):
 EXPORTS = ["mlh_abi_version", "mlh_last_error", "mlh_create", "mlh_destroy", "mlh_set_fields",
            "mlh_get_fields", "mlh_step", "mlh_stage_array", "mlh_set_kernel_timing",
            "mlh_kernel_times", "mlh_reset_kernel_times", "mlh_probe_fp64_tflops",
-           "mlh_grid_bounds_noalloc"]
+           "mlh_grid_bounds_noalloc", "mlh_ensemble_create", "mlh_member_times", "mlh_set_graph_mode"]
 
 _lib = None
 
@@ -89,6 +95,13 @@ def load(path: str = LIB_PATH):
                                           ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_double),
                                           ctypes.c_double, dp, dp]
     L.mlh_grid_bounds_noalloc.restype = ctypes.c_int
+    L.mlh_ensemble_create.argtypes = [ctypes.POINTER(CConfig), ctypes.c_int, ctypes.POINTER(MemberDesc),
+                                      ctypes.POINTER(ParticlesView), ctypes.POINTER(vp)]
+    L.mlh_ensemble_create.restype = ctypes.c_int
+    L.mlh_member_times.argtypes = [vp, ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_double), ctypes.c_int]
+    L.mlh_member_times.restype = ctypes.c_int
+    L.mlh_set_graph_mode.argtypes = [vp, ctypes.c_int]
+    L.mlh_set_graph_mode.restype = ctypes.c_int
     _lib = L
     return L
 
@@ -124,20 +137,57 @@ def probe_fp64_tflops(seconds: float = 0.5) -> float:
 
 
 class Simulation:
-    """One MFV simulation on the GPU through the C ABI."""
+    """One MFV simulation on the GPU through the C ABI.
 
-    def __init__(self, cfg: MFVConfig, pset):
+    With `members` (a list of ParticleSets) the context is an ensemble of
+    independent simulations stored back to back (mlh_ensemble_create); `pset`
+    is then ignored and the state arrays are the concatenation.
+    """
+
+    def __init__(self, cfg: MFVConfig, pset=None, members=None):
         self.L = load()
         self.cfg = cfg
         self._cfg = to_struct(cfg)
-        self.host = HostState(pset)
-        self.n = pset.n
         self.dim = cfg.dim
         h = ctypes.c_void_p()
-        st = self.L.mlh_create(ctypes.byref(self._cfg), ctypes.byref(self.host.view), ctypes.byref(h))
+        if members is None:
+            self.host = HostState(pset)
+            self.n = pset.n
+            self.nmembers = 1
+            st = self.L.mlh_create(ctypes.byref(self._cfg), ctypes.byref(self.host.view), ctypes.byref(h))
+            where = "mlh_create"
+        else:
+            from .ic import concatenate
+            allp = concatenate(members)
+            self.host = HostState(allp)
+            self.n = allp.n
+            self.nmembers = len(members)
+            self.member_sizes = [m.n for m in members]
+            descs = (MemberDesc * len(members))()
+            for k, m in enumerate(members):
+                descs[k].n = m.n
+                descs[k].kernel_size = m.kernel_size
+                for a in range(3):
+                    descs[k].box_lo[a] = float(m.box_lo[a])
+                    descs[k].box_hi[a] = float(m.box_hi[a])
+            st = self.L.mlh_ensemble_create(ctypes.byref(self._cfg), len(members), descs,
+                                            ctypes.byref(self.host.view), ctypes.byref(h))
+            where = "mlh_ensemble_create"
         if st != 0:
-            raise MLHError(st, "mlh_create", self.L.mlh_last_error().decode())
+            raise MLHError(st, where, self.L.mlh_last_error().decode())
         self.h = h
+
+    def member_times(self):
+        dt = np.zeros(self.nmembers)
+        t = np.zeros(self.nmembers)
+        st = self.L.mlh_member_times(self.h, dt.ctypes.data_as(ctypes.POINTER(ctypes.c_double)),
+                                     t.ctypes.data_as(ctypes.POINTER(ctypes.c_double)), self.nmembers)
+        if st != 0:
+            raise MLHError(st, "mlh_member_times", self.L.mlh_last_error().decode())
+        return dt, t
+
+    def set_graph_mode(self, on: bool):
+        self.L.mlh_set_graph_mode(self.h, 1 if on else 0)
 
     def step(self, nsteps: int = 1, dt_max: float = 0.0, check: bool = True) -> StepStats:
         stats = StepStats()
