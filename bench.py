@@ -34,6 +34,8 @@ WORKLOADS = {
     "sedov128": dict(kind="sedov", n_side=128, periodic=True),
     "sedov64": dict(kind="sedov", n_side=64, periodic=True),
     "kh100": dict(kind="kh", n_side=100),
+    # 256 independent 2D KH runs, N log-uniform in [2500, 40000], one context
+    "kh_ens256": dict(kind="ensemble", members=256),
 }
 METRIC = "particle-updates/s per MFV step on 1 GB300"
 LAUNCHES_PER_STEP = 18   # kernels launched by one mlh_step iteration (see csrc/mlh_kernels.cu)
@@ -51,6 +53,9 @@ def make_workload(name: str, seed_offset: int = 0):
     from meshlesshydro_gb300 import ic
     from meshlesshydro_gb300.config import MFVConfig
     w = WORKLOADS[name]
+    if w["kind"] == "ensemble":
+        members = ic.kh_ensemble(n_members=w["members"], seed=7 + seed_offset)
+        return members, MFVConfig.kelvin_helmholtz(members[0])
     if w["kind"] == "sedov":
         p = ic.sedov(n_side=w["n_side"], seed=2 + seed_offset)
         return p, MFVConfig.sedov(p, periodic=w["periodic"])
@@ -141,17 +146,24 @@ def cpu_model():
     return "unknown"
 
 
-def cpu_baseline_sample(seconds_hint: float = 20.0):
+def cpu_baseline_sample(seconds_hint: float = 20.0, kind: str = "sedov"):
     """The oracle (serial CPU restatement of the reference) on a bounded sample:
     whole MFV steps of the 32^3 Sedov lattice with the workload's particle
-    density and neighbour count (same per-particle work as 128^3)."""
+    density and neighbour count (same per-particle work as 128^3), or of the
+    100x100 Kelvin-Helmholtz set-up for the 2D workloads."""
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     import oracle
     from meshlesshydro_gb300 import ic
     from meshlesshydro_gb300.config import MFVConfig
     oracle.build()
-    p = ic.sedov(n_side=32, seed=2)
-    cfg = MFVConfig.sedov(p, periodic=True)
+    if kind == "sedov":
+        p = ic.sedov(n_side=32, seed=2)
+        cfg = MFVConfig.sedov(p, periodic=True)
+        what = "32^3 periodic Sedov lattice"
+    else:
+        p = ic.kelvin_helmholtz(n_side=100, seed=1)
+        cfg = MFVConfig.kelvin_helmholtz(p)
+        what = "100x100 Kelvin-Helmholtz set-up"
     o = oracle.Oracle(cfg, p)
     o.step()  # warm-up
     steps, t0 = 0, time.perf_counter()
@@ -162,8 +174,8 @@ def cpu_baseline_sample(seconds_hint: float = 20.0):
         if el >= seconds_hint or steps >= 50:
             break
     return {"value": p.n * steps / el, "unit": "particle-updates/s", "cores": 1, "kind": "port",
-            "sample": f"{steps} MFV steps of the 32^3 periodic Sedov lattice ({p.n} particles, same h/dx and "
-                      f"~32 neighbours as the 128^3 workload), serial oracle, {el:.1f} s, host {cpu_model()}"}
+            "sample": f"{steps} MFV steps of the {what} ({p.n} particles, the workload's h/dx and neighbour "
+                      f"count), serial oracle, {el:.1f} s, host {cpu_model()}"}
 
 
 def run_reference(args):
@@ -217,7 +229,12 @@ def run_mlh(args):
     build.build()
     fp64_peak = runtime.probe_fp64_tflops(0.5)
     p, cfg = make_workload(args.workload, seed_offset=rank)
-    sim = runtime.Simulation(cfg, p)
+    ensemble = WORKLOADS[args.workload]["kind"] == "ensemble"
+    members = p if ensemble else None
+    sim = runtime.Simulation(cfg, members=members) if ensemble else runtime.Simulation(cfg, p)
+    if ensemble:
+        p = sim.host  # concatenated state: .n
+    tuning = None if args.no_autotune else sim.autotune(1)
     sim.step(args.warmup)
     sim.reset_kernel_times()
     sim.set_kernel_timing(True)
@@ -241,6 +258,37 @@ def run_mlh(args):
     kt = sim.kernel_times()
     faces_per_step = st.faces / max(st.steps, 1)
     pairs_per_step = st.pair_interactions / max(st.steps, 1)
+
+    extra = {}
+    if ensemble:
+        # the same steps in graph mode (one CUDA graph per step), and the
+        # members run one after another as separate plain simulations
+        sim.set_graph_mode(True)
+        sim.step(1)
+        torch.cuda.synchronize()
+        stg = sim.step(args.steps)
+        graph_value = ws * p.n * stg.steps / (stg.device_ms / 1e3)
+        sim.set_graph_mode(False)
+        seq_steps = 2
+        from meshlesshydro_gb300.config import MFVConfig
+        sims = [runtime.Simulation(MFVConfig.kelvin_helmholtz(m), m) for m in members]
+        for s_ in sims:
+            s_.step(1)
+        torch.cuda.synchronize()
+        t0s = time.perf_counter()
+        for _ in range(seq_steps):
+            for s_ in sims:
+                s_.step(1)
+        torch.cuda.synchronize()
+        seq_wall = time.perf_counter() - t0s
+        seq_value = p.n * seq_steps / seq_wall
+        del sims
+        extra = {"ensemble": {"members": len(members), "particles": p.n,
+                              "batched_graph_value": graph_value,
+                              "sequential_value": seq_value,
+                              "sequential": "each member its own context, one mlh_step(1) call per member per step, "
+                                            f"{seq_steps} steps, wall clock",
+                              "batched_over_sequential": graph_value / seq_value}}
 
     # end to end through the C ABI with host buffers: H2D of the state,
     # one step, D2H of the state, every step (pinned host memory)
@@ -302,12 +350,15 @@ def run_mlh(args):
             "kernel_ms_per_step": {k: v[1] / max(v[0], 1) for k, v in kt.items()},
             "roofline": roofline,
             "clocks": ck,
+            "tuning": tuning,
+            **extra,
             "e2e": {"value": ws * n * e2e_steps / e2e_wall, "unit": "particle-updates/s",
                     "h2d_bytes_per_step": used * 8 * n, "d2h_bytes_per_step": used * 8 * n,
                     "steps": e2e_steps},
             "peaks": {"source": peak_kind, "hbm_gbs": peaks.get("hbm_gbs")}}
     if not args.no_cpu_baseline:
-        line["cpu_baseline"] = cpu_baseline_sample(args.cpu_seconds)
+        line["cpu_baseline"] = cpu_baseline_sample(args.cpu_seconds,
+                                                   "sedov" if WORKLOADS[args.workload]["kind"] == "sedov" else "kh")
     print(json.dumps(line), flush=True)
     if dist:
         dist.barrier()
@@ -323,6 +374,7 @@ def main():
     ap.add_argument("--workload", default="sedov128", choices=sorted(WORKLOADS))
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
+    ap.add_argument("--no-autotune", action="store_true")
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference(args)

@@ -121,6 +121,20 @@ int mlh_ensemble_create(const mlh_config *cfg, int nmembers, const mlh_member *m
 /* dt of the last step and simulation time of every member (host arrays of
  * nmembers doubles, either may be NULL). */
 int mlh_member_times(mlh_ctx *ctx, double *dt, double *time, int nmembers);
+/* Launch shapes of the step's main kernels. */
+typedef struct mlh_tuning {
+    int face_threads;        /* threads per block, Riemann face kernel */
+    int face_blocks_per_sm;  /* blocks per SM of its grid-stride loop */
+    int grad_threads;        /* threads per block, gradient/limiter kernel */
+    int nns_warps_per_sm;    /* warps per SM of the neighbour search */
+} mlh_tuning;
+
+/* Autotuner: times candidate launch shapes of the face, gradient and
+ * neighbour kernels over `trial_steps` steps each (from a saved copy of the
+ * state, which is restored afterwards), keeps the fastest in the context and
+ * reports them in *out (may be NULL).  Needs one state-sized temporary. */
+int mlh_autotune(mlh_ctx *ctx, int trial_steps, mlh_tuning *out);
+
 /* Graph mode: mlh_step captures one step into a CUDA graph (once, and again
  * after a capacity change) and replays it; kernel timing bypasses it. */
 int mlh_set_graph_mode(mlh_ctx *ctx, int enable);

@@ -81,6 +81,7 @@ struct mlh_ctx {
     int *stepsDone = nullptr;
     int *scanTiles = nullptr, *scanTotal = nullptr;
     bool debug_arrays = true;
+    Tuning tune;
     // CUDA graph of one step, replayed by mlh_step in graph mode
     bool graph_mode = false;
     cudaGraphExec_t graph_exec = nullptr;
@@ -198,6 +199,7 @@ StepArgs make_args(mlh_ctx *c, double dt_max) {
     std::memset(&a, 0, sizeof(a));
     a.p = c->p;
     a.stream = c->stream;
+    a.tune = c->tune;
     a.face_blocks = c->sm_count * 8;
     a.sm_count = c->sm_count;
     a.faces_cap = c->faces_cap;
@@ -513,6 +515,102 @@ int mlh_step(mlh_ctx *c, int nsteps, double dt_max, mlh_step_stats *stats) {
         stats->device_ms = dev_ms;
     }
     return (int)(accumulated & ~(unsigned)MLH_ERR_NGB_OVERFLOW & ~ST_CAPACITY) ? (int)accumulated : 0;
+}
+
+// Coordinate search over the launch shapes: each candidate runs `trial_steps`
+// steps with per-kernel timing from a saved copy of the state, which is put
+// back afterwards (positions, velocities, masses, energies, member times).
+int mlh_autotune(mlh_ctx *c, int trial_steps, mlh_tuning *out) {
+    if (!c || trial_steps < 1) { g_last_error = "invalid argument"; return MLH_ERR_INVALID; }
+    const size_t n = (size_t)c->n, nm = (size_t)c->nmembers;
+    double *save = nullptr;
+    CK(cudaMalloc(&save, sizeof(double) * (8 * n + 2 * nm)));
+    double *src[8] = {c->x, c->y, c->z, c->vx, c->vy, c->vz, c->m, c->u};
+    for (int k = 0; k < 8; ++k) CK(cudaMemcpyAsync(save + k * n, src[k], sizeof(double) * n, cudaMemcpyDeviceToDevice, c->stream));
+    CK(cudaMemcpyAsync(save + 8 * n, c->simTime, sizeof(double) * nm, cudaMemcpyDeviceToDevice, c->stream));
+    CK(cudaMemcpyAsync(save + 8 * n + nm, c->dt, sizeof(double) * nm, cudaMemcpyDeviceToDevice, c->stream));
+    const bool timing0 = c->timing, graph0 = c->graph_mode;
+    c->graph_mode = false;
+    drop_graph(c);
+    auto restore = [&]() -> int {
+        for (int k = 0; k < 8; ++k) CK(cudaMemcpyAsync(src[k], save + k * n, sizeof(double) * n, cudaMemcpyDeviceToDevice, c->stream));
+        CK(cudaMemcpyAsync(c->simTime, save + 8 * n, sizeof(double) * nm, cudaMemcpyDeviceToDevice, c->stream));
+        CK(cudaMemcpyAsync(c->dt, save + 8 * n + nm, sizeof(double) * nm, cudaMemcpyDeviceToDevice, c->stream));
+        pack_posf(c->x, c->y, c->z, c->n, c->cfg.dim, c->posf, c->stream);
+        return 0;
+    };
+    // time of kernel `id` over trial_steps steps with the current tuning
+    auto trial = [&](int id, double &ms) -> int {
+        if (int rc = restore()) return rc;
+        c->timing = true;
+        mlh_reset_kernel_times(c);
+        mlh_step_stats st;
+        int rc = mlh_step(c, trial_steps, 0., &st);
+        c->timing = false;
+        if (rc & (MLH_ERR_CUDA | MLH_ERR_INVALID)) return rc;
+        ms = c->kt_ms[id];
+        return 0;
+    };
+    int rc = 0;
+    {   // warm-up so that buffers have reached their final capacity
+        double dummy;
+        if ((rc = trial(KT_FACES, dummy))) goto done;
+    }
+    {
+        const int cand_t[] = {64, 128, 256};
+        const int cand_b[] = {2, 4, 8, 16, 32};
+        Tuning best = c->tune;
+        double best_ms = 1e300;
+        for (int t : cand_t) {
+            c->tune.face_threads = t;
+            c->tune.face_blocks_per_sm = best.face_blocks_per_sm;
+            double ms;
+            if ((rc = trial(KT_FACES, ms))) goto done;
+            if (ms < best_ms) { best_ms = ms; best.face_threads = t; }
+        }
+        c->tune.face_threads = best.face_threads;
+        for (int b : cand_b) {
+            c->tune.face_blocks_per_sm = b;
+            double ms;
+            if ((rc = trial(KT_FACES, ms))) goto done;
+            if (ms < best_ms) { best_ms = ms; best.face_blocks_per_sm = b; }
+        }
+        c->tune.face_blocks_per_sm = best.face_blocks_per_sm;
+        best_ms = 1e300;
+        for (int t : cand_t) {
+            c->tune.grad_threads = t;
+            double ms;
+            if ((rc = trial(KT_GRAD, ms))) goto done;
+            if (ms < best_ms) { best_ms = ms; best.grad_threads = t; }
+        }
+        c->tune.grad_threads = best.grad_threads;
+        best_ms = 1e300;
+        const int cand_w[] = {16, 32, 64, 128};
+        for (int w : cand_w) {
+            c->tune.nns_warps_per_sm = w;
+            double ms;
+            if ((rc = trial(KT_NNS, ms))) goto done;
+            if (ms < best_ms) { best_ms = ms; best.nns_warps_per_sm = w; }
+        }
+        c->tune.nns_warps_per_sm = best.nns_warps_per_sm;
+    }
+done:
+    {
+        int rc2 = restore();
+        CK(cudaStreamSynchronize(c->stream));
+        cudaFree(save);
+        c->timing = timing0;
+        c->graph_mode = graph0;
+        mlh_reset_kernel_times(c);
+        if (!rc) rc = rc2;
+    }
+    if (out) {
+        out->face_threads = c->tune.face_threads;
+        out->face_blocks_per_sm = c->tune.face_blocks_per_sm;
+        out->grad_threads = c->tune.grad_threads;
+        out->nns_warps_per_sm = c->tune.nns_warps_per_sm;
+    }
+    return rc;
 }
 
 int mlh_set_graph_mode(mlh_ctx *c, int enable) {

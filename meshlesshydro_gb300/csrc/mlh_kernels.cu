@@ -681,7 +681,7 @@ __device__ __forceinline__ double field_of(const Prim &q, int f) {
 }
 
 template <int D>
-__global__ void __launch_bounds__(128) k_gradients(Params p, const Member *__restrict__ members,
+__global__ void __launch_bounds__(256) k_gradients(Params p, const Member *__restrict__ members,
                                                    const int *__restrict__ memberOf, const GridInfo *__restrict__ grids,
                                                    const Prim *__restrict__ prim, Geo *__restrict__ geo,
                                                    const uint32_t *__restrict__ nbr, const double *__restrict__ ww,
@@ -820,7 +820,7 @@ __global__ void __launch_bounds__(128) k_gradients(Params p, const Member *__res
 // copied with the opposite sign), face -> (i, slot, reverse slot).  The
 // reverse slot of a non-canonical slot is the first entry of j's list (real
 // part or image part) that refers to i, as in the reference's searches.
-__global__ void __launch_bounds__(128) k_link(Params p, const uint32_t *__restrict__ nbr, const int *__restrict__ noi,
+__global__ void __launch_bounds__(256) k_link(Params p, const uint32_t *__restrict__ nbr, const int *__restrict__ noi,
                                               const int *__restrict__ noiImg, const int *__restrict__ faceOff,
                                               int *__restrict__ faceOf, FaceRef *__restrict__ faces,
                                               unsigned *__restrict__ status) {
@@ -928,7 +928,7 @@ __device__ __forceinline__ void rot3(const double *a, const double *b, double *L
 // one, bit for bit, so it is not recomputed.  Output slot order:
 // [mass, energy, px, py, pz].
 template <int D, bool ROOT5>
-__global__ void __launch_bounds__(128) k_faces(Params p, const Member *__restrict__ members,
+__global__ void __launch_bounds__(256) k_faces(Params p, const Member *__restrict__ members,
                                                const int *__restrict__ memberOf, const GridInfo *__restrict__ grids,
                                                const Prim *__restrict__ prim, const Geo *__restrict__ geo,
                                                const Grad *__restrict__ grad, const uint32_t *__restrict__ nbr,
@@ -1157,7 +1157,7 @@ __global__ void __launch_bounds__(128) k_faces(Params p, const Member *__restric
 // the neighbour search overflowed, so that the host can retry the step with
 // more slots.
 template <int D>
-__global__ void __launch_bounds__(128) k_update(Params p, const int *__restrict__ memberOf,
+__global__ void __launch_bounds__(256) k_update(Params p, const int *__restrict__ memberOf,
                                                 const GridInfo *__restrict__ grids, const int *__restrict__ noi,
                                                 const int *__restrict__ noiImg, const int *__restrict__ faceOf,
                                                 const double *__restrict__ Fface, const double *__restrict__ dtp,
@@ -1276,7 +1276,7 @@ void launch_step(StepArgs &a) {
 
     tick(KT_NNS);
     {
-        const int warps_total = a.sm_count * 64;   // grid-stride over particles, one warp each
+        const int warps_total = a.sm_count * a.tune.nns_warps_per_sm;   // grid-stride, one warp per particle
         const int blocks = (warps_total + NNS_WARPS - 1) / NNS_WARPS;
         const size_t smem = nns_smem_bytes(p.K);
         if (smem > 48 * 1024)
@@ -1295,7 +1295,8 @@ void launch_step(StepArgs &a) {
     tock(KT_DT);
 
     tick(KT_GRAD);
-    k_gradients<D><<<blocksN, T, 0, s>>>(p, a.members, a.memberOf, a.grids, a.prim, a.geo, a.nbr, a.ww, a.noi,
+    const int gT = a.tune.grad_threads;
+    k_gradients<D><<<(p.n + gT - 1) / gT, gT, 0, s>>>(p, a.members, a.memberOf, a.grids, a.prim, a.geo, a.nbr, a.ww, a.noi,
                                          a.noiImg, a.grad, a.gradRaw, a.psi);
     tock(KT_GRAD);
 
@@ -1306,12 +1307,13 @@ void launch_step(StepArgs &a) {
     tock(KT_LINK);
 
     tick(KT_FACES);
+    const int fT = a.tune.face_threads, fB = a.sm_count * a.tune.face_blocks_per_sm;
     if (a.root5)
-        k_faces<D, true><<<a.face_blocks, T, 0, s>>>(p, a.members, a.memberOf, a.grids, a.prim, a.geo, a.grad, a.nbr,
+        k_faces<D, true><<<fB, fT, 0, s>>>(p, a.members, a.memberOf, a.grids, a.prim, a.geo, a.grad, a.nbr,
                                                      a.psi, a.faceOff + p.n, a.faces, a.dt, a.Fface, a.newtonSum,
                                                      a.status);
     else
-        k_faces<D, false><<<a.face_blocks, T, 0, s>>>(p, a.members, a.memberOf, a.grids, a.prim, a.geo, a.grad, a.nbr,
+        k_faces<D, false><<<fB, fT, 0, s>>>(p, a.members, a.memberOf, a.grids, a.prim, a.geo, a.grad, a.nbr,
                                                       a.psi, a.faceOff + p.n, a.faces, a.dt, a.Fface, a.newtonSum,
                                                       a.status);
     tock(KT_FACES);

@@ -9,8 +9,17 @@ namespace mlh {
 
 enum KernelTimerId { KT_GRID = 0, KT_NNS, KT_DT, KT_GRAD, KT_LINK, KT_FACES, KT_UPDATE, KT_COUNT };
 
+// Launch shapes chosen by the autotuner (mlh_autotune).
+struct Tuning {
+    int face_threads = 128;        // threads per block of k_faces
+    int face_blocks_per_sm = 8;    // grid of the grid-stride face loop
+    int grad_threads = 128;        // threads per block of k_gradients
+    int nns_warps_per_sm = 64;     // warps (= particles in flight) of k_neighbours
+};
+
 // Device pointers and settings of one step.
 struct StepArgs {
+    Tuning tune;
     Params p;
     cudaStream_t stream;
     int face_blocks;

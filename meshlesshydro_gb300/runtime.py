@@ -40,6 +40,12 @@ class MemberDesc(ctypes.Structure):
                 ("box_lo", ctypes.c_double * 3), ("box_hi", ctypes.c_double * 3)]
 
 
+class Tuning(ctypes.Structure):
+    """mlh_tuning: launch shapes chosen by the autotuner."""
+    _fields_ = [("face_threads", ctypes.c_int), ("face_blocks_per_sm", ctypes.c_int),
+                ("grad_threads", ctypes.c_int), ("nns_warps_per_sm", ctypes.c_int)]
+
+
 class ParticlesView(ctypes.Structure):
     _fields_ = [("n", ctypes.c_int)] + [(k, ctypes.POINTER(ctypes.c_double))
                                          for k in ("x", "y", "z", "vx", "vy", "vz", "m", "u")]
@@ -55,7 +61,8 @@ class StepStats(ctypes.Structure):
 EXPORTS = ["mlh_abi_version", "mlh_last_error", "mlh_create", "mlh_destroy", "mlh_set_fields",
            "mlh_get_fields", "mlh_step", "mlh_stage_array", "mlh_set_kernel_timing",
            "mlh_kernel_times", "mlh_reset_kernel_times", "mlh_probe_fp64_tflops",
-           "mlh_grid_bounds_noalloc", "mlh_ensemble_create", "mlh_member_times", "mlh_set_graph_mode"]
+           "mlh_grid_bounds_noalloc", "mlh_ensemble_create", "mlh_member_times", "mlh_set_graph_mode",
+           "mlh_autotune"]
 
 _lib = None
 
@@ -102,6 +109,8 @@ def load(path: str = LIB_PATH):
     L.mlh_member_times.restype = ctypes.c_int
     L.mlh_set_graph_mode.argtypes = [vp, ctypes.c_int]
     L.mlh_set_graph_mode.restype = ctypes.c_int
+    L.mlh_autotune.argtypes = [vp, ctypes.c_int, ctypes.POINTER(Tuning)]
+    L.mlh_autotune.restype = ctypes.c_int
     _lib = L
     return L
 
@@ -188,6 +197,13 @@ class Simulation:
 
     def set_graph_mode(self, on: bool):
         self.L.mlh_set_graph_mode(self.h, 1 if on else 0)
+
+    def autotune(self, trial_steps: int = 1) -> dict:
+        t = Tuning()
+        st = self.L.mlh_autotune(self.h, trial_steps, ctypes.byref(t))
+        if st != 0:
+            raise MLHError(st, "mlh_autotune", self.L.mlh_last_error().decode())
+        return {k: getattr(t, k) for k, _ in Tuning._fields_}
 
     def step(self, nsteps: int = 1, dt_max: float = 0.0, check: bool = True) -> StepStats:
         stats = StepStats()
