@@ -175,6 +175,21 @@ void mlh_reset_kernel_times(mlh_ctx *ctx);
  * code); used by bench.py. */
 int mlh_probe_fp64_tflops(double seconds, double *tflops);
 
+/* Learned initial guess for the Riemann star pressure (no counterpart in the
+ * reference): a 4-64-64-64-1 SiLU MLP, 8705 float parameters laid out as
+ * W1[64][4], b1[64], W2[64][64], b2[64], W3[64][64], b3[64], W4[64], b4,
+ * evaluated on the tensor cores in BF16 with FP32 accumulation.  Input per
+ * face (4 floats): log(rhoR/rhoL), (uR-uL)/cL, log(pR/pL), log(cR/cL) of the
+ * face-frame states (left = particle i); output y = log(p* / ((pL+pR)/2)).
+ * All arrays are host arrays. */
+int mlh_pstar_infer(const float *weights, const float *x, int n, float *y);
+/* Mean squared error over n samples and its gradient (8705 floats). */
+int mlh_pstar_grad(const float *weights, const float *x, const float *t, int n, float *loss, float *grad);
+/* Adam training on the GPU (epochs over shuffled mini-batches), in place on
+ * `weights`; loss_history (epochs floats, may be NULL) gets the mean batch loss. */
+int mlh_pstar_train(const float *x, const float *t, long long n, int epochs, int batch, float lr, unsigned seed,
+                    float *weights, float *loss_history);
+
 /* Largest particle count mlh_grid_bounds_noalloc accepts (29-bit indices). */
 #define MLH_NOALLOC_MAX_PARTICLES ((1 << 29) - 1)
 

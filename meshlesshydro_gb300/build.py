@@ -20,7 +20,7 @@ BUILD = os.path.join(HERE, "_build")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVFLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "--expt-relaxed-constexpr"]
-SOURCES = ["mlh_kernels.cu", "mlh_capi.cu", "mlh_probe.cu", "mlh_noalloc.cu"]
+SOURCES = ["mlh_kernels.cu", "mlh_capi.cu", "mlh_probe.cu", "mlh_noalloc.cu", "mlh_pstar.cu"]
 
 
 def nvcc() -> str:

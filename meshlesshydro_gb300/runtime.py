@@ -62,7 +62,7 @@ EXPORTS = ["mlh_abi_version", "mlh_last_error", "mlh_create", "mlh_destroy", "ml
            "mlh_get_fields", "mlh_step", "mlh_stage_array", "mlh_set_kernel_timing",
            "mlh_kernel_times", "mlh_reset_kernel_times", "mlh_probe_fp64_tflops",
            "mlh_grid_bounds_noalloc", "mlh_ensemble_create", "mlh_member_times", "mlh_set_graph_mode",
-           "mlh_autotune"]
+           "mlh_autotune", "mlh_pstar_infer", "mlh_pstar_grad", "mlh_pstar_train"]
 
 _lib = None
 
@@ -111,6 +111,14 @@ def load(path: str = LIB_PATH):
     L.mlh_set_graph_mode.restype = ctypes.c_int
     L.mlh_autotune.argtypes = [vp, ctypes.c_int, ctypes.POINTER(Tuning)]
     L.mlh_autotune.restype = ctypes.c_int
+    fp = ctypes.POINTER(ctypes.c_float)
+    L.mlh_pstar_infer.argtypes = [fp, fp, ctypes.c_int, fp]
+    L.mlh_pstar_infer.restype = ctypes.c_int
+    L.mlh_pstar_grad.argtypes = [fp, fp, fp, ctypes.c_int, fp, fp]
+    L.mlh_pstar_grad.restype = ctypes.c_int
+    L.mlh_pstar_train.argtypes = [fp, fp, ctypes.c_longlong, ctypes.c_int, ctypes.c_int, ctypes.c_float,
+                                  ctypes.c_uint, fp, fp]
+    L.mlh_pstar_train.restype = ctypes.c_int
     _lib = L
     return L
 
@@ -143,6 +151,62 @@ def probe_fp64_tflops(seconds: float = 0.5) -> float:
     if st != 0:
         raise MLHError(st, "mlh_probe_fp64_tflops", L.mlh_last_error().decode())
     return out.value
+
+
+PSTAR_PARAMS = 8705
+
+
+def _fptr(a):
+    return a.ctypes.data_as(ctypes.POINTER(ctypes.c_float))
+
+
+def pstar_init(seed: int = 0) -> np.ndarray:
+    """Initial MLP parameters (Glorot-uniform weights, zero biases)."""
+    rng = np.random.default_rng(seed)
+    parts = []
+    for fan_in, fan_out in ((4, 64), (64, 64), (64, 64), (64, 1)):
+        lim = np.sqrt(6.0 / (fan_in + fan_out))
+        parts.append(rng.uniform(-lim, lim, fan_out * fan_in))
+        parts.append(np.zeros(fan_out))
+    w = np.concatenate(parts).astype(np.float32)
+    assert w.size == PSTAR_PARAMS
+    return w
+
+
+def pstar_infer(weights, x) -> np.ndarray:
+    L = load()
+    w = np.ascontiguousarray(weights, dtype=np.float32)
+    x = np.ascontiguousarray(x, dtype=np.float32).reshape(-1, 4)
+    y = np.empty(x.shape[0], dtype=np.float32)
+    st = L.mlh_pstar_infer(_fptr(w), _fptr(x), x.shape[0], _fptr(y))
+    if st != 0:
+        raise MLHError(st, "mlh_pstar_infer", L.mlh_last_error().decode())
+    return y
+
+
+def pstar_grad(weights, x, t):
+    L = load()
+    w = np.ascontiguousarray(weights, dtype=np.float32)
+    x = np.ascontiguousarray(x, dtype=np.float32).reshape(-1, 4)
+    t = np.ascontiguousarray(t, dtype=np.float32)
+    loss = np.zeros(1, dtype=np.float32)
+    g = np.zeros(PSTAR_PARAMS, dtype=np.float32)
+    st = L.mlh_pstar_grad(_fptr(w), _fptr(x), _fptr(t), x.shape[0], _fptr(loss), _fptr(g))
+    if st != 0:
+        raise MLHError(st, "mlh_pstar_grad", L.mlh_last_error().decode())
+    return float(loss[0]), g
+
+
+def pstar_train(x, t, weights=None, epochs: int = 10, batch: int = 4096, lr: float = 1e-3, seed: int = 0):
+    L = load()
+    w = np.ascontiguousarray(pstar_init(seed) if weights is None else weights, dtype=np.float32).copy()
+    x = np.ascontiguousarray(x, dtype=np.float32).reshape(-1, 4)
+    t = np.ascontiguousarray(t, dtype=np.float32)
+    hist = np.zeros(epochs, dtype=np.float32)
+    st = L.mlh_pstar_train(_fptr(x), _fptr(t), x.shape[0], epochs, batch, lr, seed, _fptr(w), _fptr(hist))
+    if st != 0:
+        raise MLHError(st, "mlh_pstar_train", L.mlh_last_error().decode())
+    return w, hist
 
 
 class Simulation:

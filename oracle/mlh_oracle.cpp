@@ -870,6 +870,24 @@ int orc_get(void *ctx, const char *name, void *out) {
     return getArr((Sim<3> *)hnd->sim, name, out);
 }
 
+// Exact Riemann solves of n independent states: star pressure and Newton
+// iterations, from the two-rarefaction guess or from guess[k] when given
+// (for checking learned initial guesses).
+int orc_riemann_batch(int n, const double *rhoL, const double *uL, const double *pL, const double *rhoR,
+                      const double *uR, const double *pR, double gamma, const double *guess, double *pstar,
+                      int *iters) {
+    orc::ExactRiemann rs(gamma, 1e-10, 100);
+    for (int k = 0; k < n; ++k) {
+        double cL = std::sqrt(gamma * pL[k] / rhoL[k]), cR = std::sqrt(gamma * pR[k] / rhoR[k]);
+        double p0 = guess ? guess[k] : rs.guess_two_rarefaction(uL[k], pL[k], cL, uR[k], pR[k], cR);
+        double ps = 0.;
+        int it = rs.newton(p0, rhoL[k], uL[k], pL[k], cL, rhoR[k], uR[k], pR[k], cR, ps);
+        pstar[k] = ps;
+        if (iters) iters[k] = it;
+    }
+    return 0;
+}
+
 void orc_destroy(void *ctx) {
     Handle *hnd = (Handle *)ctx;
     if (hnd->dim == 2) delete (Sim<2> *)hnd->sim;

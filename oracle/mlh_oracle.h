@@ -51,6 +51,9 @@ long orc_size(void *ctx, const char *name);
 /* Copy a named array into `out` (doubles, or int32 for integer arrays). */
 int orc_get(void *ctx, const char *name, void *out);
 void orc_destroy(void *ctx);
+int orc_riemann_batch(int n, const double *rhoL, const double *uL, const double *pL, const double *rhoR,
+                      const double *uR, const double *pR, double gamma, const double *guess, double *pstar,
+                      int *iters);
 
 #ifdef __cplusplus
 }

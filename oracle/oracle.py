@@ -56,8 +56,25 @@ def lib():
         L.orc_get.restype = ctypes.c_int
         L.orc_get.argtypes = [ctypes.c_void_p, ctypes.c_char_p, ctypes.c_void_p]
         L.orc_destroy.argtypes = [ctypes.c_void_p]
+        L.orc_riemann_batch.argtypes = [ctypes.c_int] + [dp] * 6 + [ctypes.c_double, dp, dp,
+                                                                    ctypes.POINTER(ctypes.c_int)]
+        L.orc_riemann_batch.restype = ctypes.c_int
         _lib = L
     return _lib
+
+
+def riemann_batch(rhoL, uL, pL, rhoR, uR, pR, gamma=5.0 / 3.0, guess=None):
+    """Star pressure and Newton iterations of independent Riemann problems."""
+    L = lib()
+    arrs = [np.ascontiguousarray(a, dtype=np.float64) for a in (rhoL, uL, pL, rhoR, uR, pR)]
+    n = arrs[0].size
+    ps = np.zeros(n)
+    it = np.zeros(n, dtype=np.int32)
+    dp = lambda a: a.ctypes.data_as(ctypes.POINTER(ctypes.c_double))
+    g = None if guess is None else np.ascontiguousarray(guess, dtype=np.float64)
+    L.orc_riemann_batch(n, *[dp(a) for a in arrs], gamma, None if g is None else dp(g), dp(ps),
+                        it.ctypes.data_as(ctypes.POINTER(ctypes.c_int)))
+    return ps, it
 
 
 def _cfg_struct(cfg) -> OrcConfig:
