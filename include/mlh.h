@@ -88,6 +88,9 @@ typedef struct mlh_step_stats {
     long long faces;                 /* Riemann problems solved, summed */
     long long newton_iterations;     /* summed over faces and steps */
     double device_ms;                /* device time of the call (CUDA events) */
+    long long newton_fallbacks;      /* faces whose learned p* guess did not
+                                        converge and restarted from the
+                                        two-rarefaction guess (0 without one) */
 } mlh_step_stats;
 
 /* One simulation of an ensemble: its particle count (members are stored back
@@ -180,8 +183,9 @@ int mlh_probe_fp64_tflops(double seconds, double *tflops);
  * W1[64][4], b1[64], W2[64][64], b2[64], W3[64][64], b3[64], W4[64], b4,
  * evaluated on the tensor cores in BF16 with FP32 accumulation.  Input per
  * face (4 floats): log(rhoR/rhoL), (uR-uL)/cL, log(pR/pL), log(cR/cL) of the
- * face-frame states (left = particle i); output y = log(p* / ((pL+pR)/2)).
- * All arrays are host arrays. */
+ * face-frame states (left = particle i); output y, one float per row.  The
+ * step reads y as log(p* / p_TR), p_TR the two-rarefaction guess of the face
+ * (Toro eq. 4.46).  All arrays are host arrays. */
 int mlh_pstar_infer(const float *weights, const float *x, int n, float *y);
 /* Mean squared error over n samples and its gradient (8705 floats). */
 int mlh_pstar_grad(const float *weights, const float *x, const float *t, int n, float *loss, float *grad);
@@ -189,6 +193,18 @@ int mlh_pstar_grad(const float *weights, const float *x, const float *t, int n, 
  * `weights`; loss_history (epochs floats, may be NULL) gets the mean batch loss. */
 int mlh_pstar_train(const float *x, const float *t, long long n, int epochs, int batch, float lr, unsigned seed,
                     float *weights, float *loss_history);
+
+/* Use the network (weights: 8705 floats) for the initial guess of the
+ * Riemann problems of the context's steps: p_TR * exp(y) where |y| > 0.01,
+ * p_TR (the two-rarefaction guess) elsewhere; NULL returns to p_TR
+ * everywhere.  Newton still iterates to riemann_tol and restarts from p_TR
+ * when it does not converge from the network's guess
+ * (mlh_step_stats.newton_fallbacks counts those faces). */
+int mlh_set_pstar_weights(mlh_ctx *ctx, const float *weights);
+/* One mlh_step(ctx, 1, 0, NULL) that also records the network inputs (4
+ * floats) and targets log(p* / p_TR) of every `stride`-th face into x, t
+ * (host, capacity rows); *count receives the number of rows. */
+int mlh_pstar_harvest(mlh_ctx *ctx, int stride, float *x, float *t, long long capacity, long long *count);
 
 /* Largest particle count mlh_grid_bounds_noalloc accepts (29-bit indices). */
 #define MLH_NOALLOC_MAX_PARTICLES ((1 << 29) - 1)

@@ -2,6 +2,7 @@
 // step driver with capacity retries, parity dumps and kernel timing.
 #include "../../include/mlh.h"
 #include "mlh_kernels.h"
+#include "mlh_pstar.h"
 #include "mlh_riemann.cuh"
 
 #include <cmath>
@@ -82,6 +83,14 @@ struct mlh_ctx {
     int *scanTiles = nullptr, *scanTotal = nullptr;
     bool debug_arrays = true;
     Tuning tune;
+    // learned p* guess
+    bool learned = false;
+    float *mlp_w = nullptr;
+    void *mlp_packed = nullptr;
+    FaceState *fstate = nullptr;
+    float4 *feat = nullptr;
+    float *yguess = nullptr;
+    Harvest harvest{};
     // CUDA graph of one step, replayed by mlh_step in graph mode
     bool graph_mode = false;
     cudaGraphExec_t graph_exec = nullptr;
@@ -99,8 +108,9 @@ namespace {
 void free_neighbour_buffers(mlh_ctx *c) {
     cudaFree(c->nbr); cudaFree(c->rr); cudaFree(c->ww); cudaFree(c->psi); cudaFree(c->faceOf); cudaFree(c->faces);
     cudaFree(c->Fface);
+    cudaFree(c->fstate); cudaFree(c->feat); cudaFree(c->yguess);
     c->nbr = nullptr; c->rr = nullptr; c->ww = nullptr; c->psi = nullptr; c->faceOf = nullptr; c->faces = nullptr;
-    c->Fface = nullptr;
+    c->Fface = nullptr; c->fstate = nullptr; c->feat = nullptr; c->yguess = nullptr;
 }
 
 int alloc_neighbour_buffers(mlh_ctx *c) {
@@ -114,6 +124,11 @@ int alloc_neighbour_buffers(mlh_ctx *c) {
     CK(dalloc(&c->faceOf, slots));
     CK(dalloc(&c->faces, faces));
     CK(dalloc(&c->Fface, faces * 6));
+    if (c->learned) {
+        CK(dalloc(&c->fstate, faces));
+        CK(dalloc(&c->feat, faces));
+        CK(dalloc(&c->yguess, faces));
+    }
     return 0;
 }
 
@@ -221,6 +236,9 @@ StepArgs make_args(mlh_ctx *c, double dt_max) {
     a.status = c->status; a.dtbits = c->dtbits; a.newtonSum = c->newtonSum;
     a.dt = c->dt; a.simTime = c->simTime; a.stepsDone = c->stepsDone;
     a.scanTiles = c->scanTiles; a.scanTotal = c->scanTotal;
+    a.learned = c->learned ? 1 : 0;
+    a.fstate = c->fstate; a.feat = c->feat; a.yguess = c->yguess; a.mlp_packed = c->mlp_packed;
+    a.harvest = c->harvest;
     a.timer = c->timing ? timer_cb : nullptr;
     a.timer_ctx = c;
     return a;
@@ -341,7 +359,7 @@ static int create_impl(const mlh_config *cfg, int nmembers, const mlh_member *md
     A(cell, n); A(cellList, n);
     A(noi, n); A(noiImg, n); A(faceCnt, n); A(faceOff, n + 1);
     A(prim, n); A(geo, n); A(grad, n); A(gradRaw, n); A(fluxSums, n * 5);
-    A(status, 1); A(dtbits, nm); A(newtonSum, 1); A(dt, nm); A(simTime, nm); A(stepsDone, 1);
+    A(status, 1); A(dtbits, nm); A(newtonSum, 2); A(dt, nm); A(simTime, nm); A(stepsDone, 1);
     A(scanTiles, n / 4096 + 1024); A(scanTotal, 1);
 #undef A
     if ((rc = alloc_cell_buffers(c))) return fail(rc);
@@ -358,7 +376,7 @@ static int create_impl(const mlh_config *cfg, int nmembers, const mlh_member *md
     cudaMemsetAsync(c->status, 0, sizeof(unsigned), c->stream);
     cudaMemsetAsync(c->simTime, 0, sizeof(double) * nm, c->stream);
     cudaMemsetAsync(c->dt, 0, sizeof(double) * nm, c->stream);
-    cudaMemsetAsync(c->newtonSum, 0, sizeof(unsigned long long), c->stream);
+    cudaMemsetAsync(c->newtonSum, 0, 2 * sizeof(unsigned long long), c->stream);
     cudaMemsetAsync(c->stepsDone, 0, sizeof(int), c->stream);
     if ((rc = upload(c, init))) return fail(rc);
     if (cudaStreamSynchronize(c->stream) != cudaSuccess) return fail(cuda_fail(cudaGetLastError(), "create sync"));
@@ -392,6 +410,8 @@ void mlh_destroy(mlh_ctx *c) {
     for (void *q : ptrs) if (q) cudaFree(q);
     free_cell_buffers(c);
     free_neighbour_buffers(c);
+    if (c->mlp_w) cudaFree(c->mlp_w);
+    if (c->mlp_packed) cudaFree(c->mlp_packed);
     for (auto e : c->tev) cudaEventDestroy(e);
     if (c->ev0) cudaEventDestroy(c->ev0);
     if (c->ev1) cudaEventDestroy(c->ev1);
@@ -442,7 +462,7 @@ int mlh_step(mlh_ctx *c, int nsteps, double dt_max, mlh_step_stats *stats) {
     if (!c || nsteps < 0) { g_last_error = "invalid argument"; return MLH_ERR_INVALID; }
     unsigned accumulated = 0;
     long long pairs = 0, faces = 0;
-    unsigned long long newton = 0;
+    unsigned long long newton = 0, fallbacks = 0;
     double dev_ms = 0.;
     int done_total = 0;
     int remaining = nsteps;
@@ -455,7 +475,7 @@ int mlh_step(mlh_ctx *c, int nsteps, double dt_max, mlh_step_stats *stats) {
         }
         CK(cudaMemsetAsync(c->status, 0, sizeof(unsigned), c->stream));
         CK(cudaMemsetAsync(c->stepsDone, 0, sizeof(int), c->stream));
-        CK(cudaMemsetAsync(c->newtonSum, 0, sizeof(unsigned long long), c->stream));
+        CK(cudaMemsetAsync(c->newtonSum, 0, 2 * sizeof(unsigned long long), c->stream));
         CK(cudaEventRecord(c->ev0, c->stream));
         if (use_graph) {
             for (int k = 0; k < remaining; ++k) CK(cudaGraphLaunch(c->graph_exec, c->stream));
@@ -472,11 +492,12 @@ int mlh_step(mlh_ctx *c, int nsteps, double dt_max, mlh_step_stats *stats) {
         if (c->timing) collect_timers(c);
         unsigned st = 0;
         int done = 0;
-        unsigned long long nsum = 0;
+        unsigned long long nsum[2] = {0, 0};
         CK(cudaMemcpy(&st, c->status, sizeof(unsigned), cudaMemcpyDeviceToHost));
         CK(cudaMemcpy(&done, c->stepsDone, sizeof(int), cudaMemcpyDeviceToHost));
-        CK(cudaMemcpy(&nsum, c->newtonSum, sizeof(unsigned long long), cudaMemcpyDeviceToHost));
-        newton += nsum;
+        CK(cudaMemcpy(nsum, c->newtonSum, 2 * sizeof(unsigned long long), cudaMemcpyDeviceToHost));
+        newton += nsum[0];
+        fallbacks += nsum[1];
         done_total += done;
         remaining -= done;
         // per-step interaction counts of the last step
@@ -499,6 +520,8 @@ int mlh_step(mlh_ctx *c, int nsteps, double dt_max, mlh_step_stats *stats) {
                 if (rc) return rc;
             }
             drop_graph(c);   // buffers changed
+            // the step is repeated: faces recorded by the aborted attempt go
+            if (c->harvest.count) CK(cudaMemsetAsync(c->harvest.count, 0, sizeof(int), c->stream));
             continue;
         }
         accumulated |= st;
@@ -513,6 +536,7 @@ int mlh_step(mlh_ctx *c, int nsteps, double dt_max, mlh_step_stats *stats) {
         stats->faces = faces;
         stats->newton_iterations = (long long)newton;
         stats->device_ms = dev_ms;
+        stats->newton_fallbacks = (long long)fallbacks;
     }
     return (int)(accumulated & ~(unsigned)MLH_ERR_NGB_OVERFLOW & ~ST_CAPACITY) ? (int)accumulated : 0;
 }
@@ -610,6 +634,58 @@ done:
         out->grad_threads = c->tune.grad_threads;
         out->nns_warps_per_sm = c->tune.nns_warps_per_sm;
     }
+    return rc;
+}
+
+// Learned p* guess on (weights: 8705 floats, host) or off (NULL).
+int mlh_set_pstar_weights(mlh_ctx *c, const float *weights) {
+    if (!c) return MLH_ERR_INVALID;
+    CK(cudaStreamSynchronize(c->stream));
+    drop_graph(c);
+    if (!weights) {
+        c->learned = false;
+        return 0;
+    }
+    if (!c->mlp_w) CK(dalloc(&c->mlp_w, PSTAR_PARAMS));
+    if (!c->mlp_packed) CK(cudaMalloc(&c->mlp_packed, pstar_packed_bytes()));
+    CK(cudaMemcpy(c->mlp_w, weights, sizeof(float) * PSTAR_PARAMS, cudaMemcpyHostToDevice));
+    pstar_pack(c->mlp_w, c->mlp_packed, c->stream);
+    if (!c->learned) {
+        c->learned = true;
+        free_neighbour_buffers(c);
+        if (int rc = alloc_neighbour_buffers(c)) return rc;
+    }
+    CK(cudaStreamSynchronize(c->stream));
+    return 0;
+}
+
+// One step that also records network inputs and targets log(p*/p_TR) of
+// every `stride`-th face (plain face pipeline).
+int mlh_pstar_harvest(mlh_ctx *c, int stride, float *x, float *t, long long capacity, long long *count) {
+    if (!c || stride < 1 || !x || !t || capacity < 1 || capacity > 0x7fffffff) return MLH_ERR_INVALID;
+    const bool learned0 = c->learned;
+    c->learned = false;
+    drop_graph(c);
+    float4 *hx = nullptr;
+    float *ht = nullptr;
+    int *hc = nullptr;
+    CK(cudaMalloc(&hx, sizeof(float4) * (size_t)capacity));
+    CK(cudaMalloc(&ht, sizeof(float) * (size_t)capacity));
+    CK(cudaMalloc(&hc, sizeof(int)));
+    CK(cudaMemsetAsync(hc, 0, sizeof(int), c->stream));
+    c->harvest.x = hx; c->harvest.t = ht; c->harvest.count = hc;
+    c->harvest.stride = stride; c->harvest.cap = (int)capacity;
+    mlh_step_stats st;
+    int rc = mlh_step(c, 1, 0., &st);
+    c->harvest = Harvest{};
+    c->learned = learned0;
+    int cnt = 0;
+    cudaMemcpy(&cnt, hc, sizeof(int), cudaMemcpyDeviceToHost);
+    if (cnt > capacity) cnt = (int)capacity;
+    cudaMemcpy(x, hx, sizeof(float4) * (size_t)cnt, cudaMemcpyDeviceToHost);
+    cudaMemcpy(t, ht, sizeof(float) * (size_t)cnt, cudaMemcpyDeviceToHost);
+    cudaFree(hx); cudaFree(ht); cudaFree(hc);
+    if (count) *count = cnt;
     return rc;
 }
 

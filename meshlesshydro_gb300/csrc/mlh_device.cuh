@@ -77,6 +77,18 @@ struct Geo {        // E_i^{-1}, 1/omega_i, omega_i, sound speed
 struct FaceRef {    // canonical face: owner i, slot index, reverse slot (images)
     int i, slot, rslot, pad;
 };
+// Face-frame states of one face between the two halves of the learned-guess
+// face pipeline: R[5], L[5], A[3], v_frame[3], A/|A| [3], flag
+struct FaceState {
+    double v[20];
+};
+// Where the plain face kernel records network training pairs.
+struct Harvest {
+    float4 *x;
+    float *t;
+    int *count;
+    int stride, cap;
+};
 
 // Kernel::cubicSpline, demonstrator/src/Particles.cpp:7-24.  sigma is
 // precomputed on the host with the reference's expression; pow(2-q, 3.) is

@@ -916,6 +916,21 @@ __device__ __forceinline__ void rot3(const double *a, const double *b, double *L
     L[8] = 1. - n * (v1 * v1 + v0 * v0);
 }
 
+// Network inputs of a face from its face-frame states (left = particle i):
+// log(rhoR/rhoL), (uR - uL)/cL, log(pR/pL), log(cR/cL).
+// The network predicts y = log(p* / p_TR), p_TR the two-rarefaction guess of
+// the face.  Where |y| is below PSTAR_GATE the correction is within the
+// network's own error (BF16 activations) and Newton starts from p_TR as in the
+// plain pipeline, so faces the cheap guess already serves keep its iteration
+// count and its bits.
+constexpr float PSTAR_GATE = 0.01f;
+
+__device__ __forceinline__ float4 pstar_features(const double *R, const double *L, double gamma) {
+    const float rl = (float)R[0], rr = (float)L[0], pl = (float)R[1], pr = (float)L[1];
+    const float cl = sqrtf((float)gamma * pl / rl), cr = sqrtf((float)gamma * pr / rr);
+    return make_float4(logf(rr / rl), (float)(L[2] - R[2]) / cl, logf(pr / pl), logf(cr / cl));
+}
+
 // One canonical face (i < j): effective face A_ij = psi~_j(x_i)/omega_i -
 // psi~_i(x_j)/omega_j from the psi~ of both slots (compEffectiveFace,
 // Particles.cpp:1290-1311, 2504-2531); boosted, reconstructed, optionally
@@ -927,7 +942,12 @@ __device__ __forceinline__ void rot3(const double *a, const double *b, double *L
 // Helper::rotationMatrix2D/3D(unitX, hatA) is the transpose of the forward
 // one, bit for bit, so it is not recomputed.  Output slot order:
 // [mass, energy, px, py, pz].
-template <int D, bool ROOT5>
+// MODE 0: the whole face.  MODE 1 (learned guess, first half): stop after the
+// rotation into the face frame, store the face state and the network inputs.
+// MODE 2 (second half): reload the state, solve from the network's guess,
+// project the flux.  `harvest` (MODE 0) records network inputs and targets
+// log(p*/p_TR) of every `stride`-th face.
+template <int D, bool ROOT5, int MODE>
 __global__ void __launch_bounds__(256) k_faces(Params p, const Member *__restrict__ members,
                                                const int *__restrict__ memberOf, const GridInfo *__restrict__ grids,
                                                const Prim *__restrict__ prim, const Geo *__restrict__ geo,
@@ -935,16 +955,34 @@ __global__ void __launch_bounds__(256) k_faces(Params p, const Member *__restric
                                                const double *__restrict__ psi, const int *__restrict__ faceTotal,
                                                const FaceRef *__restrict__ faces, const double *__restrict__ dtp,
                                                double *__restrict__ Fface, unsigned long long *__restrict__ newtonSum,
-                                               unsigned *__restrict__ status) {
+                                               unsigned *__restrict__ status, FaceState *__restrict__ fstate,
+                                               float4 *__restrict__ feat, const float *__restrict__ yguess,
+                                               Harvest hv) {
     constexpr int NV = D + 2;
     const int nf = *faceTotal < p.faces_cap ? *faceTotal : p.faces_cap;
     const RiemannConsts rc = make_riemann_consts(p.gamma, p.rtol, p.rmaxit);
     const double gamma = p.gamma;
-    unsigned long long iters_local = 0;
+    unsigned long long iters_local = 0, fallback_local = 0;
     unsigned st_local = 0;
     for (int f = blockIdx.x * blockDim.x + threadIdx.x; f < nf; f += gridDim.x * blockDim.x) {
+        double R[5], L[5], A[3] = {0., 0., 0.}, vf[3] = {0., 0., 0.}, hatA[3] = {0., 0., 0.}, Lam[9];
+        const double unitX[3] = {1., 0., 0.};
+        if (MODE == 2) {
+            const FaceState &fs = fstate[f];
+            if (!(fs.v[0] == fs.v[0]) && fs.v[19] == 1.) continue;   // face without owner (flagged in MODE 1)
+#pragma unroll
+            for (int k = 0; k < 5; ++k) { R[k] = fs.v[k]; L[k] = fs.v[5 + k]; }
+#pragma unroll
+            for (int a = 0; a < 3; ++a) { A[a] = fs.v[10 + a]; vf[a] = fs.v[13 + a]; hatA[a] = fs.v[16 + a]; }
+            if (D == 2) rot2(hatA, unitX, Lam);
+            else rot3(hatA, unitX, Lam);
+        } else {
         const FaceRef fr = faces[f];
-        if (fr.i < 0 || fr.slot < 0) { st_local |= ST_ASYMMETRIC; continue; }
+        if (fr.i < 0 || fr.slot < 0) {
+            st_local |= ST_ASYMMETRIC;
+            if (MODE == 1) { fstate[f].v[0] = __longlong_as_double(0x7ff8000000000000ll); fstate[f].v[19] = 1.; }
+            continue;
+        }
         const int i = fr.i;
         const int mi = memberOf ? memberOf[i] : 0;
         const double dt = dtp[mi];
@@ -959,7 +997,6 @@ __global__ void __launch_bounds__(256) k_faces(Params p, const Member *__restric
         if (img) neighbour_pos<D>(e, pj, grids[mi], h, xj);
         else { xj[0] = pj.x; xj[1] = pj.y; xj[2] = pj.z; }
         // --- effective face
-        double A[3] = {0., 0., 0.};
         {
             const double *ps_i = psi + si * 3;
             if (fr.rslot >= 0) {
@@ -987,7 +1024,6 @@ __global__ void __launch_bounds__(256) k_faces(Params p, const Member *__restric
             }
         }
         const double vi[3] = {pi.vx, pi.vy, pi.vz}, vj[3] = {pj.vx, pj.vy, pj.vz};
-        double vf[3] = {0., 0., 0.};
         if (p.move) {
             if (p.foqp) {
 #pragma unroll
@@ -1001,7 +1037,6 @@ __global__ void __launch_bounds__(256) k_faces(Params p, const Member *__restric
         }
         const double *Gi = grad[i].g, *Gj = grad[j].g;
         // gradient blocks: 0 rho, 3 vx, 6 vy, 9 vz, 12 P
-        double R[5], L[5];
         R[0] = pi.rho; L[0] = pj.rho;
         R[1] = pi.P; L[1] = pj.P;
 #pragma unroll
@@ -1071,13 +1106,10 @@ __global__ void __launch_bounds__(256) k_faces(Params p, const Member *__restric
         }
         if (R[1] < 0. || L[1] < 0.) st_local |= ST_NEG_PRESSURE;
         // --- Riemann problem in the face frame (i left, j right)
-        const double unitX[3] = {1., 0., 0.};
         double AN = sqrt(dotD<D>(A, A));
-        double hatA[3] = {0., 0., 0.};
         const double iAN = 1. / AN;
 #pragma unroll
         for (int a = 0; a < D; ++a) hatA[a] = iAN * A[a];
-        double Lam[9];
         if (D == 2) {
             rot2(hatA, unitX, Lam);
             double bR0 = L[2], bR1 = L[3], bL0 = R[2], bL1 = R[3];
@@ -1095,10 +1127,42 @@ __global__ void __launch_bounds__(256) k_faces(Params p, const Member *__restric
             R[3] = Lam[3] * bL0 + Lam[4] * bL1 + Lam[5] * bL2;
             R[4] = Lam[6] * bL0 + Lam[7] * bL1 + Lam[8] * bL2;
         }
-        RiemannResult rs = ROOT5 ? riemann_exact5(rc, R[0], R[2], R[1], L[0], L[2], L[1])
-                                 : riemann_exact(rc, R[0], R[2], R[1], L[0], L[2], L[1]);
+        if (MODE == 1) {
+            FaceState &fs = fstate[f];
+#pragma unroll
+            for (int k = 0; k < 5; ++k) { fs.v[k] = R[k]; fs.v[5 + k] = L[k]; }
+#pragma unroll
+            for (int a = 0; a < 3; ++a) { fs.v[10 + a] = A[a]; fs.v[13 + a] = vf[a]; fs.v[16 + a] = hatA[a]; }
+            fs.v[19] = 0.;
+            feat[f] = pstar_features(R, L, gamma);
+            continue;
+        }
+        }   // MODE != 2
+        double guess = -1.;
+        if (MODE == 2) {
+            const float y = yguess[f];
+            if (isfinite(y) && fabsf(y) > PSTAR_GATE && fabsf(y) < 30.f)
+                guess = two_rarefaction_guess<ROOT5>(rc, R[0], R[2], R[1], L[0], L[2], L[1]) * (double)__expf(y);
+        }
+        RiemannResult rs = ROOT5 ? riemann_exact5(rc, R[0], R[2], R[1], L[0], L[2], L[1], guess)
+                                 : riemann_exact(rc, R[0], R[2], R[1], L[0], L[2], L[1], guess);
+        if (MODE == 0 && hv.stride > 0 && f % hv.stride == 0) {
+            const int slot = f / hv.stride;
+            const double ptr = two_rarefaction_guess<ROOT5>(rc, R[0], R[2], R[1], L[0], L[2], L[1]);
+            if (slot < hv.cap && rs.iters >= 0 && rs.pstar > 0. && ptr > 0.) {
+                hv.x[slot] = pstar_features(R, L, gamma);
+                hv.t[slot] = (float)log(rs.pstar / ptr);
+                atomicMax(hv.count, slot + 1);
+            }
+        }
         if (rs.iters < 0) st_local |= ST_NEWTON;
-        else iters_local += (unsigned long long)rs.iters;
+        else {
+            // iters counts every Newton step run: a learned guess that did not
+            // converge adds max_iter wasted steps before the restart from the
+            // two-rarefaction guess
+            if (MODE == 2 && rs.iters > rc.max_iter) ++fallback_local;
+            iters_local += (unsigned long long)rs.iters;
+        }
         double vSol[3] = {rs.u, 0., 0.};
         if (rs.flag == 1) { for (int a = 1; a < D; ++a) vSol[a] = L[2 + a]; }
         else if (rs.flag == -1) { for (int a = 1; a < D; ++a) vSol[a] = R[2 + a]; }
@@ -1142,10 +1206,12 @@ __global__ void __launch_bounds__(256) k_faces(Params p, const Member *__restric
     // block-level accumulation of the counters
     for (int o = 16; o > 0; o >>= 1) {
         iters_local += __shfl_xor_sync(0xffffffffu, iters_local, o);
+        fallback_local += __shfl_xor_sync(0xffffffffu, fallback_local, o);
         st_local |= __shfl_xor_sync(0xffffffffu, st_local, o);
     }
     if ((threadIdx.x & 31) == 0) {
         if (iters_local) atomicAdd(newtonSum, iters_local);
+        if (fallback_local) atomicAdd(newtonSum + 1, fallback_local);
         if (st_local) flag(status, st_local);
     }
 }
@@ -1308,14 +1374,18 @@ void launch_step(StepArgs &a) {
 
     tick(KT_FACES);
     const int fT = a.tune.face_threads, fB = a.sm_count * a.tune.face_blocks_per_sm;
-    if (a.root5)
-        k_faces<D, true><<<fB, fT, 0, s>>>(p, a.members, a.memberOf, a.grids, a.prim, a.geo, a.grad, a.nbr,
-                                                     a.psi, a.faceOff + p.n, a.faces, a.dt, a.Fface, a.newtonSum,
-                                                     a.status);
-    else
-        k_faces<D, false><<<fB, fT, 0, s>>>(p, a.members, a.memberOf, a.grids, a.prim, a.geo, a.grad, a.nbr,
-                                                      a.psi, a.faceOff + p.n, a.faces, a.dt, a.Fface, a.newtonSum,
-                                                      a.status);
+#define MLH_FACES(R5, MODE)                                                                                      \
+    k_faces<D, R5, MODE><<<fB, fT, 0, s>>>(p, a.members, a.memberOf, a.grids, a.prim, a.geo, a.grad, a.nbr, a.psi, \
+                                           a.faceOff + p.n, a.faces, a.dt, a.Fface, a.newtonSum, a.status,       \
+                                           a.fstate, a.feat, a.yguess, a.harvest)
+    if (a.learned) {
+        if (a.root5) MLH_FACES(true, 1); else MLH_FACES(false, 1);
+        pstar_infer_dev(a.feat, a.faceOff + p.n, (int)a.faces_cap, a.mlp_packed, a.yguess, a.sm_count, s);
+        if (a.root5) MLH_FACES(true, 2); else MLH_FACES(false, 2);
+    } else {
+        if (a.root5) MLH_FACES(true, 0); else MLH_FACES(false, 0);
+    }
+#undef MLH_FACES
     tock(KT_FACES);
 
     tick(KT_UPDATE);

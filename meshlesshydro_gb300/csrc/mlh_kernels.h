@@ -56,6 +56,13 @@ struct StepArgs {
     double *dt, *simTime;
     int *stepsDone;
     int *scanTiles, *scanTotal;
+    // learned p* guess: face states, network inputs and outputs, packed weights
+    int learned;
+    FaceState *fstate;
+    float4 *feat;
+    float *yguess;
+    const void *mlp_packed;
+    Harvest harvest;
     // optional per-kernel timer callback (phase 0 = before, 1 = after)
     void (*timer)(void *, int, int);
     void *timer_ctx;
@@ -76,5 +83,8 @@ void pack_posf(const double *x, const double *y, const double *z, int n, int dim
 void exclusive_scan(const int *in, int n, int *out, int *tile_buf, int *total, cudaStream_t s);
 const char *kernel_timer_name(int id);
 void set_last_error(const char *msg);
+// MLP inference over the faces of a step: n read on the device (min with cap)
+void pstar_infer_dev(const float4 *x, const int *n_dev, int cap, const void *packed, float *y, int sm_count,
+                     cudaStream_t s);
 
 }  // namespace mlh

@@ -1,7 +1,8 @@
 // Learned initial guess for the Riemann star pressure p*.
 //
 // A 4-64-64-64-1 MLP with SiLU maps dimensionless left/right states of a face
-// to y = log(p* / p_mean), p_mean = (pL + pR)/2.  Inputs (left = particle i,
+// to a correction y = log(p* / p_TR) of the two-rarefaction guess p_TR (Toro
+// eq. 4.46; the network itself only sees x and y).  Inputs (left = particle i,
 // right = neighbour j, after rotation into the face frame):
 //   x0 = log(rhoR/rhoL), x1 = (uR - uL)/cL, x2 = log(pR/pL), x3 = log(cR/cL)
 // (the ratios enter as logarithms so that shock-strength ratios of 1e6 stay in
@@ -193,11 +194,12 @@ __device__ __forceinline__ void load_packed(PackedMlp *s, const PackedMlp *g) {
 // ------------------------------------------------------------------ inference
 
 // y = MLP(x) for n rows; one warp per 32 rows (grid-stride, warp-uniform).
-__global__ void __launch_bounds__(256) k_pstar_infer(const float4 *__restrict__ x, int n,
+__global__ void __launch_bounds__(256) k_pstar_infer(const float4 *__restrict__ x, int n, const int *__restrict__ n_dev,
                                                      const PackedMlp *__restrict__ pk, float *__restrict__ y) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     PackedMlp *s = reinterpret_cast<PackedMlp *>(smem_raw);
     load_packed(s, pk);
+    if (n_dev && *n_dev < n) n = *n_dev;
     const int lane = threadIdx.x & 31;
     const int gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, nw = (gridDim.x * blockDim.x) >> 5;
     for (int r0 = gw * 32; r0 < n; r0 += nw * 32) {
@@ -437,7 +439,12 @@ void pstar_infer(const float4 *x, int n, const void *packed, float *y, int sm_co
     int blocks = (warps + 7) / 8;
     if (blocks > sm_count * 8) blocks = sm_count * 8;
     if (blocks < 1) blocks = 1;
-    k_pstar_infer<<<blocks, 256, sizeof(PackedMlp), s>>>(x, n, (const PackedMlp *)packed, y);
+    k_pstar_infer<<<blocks, 256, sizeof(PackedMlp), s>>>(x, n, nullptr, (const PackedMlp *)packed, y);
+}
+
+void pstar_infer_dev(const float4 *x, const int *n_dev, int cap, const void *packed, float *y, int sm_count,
+                     cudaStream_t s) {
+    k_pstar_infer<<<sm_count * 4, 256, sizeof(PackedMlp), s>>>(x, cap, n_dev, (const PackedMlp *)packed, y);
 }
 
 size_t pstar_packed_bytes() { return sizeof(PackedMlp); }

@@ -57,8 +57,9 @@ __device__ __forceinline__ void pressure_fn(const RiemannConsts &c, double p, do
 
 struct RiemannResult {
     double rho, u, p;
-    int flag;    // -1: left of the contact sampled, +1: right, 0: vacuum
-    int iters;   // Newton iterations (< 0: no convergence)
+    double pstar;   // star-region pressure
+    int flag;       // -1: left of the contact sampled, +1: right, 0: vacuum
+    int iters;      // Newton iterations (< 0: no convergence)
 };
 
 // Newton-Raphson from p0; returns iterations or -1.
@@ -90,7 +91,7 @@ __device__ inline RiemannResult riemann_exact(const RiemannConsts &c, double rho
     double cL = sqrt(c.gamma * pL / rhoL);
     double cR = sqrt(c.gamma * pR / rhoR);
     if (c.g4 * (cL + cR) <= uR - uL) {
-        res.rho = 0.; res.u = 0.; res.p = 0.; res.flag = 0; res.iters = 0;
+        res.rho = 0.; res.u = 0.; res.p = 0.; res.pstar = 0.; res.flag = 0; res.iters = 0;
         return res;
     }
     double pstar;
@@ -105,6 +106,7 @@ __device__ inline RiemannResult riemann_exact(const RiemannConsts &c, double rho
         if (it2 < 0) it = -1;
     }
     res.iters = it;
+    res.pstar = pstar;
     double fL, fdL, fR, fdR;
     pressure_fn(c, pstar, rhoL, pL, cL, fL, fdL);
     pressure_fn(c, pstar, rhoR, pR, cR, fR, fdR);
@@ -185,6 +187,23 @@ __device__ __forceinline__ double root5(double x) {
     return x * (y2 * y2);
 }
 
+// Two-rarefaction estimate of p* (Toro eq. 4.46), the default starting point
+// of both solvers; ROOT5 takes the gamma = 5/3 powers.  Not positive when the
+// states generate vacuum.
+template <bool ROOT5>
+__device__ __forceinline__ double two_rarefaction_guess(const RiemannConsts &k, double rhoL, double uL, double pL,
+                                                        double rhoR, double uR, double pR) {
+    const double cL = sqrt(k.gamma * pL / rhoL), cR = sqrt(k.gamma * pR / rhoR);
+    const double num = cL + cR - k.g7 * (uR - uL);
+    if (!(num > 0.)) return -1.;
+    if (ROOT5) {
+        const double t = num / (cL * rroot5(pL) + cR * rroot5(pR));
+        const double t2 = t * t;
+        return t2 * t2 * t;
+    }
+    return pow(num / (cL / pow(pL, k.g1) + cR / pow(pR, k.g1)), k.g3);
+}
+
 struct RiemannSide {
     double rho, u, p, c, invp, C, ak, bk, g4c;
 };
@@ -230,7 +249,7 @@ __device__ inline RiemannResult riemann_exact5(const RiemannConsts &k, double rh
     RiemannResult res;
     const RiemannSide L = make_side(k, rhoL, uL, pL), R = make_side(k, rhoR, uR, pR);
     if (k.g4 * (L.c + R.c) <= uR - uL) {
-        res.rho = 0.; res.u = 0.; res.p = 0.; res.flag = 0; res.iters = 0;
+        res.rho = 0.; res.u = 0.; res.p = 0.; res.pstar = 0.; res.flag = 0; res.iters = 0;
         return res;
     }
     const double du = uR - uL;
@@ -281,6 +300,7 @@ __device__ inline RiemannResult riemann_exact5(const RiemannConsts &k, double rh
         }
     }
     const double pstar = p;
+    res.pstar = pstar;
     if (iters < 0) {
         double invp = 1. / pstar, fdL, fdR, qL, qR;
         bool rL, rR;

@@ -55,14 +55,15 @@ class StepStats(ctypes.Structure):
     _fields_ = [("steps", ctypes.c_int), ("status", ctypes.c_uint), ("dt", ctypes.c_double),
                 ("time", ctypes.c_double), ("pair_interactions", ctypes.c_longlong),
                 ("faces", ctypes.c_longlong), ("newton_iterations", ctypes.c_longlong),
-                ("device_ms", ctypes.c_double)]
+                ("device_ms", ctypes.c_double), ("newton_fallbacks", ctypes.c_longlong)]
 
 
 EXPORTS = ["mlh_abi_version", "mlh_last_error", "mlh_create", "mlh_destroy", "mlh_set_fields",
            "mlh_get_fields", "mlh_step", "mlh_stage_array", "mlh_set_kernel_timing",
            "mlh_kernel_times", "mlh_reset_kernel_times", "mlh_probe_fp64_tflops",
            "mlh_grid_bounds_noalloc", "mlh_ensemble_create", "mlh_member_times", "mlh_set_graph_mode",
-           "mlh_autotune", "mlh_pstar_infer", "mlh_pstar_grad", "mlh_pstar_train"]
+           "mlh_autotune", "mlh_pstar_infer", "mlh_pstar_grad", "mlh_pstar_train", "mlh_set_pstar_weights",
+           "mlh_pstar_harvest"]
 
 _lib = None
 
@@ -119,6 +120,10 @@ def load(path: str = LIB_PATH):
     L.mlh_pstar_train.argtypes = [fp, fp, ctypes.c_longlong, ctypes.c_int, ctypes.c_int, ctypes.c_float,
                                   ctypes.c_uint, fp, fp]
     L.mlh_pstar_train.restype = ctypes.c_int
+    L.mlh_set_pstar_weights.argtypes = [vp, fp]
+    L.mlh_set_pstar_weights.restype = ctypes.c_int
+    L.mlh_pstar_harvest.argtypes = [vp, ctypes.c_int, fp, fp, ctypes.c_longlong, ctypes.POINTER(ctypes.c_longlong)]
+    L.mlh_pstar_harvest.restype = ctypes.c_int
     _lib = L
     return L
 
@@ -261,6 +266,24 @@ class Simulation:
 
     def set_graph_mode(self, on: bool):
         self.L.mlh_set_graph_mode(self.h, 1 if on else 0)
+
+    def set_pstar_weights(self, weights):
+        """Learned initial guess for the Riemann solves (None: two-rarefaction)."""
+        self._pstar_w = None if weights is None else np.ascontiguousarray(weights, dtype=np.float32)
+        st = self.L.mlh_set_pstar_weights(self.h, None if weights is None else _fptr(self._pstar_w))
+        if st != 0:
+            raise MLHError(st, "mlh_set_pstar_weights", self.L.mlh_last_error().decode())
+
+    def harvest(self, stride: int = 1, capacity: int = 1 << 22):
+        """One step recording (network input, log(p*/p_TR)) of every stride-th face,
+        p_TR the two-rarefaction guess of the face."""
+        x = np.zeros((capacity, 4), dtype=np.float32)
+        t = np.zeros(capacity, dtype=np.float32)
+        cnt = ctypes.c_longlong()
+        st = self.L.mlh_pstar_harvest(self.h, stride, _fptr(x), _fptr(t), capacity, ctypes.byref(cnt))
+        if st != 0:
+            raise MLHError(st, "mlh_pstar_harvest", self.L.mlh_last_error().decode())
+        return x[:cnt.value], t[:cnt.value]
 
     def autotune(self, trial_steps: int = 1) -> dict:
         t = Tuning()

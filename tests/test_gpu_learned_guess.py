@@ -1,0 +1,140 @@
+"""The learned p* initial guess inside the step.
+
+Faces are solved in two passes around one batched network launch (states and
+features, inference, Newton from p_TR * exp(y), p_TR the two-rarefaction
+guess, where |y| > 0.01; from p_TR elsewhere).  The converged p* satisfies
+the same stopping rule as from the two-rarefaction guess, so the state must
+stay on the oracle's trajectory within LEARNED_RTOL: the two Newton runs stop
+at different points inside the tolerance band, which moves fluxes by
+O(riemann_tol) relative.  A guess that does not converge restarts from the
+two-rarefaction guess, so even a useless network gives correct results.
+"""
+import numpy as np
+import pytest
+
+from meshlesshydro_gb300 import ic
+from meshlesshydro_gb300.config import MFVConfig
+from helpers import assert_close
+
+pytestmark = pytest.mark.gpu
+
+# fields after a few steps, normwise relative (riemann_tol is 1e-10)
+LEARNED_RTOL = 1e-9
+
+
+def _runtime():
+    from meshlesshydro_gb300 import build, runtime
+    build.build()
+    return runtime
+
+
+def _cases():
+    kh = ic.kelvin_helmholtz(n_side=40, seed=5)
+    sd = ic.sedov(n_side=12, seed=4, energy=0.05)
+    return [(MFVConfig.kelvin_helmholtz(kh), kh), (MFVConfig.sedov(sd, periodic=True), sd)]
+
+
+@pytest.fixture(scope="module")
+def trained():
+    """Weights fitted to faces harvested from the two cases."""
+    rt = _runtime()
+    xs, ts = [], []
+    for cfg, p in _cases():
+        s = rt.Simulation(cfg, p)
+        for _ in range(2):
+            x, t = s.harvest(stride=1, capacity=1 << 20)
+            xs.append(x); ts.append(t)
+        s.close()
+    x = np.concatenate(xs); t = np.concatenate(ts)
+    w, hist = rt.pstar_train(x, t, epochs=40, batch=2048, lr=2e-3, seed=1)
+    return w, hist, x, t
+
+
+def test_harvest_records_faces():
+    rt = _runtime()
+    cfg, p = _cases()[0]
+    s = rt.Simulation(cfg, p)
+    ref = rt.Simulation(cfg, p)
+    st = ref.step(1)
+    x, t = s.harvest(stride=3, capacity=1 << 20)
+    # every third canonical face with a converged solve
+    assert abs(x.shape[0] - (st.faces + 2) // 3) <= 1
+    assert np.all(np.isfinite(x)) and np.all(np.isfinite(t))
+    # harvesting is one ordinary step
+    a, b = s.get_state(), ref.get_state()
+    for k in a:
+        assert np.array_equal(a[k], b[k]), k
+
+
+def test_training_on_harvest(trained):
+    w, hist, x, t = trained
+    assert hist[-1] < 0.5 * hist[0], hist
+    rt = _runtime()
+    y = rt.pstar_infer(w, x)
+    rel = np.abs(np.exp(y - t) - 1.0)
+    assert np.median(rel) < 0.05, np.median(rel)
+
+
+@pytest.mark.parametrize("case", [0, 1], ids=["kh40", "sedov12"])
+def test_learned_guess_matches_oracle(trained, oracle_mod, case):
+    w = trained[0]
+    rt = _runtime()
+    cfg, p = _cases()[case]
+    s = rt.Simulation(cfg, p)
+    s.set_pstar_weights(w)
+    o = oracle_mod.Oracle(cfg, p)
+    nsteps = 3
+    st = s.step(nsteps)
+    for _ in range(nsteps):
+        assert o.step() == 0
+    assert st.status == 0
+    plain = rt.Simulation(cfg, p).step(nsteps)
+    print(f"newton iterations per face: learned {st.newton_iterations / st.faces:.4f} "
+          f"plain {plain.newton_iterations / plain.faces:.4f}; fallbacks {st.newton_fallbacks}")
+    assert st.newton_fallbacks <= 0.01 * st.faces, (st.newton_fallbacks, st.faces)
+    assert st.newton_iterations <= 2 * plain.newton_iterations
+    gs = s.get_state()
+    for key, v in o.state().items():
+        assert_close(gs[key], v, rtol=LEARNED_RTOL, what=key)
+
+
+def test_bad_guess_falls_back(oracle_mod):
+    """A network whose guess is e^20 times p_TR: Newton from there either
+    converges or restarts from the two-rarefaction guess; the state stays on
+    the oracle's trajectory either way."""
+    rt = _runtime()
+    cfg, p = _cases()[0]
+    w = rt.pstar_init(2)
+    w[-1] = 20.0            # output bias
+    s = rt.Simulation(cfg, p)
+    s.set_pstar_weights(w)
+    o = oracle_mod.Oracle(cfg, p)
+    st = s.step(2)
+    o.step(); o.step()
+    assert st.status == 0
+    gs = s.get_state()
+    for key, v in o.state().items():
+        assert_close(gs[key], v, rtol=LEARNED_RTOL, what=key)
+
+
+def test_learned_then_plain_graph_mode(trained):
+    """Switching the guess on and off drops the captured graph; graph replay
+    of the learned pipeline gives the bits of direct launches."""
+    w = trained[0]
+    rt = _runtime()
+    cfg, p = _cases()[0]
+    a = rt.Simulation(cfg, p)
+    b = rt.Simulation(cfg, p)
+    a.set_pstar_weights(w)
+    b.set_pstar_weights(w)
+    b.set_graph_mode(True)
+    a.step(3); b.step(3)
+    sa, sb = a.get_state(), b.get_state()
+    for k in sa:
+        assert np.array_equal(sa[k], sb[k]), k
+    a.set_pstar_weights(None)
+    b.set_pstar_weights(None)
+    a.step(1); b.step(1)
+    sa, sb = a.get_state(), b.get_state()
+    for k in sa:
+        assert np.array_equal(sa[k], sb[k]), k
