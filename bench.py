@@ -216,6 +216,56 @@ def run_reference(args):
     return 0
 
 
+def learned_section(runtime, make_sim, tuning, args, faces_per_step, st_plain, kt_plain, rho_plain, ws, n):
+    """The same steps with the learned p* guess: harvest faces of step 1
+    (plain pipeline), train the MLP on 90 % of them, step with the network
+    guess to the same step count and compare with the plain run."""
+    import torch
+    sim2 = make_sim()
+    if tuning:
+        sim2.set_tuning(tuning)
+    stride = max(1, int(faces_per_step // 2_000_000))
+    t0 = time.perf_counter()
+    x, t = sim2.harvest(stride=stride, capacity=int(faces_per_step // stride) + 64)
+    rng = np.random.default_rng(0)
+    perm = rng.permutation(x.shape[0])
+    nval = x.shape[0] // 10
+    val, tr = perm[:nval], perm[nval:]
+    t1 = time.perf_counter()
+    w, hist = runtime.pstar_train(x[tr], t[tr], epochs=20, batch=4096, lr=2e-3, seed=0)
+    t2 = time.perf_counter()
+    yv = runtime.pstar_infer(w, x[val])
+    rel = np.abs(np.exp(yv.astype(np.float64) - t[val]) - 1.0)
+    sim2.set_pstar_weights(w)
+    if args.warmup > 1:
+        sim2.step(args.warmup - 1)
+    sim2.reset_kernel_times()
+    sim2.set_kernel_timing(True)
+    torch.cuda.synchronize()
+    st = sim2.step(args.steps)
+    sim2.set_kernel_timing(False)
+    kt = sim2.kernel_times()
+    rho = sim2.get("rho")
+    sim2.close()
+    l1 = float(np.sum(np.abs(rho - rho_plain)) / np.sum(np.abs(rho_plain)))
+    return {"value": ws * n * st.steps / (st.device_ms / 1e3),
+            "plain_value": ws * n * st_plain.steps / (st_plain.device_ms / 1e3),
+            "newton_iterations_per_face": st.newton_iterations / max(st.faces, 1),
+            "plain_newton_iterations_per_face": st_plain.newton_iterations / max(st_plain.faces, 1),
+            "fallback_rate": st.newton_fallbacks / max(st.faces, 1),
+            "faces_kernel_ms_per_step": kt["faces_riemann"][1] / max(kt["faces_riemann"][0], 1),
+            "plain_faces_kernel_ms_per_step": kt_plain["faces_riemann"][1] / max(kt_plain["faces_riemann"][0], 1),
+            "density_L1_vs_plain": l1,
+            "status": runtime.status_names(st.status),
+            "guess": "p_TR * exp(y) where |y| > 0.01, else p_TR (two-rarefaction)",
+            "train": {"samples": int(tr.size), "val_samples": int(nval), "harvest_stride": stride,
+                      "harvest_step": 1, "epochs": 20, "batch": 4096, "lr": 2e-3,
+                      "loss_first_epoch": float(hist[0]), "loss_last_epoch": float(hist[-1]),
+                      "val_median_rel_err": float(np.median(rel)) if nval else None,
+                      "val_p90_rel_err": float(np.quantile(rel, 0.9)) if nval else None,
+                      "harvest_s": t1 - t0, "train_s": t2 - t1}}
+
+
 def run_mlh(args):
     import torch
     ws, rank, local = dist_env()
@@ -258,6 +308,9 @@ def run_mlh(args):
     kt = sim.kernel_times()
     faces_per_step = st.faces / max(st.steps, 1)
     pairs_per_step = st.pair_interactions / max(st.steps, 1)
+    rho_plain = sim.get("rho")      # density of step warmup + steps (autotune restored its trials)
+    make_sim = ((lambda: runtime.Simulation(cfg, members=members)) if ensemble
+                else (lambda: runtime.Simulation(cfg, p)))
 
     extra = {}
     if ensemble:
@@ -289,6 +342,9 @@ def run_mlh(args):
                               "sequential": "each member its own context, one mlh_step(1) call per member per step, "
                                             f"{seq_steps} steps, wall clock",
                               "batched_over_sequential": graph_value / seq_value}}
+
+    if not args.no_learned:
+        extra["learned"] = learned_section(runtime, make_sim, tuning, args, faces_per_step, st, kt, rho_plain, ws, p.n)
 
     # end to end through the C ABI with host buffers: H2D of the state,
     # one step, D2H of the state, every step (pinned host memory)
@@ -375,6 +431,7 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
     ap.add_argument("--no-autotune", action="store_true")
+    ap.add_argument("--no-learned", action="store_true", help="skip the learned p* guess comparison")
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference(args)

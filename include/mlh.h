@@ -137,6 +137,10 @@ typedef struct mlh_tuning {
  * state, which is restored afterwards), keeps the fastest in the context and
  * reports them in *out (may be NULL).  Needs one state-sized temporary. */
 int mlh_autotune(mlh_ctx *ctx, int trial_steps, mlh_tuning *out);
+/* Set the launch shapes directly (for example those an autotuned context of
+ * the same workload reported).  Threads per block: 64, 128 or 256; blocks
+ * per SM 1..32; warps per SM 8..256.  MLH_ERR_INVALID otherwise. */
+int mlh_set_tuning(mlh_ctx *ctx, const mlh_tuning *tuning);
 
 /* Graph mode: mlh_step captures one step into a CUDA graph (once, and again
  * after a capacity change) and replays it; kernel timing bypasses it. */

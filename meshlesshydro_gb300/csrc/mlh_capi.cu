@@ -90,6 +90,8 @@ struct mlh_ctx {
     FaceState *fstate = nullptr;
     float4 *feat = nullptr;
     float *yguess = nullptr;
+    int *queueFace = nullptr;   // faces handed to the network (learned guess)
+    int *queueCount = nullptr;
     Harvest harvest{};
     // CUDA graph of one step, replayed by mlh_step in graph mode
     bool graph_mode = false;
@@ -108,7 +110,8 @@ namespace {
 void free_neighbour_buffers(mlh_ctx *c) {
     cudaFree(c->nbr); cudaFree(c->rr); cudaFree(c->ww); cudaFree(c->psi); cudaFree(c->faceOf); cudaFree(c->faces);
     cudaFree(c->Fface);
-    cudaFree(c->fstate); cudaFree(c->feat); cudaFree(c->yguess);
+    cudaFree(c->fstate); cudaFree(c->feat); cudaFree(c->yguess); cudaFree(c->queueFace); cudaFree(c->queueCount);
+    c->queueFace = nullptr; c->queueCount = nullptr;
     c->nbr = nullptr; c->rr = nullptr; c->ww = nullptr; c->psi = nullptr; c->faceOf = nullptr; c->faces = nullptr;
     c->Fface = nullptr; c->fstate = nullptr; c->feat = nullptr; c->yguess = nullptr;
 }
@@ -128,6 +131,8 @@ int alloc_neighbour_buffers(mlh_ctx *c) {
         CK(dalloc(&c->fstate, faces));
         CK(dalloc(&c->feat, faces));
         CK(dalloc(&c->yguess, faces));
+        CK(dalloc(&c->queueFace, faces));
+        CK(dalloc(&c->queueCount, 1));
     }
     return 0;
 }
@@ -237,7 +242,8 @@ StepArgs make_args(mlh_ctx *c, double dt_max) {
     a.dt = c->dt; a.simTime = c->simTime; a.stepsDone = c->stepsDone;
     a.scanTiles = c->scanTiles; a.scanTotal = c->scanTotal;
     a.learned = c->learned ? 1 : 0;
-    a.fstate = c->fstate; a.feat = c->feat; a.yguess = c->yguess; a.mlp_packed = c->mlp_packed;
+    a.fstate = c->fstate; a.feat = c->feat; a.yguess = c->yguess;
+    a.queueFace = c->queueFace; a.queueCount = c->queueCount; a.mlp_packed = c->mlp_packed;
     a.harvest = c->harvest;
     a.timer = c->timing ? timer_cb : nullptr;
     a.timer_ctx = c;
@@ -544,6 +550,22 @@ int mlh_step(mlh_ctx *c, int nsteps, double dt_max, mlh_step_stats *stats) {
 // Coordinate search over the launch shapes: each candidate runs `trial_steps`
 // steps with per-kernel timing from a saved copy of the state, which is put
 // back afterwards (positions, velocities, masses, energies, member times).
+int mlh_set_tuning(mlh_ctx *c, const mlh_tuning *t) {
+    auto threads_ok = [](int v) { return v == 64 || v == 128 || v == 256; };
+    if (!c || !t || !threads_ok(t->face_threads) || !threads_ok(t->grad_threads) || t->face_blocks_per_sm < 1 ||
+        t->face_blocks_per_sm > 32 || t->nns_warps_per_sm < 8 || t->nns_warps_per_sm > 256) {
+        g_last_error = "invalid tuning";
+        return MLH_ERR_INVALID;
+    }
+    CK(cudaStreamSynchronize(c->stream));
+    c->tune.face_threads = t->face_threads;
+    c->tune.face_blocks_per_sm = t->face_blocks_per_sm;
+    c->tune.grad_threads = t->grad_threads;
+    c->tune.nns_warps_per_sm = t->nns_warps_per_sm;
+    drop_graph(c);
+    return 0;
+}
+
 int mlh_autotune(mlh_ctx *c, int trial_steps, mlh_tuning *out) {
     if (!c || trial_steps < 1) { g_last_error = "invalid argument"; return MLH_ERR_INVALID; }
     const size_t n = (size_t)c->n, nm = (size_t)c->nmembers;

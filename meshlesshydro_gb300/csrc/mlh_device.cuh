@@ -77,8 +77,8 @@ struct Geo {        // E_i^{-1}, 1/omega_i, omega_i, sound speed
 struct FaceRef {    // canonical face: owner i, slot index, reverse slot (images)
     int i, slot, rslot, pad;
 };
-// Face-frame states of one face between the two halves of the learned-guess
-// face pipeline: R[5], L[5], A[3], v_frame[3], A/|A| [3], flag
+// Face-frame state of one deferred face between the two passes of the
+// learned-guess face pipeline: R[5], L[5], A[3], v_frame[3], A/|A| [3], p_TR
 struct FaceState {
     double v[20];
 };

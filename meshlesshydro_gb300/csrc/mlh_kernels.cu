@@ -919,10 +919,14 @@ __device__ __forceinline__ void rot3(const double *a, const double *b, double *L
 // Network inputs of a face from its face-frame states (left = particle i):
 // log(rhoR/rhoL), (uR - uL)/cL, log(pR/pL), log(cR/cL).
 // The network predicts y = log(p* / p_TR), p_TR the two-rarefaction guess of
-// the face.  Where |y| is below PSTAR_GATE the correction is within the
-// network's own error (BF16 activations) and Newton starts from p_TR as in the
-// plain pipeline, so faces the cheap guess already serves keep its iteration
-// count and its bits.
+// the face.  p_TR is exact when both waves are rarefactions and its error grows
+// with the shock strength p_TR / min(pL, pR) - 1 (about 1e-6 at 0.2, 3e-3 at
+// 2-4, 2e-2 beyond 4, measured on random states), so only faces with
+// p_TR > PSTAR_HARD * min(pL, pR) are handed to the network; the others are
+// solved from p_TR in the first pass.  Where |y| is below PSTAR_GATE the
+// correction is within the network's own error (BF16 activations) and Newton
+// starts from p_TR as well.
+constexpr double PSTAR_HARD = 2.0;
 constexpr float PSTAR_GATE = 0.01f;
 
 __device__ __forceinline__ float4 pstar_features(const double *R, const double *L, double gamma) {
@@ -942,11 +946,13 @@ __device__ __forceinline__ float4 pstar_features(const double *R, const double *
 // Helper::rotationMatrix2D/3D(unitX, hatA) is the transpose of the forward
 // one, bit for bit, so it is not recomputed.  Output slot order:
 // [mass, energy, px, py, pz].
-// MODE 0: the whole face.  MODE 1 (learned guess, first half): stop after the
-// rotation into the face frame, store the face state and the network inputs.
-// MODE 2 (second half): reload the state, solve from the network's guess,
-// project the flux.  `harvest` (MODE 0) records network inputs and targets
-// log(p*/p_TR) of every `stride`-th face.
+// MODE 0: the whole face.  MODE 1 (learned guess, first pass): faces with a
+// strong shock in p_TR stop after the rotation into the face frame and are
+// queued (state and network inputs at the queue position, order immaterial:
+// each face writes only its own flux); all other faces are finished as in
+// MODE 0.  MODE 2 (second pass, over the queue): reload the state, solve from
+// the network's guess, project the flux.  `harvest` (MODE 0) records network
+// inputs and targets log(p*/p_TR) of every `stride`-th face.
 template <int D, bool ROOT5, int MODE>
 __global__ void __launch_bounds__(256) k_faces(Params p, const Member *__restrict__ members,
                                                const int *__restrict__ memberOf, const GridInfo *__restrict__ grids,
@@ -957,19 +963,23 @@ __global__ void __launch_bounds__(256) k_faces(Params p, const Member *__restric
                                                double *__restrict__ Fface, unsigned long long *__restrict__ newtonSum,
                                                unsigned *__restrict__ status, FaceState *__restrict__ fstate,
                                                float4 *__restrict__ feat, const float *__restrict__ yguess,
-                                               Harvest hv) {
+                                               int *__restrict__ queueFace, int *__restrict__ queueCount, Harvest hv) {
     constexpr int NV = D + 2;
-    const int nf = *faceTotal < p.faces_cap ? *faceTotal : p.faces_cap;
+    int nf = *faceTotal < p.faces_cap ? *faceTotal : p.faces_cap;
+    if (MODE == 2) nf = *queueCount < nf ? *queueCount : nf;
     const RiemannConsts rc = make_riemann_consts(p.gamma, p.rtol, p.rmaxit);
     const double gamma = p.gamma;
     unsigned long long iters_local = 0, fallback_local = 0;
     unsigned st_local = 0;
-    for (int f = blockIdx.x * blockDim.x + threadIdx.x; f < nf; f += gridDim.x * blockDim.x) {
+    for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < nf; t += gridDim.x * blockDim.x) {
+        // MODE 2 walks the queue: t is the queue position, f the face
+        const int f = MODE == 2 ? queueFace[t] : t;
         double R[5], L[5], A[3] = {0., 0., 0.}, vf[3] = {0., 0., 0.}, hatA[3] = {0., 0., 0.}, Lam[9];
         const double unitX[3] = {1., 0., 0.};
+        double ptr_q = -1.;   // MODE 2: two-rarefaction guess found in MODE 1
         if (MODE == 2) {
-            const FaceState &fs = fstate[f];
-            if (!(fs.v[0] == fs.v[0]) && fs.v[19] == 1.) continue;   // face without owner (flagged in MODE 1)
+            const FaceState &fs = fstate[t];
+            ptr_q = fs.v[19];
 #pragma unroll
             for (int k = 0; k < 5; ++k) { R[k] = fs.v[k]; L[k] = fs.v[5 + k]; }
 #pragma unroll
@@ -980,7 +990,6 @@ __global__ void __launch_bounds__(256) k_faces(Params p, const Member *__restric
         const FaceRef fr = faces[f];
         if (fr.i < 0 || fr.slot < 0) {
             st_local |= ST_ASYMMETRIC;
-            if (MODE == 1) { fstate[f].v[0] = __longlong_as_double(0x7ff8000000000000ll); fstate[f].v[19] = 1.; }
             continue;
         }
         const int i = fr.i;
@@ -1127,25 +1136,29 @@ __global__ void __launch_bounds__(256) k_faces(Params p, const Member *__restric
             R[3] = Lam[3] * bL0 + Lam[4] * bL1 + Lam[5] * bL2;
             R[4] = Lam[6] * bL0 + Lam[7] * bL1 + Lam[8] * bL2;
         }
-        if (MODE == 1) {
-            FaceState &fs = fstate[f];
+        }   // MODE != 2
+        double guess = -1.;
+        if (MODE == 2) {
+            const float y = yguess[t];
+            if (isfinite(y) && fabsf(y) > PSTAR_GATE && fabsf(y) < 30.f)
+                guess = ptr_q * (double)__expf(y);
+        }
+        // MODE 1 defers faces whose two-rarefaction guess says strong shock
+        const double defer = MODE == 1 ? PSTAR_HARD * fmin(R[1], L[1]) : 0.;
+        RiemannResult rs = ROOT5 ? riemann_exact5(rc, R[0], R[2], R[1], L[0], L[2], L[1], guess, defer)
+                                 : riemann_exact(rc, R[0], R[2], R[1], L[0], L[2], L[1], guess, defer);
+        if (MODE == 1 && rs.flag == 2) {
+            const int q = atomicAdd(queueCount, 1);   // < faces on this step <= faces_cap
+            FaceState &fs = fstate[q];
 #pragma unroll
             for (int k = 0; k < 5; ++k) { fs.v[k] = R[k]; fs.v[5 + k] = L[k]; }
 #pragma unroll
             for (int a = 0; a < 3; ++a) { fs.v[10 + a] = A[a]; fs.v[13 + a] = vf[a]; fs.v[16 + a] = hatA[a]; }
-            fs.v[19] = 0.;
-            feat[f] = pstar_features(R, L, gamma);
+            fs.v[19] = rs.pstar;   // the two-rarefaction guess
+            feat[q] = pstar_features(R, L, gamma);
+            queueFace[q] = f;
             continue;
         }
-        }   // MODE != 2
-        double guess = -1.;
-        if (MODE == 2) {
-            const float y = yguess[f];
-            if (isfinite(y) && fabsf(y) > PSTAR_GATE && fabsf(y) < 30.f)
-                guess = two_rarefaction_guess<ROOT5>(rc, R[0], R[2], R[1], L[0], L[2], L[1]) * (double)__expf(y);
-        }
-        RiemannResult rs = ROOT5 ? riemann_exact5(rc, R[0], R[2], R[1], L[0], L[2], L[1], guess)
-                                 : riemann_exact(rc, R[0], R[2], R[1], L[0], L[2], L[1], guess);
         if (MODE == 0 && hv.stride > 0 && f % hv.stride == 0) {
             const int slot = f / hv.stride;
             const double ptr = two_rarefaction_guess<ROOT5>(rc, R[0], R[2], R[1], L[0], L[2], L[1]);
@@ -1377,10 +1390,11 @@ void launch_step(StepArgs &a) {
 #define MLH_FACES(R5, MODE)                                                                                      \
     k_faces<D, R5, MODE><<<fB, fT, 0, s>>>(p, a.members, a.memberOf, a.grids, a.prim, a.geo, a.grad, a.nbr, a.psi, \
                                            a.faceOff + p.n, a.faces, a.dt, a.Fface, a.newtonSum, a.status,       \
-                                           a.fstate, a.feat, a.yguess, a.harvest)
+                                           a.fstate, a.feat, a.yguess, a.queueFace, a.queueCount, a.harvest)
     if (a.learned) {
+        cudaMemsetAsync(a.queueCount, 0, sizeof(int), s);
         if (a.root5) MLH_FACES(true, 1); else MLH_FACES(false, 1);
-        pstar_infer_dev(a.feat, a.faceOff + p.n, (int)a.faces_cap, a.mlp_packed, a.yguess, a.sm_count, s);
+        pstar_infer_dev(a.feat, a.queueCount, (int)a.faces_cap, a.mlp_packed, a.yguess, a.sm_count, s);
         if (a.root5) MLH_FACES(true, 2); else MLH_FACES(false, 2);
     } else {
         if (a.root5) MLH_FACES(true, 0); else MLH_FACES(false, 0);

@@ -56,11 +56,14 @@ struct StepArgs {
     double *dt, *simTime;
     int *stepsDone;
     int *scanTiles, *scanTotal;
-    // learned p* guess: face states, network inputs and outputs, packed weights
+    // learned p* guess: queue of the faces handed to the network (face ids,
+    // their face-frame states, network inputs and outputs), packed weights
     int learned;
     FaceState *fstate;
     float4 *feat;
     float *yguess;
+    int *queueFace;
+    int *queueCount;
     const void *mlp_packed;
     Harvest harvest;
     // optional per-kernel timer callback (phase 0 = before, 1 = after)

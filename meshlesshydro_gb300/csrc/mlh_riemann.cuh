@@ -58,7 +58,8 @@ __device__ __forceinline__ void pressure_fn(const RiemannConsts &c, double p, do
 struct RiemannResult {
     double rho, u, p;
     double pstar;   // star-region pressure
-    int flag;       // -1: left of the contact sampled, +1: right, 0: vacuum
+    int flag;       // -1: left of the contact sampled, +1: right, 0: vacuum,
+                    // 2: not solved (two-rarefaction guess above `defer_above`)
     int iters;      // Newton iterations (< 0: no convergence)
 };
 
@@ -84,9 +85,12 @@ __device__ __forceinline__ int newton_pstar(const RiemannConsts &c, double p0, d
 
 // Solve with the two-rarefaction guess (or `guess` when > 0, falling back to
 // the two-rarefaction guess if Newton does not converge from it), then sample
-// at S = 0 (Toro section 4.5).
+// at S = 0 (Toro section 4.5).  With defer_above > 0 and no guess, a problem
+// whose two-rarefaction guess exceeds defer_above returns unsolved (flag 2,
+// pstar = that guess) for a second pass with a better guess.
 __device__ inline RiemannResult riemann_exact(const RiemannConsts &c, double rhoL, double uL, double pL,
-                                              double rhoR, double uR, double pR, double guess = -1.) {
+                                              double rhoR, double uR, double pR, double guess = -1.,
+                                              double defer_above = 0.) {
     RiemannResult res;
     double cL = sqrt(c.gamma * pL / rhoL);
     double cR = sqrt(c.gamma * pR / rhoR);
@@ -101,6 +105,10 @@ __device__ inline RiemannResult riemann_exact(const RiemannConsts &c, double rho
         double num = cL + cR - c.g7 * (uR - uL);
         double den = cL / pow(pL, c.g1) + cR / pow(pR, c.g1);
         double p0 = pow(num / den, c.g3);
+        if (defer_above > 0. && !(guess > 0.) && p0 > defer_above) {
+            res.rho = 0.; res.u = 0.; res.p = 0.; res.pstar = p0; res.flag = 2; res.iters = 0;
+            return res;
+        }
         int it2 = newton_pstar(c, p0, rhoL, uL, pL, cL, rhoR, uR, pR, cR, pstar);
         it = (guess > 0. && it2 >= 0) ? it2 + c.max_iter : it2;
         if (it2 < 0) it = -1;
@@ -245,7 +253,8 @@ __device__ __forceinline__ void pressure_fn5(const RiemannSide &s, double p, dou
 // evaluation plus its derivative times the final (<= tol relative) step,
 // which differs from re-evaluating f at p* by O(tol^2) relative.
 __device__ inline RiemannResult riemann_exact5(const RiemannConsts &k, double rhoL, double uL, double pL,
-                                               double rhoR, double uR, double pR, double guess = -1.) {
+                                               double rhoR, double uR, double pR, double guess = -1.,
+                                               double defer_above = 0.) {
     RiemannResult res;
     const RiemannSide L = make_side(k, rhoL, uL, pL), R = make_side(k, rhoR, uR, pR);
     if (k.g4 * (L.c + R.c) <= uR - uL) {
@@ -263,6 +272,10 @@ __device__ inline RiemannResult riemann_exact5(const RiemannConsts &k, double rh
         double t = num / den;
         double t2 = t * t;
         p0 = t2 * t2 * t;
+        if (defer_above > 0. && p0 > defer_above) {   // see riemann_exact
+            res.rho = 0.; res.u = 0.; res.p = 0.; res.pstar = p0; res.flag = 2; res.iters = 0;
+            return res;
+        }
     }
     double p, fLs = 0., fRs = 0., qLs = -1., qRs = -1.;
     int iters = -1, extra = 0;

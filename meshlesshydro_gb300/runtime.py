@@ -62,7 +62,7 @@ EXPORTS = ["mlh_abi_version", "mlh_last_error", "mlh_create", "mlh_destroy", "ml
            "mlh_get_fields", "mlh_step", "mlh_stage_array", "mlh_set_kernel_timing",
            "mlh_kernel_times", "mlh_reset_kernel_times", "mlh_probe_fp64_tflops",
            "mlh_grid_bounds_noalloc", "mlh_ensemble_create", "mlh_member_times", "mlh_set_graph_mode",
-           "mlh_autotune", "mlh_pstar_infer", "mlh_pstar_grad", "mlh_pstar_train", "mlh_set_pstar_weights",
+           "mlh_autotune", "mlh_set_tuning", "mlh_pstar_infer", "mlh_pstar_grad", "mlh_pstar_train", "mlh_set_pstar_weights",
            "mlh_pstar_harvest"]
 
 _lib = None
@@ -112,6 +112,8 @@ def load(path: str = LIB_PATH):
     L.mlh_set_graph_mode.restype = ctypes.c_int
     L.mlh_autotune.argtypes = [vp, ctypes.c_int, ctypes.POINTER(Tuning)]
     L.mlh_autotune.restype = ctypes.c_int
+    L.mlh_set_tuning.argtypes = [vp, ctypes.POINTER(Tuning)]
+    L.mlh_set_tuning.restype = ctypes.c_int
     fp = ctypes.POINTER(ctypes.c_float)
     L.mlh_pstar_infer.argtypes = [fp, fp, ctypes.c_int, fp]
     L.mlh_pstar_infer.restype = ctypes.c_int
@@ -291,6 +293,12 @@ class Simulation:
         if st != 0:
             raise MLHError(st, "mlh_autotune", self.L.mlh_last_error().decode())
         return {k: getattr(t, k) for k, _ in Tuning._fields_}
+
+    def set_tuning(self, tuning: dict):
+        t = Tuning(**{k: int(tuning[k]) for k, _ in Tuning._fields_})
+        st = self.L.mlh_set_tuning(self.h, ctypes.byref(t))
+        if st != 0:
+            raise MLHError(st, "mlh_set_tuning", self.L.mlh_last_error().decode())
 
     def step(self, nsteps: int = 1, dt_max: float = 0.0, check: bool = True) -> StepStats:
         stats = StepStats()

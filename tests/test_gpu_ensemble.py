@@ -114,3 +114,19 @@ def test_autotune_keeps_results_bitwise():
     for key in sa:
         assert np.array_equal(sa[key], sb[key]), key
     assert np.array_equal(a.member_times()[1], b.member_times()[1])
+
+
+def test_set_tuning_validates_and_keeps_bits():
+    from meshlesshydro_gb300 import runtime
+    members = _members()
+    cfg = MFVConfig.kelvin_helmholtz(members[0])
+    a = _sim(cfg, members)
+    b = _sim(cfg, members)
+    b.set_tuning({"face_threads": 256, "face_blocks_per_sm": 3, "grad_threads": 64, "nns_warps_per_sm": 16})
+    with pytest.raises(runtime.MLHError):
+        b.set_tuning({"face_threads": 96, "face_blocks_per_sm": 3, "grad_threads": 64, "nns_warps_per_sm": 16})
+    a.step(2)
+    b.step(2)
+    sa, sb = a.get_state(), b.get_state()
+    for key in sa:
+        assert np.array_equal(sa[key], sb[key]), key
