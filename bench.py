@@ -252,7 +252,8 @@ def learned_section(runtime, make_sim, tuning, args, faces_per_step, st_plain, k
             "plain_value": ws * n * st_plain.steps / (st_plain.device_ms / 1e3),
             "newton_iterations_per_face": st.newton_iterations / max(st.faces, 1),
             "plain_newton_iterations_per_face": st_plain.newton_iterations / max(st_plain.faces, 1),
-            "fallback_rate": st.newton_fallbacks / max(st.faces, 1),
+            "fallback_rate": st.newton_fallbacks / max(st.learned_faces, 1),
+            "learned_face_fraction": st.learned_faces / max(st.faces, 1),
             "faces_kernel_ms_per_step": kt["faces_riemann"][1] / max(kt["faces_riemann"][0], 1),
             "plain_faces_kernel_ms_per_step": kt_plain["faces_riemann"][1] / max(kt_plain["faces_riemann"][0], 1),
             "density_L1_vs_plain": l1,

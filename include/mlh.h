@@ -91,6 +91,8 @@ typedef struct mlh_step_stats {
     long long newton_fallbacks;      /* faces whose learned p* guess did not
                                         converge and restarted from the
                                         two-rarefaction guess (0 without one) */
+    long long learned_faces;         /* faces solved from the learned guess
+                                        (strong shocks; 0 without one) */
 } mlh_step_stats;
 
 /* One simulation of an ensemble: its particle count (members are stored back

@@ -365,7 +365,7 @@ static int create_impl(const mlh_config *cfg, int nmembers, const mlh_member *md
     A(cell, n); A(cellList, n);
     A(noi, n); A(noiImg, n); A(faceCnt, n); A(faceOff, n + 1);
     A(prim, n); A(geo, n); A(grad, n); A(gradRaw, n); A(fluxSums, n * 5);
-    A(status, 1); A(dtbits, nm); A(newtonSum, 2); A(dt, nm); A(simTime, nm); A(stepsDone, 1);
+    A(status, 1); A(dtbits, nm); A(newtonSum, 3); A(dt, nm); A(simTime, nm); A(stepsDone, 1);
     A(scanTiles, n / 4096 + 1024); A(scanTotal, 1);
 #undef A
     if ((rc = alloc_cell_buffers(c))) return fail(rc);
@@ -382,7 +382,7 @@ static int create_impl(const mlh_config *cfg, int nmembers, const mlh_member *md
     cudaMemsetAsync(c->status, 0, sizeof(unsigned), c->stream);
     cudaMemsetAsync(c->simTime, 0, sizeof(double) * nm, c->stream);
     cudaMemsetAsync(c->dt, 0, sizeof(double) * nm, c->stream);
-    cudaMemsetAsync(c->newtonSum, 0, 2 * sizeof(unsigned long long), c->stream);
+    cudaMemsetAsync(c->newtonSum, 0, 3 * sizeof(unsigned long long), c->stream);
     cudaMemsetAsync(c->stepsDone, 0, sizeof(int), c->stream);
     if ((rc = upload(c, init))) return fail(rc);
     if (cudaStreamSynchronize(c->stream) != cudaSuccess) return fail(cuda_fail(cudaGetLastError(), "create sync"));
@@ -468,7 +468,7 @@ int mlh_step(mlh_ctx *c, int nsteps, double dt_max, mlh_step_stats *stats) {
     if (!c || nsteps < 0) { g_last_error = "invalid argument"; return MLH_ERR_INVALID; }
     unsigned accumulated = 0;
     long long pairs = 0, faces = 0;
-    unsigned long long newton = 0, fallbacks = 0;
+    unsigned long long newton = 0, fallbacks = 0, deferred = 0;
     double dev_ms = 0.;
     int done_total = 0;
     int remaining = nsteps;
@@ -481,7 +481,7 @@ int mlh_step(mlh_ctx *c, int nsteps, double dt_max, mlh_step_stats *stats) {
         }
         CK(cudaMemsetAsync(c->status, 0, sizeof(unsigned), c->stream));
         CK(cudaMemsetAsync(c->stepsDone, 0, sizeof(int), c->stream));
-        CK(cudaMemsetAsync(c->newtonSum, 0, 2 * sizeof(unsigned long long), c->stream));
+        CK(cudaMemsetAsync(c->newtonSum, 0, 3 * sizeof(unsigned long long), c->stream));
         CK(cudaEventRecord(c->ev0, c->stream));
         if (use_graph) {
             for (int k = 0; k < remaining; ++k) CK(cudaGraphLaunch(c->graph_exec, c->stream));
@@ -498,12 +498,13 @@ int mlh_step(mlh_ctx *c, int nsteps, double dt_max, mlh_step_stats *stats) {
         if (c->timing) collect_timers(c);
         unsigned st = 0;
         int done = 0;
-        unsigned long long nsum[2] = {0, 0};
+        unsigned long long nsum[3] = {0, 0, 0};
         CK(cudaMemcpy(&st, c->status, sizeof(unsigned), cudaMemcpyDeviceToHost));
         CK(cudaMemcpy(&done, c->stepsDone, sizeof(int), cudaMemcpyDeviceToHost));
-        CK(cudaMemcpy(nsum, c->newtonSum, 2 * sizeof(unsigned long long), cudaMemcpyDeviceToHost));
+        CK(cudaMemcpy(nsum, c->newtonSum, 3 * sizeof(unsigned long long), cudaMemcpyDeviceToHost));
         newton += nsum[0];
         fallbacks += nsum[1];
+        deferred += nsum[2];
         done_total += done;
         remaining -= done;
         // per-step interaction counts of the last step
@@ -543,6 +544,7 @@ int mlh_step(mlh_ctx *c, int nsteps, double dt_max, mlh_step_stats *stats) {
         stats->newton_iterations = (long long)newton;
         stats->device_ms = dev_ms;
         stats->newton_fallbacks = (long long)fallbacks;
+        stats->learned_faces = (long long)deferred;
     }
     return (int)(accumulated & ~(unsigned)MLH_ERR_NGB_OVERFLOW & ~ST_CAPACITY) ? (int)accumulated : 0;
 }

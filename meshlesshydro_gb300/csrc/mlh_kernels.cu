@@ -969,7 +969,7 @@ __global__ void __launch_bounds__(256) k_faces(Params p, const Member *__restric
     if (MODE == 2) nf = *queueCount < nf ? *queueCount : nf;
     const RiemannConsts rc = make_riemann_consts(p.gamma, p.rtol, p.rmaxit);
     const double gamma = p.gamma;
-    unsigned long long iters_local = 0, fallback_local = 0;
+    unsigned long long iters_local = 0, fallback_local = 0, deferred_local = 0;
     unsigned st_local = 0;
     for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < nf; t += gridDim.x * blockDim.x) {
         // MODE 2 walks the queue: t is the queue position, f the face
@@ -1174,6 +1174,7 @@ __global__ void __launch_bounds__(256) k_faces(Params p, const Member *__restric
             // converge adds max_iter wasted steps before the restart from the
             // two-rarefaction guess
             if (MODE == 2 && rs.iters > rc.max_iter) ++fallback_local;
+            if (MODE == 2) ++deferred_local;
             iters_local += (unsigned long long)rs.iters;
         }
         double vSol[3] = {rs.u, 0., 0.};
@@ -1220,11 +1221,13 @@ __global__ void __launch_bounds__(256) k_faces(Params p, const Member *__restric
     for (int o = 16; o > 0; o >>= 1) {
         iters_local += __shfl_xor_sync(0xffffffffu, iters_local, o);
         fallback_local += __shfl_xor_sync(0xffffffffu, fallback_local, o);
+        deferred_local += __shfl_xor_sync(0xffffffffu, deferred_local, o);
         st_local |= __shfl_xor_sync(0xffffffffu, st_local, o);
     }
     if ((threadIdx.x & 31) == 0) {
         if (iters_local) atomicAdd(newtonSum, iters_local);
         if (fallback_local) atomicAdd(newtonSum + 1, fallback_local);
+        if (deferred_local) atomicAdd(newtonSum + 2, deferred_local);
         if (st_local) flag(status, st_local);
     }
 }

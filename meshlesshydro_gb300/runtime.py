@@ -55,7 +55,8 @@ class StepStats(ctypes.Structure):
     _fields_ = [("steps", ctypes.c_int), ("status", ctypes.c_uint), ("dt", ctypes.c_double),
                 ("time", ctypes.c_double), ("pair_interactions", ctypes.c_longlong),
                 ("faces", ctypes.c_longlong), ("newton_iterations", ctypes.c_longlong),
-                ("device_ms", ctypes.c_double), ("newton_fallbacks", ctypes.c_longlong)]
+                ("device_ms", ctypes.c_double), ("newton_fallbacks", ctypes.c_longlong),
+                ("learned_faces", ctypes.c_longlong)]
 
 
 EXPORTS = ["mlh_abi_version", "mlh_last_error", "mlh_create", "mlh_destroy", "mlh_set_fields",

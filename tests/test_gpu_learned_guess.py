@@ -90,7 +90,9 @@ def test_learned_guess_matches_oracle(trained, oracle_mod, case):
     assert st.status == 0
     plain = rt.Simulation(cfg, p).step(nsteps)
     print(f"newton iterations per face: learned {st.newton_iterations / st.faces:.4f} "
-          f"plain {plain.newton_iterations / plain.faces:.4f}; fallbacks {st.newton_fallbacks}")
+          f"plain {plain.newton_iterations / plain.faces:.4f}; fallbacks {st.newton_fallbacks}; "
+          f"learned faces {st.learned_faces} of {st.faces}")
+    assert 0 <= st.learned_faces <= st.faces
     assert st.newton_fallbacks <= 0.01 * st.faces, (st.newton_fallbacks, st.faces)
     assert st.newton_iterations <= 2 * plain.newton_iterations
     gs = s.get_state()
