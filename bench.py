@@ -45,7 +45,7 @@ LAUNCHES_PER_STEP = 18   # kernels launched by one mlh_step iteration (see csrc/
 # (profiles/sedov64_step_kernels.md): FP64 operations executed per face
 # (2 x DFMA + DADD + DMUL thread instructions / faces) and DRAM bytes
 # (read + write) per face.
-FACE_FP64_FLOPS = {3: 772.0}
+FACE_FP64_FLOPS = {3: 786.0}
 FACE_DRAM_BYTES = {3: 209.0}
 
 
