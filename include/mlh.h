@@ -15,7 +15,7 @@
 extern "C" {
 #endif
 
-#define MLH_ABI_VERSION 1
+#define MLH_ABI_VERSION 2
 
 /* Status bits.  The reference exits instead (demonstrator/src/Particles.cpp:
  * 348-352 exit(1) neighbour overflow, :2249-2253 exit(3), :1878-1881 exit(6)
@@ -52,7 +52,8 @@ typedef struct mlh_config {
     int meshless_finite_mass;   /* MESHLESS_FINITE_MASS */
     int move_particles;         /* MOVE_PARTICLES */
     int first_order_quad_point; /* FIRST_ORDER_QUAD_POINT */
-    int int_abs;                /* limiters use int abs(int) (see DESIGN) */
+    int int_abs;                /* limiters use int abs(int), the binding of the reference's unqualified
+                                   abs(double) when no <math.h>/<stdlib.h> is seen */
     int image_pairwise_limiter; /* pairwise limiter also on periodic-image faces */
     int riemann_max_iter;       /* Newton iteration cap */
     int max_neighbours;         /* slots per particle; 0 = automatic */
@@ -66,6 +67,14 @@ typedef struct mlh_config {
     double psi1;                /* PSI_1 */
     double psi2;                /* PSI_2 */
     double riemann_tol;         /* relative Newton tolerance on p* */
+    /* Per-particle smoothing lengths (no counterpart in the reference, which
+     * uses one global kernelSize).  With adaptive_h set, every step first
+     * solves h_i <= kernel_size (see mlh_smoothing_lengths) and the step uses
+     * them: neighbours are the pairs with r_ij < max(h_i, h_j), particle i's
+     * kernel sums (omega, E_i, psi) use W(r, h_i), its dt uses CFL * h_i.
+     * kernel_size stays the search radius (cell size, image band). */
+    double n_ngb;               /* target effective neighbour number */
+    int adaptive_h;
 } mlh_config;
 
 /* Caller-owned host arrays (structure of arrays, float64), the fields of the
@@ -144,6 +153,21 @@ int mlh_autotune(mlh_ctx *ctx, int trial_steps, mlh_tuning *out);
  * per SM 1..32; warps per SM 8..256.  MLH_ERR_INVALID otherwise. */
 int mlh_set_tuning(mlh_ctx *ctx, const mlh_tuning *tuning);
 
+/* Per-particle smoothing lengths of the current state (no counterpart in the
+ * reference, which uses one global kernelSize): for every particle i the
+ * support radius h_i in (0, H], H the simulation's kernel_size, at which the
+ * effective neighbour number
+ *     N_i(h) = V_D h^D (W(0, h) + sum_j W(|x_j - x_i|, h))
+ * (V_D = pi in 2D, 4 pi / 3 in 3D; W the cubic spline of support h; images
+ * by the periodic ghost rule) equals n_ngb, by a bracketed Newton iteration
+ * over the particles within H, started from the context's current h_i.
+ * A particle with N_i(H) < n_ngb keeps H and is counted in *clamped.  The
+ * result is stored in the context (the start of the next solve, and the
+ * smoothing lengths of adaptive_h steps) and copied to the host arrays h_out
+ * and n_eff_out (N doubles each, either may be NULL).  n_ngb must exceed a
+ * particle's own count, 32/3 in 3D and 40/7 in 2D (MLH_ERR_INVALID). */
+int mlh_smoothing_lengths(mlh_ctx *ctx, double n_ngb, double *h_out, double *n_eff_out, long long *clamped);
+
 /* Graph mode: mlh_step captures one step into a CUDA graph (once, and again
  * after a capacity change) and replays it; kernel timing bypasses it. */
 int mlh_set_graph_mode(mlh_ctx *ctx, int enable);
@@ -159,7 +183,9 @@ int mlh_get_fields(mlh_ctx *ctx, mlh_particles_view *dst);
 int mlh_step(mlh_ctx *ctx, int nsteps, double dt_max, mlh_step_stats *stats);
 
 /* Copy a named per-step array of the last step to host memory, for parity
- * checks (the arrays the reference keeps as Particles members):
+ * checks (the arrays the reference keeps as Particles members, and the
+ * smoothing lengths "h", "n_eff" (N) and "h_stats" (2: solve iterations,
+ * clamped particles) of the last solve):
  *   int32 : "off" (N+1), "noi", "noi_img" (N), "nnl" (uint32 index|image bits,
  *           real neighbours first in the reference's order, then images by
  *           parent index), "face_of" (per slot)

@@ -43,6 +43,10 @@ class MFVConfig:
     psi1: float = 0.5
     psi2: float = 0.25
     riemann_tol: float = 1e-10
+    # per-particle smoothing lengths (no reference counterpart): each step
+    # solves h_i <= kernel_size so that the effective neighbour number is n_ngb
+    n_ngb: float = 0.0
+    adaptive_h: bool = False
 
     @classmethod
     def kelvin_helmholtz(cls, pset, **kw) -> "MFVConfig":
@@ -71,7 +75,8 @@ class CConfig(ctypes.Structure):
     """ctypes image of `mlh_config` (include/mlh.h)."""
     _fields_ = ([(f, ctypes.c_int) for f in _INT_FIELDS]
                 + [("box_lo", ctypes.c_double * 3), ("box_hi", ctypes.c_double * 3)]
-                + [(f, ctypes.c_double) for f in _DBL_FIELDS])
+                + [(f, ctypes.c_double) for f in _DBL_FIELDS]
+                + [("n_ngb", ctypes.c_double), ("adaptive_h", ctypes.c_int)])
 
 
 def to_struct(cfg: MFVConfig, struct_type=CConfig):
@@ -83,6 +88,8 @@ def to_struct(cfg: MFVConfig, struct_type=CConfig):
         s.box_hi[a] = float(cfg.box_hi[a])
     for f in _DBL_FIELDS:
         setattr(s, f, float(getattr(cfg, f)))
+    s.n_ngb = float(getattr(cfg, "n_ngb", 0.0))
+    s.adaptive_h = int(getattr(cfg, "adaptive_h", False))
     return s
 
 

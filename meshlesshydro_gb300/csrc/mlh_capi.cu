@@ -75,6 +75,10 @@ struct mlh_ctx {
     Geo *geo = nullptr;
     Grad *grad = nullptr, *gradRaw = nullptr;
     double *fluxSums = nullptr;
+    // per-particle smoothing lengths and the effective neighbour number of
+    // the last solve; counters [iterations, clamped]
+    double *hp = nullptr, *neff = nullptr;
+    unsigned long long *hstat = nullptr;
     // scalars
     unsigned *status = nullptr;
     unsigned long long *dtbits = nullptr, *newtonSum = nullptr;
@@ -245,9 +249,19 @@ StepArgs make_args(mlh_ctx *c, double dt_max) {
     a.fstate = c->fstate; a.feat = c->feat; a.yguess = c->yguess;
     a.queueFace = c->queueFace; a.queueCount = c->queueCount; a.mlp_packed = c->mlp_packed;
     a.harvest = c->harvest;
+    a.hp = c->hp; a.neff = c->neff; a.hstat = c->hstat;
+    a.p.hp = c->hp;
     a.timer = c->timing ? timer_cb : nullptr;
     a.timer_ctx = c;
     return a;
+}
+
+// Target of S = sum_j f(2 r_ij / h_i) for an effective neighbour number
+// n_ngb: n_ngb / K_D - 1 (K_D = 32/3 in 3D, 40/7 in 2D, the count of the
+// particle itself).
+double sngb_target(int dim, double n_ngb) {
+    const double KD = dim == 3 ? 32. / 3. : 40. / 7.;
+    return n_ngb / KD - 1.;
 }
 
 void fill_params(mlh_ctx *c) {
@@ -283,6 +297,9 @@ void fill_params(mlh_ctx *c) {
     // single-precision pre-filter bound: positions rounded to float move a
     // distance of ~1e-7 relative to the box; 1e-3 relative on h^2 is ample
     p.hsq_f = (float)(p.hsq * (1. + 1e-3));
+    p.adaptive_h = f.adaptive_h;
+    p.cfl = f.cfl;
+    p.sngb_t = sngb_target(f.dim, f.n_ngb);
 }
 
 int upload(mlh_ctx *c, const mlh_particles_view *v) {
@@ -322,6 +339,10 @@ static int create_impl(const mlh_config *cfg, int nmembers, const mlh_member *md
         return MLH_ERR_INVALID;
     }
     if (init->n > (int)IDX_MASK) { g_last_error = "too many particles"; return MLH_ERR_CAPACITY; }
+    if (cfg->adaptive_h && !(sngb_target(cfg->dim, cfg->n_ngb) > 0.)) {
+        g_last_error = "adaptive_h needs n_ngb above the particle's own count (32/3 in 3D, 40/7 in 2D)";
+        return MLH_ERR_INVALID;
+    }
     std::vector<Member> mem;
     {
         int first = 0;
@@ -366,6 +387,7 @@ static int create_impl(const mlh_config *cfg, int nmembers, const mlh_member *md
     A(noi, n); A(noiImg, n); A(faceCnt, n); A(faceOff, n + 1);
     A(prim, n); A(geo, n); A(grad, n); A(gradRaw, n); A(fluxSums, n * 5);
     A(status, 1); A(dtbits, nm); A(newtonSum, 3); A(dt, nm); A(simTime, nm); A(stepsDone, 1);
+    A(hp, n); A(neff, n); A(hstat, 2);
     A(scanTiles, n / 4096 + 1024); A(scanTotal, 1);
 #undef A
     if ((rc = alloc_cell_buffers(c))) return fail(rc);
@@ -384,6 +406,16 @@ static int create_impl(const mlh_config *cfg, int nmembers, const mlh_member *md
     cudaMemsetAsync(c->dt, 0, sizeof(double) * nm, c->stream);
     cudaMemsetAsync(c->newtonSum, 0, 3 * sizeof(unsigned long long), c->stream);
     cudaMemsetAsync(c->stepsDone, 0, sizeof(int), c->stream);
+    cudaMemsetAsync(c->neff, 0, sizeof(double) * n, c->stream);
+    cudaMemsetAsync(c->hstat, 0, 2 * sizeof(unsigned long long), c->stream);
+    {
+        // every particle starts at its simulation's kernelSize
+        std::vector<double> h0(n);
+        for (const Member &mb : mem)
+            for (int i = mb.first; i < mb.first + mb.count; ++i) h0[i] = mb.h;
+        if (cudaMemcpy(c->hp, h0.data(), sizeof(double) * n, cudaMemcpyHostToDevice) != cudaSuccess)
+            return fail(cuda_fail(cudaGetLastError(), "hp"));
+    }
     if ((rc = upload(c, init))) return fail(rc);
     if (cudaStreamSynchronize(c->stream) != cudaSuccess) return fail(cuda_fail(cudaGetLastError(), "create sync"));
     *out = c;
@@ -412,7 +444,7 @@ void mlh_destroy(mlh_ctx *c) {
     void *ptrs[] = {c->x, c->y, c->z, c->vx, c->vy, c->vz, c->m, c->u, c->posf, c->members, c->memberOf, c->grids,
                     c->cellTotal, c->boundsPart, c->cell, c->cellList, c->noi, c->noiImg, c->faceCnt, c->faceOff,
                     c->prim, c->geo, c->grad, c->gradRaw, c->fluxSums, c->status, c->dtbits, c->newtonSum, c->dt,
-                    c->simTime, c->stepsDone, c->scanTiles, c->scanTotal};
+                    c->simTime, c->stepsDone, c->scanTiles, c->scanTotal, c->hp, c->neff, c->hstat};
     for (void *q : ptrs) if (q) cudaFree(q);
     free_cell_buffers(c);
     free_neighbour_buffers(c);
@@ -572,18 +604,19 @@ int mlh_autotune(mlh_ctx *c, int trial_steps, mlh_tuning *out) {
     if (!c || trial_steps < 1) { g_last_error = "invalid argument"; return MLH_ERR_INVALID; }
     const size_t n = (size_t)c->n, nm = (size_t)c->nmembers;
     double *save = nullptr;
-    CK(cudaMalloc(&save, sizeof(double) * (8 * n + 2 * nm)));
-    double *src[8] = {c->x, c->y, c->z, c->vx, c->vy, c->vz, c->m, c->u};
-    for (int k = 0; k < 8; ++k) CK(cudaMemcpyAsync(save + k * n, src[k], sizeof(double) * n, cudaMemcpyDeviceToDevice, c->stream));
-    CK(cudaMemcpyAsync(save + 8 * n, c->simTime, sizeof(double) * nm, cudaMemcpyDeviceToDevice, c->stream));
-    CK(cudaMemcpyAsync(save + 8 * n + nm, c->dt, sizeof(double) * nm, cudaMemcpyDeviceToDevice, c->stream));
+    // the state, and the smoothing lengths (the start of the next solve)
+    CK(cudaMalloc(&save, sizeof(double) * (9 * n + 2 * nm)));
+    double *src[9] = {c->x, c->y, c->z, c->vx, c->vy, c->vz, c->m, c->u, c->hp};
+    for (int k = 0; k < 9; ++k) CK(cudaMemcpyAsync(save + k * n, src[k], sizeof(double) * n, cudaMemcpyDeviceToDevice, c->stream));
+    CK(cudaMemcpyAsync(save + 9 * n, c->simTime, sizeof(double) * nm, cudaMemcpyDeviceToDevice, c->stream));
+    CK(cudaMemcpyAsync(save + 9 * n + nm, c->dt, sizeof(double) * nm, cudaMemcpyDeviceToDevice, c->stream));
     const bool timing0 = c->timing, graph0 = c->graph_mode;
     c->graph_mode = false;
     drop_graph(c);
     auto restore = [&]() -> int {
-        for (int k = 0; k < 8; ++k) CK(cudaMemcpyAsync(src[k], save + k * n, sizeof(double) * n, cudaMemcpyDeviceToDevice, c->stream));
-        CK(cudaMemcpyAsync(c->simTime, save + 8 * n, sizeof(double) * nm, cudaMemcpyDeviceToDevice, c->stream));
-        CK(cudaMemcpyAsync(c->dt, save + 8 * n + nm, sizeof(double) * nm, cudaMemcpyDeviceToDevice, c->stream));
+        for (int k = 0; k < 9; ++k) CK(cudaMemcpyAsync(src[k], save + k * n, sizeof(double) * n, cudaMemcpyDeviceToDevice, c->stream));
+        CK(cudaMemcpyAsync(c->simTime, save + 9 * n, sizeof(double) * nm, cudaMemcpyDeviceToDevice, c->stream));
+        CK(cudaMemcpyAsync(c->dt, save + 9 * n + nm, sizeof(double) * nm, cudaMemcpyDeviceToDevice, c->stream));
         pack_posf(c->x, c->y, c->z, c->n, c->cfg.dim, c->posf, c->stream);
         return 0;
     };
@@ -713,6 +746,50 @@ int mlh_pstar_harvest(mlh_ctx *c, int stride, float *x, float *t, long long capa
     return rc;
 }
 
+int mlh_smoothing_lengths(mlh_ctx *c, double n_ngb, double *h_out, double *n_eff_out, long long *clamped) {
+    if (!c) { g_last_error = "null context"; return MLH_ERR_INVALID; }
+    if (!(sngb_target(c->cfg.dim, n_ngb) > 0.)) {
+        g_last_error = "n_ngb must exceed the particle's own count (32/3 in 3D, 40/7 in 2D)";
+        return MLH_ERR_INVALID;
+    }
+    for (int retries = 0;; ++retries) {
+        StepArgs a = make_args(c, 0.);
+        a.p.sngb_t = sngb_target(c->cfg.dim, n_ngb);
+        CK(cudaMemsetAsync(c->status, 0, sizeof(unsigned), c->stream));
+        smoothing_lengths(a);
+        CK(cudaGetLastError());
+        unsigned st = 0;
+        CK(cudaMemcpyAsync(&st, c->status, sizeof(unsigned), cudaMemcpyDeviceToHost, c->stream));
+        CK(cudaStreamSynchronize(c->stream));
+        if (st & (MLH_ERR_NGB_OVERFLOW | ST_CAPACITY)) {
+            if (retries >= 8) { g_last_error = "capacity retries exhausted"; return (int)st; }
+            if (st & MLH_ERR_NGB_OVERFLOW) {
+                free_neighbour_buffers(c);
+                c->p.K = c->p.K + c->p.K / 2;
+                if (int rc = alloc_neighbour_buffers(c)) return rc;
+            }
+            if (st & ST_CAPACITY) {
+                free_cell_buffers(c);
+                c->p.ncells_cap = c->p.ncells_cap * 2;
+                if (int rc = alloc_cell_buffers(c)) return rc;
+            }
+            drop_graph(c);
+            continue;
+        }
+        if (st) return (int)st;
+        break;
+    }
+    const size_t b = sizeof(double) * (size_t)c->n;
+    if (h_out) CK(cudaMemcpy(h_out, c->hp, b, cudaMemcpyDeviceToHost));
+    if (n_eff_out) CK(cudaMemcpy(n_eff_out, c->neff, b, cudaMemcpyDeviceToHost));
+    if (clamped) {
+        unsigned long long hs[2];
+        CK(cudaMemcpy(hs, c->hstat, sizeof(hs), cudaMemcpyDeviceToHost));
+        *clamped = (long long)hs[1];
+    }
+    return 0;
+}
+
 int mlh_set_graph_mode(mlh_ctx *c, int enable) {
     if (!c) return MLH_ERR_INVALID;
     c->graph_mode = enable != 0;
@@ -819,6 +896,17 @@ int mlh_stage_array(mlh_ctx *c, const char *name, void *out, long long capacity,
             else for (int a = 0; a < 3; ++a) o.push_back(fs[(size_t)i * 5 + 2 + a]);
         }
         return put(o.data(), o.size(), 8);
+    }
+    if (nm == "h" || nm == "n_eff") {
+        std::vector<double> o(n);
+        CK(cudaMemcpy(o.data(), nm == "h" ? c->hp : c->neff, sizeof(double) * n, cudaMemcpyDeviceToHost));
+        return put(o.data(), o.size(), 8);
+    }
+    if (nm == "h_stats") {
+        unsigned long long hs[2];
+        CK(cudaMemcpy(hs, c->hstat, sizeof(hs), cudaMemcpyDeviceToHost));
+        double o[2] = {(double)hs[0], (double)hs[1]};
+        return put(o, 2, 8);
     }
     if (nm == "dt") {
         double d;

@@ -60,6 +60,13 @@ struct Params {
     double h, hsq, h2, sigma, w0, gamma, cfl_h, beta, psi1, psi2, rtol, time_step;
     double box_lo[3], box_hi[3];
     float hsq_f;           // conservative single-precision bound for the pre-filter
+    // per-particle smoothing lengths (adaptive_h): the step's support radius
+    // of particle i is hp[i] <= the member's kernelSize, which stays the
+    // search radius (grid cells, periodic-image band)
+    int adaptive_h;
+    double cfl;            // CFL (cfl_h = CFL * kernelSize without adaptive_h)
+    double sngb_t;         // target of S = sum_j f(2 r_ij / h_i): n_ngb / K_D - 1
+    const double *hp;
 };
 
 // Per-particle records (array of structures: one particle's values sit in
@@ -90,14 +97,41 @@ struct Harvest {
     int stride, cap;
 };
 
-// Kernel::cubicSpline, demonstrator/src/Particles.cpp:7-24.  sigma is
-// precomputed on the host with the reference's expression; pow(2-q, 3.) is
-// written as a product.
-__device__ __forceinline__ double kernelW(double r, const Member &mb) {
-    double q = r / mb.h2;
-    if (0. <= q && q <= 1.) return mb.sigma * (1. - 3. / 2. * q * q * (1. - q / 2.));
-    if (1. < q && q < 2.) { double t = 2. - q; return mb.sigma / 4. * (t * t * t); }
+// Kernel::cubicSpline, demonstrator/src/Particles.cpp:7-24, for a support
+// radius h: h2 = h / 2 and sigma computed with the reference's expression
+// (kernel_sigma); pow(2-q, 3.) is written as a product.
+__device__ __forceinline__ double kernelW2(double r, double h2, double sigma) {
+    double q = r / h2;
+    if (0. <= q && q <= 1.) return sigma * (1. - 3. / 2. * q * q * (1. - q / 2.));
+    if (1. < q && q < 2.) { double t = 2. - q; return sigma / 4. * (t * t * t); }
     return 0.;
+}
+__device__ __forceinline__ double kernelW(double r, const Member &mb) { return kernelW2(r, mb.h2, mb.sigma); }
+// Particles.cpp:10-15 (the value of the kernel at r = 0 is sigma)
+template <int D>
+__device__ __forceinline__ double kernel_sigma(double h2) {
+    constexpr double PI = 3.14159265358979323846;
+    return D == 2 ? 10. / (7. * PI * h2 * h2) : 1. / (PI * h2 * h2 * h2);
+}
+
+// Shape of the cubic spline and its scaled derivative for the smoothing-length
+// solve: q = r / (h/2) (given as r times 1 / (h/2)), f(q) with f(0) = 1 and
+// g(q) = -f'(q) q.  Every operation is an explicitly rounded intrinsic so that
+// the CPU restatement, which performs the same operations, gets the same bits.
+__device__ __forceinline__ void hsolve_shape(double r, double ihh2, double &f, double &g) {
+    const double q = __dmul_rn(r, ihh2);
+    if (q <= 1.) {
+        const double q2 = __dmul_rn(q, q);
+        f = __fma_rn(q2, __fma_rn(0.75, q, -1.5), 1.);
+        g = __dmul_rn(q2, __fma_rn(-2.25, q, 3.));
+    } else if (q < 2.) {
+        const double t = __dsub_rn(2., q), t2 = __dmul_rn(t, t);
+        f = __dmul_rn(__dmul_rn(0.25, t2), t);
+        g = __dmul_rn(__dmul_rn(0.75, t2), q);
+    } else {
+        f = 0.;
+        g = 0.;
+    }
 }
 
 // Ghost image coordinate, Particles.cpp:2123-2142.

@@ -338,6 +338,108 @@ __host__ __device__ constexpr size_t nns_warp_bytes(int K) {
     return ((size_t)(K + 32) * 4 + 15) / 16 * 16 + (size_t)K * 16 + ((size_t)K * 4 + 15) / 16 * 16;
 }
 
+// Candidates of particle i, shared by the neighbour search and the
+// smoothing-length solve: the 3^D stencil cells in the reference's order
+// (Domain::getNeighborCells, demonstrator/src/Domain.cpp:83-118; lane k
+// holds cell k) written to the warp's NnsCells, then every particle of those
+// cells that passes a single-precision distance pre-filter against the
+// search radius (a conservative bound), in stencil order and ascending index
+// within a cell, appended to cand[] (the entry carries the wrapped axes as
+// image bits).  Returns the number of candidates (at most CAP); `overflow`
+// is set when more passed.
+template <int D>
+__device__ __forceinline__ int nns_candidates(const Params &p, const GridInfo &g, const Member &mb, int i,
+                                              const int *__restrict__ cell, const int *__restrict__ cellStart,
+                                              const int *__restrict__ cellList, const float4 *__restrict__ posf,
+                                              NnsCells *cs, uint32_t *cand, int CAP, bool &overflow) {
+    constexpr int NC = D == 3 ? 27 : 9;
+    const int lane = threadIdx.x & 31;
+    const unsigned lt_mask = (1u << lane) - 1u;
+    float Lf[3];
+#pragma unroll
+    for (int a = 0; a < 3; ++a) Lf[a] = (float)(g.hi[a] - g.lo[a]);
+    const int ic = cell[i] - g.cell_base;
+    const int ix = ic % g.cells[0];
+    const int iy = (ic / g.cells[0]) % g.cells[1];
+    const int iz = D == 3 ? ic / (g.cells[0] * g.cells[1]) : 0;
+    // --- stencil cells in the reference's order, lane k holds cell k
+    int cnt = 0, start = 0;
+    unsigned wrap = 0;
+    int sh[3] = {0, 0, 0};
+    if (lane < NC) {
+        int off[3] = {D == 3 ? lane / 9 - 1 : lane / 3 - 1, D == 3 ? (lane / 3) % 3 - 1 : lane % 3 - 1,
+                      D == 3 ? lane % 3 - 1 : 0};
+        int cc[3] = {ix + off[0], iy + off[1], iz + off[2]};
+        bool skip = false;
+#pragma unroll
+        for (int a = 0; a < D; ++a) {
+            if (cc[a] < 0 || cc[a] >= g.cells[a]) {
+                if (!p.periodic) skip = true;
+                cc[a] = cc[a] < 0 ? cc[a] + g.cells[a] : cc[a] - g.cells[a];
+                wrap |= 1u << a;
+                sh[a] = off[a];
+            }
+        }
+        if (!skip) {
+            int c = g.cell_base + cc[0] + cc[1] * g.cells[0] + (D == 3 ? cc[2] * g.cells[0] * g.cells[1] : 0);
+            start = cellStart[c];
+            cnt = cellStart[c + 1] - start;
+        }
+    }
+    int incl = cnt;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        int t = __shfl_up_sync(0xffffffffu, incl, o);
+        if (lane >= o) incl += t;
+    }
+    const int total = __shfl_sync(0xffffffffu, incl, 31);
+    if (lane < NC) {
+        cs->excl[lane] = incl - cnt;
+        cs->start[lane] = start;
+        cs->wrap[lane] = wrap;
+        cs->shift[lane][0] = sh[0]; cs->shift[lane][1] = sh[1]; cs->shift[lane][2] = sh[2];
+    }
+    __syncwarp();
+    const float4 fi = posf[i];
+    // --- phase 1: single-precision pre-filter, ordered compaction
+    int ncand = 0;
+    for (int t0 = 0; t0 < total; t0 += 32) {
+        const int t = t0 + lane;
+        bool pass = false;
+        uint32_t ent = 0;
+        if (t < total) {
+            int k = 0;
+            for (int kk = 1; kk < NC; ++kk)
+                if (cs->excl[kk] <= t) k = kk;
+            // empty cells share their offset with the next one: take the
+            // last cell whose range contains t
+            const int j = cellList[cs->start[k] + (t - cs->excl[k])];
+            const unsigned wr = cs->wrap[k];
+            if (wr || j != i) {
+                float4 fj = posf[j];
+                float dx = fj.x - fi.x, dy = fj.y - fi.y, dz = fj.z - fi.z;
+                if (wr) {
+                    dx += (float)cs->shift[k][0] * Lf[0];
+                    dy += (float)cs->shift[k][1] * Lf[1];
+                    if (D == 3) dz += (float)cs->shift[k][2] * Lf[2];
+                }
+                float d2f = dx * dx + dy * dy + (D == 3 ? dz * dz : 0.f);
+                pass = d2f <= mb.hsq_f;
+                ent = (uint32_t)j | (wr << IMG_SHIFT);
+            }
+        }
+        const unsigned bal = __ballot_sync(0xffffffffu, pass);
+        if (pass) {
+            const int pos = ncand + __popc(bal & lt_mask);
+            if (pos < CAP) cand[pos] = ent;
+        }
+        ncand += __popc(bal);
+    }
+    if (ncand > CAP) { overflow = true; ncand = CAP; }
+    __syncwarp();
+    return ncand;
+}
+
 template <int D>
 __global__ void __launch_bounds__(NNS_WARPS * 32) k_neighbours(
     Params p, const Member *__restrict__ members, const int *__restrict__ memberOf,
@@ -371,93 +473,21 @@ __global__ void __launch_bounds__(NNS_WARPS * 32) k_neighbours(
         const int mi = memberOf ? memberOf[i] : 0;
         const GridInfo g = grids[mi];
         const Member mb = members[mi];
-        float Lf[3];
-#pragma unroll
-        for (int a = 0; a < 3; ++a) Lf[a] = (float)(g.hi[a] - g.lo[a]);
-        const int ic = cell[i] - g.cell_base;
-        const int ix = ic % g.cells[0];
-        const int iy = (ic / g.cells[0]) % g.cells[1];
-        const int iz = D == 3 ? ic / (g.cells[0] * g.cells[1]) : 0;
-        // --- stencil cells in the reference's order, lane k holds cell k
-        int cnt = 0, start = 0;
-        unsigned wrap = 0;
-        int sh[3] = {0, 0, 0};
-        if (lane < NC) {
-            int off[3] = {D == 3 ? lane / 9 - 1 : lane / 3 - 1, D == 3 ? (lane / 3) % 3 - 1 : lane % 3 - 1,
-                          D == 3 ? lane % 3 - 1 : 0};
-            int cc[3] = {ix + off[0], iy + off[1], iz + off[2]};
-            bool skip = false;
-#pragma unroll
-            for (int a = 0; a < D; ++a) {
-                if (cc[a] < 0 || cc[a] >= g.cells[a]) {
-                    if (!p.periodic) skip = true;
-                    cc[a] = cc[a] < 0 ? cc[a] + g.cells[a] : cc[a] - g.cells[a];
-                    wrap |= 1u << a;
-                    sh[a] = off[a];
-                }
-            }
-            if (!skip) {
-                int c = g.cell_base + cc[0] + cc[1] * g.cells[0] + (D == 3 ? cc[2] * g.cells[0] * g.cells[1] : 0);
-                start = cellStart[c];
-                cnt = cellStart[c + 1] - start;
-            }
-        }
-        int incl = cnt;
-#pragma unroll
-        for (int o = 1; o < 32; o <<= 1) {
-            int t = __shfl_up_sync(0xffffffffu, incl, o);
-            if (lane >= o) incl += t;
-        }
-        const int total = __shfl_sync(0xffffffffu, incl, 31);
-        if (lane < NC) {
-            cs->excl[lane] = incl - cnt;
-            cs->start[lane] = start;
-            cs->wrap[lane] = wrap;
-            cs->shift[lane][0] = sh[0]; cs->shift[lane][1] = sh[1]; cs->shift[lane][2] = sh[2];
-        }
-        __syncwarp();
-        const float4 fi = posf[i];
-        // --- phase 1: single-precision pre-filter, ordered compaction
-        int ncand = 0;
         bool overflow = false;
-        for (int t0 = 0; t0 < total; t0 += 32) {
-            const int t = t0 + lane;
-            bool pass = false;
-            uint32_t ent = 0;
-            if (t < total) {
-                int k = 0;
-                for (int kk = 1; kk < NC; ++kk)
-                    if (cs->excl[kk] <= t) k = kk;
-                // empty cells share their offset with the next one: take the
-                // last cell whose range contains t
-                const int j = cellList[cs->start[k] + (t - cs->excl[k])];
-                const unsigned wr = cs->wrap[k];
-                if (wr || j != i) {
-                    float4 fj = posf[j];
-                    float dx = fj.x - fi.x, dy = fj.y - fi.y, dz = fj.z - fi.z;
-                    if (wr) {
-                        dx += (float)cs->shift[k][0] * Lf[0];
-                        dy += (float)cs->shift[k][1] * Lf[1];
-                        if (D == 3) dz += (float)cs->shift[k][2] * Lf[2];
-                    }
-                    float d2f = dx * dx + dy * dy + (D == 3 ? dz * dz : 0.f);
-                    pass = d2f <= mb.hsq_f;
-                    ent = (uint32_t)j | (wr << IMG_SHIFT);
-                }
-            }
-            const unsigned bal = __ballot_sync(0xffffffffu, pass);
-            if (pass) {
-                const int pos = ncand + __popc(bal & lt_mask);
-                if (pos < CAP) cand[pos] = ent;
-            }
-            ncand += __popc(bal);
-        }
-        if (ncand > CAP) { overflow = true; ncand = CAP; }
-        __syncwarp();
-        // --- phase 2: exact FP64 test, r, W
+        int ncand = nns_candidates<D>(p, g, mb, i, cell, cellStart, cellList, posf, cs, cand, CAP, overflow);
+        // --- phase 2: exact FP64 test, r, W.  With per-particle smoothing
+        // lengths the pair test is r^2 < max(h_i^2, h_j^2) and W uses h_i.
         int nr = 0, ni = 0, fc = 0;
         double wsumR = 0., wsumI = 0.;
         const size_t base = (size_t)i * K;
+        double hsq_i = mb.hsq, h2_i = mb.h2, sigma_i = mb.sigma, w0_i = mb.w0;
+        if (p.adaptive_h) {
+            const double hi_ = p.hp[i];
+            hsq_i = __dmul_rn(hi_, hi_);
+            h2_i = hi_ / 2.;
+            sigma_i = kernel_sigma<D>(h2_i);
+            w0_i = sigma_i;
+        }
         double xi[3] = {0., 0., 0.};
 #pragma unroll
         for (int a = 0; a < D; ++a) xi[a] = X[a][i];
@@ -485,10 +515,15 @@ __global__ void __launch_bounds__(NNS_WARPS * 32) k_neighbours(
                     double ex = __dsub_rn(xj[0], xi[0]), ey = __dsub_rn(xj[1], xi[1]);
                     double d2 = __dadd_rn(__dmul_rn(ex, ex), __dmul_rn(ey, ey));
                     if (D == 3) { double ez = __dsub_rn(xj[2], xi[2]); d2 = __dadd_rn(d2, __dmul_rn(ez, ez)); }
-                    pass = d2 < mb.hsq;
+                    if (p.adaptive_h) {
+                        const double hj = p.hp[j];
+                        pass = d2 < fmax(hsq_i, __dmul_rn(hj, hj));
+                    } else {
+                        pass = d2 < mb.hsq;
+                    }
                     if (pass) {
                         r = sqrt(d2);
-                        w = kernelW(r, mb);
+                        w = kernelW2(r, h2_i, sigma_i);
                     }
                 }
             }
@@ -537,7 +572,7 @@ __global__ void __launch_bounds__(NNS_WARPS * 32) k_neighbours(
         if (lane == 0) {
             if (overflow) flag(status, ST_NGB_OVERFLOW);
             if (nr + ni == 0) flag(status, ST_NO_NEIGHBOUR);
-            const double omega = (wsumR + mb.w0) + wsumI;
+            const double omega = (wsumR + w0_i) + wsumI;
             const double rho = m[i] * omega;
             const double P = (p.gamma - 1.) * rho * u[i];
             if (rho <= 0.) flag(status, ST_NEG_DENSITY);
@@ -556,6 +591,151 @@ __global__ void __launch_bounds__(NNS_WARPS * 32) k_neighbours(
         }
         __syncwarp();
     }
+}
+
+// ------------------------------------------------------------------ smoothing lengths
+
+// Per-particle smoothing lengths (no counterpart in the reference, which uses
+// one global kernelSize).  For particle i the support radius x in (0, H],
+// H the member's kernelSize (the search radius), at which the effective
+// neighbour number N(x) = V_D x^D (W(0, x) + sum_j W(r_ij, x)) equals n_ngb.
+// With the cubic spline of support x, N(x) = K_D (1 + S(x)) where
+// S(x) = sum_j f(2 r_ij / x) (f the spline's shape, f(0) = 1; K_D = 32/3 in
+// 3D, 40/7 in 2D); S increases with x and dS/dx = G(x) / x with
+// G = sum_j -f'(q) q.  One warp per particle: the candidates within H (the
+// neighbour search's stencil, pre-filter and exact test, images by the ghost
+// rule) are kept in shared memory in stencil order; every Newton iteration
+// sums f and g over them in 32 lane-strided partial sums combined by an xor
+// butterfly, so every lane holds the same bits and the iteration (bracketed,
+// bisection when Newton leaves the bracket) runs in lockstep.  The start is
+// the previous h_i (H at first); a particle with N(H) < n_ngb keeps H and is
+// counted in hstat[1]; hstat[0] counts iterations.  The CPU restatement
+// performs the same operations in the same order and gets the same bits.
+constexpr int HSOLVE_MAXIT = 50;
+
+__host__ __device__ constexpr size_t hsolve_warp_bytes(int K) {
+    return ((size_t)(K + 32) * 4 + 15) / 16 * 16 + (size_t)(K + 32) * 8;
+}
+
+template <int D>
+__global__ void __launch_bounds__(NNS_WARPS * 32) k_hsolve(
+    Params p, const Member *__restrict__ members, const int *__restrict__ memberOf,
+    const GridInfo *__restrict__ grids, const double *__restrict__ x, const double *__restrict__ y,
+    const double *__restrict__ z, const float4 *__restrict__ posf, const int *__restrict__ cell,
+    const int *__restrict__ cellStart, const int *__restrict__ cellList, double *__restrict__ hp,
+    double *__restrict__ neff, unsigned long long *__restrict__ hstat, unsigned *__restrict__ status) {
+    const int K = p.K;
+    const int CAP = K + 32;
+    extern __shared__ __align__(16) unsigned char hs_smem[];
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const unsigned lt_mask = (1u << lane) - 1u;
+    NnsCells *cs = reinterpret_cast<NnsCells *>(hs_smem) + warp;
+    unsigned char *wbase = hs_smem + nns_cells_bytes() + (size_t)warp * hsolve_warp_bytes(K);
+    uint32_t *cand = reinterpret_cast<uint32_t *>(wbase);
+    double *rl = reinterpret_cast<double *>(wbase + ((size_t)CAP * 4 + 15) / 16 * 16);
+    constexpr double KD = D == 3 ? 32. / 3. : 40. / 7.;
+    const double St = p.sngb_t;
+    const double tolS = __dmul_rn(1e-12, St);
+    const double *X[3] = {x, y, z};
+    unsigned long long iters = 0, clamped = 0;
+    bool overflow_any = false;
+    const int gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int nw = (gridDim.x * blockDim.x) >> 5;
+    for (int i = gw; i < p.n; i += nw) {
+        const int mi = memberOf ? memberOf[i] : 0;
+        const GridInfo g = grids[mi];
+        const Member mb = members[mi];
+        bool overflow = false;
+        const int ncand = nns_candidates<D>(p, g, mb, i, cell, cellStart, cellList, posf, cs, cand, CAP, overflow);
+        if (overflow) {   // the host grows the slots and repeats
+            overflow_any = true;
+            continue;
+        }
+        // exact FP64 distances of the candidates within H, in order
+        double xi[3] = {0., 0., 0.};
+#pragma unroll
+        for (int a = 0; a < D; ++a) xi[a] = X[a][i];
+        int nr = 0;
+        for (int t0 = 0; t0 < ncand; t0 += 32) {
+            const int t = t0 + lane;
+            bool pass = false;
+            double r = 0.;
+            if (t < ncand) {
+                const uint32_t e = cand[t];
+                const int j = (int)(e & IDX_MASK);
+                const unsigned wr = e >> IMG_SHIFT;
+                double xj[3];
+                bool ok = true;
+#pragma unroll
+                for (int a = 0; a < D; ++a) {
+                    xj[a] = X[a][j];
+                    if (wr & (1u << a)) {
+                        if (in_band(xj[a], g.lo[a], g.hi[a], mb.h)) xj[a] = image_coord(xj[a], g.lo[a], g.hi[a], mb.h);
+                        else ok = false;
+                    }
+                }
+                if (ok) {
+                    double ex = __dsub_rn(xj[0], xi[0]), ey = __dsub_rn(xj[1], xi[1]);
+                    double d2 = __dadd_rn(__dmul_rn(ex, ex), __dmul_rn(ey, ey));
+                    if (D == 3) { double ez = __dsub_rn(xj[2], xi[2]); d2 = __dadd_rn(d2, __dmul_rn(ez, ez)); }
+                    pass = d2 < mb.hsq;
+                    if (pass) r = __dsqrt_rn(d2);
+                }
+            }
+            const unsigned bal = __ballot_sync(0xffffffffu, pass);
+            if (pass) rl[nr + __popc(bal & lt_mask)] = r;
+            nr += __popc(bal);
+        }
+        __syncwarp();
+        // bracketed Newton on S(x) = St, in lockstep on all lanes
+        const double H = mb.h;
+        double xh = hp[i];
+        if (!(xh > 0. && xh <= H)) xh = H;
+        double lo = 0., hi = H, S = 0.;
+        bool upper = false;
+        for (int it = 0;; ++it) {
+            const double ihh2 = __ddiv_rn(1., __dmul_rn(0.5, xh));
+            double sf = 0., sg = 0.;
+            for (int t = lane; t < nr; t += 32) {
+                double f, gg;
+                hsolve_shape(rl[t], ihh2, f, gg);
+                sf = __dadd_rn(sf, f);
+                sg = __dadd_rn(sg, gg);
+            }
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) {
+                sf = __dadd_rn(sf, __shfl_xor_sync(0xffffffffu, sf, o));
+                sg = __dadd_rn(sg, __shfl_xor_sync(0xffffffffu, sg, o));
+            }
+            S = sf;
+            const double G = sg;
+            ++iters;
+            const double F = __dsub_rn(S, St);
+            if (fabs(F) <= tolS) break;
+            if (F < 0. && xh >= H) { ++clamped; break; }
+            if (it + 1 >= HSOLVE_MAXIT) break;
+            if (F > 0.) { hi = xh; upper = true; }
+            else lo = xh;
+            double xn = G > 0. ? __dsub_rn(xh, __ddiv_rn(__dmul_rn(F, xh), G)) : __dmul_rn(0.5, __dadd_rn(lo, hi));
+            if (!(xn > lo && xn < hi)) xn = (!upper && xn >= hi) ? H : __dmul_rn(0.5, __dadd_rn(lo, hi));
+            if (xn == xh) break;
+            xh = xn;
+        }
+        if (lane == 0) {
+            hp[i] = xh;
+            if (neff) neff[i] = __dmul_rn(KD, __dadd_rn(S, 1.));
+        }
+        __syncwarp();
+    }
+    if (lane == 0) {
+        if (iters) atomicAdd(hstat, iters);
+        if (clamped) atomicAdd(hstat + 1, clamped);
+        if (overflow_any) flag(status, ST_NGB_OVERFLOW);
+    }
+}
+
+size_t hsolve_smem_bytes(int K) {
+    return nns_cells_bytes() + (size_t)NNS_WARPS * hsolve_warp_bytes(K);
 }
 
 size_t nns_smem_bytes(int K) {
@@ -600,7 +780,7 @@ __global__ void __launch_bounds__(256) k_timestep(Params p, const Member *__rest
                 double vs = ci + cj - vijxij;
                 vSig = vs > vSig ? vs : vSig;
             }
-            dti = members[mi].cfl_h / vSig;
+            dti = (p.adaptive_h ? p.cfl * p.hp[i] : members[mi].cfl_h) / vSig;
         }
         // the minimum over particles does not depend on the order of the
         // atomicMin calls: a warp inside one simulation (the common case)
@@ -693,6 +873,7 @@ __global__ void __launch_bounds__(256) k_gradients(Params p, const Member *__res
         const int mi = memberOf ? memberOf[i] : 0;
         const GridInfo g = grids[mi];
         const double h = members[mi].h;
+        const double hq = p.adaptive_h ? p.hp[i] : h;   // quadrature-point radius
         const Prim pi = prim[i];
         const double xi[3] = {pi.x, pi.y, pi.z};
         const double Vi = geo[i].V;
@@ -771,7 +952,7 @@ __global__ void __launch_bounds__(256) k_gradients(Params p, const Member *__res
                 neighbour_pos<D>(e, pj, g, h, xj);
 #pragma unroll
                 for (int a = 0; a < D; ++a) {
-                    double xij = p.foqp ? (xi[a] + xj[a]) / 2. : xi[a] + h / 4. * (xj[a] - xi[a]);
+                    double xij = p.foqp ? (xi[a] + xj[a]) / 2. : xi[a] + hq / 4. * (xj[a] - xi[a]);
                     xijxi[a] = xij - xi[a];
                 }
 #pragma unroll
@@ -996,6 +1177,7 @@ __global__ void __launch_bounds__(256) k_faces(Params p, const Member *__restric
         const int mi = memberOf ? memberOf[i] : 0;
         const double dt = dtp[mi];
         const double h = members[mi].h;
+        const double hq = p.adaptive_h ? p.hp[i] : h;   // quadrature-point radius
         const size_t si = (size_t)i * p.K + fr.slot;
         const uint32_t e = nbr[si];
         const int j = (int)(e & IDX_MASK);
@@ -1027,7 +1209,7 @@ __global__ void __launch_bounds__(256) k_faces(Params p, const Member *__restric
                 xijxj[a] = .5 * (xi[a] - xj[a]);
                 xijxi[a] = .5 * (xj[a] - xi[a]);
             } else {
-                double xij = xi[a] + h / 4. * xjxi[a];
+                double xij = xi[a] + hq / 4. * xjxi[a];
                 xijxi[a] = xij - xi[a];
                 xijxj[a] = xij - xj[a];
             }
@@ -1335,6 +1517,40 @@ __global__ void k_pack_posf(const double *__restrict__ x, const double *__restri
 
 // ------------------------------------------------------------------ launchers
 
+// Particles::getDomainLimits + Domain::createGrid + assignParticlesAndCells
+// (Particles.cpp:228-322, Domain.cpp:9-54): grids, cell of every particle,
+// cell lists sorted by particle index.
+template <int D>
+void launch_binning(StepArgs &a) {
+    const Params &p = a.p;
+    cudaStream_t s = a.stream;
+    const int T = 128;
+    const int blocksN = (p.n + T - 1) / T;
+    k_bounds_partial<D><<<a.nmembers * a.bpm, BOUNDS_T, 0, s>>>(a.x, a.y, a.z, p, a.members, a.bpm, a.boundsPart);
+    k_bounds_final<D><<<1, 256, 0, s>>>(a.x, a.y, a.z, a.boundsPart, a.bpm, p, a.members, a.nmembers, a.grids,
+                                        a.cellTotal, a.status);
+    cudaMemsetAsync(a.cellCount, 0, sizeof(int) * (size_t)(p.ncells_cap + 1), s);
+    cudaMemsetAsync(a.cellFill, 0, sizeof(int) * (size_t)(p.ncells_cap + 1), s);
+    k_assign<D><<<blocksN, T, 0, s>>>(a.x, a.y, a.z, p.n, a.memberOf, a.grids, a.cell, a.cellCount, a.status);
+    exclusive_scan(a.cellCount, p.ncells_cap, a.cellStart, a.scanTiles, a.scanTotal, s);
+    k_fill_cells<<<blocksN, T, 0, s>>>(a.cell, p.n, a.cellStart, a.cellFill, a.cellList);
+    k_sort_cells<<<(p.ncells_cap + T - 1) / T, T, 0, s>>>(a.cellTotal, a.cellStart, a.cellList);
+}
+
+// Smoothing lengths of every particle on the current grid (k_hsolve).
+template <int D>
+void launch_hsolve(StepArgs &a) {
+    const Params &p = a.p;
+    cudaStream_t s = a.stream;
+    cudaMemsetAsync(a.hstat, 0, 2 * sizeof(unsigned long long), s);
+    const int warps_total = a.sm_count * a.tune.nns_warps_per_sm;
+    const int blocks = (warps_total + NNS_WARPS - 1) / NNS_WARPS;
+    const size_t smem = hsolve_smem_bytes(p.K);
+    if (smem > 48 * 1024) cudaFuncSetAttribute(k_hsolve<D>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    k_hsolve<D><<<blocks, NNS_WARPS * 32, smem, s>>>(p, a.members, a.memberOf, a.grids, a.x, a.y, a.z, a.posf, a.cell,
+                                                     a.cellStart, a.cellList, a.hp, a.neff, a.hstat, a.status);
+}
+
 template <int D>
 void launch_step(StepArgs &a) {
     const Params &p = a.p;
@@ -1345,16 +1561,14 @@ void launch_step(StepArgs &a) {
     auto tock = [&](int id) { if (a.timer) a.timer(a.timer_ctx, id, 1); };
 
     tick(KT_GRID);
-    k_bounds_partial<D><<<a.nmembers * a.bpm, BOUNDS_T, 0, s>>>(a.x, a.y, a.z, p, a.members, a.bpm, a.boundsPart);
-    k_bounds_final<D><<<1, 256, 0, s>>>(a.x, a.y, a.z, a.boundsPart, a.bpm, p, a.members, a.nmembers, a.grids,
-                                        a.cellTotal, a.status);
-    cudaMemsetAsync(a.cellCount, 0, sizeof(int) * (size_t)(p.ncells_cap + 1), s);
-    cudaMemsetAsync(a.cellFill, 0, sizeof(int) * (size_t)(p.ncells_cap + 1), s);
-    k_assign<D><<<blocksN, T, 0, s>>>(a.x, a.y, a.z, p.n, a.memberOf, a.grids, a.cell, a.cellCount, a.status);
-    exclusive_scan(a.cellCount, p.ncells_cap, a.cellStart, a.scanTiles, a.scanTotal, s);
-    k_fill_cells<<<blocksN, T, 0, s>>>(a.cell, p.n, a.cellStart, a.cellFill, a.cellList);
-    k_sort_cells<<<(p.ncells_cap + T - 1) / T, T, 0, s>>>(a.cellTotal, a.cellStart, a.cellList);
+    launch_binning<D>(a);
     tock(KT_GRID);
+
+    if (p.adaptive_h) {
+        tick(KT_HSOLVE);
+        launch_hsolve<D>(a);
+        tock(KT_HSOLVE);
+    }
 
     tick(KT_NNS);
     {
@@ -1430,6 +1644,11 @@ void step(StepArgs &a) {
     else launch_step<3>(a);
 }
 
+void smoothing_lengths(StepArgs &a) {
+    if (a.p.dim == 2) { launch_binning<2>(a); launch_hsolve<2>(a); }
+    else { launch_binning<3>(a); launch_hsolve<3>(a); }
+}
+
 void pack_posf(const double *x, const double *y, const double *z, int n, int dim, float4 *posf, cudaStream_t s) {
     int blocks = (n + 255) / 256;
     if (blocks < 1) blocks = 1;
@@ -1446,6 +1665,7 @@ const char *kernel_timer_name(int id) {
         case KT_LINK: return "face_links";
         case KT_FACES: return "faces_riemann";
         case KT_UPDATE: return "gather_update";
+        case KT_HSOLVE: return "smoothing_lengths";
     }
     return "?";
 }

@@ -7,7 +7,7 @@
 
 namespace mlh {
 
-enum KernelTimerId { KT_GRID = 0, KT_NNS, KT_DT, KT_GRAD, KT_LINK, KT_FACES, KT_UPDATE, KT_COUNT };
+enum KernelTimerId { KT_GRID = 0, KT_NNS, KT_DT, KT_GRAD, KT_LINK, KT_FACES, KT_UPDATE, KT_HSOLVE, KT_COUNT };
 
 // Launch shapes chosen by the autotuner (mlh_autotune).
 struct Tuning {
@@ -66,6 +66,10 @@ struct StepArgs {
     int *queueCount;
     const void *mlp_packed;
     Harvest harvest;
+    // per-particle smoothing lengths: h (also p.hp), effective neighbour
+    // number (may be null), counters [iterations, clamped particles]
+    double *hp, *neff;
+    unsigned long long *hstat;
     // optional per-kernel timer callback (phase 0 = before, 1 = after)
     void (*timer)(void *, int, int);
     void *timer_ctx;
@@ -76,6 +80,8 @@ struct StepArgs {
 constexpr int BOUNDS_BLOCKS = 304;
 
 void step(StepArgs &a);
+// binning and the smoothing-length solve alone, on the current positions
+void smoothing_lengths(StepArgs &a);
 // Particles::getDomainLimits + Domain::createGrid alone: per-block partial
 // minima/maxima in `partials` (nmembers * bpm * 6 doubles), one GridInfo per
 // member in `grids`, the concatenated cell count in `cellTotal`.

@@ -64,7 +64,7 @@ EXPORTS = ["mlh_abi_version", "mlh_last_error", "mlh_create", "mlh_destroy", "ml
            "mlh_kernel_times", "mlh_reset_kernel_times", "mlh_probe_fp64_tflops",
            "mlh_grid_bounds_noalloc", "mlh_ensemble_create", "mlh_member_times", "mlh_set_graph_mode",
            "mlh_autotune", "mlh_set_tuning", "mlh_pstar_infer", "mlh_pstar_grad", "mlh_pstar_train", "mlh_set_pstar_weights",
-           "mlh_pstar_harvest"]
+           "mlh_pstar_harvest", "mlh_smoothing_lengths"]
 
 _lib = None
 
@@ -127,6 +127,9 @@ def load(path: str = LIB_PATH):
     L.mlh_set_pstar_weights.restype = ctypes.c_int
     L.mlh_pstar_harvest.argtypes = [vp, ctypes.c_int, fp, fp, ctypes.c_longlong, ctypes.POINTER(ctypes.c_longlong)]
     L.mlh_pstar_harvest.restype = ctypes.c_int
+    L.mlh_smoothing_lengths.argtypes = [vp, ctypes.c_double, ctypes.POINTER(ctypes.c_double),
+                                        ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_longlong)]
+    L.mlh_smoothing_lengths.restype = ctypes.c_int
     _lib = L
     return L
 
@@ -287,6 +290,18 @@ class Simulation:
         if st != 0:
             raise MLHError(st, "mlh_pstar_harvest", self.L.mlh_last_error().decode())
         return x[:cnt.value], t[:cnt.value]
+
+    def smoothing_lengths(self, n_ngb: float):
+        """Per-particle smoothing lengths of the current state (mlh_smoothing_lengths):
+        (h, effective neighbour number, number of particles clamped at kernel_size)."""
+        h = np.empty(self.host.n)
+        ne = np.empty(self.host.n)
+        cl = ctypes.c_longlong()
+        dp = lambda a: a.ctypes.data_as(ctypes.POINTER(ctypes.c_double))
+        st = self.L.mlh_smoothing_lengths(self.h, float(n_ngb), dp(h), dp(ne), ctypes.byref(cl))
+        if st != 0:
+            raise MLHError(st, "mlh_smoothing_lengths", self.L.mlh_last_error().decode())
+        return h, ne, int(cl.value)
 
     def autotune(self, trial_steps: int = 1) -> dict:
         t = Tuning()

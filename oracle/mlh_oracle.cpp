@@ -25,6 +25,14 @@
 //    xjxi[2] in the pairwise limiter (Particles.cpp:1498-1539, 1623-1631); this
 //    restatement uses z_j - z_i.
 //  * Errors set bits in the returned status instead of calling exit().
+//
+// Addition without a reference counterpart (the reference uses one global
+// kernelSize): per-particle smoothing lengths (hsolve) and the step mode that
+// uses them (adaptive_h).  Its arithmetic is fixed operation by operation
+// (explicit fma, the candidate order of the cell stencil, 32 strided partial
+// sums combined pairwise at distances 16, 8, 4, 2, 1) so that a data-parallel
+// implementation that sums the same way gets the same smoothing lengths bit
+// for bit.
 #include "mlh_oracle.h"
 #include "riemann_exact.hpp"
 
@@ -72,7 +80,10 @@ template <int D>
 struct Sim {
     orc_config c;
     int N;
-    double h;
+    double h;                          // kernelSize: the support radius, or its maximum with adaptive_h
+    std::vector<double> hp;            // per-particle support radius (h everywhere without adaptive_h)
+    std::vector<double> nEff;          // effective neighbour number of the last h solve
+    long hClamped = 0, hIters = 0;
     std::vector<double> X[3], V[3], m, u, rho, P, omega;
     // gradients in the reference's call order: rho, vx, vy, (vz), P
     std::vector<double> G[5];          // [field][i*3+alpha]
@@ -95,9 +106,11 @@ struct Sim {
     unsigned status = 0;
     long riemannSolves = 0, newtonTotal = 0;
 
-    // --- Kernel::cubicSpline, demonstrator/src/Particles.cpp:7-24
-    double kernel(double r) const {
-        double h2 = h / 2.;
+    // --- Kernel::cubicSpline, demonstrator/src/Particles.cpp:7-24, for a
+    // support radius hh (the reference's kernelSize)
+    double kernel(double r) const { return kernelH(r, h); }
+    double kernelH(double r, double hh) const {
+        double h2 = hh / 2.;
         double sigma = (D == 2) ? 10. / (7. * M_PI * h2 * h2) : 1. / (M_PI * h2 * h2 * h2);
         double q = r / h2;
         if (0. <= q && q <= 1.) return sigma * (1. - 3. / 2. * q * q * (1. - q / 2.));
@@ -174,6 +187,14 @@ struct Sim {
     // --- Particles::gridNNS (Particles.cpp:324-365) with the stencil of
     // Domain::getNeighborCells (Domain.cpp:83-118), plus the periodic images
     // (Particles::ghostNNS, Particles.cpp:2237-2260) found through wrapped cells.
+    // squared search radius of a pair: h^2, or max(h_i^2, h_j^2) with
+    // per-particle smoothing lengths (j the parent of an image)
+    double pairSq(int i, int j, double hSqr) const {
+        if (!c.adaptive_h) return hSqr;
+        double a = hp[i] * hp[i], b = hp[j] * hp[j];
+        return a > b ? a : b;
+    }
+
     void nns() {
         const double hSqr = h * h;
         off.assign(N + 1, 0);
@@ -207,7 +228,7 @@ struct Sim {
                                 double dSqr = (X[0][j] - X[0][i]) * (X[0][j] - X[0][i])
                                             + (X[1][j] - X[1][i]) * (X[1][j] - X[1][i]);
                                 if (D == 3) dSqr += (X[2][j] - X[2][i]) * (X[2][j] - X[2][i]);
-                                if (dSqr < hSqr) real.push_back((uint32_t)j);
+                                if (dSqr < pairSq(i, j, hSqr)) real.push_back((uint32_t)j);
                             } else {
                                 double xj[3];
                                 bool ok = true;
@@ -219,7 +240,7 @@ struct Sim {
                                 double dSqr = (xj[0] - X[0][i]) * (xj[0] - X[0][i])
                                             + (xj[1] - X[1][i]) * (xj[1] - X[1][i]);
                                 if (D == 3) dSqr += (xj[2] - X[2][i]) * (xj[2] - X[2][i]);
-                                if (dSqr < hSqr) img.push_back((uint32_t)j | (wrap << IMG_SHIFT));
+                                if (dSqr < pairSq(i, j, hSqr)) img.push_back((uint32_t)j | (wrap << IMG_SHIFT));
                             }
                         }
                     }
@@ -262,15 +283,15 @@ struct Sim {
         omega.assign(N, 0.);
         for (int i = 0; i < N; ++i) {
             double omg = 0.;
-            for (int s = off[i]; s < off[i] + noi[i]; ++s) omg += kernel(dist(i, s));
-            omega[i] = omg + kernel(0.);
+            for (int s = off[i]; s < off[i] + noi[i]; ++s) omg += kernelH(dist(i, s), hp[i]);
+            omega[i] = omg + kernelH(0., hp[i]);
             rho[i] = m[i] * omega[i];
             if (rho[i] <= 0.) status |= ST_NEG_DENSITY;
         }
         if (c.periodic)
             for (int i = 0; i < N; ++i) {
                 double omg = omega[i];
-                for (int s = off[i] + noi[i]; s < off[i + 1]; ++s) omg += kernel(dist(i, s));
+                for (int s = off[i] + noi[i]; s < off[i + 1]; ++s) omg += kernelH(dist(i, s), hp[i]);
                 omega[i] = omg;
                 rho[i] = m[i] * omega[i];
             }
@@ -307,7 +328,7 @@ struct Sim {
                 double vSig_i = ci + cj - vijxij;
                 vSig = vSig_i > vSig ? vSig_i : vSig;
             }
-            double dti = c.cfl * h / vSig;
+            double dti = c.cfl * hp[i] / vSig;
             dt_ = dti < dt_ ? dti : dt_;
         }
         return dt_;
@@ -349,7 +370,7 @@ struct Sim {
             for (int a = 0; a < D; ++a) xi[a] = X[a][i];
             for (int s = off[i]; s < off[i + 1]; ++s) {
                 double r = dist(i, s);
-                double psij_xi = kernel(r) / omega[i];
+                double psij_xi = kernelH(r, hp[i]) / omega[i];
                 double xj[3];
                 coords(nb[s], xj);
                 for (int al = 0; al < D; ++al)
@@ -360,7 +381,7 @@ struct Sim {
             for (int k = 0; k < D * D; ++k) B[(size_t)i * D * D + k] = Bi[k];
             for (int s = off[i]; s < off[i + 1]; ++s) {
                 double r = dist(i, s);
-                double psij_xi = kernel(r) / omega[i];
+                double psij_xi = kernelH(r, hp[i]) / omega[i];
                 double xj[3];
                 coords(nb[s], xj);
                 for (int al = 0; al < D; ++al) {
@@ -402,7 +423,7 @@ struct Sim {
                     coords(nb[s], xj);
                     for (int a = 0; a < D; ++a) {
                         if (c.first_order_quad_point) xij[a] = (X[a][i] + xj[a]) / 2.;
-                        else xij[a] = X[a][i] + h / 4. * (xj[a] - X[a][i]);
+                        else xij[a] = X[a][i] + hp[i] / 4. * (xj[a] - X[a][i]);
                         xijxi[a] = xij[a] - X[a][i];
                     }
                     if (psiMaxNgb < fv[j]) psiMaxNgb = fv[j];
@@ -480,7 +501,7 @@ struct Sim {
                         xijxj[a] = .5 * (X[a][i] - xj[a]);
                         xijxi[a] = .5 * (xj[a] - X[a][i]);
                     } else {
-                        xij[a] = X[a][i] + h / 4. * xjxi[a];
+                        xij[a] = X[a][i] + hp[i] / 4. * xjxi[a];
                         xijxi[a] = xij[a] - X[a][i];
                         xijxj[a] = xij[a] - xj[a];
                     }
@@ -715,10 +736,117 @@ struct Sim {
         }
     }
 
-    // MeshlessScheme::run loop body, MeshlessScheme.cpp:39-253 (no dumps)
-    int step() {
-        status = 0;
-        riemannSolves = 0; newtonTotal = 0;
+    // --- Per-particle smoothing lengths (no reference counterpart).  For each
+    // particle the support radius x in (0, h] at which the effective
+    // neighbour number N(x) = V_D x^D (W(0, x) + sum_j W(r_ij, x)) equals
+    // n_ngb (V_D the volume of the unit ball).  With the cubic spline of
+    // support x, N(x) = K_D (1 + S(x)), S(x) = sum_j f(2 r_ij / x), f the
+    // spline's shape (f(0) = 1) and K_D = 32/3 in 3D, 40/7 in 2D.  S is
+    // increasing in x; dS/dx = G(x) / x with G = sum_j -f'(q) q.  Bracketed
+    // Newton from the previous h_i (or h); the candidates are the particles
+    // of the 3^D cell stencil within h (images by the ghost rule), in stencil
+    // order; a particle with N(h) < n_ngb keeps h (counted as clamped).
+    static void shape(double r, double ihh2, double &f, double &g) {
+        double q = r * ihh2;
+        if (q <= 1.) {
+            double q2 = q * q;
+            f = std::fma(q2, std::fma(0.75, q, -1.5), 1.);
+            g = q2 * std::fma(-2.25, q, 3.);
+        } else if (q < 2.) {
+            double t = 2. - q, t2 = t * t;
+            f = 0.25 * t2 * t;
+            g = 0.75 * t2 * q;
+        } else {
+            f = 0.;
+            g = 0.;
+        }
+    }
+
+    void hsolve(double n_ngb) {
+        const double KD = D == 3 ? 32. / 3. : 40. / 7.;
+        const double St = n_ngb / KD - 1.;
+        const double tolS = 1e-12 * St;
+        const double hSqr = h * h;
+        hp.resize(N, h);
+        nEff.assign(N, 0.);
+        hClamped = 0;
+        hIters = 0;
+        std::vector<double> r;
+        for (int i = 0; i < N; ++i) {
+            r.clear();
+            int ic = cellOf[i];
+            int ix = ic % cells[0];
+            int iy = (ic / cells[0]) % cells[1];
+            int iz = D == 3 ? ic / (cells[0] * cells[1]) : 0;
+            for (int k = ix - 1; k <= ix + 1; ++k)
+                for (int l = iy - 1; l <= iy + 1; ++l)
+                    for (int mm = (D == 3 ? iz - 1 : 0); mm <= (D == 3 ? iz + 1 : 0); ++mm) {
+                        int cc[3] = {k, l, mm};
+                        unsigned wrap = 0;
+                        bool skip = false;
+                        for (int a = 0; a < D; ++a)
+                            if (cc[a] < 0 || cc[a] >= cells[a]) {
+                                if (!c.periodic) { skip = true; break; }
+                                cc[a] = cc[a] < 0 ? cc[a] + cells[a] : cc[a] - cells[a];
+                                wrap |= 1u << a;
+                            }
+                        if (skip) continue;
+                        int cell = cc[0] + cc[1] * cells[0] + (D == 3 ? cc[2] * cells[0] * cells[1] : 0);
+                        for (int j : grid[cell]) {
+                            if (!wrap && j == i) continue;
+                            double xj[3];
+                            bool ok = true;
+                            for (int a = 0; a < D; ++a) {
+                                xj[a] = X[a][j];
+                                if (wrap & (1u << a)) ok = ok && image(a, X[a][j], xj[a]);
+                            }
+                            if (!ok) continue;
+                            double dSqr = (xj[0] - X[0][i]) * (xj[0] - X[0][i]) + (xj[1] - X[1][i]) * (xj[1] - X[1][i]);
+                            if (D == 3) dSqr += (xj[2] - X[2][i]) * (xj[2] - X[2][i]);
+                            if (dSqr < hSqr) r.push_back(std::sqrt(dSqr));
+                        }
+                    }
+            double x = hp[i];
+            if (!(x > 0. && x <= h)) x = h;
+            double lo_ = 0., hi_ = h, S = 0.;
+            bool upper = false;
+            for (int it = 0;; ++it) {
+                // 32 strided partial sums, then pairwise at distance 16 .. 1
+                double sf[32], sg[32];
+                for (int l = 0; l < 32; ++l) { sf[l] = 0.; sg[l] = 0.; }
+                const double ihh2 = 1. / (0.5 * x);
+                for (size_t t = 0; t < r.size(); ++t) {
+                    double f, g;
+                    shape(r[t], ihh2, f, g);
+                    sf[t % 32] += f;
+                    sg[t % 32] += g;
+                }
+                for (int o = 16; o > 0; o >>= 1) {
+                    double tf[32], tg[32];
+                    for (int l = 0; l < 32; ++l) { tf[l] = sf[l] + sf[l ^ o]; tg[l] = sg[l] + sg[l ^ o]; }
+                    for (int l = 0; l < 32; ++l) { sf[l] = tf[l]; sg[l] = tg[l]; }
+                }
+                S = sf[0];
+                const double G = sg[0];
+                ++hIters;
+                const double F = S - St;
+                if (std::fabs(F) <= tolS) break;
+                if (F < 0. && x >= h) { ++hClamped; break; }
+                if (it + 1 >= 50) break;
+                if (F > 0.) { hi_ = x; upper = true; }
+                else lo_ = x;
+                double xn = G > 0. ? x - F * x / G : 0.5 * (lo_ + hi_);
+                if (!(xn > lo_ && xn < hi_)) xn = (!upper && xn >= hi_) ? h : 0.5 * (lo_ + hi_);
+                if (xn == x) break;
+                x = xn;
+            }
+            hp[i] = x;
+            nEff[i] = KD * (S + 1.);
+        }
+    }
+
+    // grid of the current positions: the periodic box, or the bounding box
+    void binning() {
         if (c.periodic) {
             for (int a = 0; a < D; ++a) { lo[a] = c.box_lo[a]; hi[a] = c.box_hi[a]; }
         } else {
@@ -726,6 +854,14 @@ struct Sim {
         }
         createGrid();
         assign();
+    }
+
+    // MeshlessScheme::run loop body, MeshlessScheme.cpp:39-253 (no dumps)
+    int step() {
+        status = 0;
+        riemannSolves = 0; newtonTotal = 0;
+        binning();
+        if (c.adaptive_h) hsolve(c.n_ngb);
         nns();
         density();
         pressure();
@@ -754,6 +890,7 @@ Sim<D> *make(const orc_config *cfg, int n, const double *x, const double *y, con
     s->c = *cfg;
     s->N = n;
     s->h = cfg->kernel_size;
+    s->hp.assign(n, cfg->kernel_size);
     const double *xs[3] = {x, y, z}, *vs[3] = {vx, vy, vz};
     for (int a = 0; a < 3; ++a) {
         s->X[a].assign(n, 0.);
@@ -774,7 +911,8 @@ template <int D>
 long sizeOf(Sim<D> *s, const std::string &nm) {
     long N = s->N, S = s->off.empty() ? 0 : s->off[N];
     if (nm == "x" || nm == "y" || nm == "z" || nm == "vx" || nm == "vy" || nm == "vz" || nm == "m" || nm == "u" ||
-        nm == "rho" || nm == "P" || nm == "omega" || nm == "noi" || nm == "noi_img" || nm == "mF" || nm == "eF")
+        nm == "rho" || nm == "P" || nm == "omega" || nm == "noi" || nm == "noi_img" || nm == "mF" || nm == "eF" ||
+        nm == "h" || nm == "n_eff")
         return N;
     if (nm == "off") return N + 1;
     if (nm == "nnl" || nm == "rev" ) return S;
@@ -805,6 +943,8 @@ int getArr(Sim<D> *s, const std::string &nm, void *out) {
     if (nm == "rho") return cp(s->rho);
     if (nm == "P") return cp(s->P);
     if (nm == "omega") return cp(s->omega);
+    if (nm == "h") return cp(s->hp);
+    if (nm == "n_eff") { if (s->nEff.size() != (size_t)s->N) return -1; return cp(s->nEff); }
     if (nm == "mF") return cp(s->mF);
     if (nm == "eF") return cp(s->eF);
     if (nm == "vF") return cp(s->vF);
@@ -837,6 +977,16 @@ int getArr(Sim<D> *s, const std::string &nm, void *out) {
         if (nm == std::string("gradraw_") + names[k]) return cp(s->Graw[f]);
     }
     return -1;
+}
+
+template <int D>
+long smoothing(Sim<D> *s, double n_ngb, double *h_out, double *neff_out) {
+    s->status = 0;
+    s->binning();
+    s->hsolve(n_ngb);
+    if (h_out) std::copy(s->hp.begin(), s->hp.end(), h_out);
+    if (neff_out) std::copy(s->nEff.begin(), s->nEff.end(), neff_out);
+    return s->hClamped;
 }
 
 }  // namespace
@@ -886,6 +1036,12 @@ int orc_riemann_batch(int n, const double *rhoL, const double *uL, const double 
         if (iters) iters[k] = it;
     }
     return 0;
+}
+
+long orc_smoothing_lengths(void *ctx, double n_ngb, double *h_out, double *neff_out) {
+    Handle *hnd = (Handle *)ctx;
+    if (hnd->dim == 2) return smoothing((Sim<2> *)hnd->sim, n_ngb, h_out, neff_out);
+    return smoothing((Sim<3> *)hnd->sim, n_ngb, h_out, neff_out);
 }
 
 void orc_destroy(void *ctx) {

@@ -38,6 +38,8 @@ typedef struct orc_config {
     double psi1;
     double psi2;
     double riemann_tol;
+    double n_ngb;       /* target effective neighbour number of the h solve */
+    int adaptive_h;     /* per-particle smoothing lengths in the step */
 } orc_config;
 
 void *orc_create(const orc_config *cfg, int n,
@@ -51,6 +53,10 @@ long orc_size(void *ctx, const char *name);
 /* Copy a named array into `out` (doubles, or int32 for integer arrays). */
 int orc_get(void *ctx, const char *name, void *out);
 void orc_destroy(void *ctx);
+/* Per-particle smoothing lengths on the current positions (see the .cpp):
+ * h_out, neff_out: n doubles each (may be NULL).  Returns the number of
+ * particles clamped at kernel_size. */
+long orc_smoothing_lengths(void *ctx, double n_ngb, double *h_out, double *neff_out);
 int orc_riemann_batch(int n, const double *rhoL, const double *uL, const double *pL, const double *rhoR,
                       const double *uR, const double *pR, double gamma, const double *guess, double *pstar,
                       int *iters);

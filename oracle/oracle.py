@@ -27,7 +27,8 @@ _DBL_FIELDS = ["kernel_size", "gamma", "cfl", "time_step", "beta", "psi1", "psi2
 class OrcConfig(ctypes.Structure):
     _fields_ = ([(f, ctypes.c_int) for f in _INT_FIELDS]
                 + [("box_lo", ctypes.c_double * 3), ("box_hi", ctypes.c_double * 3)]
-                + [(f, ctypes.c_double) for f in _DBL_FIELDS])
+                + [(f, ctypes.c_double) for f in _DBL_FIELDS]
+                + [("n_ngb", ctypes.c_double), ("adaptive_h", ctypes.c_int)])
 
 
 INT_ARRAYS = {"noi", "noi_img", "off", "rev", "newton_iters", "nnl"}
@@ -59,6 +60,8 @@ def lib():
         L.orc_riemann_batch.argtypes = [ctypes.c_int] + [dp] * 6 + [ctypes.c_double, dp, dp,
                                                                     ctypes.POINTER(ctypes.c_int)]
         L.orc_riemann_batch.restype = ctypes.c_int
+        L.orc_smoothing_lengths.restype = ctypes.c_long
+        L.orc_smoothing_lengths.argtypes = [ctypes.c_void_p, ctypes.c_double, dp, dp]
         _lib = L
     return _lib
 
@@ -86,6 +89,8 @@ def _cfg_struct(cfg) -> OrcConfig:
         s.box_hi[a] = float(cfg.box_hi[a])
     for f in _DBL_FIELDS:
         setattr(s, f, float(getattr(cfg, f)))
+    s.n_ngb = float(getattr(cfg, "n_ngb", 0.0))
+    s.adaptive_h = int(getattr(cfg, "adaptive_h", False))
     return s
 
 
@@ -114,6 +119,16 @@ class Oracle:
         if self.L.orc_get(self.h, name.encode(), out.ctypes.data) != 0:
             raise KeyError(name)
         return out
+
+    def smoothing_lengths(self, n_ngb: float):
+        """Per-particle smoothing lengths on the current positions: (h,
+        effective neighbour number, number clamped at kernel_size)."""
+        n = self.L.orc_size(self.h, b"x")
+        h = np.empty(n)
+        ne = np.empty(n)
+        dp = lambda a: a.ctypes.data_as(ctypes.POINTER(ctypes.c_double))
+        clamped = self.L.orc_smoothing_lengths(self.h, float(n_ngb), dp(h), dp(ne))
+        return h, ne, int(clamped)
 
     def state(self) -> dict:
         names = ["x", "y", "vx", "vy", "m", "u"] + (["z", "vz"] if self.dim == 3 else [])

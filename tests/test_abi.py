@@ -21,7 +21,7 @@ def test_header_and_exports_agree():
     for n in names:
         assert hasattr(L, n), n
     assert set(names) == set(runtime.EXPORTS)
-    assert L.mlh_abi_version() == 1
+    assert L.mlh_abi_version() == 2
 
 
 def test_create_without_gpu_fails_cleanly():
@@ -42,4 +42,9 @@ def test_create_without_gpu_fails_cleanly():
         L.mlh_destroy(h)
     # invalid arguments are rejected before touching the device
     cfg.dim = 4
+    assert L.mlh_create(ctypes.byref(cfg), ctypes.byref(hs.view), ctypes.byref(h)) == (1 << 20)
+    # adaptive smoothing lengths need a target above the particle's own count
+    cfg.dim = 2
+    cfg.adaptive_h = 1
+    cfg.n_ngb = 5.0
     assert L.mlh_create(ctypes.byref(cfg), ctypes.byref(hs.view), ctypes.byref(h)) == (1 << 20)
