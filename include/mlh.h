@@ -182,6 +182,34 @@ int mlh_get_fields(mlh_ctx *ctx, mlh_particles_view *dst);
  * MeshlessScheme.cpp:98-101); pass 0 for none.  stats may be NULL. */
 int mlh_step(mlh_ctx *ctx, int nsteps, double dt_max, mlh_step_stats *stats);
 
+/* The first stages of a step on the current state, without advancing it:
+ * grid, smoothing lengths (adaptive_h), neighbour search, density, pressure,
+ * dt (clamped to dt_max > 0) and the limited gradients
+ * (demonstrator/src/MeshlessScheme.cpp:39-144).  Afterwards the stage arrays
+ * ("rho", "P", "omega", "noi", "nnl", "grad_*", "dt", "h", ...) describe the
+ * current state: what the reference writes in Particles::dump2file
+ * (demonstrator/src/Particles.cpp:2978-3076), which it calls after these
+ * stages and before the Riemann solve of the same step.  mlh_step recomputes
+ * them. */
+int mlh_prepare(mlh_ctx *ctx, double dt_max);
+
+/* Riemann::Riemann + Riemann::exact (demonstrator/include/Riemann.h:19-26,
+ * demonstrator/src/Riemann.cpp:7-229) for n independent faces on the GPU, the
+ * same device code as the step's face kernel.  Per face (host arrays, face
+ * after face): Wi, the state of particle i, which is the LEFT state of the
+ * solve (the reference passes it as the constructor's WL, Particles.cpp:1852),
+ * and Wj, the neighbour's (RIGHT) state, each [rho, P, v_x, v_y(, v_z)]
+ * (dim + 2 doubles, velocities in the frame of vFrame); vFrame and Aij (dim
+ * doubles each).  Writes F (dim + 2 doubles per face: mass, energy, momentum,
+ * the order of the reference's Fij) and, if iters is not NULL, the Newton
+ * iterations per face (-1: no convergence).  meshless_finite_mass: the
+ * MESHLESS_FINITE_MASS variant (no mass flux through the face frame).  Newton
+ * tolerance 1e-10 relative, at most 100 iterations.  Returns MLH_ERR_* bits
+ * (MLH_ERR_NEWTON, MLH_ERR_VACUUM, MLH_ERR_NEG_PRESSURE) accumulated over the
+ * faces. */
+int mlh_riemann_fluxes(int dim, int n, const double *Wi, const double *Wj, const double *vFrame, const double *Aij,
+                       double gamma, int meshless_finite_mass, double *F, int *iters);
+
 /* Copy a named per-step array of the last step to host memory, for parity
  * checks (the arrays the reference keeps as Particles members, and the
  * smoothing lengths "h", "n_eff" (N) and "h_stats" (2: solve iterations,

@@ -20,7 +20,7 @@ BUILD = os.path.join(HERE, "_build")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVFLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "--expt-relaxed-constexpr"]
-SOURCES = ["mlh_kernels.cu", "mlh_capi.cu", "mlh_probe.cu", "mlh_noalloc.cu", "mlh_pstar.cu"]
+SOURCES = ["mlh_kernels.cu", "mlh_capi.cu", "mlh_probe.cu", "mlh_noalloc.cu", "mlh_pstar.cu", "mlh_io.cpp"]
 
 
 def nvcc() -> str:
@@ -49,6 +49,8 @@ def _deps():
 def build(verbose: bool = False, force: bool = False, extra_flags=()) -> str:
     deps = _deps()
     if not force and _newer(LIB, deps):
+        if not _newer(CLI, deps + [LIB]):
+            build_cli(verbose)
         return LIB
     os.makedirs(BUILD, exist_ok=True)
     cc = nvcc()
@@ -71,7 +73,27 @@ def build(verbose: bool = False, force: bool = False, extra_flags=()) -> str:
     if r.returncode != 0:
         raise RuntimeError(f"link failed:\n{r.stderr}")
     os.replace(tmp, LIB)
+    build_cli(verbose)
     return LIB
+
+
+CLI = os.path.join(HERE, "mlh")
+
+
+def build_cli(verbose: bool = False) -> str:
+    """The `mlh` command-line driver (csrc/mlh_main.cpp over include/mlh.hpp),
+    linked against libmlh.so next to it."""
+    src = os.path.join(CSRC, "mlh_main.cpp")
+    cxx = os.environ.get("CXX") or shutil.which("g++") or "g++"
+    cmd = [cxx, "-std=c++17", "-O2", "-Wall", src, "-o", CLI + ".tmp", "-L" + HERE, "-lmlh",
+           "-Wl,-rpath,$ORIGIN"]
+    if verbose:
+        print(" ".join(cmd), file=sys.stderr)
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError(f"mlh driver build failed:\n{r.stderr}")
+    os.replace(CLI + ".tmp", CLI)
+    return CLI
 
 
 if __name__ == "__main__":

@@ -437,6 +437,24 @@ static void drop_graph(mlh_ctx *c) {
     c->graph_exec = nullptr;
 }
 
+// After a launch sequence reported a capacity overflow: 1.5x neighbour slots
+// (MLH_ERR_NGB_OVERFLOW) and/or 2x cells (ST_CAPACITY); the work is repeated
+// by the caller.
+static int grow_buffers(mlh_ctx *c, unsigned st) {
+    if (st & MLH_ERR_NGB_OVERFLOW) {
+        free_neighbour_buffers(c);
+        c->p.K = c->p.K + c->p.K / 2;
+        if (int rc = alloc_neighbour_buffers(c)) return rc;
+    }
+    if (st & ST_CAPACITY) {
+        free_cell_buffers(c);
+        c->p.ncells_cap = c->p.ncells_cap * 2;
+        if (int rc = alloc_cell_buffers(c)) return rc;
+    }
+    drop_graph(c);   // buffers changed
+    return 0;
+}
+
 void mlh_destroy(mlh_ctx *c) {
     if (!c) return;
     if (c->stream) cudaStreamSynchronize(c->stream);
@@ -546,19 +564,7 @@ int mlh_step(mlh_ctx *c, int nsteps, double dt_max, mlh_step_stats *stats) {
         pairs += 2ll * ftot * done;
         if (st & (MLH_ERR_NGB_OVERFLOW | ST_CAPACITY)) {
             if (++retries > 8) { accumulated |= st; g_last_error = "capacity retries exhausted"; break; }
-            if (st & MLH_ERR_NGB_OVERFLOW) {
-                free_neighbour_buffers(c);
-                c->p.K = c->p.K + c->p.K / 2;
-                int rc = alloc_neighbour_buffers(c);
-                if (rc) return rc;
-            }
-            if (st & ST_CAPACITY) {
-                free_cell_buffers(c);
-                c->p.ncells_cap = c->p.ncells_cap * 2;
-                int rc = alloc_cell_buffers(c);
-                if (rc) return rc;
-            }
-            drop_graph(c);   // buffers changed
+            if (int rc = grow_buffers(c, st)) return rc;
             // the step is repeated: faces recorded by the aborted attempt go
             if (c->harvest.count) CK(cudaMemsetAsync(c->harvest.count, 0, sizeof(int), c->stream));
             continue;
@@ -763,17 +769,7 @@ int mlh_smoothing_lengths(mlh_ctx *c, double n_ngb, double *h_out, double *n_eff
         CK(cudaStreamSynchronize(c->stream));
         if (st & (MLH_ERR_NGB_OVERFLOW | ST_CAPACITY)) {
             if (retries >= 8) { g_last_error = "capacity retries exhausted"; return (int)st; }
-            if (st & MLH_ERR_NGB_OVERFLOW) {
-                free_neighbour_buffers(c);
-                c->p.K = c->p.K + c->p.K / 2;
-                if (int rc = alloc_neighbour_buffers(c)) return rc;
-            }
-            if (st & ST_CAPACITY) {
-                free_cell_buffers(c);
-                c->p.ncells_cap = c->p.ncells_cap * 2;
-                if (int rc = alloc_cell_buffers(c)) return rc;
-            }
-            drop_graph(c);
+            if (int rc = grow_buffers(c, st)) return rc;
             continue;
         }
         if (st) return (int)st;
@@ -788,6 +784,64 @@ int mlh_smoothing_lengths(mlh_ctx *c, double n_ngb, double *h_out, double *n_eff
         *clamped = (long long)hs[1];
     }
     return 0;
+}
+
+int mlh_prepare(mlh_ctx *c, double dt_max) {
+    if (!c) { g_last_error = "null context"; return MLH_ERR_INVALID; }
+    for (int retries = 0;; ++retries) {
+        StepArgs a = make_args(c, dt_max);
+        a.stop_after_gradients = 1;
+        a.timer = nullptr;
+        CK(cudaMemsetAsync(c->status, 0, sizeof(unsigned), c->stream));
+        step(a);
+        CK(cudaGetLastError());
+        unsigned st = 0;
+        CK(cudaMemcpyAsync(&st, c->status, sizeof(unsigned), cudaMemcpyDeviceToHost, c->stream));
+        CK(cudaStreamSynchronize(c->stream));
+        if (st & (MLH_ERR_NGB_OVERFLOW | ST_CAPACITY)) {
+            if (retries >= 8) { g_last_error = "capacity retries exhausted"; return (int)st; }
+            if (int rc = grow_buffers(c, st)) return rc;
+            continue;
+        }
+        return (int)st;
+    }
+}
+
+int mlh_riemann_fluxes(int dim, int n, const double *Wi, const double *Wj, const double *vFrame, const double *Aij,
+                       double gamma, int mfm, double *F, int *iters) {
+    if ((dim != 2 && dim != 3) || n < 0 || !(gamma > 1.) || (n > 0 && (!Wi || !Wj || !vFrame || !Aij || !F))) {
+        g_last_error = "invalid argument";
+        return MLH_ERR_INVALID;
+    }
+    if (n == 0) return 0;
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) { g_last_error = "no CUDA device"; return MLH_ERR_NO_DEVICE; }
+    const size_t NV = (size_t)dim + 2, nn = (size_t)n;
+    double *d = nullptr;
+    int *dit = nullptr;
+    unsigned *dst = nullptr;
+    const size_t doubles = nn * (3 * NV + 2 * dim);
+    CK(cudaMalloc(&d, sizeof(double) * doubles));
+    auto cleanup = [&]() { cudaFree(d); cudaFree(dit); cudaFree(dst); };
+    double *dWi = d, *dWj = d + nn * NV, *dv = d + 2 * nn * NV, *dA = dv + nn * dim, *dF = dA + nn * dim;
+    cudaError_t e = cudaMalloc(&dit, sizeof(int) * nn);
+    if (e == cudaSuccess) e = cudaMalloc(&dst, sizeof(unsigned));
+    if (e == cudaSuccess) e = cudaMemset(dst, 0, sizeof(unsigned));
+    if (e == cudaSuccess) e = cudaMemcpy(dWi, Wi, sizeof(double) * nn * NV, cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = cudaMemcpy(dWj, Wj, sizeof(double) * nn * NV, cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = cudaMemcpy(dv, vFrame, sizeof(double) * nn * dim, cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = cudaMemcpy(dA, Aij, sizeof(double) * nn * dim, cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) {
+        riemann_batch(dim, n, gamma, 1e-10, 100, mfm, dWi, dWj, dv, dA, dF, dit, dst, 0);
+        e = cudaGetLastError();
+    }
+    unsigned st = 0;
+    if (e == cudaSuccess) e = cudaMemcpy(F, dF, sizeof(double) * nn * NV, cudaMemcpyDeviceToHost);
+    if (e == cudaSuccess && iters) e = cudaMemcpy(iters, dit, sizeof(int) * nn, cudaMemcpyDeviceToHost);
+    if (e == cudaSuccess) e = cudaMemcpy(&st, dst, sizeof(unsigned), cudaMemcpyDeviceToHost);
+    cleanup();
+    if (e != cudaSuccess) return cuda_fail(e, "mlh_riemann_fluxes");
+    return (int)st;
 }
 
 int mlh_set_graph_mode(mlh_ctx *c, int enable) {

@@ -1134,6 +1134,82 @@ __device__ __forceinline__ float4 pstar_features(const double *R, const double *
 // MODE 0.  MODE 2 (second pass, over the queue): reload the state, solve from
 // the network's guess, project the flux.  `harvest` (MODE 0) records network
 // inputs and targets log(p*/p_TR) of every `stride`-th face.
+// Helper::rotationMatrix2D/3D(hatA, unitX) applied to the velocities of both
+// states (Riemann::Riemann, demonstrator/src/Riemann.cpp:7-81): hatA = A/|A|,
+// Lam the rotation taking hatA to the x axis.
+template <int D>
+__device__ __forceinline__ void face_frame(const double *A, double *hatA, double *Lam, double *R, double *L) {
+    const double unitX[3] = {1., 0., 0.};
+    double AN = sqrt(dotD<D>(A, A));
+    const double iAN = 1. / AN;
+#pragma unroll
+    for (int a = 0; a < D; ++a) hatA[a] = iAN * A[a];
+    if (D == 2) {
+        rot2(hatA, unitX, Lam);
+        double bR0 = L[2], bR1 = L[3], bL0 = R[2], bL1 = R[3];
+        L[2] = Lam[0] * bR0 + Lam[1] * bR1;
+        L[3] = Lam[2] * bR0 + Lam[3] * bR1;
+        R[2] = Lam[0] * bL0 + Lam[1] * bL1;
+        R[3] = Lam[2] * bL0 + Lam[3] * bL1;
+    } else {
+        rot3(hatA, unitX, Lam);
+        double bR0 = L[2], bR1 = L[3], bR2 = L[4], bL0 = R[2], bL1 = R[3], bL2 = R[4];
+        L[2] = Lam[0] * bR0 + Lam[1] * bR1 + Lam[2] * bR2;
+        L[3] = Lam[3] * bR0 + Lam[4] * bR1 + Lam[5] * bR2;
+        L[4] = Lam[6] * bR0 + Lam[7] * bR1 + Lam[8] * bR2;
+        R[2] = Lam[0] * bL0 + Lam[1] * bL1 + Lam[2] * bL2;
+        R[3] = Lam[3] * bL0 + Lam[4] * bL1 + Lam[5] * bL2;
+        R[4] = Lam[6] * bL0 + Lam[7] * bL1 + Lam[8] * bL2;
+    }
+}
+
+// Riemann::exact after the solve and rotateAndProjectFluxes2D/3D
+// (demonstrator/src/Riemann.cpp:100-229): tangential velocity from the
+// sampled side, back rotation (the transpose of Lam), boost by the frame
+// velocity and projection on A_ij.  Fo: [mass, energy, px, py, pz].  Returns
+// ST_VACUUM when the solution is vacuum, else 0.
+template <int D>
+__device__ __forceinline__ unsigned project_flux(const RiemannResult &rs, const double *R, const double *L,
+                                                 const double *Lam, const double *A, const double *vf,
+                                                 double inv_gm1, int mfm, double *Fo) {
+    unsigned st = 0;
+    double vSol[3] = {rs.u, 0., 0.};
+    if (rs.flag == 1) { for (int a = 1; a < D; ++a) vSol[a] = L[2 + a]; }
+    else if (rs.flag == -1) { for (int a = 1; a < D; ++a) vSol[a] = R[2 + a]; }
+    else st = ST_VACUUM;
+    const double rhoSol = rs.rho, PSol = rs.p;
+    const double pe = PSol * inv_gm1;
+    if (D == 2) {
+        // back rotation = transpose of Lam
+        double b0 = vSol[0], b1 = vSol[1];
+        vSol[0] = Lam[0] * b0 + Lam[2] * b1;
+        vSol[1] = Lam[1] * b0 + Lam[3] * b1;
+        Fo[0] = A[0] * rhoSol * vSol[0] + A[1] * rhoSol * vSol[1];
+        double vLab[2] = {vSol[0] + vf[0], vSol[1] + vf[1]};
+        if (mfm) { vSol[0] = 0.; vSol[1] = 0.; }
+        Fo[2] = A[0] * (rhoSol * vLab[0] * vSol[0] + PSol) + A[1] * rhoSol * vLab[0] * vSol[1];
+        Fo[3] = A[0] * rhoSol * vLab[1] * vSol[0] + A[1] * (rhoSol * vLab[1] * vSol[1] + PSol);
+        const double ek = rhoSol * .5 * (vLab[0] * vLab[0] + vLab[1] * vLab[1]);
+        Fo[1] = A[0] * (vSol[0] * (pe + ek) + PSol * vLab[0]) + A[1] * (vSol[1] * (pe + ek) + PSol * vLab[1]);
+        Fo[4] = 0.;
+    } else {
+        double b0 = vSol[0], b1 = vSol[1], b2 = vSol[2];
+        vSol[0] = Lam[0] * b0 + Lam[3] * b1 + Lam[6] * b2;
+        vSol[1] = Lam[1] * b0 + Lam[4] * b1 + Lam[7] * b2;
+        vSol[2] = Lam[2] * b0 + Lam[5] * b1 + Lam[8] * b2;
+        Fo[0] = A[0] * rhoSol * vSol[0] + A[1] * rhoSol * vSol[1] + A[2] * rhoSol * vSol[2];
+        double vLab[3] = {vSol[0] + vf[0], vSol[1] + vf[1], vSol[2] + vf[2]};
+        if (mfm) { vSol[0] = 0.; vSol[1] = 0.; vSol[2] = 0.; }
+        Fo[2] = A[0] * (rhoSol * vLab[0] * vSol[0] + PSol) + A[1] * rhoSol * vLab[0] * vSol[1] + A[2] * rhoSol * vLab[0] * vSol[2];
+        Fo[3] = A[0] * rhoSol * vLab[1] * vSol[0] + A[1] * (rhoSol * vLab[1] * vSol[1] + PSol) + A[2] * rhoSol * vLab[1] * vSol[2];
+        Fo[4] = A[0] * rhoSol * vLab[2] * vSol[0] + A[1] * rhoSol * vLab[2] * vSol[1] + A[2] * (rhoSol * vLab[2] * vSol[2] + PSol);
+        const double ek = rhoSol * .5 * ((vLab[0] * vLab[0] + vLab[1] * vLab[1]) + vLab[2] * vLab[2]);
+        Fo[1] = A[0] * (vSol[0] * (pe + ek) + PSol * vLab[0]) + A[1] * (vSol[1] * (pe + ek) + PSol * vLab[1])
+              + A[2] * (vSol[2] * (pe + ek) + PSol * vLab[2]);
+    }
+    return st;
+}
+
 template <int D, bool ROOT5, int MODE>
 __global__ void __launch_bounds__(256) k_faces(Params p, const Member *__restrict__ members,
                                                const int *__restrict__ memberOf, const GridInfo *__restrict__ grids,
@@ -1297,27 +1373,7 @@ __global__ void __launch_bounds__(256) k_faces(Params p, const Member *__restric
         }
         if (R[1] < 0. || L[1] < 0.) st_local |= ST_NEG_PRESSURE;
         // --- Riemann problem in the face frame (i left, j right)
-        double AN = sqrt(dotD<D>(A, A));
-        const double iAN = 1. / AN;
-#pragma unroll
-        for (int a = 0; a < D; ++a) hatA[a] = iAN * A[a];
-        if (D == 2) {
-            rot2(hatA, unitX, Lam);
-            double bR0 = L[2], bR1 = L[3], bL0 = R[2], bL1 = R[3];
-            L[2] = Lam[0] * bR0 + Lam[1] * bR1;
-            L[3] = Lam[2] * bR0 + Lam[3] * bR1;
-            R[2] = Lam[0] * bL0 + Lam[1] * bL1;
-            R[3] = Lam[2] * bL0 + Lam[3] * bL1;
-        } else {
-            rot3(hatA, unitX, Lam);
-            double bR0 = L[2], bR1 = L[3], bR2 = L[4], bL0 = R[2], bL1 = R[3], bL2 = R[4];
-            L[2] = Lam[0] * bR0 + Lam[1] * bR1 + Lam[2] * bR2;
-            L[3] = Lam[3] * bR0 + Lam[4] * bR1 + Lam[5] * bR2;
-            L[4] = Lam[6] * bR0 + Lam[7] * bR1 + Lam[8] * bR2;
-            R[2] = Lam[0] * bL0 + Lam[1] * bL1 + Lam[2] * bL2;
-            R[3] = Lam[3] * bL0 + Lam[4] * bL1 + Lam[5] * bL2;
-            R[4] = Lam[6] * bL0 + Lam[7] * bL1 + Lam[8] * bL2;
-        }
+        face_frame<D>(A, hatA, Lam, R, L);
         }   // MODE != 2
         double guess = -1.;
         if (MODE == 2) {
@@ -1359,41 +1415,8 @@ __global__ void __launch_bounds__(256) k_faces(Params p, const Member *__restric
             if (MODE == 2) ++deferred_local;
             iters_local += (unsigned long long)rs.iters;
         }
-        double vSol[3] = {rs.u, 0., 0.};
-        if (rs.flag == 1) { for (int a = 1; a < D; ++a) vSol[a] = L[2 + a]; }
-        else if (rs.flag == -1) { for (int a = 1; a < D; ++a) vSol[a] = R[2 + a]; }
-        else st_local |= ST_VACUUM;
-        const double rhoSol = rs.rho, PSol = rs.p;
-        const double pe = PSol * rc.inv_gm1;
         double Fo[5];
-        if (D == 2) {
-            // back rotation = transpose of Lam
-            double b0 = vSol[0], b1 = vSol[1];
-            vSol[0] = Lam[0] * b0 + Lam[2] * b1;
-            vSol[1] = Lam[1] * b0 + Lam[3] * b1;
-            Fo[0] = A[0] * rhoSol * vSol[0] + A[1] * rhoSol * vSol[1];
-            double vLab[2] = {vSol[0] + vf[0], vSol[1] + vf[1]};
-            if (p.mfm) { vSol[0] = 0.; vSol[1] = 0.; }
-            Fo[2] = A[0] * (rhoSol * vLab[0] * vSol[0] + PSol) + A[1] * rhoSol * vLab[0] * vSol[1];
-            Fo[3] = A[0] * rhoSol * vLab[1] * vSol[0] + A[1] * (rhoSol * vLab[1] * vSol[1] + PSol);
-            const double ek = rhoSol * .5 * (vLab[0] * vLab[0] + vLab[1] * vLab[1]);
-            Fo[1] = A[0] * (vSol[0] * (pe + ek) + PSol * vLab[0]) + A[1] * (vSol[1] * (pe + ek) + PSol * vLab[1]);
-            Fo[4] = 0.;
-        } else {
-            double b0 = vSol[0], b1 = vSol[1], b2 = vSol[2];
-            vSol[0] = Lam[0] * b0 + Lam[3] * b1 + Lam[6] * b2;
-            vSol[1] = Lam[1] * b0 + Lam[4] * b1 + Lam[7] * b2;
-            vSol[2] = Lam[2] * b0 + Lam[5] * b1 + Lam[8] * b2;
-            Fo[0] = A[0] * rhoSol * vSol[0] + A[1] * rhoSol * vSol[1] + A[2] * rhoSol * vSol[2];
-            double vLab[3] = {vSol[0] + vf[0], vSol[1] + vf[1], vSol[2] + vf[2]};
-            if (p.mfm) { vSol[0] = 0.; vSol[1] = 0.; vSol[2] = 0.; }
-            Fo[2] = A[0] * (rhoSol * vLab[0] * vSol[0] + PSol) + A[1] * rhoSol * vLab[0] * vSol[1] + A[2] * rhoSol * vLab[0] * vSol[2];
-            Fo[3] = A[0] * rhoSol * vLab[1] * vSol[0] + A[1] * (rhoSol * vLab[1] * vSol[1] + PSol) + A[2] * rhoSol * vLab[1] * vSol[2];
-            Fo[4] = A[0] * rhoSol * vLab[2] * vSol[0] + A[1] * rhoSol * vLab[2] * vSol[1] + A[2] * (rhoSol * vLab[2] * vSol[2] + PSol);
-            const double ek = rhoSol * .5 * ((vLab[0] * vLab[0] + vLab[1] * vLab[1]) + vLab[2] * vLab[2]);
-            Fo[1] = A[0] * (vSol[0] * (pe + ek) + PSol * vLab[0]) + A[1] * (vSol[1] * (pe + ek) + PSol * vLab[1])
-                  + A[2] * (vSol[2] * (pe + ek) + PSol * vLab[2]);
-        }
+        st_local |= project_flux<D>(rs, R, L, Lam, A, vf, rc.inv_gm1, p.mfm, Fo);
         double2 *dst = reinterpret_cast<double2 *>(Fface + (size_t)f * 6);
         dst[0] = make_double2(Fo[0], Fo[1]);
         dst[1] = make_double2(Fo[2], Fo[3]);
@@ -1412,6 +1435,52 @@ __global__ void __launch_bounds__(256) k_faces(Params p, const Member *__restric
         if (deferred_local) atomicAdd(newtonSum + 2, deferred_local);
         if (st_local) flag(status, st_local);
     }
+}
+
+// Riemann::Riemann + Riemann::exact (demonstrator/src/Riemann.cpp:7-229) for a
+// batch of independent faces: per face the left state Wi (particle i) and the
+// right state Wj (neighbour j), each [rho, P, v_x, v_y(, v_z)], the frame
+// velocity and A_ij; one thread per face, the same device functions as
+// k_faces.  F: [mass, energy, momentum] per face; iters: Newton iterations
+// (-1 when the iteration did not converge).
+template <int D, bool ROOT5>
+__global__ void __launch_bounds__(256) k_riemann_batch(int n, RiemannConsts rc, int mfm,
+                                                       const double *__restrict__ Wi, const double *__restrict__ Wj,
+                                                       const double *__restrict__ vFrame,
+                                                       const double *__restrict__ Aij, double *__restrict__ F,
+                                                       int *__restrict__ iters, unsigned *__restrict__ status) {
+    constexpr int NV = D + 2;
+    unsigned st = 0;
+    for (int f = blockIdx.x * blockDim.x + threadIdx.x; f < n; f += gridDim.x * blockDim.x) {
+        double R[5] = {0., 0., 0., 0., 0.}, L[5] = {0., 0., 0., 0., 0.};
+        double A[3] = {0., 0., 0.}, vf[3] = {0., 0., 0.}, hatA[3], Lam[9];
+#pragma unroll
+        for (int k = 0; k < NV; ++k) { R[k] = Wi[(size_t)f * NV + k]; L[k] = Wj[(size_t)f * NV + k]; }
+#pragma unroll
+        for (int a = 0; a < D; ++a) { A[a] = Aij[(size_t)f * D + a]; vf[a] = vFrame[(size_t)f * D + a]; }
+        if (R[1] < 0. || L[1] < 0.) st |= ST_NEG_PRESSURE;
+        face_frame<D>(A, hatA, Lam, R, L);
+        const RiemannResult rs = ROOT5 ? riemann_exact5(rc, R[0], R[2], R[1], L[0], L[2], L[1], -1., 0.)
+                                       : riemann_exact(rc, R[0], R[2], R[1], L[0], L[2], L[1], -1., 0.);
+        if (rs.iters < 0) st |= ST_NEWTON;
+        double Fo[5];
+        st |= project_flux<D>(rs, R, L, Lam, A, vf, rc.inv_gm1, mfm, Fo);
+#pragma unroll
+        for (int k = 0; k < NV; ++k) F[(size_t)f * NV + k] = Fo[k];
+        if (iters) iters[f] = rs.iters;
+    }
+    if (st) flag(status, st);
+}
+
+void riemann_batch(int dim, int n, double gamma, double rtol, int max_iter, int mfm, const double *Wi,
+                   const double *Wj, const double *vFrame, const double *Aij, double *F, int *iters,
+                   unsigned *status, cudaStream_t s) {
+    const RiemannConsts rc = make_riemann_consts(gamma, rtol, max_iter);
+    const int blocks = n > 0 ? (n + 255) / 256 : 1;
+#define MLH_RB(DD, R5) k_riemann_batch<DD, R5><<<blocks, 256, 0, s>>>(n, rc, mfm, Wi, Wj, vFrame, Aij, F, iters, status)
+    if (dim == 2) { if (rc.root5) MLH_RB(2, true); else MLH_RB(2, false); }
+    else { if (rc.root5) MLH_RB(3, true); else MLH_RB(3, false); }
+#undef MLH_RB
 }
 
 // ------------------------------------------------------------------ gather + update
@@ -1595,6 +1664,7 @@ void launch_step(StepArgs &a) {
     k_gradients<D><<<(p.n + gT - 1) / gT, gT, 0, s>>>(p, a.members, a.memberOf, a.grids, a.prim, a.geo, a.nbr, a.ww, a.noi,
                                          a.noiImg, a.grad, a.gradRaw, a.psi);
     tock(KT_GRAD);
+    if (a.stop_after_gradients) return;
 
     tick(KT_LINK);
     exclusive_scan(a.faceCnt, p.n, a.faceOff, a.scanTiles, a.scanTotal, s);

@@ -70,6 +70,8 @@ struct StepArgs {
     // number (may be null), counters [iterations, clamped particles]
     double *hp, *neff;
     unsigned long long *hstat;
+    // end the step after the gradients and the limiter (mlh_prepare)
+    int stop_after_gradients;
     // optional per-kernel timer callback (phase 0 = before, 1 = after)
     void (*timer)(void *, int, int);
     void *timer_ctx;
@@ -91,6 +93,10 @@ void launch_grid_bounds(const double *x, const double *y, const double *z, const
 void pack_posf(const double *x, const double *y, const double *z, int n, int dim, float4 *posf, cudaStream_t s);
 void exclusive_scan(const int *in, int n, int *out, int *tile_buf, int *total, cudaStream_t s);
 const char *kernel_timer_name(int id);
+// Riemann problems of n independent faces (device arrays; see k_riemann_batch)
+void riemann_batch(int dim, int n, double gamma, double rtol, int max_iter, int mfm, const double *Wi,
+                   const double *Wj, const double *vFrame, const double *Aij, double *F, int *iters,
+                   unsigned *status, cudaStream_t s);
 void set_last_error(const char *msg);
 // MLP inference over the faces of a step: n read on the device (min with cap)
 void pstar_infer_dev(const float4 *x, const int *n_dev, int cap, const void *packed, float *y, int sm_count,

@@ -64,7 +64,7 @@ EXPORTS = ["mlh_abi_version", "mlh_last_error", "mlh_create", "mlh_destroy", "ml
            "mlh_kernel_times", "mlh_reset_kernel_times", "mlh_probe_fp64_tflops",
            "mlh_grid_bounds_noalloc", "mlh_ensemble_create", "mlh_member_times", "mlh_set_graph_mode",
            "mlh_autotune", "mlh_set_tuning", "mlh_pstar_infer", "mlh_pstar_grad", "mlh_pstar_train", "mlh_set_pstar_weights",
-           "mlh_pstar_harvest", "mlh_smoothing_lengths"]
+           "mlh_pstar_harvest", "mlh_smoothing_lengths", "mlh_prepare", "mlh_riemann_fluxes"]
 
 _lib = None
 
@@ -130,6 +130,10 @@ def load(path: str = LIB_PATH):
     L.mlh_smoothing_lengths.argtypes = [vp, ctypes.c_double, ctypes.POINTER(ctypes.c_double),
                                         ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_longlong)]
     L.mlh_smoothing_lengths.restype = ctypes.c_int
+    L.mlh_prepare.argtypes = [vp, ctypes.c_double]
+    L.mlh_prepare.restype = ctypes.c_int
+    L.mlh_riemann_fluxes.argtypes = [ctypes.c_int, ctypes.c_int] + [dp] * 4 + [ctypes.c_double, ctypes.c_int, dp, dp]
+    L.mlh_riemann_fluxes.restype = ctypes.c_int
     _lib = L
     return L
 
@@ -220,6 +224,26 @@ def pstar_train(x, t, weights=None, epochs: int = 10, batch: int = 4096, lr: flo
     return w, hist
 
 
+def riemann_fluxes(Wi, Wj, vframe, aij, gamma: float = 5.0 / 3.0, mfm: bool = False):
+    """Face fluxes of independent Riemann problems on the GPU (mlh_riemann_fluxes).
+    Wi (left, particle i), Wj (right): (n, dim + 2) [rho, P, v...]; vframe, aij: (n, dim).
+    Returns (F (n, dim + 2) [mass, energy, momentum], Newton iterations, status)."""
+    L = load()
+    Wi = np.ascontiguousarray(Wi, dtype=np.float64)
+    Wj = np.ascontiguousarray(Wj, dtype=np.float64)
+    vframe = np.ascontiguousarray(vframe, dtype=np.float64)
+    aij = np.ascontiguousarray(aij, dtype=np.float64)
+    n, nv = Wi.shape
+    dim = nv - 2
+    F = np.zeros((n, nv))
+    it = np.zeros(n, dtype=np.int32)
+    st = L.mlh_riemann_fluxes(dim, n, Wi.ctypes.data, Wj.ctypes.data, vframe.ctypes.data, aij.ctypes.data,
+                              float(gamma), int(mfm), F.ctypes.data, it.ctypes.data)
+    if st & ((1 << 20) | (1 << 21) | (1 << 22)):
+        raise MLHError(st, "mlh_riemann_fluxes", L.mlh_last_error().decode())
+    return F, it, st
+
+
 class Simulation:
     """One MFV simulation on the GPU through the C ABI.
 
@@ -302,6 +326,12 @@ class Simulation:
         if st != 0:
             raise MLHError(st, "mlh_smoothing_lengths", self.L.mlh_last_error().decode())
         return h, ne, int(cl.value)
+
+    def prepare(self, dt_max: float = 0.0):
+        """Density, dt and limited gradients of the current state (mlh_prepare)."""
+        st = self.L.mlh_prepare(self.h, dt_max)
+        if st != 0:
+            raise MLHError(st, "mlh_prepare", self.L.mlh_last_error().decode())
 
     def autotune(self, trial_steps: int = 1) -> dict:
         t = Tuning()

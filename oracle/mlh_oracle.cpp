@@ -989,6 +989,33 @@ long smoothing(Sim<D> *s, double n_ngb, double *h_out, double *neff_out) {
     return s->hClamped;
 }
 
+// Riemann::Riemann + Riemann::exact for independent faces (the step's
+// riemann() on a simulation without particles).
+template <int D>
+int riemannFaces(int n, const double *Wi, const double *Wj, const double *vFrame, const double *Aij, double gamma,
+                 int mfm, double *F, int *iters) {
+    orc_config cfg;
+    std::memset(&cfg, 0, sizeof(cfg));
+    cfg.dim = D;
+    cfg.gamma = gamma;
+    cfg.meshless_finite_mass = mfm;
+    cfg.riemann_tol = 1e-10;
+    cfg.riemann_max_iter = 100;
+    Sim<D> s;
+    s.c = cfg;
+    s.N = 0;
+    orc::ExactRiemann rs(gamma, cfg.riemann_tol, cfg.riemann_max_iter);
+    const int NV = D + 2;
+    for (int f = 0; f < n; ++f) {
+        double wi[5], wj[5];
+        for (int k = 0; k < NV; ++k) { wi[k] = Wi[(size_t)f * NV + k]; wj[k] = Wj[(size_t)f * NV + k]; }
+        if (wi[1] < 0. || wj[1] < 0.) s.status |= ST_NEG_PRESSURE;
+        s.riemann(wi, wj, vFrame + (size_t)f * D, Aij + (size_t)f * D, F + (size_t)f * NV, rs);
+        if (iters) iters[f] = s.newtonIters.back();
+    }
+    return (int)s.status;
+}
+
 }  // namespace
 
 extern "C" {
@@ -1042,6 +1069,12 @@ long orc_smoothing_lengths(void *ctx, double n_ngb, double *h_out, double *neff_
     Handle *hnd = (Handle *)ctx;
     if (hnd->dim == 2) return smoothing((Sim<2> *)hnd->sim, n_ngb, h_out, neff_out);
     return smoothing((Sim<3> *)hnd->sim, n_ngb, h_out, neff_out);
+}
+
+int orc_riemann_fluxes(int dim, int n, const double *Wi, const double *Wj, const double *vFrame, const double *Aij,
+                       double gamma, int mfm, double *F, int *iters) {
+    if (dim == 2) return riemannFaces<2>(n, Wi, Wj, vFrame, Aij, gamma, mfm, F, iters);
+    return riemannFaces<3>(n, Wi, Wj, vFrame, Aij, gamma, mfm, F, iters);
 }
 
 void orc_destroy(void *ctx) {

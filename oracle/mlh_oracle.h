@@ -53,6 +53,11 @@ long orc_size(void *ctx, const char *name);
 /* Copy a named array into `out` (doubles, or int32 for integer arrays). */
 int orc_get(void *ctx, const char *name, void *out);
 void orc_destroy(void *ctx);
+/* Riemann::Riemann + Riemann::exact of n independent faces: Wi (left, particle
+ * i) and Wj (right) [rho, P, v..] (dim + 2 each), vFrame, Aij (dim each); F
+ * (dim + 2: mass, energy, momentum), iters (may be NULL). */
+int orc_riemann_fluxes(int dim, int n, const double *Wi, const double *Wj, const double *vFrame, const double *Aij,
+                       double gamma, int mfm, double *F, int *iters);
 /* Per-particle smoothing lengths on the current positions (see the .cpp):
  * h_out, neff_out: n doubles each (may be NULL).  Returns the number of
  * particles clamped at kernel_size. */

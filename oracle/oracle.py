@@ -60,6 +60,9 @@ def lib():
         L.orc_riemann_batch.argtypes = [ctypes.c_int] + [dp] * 6 + [ctypes.c_double, dp, dp,
                                                                     ctypes.POINTER(ctypes.c_int)]
         L.orc_riemann_batch.restype = ctypes.c_int
+        L.orc_riemann_fluxes.argtypes = [ctypes.c_int, ctypes.c_int] + [ctypes.c_void_p] * 4 + [
+            ctypes.c_double, ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p]
+        L.orc_riemann_fluxes.restype = ctypes.c_int
         L.orc_smoothing_lengths.restype = ctypes.c_long
         L.orc_smoothing_lengths.argtypes = [ctypes.c_void_p, ctypes.c_double, dp, dp]
         _lib = L
@@ -78,6 +81,21 @@ def riemann_batch(rhoL, uL, pL, rhoR, uR, pR, gamma=5.0 / 3.0, guess=None):
     L.orc_riemann_batch(n, *[dp(a) for a in arrs], gamma, None if g is None else dp(g), dp(ps),
                         it.ctypes.data_as(ctypes.POINTER(ctypes.c_int)))
     return ps, it
+
+
+def riemann_fluxes(Wi, Wj, vframe, aij, gamma=5.0 / 3.0, mfm=False):
+    """Face fluxes of independent Riemann problems (Riemann::Riemann + exact)."""
+    L = lib()
+    Wi = np.ascontiguousarray(Wi, dtype=np.float64)
+    Wj = np.ascontiguousarray(Wj, dtype=np.float64)
+    vframe = np.ascontiguousarray(vframe, dtype=np.float64)
+    aij = np.ascontiguousarray(aij, dtype=np.float64)
+    n, nv = Wi.shape
+    F = np.zeros((n, nv))
+    it = np.zeros(n, dtype=np.int32)
+    st = L.orc_riemann_fluxes(nv - 2, n, Wi.ctypes.data, Wj.ctypes.data, vframe.ctypes.data, aij.ctypes.data,
+                              float(gamma), int(mfm), F.ctypes.data, it.ctypes.data)
+    return F, it, st
 
 
 def _cfg_struct(cfg) -> OrcConfig:

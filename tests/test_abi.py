@@ -8,9 +8,10 @@ from meshlesshydro_gb300 import build, runtime
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 
 
-def declared_functions():
-    text = open(os.path.join(ROOT, "include", "mlh.h")).read()
-    return sorted(set(re.findall(r"\b(mlh_[a-z_0-9]+)\s*\(", text)))
+def declared_functions(header="mlh.h"):
+    text = open(os.path.join(ROOT, "include", header)).read()
+    decl = r"^(?:int|void|double|const char \*)\s*\*?\s*(mlh_[a-z_0-9]+)\s*\("
+    return sorted(set(re.findall(decl, text, flags=re.MULTILINE)))
 
 
 def test_header_and_exports_agree():
@@ -22,6 +23,11 @@ def test_header_and_exports_agree():
         assert hasattr(L, n), n
     assert set(names) == set(runtime.EXPORTS)
     assert L.mlh_abi_version() == 2
+    from meshlesshydro_gb300 import io
+    io_names = declared_functions("mlh_io.h")
+    for n in io_names:
+        assert hasattr(L, n), n
+    assert set(io_names) == set(io.EXPORTS)
 
 
 def test_create_without_gpu_fails_cleanly():
