@@ -183,6 +183,7 @@ Member make_member(const mlh_config &f, double h, const double *lo, const double
     m.h = h;
     m.hsq = h * h;
     m.h2 = h / 2.;
+    m.ih2 = 1. / m.h2;
     const double h2 = m.h2;
     m.sigma = f.dim == 2 ? 10. / (7. * M_PI * h2 * h2) : 1. / (M_PI * h2 * h2 * h2);
     m.w0 = m.sigma * (1. - 3. / 2. * 0. * 0. * (1. - 0. / 2.));

@@ -45,7 +45,7 @@ struct GridInfo {
 // independent simulations stored back to back): its kernel size and the
 // quantities derived from it, its periodic box and its particle range.
 struct Member {
-    double h, hsq, h2, sigma, w0, cfl_h;
+    double h, hsq, h2, ih2, sigma, w0, cfl_h;
     double box_lo[3], box_hi[3];
     float hsq_f;           // conservative single-precision bound for the pre-filter
     int first, count;
@@ -98,15 +98,16 @@ struct Harvest {
 };
 
 // Kernel::cubicSpline, demonstrator/src/Particles.cpp:7-24, for a support
-// radius h: h2 = h / 2 and sigma computed with the reference's expression
-// (kernel_sigma); pow(2-q, 3.) is written as a product.
-__device__ __forceinline__ double kernelW2(double r, double h2, double sigma) {
-    double q = r / h2;
+// radius h: ih2 = 2 / h and sigma computed with the reference's expression
+// (kernel_sigma); q = r / (h/2) is taken as r * (2/h) (within an ulp of the
+// quotient) and pow(2-q, 3.) is written as a product.
+__device__ __forceinline__ double kernelW2(double r, double ih2, double sigma) {
+    double q = r * ih2;
     if (0. <= q && q <= 1.) return sigma * (1. - 3. / 2. * q * q * (1. - q / 2.));
     if (1. < q && q < 2.) { double t = 2. - q; return sigma / 4. * (t * t * t); }
     return 0.;
 }
-__device__ __forceinline__ double kernelW(double r, const Member &mb) { return kernelW2(r, mb.h2, mb.sigma); }
+__device__ __forceinline__ double kernelW(double r, const Member &mb) { return kernelW2(r, mb.ih2, mb.sigma); }
 // Particles.cpp:10-15 (the value of the kernel at r = 0 is sigma)
 template <int D>
 __device__ __forceinline__ double kernel_sigma(double h2) {
@@ -152,6 +153,22 @@ __device__ __forceinline__ double ref_abs(double x, int int_abs) {
     if (t == (int)0x80000000) return -2147483648.0;
     return (double)(t < 0 ? -t : t);
 }
+
+// Order-preserving integer keys of doubles.  On GB300 an FP64 compare or
+// min/max occupies the scarce FP64 pipe like an FMA; comparing these keys on
+// the integer pipe instead gives the same answer for non-NaN operands:
+// ord_key(a) < ord_key(b) exactly when a < b, with -0 and +0 on the same key
+// 0 (so ord_key(x) >= 0 exactly when x >= 0).  The map is its own inverse on
+// keys (key_double), except that -0 comes back as +0.
+__device__ __forceinline__ long long ord_key(double x) {
+    const long long s = __double_as_longlong(x);
+    return s >= 0 ? s : (long long)(0x8000000000000000ull - (unsigned long long)s);
+}
+__device__ __forceinline__ double key_double(long long k) {
+    return __longlong_as_double(k >= 0 ? k : (long long)(0x8000000000000000ull - (unsigned long long)k));
+}
+__device__ __forceinline__ bool dlt(double a, double b) { return ord_key(a) < ord_key(b); }
+__device__ __forceinline__ bool dneg(double x) { return ord_key(x) < 0; }   // x < 0
 
 template <int D>
 __device__ __forceinline__ double dotD(const double *a, const double *b) {

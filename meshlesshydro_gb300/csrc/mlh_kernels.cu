@@ -480,11 +480,12 @@ __global__ void __launch_bounds__(NNS_WARPS * 32) k_neighbours(
         int nr = 0, ni = 0, fc = 0;
         double wsumR = 0., wsumI = 0.;
         const size_t base = (size_t)i * K;
-        double hsq_i = mb.hsq, h2_i = mb.h2, sigma_i = mb.sigma, w0_i = mb.w0;
+        double hsq_i = mb.hsq, ih2_i = mb.ih2, sigma_i = mb.sigma, w0_i = mb.w0;
         if (p.adaptive_h) {
             const double hi_ = p.hp[i];
+            const double h2_i = hi_ / 2.;
             hsq_i = __dmul_rn(hi_, hi_);
-            h2_i = hi_ / 2.;
+            ih2_i = 1. / h2_i;
             sigma_i = kernel_sigma<D>(h2_i);
             w0_i = sigma_i;
         }
@@ -523,7 +524,7 @@ __global__ void __launch_bounds__(NNS_WARPS * 32) k_neighbours(
                     }
                     if (pass) {
                         r = sqrt(d2);
-                        w = kernelW2(r, h2_i, sigma_i);
+                        w = kernelW2(r, ih2_i, sigma_i);
                     }
                 }
             }
@@ -942,9 +943,12 @@ __global__ void __launch_bounds__(256) k_gradients(Params p, const Member *__res
             gradRaw[i] = graw;
         }
         if (p.slope) {
-            double mxN[NF], mnN[NF], mxM[NF], mnM[NF];
+            // running extrema as integer keys (ord_key): the comparisons of
+            // the reference's if (max < f) max = f stay off the FP64 pipe
+            long long mxN[NF], mnN[NF], mxM[NF], mnM[NF];
+            const long long kmin = ord_key(DBL_MIN_), kmax = ord_key(DBL_MAX_);
 #pragma unroll
-            for (int f = 0; f < NF; ++f) { mxN[f] = DBL_MIN_; mnN[f] = DBL_MAX_; mxM[f] = DBL_MIN_; mnM[f] = DBL_MAX_; }
+            for (int f = 0; f < NF; ++f) { mxN[f] = kmin; mnN[f] = kmax; mxM[f] = kmin; mnM[f] = kmax; }
             for (int s = 0; s < tot; ++s) {
                 const uint32_t e = nbr[base + s];
                 const Prim pj = prim[e & IDX_MASK];
@@ -957,18 +961,20 @@ __global__ void __launch_bounds__(256) k_gradients(Params p, const Member *__res
                 }
 #pragma unroll
                 for (int f = 0; f < NF; ++f) {
-                    const double fj = field_of<D>(pj, f);
-                    if (mxN[f] < fj) mxN[f] = fj;
-                    if (mnN[f] > fj) mnN[f] = fj;
-                    const double fij = fi[f] + dotD<D>(gr[f], xijxi);
-                    if (mxM[f] < fij) mxM[f] = fij;
-                    if (mnM[f] > fij) mnM[f] = fij;
+                    const long long kj = ord_key(field_of<D>(pj, f));
+                    if (mxN[f] < kj) mxN[f] = kj;
+                    if (mnN[f] > kj) mnN[f] = kj;
+                    const long long kij = ord_key(fi[f] + dotD<D>(gr[f], xijxi));
+                    if (mxM[f] < kij) mxM[f] = kij;
+                    if (mnM[f] > kij) mnM[f] = kij;
                 }
             }
 #pragma unroll
             for (int f = 0; f < NF; ++f) {
-                double aMax = ref_abs((mxN[f] - fi[f]) / (mxM[f] - fi[f]), p.int_abs);
-                double aMin = ref_abs((fi[f] - mnN[f]) / (fi[f] - mnM[f]), p.int_abs);
+                const double xN = key_double(mxN[f]), nN = key_double(mnN[f]);
+                const double xM = key_double(mxM[f]), nM = key_double(mnM[f]);
+                double aMax = ref_abs((xN - fi[f]) / (xM - fi[f]), p.int_abs);
+                double aMin = ref_abs((fi[f] - nN) / (fi[f] - nM), p.int_abs);
                 if (aMin <= aMax && p.beta * aMin < 1.) {
 #pragma unroll
                     for (int a = 0; a < D; ++a) gr[f][a] *= aMin;
@@ -1050,27 +1056,31 @@ __global__ void __launch_bounds__(256) k_link(Params p, const uint32_t *__restri
 // `ratio` = |x_ij - x_i| / |x_j - x_i|.
 __device__ __forceinline__ double pairwise_limiter(const Params &p, double phi0, double phi_i, double phi_j,
                                                    double ratio) {
-    double phi_ = phi_i;
-    double phi_ij = phi_i + ratio * (phi_j - phi_i);
-    double phiMin, phiMax;
-    if (phi_i < phi_j) { phiMin = phi_i; phiMax = phi_j; }
-    else { phiMin = phi_j; phiMax = phi_i; }
-    double ad = ref_abs(phi_i - phi_j, p.int_abs);
-    double delta1 = p.psi1 * ad;
-    double delta2 = p.psi2 * ad;
-    double phiMinus, phiPlus;
-    if ((phiMax + delta1 >= 0. && phiMax >= 0.) || (phiMax + delta1 < 0. && phiMax < 0.)) phiPlus = phiMax + delta1;
-    else phiPlus = phiMax / (1. + delta1 / ref_abs(phiMax, p.int_abs));
-    if ((phiMin - delta1 >= 0. && phiMin >= 0.) || (phiMin - delta1 < 0. && phiMin < 0.)) phiMinus = phiMin - delta1;
-    else phiMinus = phiMin / (1. + delta1 / ref_abs(phiMin, p.int_abs));
-    if (phi_i < phi_j) {
-        double minPhiD2 = (phi_ij + delta2 < phi0) ? phi_ij + delta2 : phi0;
-        phi_ = phiMinus > minPhiD2 ? phiMinus : minPhiD2;
-    } else if (phi_i > phi_j) {
-        double maxPhiD2 = (phi_ij - delta2 > phi0) ? phi_ij - delta2 : phi0;
-        phi_ = phiPlus < maxPhiD2 ? phiPlus : maxPhiD2;
+    // every comparison on integer keys (ord_key), off the FP64 pipe
+    const long long ki = ord_key(phi_i), kj = ord_key(phi_j);
+    const bool i_lt_j = ki < kj;
+    const double phi_ij = phi_i + ratio * (phi_j - phi_i);
+    const double phiMin = i_lt_j ? phi_i : phi_j, phiMax = i_lt_j ? phi_j : phi_i;
+    const double ad = ref_abs(phi_i - phi_j, p.int_abs);
+    const double delta1 = p.psi1 * ad;
+    const double delta2 = p.psi2 * ad;
+    // (a >= 0 && b >= 0) || (a < 0 && b < 0): a and b on the same side of zero
+    const double up = phiMax + delta1, dn = phiMin - delta1;
+    const double phiPlus = (ord_key(up) >= 0) == (ord_key(phiMax) >= 0)
+                               ? up : phiMax / (1. + delta1 / ref_abs(phiMax, p.int_abs));
+    const double phiMinus = (ord_key(dn) >= 0) == (ord_key(phiMin) >= 0)
+                                ? dn : phiMin / (1. + delta1 / ref_abs(phiMin, p.int_abs));
+    if (i_lt_j) {
+        const double t = phi_ij + delta2;
+        const double minPhiD2 = dlt(t, phi0) ? t : phi0;
+        return dlt(minPhiD2, phiMinus) ? phiMinus : minPhiD2;
     }
-    return phi_;
+    if (kj < ki) {
+        const double t = phi_ij - delta2;
+        const double maxPhiD2 = dlt(phi0, t) ? t : phi0;
+        return dlt(phiPlus, maxPhiD2) ? phiPlus : maxPhiD2;
+    }
+    return phi_i;
 }
 
 // Helper::rotationMatrix2D/3D, demonstrator/src/Helper.cpp:39-77.
@@ -1371,7 +1381,7 @@ __global__ void __launch_bounds__(256) k_faces(Params p, const Member *__restric
                 L[4] -= hdt * (Gj[14] * irj + uj0 * Gj[9] + uj1 * Gj[10] + uj2 * Gj[11]);
             }
         }
-        if (R[1] < 0. || L[1] < 0.) st_local |= ST_NEG_PRESSURE;
+        if (dneg(R[1]) || dneg(L[1])) st_local |= ST_NEG_PRESSURE;
         // --- Riemann problem in the face frame (i left, j right)
         face_frame<D>(A, hatA, Lam, R, L);
         }   // MODE != 2
