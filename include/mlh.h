@@ -238,6 +238,12 @@ void mlh_reset_kernel_times(mlh_ctx *ctx);
  * code); used by bench.py. */
 int mlh_probe_fp64_tflops(double seconds, double *tflops);
 
+/* The reciprocal, quotient and reciprocal square root the kernels use in
+ * place of IEEE division (Newton-Raphson from the hardware estimates), for n
+ * host values: rcp = 1/x, quot = y/x, rsqrt = 1/sqrt(x); for checking their
+ * error against exact values.  No counterpart in the reference. */
+int mlh_probe_fast_math(int n, const double *x, const double *y, double *rcp, double *quot, double *rsqrt);
+
 /* Learned initial guess for the Riemann star pressure (no counterpart in the
  * reference): a 4-64-64-64-1 SiLU MLP, 8705 float parameters laid out as
  * W1[64][4], b1[64], W2[64][64], b2[64], W3[64][64], b3[64], W4[64], b4,

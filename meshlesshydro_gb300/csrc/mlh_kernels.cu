@@ -1095,7 +1095,7 @@ __device__ __forceinline__ void rot3(const double *a, const double *b, double *L
     double v1 = a[2] * b[0] - a[0] * b[2];
     double v2 = a[0] * b[1] - a[1] * b[0];
     double cosAB = ((0. + a[0] * b[0]) + a[1] * b[1]) + a[2] * b[2];
-    double n = 1. / (1. + cosAB);
+    double n = frcp(1. + cosAB);
     L[0] = 1. - n * (v2 * v2 + v1 * v1);
     L[1] = -v2 + n * v0 * v1;
     L[2] = v1 + n * v0 * v2;
@@ -1150,8 +1150,7 @@ __device__ __forceinline__ float4 pstar_features(const double *R, const double *
 template <int D>
 __device__ __forceinline__ void face_frame(const double *A, double *hatA, double *Lam, double *R, double *L) {
     const double unitX[3] = {1., 0., 0.};
-    double AN = sqrt(dotD<D>(A, A));
-    const double iAN = 1. / AN;
+    const double iAN = frsqrt(dotD<D>(A, A));
 #pragma unroll
     for (int a = 0; a < D; ++a) hatA[a] = iAN * A[a];
     if (D == 2) {
@@ -1356,7 +1355,7 @@ __global__ void __launch_bounds__(256) k_faces(Params p, const Member *__restric
             double vjDiv = Gj[3 + 0] + Gj[6 + 1];
             if (D == 3) { viDiv += Gi[9 + 2]; vjDiv += Gj[9 + 2]; }
             const double hdt = dt / 2.;
-            const double iri = 1. / pi.rho, irj = 1. / pj.rho;
+            const double iri = frcp(pi.rho), irj = frcp(pj.rho);
             const double ui0 = vi[0] - vf[0], ui1 = vi[1] - vf[1], uj0 = vj[0] - vf[0], uj1 = vj[1] - vf[1];
             R[0] -= hdt * (pi.rho * viDiv + ui0 * Gi[0] + ui1 * Gi[1]);
             L[0] -= hdt * (pj.rho * vjDiv + uj0 * Gj[0] + uj1 * Gj[1]);

@@ -3,6 +3,7 @@
 // Independent fused multiply-add chains keep the FP64 pipe busy; one FMA
 // counts as two floating-point operations.
 #include "../../include/mlh.h"
+#include "mlh_device.cuh"
 
 #include <cuda_runtime.h>
 
@@ -60,4 +61,40 @@ extern "C" int mlh_probe_fp64_tflops(double seconds, double *tflops) {
     if (cudaGetLastError() != cudaSuccess) return MLH_ERR_CUDA;
     *tflops = best;
     return 0;
+}
+
+namespace {
+
+__global__ void k_fast_math(int n, const double *__restrict__ x, const double *__restrict__ y,
+                            double *__restrict__ rcp, double *__restrict__ quot, double *__restrict__ rsq) {
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        rcp[i] = mlh::frcp(x[i]);
+        quot[i] = mlh::fdiv(y[i], x[i]);
+        rsq[i] = mlh::frsqrt(x[i]);
+    }
+}
+
+}  // namespace
+
+// The library's reciprocal, quotient and reciprocal square root
+// (mlh_device.cuh: frcp, fdiv, frsqrt) of host arrays, for checking them
+// against exact values: rcp = 1/x, quot = y/x, rsqrt = 1/sqrt(x).
+extern "C" int mlh_probe_fast_math(int n, const double *x, const double *y, double *rcp, double *quot,
+                                   double *rsqrt) {
+    if (n < 0 || (n > 0 && (!x || !y || !rcp || !quot || !rsqrt))) return MLH_ERR_INVALID;
+    if (n == 0) return 0;
+    double *d = nullptr;
+    if (cudaMalloc(&d, sizeof(double) * 5 * (size_t)n) != cudaSuccess) return MLH_ERR_CUDA;
+    const size_t b = sizeof(double) * (size_t)n;
+    cudaError_t e = cudaMemcpy(d, x, b, cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = cudaMemcpy(d + n, y, b, cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) {
+        k_fast_math<<<(n + 255) / 256, 256>>>(n, d, d + n, d + 2 * (size_t)n, d + 3 * (size_t)n, d + 4 * (size_t)n);
+        e = cudaGetLastError();
+    }
+    if (e == cudaSuccess) e = cudaMemcpy(rcp, d + 2 * (size_t)n, b, cudaMemcpyDeviceToHost);
+    if (e == cudaSuccess) e = cudaMemcpy(quot, d + 3 * (size_t)n, b, cudaMemcpyDeviceToHost);
+    if (e == cudaSuccess) e = cudaMemcpy(rsqrt, d + 4 * (size_t)n, b, cudaMemcpyDeviceToHost);
+    cudaFree(d);
+    return e == cudaSuccess ? 0 : MLH_ERR_CUDA;
 }

@@ -171,16 +171,24 @@ __device__ inline RiemannResult riemann_exact(const RiemannConsts &c, double rho
 
 // ---------------------------------------------------------------- fast path
 
-// x^(-1/5): single-precision seed (relative error ~1e-7) refined by two
-// Newton steps y <- y + y (1 - x y^5) / 5, whose error contracts as 3 e^2, so
-// the result is within a few ulp of the correctly rounded value.  Values
-// outside the float range go through pow.
+// Comparison of non-negative doubles on the integer pipe: their bit patterns
+// are ordered as the values.
+__device__ __forceinline__ bool nn_le(double a, double b) { return __double_as_longlong(a) <= __double_as_longlong(b); }
+
+// x^(-1/5): single-precision seed (relative error ~1e-7) refined by `steps`
+// Newton steps y <- y + y (1 - x y^5) / 5, whose error contracts as 3 e^2:
+// two steps give a result within a few ulp of the correctly rounded value,
+// one step ~1e-13 relative (enough for an initial guess).  Values outside the
+// float range go through pow.
+template <int STEPS = 2>
 __device__ __forceinline__ double rroot5(double x) {
-    if (!(x > 1e-30 && x < 1e30)) return pow(x, -0.2);
+    // 1e-30 < x < 1e30 on the bit patterns (the test is false for NaN and x <= 0)
+    const long long b = __double_as_longlong(x);
+    if (!(b > 0x39B4484BFEEBC2A0ll && b < 0x46293E5939A08CEAll)) return pow(x, -0.2);
     float xf = (float)x;
     double y = (double)exp2f(-0.2f * __log2f(xf));
 #pragma unroll
-    for (int k = 0; k < 2; ++k) {
+    for (int k = 0; k < STEPS; ++k) {
         double y2 = y * y;
         double y5 = y2 * y2 * y;
         double r = fma(-x, y5, 1.);
@@ -205,7 +213,7 @@ __device__ __forceinline__ double two_rarefaction_guess(const RiemannConsts &k, 
     const double num = cL + cR - k.g7 * (uR - uL);
     if (!(num > 0.)) return -1.;
     if (ROOT5) {
-        const double t = num / (cL * rroot5(pL) + cR * rroot5(pR));
+        const double t = fdiv(num, cL * rroot5<1>(pL) + cR * rroot5<1>(pR));
         const double t2 = t * t;
         return t2 * t2 * t;
     }
@@ -219,9 +227,9 @@ struct RiemannSide {
 __device__ __forceinline__ RiemannSide make_side(const RiemannConsts &k, double rho, double u, double p) {
     RiemannSide s;
     s.rho = rho; s.u = u; s.p = p;
-    const double irho = 1. / rho;
+    const double irho = frcp(rho);
     s.c = sqrt(k.gamma * p * irho);
-    s.invp = 1. / p;
+    s.invp = frcp(p);
     s.C = s.c * k.inv_gamma;     // pK / (rhoK cK) = cK / gamma: f' = (p/pK)^g1 C / p
     s.ak = k.g5 * irho;
     s.bk = k.g6 * p;
@@ -232,13 +240,13 @@ __device__ __forceinline__ RiemannSide make_side(const RiemannConsts &k, double 
 // f_K, f_K' at p (1/p given); q = (p/pK)^g1 on the rarefaction branch
 __device__ __forceinline__ void pressure_fn5(const RiemannSide &s, double p, double invp, double &f, double &fd,
                                              double &q, bool &rare) {
-    if (p <= s.p) {
+    if (nn_le(p, s.p)) {
         q = root5(p * s.invp);
         f = s.g4c * (q - 1.);
         fd = q * s.C * invp;
         rare = true;
     } else {
-        double t = 1. / (s.bk + p);
+        double t = frcp(s.bk + p);
         double qrt = sqrt(s.ak * t);
         f = (p - s.p) * qrt;
         fd = (1. - .5 * (p - s.p) * t) * qrt;
@@ -248,10 +256,12 @@ __device__ __forceinline__ void pressure_fn5(const RiemannSide &s, double p, dou
 }
 
 // Same solution as riemann_exact for gamma = 5/3 with cheaper arithmetic:
-// fifth roots instead of pow, integer powers for g3, g4 and 1/gamma, one
-// reciprocal of p per Newton step, and f_K(p*) from the last Newton
+// fifth roots instead of pow, integer powers for g3, g4 and 1/gamma,
+// reciprocals by Newton-Raphson (frcp), f_K(p*) from the last Newton
 // evaluation plus its derivative times the final (<= tol relative) step,
-// which differs from re-evaluating f at p* by O(tol^2) relative.
+// which differs from re-evaluating f at p* by O(tol^2) relative, and sign
+// and order tests on the integer pipe.  The two-rarefaction guess takes its
+// fifth roots to ~1e-13: it only seeds Newton, whose result is the same.
 __device__ inline RiemannResult riemann_exact5(const RiemannConsts &k, double rhoL, double uL, double pL,
                                                double rhoR, double uR, double pR, double guess = -1.,
                                                double defer_above = 0.) {
@@ -268,8 +278,8 @@ __device__ inline RiemannResult riemann_exact5(const RiemannConsts &k, double rh
     if (tried_guess) p0 = guess;
     else {
         double num = L.c + R.c - k.g7 * du;
-        double den = L.c * rroot5(pL) + R.c * rroot5(pR);
-        double t = num / den;
+        double den = L.c * rroot5<1>(pL) + R.c * rroot5<1>(pR);
+        double t = fdiv(num, den);
         double t2 = t * t;
         p0 = t2 * t2 * t;
         if (defer_above > 0. && p0 > defer_above) {   // see riemann_exact
@@ -284,22 +294,22 @@ __device__ inline RiemannResult riemann_exact5(const RiemannConsts &k, double rh
             if (!tried_guess) break;
             extra = k.max_iter;
             double num = L.c + R.c - k.g7 * du;
-            double den = L.c * rroot5(pL) + R.c * rroot5(pR);
-            double t = num / den;
+            double den = L.c * rroot5<1>(pL) + R.c * rroot5<1>(pR);
+            double t = fdiv(num, den);
             double t2 = t * t;
             p0 = t2 * t2 * t;
         }
         p = p0 > pfloor ? p0 : pfloor;
         for (int it = 1; it <= k.max_iter; ++it) {
-            double invp = 1. / p;
+            double invp = frcp(p);
             double fL, fdL, qL, fR, fdR, qR;
             bool rL, rR;
             pressure_fn5(L, p, invp, fL, fdL, qL, rL);
             pressure_fn5(R, p, invp, fR, fdR, qR, rR);
-            double pnew = p - (fL + fR + du) / (fdL + fdR);
+            double pnew = p - (fL + fR + du) * frcp(fdL + fdR);
             if (!(pnew > 0.)) pnew = pfloor;
             double dp = pnew - p;
-            if (2. * fabs(dp) <= k.tol * (pnew + p)) {
+            if (nn_le(2. * fabs(dp), k.tol * (pnew + p))) {
                 fLs = fL + fdL * dp;
                 fRs = fR + fdR * dp;
                 double rel = dp * invp;
@@ -315,7 +325,7 @@ __device__ inline RiemannResult riemann_exact5(const RiemannConsts &k, double rh
     const double pstar = p;
     res.pstar = pstar;
     if (iters < 0) {
-        double invp = 1. / pstar, fdL, fdR, qL, qR;
+        double invp = frcp(pstar), fdL, fdR, qL, qR;
         bool rL, rR;
         pressure_fn5(L, pstar, invp, fLs, fdL, qL, rL);
         pressure_fn5(R, pstar, invp, fRs, fdR, qR, rR);
@@ -327,43 +337,43 @@ __device__ inline RiemannResult riemann_exact5(const RiemannConsts &k, double rh
     }
     const double ustar = .5 * (uL + uR) + .5 * (fRs - fLs);
     double rho, u, pp;
-    if (0. <= ustar) {
-        if (pstar <= pL) {
+    if (!dneg(ustar)) {
+        if (nn_le(pstar, pL)) {
             double shl = uL - L.c;
-            if (0. <= shl) { rho = rhoL; u = uL; pp = pL; }
+            if (!dneg(shl)) { rho = rhoL; u = uL; pp = pL; }
             else {
                 double q = qLs >= 0. ? qLs : root5(pstar * L.invp);
                 double stl = ustar - L.c * q;
-                if (0. > stl) { rho = rhoL * (q * q * q); u = ustar; pp = pstar; }
+                if (dneg(stl)) { rho = rhoL * (q * q * q); u = ustar; pp = pstar; }
                 else {
                     double cf = k.g5 * (L.c + k.g7 * uL);
-                    double r = cf / L.c, r3 = r * r * r;
+                    double r = fdiv(cf, L.c), r3 = r * r * r;
                     u = cf; rho = rhoL * r3; pp = pL * (r3 * r * r);
                 }
             }
         } else {
             double pml = pstar * L.invp;
             double sl = uL - L.c * sqrt(k.g2 * pml + k.g1);
-            if (0. <= sl) { rho = rhoL; u = uL; pp = pL; }
-            else { rho = rhoL * (pml + k.g6) / (pml * k.g6 + 1.); u = ustar; pp = pstar; }
+            if (!dneg(sl)) { rho = rhoL; u = uL; pp = pL; }
+            else { rho = rhoL * fdiv(pml + k.g6, pml * k.g6 + 1.); u = ustar; pp = pstar; }
         }
         res.flag = -1;
     } else {
-        if (pstar > pR) {
+        if (!nn_le(pstar, pR)) {
             double pmr = pstar * R.invp;
             double sr = uR + R.c * sqrt(k.g2 * pmr + k.g1);
-            if (0. >= sr) { rho = rhoR; u = uR; pp = pR; }
-            else { rho = rhoR * (pmr + k.g6) / (pmr * k.g6 + 1.); u = ustar; pp = pstar; }
+            if (ord_key(sr) <= 0) { rho = rhoR; u = uR; pp = pR; }
+            else { rho = rhoR * fdiv(pmr + k.g6, pmr * k.g6 + 1.); u = ustar; pp = pstar; }
         } else {
             double shr = uR + R.c;
-            if (0. >= shr) { rho = rhoR; u = uR; pp = pR; }
+            if (ord_key(shr) <= 0) { rho = rhoR; u = uR; pp = pR; }
             else {
                 double q = qRs >= 0. ? qRs : root5(pstar * R.invp);
                 double str = ustar + R.c * q;
-                if (0. <= str) { rho = rhoR * (q * q * q); u = ustar; pp = pstar; }
+                if (!dneg(str)) { rho = rhoR * (q * q * q); u = ustar; pp = pstar; }
                 else {
                     double cf = k.g5 * (R.c - k.g7 * uR);
-                    double r = cf / R.c, r3 = r * r * r;
+                    double r = fdiv(cf, R.c), r3 = r * r * r;
                     u = -cf; rho = rhoR * r3; pp = pR * (r3 * r * r);
                 }
             }

@@ -64,7 +64,8 @@ EXPORTS = ["mlh_abi_version", "mlh_last_error", "mlh_create", "mlh_destroy", "ml
            "mlh_kernel_times", "mlh_reset_kernel_times", "mlh_probe_fp64_tflops",
            "mlh_grid_bounds_noalloc", "mlh_ensemble_create", "mlh_member_times", "mlh_set_graph_mode",
            "mlh_autotune", "mlh_set_tuning", "mlh_pstar_infer", "mlh_pstar_grad", "mlh_pstar_train", "mlh_set_pstar_weights",
-           "mlh_pstar_harvest", "mlh_smoothing_lengths", "mlh_prepare", "mlh_riemann_fluxes"]
+           "mlh_pstar_harvest", "mlh_smoothing_lengths", "mlh_prepare", "mlh_riemann_fluxes",
+           "mlh_probe_fast_math"]
 
 _lib = None
 
@@ -134,6 +135,8 @@ def load(path: str = LIB_PATH):
     L.mlh_prepare.restype = ctypes.c_int
     L.mlh_riemann_fluxes.argtypes = [ctypes.c_int, ctypes.c_int] + [dp] * 4 + [ctypes.c_double, ctypes.c_int, dp, dp]
     L.mlh_riemann_fluxes.restype = ctypes.c_int
+    L.mlh_probe_fast_math.argtypes = [ctypes.c_int] + [dp] * 5
+    L.mlh_probe_fast_math.restype = ctypes.c_int
     _lib = L
     return L
 
