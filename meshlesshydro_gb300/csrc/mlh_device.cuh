@@ -102,9 +102,12 @@ struct Harvest {
 // (kernel_sigma); q = r / (h/2) is taken as r * (2/h) (within an ulp of the
 // quotient) and pow(2-q, 3.) is written as a product.
 __device__ __forceinline__ double kernelW2(double r, double ih2, double sigma) {
-    double q = r * ih2;
-    if (0. <= q && q <= 1.) return sigma * (1. - 3. / 2. * q * q * (1. - q / 2.));
-    if (1. < q && q < 2.) { double t = 2. - q; return sigma / 4. * (t * t * t); }
+    // r >= 0, so q >= 0 and the range tests compare bit patterns (integer
+    // pipe): q <= 1 and q < 2
+    const double q = r * ih2;
+    const long long qb = __double_as_longlong(q);
+    if (qb <= 0x3FF0000000000000ll) return sigma * (1. - 3. / 2. * q * q * (1. - q / 2.));
+    if (qb < 0x4000000000000000ll) { double t = 2. - q; return sigma / 4. * (t * t * t); }
     return 0.;
 }
 __device__ __forceinline__ double kernelW(double r, const Member &mb) { return kernelW2(r, mb.ih2, mb.sigma); }

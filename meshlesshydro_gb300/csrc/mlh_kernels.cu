@@ -516,12 +516,14 @@ __global__ void __launch_bounds__(NNS_WARPS * 32) k_neighbours(
                     double ex = __dsub_rn(xj[0], xi[0]), ey = __dsub_rn(xj[1], xi[1]);
                     double d2 = __dadd_rn(__dmul_rn(ex, ex), __dmul_rn(ey, ey));
                     if (D == 3) { double ez = __dsub_rn(xj[2], xi[2]); d2 = __dadd_rn(d2, __dmul_rn(ez, ez)); }
+                    // d2, h^2 >= 0: compared as bit patterns on the integer pipe
+                    double lim = mb.hsq;
                     if (p.adaptive_h) {
                         const double hj = p.hp[j];
-                        pass = d2 < fmax(hsq_i, __dmul_rn(hj, hj));
-                    } else {
-                        pass = d2 < mb.hsq;
+                        const double hsq_j = __dmul_rn(hj, hj);
+                        lim = __double_as_longlong(hsq_i) < __double_as_longlong(hsq_j) ? hsq_j : hsq_i;
                     }
+                    pass = __double_as_longlong(d2) < __double_as_longlong(lim);
                     if (pass) {
                         r = sqrt(d2);
                         w = kernelW2(r, ih2_i, sigma_i);
@@ -777,9 +779,9 @@ __global__ void __launch_bounds__(256) k_timestep(Params p, const Member *__rest
                 // min(0, v_ij . x_ij / r): the quotient is needed only when the
                 // dot product is negative (same value and sign as the reference's)
                 const double dv = dotD<D>(vij, xij);
-                const double vijxij = dv < 0. ? dv / rr[base + s] : 0.;
+                const double vijxij = dneg(dv) ? fdiv(dv, rr[base + s]) : 0.;
                 double vs = ci + cj - vijxij;
-                vSig = vs > vSig ? vs : vSig;
+                vSig = dlt(vSig, vs) ? vs : vSig;
             }
             dti = (p.adaptive_h ? p.cfl * p.hp[i] : members[mi].cfl_h) / vSig;
         }
@@ -887,13 +889,13 @@ __global__ void __launch_bounds__(256) k_gradients(Params p, const Member *__res
             double xj[3];
             neighbour_pos<D>(e, pj, g, h, xj);
             const double psij = ww[base + s] * Vi;
-            double d[3];
+            double d[3], dp[3];
 #pragma unroll
-            for (int a = 0; a < D; ++a) d[a] = xj[a] - xi[a];
+            for (int a = 0; a < D; ++a) { d[a] = xj[a] - xi[a]; dp[a] = d[a] * psij; }
 #pragma unroll
             for (int a = 0; a < D; ++a)
 #pragma unroll
-                for (int b = a; b < D; ++b) E[D * a + b] += d[a] * d[b] * psij;
+                for (int b = a; b < D; ++b) E[D * a + b] = fma(d[a], dp[b], E[D * a + b]);
         }
 #pragma unroll
         for (int a = 0; a < D; ++a)
@@ -915,10 +917,10 @@ __global__ void __launch_bounds__(256) k_gradients(Params p, const Member *__res
             for (int a = 0; a < D; ++a) d[a] = xj[a] - xi[a];
 #pragma unroll
             for (int a = 0; a < D; ++a) {
-                double t = 0.;
+                double t = E[D * a] * d[0];
 #pragma unroll
-                for (int b = 0; b < D; ++b) t += E[D * a + b] * d[b] * psij;
-                ps[a] = t;
+                for (int b = 1; b < D; ++b) t = fma(E[D * a + b], d[b], t);
+                ps[a] = t * psij;
             }
             // psi~_j(x_i) of this slot, reused by the face kernel for A_ij
             double *po = psiOut + (base + s) * 3;
@@ -952,19 +954,22 @@ __global__ void __launch_bounds__(256) k_gradients(Params p, const Member *__res
             for (int s = 0; s < tot; ++s) {
                 const uint32_t e = nbr[base + s];
                 const Prim pj = prim[e & IDX_MASK];
-                double xj[3], xijxi[3];
+                double xj[3], d[3];
                 neighbour_pos<D>(e, pj, g, h, xj);
+                // face point x_ij = x_i + c (x_j - x_i): c = 1/2 (first-order
+                // quadrature point) or h/4 (the reference's other choice)
+                const double cq = p.foqp ? .5 : hq / 4.;
 #pragma unroll
-                for (int a = 0; a < D; ++a) {
-                    double xij = p.foqp ? (xi[a] + xj[a]) / 2. : xi[a] + hq / 4. * (xj[a] - xi[a]);
-                    xijxi[a] = xij - xi[a];
-                }
+                for (int a = 0; a < D; ++a) d[a] = xj[a] - xi[a];
 #pragma unroll
                 for (int f = 0; f < NF; ++f) {
                     const long long kj = ord_key(field_of<D>(pj, f));
                     if (mxN[f] < kj) mxN[f] = kj;
                     if (mnN[f] > kj) mnN[f] = kj;
-                    const long long kij = ord_key(fi[f] + dotD<D>(gr[f], xijxi));
+                    double gd = gr[f][0] * d[0];
+#pragma unroll
+                    for (int a = 1; a < D; ++a) gd = fma(gr[f][a], d[a], gd);
+                    const long long kij = ord_key(fma(cq, gd, fi[f]));
                     if (mxM[f] < kij) mxM[f] = kij;
                     if (mnM[f] > kij) mnM[f] = kij;
                 }
