@@ -68,6 +68,7 @@ struct mlh_ctx {
     uint32_t *nbr = nullptr;
     double *rr = nullptr, *ww = nullptr, *psi = nullptr;
     size_t faces_cap = 0;
+    size_t queue_cap = 0;
     int *noi = nullptr, *noiImg = nullptr, *faceCnt = nullptr, *faceOff = nullptr, *faceOf = nullptr;
     FaceRef *faces = nullptr;
     double *Fface = nullptr;
@@ -131,12 +132,17 @@ int alloc_neighbour_buffers(mlh_ctx *c) {
     CK(dalloc(&c->faceOf, slots));
     CK(dalloc(&c->faces, faces));
     CK(dalloc(&c->Fface, faces * 6));
+    // queue of faces for a second face pass: every face with the learned
+    // guess; in the plain step the faces Newton has not finished after one
+    // step (a fifth to two thirds of them; faces_cap is about twice the faces
+    // of a step; a full queue finishes its faces in the first pass)
+    c->queue_cap = c->learned ? faces : faces / 2 + 1024;
+    CK(dalloc(&c->fstate, c->queue_cap));
+    CK(dalloc(&c->queueFace, c->queue_cap));
+    CK(dalloc(&c->queueCount, 1));
     if (c->learned) {
-        CK(dalloc(&c->fstate, faces));
         CK(dalloc(&c->feat, faces));
         CK(dalloc(&c->yguess, faces));
-        CK(dalloc(&c->queueFace, faces));
-        CK(dalloc(&c->queueCount, 1));
     }
     return 0;
 }
@@ -229,6 +235,7 @@ StepArgs make_args(mlh_ctx *c, double dt_max) {
     a.sm_count = c->sm_count;
     a.faces_cap = c->faces_cap;
     a.p.faces_cap = c->faces_cap > 0x7fffffff ? 0x7fffffff : (int)c->faces_cap;
+    a.p.queue_cap = c->queue_cap > 0x7fffffff ? 0x7fffffff : (int)c->queue_cap;
     a.root5 = make_riemann_consts(c->p.gamma, c->p.rtol, c->p.rmaxit).root5;
     a.dt_max = dt_max;
     a.x = c->x; a.y = c->y; a.z = c->z; a.vx = c->vx; a.vy = c->vy; a.vz = c->vz; a.m = c->m; a.u = c->u;

@@ -57,6 +57,7 @@ struct Params {
     int K;                 // neighbour slots per particle
     int ncells_cap;
     int faces_cap;         // capacity of the face arrays
+    int queue_cap;         // capacity of the queue of faces for a second face pass
     double h, hsq, h2, sigma, w0, gamma, cfl_h, beta, psi1, psi2, rtol, time_step;
     double box_lo[3], box_hi[3];
     float hsq_f;           // conservative single-precision bound for the pre-filter

@@ -1149,6 +1149,13 @@ __device__ __forceinline__ float4 pstar_features(const double *R, const double *
 // MODE 0.  MODE 2 (second pass, over the queue): reload the state, solve from
 // the network's guess, project the flux.  `harvest` (MODE 0) records network
 // inputs and targets log(p*/p_TR) of every `stride`-th face.
+// MODE 3 (plain first pass, gamma = 5/3): one Newton step from the
+// two-rarefaction guess; faces that have not converged are queued with their
+// iterate, so that the warps of this pass do not all run the second step that
+// a fifth of the faces need (nearly every warp holds one).  MODE 4 (second
+// pass over that queue): continue Newton from the stored iterate, which is the
+// same iteration with the same arithmetic, densely packed.  A full queue
+// keeps the face in MODE 3 and finishes it there.
 // Helper::rotationMatrix2D/3D(hatA, unitX) applied to the velocities of both
 // states (Riemann::Riemann, demonstrator/src/Riemann.cpp:7-81): hatA = A/|A|,
 // Lam the rotation taking hatA to the x axis.
@@ -1237,18 +1244,22 @@ __global__ void __launch_bounds__(256) k_faces(Params p, const Member *__restric
                                                int *__restrict__ queueFace, int *__restrict__ queueCount, Harvest hv) {
     constexpr int NV = D + 2;
     int nf = *faceTotal < p.faces_cap ? *faceTotal : p.faces_cap;
-    if (MODE == 2) nf = *queueCount < nf ? *queueCount : nf;
+    constexpr bool QUEUED = MODE == 2 || MODE == 4;   // passes over the queue
+    if (QUEUED) {   // the queue holds min(count, capacity) faces; MODE 3 finished the rest itself
+        const int qn = *queueCount < p.queue_cap ? *queueCount : p.queue_cap;
+        nf = qn < nf ? qn : nf;
+    }
     const RiemannConsts rc = make_riemann_consts(p.gamma, p.rtol, p.rmaxit);
     const double gamma = p.gamma;
     unsigned long long iters_local = 0, fallback_local = 0, deferred_local = 0;
     unsigned st_local = 0;
     for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < nf; t += gridDim.x * blockDim.x) {
         // MODE 2 walks the queue: t is the queue position, f the face
-        const int f = MODE == 2 ? queueFace[t] : t;
+        const int f = QUEUED ? queueFace[t] : t;
         double R[5], L[5], A[3] = {0., 0., 0.}, vf[3] = {0., 0., 0.}, hatA[3] = {0., 0., 0.}, Lam[9];
         const double unitX[3] = {1., 0., 0.};
-        double ptr_q = -1.;   // MODE 2: two-rarefaction guess found in MODE 1
-        if (MODE == 2) {
+        double ptr_q = -1.;   // MODE 2: two-rarefaction guess found in MODE 1; MODE 4: Newton iterate
+        if (QUEUED) {
             const FaceState &fs = fstate[t];
             ptr_q = fs.v[19];
 #pragma unroll
@@ -1388,17 +1399,37 @@ __global__ void __launch_bounds__(256) k_faces(Params p, const Member *__restric
         if (dneg(R[1]) || dneg(L[1])) st_local |= ST_NEG_PRESSURE;
         // --- Riemann problem in the face frame (i left, j right)
         face_frame<D>(A, hatA, Lam, R, L);
-        }   // MODE != 2
+        }   // !QUEUED
         double guess = -1.;
         if (MODE == 2) {
             const float y = yguess[t];
             if (isfinite(y) && fabsf(y) > PSTAR_GATE && fabsf(y) < 30.f)
                 guess = ptr_q * (double)__expf(y);
         }
+        if (MODE == 4) guess = ptr_q;
         // MODE 1 defers faces whose two-rarefaction guess says strong shock
         const double defer = MODE == 1 ? PSTAR_HARD * fmin(R[1], L[1]) : 0.;
-        RiemannResult rs = ROOT5 ? riemann_exact5(rc, R[0], R[2], R[1], L[0], L[2], L[1], guess, defer)
+        RiemannResult rs = ROOT5 ? riemann_exact5(rc, R[0], R[2], R[1], L[0], L[2], L[1], guess, defer,
+                                                  MODE == 3 ? 1 : 0)
                                  : riemann_exact(rc, R[0], R[2], R[1], L[0], L[2], L[1], guess, defer);
+        if (MODE == 3 && rs.flag == 2) {
+            const int q = atomicAdd(queueCount, 1);
+            if (q < p.queue_cap) {
+                FaceState &fs = fstate[q];
+#pragma unroll
+                for (int k = 0; k < 5; ++k) { fs.v[k] = R[k]; fs.v[5 + k] = L[k]; }
+#pragma unroll
+                for (int a = 0; a < 3; ++a) { fs.v[10 + a] = A[a]; fs.v[13 + a] = vf[a]; fs.v[16 + a] = hatA[a]; }
+                fs.v[19] = rs.pstar;   // the Newton iterate
+                queueFace[q] = f;
+                iters_local += (unsigned long long)rs.iters;
+                continue;
+            }
+            // queue full: continue here
+            const int done = rs.iters;
+            rs = riemann_exact5(rc, R[0], R[2], R[1], L[0], L[2], L[1], rs.pstar, 0.);
+            if (rs.iters >= 0) rs.iters += done;
+        }
         if (MODE == 1 && rs.flag == 2) {
             const int q = atomicAdd(queueCount, 1);   // < faces on this step <= faces_cap
             FaceState &fs = fstate[q];
@@ -1697,6 +1728,11 @@ void launch_step(StepArgs &a) {
         if (a.root5) MLH_FACES(true, 1); else MLH_FACES(false, 1);
         pstar_infer_dev(a.feat, a.queueCount, (int)a.faces_cap, a.mlp_packed, a.yguess, a.sm_count, s);
         if (a.root5) MLH_FACES(true, 2); else MLH_FACES(false, 2);
+    } else if (a.root5 && a.fstate && a.harvest.stride == 0) {
+        // unconverged faces after one Newton step go to a second, dense pass
+        cudaMemsetAsync(a.queueCount, 0, sizeof(int), s);
+        MLH_FACES(true, 3);
+        MLH_FACES(true, 4);
     } else {
         if (a.root5) MLH_FACES(true, 0); else MLH_FACES(false, 0);
     }

@@ -262,9 +262,13 @@ __device__ __forceinline__ void pressure_fn5(const RiemannSide &s, double p, dou
 // which differs from re-evaluating f at p* by O(tol^2) relative, and sign
 // and order tests on the integer pipe.  The two-rarefaction guess takes its
 // fifth roots to ~1e-13: it only seeds Newton, whose result is the same.
+// first_iters > 0: when Newton from the two-rarefaction guess has not
+// converged after that many steps, return unsolved (flag 2, pstar = the
+// current iterate, iters = steps run); solving again with that iterate as
+// `guess` continues the same iteration with the same arithmetic.
 __device__ inline RiemannResult riemann_exact5(const RiemannConsts &k, double rhoL, double uL, double pL,
                                                double rhoR, double uR, double pR, double guess = -1.,
-                                               double defer_above = 0.) {
+                                               double defer_above = 0., int first_iters = 0) {
     RiemannResult res;
     const RiemannSide L = make_side(k, rhoL, uL, pL), R = make_side(k, rhoR, uR, pR);
     if (k.g4 * (L.c + R.c) <= uR - uL) {
@@ -320,6 +324,10 @@ __device__ inline RiemannResult riemann_exact5(const RiemannConsts &k, double rh
                 break;
             }
             p = pnew;
+            if (first_iters > 0 && !tried_guess && it >= first_iters) {
+                res.rho = 0.; res.u = 0.; res.p = 0.; res.pstar = p; res.flag = 2; res.iters = it;
+                return res;
+            }
         }
     }
     const double pstar = p;
