@@ -112,6 +112,8 @@ struct mlh_ctx {
 
 namespace {
 
+int round_slots(int k) { return (k + 3) & ~3; }
+
 void free_neighbour_buffers(mlh_ctx *c) {
     cudaFree(c->nbr); cudaFree(c->rr); cudaFree(c->ww); cudaFree(c->psi); cudaFree(c->faceOf); cudaFree(c->faces);
     cudaFree(c->Fface);
@@ -375,7 +377,9 @@ static int create_impl(const mlh_config *cfg, int nmembers, const mlh_member *md
     cudaGetDevice(&c->device);
     cudaDeviceGetAttribute(&c->sm_count, cudaDevAttrMultiProcessorCount, c->device);
     fill_params(c);
-    c->p.K = cfg->max_neighbours > 0 ? cfg->max_neighbours : (cfg->dim == 2 ? 40 : 64);
+    // slots per particle: a multiple of 4, so that every particle's list
+    // starts on a 16-byte boundary (read as uint4 by k_link)
+    c->p.K = round_slots(cfg->max_neighbours > 0 ? cfg->max_neighbours : (cfg->dim == 2 ? 40 : 64));
     long long nc = 0;
     for (const Member &mb : mem) nc += estimate_cells(*cfg, init, mb);
     if (nc > (1ll << 30)) { delete c; g_last_error = "grid too large"; return MLH_ERR_CAPACITY; }
@@ -451,7 +455,7 @@ static void drop_graph(mlh_ctx *c) {
 static int grow_buffers(mlh_ctx *c, unsigned st) {
     if (st & MLH_ERR_NGB_OVERFLOW) {
         free_neighbour_buffers(c);
-        c->p.K = c->p.K + c->p.K / 2;
+        c->p.K = round_slots(c->p.K + c->p.K / 2);
         if (int rc = alloc_neighbour_buffers(c)) return rc;
     }
     if (st & ST_CAPACITY) {

@@ -1034,19 +1034,28 @@ __global__ void __launch_bounds__(256) k_link(Params p, const uint32_t *__restri
                 faces[fid].slot = s;
                 continue;
             }
-            // search j's list (real part or image part) for i
+            // search j's list (real part or image part) for i, counting on
+            // the way j's canonical slots before it (the face's rank); the
+            // list is read 4 entries at a time (K is a multiple of 4)
             const bool img = s >= nr;
-            const size_t jb = (size_t)j * p.K;
+            const uint4 *lst = reinterpret_cast<const uint4 *>(nbr + (size_t)j * p.K);
             const int jnr = noi[j];
             const int b = img ? jnr : 0, en = img ? jnr + noiImg[j] : jnr;
-            int found = -1;
-            for (int t = b; t < en; ++t)
-                if ((int)(nbr[jb + t] & IDX_MASK) == i) { found = t; break; }
+            int found = -1, crank = 0;
+            for (int t4 = 0; t4 * 4 < en && found < 0; ++t4) {
+                const uint4 q = lst[t4];
+                const uint32_t v[4] = {q.x, q.y, q.z, q.w};
+#pragma unroll
+                for (int k = 0; k < 4; ++k) {
+                    const int t = t4 * 4 + k;
+                    const int idx = (int)(v[k] & IDX_MASK);
+                    if (found < 0 && t < en) {
+                        if (t >= b && idx == i) found = t;
+                        else crank += idx > j;
+                    }
+                }
+            }
             if (found < 0) { flag(status, ST_ASYMMETRIC); faceOf[base + s] = 0; continue; }
-            // rank of slot `found` among j's canonical slots
-            int crank = 0;
-            for (int t = 0; t < found; ++t)
-                if ((int)(nbr[jb + t] & IDX_MASK) > j) ++crank;
             const int fid = faceOff[j] + crank;
             if (fid >= p.faces_cap) { flag(status, ST_CAPACITY); faceOf[base + s] = 0; continue; }
             faceOf[base + s] = -(fid + 1);
