@@ -1097,31 +1097,8 @@ __device__ __forceinline__ double pairwise_limiter(const Params &p, double phi0,
     return phi_i;
 }
 
-// Helper::rotationMatrix2D/3D, demonstrator/src/Helper.cpp:39-77.
-__device__ __forceinline__ void rot2(const double *a, const double *b, double *L) {
-    L[0] = a[0] * b[0] + a[1] * b[1];
-    L[1] = -(a[0] * b[1] - a[1] * b[0]);
-    L[2] = -L[1];
-    L[3] = L[0];
-}
-__device__ __forceinline__ void rot3(const double *a, const double *b, double *L) {
-    double v0 = a[1] * b[2] - a[2] * b[1];
-    double v1 = a[2] * b[0] - a[0] * b[2];
-    double v2 = a[0] * b[1] - a[1] * b[0];
-    double cosAB = ((0. + a[0] * b[0]) + a[1] * b[1]) + a[2] * b[2];
-    double n = frcp(1. + cosAB);
-    L[0] = 1. - n * (v2 * v2 + v1 * v1);
-    L[1] = -v2 + n * v0 * v1;
-    L[2] = v1 + n * v0 * v2;
-    L[3] = v2 + n * v0 * v1;
-    L[4] = 1. - n * (v2 * v2 + v0 * v0);
-    L[5] = -v0 + n * v1 * v2;
-    L[6] = -v1 + n * v0 * v2;
-    L[7] = v0 + n * v1 * v2;
-    L[8] = 1. - n * (v1 * v1 + v0 * v0);
-}
-
-// Network inputs of a face from its face-frame states (left = particle i):
+// Network inputs of a face from its face-frame states (left = particle i,
+// un the velocity components along the face normal):
 // log(rhoR/rhoL), (uR - uL)/cL, log(pR/pL), log(cR/cL).
 // The network predicts y = log(p* / p_TR), p_TR the two-rarefaction guess of
 // the face.  p_TR is exact when both waves are rarefactions and its error grows
@@ -1134,25 +1111,25 @@ __device__ __forceinline__ void rot3(const double *a, const double *b, double *L
 constexpr double PSTAR_HARD = 2.0;
 constexpr float PSTAR_GATE = 0.01f;
 
-__device__ __forceinline__ float4 pstar_features(const double *R, const double *L, double gamma) {
+__device__ __forceinline__ float4 pstar_features(const double *R, const double *L, double unR, double unL,
+                                                double gamma) {
     const float rl = (float)R[0], rr = (float)L[0], pl = (float)R[1], pr = (float)L[1];
     const float cl = sqrtf((float)gamma * pl / rl), cr = sqrtf((float)gamma * pr / rr);
-    return make_float4(logf(rr / rl), (float)(L[2] - R[2]) / cl, logf(pr / pl), logf(cr / cl));
+    return make_float4(logf(rr / rl), (float)(unL - unR) / cl, logf(pr / pl), logf(cr / cl));
 }
 
 // One canonical face (i < j): effective face A_ij = psi~_j(x_i)/omega_i -
 // psi~_i(x_j)/omega_j from the psi~ of both slots (compEffectiveFace,
 // Particles.cpp:1290-1311, 2504-2531); boosted, reconstructed, optionally
 // pairwise-limited and half-step-predicted states (compRiemannStatesLR,
-// :1488-1733 / 2533-2683, including the vz[i] of :1717,1719); rotation to the
-// face frame, exact solve with i as the left state, rotation back and
-// projection on A_ij (Riemann::Riemann/exact/rotateAndProjectFluxes2D/3D,
-// demonstrator/src/Riemann.cpp:7-229).  The back rotation of
-// Helper::rotationMatrix2D/3D(unitX, hatA) is the transpose of the forward
-// one, bit for bit, so it is not recomputed.  Output slot order:
-// [mass, energy, px, py, pz].
+// :1488-1733 / 2533-2683, including the vz[i] of :1717,1719); the face-frame
+// problem (normal velocity components, face_normal), exact solve with i as
+// the left state, back to the lab frame and projection on A_ij
+// (Riemann::Riemann/exact/rotateAndProjectFluxes2D/3D,
+// demonstrator/src/Riemann.cpp:7-229; project_flux says why no rotation
+// matrix is needed).  Output slot order: [mass, energy, px, py, pz].
 // MODE 0: the whole face.  MODE 1 (learned guess, first pass): faces with a
-// strong shock in p_TR stop after the rotation into the face frame and are
+// strong shock in p_TR stop before the exact solve and are
 // queued (state and network inputs at the queue position, order immaterial:
 // each face writes only its own flux); all other faces are finished as in
 // MODE 0.  MODE 2 (second pass, over the queue): reload the state, solve from
@@ -1165,55 +1142,50 @@ __device__ __forceinline__ float4 pstar_features(const double *R, const double *
 // pass over that queue): continue Newton from the stored iterate, which is the
 // same iteration with the same arithmetic, densely packed.  A full queue
 // keeps the face in MODE 3 and finishes it there.
-// Helper::rotationMatrix2D/3D(hatA, unitX) applied to the velocities of both
-// states (Riemann::Riemann, demonstrator/src/Riemann.cpp:7-81): hatA = A/|A|,
-// Lam the rotation taking hatA to the x axis.
+// Riemann::Riemann (demonstrator/src/Riemann.cpp:7-81) rotates both states
+// with Helper::rotationMatrix2D/3D(hatA, unitX) (Helper.cpp:39-77), hatA =
+// A/|A|.  The one-dimensional problem reads only the first rotated velocity
+// component, and the first row of that rotation is hatA: u = hatA . v.  The
+// velocities themselves stay unrotated (see project_flux).
 template <int D>
-__device__ __forceinline__ void face_frame(const double *A, double *hatA, double *Lam, double *R, double *L) {
-    const double unitX[3] = {1., 0., 0.};
+__device__ __forceinline__ void face_normal(const double *A, const double *R, const double *L, double *hatA,
+                                            double &unR, double &unL) {
     const double iAN = frsqrt(dotD<D>(A, A));
 #pragma unroll
     for (int a = 0; a < D; ++a) hatA[a] = iAN * A[a];
-    if (D == 2) {
-        rot2(hatA, unitX, Lam);
-        double bR0 = L[2], bR1 = L[3], bL0 = R[2], bL1 = R[3];
-        L[2] = Lam[0] * bR0 + Lam[1] * bR1;
-        L[3] = Lam[2] * bR0 + Lam[3] * bR1;
-        R[2] = Lam[0] * bL0 + Lam[1] * bL1;
-        R[3] = Lam[2] * bL0 + Lam[3] * bL1;
-    } else {
-        rot3(hatA, unitX, Lam);
-        double bR0 = L[2], bR1 = L[3], bR2 = L[4], bL0 = R[2], bL1 = R[3], bL2 = R[4];
-        L[2] = Lam[0] * bR0 + Lam[1] * bR1 + Lam[2] * bR2;
-        L[3] = Lam[3] * bR0 + Lam[4] * bR1 + Lam[5] * bR2;
-        L[4] = Lam[6] * bR0 + Lam[7] * bR1 + Lam[8] * bR2;
-        R[2] = Lam[0] * bL0 + Lam[1] * bL1 + Lam[2] * bL2;
-        R[3] = Lam[3] * bL0 + Lam[4] * bL1 + Lam[5] * bL2;
-        R[4] = Lam[6] * bL0 + Lam[7] * bL1 + Lam[8] * bL2;
-    }
+    unR = dotD<D>(hatA, R + 2);
+    unL = dotD<D>(hatA, L + 2);
 }
 
 // Riemann::exact after the solve and rotateAndProjectFluxes2D/3D
-// (demonstrator/src/Riemann.cpp:100-229): tangential velocity from the
-// sampled side, back rotation (the transpose of Lam), boost by the frame
-// velocity and projection on A_ij.  Fo: [mass, energy, px, py, pz].  Returns
-// ST_VACUUM when the solution is vacuum, else 0.
+// (demonstrator/src/Riemann.cpp:100-229): the sampled velocity takes its
+// tangential components from the sampled side, is rotated back and boosted by
+// the frame velocity, and the flux is projected on A_ij.  Rotating a state
+// into the face frame, replacing its normal component by u* and rotating back
+// leaves its tangential part unchanged, so v* = v_side + (u* - u_side) hatA
+// (u* hatA for vacuum), without the rotation matrices.  R (particle i, the
+// left state) and L: [rho, P, v..] with unrotated velocities, unR/unL their
+// normal components.  Fo: [mass, energy, px, py, pz].  Returns ST_VACUUM
+// when the solution is vacuum, else 0.
 template <int D>
 __device__ __forceinline__ unsigned project_flux(const RiemannResult &rs, const double *R, const double *L,
-                                                 const double *Lam, const double *A, const double *vf,
-                                                 double inv_gm1, int mfm, double *Fo) {
+                                                 double unR, double unL, const double *hatA, const double *A,
+                                                 const double *vf, double inv_gm1, int mfm, double *Fo) {
     unsigned st = 0;
-    double vSol[3] = {rs.u, 0., 0.};
-    if (rs.flag == 1) { for (int a = 1; a < D; ++a) vSol[a] = L[2 + a]; }
-    else if (rs.flag == -1) { for (int a = 1; a < D; ++a) vSol[a] = R[2 + a]; }
-    else st = ST_VACUUM;
+    double vSol[3] = {0., 0., 0.};
+    if (rs.flag == 1 || rs.flag == -1) {
+        const double *side = rs.flag == 1 ? L : R;
+        const double du = rs.u - (rs.flag == 1 ? unL : unR);
+#pragma unroll
+        for (int a = 0; a < D; ++a) vSol[a] = fma(du, hatA[a], side[2 + a]);
+    } else {
+        st = ST_VACUUM;
+#pragma unroll
+        for (int a = 0; a < D; ++a) vSol[a] = rs.u * hatA[a];
+    }
     const double rhoSol = rs.rho, PSol = rs.p;
     const double pe = PSol * inv_gm1;
     if (D == 2) {
-        // back rotation = transpose of Lam
-        double b0 = vSol[0], b1 = vSol[1];
-        vSol[0] = Lam[0] * b0 + Lam[2] * b1;
-        vSol[1] = Lam[1] * b0 + Lam[3] * b1;
         Fo[0] = A[0] * rhoSol * vSol[0] + A[1] * rhoSol * vSol[1];
         double vLab[2] = {vSol[0] + vf[0], vSol[1] + vf[1]};
         if (mfm) { vSol[0] = 0.; vSol[1] = 0.; }
@@ -1223,10 +1195,6 @@ __device__ __forceinline__ unsigned project_flux(const RiemannResult &rs, const 
         Fo[1] = A[0] * (vSol[0] * (pe + ek) + PSol * vLab[0]) + A[1] * (vSol[1] * (pe + ek) + PSol * vLab[1]);
         Fo[4] = 0.;
     } else {
-        double b0 = vSol[0], b1 = vSol[1], b2 = vSol[2];
-        vSol[0] = Lam[0] * b0 + Lam[3] * b1 + Lam[6] * b2;
-        vSol[1] = Lam[1] * b0 + Lam[4] * b1 + Lam[7] * b2;
-        vSol[2] = Lam[2] * b0 + Lam[5] * b1 + Lam[8] * b2;
         Fo[0] = A[0] * rhoSol * vSol[0] + A[1] * rhoSol * vSol[1] + A[2] * rhoSol * vSol[2];
         double vLab[3] = {vSol[0] + vf[0], vSol[1] + vf[1], vSol[2] + vf[2]};
         if (mfm) { vSol[0] = 0.; vSol[1] = 0.; vSol[2] = 0.; }
@@ -1273,8 +1241,8 @@ __global__ void MLH_FACE_BOUNDS k_faces(Params p, const Member *__restrict__ mem
     for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < nf; t += gridDim.x * blockDim.x) {
         // MODE 2 walks the queue: t is the queue position, f the face
         const int f = QUEUED ? queueFace[t] : t;
-        double R[5], L[5], A[3] = {0., 0., 0.}, vf[3] = {0., 0., 0.}, hatA[3] = {0., 0., 0.}, Lam[9];
-        const double unitX[3] = {1., 0., 0.};
+        double R[5], L[5], A[3] = {0., 0., 0.}, vf[3] = {0., 0., 0.}, hatA[3] = {0., 0., 0.};
+        double unR = 0., unL = 0.;   // velocity components along the face normal
         double ptr_q = -1.;   // MODE 2: two-rarefaction guess found in MODE 1; MODE 4: Newton iterate
         if (QUEUED) {
             const FaceState &fs = fstate[t];
@@ -1283,8 +1251,8 @@ __global__ void MLH_FACE_BOUNDS k_faces(Params p, const Member *__restrict__ mem
             for (int k = 0; k < 5; ++k) { R[k] = fs.v[k]; L[k] = fs.v[5 + k]; }
 #pragma unroll
             for (int a = 0; a < 3; ++a) { A[a] = fs.v[10 + a]; vf[a] = fs.v[13 + a]; hatA[a] = fs.v[16 + a]; }
-            if (D == 2) rot2(hatA, unitX, Lam);
-            else rot3(hatA, unitX, Lam);
+            unR = dotD<D>(hatA, R + 2);
+            unL = dotD<D>(hatA, L + 2);
         } else {
         const FaceRef fr = faces[f];
         if (fr.i < 0 || fr.slot < 0) {
@@ -1415,7 +1383,7 @@ __global__ void MLH_FACE_BOUNDS k_faces(Params p, const Member *__restrict__ mem
         }
         if (dneg(R[1]) || dneg(L[1])) st_local |= ST_NEG_PRESSURE;
         // --- Riemann problem in the face frame (i left, j right)
-        face_frame<D>(A, hatA, Lam, R, L);
+        face_normal<D>(A, R, L, hatA, unR, unL);
         }   // !QUEUED
         double guess = -1.;
         if (MODE == 2) {
@@ -1426,9 +1394,9 @@ __global__ void MLH_FACE_BOUNDS k_faces(Params p, const Member *__restrict__ mem
         if (MODE == 4) guess = ptr_q;
         // MODE 1 defers faces whose two-rarefaction guess says strong shock
         const double defer = MODE == 1 ? PSTAR_HARD * fmin(R[1], L[1]) : 0.;
-        RiemannResult rs = ROOT5 ? riemann_exact5(rc, R[0], R[2], R[1], L[0], L[2], L[1], guess, defer,
+        RiemannResult rs = ROOT5 ? riemann_exact5(rc, R[0], unR, R[1], L[0], unL, L[1], guess, defer,
                                                   MODE == 3 ? 1 : 0)
-                                 : riemann_exact(rc, R[0], R[2], R[1], L[0], L[2], L[1], guess, defer);
+                                 : riemann_exact(rc, R[0], unR, R[1], L[0], unL, L[1], guess, defer);
         if (MODE == 3 && rs.flag == 2) {
             const int q = atomicAdd(queueCount, 1);
             if (q < p.queue_cap) {
@@ -1444,7 +1412,7 @@ __global__ void MLH_FACE_BOUNDS k_faces(Params p, const Member *__restrict__ mem
             }
             // queue full: continue here
             const int done = rs.iters;
-            rs = riemann_exact5(rc, R[0], R[2], R[1], L[0], L[2], L[1], rs.pstar, 0.);
+            rs = riemann_exact5(rc, R[0], unR, R[1], L[0], unL, L[1], rs.pstar, 0.);
             if (rs.iters >= 0) rs.iters += done;
         }
         if (MODE == 1 && rs.flag == 2) {
@@ -1455,15 +1423,15 @@ __global__ void MLH_FACE_BOUNDS k_faces(Params p, const Member *__restrict__ mem
 #pragma unroll
             for (int a = 0; a < 3; ++a) { fs.v[10 + a] = A[a]; fs.v[13 + a] = vf[a]; fs.v[16 + a] = hatA[a]; }
             fs.v[19] = rs.pstar;   // the two-rarefaction guess
-            feat[q] = pstar_features(R, L, gamma);
+            feat[q] = pstar_features(R, L, unR, unL, gamma);
             queueFace[q] = f;
             continue;
         }
         if (MODE == 0 && hv.stride > 0 && f % hv.stride == 0) {
             const int slot = f / hv.stride;
-            const double ptr = two_rarefaction_guess<ROOT5>(rc, R[0], R[2], R[1], L[0], L[2], L[1]);
+            const double ptr = two_rarefaction_guess<ROOT5>(rc, R[0], unR, R[1], L[0], unL, L[1]);
             if (slot < hv.cap && rs.iters >= 0 && rs.pstar > 0. && ptr > 0.) {
-                hv.x[slot] = pstar_features(R, L, gamma);
+                hv.x[slot] = pstar_features(R, L, unR, unL, gamma);
                 hv.t[slot] = (float)log(rs.pstar / ptr);
                 atomicMax(hv.count, slot + 1);
             }
@@ -1478,7 +1446,7 @@ __global__ void MLH_FACE_BOUNDS k_faces(Params p, const Member *__restrict__ mem
             iters_local += (unsigned long long)rs.iters;
         }
         double Fo[5];
-        st_local |= project_flux<D>(rs, R, L, Lam, A, vf, rc.inv_gm1, p.mfm, Fo);
+        st_local |= project_flux<D>(rs, R, L, unR, unL, hatA, A, vf, rc.inv_gm1, p.mfm, Fo);
         double2 *dst = reinterpret_cast<double2 *>(Fface + (size_t)f * 6);
         dst[0] = make_double2(Fo[0], Fo[1]);
         dst[1] = make_double2(Fo[2], Fo[3]);
@@ -1515,18 +1483,18 @@ __global__ void __launch_bounds__(256) k_riemann_batch(int n, RiemannConsts rc, 
     unsigned st = 0;
     for (int f = blockIdx.x * blockDim.x + threadIdx.x; f < n; f += gridDim.x * blockDim.x) {
         double R[5] = {0., 0., 0., 0., 0.}, L[5] = {0., 0., 0., 0., 0.};
-        double A[3] = {0., 0., 0.}, vf[3] = {0., 0., 0.}, hatA[3], Lam[9];
+        double A[3] = {0., 0., 0.}, vf[3] = {0., 0., 0.}, hatA[3], unR, unL;
 #pragma unroll
         for (int k = 0; k < NV; ++k) { R[k] = Wi[(size_t)f * NV + k]; L[k] = Wj[(size_t)f * NV + k]; }
 #pragma unroll
         for (int a = 0; a < D; ++a) { A[a] = Aij[(size_t)f * D + a]; vf[a] = vFrame[(size_t)f * D + a]; }
         if (R[1] < 0. || L[1] < 0.) st |= ST_NEG_PRESSURE;
-        face_frame<D>(A, hatA, Lam, R, L);
-        const RiemannResult rs = ROOT5 ? riemann_exact5(rc, R[0], R[2], R[1], L[0], L[2], L[1], -1., 0.)
-                                       : riemann_exact(rc, R[0], R[2], R[1], L[0], L[2], L[1], -1., 0.);
+        face_normal<D>(A, R, L, hatA, unR, unL);
+        const RiemannResult rs = ROOT5 ? riemann_exact5(rc, R[0], unR, R[1], L[0], unL, L[1], -1., 0.)
+                                       : riemann_exact(rc, R[0], unR, R[1], L[0], unL, L[1], -1., 0.);
         if (rs.iters < 0) st |= ST_NEWTON;
         double Fo[5];
-        st |= project_flux<D>(rs, R, L, Lam, A, vf, rc.inv_gm1, mfm, Fo);
+        st |= project_flux<D>(rs, R, L, unR, unL, hatA, A, vf, rc.inv_gm1, mfm, Fo);
 #pragma unroll
         for (int k = 0; k < NV; ++k) F[(size_t)f * NV + k] = Fo[k];
         if (iters) iters[f] = rs.iters;
