@@ -1072,29 +1072,28 @@ __device__ __forceinline__ double pairwise_limiter(const Params &p, double phi0,
                                                    double ratio) {
     // every comparison on integer keys (ord_key), off the FP64 pipe
     const long long ki = ord_key(phi_i), kj = ord_key(phi_j);
+    if (ki == kj) return phi_i;   // neither phi_i < phi_j nor phi_i > phi_j
     const bool i_lt_j = ki < kj;
-    const double phi_ij = phi_i + ratio * (phi_j - phi_i);
-    const double phiMin = i_lt_j ? phi_i : phi_j, phiMax = i_lt_j ? phi_j : phi_i;
-    const double ad = ref_abs(phi_i - phi_j, p.int_abs);
+    const double d = phi_i - phi_j;              // phi_j - phi_i = -d exactly
+    const double phi_ij = fma(ratio, -d, phi_i);
+    const double ad = ref_abs(d, p.int_abs);
     const double delta1 = p.psi1 * ad;
     const double delta2 = p.psi2 * ad;
-    // (a >= 0 && b >= 0) || (a < 0 && b < 0): a and b on the same side of zero
-    const double up = phiMax + delta1, dn = phiMin - delta1;
-    const double phiPlus = (ord_key(up) >= 0) == (ord_key(phiMax) >= 0)
-                               ? up : phiMax / (1. + delta1 / ref_abs(phiMax, p.int_abs));
-    const double phiMinus = (ord_key(dn) >= 0) == (ord_key(phiMin) >= 0)
-                                ? dn : phiMin / (1. + delta1 / ref_abs(phiMin, p.int_abs));
+    // the bound that is used is phi_minus = phi_min - delta1 when phi_i <
+    // phi_j and phi_plus = phi_max + delta1 otherwise, and in both cases the
+    // extreme it starts from is phi_i; the reference takes the shift when it
+    // keeps the sign, (a >= 0 && b >= 0) || (a < 0 && b < 0), else
+    // phi / (1 + delta1 / |phi|)
+    const double shifted = phi_i + (i_lt_j ? -delta1 : delta1);
+    const double bound = (ord_key(shifted) >= 0) == (ord_key(phi_i) >= 0)
+                             ? shifted : phi_i / (1. + delta1 / ref_abs(phi_i, p.int_abs));
+    const double t = phi_ij + (i_lt_j ? delta2 : -delta2);
     if (i_lt_j) {
-        const double t = phi_ij + delta2;
         const double minPhiD2 = dlt(t, phi0) ? t : phi0;
-        return dlt(minPhiD2, phiMinus) ? phiMinus : minPhiD2;
+        return dlt(minPhiD2, bound) ? bound : minPhiD2;
     }
-    if (kj < ki) {
-        const double t = phi_ij - delta2;
-        const double maxPhiD2 = dlt(phi0, t) ? t : phi0;
-        return dlt(phiPlus, maxPhiD2) ? phiPlus : maxPhiD2;
-    }
-    return phi_i;
+    const double maxPhiD2 = dlt(phi0, t) ? t : phi0;
+    return dlt(bound, maxPhiD2) ? bound : maxPhiD2;
 }
 
 // Network inputs of a face from its face-frame states (left = particle i,
@@ -1183,28 +1182,23 @@ __device__ __forceinline__ unsigned project_flux(const RiemannResult &rs, const 
 #pragma unroll
         for (int a = 0; a < D; ++a) vSol[a] = rs.u * hatA[a];
     }
+    // F_m = rho* (A . v*), F_p = F_m v_lab + P* A,
+    // F_E = (A . v*) (P*/(gamma-1) + rho*/2 |v_lab|^2) + P* (A . v_lab);
+    // MESHLESS_FINITE_MASS keeps F_m and drops the advective terms
     const double rhoSol = rs.rho, PSol = rs.p;
     const double pe = PSol * inv_gm1;
-    if (D == 2) {
-        Fo[0] = A[0] * rhoSol * vSol[0] + A[1] * rhoSol * vSol[1];
-        double vLab[2] = {vSol[0] + vf[0], vSol[1] + vf[1]};
-        if (mfm) { vSol[0] = 0.; vSol[1] = 0.; }
-        Fo[2] = A[0] * (rhoSol * vLab[0] * vSol[0] + PSol) + A[1] * rhoSol * vLab[0] * vSol[1];
-        Fo[3] = A[0] * rhoSol * vLab[1] * vSol[0] + A[1] * (rhoSol * vLab[1] * vSol[1] + PSol);
-        const double ek = rhoSol * .5 * (vLab[0] * vLab[0] + vLab[1] * vLab[1]);
-        Fo[1] = A[0] * (vSol[0] * (pe + ek) + PSol * vLab[0]) + A[1] * (vSol[1] * (pe + ek) + PSol * vLab[1]);
-        Fo[4] = 0.;
-    } else {
-        Fo[0] = A[0] * rhoSol * vSol[0] + A[1] * rhoSol * vSol[1] + A[2] * rhoSol * vSol[2];
-        double vLab[3] = {vSol[0] + vf[0], vSol[1] + vf[1], vSol[2] + vf[2]};
-        if (mfm) { vSol[0] = 0.; vSol[1] = 0.; vSol[2] = 0.; }
-        Fo[2] = A[0] * (rhoSol * vLab[0] * vSol[0] + PSol) + A[1] * rhoSol * vLab[0] * vSol[1] + A[2] * rhoSol * vLab[0] * vSol[2];
-        Fo[3] = A[0] * rhoSol * vLab[1] * vSol[0] + A[1] * (rhoSol * vLab[1] * vSol[1] + PSol) + A[2] * rhoSol * vLab[1] * vSol[2];
-        Fo[4] = A[0] * rhoSol * vLab[2] * vSol[0] + A[1] * rhoSol * vLab[2] * vSol[1] + A[2] * (rhoSol * vLab[2] * vSol[2] + PSol);
-        const double ek = rhoSol * .5 * ((vLab[0] * vLab[0] + vLab[1] * vLab[1]) + vLab[2] * vLab[2]);
-        Fo[1] = A[0] * (vSol[0] * (pe + ek) + PSol * vLab[0]) + A[1] * (vSol[1] * (pe + ek) + PSol * vLab[1])
-              + A[2] * (vSol[2] * (pe + ek) + PSol * vLab[2]);
-    }
+    const double Av = dotD<D>(A, vSol);
+    double vLab[3] = {0., 0., 0.};
+#pragma unroll
+    for (int a = 0; a < D; ++a) vLab[a] = vSol[a] + vf[a];
+    Fo[0] = rhoSol * Av;
+    const double Avm = mfm ? 0. : Av;
+    const double mflux = rhoSol * Avm;
+#pragma unroll
+    for (int a = 0; a < D; ++a) Fo[2 + a] = fma(mflux, vLab[a], PSol * A[a]);
+    if (D == 2) Fo[4] = 0.;
+    const double ek = rhoSol * .5 * dotD<D>(vLab, vLab);
+    Fo[1] = fma(Avm, pe + ek, PSol * dotD<D>(A, vLab));
     return st;
 }
 
