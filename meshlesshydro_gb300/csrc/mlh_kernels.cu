@@ -469,6 +469,26 @@ __global__ void __launch_bounds__(NNS_WARPS * 32) k_neighbours(
     const double *X[3] = {x, y, z};
     const int gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const int nw = (gridDim.x * blockDim.x) >> 5;
+    // density, pressure, 1/omega and sound speed of particle bi (per lane)
+    int bi = -1, iter = 0;
+    double bomega = 0.;
+    auto finish = [&]() {
+        if (bi < 0) return;
+        const double rho = m[bi] * bomega;
+        const double P = (p.gamma - 1.) * rho * u[bi];
+        unsigned st = 0;
+        if (rho <= 0.) st |= ST_NEG_DENSITY;
+        if (P <= 0.) st |= ST_NEG_PRESSURE;
+        if (st) flag(status, st);
+        Prim pr;
+        pr.x = x[bi]; pr.y = y[bi]; pr.z = D == 3 ? z[bi] : 0.;
+        pr.rho = rho; pr.P = P;
+        pr.vx = vx[bi]; pr.vy = vy[bi]; pr.vz = D == 3 ? vz[bi] : 0.;
+        prim[bi] = pr;
+        geo[bi].omega = bomega;
+        geo[bi].V = frcp(bomega);
+        geo[bi].c = sqrt(p.gamma * P * frcp(rho));
+    };
     for (int i = gw; i < p.n; i += nw) {
         const int mi = memberOf ? memberOf[i] : 0;
         const GridInfo g = grids[mi];
@@ -565,35 +585,28 @@ __global__ void __launch_bounds__(NNS_WARPS * 32) k_neighbours(
         // canonical faces among the stored slots (neighbour or parent > i);
         // counted from the final list so that it matches k_link exactly
         for (int t = lane; t < nr + ni; t += 32) fc += (int)(nbr[base + t] & IDX_MASK) > i;
-        // --- omega = (sum over real neighbours) + W(0) + (sum over images)
+        // --- omega = W(0) + sum over the neighbours (real and images)
+        double wsum = wsumR + wsumI;
 #pragma unroll
         for (int o = 16; o > 0; o >>= 1) {
-            wsumR += __shfl_xor_sync(0xffffffffu, wsumR, o);
-            wsumI += __shfl_xor_sync(0xffffffffu, wsumI, o);
+            wsum += __shfl_xor_sync(0xffffffffu, wsum, o);
             fc += __shfl_xor_sync(0xffffffffu, fc, o);
         }
         if (lane == 0) {
             if (overflow) flag(status, ST_NGB_OVERFLOW);
             if (nr + ni == 0) flag(status, ST_NO_NEIGHBOUR);
-            const double omega = (wsumR + w0_i) + wsumI;
-            const double rho = m[i] * omega;
-            const double P = (p.gamma - 1.) * rho * u[i];
-            if (rho <= 0.) flag(status, ST_NEG_DENSITY);
-            if (P <= 0.) flag(status, ST_NEG_PRESSURE);
             noi[i] = nr;
             noiImg[i] = ni;
             faceCnt[i] = fc;
-            Prim pr;
-            pr.x = xi[0]; pr.y = xi[1]; pr.z = xi[2];
-            pr.rho = rho; pr.P = P;
-            pr.vx = vx[i]; pr.vy = vy[i]; pr.vz = D == 3 ? vz[i] : 0.;
-            prim[i] = pr;
-            geo[i].omega = omega;
-            geo[i].V = 1. / omega;
-            geo[i].c = sqrt(p.gamma * P / rho);
         }
+        // the floating-point tail of every 32 particles of this warp runs
+        // once on all 32 lanes (lane k keeps the k-th particle)
+        if (lane == (iter & 31)) { bi = i; bomega = wsum + w0_i; }
+        if ((iter & 31) == 31) { finish(); bi = -1; }
+        ++iter;
         __syncwarp();
     }
+    finish();
 }
 
 // ------------------------------------------------------------------ smoothing lengths

@@ -161,9 +161,12 @@ def test_negative_pressure_reported():
 
 
 @pytest.mark.parametrize("name,nsteps,rtol", [("kh100", 100, 1e-8), ("sedov16_periodic", 30, 1e-8),
-                                              ("sedov16_nonperiodic", 60, 1e-8)])
+                                              ("sedov16_nonperiodic", 40, 1e-8)])
 def test_multistep_density_l1(oracle_mod, name, nsteps, rtol):
-    """Density after many steps: L1 relative difference to the oracle."""
+    """Density after many steps: L1 relative difference to the oracle.  The
+    non-periodic 16^3 blast becomes unstable at the edge of the particle
+    cloud after about 61-63 steps in the oracle and on the GPU alike (which
+    step depends on rounding), so its comparison stops at 40 steps."""
     p, cfg = CASES[name]
     o = oracle_mod.Oracle(cfg, p)
     g = _sim(cfg, p)
