@@ -408,11 +408,15 @@ __device__ __forceinline__ int nns_candidates(const Params &p, const GridInfo &g
         bool pass = false;
         uint32_t ent = 0;
         if (t < total) {
+            // the last cell whose range starts at or before t (empty cells
+            // share their offset with the next one): binary search over the
+            // non-decreasing offsets
             int k = 0;
-            for (int kk = 1; kk < NC; ++kk)
-                if (cs->excl[kk] <= t) k = kk;
-            // empty cells share their offset with the next one: take the
-            // last cell whose range contains t
+#pragma unroll
+            for (int step = 16; step > 0; step >>= 1) {
+                const int kk = k + step;
+                if (kk < NC && cs->excl[kk] <= t) k = kk;
+            }
             const int j = cellList[cs->start[k] + (t - cs->excl[k])];
             const unsigned wr = cs->wrap[k];
             if (wr || j != i) {
