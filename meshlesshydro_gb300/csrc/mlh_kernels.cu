@@ -321,6 +321,12 @@ __global__ void k_sort_cells(const int *__restrict__ cellTotal, const int *__res
 // the slot list and images to a shared list, which is then placed behind the
 // real neighbours sorted by parent index.
 constexpr int NNS_WARPS = 8;
+// blocks of the neighbour search resident per SM: 3 caps it at 80 registers
+// (a 4-byte spill) and gives 24 warps per SM (measured on the Sedov 128^3
+// step: 9.7 ms with 1, 8.6 ms with 3, 12.3 ms with 4)
+#ifndef MLH_NNS_MINB
+#define MLH_NNS_MINB 3
+#endif
 
 struct NnsCells {
     int excl[27], start[27];
@@ -445,7 +451,7 @@ __device__ __forceinline__ int nns_candidates(const Params &p, const GridInfo &g
 }
 
 template <int D>
-__global__ void __launch_bounds__(NNS_WARPS * 32) k_neighbours(
+__global__ void __launch_bounds__(NNS_WARPS * 32, MLH_NNS_MINB) k_neighbours(
     Params p, const Member *__restrict__ members, const int *__restrict__ memberOf,
     const GridInfo *__restrict__ grids, const double *__restrict__ x, const double *__restrict__ y,
     const double *__restrict__ z, const float4 *__restrict__ posf, const double *__restrict__ vx,
