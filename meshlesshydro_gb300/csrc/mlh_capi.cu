@@ -68,7 +68,7 @@ struct mlh_ctx {
     uint32_t *nbr = nullptr;
     double *rr = nullptr, *ww = nullptr, *psi = nullptr;
     size_t faces_cap = 0;
-    size_t queue_cap = 0;
+    size_t queue_cap = 0, queue_cap2 = 0;
     int *noi = nullptr, *noiImg = nullptr, *faceCnt = nullptr, *faceOff = nullptr, *faceOf = nullptr;
     FaceRef *faces = nullptr;
     double *Fface = nullptr;
@@ -92,7 +92,8 @@ struct mlh_ctx {
     bool learned = false;
     float *mlp_w = nullptr;
     void *mlp_packed = nullptr;
-    FaceState *fstate = nullptr;
+    FaceState *fstate = nullptr, *fstate2 = nullptr;
+    int *queueFace2 = nullptr, *queueCount2 = nullptr;
     float4 *feat = nullptr;
     float *yguess = nullptr;
     int *queueFace = nullptr;   // faces handed to the network (learned guess)
@@ -118,7 +119,9 @@ void free_neighbour_buffers(mlh_ctx *c) {
     cudaFree(c->nbr); cudaFree(c->rr); cudaFree(c->ww); cudaFree(c->psi); cudaFree(c->faceOf); cudaFree(c->faces);
     cudaFree(c->Fface);
     cudaFree(c->fstate); cudaFree(c->feat); cudaFree(c->yguess); cudaFree(c->queueFace); cudaFree(c->queueCount);
+    cudaFree(c->fstate2); cudaFree(c->queueFace2); cudaFree(c->queueCount2);
     c->queueFace = nullptr; c->queueCount = nullptr;
+    c->fstate2 = nullptr; c->queueFace2 = nullptr; c->queueCount2 = nullptr;
     c->nbr = nullptr; c->rr = nullptr; c->ww = nullptr; c->psi = nullptr; c->faceOf = nullptr; c->faces = nullptr;
     c->Fface = nullptr; c->fstate = nullptr; c->feat = nullptr; c->yguess = nullptr;
 }
@@ -134,17 +137,25 @@ int alloc_neighbour_buffers(mlh_ctx *c) {
     CK(dalloc(&c->faceOf, slots));
     CK(dalloc(&c->faces, faces));
     CK(dalloc(&c->Fface, faces * 6));
-    // queue of faces for a second face pass: every face with the learned
-    // guess; in the plain step the faces Newton has not finished after one
-    // step (a fifth to two thirds of them; faces_cap is about twice the faces
-    // of a step; a full queue finishes its faces in the first pass)
-    c->queue_cap = c->learned ? faces : faces / 2 + 1024;
+    // queues of faces for second face passes.  A: in the plain step the
+    // faces Newton has not finished after one step (a fifth to two thirds of
+    // them; faces_cap is about twice the faces of a step; a full queue
+    // finishes its faces in the first pass); with the learned guess the
+    // strong shocks handed to the network (room for every face).  B (learned
+    // guess only): the faces Newton has not finished after one step.
+    const size_t half = faces / 2 + 1024;
+    c->queue_cap = c->learned ? faces : half;
     CK(dalloc(&c->fstate, c->queue_cap));
     CK(dalloc(&c->queueFace, c->queue_cap));
     CK(dalloc(&c->queueCount, 1));
+    c->queue_cap2 = 0;
     if (c->learned) {
         CK(dalloc(&c->feat, faces));
         CK(dalloc(&c->yguess, faces));
+        c->queue_cap2 = half;
+        CK(dalloc(&c->fstate2, half));
+        CK(dalloc(&c->queueFace2, half));
+        CK(dalloc(&c->queueCount2, 1));
     }
     return 0;
 }
@@ -237,7 +248,8 @@ StepArgs make_args(mlh_ctx *c, double dt_max) {
     a.sm_count = c->sm_count;
     a.faces_cap = c->faces_cap;
     a.p.faces_cap = c->faces_cap > 0x7fffffff ? 0x7fffffff : (int)c->faces_cap;
-    a.p.queue_cap = c->queue_cap > 0x7fffffff ? 0x7fffffff : (int)c->queue_cap;
+    a.qcap = c->queue_cap > 0x7fffffff ? 0x7fffffff : (int)c->queue_cap;
+    a.qcap2 = c->queue_cap2 > 0x7fffffff ? 0x7fffffff : (int)c->queue_cap2;
     a.root5 = make_riemann_consts(c->p.gamma, c->p.rtol, c->p.rmaxit).root5;
     a.dt_max = dt_max;
     a.x = c->x; a.y = c->y; a.z = c->z; a.vx = c->vx; a.vy = c->vy; a.vz = c->vz; a.m = c->m; a.u = c->u;
@@ -258,6 +270,7 @@ StepArgs make_args(mlh_ctx *c, double dt_max) {
     a.learned = c->learned ? 1 : 0;
     a.fstate = c->fstate; a.feat = c->feat; a.yguess = c->yguess;
     a.queueFace = c->queueFace; a.queueCount = c->queueCount; a.mlp_packed = c->mlp_packed;
+    a.fstate2 = c->fstate2; a.queueFace2 = c->queueFace2; a.queueCount2 = c->queueCount2;
     a.harvest = c->harvest;
     a.hp = c->hp; a.neff = c->neff; a.hstat = c->hstat;
     a.p.hp = c->hp;

@@ -57,7 +57,6 @@ struct Params {
     int K;                 // neighbour slots per particle
     int ncells_cap;
     int faces_cap;         // capacity of the face arrays
-    int queue_cap;         // capacity of the queue of faces for a second face pass
     double h, hsq, h2, sigma, w0, gamma, cfl_h, beta, psi1, psi2, rtol, time_step;
     double box_lo[3], box_hi[3];
     float hsq_f;           // conservative single-precision bound for the pre-filter
@@ -89,6 +88,14 @@ struct FaceRef {    // canonical face: owner i, slot index, reverse slot (images
 // learned-guess face pipeline: R[5], L[5], A[3], v_frame[3], A/|A| [3], p_TR
 struct FaceState {
     double v[20];
+};
+// A queue of faces for a second face pass: their face-frame states, face ids
+// and the number of faces offered (entries at or beyond cap were not stored).
+struct FaceQueue {
+    FaceState *st;
+    int *face;
+    int *count;
+    int cap;
 };
 // Where the plain face kernel records network training pairs.
 struct Harvest {

@@ -1241,14 +1241,14 @@ __global__ void MLH_FACE_BOUNDS k_faces(Params p, const Member *__restrict__ mem
                                                const double *__restrict__ psi, const int *__restrict__ faceTotal,
                                                const FaceRef *__restrict__ faces, const double *__restrict__ dtp,
                                                double *__restrict__ Fface, unsigned long long *__restrict__ newtonSum,
-                                               unsigned *__restrict__ status, FaceState *__restrict__ fstate,
+                                               unsigned *__restrict__ status, FaceQueue qa, FaceQueue qb,
                                                float4 *__restrict__ feat, const float *__restrict__ yguess,
-                                               int *__restrict__ queueFace, int *__restrict__ queueCount, Harvest hv) {
+                                               Harvest hv) {
     constexpr int NV = D + 2;
     int nf = *faceTotal < p.faces_cap ? *faceTotal : p.faces_cap;
     constexpr bool QUEUED = MODE == 2 || MODE == 4;   // passes over the queue
     if (QUEUED) {   // the queue holds min(count, capacity) faces; MODE 3 finished the rest itself
-        const int qn = *queueCount < p.queue_cap ? *queueCount : p.queue_cap;
+        const int qn = *qa.count < qa.cap ? *qa.count : qa.cap;
         nf = qn < nf ? qn : nf;
     }
     const RiemannConsts rc = make_riemann_consts(p.gamma, p.rtol, p.rmaxit);
@@ -1257,12 +1257,12 @@ __global__ void MLH_FACE_BOUNDS k_faces(Params p, const Member *__restrict__ mem
     unsigned st_local = 0;
     for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < nf; t += gridDim.x * blockDim.x) {
         // MODE 2 walks the queue: t is the queue position, f the face
-        const int f = QUEUED ? queueFace[t] : t;
+        const int f = QUEUED ? qa.face[t] : t;
         double R[5], L[5], A[3] = {0., 0., 0.}, vf[3] = {0., 0., 0.}, hatA[3] = {0., 0., 0.};
         double unR = 0., unL = 0.;   // velocity components along the face normal
         double ptr_q = -1.;   // MODE 2: two-rarefaction guess found in MODE 1; MODE 4: Newton iterate
         if (QUEUED) {
-            const FaceState &fs = fstate[t];
+            const FaceState &fs = qa.st[t];
             ptr_q = fs.v[19];
 #pragma unroll
             for (int k = 0; k < 5; ++k) { R[k] = fs.v[k]; L[k] = fs.v[5 + k]; }
@@ -1412,37 +1412,32 @@ __global__ void MLH_FACE_BOUNDS k_faces(Params p, const Member *__restrict__ mem
         // MODE 1 defers faces whose two-rarefaction guess says strong shock
         const double defer = MODE == 1 ? PSTAR_HARD * fmin(R[1], L[1]) : 0.;
         RiemannResult rs = ROOT5 ? riemann_exact5(rc, R[0], unR, R[1], L[0], unL, L[1], guess, defer,
-                                                  MODE == 3 ? 1 : 0)
+                                                  (MODE == 1 || MODE == 3) ? 1 : 0)
                                  : riemann_exact(rc, R[0], unR, R[1], L[0], unL, L[1], guess, defer);
-        if (MODE == 3 && rs.flag == 2) {
-            const int q = atomicAdd(queueCount, 1);
-            if (q < p.queue_cap) {
-                FaceState &fs = fstate[q];
+        // deferred faces: strong shocks of MODE 1 (unsolved, iters 0) go to
+        // queue A for the network; faces Newton has not finished after one
+        // step go to queue A (MODE 3) or B (MODE 1) with their iterate
+        if ((MODE == 1 || MODE == 3) && rs.flag == 2) {
+            const bool strong = MODE == 1 && rs.iters == 0;
+            const FaceQueue &fq = (MODE == 1 && !strong) ? qb : qa;
+            const int q = atomicAdd(fq.count, 1);
+            if (q < fq.cap) {
+                FaceState &fs = fq.st[q];
 #pragma unroll
                 for (int k = 0; k < 5; ++k) { fs.v[k] = R[k]; fs.v[5 + k] = L[k]; }
 #pragma unroll
                 for (int a = 0; a < 3; ++a) { fs.v[10 + a] = A[a]; fs.v[13 + a] = vf[a]; fs.v[16 + a] = hatA[a]; }
-                fs.v[19] = rs.pstar;   // the Newton iterate
-                queueFace[q] = f;
-                iters_local += (unsigned long long)rs.iters;
+                fs.v[19] = rs.pstar;   // the two-rarefaction guess (strong) or the Newton iterate
+                fq.face[q] = f;
+                if (strong) feat[q] = pstar_features(R, L, unR, unL, gamma);
+                else iters_local += (unsigned long long)rs.iters;
                 continue;
             }
-            // queue full: continue here
+            // queue full: finish here, from the iterate or from p_TR
             const int done = rs.iters;
-            rs = riemann_exact5(rc, R[0], unR, R[1], L[0], unL, L[1], rs.pstar, 0.);
+            rs = ROOT5 ? riemann_exact5(rc, R[0], unR, R[1], L[0], unL, L[1], strong ? -1. : rs.pstar, 0.)
+                       : riemann_exact(rc, R[0], unR, R[1], L[0], unL, L[1], -1., 0.);
             if (rs.iters >= 0) rs.iters += done;
-        }
-        if (MODE == 1 && rs.flag == 2) {
-            const int q = atomicAdd(queueCount, 1);   // < faces on this step <= faces_cap
-            FaceState &fs = fstate[q];
-#pragma unroll
-            for (int k = 0; k < 5; ++k) { fs.v[k] = R[k]; fs.v[5 + k] = L[k]; }
-#pragma unroll
-            for (int a = 0; a < 3; ++a) { fs.v[10 + a] = A[a]; fs.v[13 + a] = vf[a]; fs.v[16 + a] = hatA[a]; }
-            fs.v[19] = rs.pstar;   // the two-rarefaction guess
-            feat[q] = pstar_features(R, L, unR, unL, gamma);
-            queueFace[q] = f;
-            continue;
         }
         if (MODE == 0 && hv.stride > 0 && f % hv.stride == 0) {
             const int slot = f / hv.stride;
@@ -1721,22 +1716,27 @@ void launch_step(StepArgs &a) {
 
     tick(KT_FACES);
     const int fT = a.tune.face_threads, fB = a.sm_count * a.tune.face_blocks_per_sm;
-#define MLH_FACES(R5, MODE)                                                                                      \
+    const FaceQueue qa{a.fstate, a.queueFace, a.queueCount, a.qcap};
+    const FaceQueue qb{a.fstate2, a.queueFace2, a.queueCount2, a.qcap2};
+#define MLH_FACES(R5, MODE, QA, QB)                                                                              \
     k_faces<D, R5, MODE><<<fB, fT, 0, s>>>(p, a.members, a.memberOf, a.grids, a.prim, a.geo, a.grad, a.nbr, a.psi, \
-                                           a.faceOff + p.n, a.faces, a.dt, a.Fface, a.newtonSum, a.status,       \
-                                           a.fstate, a.feat, a.yguess, a.queueFace, a.queueCount, a.harvest)
+                                           a.faceOff + p.n, a.faces, a.dt, a.Fface, a.newtonSum, a.status, QA,   \
+                                           QB, a.feat, a.yguess, a.harvest)
     if (a.learned) {
+        // strong shocks: network guess (queue A); the rest as the plain step
         cudaMemsetAsync(a.queueCount, 0, sizeof(int), s);
-        if (a.root5) MLH_FACES(true, 1); else MLH_FACES(false, 1);
+        if (a.queueCount2) cudaMemsetAsync(a.queueCount2, 0, sizeof(int), s);
+        if (a.root5) MLH_FACES(true, 1, qa, qb); else MLH_FACES(false, 1, qa, qb);
         pstar_infer_dev(a.feat, a.queueCount, (int)a.faces_cap, a.mlp_packed, a.yguess, a.sm_count, s);
-        if (a.root5) MLH_FACES(true, 2); else MLH_FACES(false, 2);
+        if (a.root5) MLH_FACES(true, 2, qa, qb); else MLH_FACES(false, 2, qa, qb);
+        if (a.root5 && a.fstate2) MLH_FACES(true, 4, qb, qb);
     } else if (a.root5 && a.fstate && a.harvest.stride == 0) {
         // unconverged faces after one Newton step go to a second, dense pass
         cudaMemsetAsync(a.queueCount, 0, sizeof(int), s);
-        MLH_FACES(true, 3);
-        MLH_FACES(true, 4);
+        MLH_FACES(true, 3, qa, qb);
+        MLH_FACES(true, 4, qa, qb);
     } else {
-        if (a.root5) MLH_FACES(true, 0); else MLH_FACES(false, 0);
+        if (a.root5) MLH_FACES(true, 0, qa, qb); else MLH_FACES(false, 0, qa, qb);
     }
 #undef MLH_FACES
     tock(KT_FACES);

@@ -59,7 +59,11 @@ struct StepArgs {
     // learned p* guess: queue of the faces handed to the network (face ids,
     // their face-frame states, network inputs and outputs), packed weights
     int learned;
-    FaceState *fstate;
+    FaceState *fstate;      // queue A: strong shocks (learned) or the plain second pass
+    FaceState *fstate2;     // queue B: the learned step's second Newton pass
+    int *queueFace2;
+    int *queueCount2;
+    int qcap, qcap2;
     float4 *feat;
     float *yguess;
     int *queueFace;
