@@ -216,6 +216,16 @@ def run_reference(args):
     return 0
 
 
+def kernel_breakdown(sim, steps):
+    """Per-kernel device times of a few more steps with per-kernel CUDA events
+    (which serialise the step's streams), after the timed region."""
+    sim.reset_kernel_times()
+    sim.set_kernel_timing(True)
+    sim.step(max(1, min(steps, 3)))
+    sim.set_kernel_timing(False)
+    return sim.kernel_times()
+
+
 def learned_section(runtime, make_sim, tuning, args, faces_per_step, st_plain, kt_plain, rho_plain, ws, n):
     """The same steps with the learned p* guess: harvest faces of step 1
     (plain pipeline), train the MLP on 90 % of them, step with the network
@@ -239,13 +249,10 @@ def learned_section(runtime, make_sim, tuning, args, faces_per_step, st_plain, k
     sim2.set_pstar_weights(w)
     if args.warmup > 1:
         sim2.step(args.warmup - 1)
-    sim2.reset_kernel_times()
-    sim2.set_kernel_timing(True)
     torch.cuda.synchronize()
     st = sim2.step(args.steps)
-    sim2.set_kernel_timing(False)
-    kt = sim2.kernel_times()
     rho = sim2.get("rho")
+    kt = kernel_breakdown(sim2, args.steps)
     sim2.close()
     l1 = float(np.sum(np.abs(rho - rho_plain)) / np.sum(np.abs(rho_plain)))
     return {"value": ws * n * st.steps / (st.device_ms / 1e3),
@@ -287,8 +294,6 @@ def run_mlh(args):
         p = sim.host  # concatenated state: .n
     tuning = None if args.no_autotune else sim.autotune(1)
     sim.step(args.warmup)
-    sim.reset_kernel_times()
-    sim.set_kernel_timing(True)
     if dist:
         dist.barrier()
     torch.cuda.synchronize()
@@ -299,17 +304,16 @@ def run_mlh(args):
     torch.cuda.synchronize()
     wall = time.perf_counter() - t0
     ck = clocks.stop()
-    sim.set_kernel_timing(False)
     dev_s = st.device_ms / 1e3
     t_max = dev_s
     if dist:
         t = torch.tensor([dev_s], dtype=torch.float64)
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
         t_max = float(t.item())
-    kt = sim.kernel_times()
     faces_per_step = st.faces / max(st.steps, 1)
     pairs_per_step = st.pair_interactions / max(st.steps, 1)
     rho_plain = sim.get("rho")      # density of step warmup + steps (autotune restored its trials)
+    kt = kernel_breakdown(sim, args.steps)
     make_sim = ((lambda: runtime.Simulation(cfg, members=members)) if ensemble
                 else (lambda: runtime.Simulation(cfg, p)))
 
@@ -405,6 +409,8 @@ def run_mlh(args):
             "wall_s_timed": wall,
             "gpu_launches": LAUNCHES_PER_STEP * st.steps,
             "kernel_ms_per_step": {k: v[1] / max(v[0], 1) for k, v in kt.items()},
+            "kernel_ms_source": "up to 3 further steps with per-kernel CUDA events, which serialise the face-link "
+                                "stream that the timed steps overlap with the time step and gradients",
             "roofline": roofline,
             "clocks": ck,
             "tuning": tuning,

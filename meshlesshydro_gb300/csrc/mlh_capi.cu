@@ -49,7 +49,9 @@ struct mlh_ctx {
     int device = 0;
     int sm_count = 152;
     cudaStream_t stream = nullptr;
+    cudaStream_t stream2 = nullptr;              // face links, overlapped
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+    cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
     // state
     double *x = nullptr, *y = nullptr, *z = nullptr, *vx = nullptr, *vy = nullptr, *vz = nullptr, *m = nullptr, *u = nullptr;
     float4 *posf = nullptr;
@@ -243,6 +245,9 @@ StepArgs make_args(mlh_ctx *c, double dt_max) {
     std::memset(&a, 0, sizeof(a));
     a.p = c->p;
     a.stream = c->stream;
+    a.stream2 = c->stream2;
+    a.ev_fork = c->ev_fork;
+    a.ev_join = c->ev_join;
     a.tune = c->tune;
     a.face_blocks = c->sm_count * 8;
     a.sm_count = c->sm_count;
@@ -402,6 +407,10 @@ static int create_impl(const mlh_config *cfg, int nmembers, const mlh_member *md
     if (cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking) != cudaSuccess) return fail(cuda_fail(cudaGetLastError(), "stream"));
     cudaEventCreate(&c->ev0);
     cudaEventCreate(&c->ev1);
+    if (cudaStreamCreateWithFlags(&c->stream2, cudaStreamNonBlocking) != cudaSuccess ||
+        cudaEventCreateWithFlags(&c->ev_fork, cudaEventDisableTiming) != cudaSuccess ||
+        cudaEventCreateWithFlags(&c->ev_join, cudaEventDisableTiming) != cudaSuccess)
+        return fail(cuda_fail(cudaGetLastError(), "second stream"));
     size_t n = (size_t)c->n, nm = (size_t)nmembers;
 #define A(ptr, cnt) if (dalloc(&c->ptr, cnt) != cudaSuccess) return fail(cuda_fail(cudaGetLastError(), "cudaMalloc " #ptr))
     A(x, n); A(y, n); A(z, n); A(vx, n); A(vy, n); A(vz, n); A(m, n); A(u, n);
@@ -496,6 +505,9 @@ void mlh_destroy(mlh_ctx *c) {
     for (auto e : c->tev) cudaEventDestroy(e);
     if (c->ev0) cudaEventDestroy(c->ev0);
     if (c->ev1) cudaEventDestroy(c->ev1);
+    if (c->ev_fork) cudaEventDestroy(c->ev_fork);
+    if (c->ev_join) cudaEventDestroy(c->ev_join);
+    if (c->stream2) { cudaStreamSynchronize(c->stream2); cudaStreamDestroy(c->stream2); }
     if (c->stream) cudaStreamDestroy(c->stream);
     delete c;
 }

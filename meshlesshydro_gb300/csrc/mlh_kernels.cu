@@ -1694,6 +1694,23 @@ void launch_step(StepArgs &a) {
     }
     tock(KT_NNS);
 
+    // the face links (integer work) need only the neighbour lists: without
+    // per-kernel timing they run on the second stream while the time step and
+    // the gradients keep the FP64 pipe busy
+    const bool overlap = a.stream2 && !a.timer && !a.stop_after_gradients;
+    const int blocksLink = blocksN;
+    auto launch_links = [&](cudaStream_t ls) {
+        exclusive_scan(a.faceCnt, p.n, a.faceOff, a.scanTiles, a.scanTotal, ls);
+        cudaMemsetAsync(a.faces, 0xff, sizeof(FaceRef) * a.faces_cap, ls);
+        k_link<<<blocksLink, T, 0, ls>>>(p, a.nbr, a.noi, a.noiImg, a.faceOff, a.faceOf, a.faces, a.status);
+    };
+    if (overlap) {
+        cudaEventRecord(a.ev_fork, s);
+        cudaStreamWaitEvent(a.stream2, a.ev_fork, 0);
+        launch_links(a.stream2);
+        cudaEventRecord(a.ev_join, a.stream2);
+    }
+
     tick(KT_DT);
     cudaMemsetAsync(a.dtbits, 0xff, sizeof(unsigned long long) * (size_t)a.nmembers, s);
     k_timestep<D><<<(p.n + 255) / 256, 256, 0, s>>>(p, a.members, a.memberOf, a.prim, a.geo, a.nbr, a.rr, a.noi,
@@ -1708,11 +1725,13 @@ void launch_step(StepArgs &a) {
     tock(KT_GRAD);
     if (a.stop_after_gradients) return;
 
-    tick(KT_LINK);
-    exclusive_scan(a.faceCnt, p.n, a.faceOff, a.scanTiles, a.scanTotal, s);
-    cudaMemsetAsync(a.faces, 0xff, sizeof(FaceRef) * a.faces_cap, s);
-    k_link<<<blocksN, T, 0, s>>>(p, a.nbr, a.noi, a.noiImg, a.faceOff, a.faceOf, a.faces, a.status);
-    tock(KT_LINK);
+    if (overlap) {
+        cudaStreamWaitEvent(s, a.ev_join, 0);
+    } else {
+        tick(KT_LINK);
+        launch_links(s);
+        tock(KT_LINK);
+    }
 
     tick(KT_FACES);
     const int fT = a.tune.face_threads, fB = a.sm_count * a.tune.face_blocks_per_sm;

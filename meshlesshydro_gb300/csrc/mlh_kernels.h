@@ -22,6 +22,10 @@ struct StepArgs {
     Tuning tune;
     Params p;
     cudaStream_t stream;
+    // second stream for the face links, with the events of its fork and join
+    // (null: everything on `stream`)
+    cudaStream_t stream2;
+    cudaEvent_t ev_fork, ev_join;
     int face_blocks;
     int sm_count;
     int root5;              // gamma = 5/3 fast path of the Riemann solver
