@@ -185,8 +185,12 @@ __device__ __forceinline__ double rroot5(double x) {
     // 1e-30 < x < 1e30 on the bit patterns (the test is false for NaN and x <= 0)
     const long long b = __double_as_longlong(x);
     if (!(b > 0x39B4484BFEEBC2A0ll && b < 0x46293E5939A08CEAll)) return pow(x, -0.2);
-    float xf = (float)x;
-    double y = (double)exp2f(-0.2f * __log2f(xf));
+    // double -> float and back on the bit patterns (integer pipe): rebias the
+    // exponent (1023 - 127 = 896) and keep the top 23 mantissa bits; x and
+    // the seed are positive and normal in both formats in this range
+    const float xf = __int_as_float((int)((b >> 29) - (896ll << 23)));
+    const float yf = exp2f(-0.2f * __log2f(xf));
+    double y = __longlong_as_double(((long long)__float_as_int(yf) + (896ll << 23)) << 29);
 #pragma unroll
     for (int k = 0; k < STEPS; ++k) {
         double y2 = y * y;
