@@ -275,14 +275,14 @@ __device__ inline RiemannResult riemann_exact5(const RiemannConsts &k, double rh
                                                double defer_above = 0., int first_iters = 0) {
     RiemannResult res;
     const RiemannSide L = make_side(k, rhoL, uL, pL), R = make_side(k, rhoR, uR, pR);
-    if (k.g4 * (L.c + R.c) <= uR - uL) {
+    if (!dlt(uR - uL, k.g4 * (L.c + R.c))) {   // g4 (cL + cR) <= uR - uL: vacuum
         res.rho = 0.; res.u = 0.; res.p = 0.; res.pstar = 0.; res.flag = 0; res.iters = 0;
         return res;
     }
     const double du = uR - uL;
-    const double pfloor = 1e-12 * (pL > pR ? pL : pR);
+    const double pfloor = 1e-12 * (nn_le(pL, pR) ? pR : pL);
     double p0;
-    bool tried_guess = guess > 0.;
+    bool tried_guess = __double_as_longlong(guess) > 0;   // guess > 0 (-1: none)
     if (tried_guess) p0 = guess;
     else {
         double num = L.c + R.c - k.g7 * du;
@@ -307,7 +307,7 @@ __device__ inline RiemannResult riemann_exact5(const RiemannConsts &k, double rh
             double t2 = t * t;
             p0 = t2 * t2 * t;
         }
-        p = p0 > pfloor ? p0 : pfloor;
+        p = nn_le(p0, pfloor) ? pfloor : p0;
         for (int it = 1; it <= k.max_iter; ++it) {
             double invp = frcp(p);
             double fL, fdL, qL, fR, fdR, qR;
@@ -315,7 +315,10 @@ __device__ inline RiemannResult riemann_exact5(const RiemannConsts &k, double rh
             pressure_fn5(L, p, invp, fL, fdL, qL, rL);
             pressure_fn5(R, p, invp, fR, fdR, qR, rR);
             double pnew = p - (fL + fR + du) * frcp(fdL + fdR);
-            if (!(pnew > 0.)) pnew = pfloor;
+            {   // !(pnew > 0): zero, negative or NaN (bit patterns)
+                const long long pb = __double_as_longlong(pnew);
+                if (pb <= 0 || pb > 0x7FF0000000000000ll) pnew = pfloor;
+            }
             double dp = pnew - p;
             if (nn_le(2. * fabs(dp), k.tol * (pnew + p))) {
                 fLs = fL + fdL * dp;
@@ -354,7 +357,7 @@ __device__ inline RiemannResult riemann_exact5(const RiemannConsts &k, double rh
             double shl = uL - L.c;
             if (!dneg(shl)) { rho = rhoL; u = uL; pp = pL; }
             else {
-                double q = qLs >= 0. ? qLs : root5(pstar * L.invp);
+                double q = !dneg(qLs) ? qLs : root5(pstar * L.invp);
                 double stl = ustar - L.c * q;
                 if (dneg(stl)) { rho = rhoL * (q * q * q); u = ustar; pp = pstar; }
                 else {
@@ -380,7 +383,7 @@ __device__ inline RiemannResult riemann_exact5(const RiemannConsts &k, double rh
             double shr = uR + R.c;
             if (ord_key(shr) <= 0) { rho = rhoR; u = uR; pp = pR; }
             else {
-                double q = qRs >= 0. ? qRs : root5(pstar * R.invp);
+                double q = !dneg(qRs) ? qRs : root5(pstar * R.invp);
                 double str = ustar + R.c * q;
                 if (!dneg(str)) { rho = rhoR * (q * q * q); u = ustar; pp = pstar; }
                 else {
