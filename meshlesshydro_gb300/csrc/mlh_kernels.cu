@@ -1575,15 +1575,20 @@ __global__ void __launch_bounds__(256) k_update(Params p, const int *__restrict_
                            : mi * (ui + .5 * (vo[0] * vo[0] + vo[1] * vo[1]));
         double Qv[3] = {mi * vo[0], mi * vo[1], mi * vo[2]};
         if (!p.mfm) mi -= dt * mF;
-        if (mi <= 0.) st_local |= ST_NEG_MASS;
+        // sign and NaN tests on the bit patterns; one reciprocal of the mass
+        const long long mb_ = __double_as_longlong(mi);
+        if (mb_ <= 0) st_local |= ST_NEG_MASS;   // mi <= 0 (or a negative NaN)
+        const double imi = frcp(mi);
         double vn[3];
 #pragma unroll
-        for (int a = 0; a < D; ++a) { Qv[a] -= dt * vF[a]; vn[a] = Qv[a] / mi; }
+        for (int a = 0; a < D; ++a) { Qv[a] -= dt * vF[a]; vn[a] = Qv[a] * imi; }
         Q0 -= dt * eF;
-        double un = D == 3 ? Q0 / mi - .5 * (vn[0] * vn[0] + vn[1] * vn[1] + vn[2] * vn[2])
-                           : Q0 / mi - .5 * (vn[0] * vn[0] + vn[1] * vn[1]);
-        if (un <= 0.) st_local |= ST_NEG_ENERGY;
-        if (!(un == un) || !(mi == mi)) st_local |= ST_NAN;
+        double un = D == 3 ? Q0 * imi - .5 * (vn[0] * vn[0] + vn[1] * vn[1] + vn[2] * vn[2])
+                           : Q0 * imi - .5 * (vn[0] * vn[0] + vn[1] * vn[1]);
+        const long long ub = __double_as_longlong(un);
+        if (ub <= 0) st_local |= ST_NEG_ENERGY;
+        if ((ub & 0x7FFFFFFFFFFFFFFFll) > 0x7FF0000000000000ll || (mb_ & 0x7FFFFFFFFFFFFFFFll) > 0x7FF0000000000000ll)
+            st_local |= ST_NAN;
         m[i] = mi;
         u[i] = un;
 #pragma unroll
