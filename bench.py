@@ -64,10 +64,8 @@ def make_workload(name: str, seed_offset: int = 0):
 
 
 def dist_env():
-    ws = int(os.environ.get("WORLD_SIZE", "1"))
-    rank = int(os.environ.get("RANK", "0"))
-    local = int(os.environ.get("LOCAL_RANK", "0"))
-    return ws, rank, local
+    from meshlesshydro_gb300.replicas import dist_env as env
+    return env()
 
 
 class ClockSampler:
@@ -284,9 +282,10 @@ def run_mlh(args):
     else:
         dist = None
     from meshlesshydro_gb300 import build, runtime
+    from meshlesshydro_gb300.replicas import gather_units, job_rate, job_seconds, replica_seed
     build.build()
     fp64_peak = runtime.probe_fp64_tflops(0.5)
-    p, cfg = make_workload(args.workload, seed_offset=rank)
+    p, cfg = make_workload(args.workload, seed_offset=replica_seed(0, rank))
     ensemble = WORKLOADS[args.workload]["kind"] == "ensemble"
     members = p if ensemble else None
     sim = runtime.Simulation(cfg, members=members) if ensemble else runtime.Simulation(cfg, p)
@@ -304,12 +303,7 @@ def run_mlh(args):
     torch.cuda.synchronize()
     wall = time.perf_counter() - t0
     ck = clocks.stop()
-    dev_s = st.device_ms / 1e3
-    t_max = dev_s
-    if dist:
-        t = torch.tensor([dev_s], dtype=torch.float64)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        t_max = float(t.item())
+    t_max = job_seconds(st.device_ms / 1e3, dist)
     faces_per_step = st.faces / max(st.steps, 1)
     pairs_per_step = st.pair_interactions / max(st.steps, 1)
     rho_plain = sim.get("rho")      # density of step warmup + steps (autotune restored its trials)
@@ -369,13 +363,14 @@ def run_mlh(args):
         L.mlh_set_fields(sim.h, ctypes.byref(view))
         sim.step(1)
         L.mlh_get_fields(sim.h, ctypes.byref(view))
-    e2e_wall = time.perf_counter() - t0
+    e2e_wall = job_seconds(time.perf_counter() - t0, dist)
+    units = gather_units(n * st.steps, dist)
 
     if rank != 0:
         if dist:
             dist.barrier()
         return 0
-    value = ws * n * st.steps / t_max
+    value = job_rate(units, t_max)
     peaks, peak_kind = measured_peaks()
     # dominant kernel and its roofline
     dom = max(kt.items(), key=lambda kv: kv[1][1])
@@ -415,7 +410,8 @@ def run_mlh(args):
             "clocks": ck,
             "tuning": tuning,
             **extra,
-            "e2e": {"value": ws * n * e2e_steps / e2e_wall, "unit": "particle-updates/s",
+            "e2e": {"value": job_rate([u / st.steps * e2e_steps for u in units], e2e_wall),
+                    "unit": "particle-updates/s",
                     "h2d_bytes_per_step": used * 8 * n, "d2h_bytes_per_step": used * 8 * n,
                     "steps": e2e_steps},
             "peaks": {"source": peak_kind, "hbm_gbs": peaks.get("hbm_gbs")}}
