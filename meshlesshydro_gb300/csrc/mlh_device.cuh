@@ -36,6 +36,10 @@ enum : unsigned {
 // the concatenated cell array of all simulations of a context.
 struct GridInfo {
     double lo[3], hi[3], cs[3];
+    // ghost bands of the periodic box: a coordinate x has an image when
+    // x <= band_lo = lo + h or band_hi = hi - h < x (Particles.cpp:2123-2142)
+    double band_lo[3], band_hi[3];
+    float Lf[3];           // box lengths hi - lo in single precision (pre-filter)
     int cells[3];
     int ncells;
     int cell_base;
@@ -108,15 +112,26 @@ struct Harvest {
 // Kernel::cubicSpline, demonstrator/src/Particles.cpp:7-24, for a support
 // radius h: ih2 = 2 / h and sigma computed with the reference's expression
 // (kernel_sigma); q = r / (h/2) is taken as r * (2/h) (within an ulp of the
-// quotient) and pow(2-q, 3.) is written as a product.
+// quotient) and pow(2-q, 3.) is written as a product.  The two pieces run as
+// the same five operations with selected operands, so that a warp whose
+// lanes fall on both sides of q = 1 issues them once:
+//   q <= 1:     sigma   * fma(-(1.5 q) q, t, 1),  t = fma(-0.5, q, 1) = 1 - q/2
+//   1 < q < 2:  sigma/4 * fma((t t) t, 1, 0),     t = fma(-1, q, 2) = 2 - q
+// (fma(z, 1, 0) = z for z >= 0, and sigma/4 is exact), each the value of the
+// reference's expression for its piece.
 __device__ __forceinline__ double kernelW2(double r, double ih2, double sigma) {
     // r >= 0, so q >= 0 and the range tests compare bit patterns (integer
     // pipe): q <= 1 and q < 2
-    const double q = r * ih2;
+    const double q = __dmul_rn(r, ih2);
     const long long qb = __double_as_longlong(q);
-    if (qb <= 0x3FF0000000000000ll) return sigma * (1. - 3. / 2. * q * q * (1. - q / 2.));
-    if (qb < 0x4000000000000000ll) { double t = 2. - q; return sigma / 4. * (t * t * t); }
-    return 0.;
+    const bool inner = qb <= 0x3FF0000000000000ll;
+    const double t = __fma_rn(inner ? -0.5 : -1., q, inner ? 1. : 2.);
+    const double y = __dmul_rn(inner ? 1.5 : t, inner ? q : t);
+    const double z = __dmul_rn(y, inner ? q : t);
+    const double zs = __longlong_as_double(__double_as_longlong(z) ^ (inner ? (long long)0x8000000000000000ull : 0ll));
+    const double w = __fma_rn(zs, inner ? t : 1., inner ? 1. : 0.);
+    const double W = __dmul_rn(inner ? sigma : 0.25 * sigma, w);
+    return qb < 0x4000000000000000ll ? W : 0.;
 }
 __device__ __forceinline__ double kernelW(double r, const Member &mb) { return kernelW2(r, mb.ih2, mb.sigma); }
 // Particles.cpp:10-15 (the value of the kernel at r = 0 is sigma)
@@ -146,15 +161,6 @@ __device__ __forceinline__ void hsolve_shape(double r, double ihh2, double &f, d
     }
 }
 
-// Ghost image coordinate, Particles.cpp:2123-2142.
-__device__ __forceinline__ bool in_band(double xa, double lo, double hi, double h) {
-    return xa <= lo + h || hi - h < xa;
-}
-__device__ __forceinline__ double image_coord(double xa, double lo, double hi, double h) {
-    if (xa <= lo + h) return hi + (xa - lo);
-    return lo - (hi - xa);
-}
-
 // abs() as bound by the reference's limiter code (fabs, or int abs(int) with
 // x86 conversion semantics: NaN / out of range -> INT_MIN, abs(INT_MIN) = INT_MIN).
 __device__ __forceinline__ double ref_abs(double x, int int_abs) {
@@ -180,6 +186,22 @@ __device__ __forceinline__ double key_double(long long k) {
 }
 __device__ __forceinline__ bool dlt(double a, double b) { return ord_key(a) < ord_key(b); }
 __device__ __forceinline__ bool dneg(double x) { return ord_key(x) < 0; }   // x < 0
+
+// Ghost image coordinate, Particles.cpp:2123-2142: a coordinate in the
+// lower band (x <= lo + h) is mirrored to hi + (x - lo), one in the upper
+// band (hi - h < x) to lo - (hi - x) = lo + (x - hi) (the same double: RN
+// rounding is symmetric).  The band limits are precomputed in GridInfo and
+// compared as order-preserving integer keys (ord_key), so neither
+// test nor mirror takes FP64 compares; the mirror is two additions with
+// selected operands.
+__device__ __forceinline__ bool in_band(double xa, const GridInfo &g, int a) {
+    const long long k = ord_key(xa);
+    return k <= ord_key(g.band_lo[a]) || ord_key(g.band_hi[a]) < k;
+}
+__device__ __forceinline__ double image_coord(double xa, const GridInfo &g, int a) {
+    const bool low = ord_key(xa) <= ord_key(g.band_lo[a]);
+    return __dadd_rn(low ? g.hi[a] : g.lo[a], __dsub_rn(xa, low ? g.lo[a] : g.hi[a]));
+}
 
 // Reciprocal and reciprocal square root by Newton-Raphson iteration from the
 // hardware estimates of PTX rcp.approx.ftz.f64 / rsqrt.approx.ftz.f64: each

@@ -232,6 +232,11 @@ __global__ void k_bounds_final(const double *__restrict__ x, const double *__res
             total *= ci;
         }
         for (int a = 0; a < D; ++a) g.cs[a] = (g.hi[a] - g.lo[a]) / (double)g.cells[a];
+        for (int a = 0; a < 3; ++a) {
+            g.band_lo[a] = g.lo[a] + mb.h;
+            g.band_hi[a] = g.hi[a] - mb.h;
+            g.Lf[a] = (float)(g.hi[a] - g.lo[a]);
+        }
         if (total > p.ncells_cap) { flag(status, ST_CAPACITY); total = 1; }
         g.ncells = (int)total;
         g.cell_base = 0;
@@ -331,7 +336,7 @@ constexpr int NNS_WARPS = 8;
 struct NnsCells {
     int excl[27], start[27];
     unsigned wrap[27];
-    int shift[27][3];   // stencil offset of a wrapped axis (-1 or +1), else 0
+    float shift[27][3];   // image shift of a wrapped axis (-L or +L, single precision), else 0
 };
 
 // shared memory of k_neighbours: NNS_WARPS NnsCells, then per warp the
@@ -361,9 +366,6 @@ __device__ __forceinline__ int nns_candidates(const Params &p, const GridInfo &g
     constexpr int NC = D == 3 ? 27 : 9;
     const int lane = threadIdx.x & 31;
     const unsigned lt_mask = (1u << lane) - 1u;
-    float Lf[3];
-#pragma unroll
-    for (int a = 0; a < 3; ++a) Lf[a] = (float)(g.hi[a] - g.lo[a]);
     const int ic = cell[i] - g.cell_base;
     const int ix = ic % g.cells[0];
     const int iy = (ic / g.cells[0]) % g.cells[1];
@@ -371,7 +373,7 @@ __device__ __forceinline__ int nns_candidates(const Params &p, const GridInfo &g
     // --- stencil cells in the reference's order, lane k holds cell k
     int cnt = 0, start = 0;
     unsigned wrap = 0;
-    int sh[3] = {0, 0, 0};
+    float sh[3] = {0.f, 0.f, 0.f};
     if (lane < NC) {
         int off[3] = {D == 3 ? lane / 9 - 1 : lane / 3 - 1, D == 3 ? (lane / 3) % 3 - 1 : lane % 3 - 1,
                       D == 3 ? lane % 3 - 1 : 0};
@@ -383,7 +385,7 @@ __device__ __forceinline__ int nns_candidates(const Params &p, const GridInfo &g
                 if (!p.periodic) skip = true;
                 cc[a] = cc[a] < 0 ? cc[a] + g.cells[a] : cc[a] - g.cells[a];
                 wrap |= 1u << a;
-                sh[a] = off[a];
+                sh[a] = off[a] < 0 ? -g.Lf[a] : g.Lf[a];
             }
         }
         if (!skip) {
@@ -429,9 +431,9 @@ __device__ __forceinline__ int nns_candidates(const Params &p, const GridInfo &g
                 float4 fj = posf[j];
                 float dx = fj.x - fi.x, dy = fj.y - fi.y, dz = fj.z - fi.z;
                 if (wr) {
-                    dx += (float)cs->shift[k][0] * Lf[0];
-                    dy += (float)cs->shift[k][1] * Lf[1];
-                    if (D == 3) dz += (float)cs->shift[k][2] * Lf[2];
+                    dx += cs->shift[k][0];
+                    dy += cs->shift[k][1];
+                    if (D == 3) dz += cs->shift[k][2];
                 }
                 float d2f = dx * dx + dy * dy + (D == 3 ? dz * dz : 0.f);
                 pass = d2f <= mb.hsq_f;
@@ -479,16 +481,26 @@ __global__ void __launch_bounds__(NNS_WARPS * 32, MLH_NNS_MINB) k_neighbours(
     const double *X[3] = {x, y, z};
     const int gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const int nw = (gridDim.x * blockDim.x) >> 5;
-    // density, pressure, 1/omega and sound speed of particle bi (per lane)
-    int bi = -1, iter = 0;
-    double bomega = 0.;
+    // omega, density, pressure, 1/omega and sound speed of particle bi (per
+    // lane): omega sums the stored W of the real neighbours in list order,
+    // then W(0), then the images (Particles::compDensity, Particles.cpp:
+    // 1151-1184, and its image part :2262-2290, in that order)
+    int bi = -1, bnr = 0, bni = 0, iter = 0;
+    double bw0 = 0.;
     auto finish = [&]() {
         if (bi < 0) return;
+        const double *wb = ww + (size_t)bi * K;
+        double bomega = 0.;
+        for (int s = 0; s < bnr; ++s) bomega += wb[s];
+        bomega += bw0;
+        for (int s = bnr; s < bnr + bni; ++s) bomega += wb[s];
         const double rho = m[bi] * bomega;
         const double P = (p.gamma - 1.) * rho * u[bi];
+        // rho <= 0 and P <= 0 as sign tests on the bit patterns (a NaN with
+        // the sign bit set also counts)
         unsigned st = 0;
-        if (rho <= 0.) st |= ST_NEG_DENSITY;
-        if (P <= 0.) st |= ST_NEG_PRESSURE;
+        if (__double_as_longlong(rho) <= 0) st |= ST_NEG_DENSITY;
+        if (__double_as_longlong(P) <= 0) st |= ST_NEG_PRESSURE;
         if (st) flag(status, st);
         Prim pr;
         pr.x = x[bi]; pr.y = y[bi]; pr.z = D == 3 ? z[bi] : 0.;
@@ -508,7 +520,6 @@ __global__ void __launch_bounds__(NNS_WARPS * 32, MLH_NNS_MINB) k_neighbours(
         // --- phase 2: exact FP64 test, r, W.  With per-particle smoothing
         // lengths the pair test is r^2 < max(h_i^2, h_j^2) and W uses h_i.
         int nr = 0, ni = 0, fc = 0;
-        double wsumR = 0., wsumI = 0.;
         const size_t base = (size_t)i * K;
         double hsq_i = mb.hsq, ih2_i = mb.ih2, sigma_i = mb.sigma, w0_i = mb.w0;
         if (p.adaptive_h) {
@@ -538,7 +549,7 @@ __global__ void __launch_bounds__(NNS_WARPS * 32, MLH_NNS_MINB) k_neighbours(
                 for (int a = 0; a < D; ++a) {
                     xj[a] = X[a][j];
                     if (wr & (1u << a)) {
-                        if (in_band(xj[a], g.lo[a], g.hi[a], mb.h)) xj[a] = image_coord(xj[a], g.lo[a], g.hi[a], mb.h);
+                        if (in_band(xj[a], g, a)) xj[a] = image_coord(xj[a], g, a);
                         else ok = false;
                     }
                 }
@@ -565,12 +576,10 @@ __global__ void __launch_bounds__(NNS_WARPS * 32, MLH_NNS_MINB) k_neighbours(
             if (pass && !img) {
                 const int pos = nr + __popc(balR & lt_mask);
                 if (pos < K) { nbr[base + pos] = e; rr[base + pos] = r; ww[base + pos] = w; }
-                wsumR += w;
             }
             if (pass && img) {
                 const int pos = ni + __popc(balI & lt_mask);
                 if (pos < K) { imgE[pos] = e; imgR[pos] = r; imgW[pos] = w; }
-                wsumI += w;
             }
             nr += __popc(balR);
             ni += __popc(balI);
@@ -595,13 +604,8 @@ __global__ void __launch_bounds__(NNS_WARPS * 32, MLH_NNS_MINB) k_neighbours(
         // canonical faces among the stored slots (neighbour or parent > i);
         // counted from the final list so that it matches k_link exactly
         for (int t = lane; t < nr + ni; t += 32) fc += (int)(nbr[base + t] & IDX_MASK) > i;
-        // --- omega = W(0) + sum over the neighbours (real and images)
-        double wsum = wsumR + wsumI;
 #pragma unroll
-        for (int o = 16; o > 0; o >>= 1) {
-            wsum += __shfl_xor_sync(0xffffffffu, wsum, o);
-            fc += __shfl_xor_sync(0xffffffffu, fc, o);
-        }
+        for (int o = 16; o > 0; o >>= 1) fc += __shfl_xor_sync(0xffffffffu, fc, o);
         if (lane == 0) {
             if (overflow) flag(status, ST_NGB_OVERFLOW);
             if (nr + ni == 0) flag(status, ST_NO_NEIGHBOUR);
@@ -610,8 +614,9 @@ __global__ void __launch_bounds__(NNS_WARPS * 32, MLH_NNS_MINB) k_neighbours(
             faceCnt[i] = fc;
         }
         // the floating-point tail of every 32 particles of this warp runs
-        // once on all 32 lanes (lane k keeps the k-th particle)
-        if (lane == (iter & 31)) { bi = i; bomega = wsum + w0_i; }
+        // once on all 32 lanes (lane k keeps the k-th particle); the stored
+        // slots are visible to every lane after the __syncwarp above
+        if (lane == (iter & 31)) { bi = i; bnr = nr; bni = ni; bw0 = w0_i; }
         if ((iter & 31) == 31) { finish(); bi = -1; }
         ++iter;
         __syncwarp();
@@ -696,7 +701,7 @@ __global__ void __launch_bounds__(NNS_WARPS * 32) k_hsolve(
                 for (int a = 0; a < D; ++a) {
                     xj[a] = X[a][j];
                     if (wr & (1u << a)) {
-                        if (in_band(xj[a], g.lo[a], g.hi[a], mb.h)) xj[a] = image_coord(xj[a], g.lo[a], g.hi[a], mb.h);
+                        if (in_band(xj[a], g, a)) xj[a] = image_coord(xj[a], g, a);
                         else ok = false;
                     }
                 }
@@ -841,12 +846,12 @@ __global__ void k_dt_final(Params p, int nmembers, const unsigned long long *__r
 // psi~_j(x_i) = B_i (x_j - x_i) W_ij / omega_i; Particles::slopeLimiter
 // (:1313-1444) with the face midpoint x_ij = (x_i + x_j)/2.
 template <int D>
-__device__ __forceinline__ void neighbour_pos(uint32_t e, const Prim &pj, const GridInfo &g, double h, double *xj) {
+__device__ __forceinline__ void neighbour_pos(uint32_t e, const Prim &pj, const GridInfo &g, double *xj) {
     xj[0] = pj.x; xj[1] = pj.y; if (D == 3) xj[2] = pj.z;
     if (e >> IMG_SHIFT) {
 #pragma unroll
         for (int a = 0; a < D; ++a)
-            if (e & (1u << (IMG_SHIFT + a))) xj[a] = image_coord(xj[a], g.lo[a], g.hi[a], h);
+            if (e & (1u << (IMG_SHIFT + a))) xj[a] = image_coord(xj[a], g, a);
     }
 }
 
@@ -910,7 +915,7 @@ __global__ void __launch_bounds__(256) k_gradients(Params p, const Member *__res
             const uint32_t e = nbr[base + s];
             const Prim pj = prim[e & IDX_MASK];
             double xj[3];
-            neighbour_pos<D>(e, pj, g, h, xj);
+            neighbour_pos<D>(e, pj, g, xj);
             const double psij = ww[base + s] * Vi;
             double d[3], dp[3];
 #pragma unroll
@@ -933,7 +938,7 @@ __global__ void __launch_bounds__(256) k_gradients(Params p, const Member *__res
             const uint32_t e = nbr[base + s];
             const Prim pj = prim[e & IDX_MASK];
             double xj[3];
-            neighbour_pos<D>(e, pj, g, h, xj);
+            neighbour_pos<D>(e, pj, g, xj);
             const double psij = ww[base + s] * Vi;
             double d[3], ps[3];
 #pragma unroll
@@ -978,7 +983,7 @@ __global__ void __launch_bounds__(256) k_gradients(Params p, const Member *__res
                 const uint32_t e = nbr[base + s];
                 const Prim pj = prim[e & IDX_MASK];
                 double xj[3], d[3];
-                neighbour_pos<D>(e, pj, g, h, xj);
+                neighbour_pos<D>(e, pj, g, xj);
                 // face point x_ij = x_i + c (x_j - x_i): c = 1/2 (first-order
                 // quadrature point) or h/4 (the reference's other choice)
                 const double cq = p.foqp ? .5 : hq / 4.;
@@ -1288,7 +1293,7 @@ __global__ void MLH_FACE_BOUNDS k_faces(Params p, const Member *__restrict__ mem
         const Prim pi = prim[i], pj = prim[j];
         const double Vi = geo[i].V, Vj = geo[j].V;
         double xi[3] = {pi.x, pi.y, pi.z}, xj[3];
-        if (img) neighbour_pos<D>(e, pj, grids[mi], h, xj);
+        if (img) neighbour_pos<D>(e, pj, grids[mi], xj);
         else { xj[0] = pj.x; xj[1] = pj.y; xj[2] = pj.z; }
         // --- effective face
         {
@@ -1556,11 +1561,13 @@ __global__ void __launch_bounds__(256) k_update(Params p, const int *__restrict_
             if (fo == 0 || (fo > 0 ? fo : -fo) > p.faces_cap) continue;
             const double2 *src = reinterpret_cast<const double2 *>(Fface + (size_t)((fo > 0 ? fo : -fo) - 1) * 6);
             const double2 a = src[0], b = src[1], c = src[2];
-            if (fo > 0) {
-                mF += a.x; vF[0] += b.x; vF[1] += b.y; if (D == 3) vF[2] += c.x; eF += a.y;
-            } else {
-                mF += -a.x; vF[0] += -b.x; vF[1] += -b.y; if (D == 3) vF[2] += -c.x; eF += -a.y;
-            }
+            // the flux with the slot's sign: the sign bit flipped on the
+            // integer pipe for a copied face, so that both kinds of slot
+            // share one set of additions (x + (-f) is the same double as
+            // adding the negated flux)
+            const long long sg = fo > 0 ? 0ll : (long long)0x8000000000000000ull;
+            auto sgn = [sg](double f) { return __longlong_as_double(__double_as_longlong(f) ^ sg); };
+            mF += sgn(a.x); vF[0] += sgn(b.x); vF[1] += sgn(b.y); if (D == 3) vF[2] += sgn(c.x); eF += sgn(a.y);
         }
         if (fluxSums) {
             fluxSums[(size_t)i * 5 + 0] = mF;
@@ -1600,9 +1607,10 @@ __global__ void __launch_bounds__(256) k_update(Params p, const int *__restrict_
             if (p.move) {
                 xa += vo[a] * dt;
                 if (p.periodic) {
+                    // the box tests on integer keys (ord_key), off the FP64 pipe
                     const double lo = grids[sim].lo[a], hi = grids[sim].hi[a];
-                    if (xa < lo) xa = hi - (lo - xa);
-                    else if (hi <= xa) xa = lo + (xa - hi);
+                    if (dlt(xa, lo)) xa = hi - (lo - xa);
+                    else if (!dlt(xa, hi)) xa = lo + (xa - hi);
                 }
                 X[a][i] = xa;
             }
