@@ -259,6 +259,11 @@ __device__ __forceinline__ void pressure_fn5(const RiemannSide &s, double p, dou
     }
 }
 
+// x with its sign bit flipped when f (integer pipe; exact negation)
+__device__ __forceinline__ double flip_if(double x, bool f) {
+    return __longlong_as_double(__double_as_longlong(x) ^ ((long long)f << 63));
+}
+
 // Same solution as riemann_exact for gamma = 5/3 with cheaper arithmetic:
 // fifth roots instead of pow, integer powers for g3, g4 and 1/gamma,
 // reciprocals by Newton-Raphson (frcp), f_K(p*) from the last Newton
@@ -270,23 +275,45 @@ __device__ __forceinline__ void pressure_fn5(const RiemannSide &s, double p, dou
 // converged after that many steps, return unsolved (flag 2, pstar = the
 // current iterate, iters = steps run); solving again with that iterate as
 // `guess` continues the same iteration with the same arithmetic.
+//
+// Two mirror images keep the lanes of a warp on one branch (a warp issues
+// every branch that any of its lanes takes, and on this GPU an FP64
+// instruction costs the same with one active lane as with 32).  The Euler
+// equations are symmetric under swapping the sides and negating the
+// velocities: p* is unchanged and u* and the sampled velocity change sign.
+// (1) Newton solves the problem with the lower pressure on the left (A) and
+// the higher on the right (B).  It performs the same operations on the same
+// operands as for the unsorted problem, with the two sides' terms added in
+// the other order (IEEE addition commutes, and uR - uL is unchanged), so p*
+// is the same double.  In the weak-wave faces that make up most of a step,
+// p* lies between pL and pR: A is a shock and B a rarefaction in nearly
+// every lane, where the unsorted problem splits each side's branch of
+// pressure_fn5 at random.  (2) The solution is sampled at S = 0 by the
+// left-side logic only: on the left state as given when the contact moves
+// right (u* >= 0), on the mirror image of the right state otherwise.  Every
+// speed of the mirrored sampling is the exact negation of the right-side
+// speed it stands for, and the ties at zero are resolved as the right-side
+// tests resolve them, so the sampled state is the one of the two-sided
+// sampling (Toro section 4.5).
 __device__ inline RiemannResult riemann_exact5(const RiemannConsts &k, double rhoL, double uL, double pL,
                                                double rhoR, double uR, double pR, double guess = -1.,
                                                double defer_above = 0., int first_iters = 0) {
     RiemannResult res;
-    const RiemannSide L = make_side(k, rhoL, uL, pL), R = make_side(k, rhoR, uR, pR);
-    if (!dlt(uR - uL, k.g4 * (L.c + R.c))) {   // g4 (cL + cR) <= uR - uL: vacuum
+    const bool mir = dlt(pR, pL);
+    const RiemannSide A = make_side(k, mir ? rhoR : rhoL, mir ? flip_if(uR, true) : uL, mir ? pR : pL);
+    const RiemannSide B = make_side(k, mir ? rhoL : rhoR, mir ? flip_if(uL, true) : uR, mir ? pL : pR);
+    if (!dlt(B.u - A.u, k.g4 * (A.c + B.c))) {   // g4 (cL + cR) <= uR - uL: vacuum
         res.rho = 0.; res.u = 0.; res.p = 0.; res.pstar = 0.; res.flag = 0; res.iters = 0;
         return res;
     }
-    const double du = uR - uL;
-    const double pfloor = 1e-12 * (nn_le(pL, pR) ? pR : pL);
+    const double du = B.u - A.u;
+    const double pfloor = 1e-12 * B.p;                   // 1e-12 max(pL, pR)
     double p0;
     bool tried_guess = __double_as_longlong(guess) > 0;   // guess > 0 (-1: none)
     if (tried_guess) p0 = guess;
     else {
-        double num = L.c + R.c - k.g7 * du;
-        double den = L.c * rroot5<1>(pL) + R.c * rroot5<1>(pR);
+        double num = A.c + B.c - k.g7 * du;
+        double den = A.c * rroot5<1>(A.p) + B.c * rroot5<1>(B.p);
         double t = fdiv(num, den);
         double t2 = t * t;
         p0 = t2 * t2 * t;
@@ -295,14 +322,14 @@ __device__ inline RiemannResult riemann_exact5(const RiemannConsts &k, double rh
             return res;
         }
     }
-    double p, fLs = 0., fRs = 0., qLs = -1., qRs = -1.;
+    double p, fAs = 0., fBs = 0., qAs = -1., qBs = -1.;
     int iters = -1, extra = 0;
     for (int attempt = 0; attempt < 2 && iters < 0; ++attempt) {
         if (attempt == 1) {
             if (!tried_guess) break;
             extra = k.max_iter;
-            double num = L.c + R.c - k.g7 * du;
-            double den = L.c * rroot5<1>(pL) + R.c * rroot5<1>(pR);
+            double num = A.c + B.c - k.g7 * du;
+            double den = A.c * rroot5<1>(A.p) + B.c * rroot5<1>(B.p);
             double t = fdiv(num, den);
             double t2 = t * t;
             p0 = t2 * t2 * t;
@@ -310,22 +337,22 @@ __device__ inline RiemannResult riemann_exact5(const RiemannConsts &k, double rh
         p = nn_le(p0, pfloor) ? pfloor : p0;
         for (int it = 1; it <= k.max_iter; ++it) {
             double invp = frcp(p);
-            double fL, fdL, qL, fR, fdR, qR;
-            bool rL, rR;
-            pressure_fn5(L, p, invp, fL, fdL, qL, rL);
-            pressure_fn5(R, p, invp, fR, fdR, qR, rR);
-            double pnew = p - (fL + fR + du) * frcp(fdL + fdR);
+            double fA, fdA, qA, fB, fdB, qB;
+            bool rA, rB;
+            pressure_fn5(A, p, invp, fA, fdA, qA, rA);
+            pressure_fn5(B, p, invp, fB, fdB, qB, rB);
+            double pnew = p - (fA + fB + du) * frcp(fdA + fdB);
             {   // !(pnew > 0): zero, negative or NaN (bit patterns)
                 const long long pb = __double_as_longlong(pnew);
                 if (pb <= 0 || pb > 0x7FF0000000000000ll) pnew = pfloor;
             }
             double dp = pnew - p;
             if (nn_le(2. * fabs(dp), k.tol * (pnew + p))) {
-                fLs = fL + fdL * dp;
-                fRs = fR + fdR * dp;
+                fAs = fA + fdA * dp;
+                fBs = fB + fdB * dp;
                 double rel = dp * invp;
-                qLs = rL ? qL + qL * (k.g1 * rel) : -1.;
-                qRs = rR ? qR + qR * (k.g1 * rel) : -1.;
+                qAs = rA ? qA + qA * (k.g1 * rel) : -1.;
+                qBs = rB ? qB + qB * (k.g1 * rel) : -1.;
                 p = pnew;
                 iters = it;
                 break;
@@ -340,62 +367,52 @@ __device__ inline RiemannResult riemann_exact5(const RiemannConsts &k, double rh
     const double pstar = p;
     res.pstar = pstar;
     if (iters < 0) {
-        double invp = frcp(pstar), fdL, fdR, qL, qR;
-        bool rL, rR;
-        pressure_fn5(L, pstar, invp, fLs, fdL, qL, rL);
-        pressure_fn5(R, pstar, invp, fRs, fdR, qR, rR);
-        qLs = rL ? qL : -1.;
-        qRs = rR ? qR : -1.;
+        double invp = frcp(pstar), fdA, fdB, qA, qB;
+        bool rA, rB;
+        pressure_fn5(A, pstar, invp, fAs, fdA, qA, rA);
+        pressure_fn5(B, pstar, invp, fBs, fdB, qB, rB);
+        qAs = rA ? qA : -1.;
+        qBs = rB ? qB : -1.;
         res.iters = -1;
     } else {
         res.iters = iters + extra;
     }
-    const double ustar = .5 * (uL + uR) + .5 * (fRs - fLs);
+    // u* of the given problem (the sorted one's, negated when mirrored)
+    const double ustar = flip_if(.5 * (A.u + B.u) + .5 * (fBs - fAs), mir);
+    // --- sampling at S = 0: side s of the contact, as the left side
+    const bool right = dneg(ustar);               // u* < 0: the right state
+    const bool useB = right != mir;               // where side s sits in the sorted problem
+    const double rho_s = useB ? B.rho : A.rho, p_s = useB ? B.p : A.p, c_s = useB ? B.c : A.c;
+    const double invp_s = useB ? B.invp : A.invp, q_s = useB ? qBs : qAs;
+    // the side's velocity, mirrored for the right side: the sorted problem
+    // holds it negated when mirrored, so the two flips combine into useB
+    const double u_s = flip_if(useB ? B.u : A.u, useB);
+    const double ustar_s = flip_if(ustar, right);
     double rho, u, pp;
-    if (!dneg(ustar)) {
-        if (nn_le(pstar, pL)) {
-            double shl = uL - L.c;
-            if (!dneg(shl)) { rho = rhoL; u = uL; pp = pL; }
+    if (nn_le(pstar, p_s)) {                      // rarefaction on side s
+        const double sh = __dsub_rn(u_s, c_s);    // head speed
+        if (!dneg(sh)) { rho = rho_s; u = u_s; pp = p_s; }
+        else {
+            const double q = !dneg(q_s) ? q_s : root5(pstar * invp_s);
+            const double st = __fma_rn(-c_s, q, ustar_s);   // tail speed
+            // tail < 0 puts S = 0 in the star region (left side); the right
+            // side's test, tail >= 0 there, reads tail <= 0 mirrored
+            const long long kst = ord_key(st);
+            if (right ? kst <= 0 : kst < 0) { rho = rho_s * (q * q * q); u = ustar_s; pp = pstar; }
             else {
-                double q = !dneg(qLs) ? qLs : root5(pstar * L.invp);
-                double stl = ustar - L.c * q;
-                if (dneg(stl)) { rho = rhoL * (q * q * q); u = ustar; pp = pstar; }
-                else {
-                    double cf = k.g5 * (L.c + k.g7 * uL);
-                    double r = fdiv(cf, L.c), r3 = r * r * r;
-                    u = cf; rho = rhoL * r3; pp = pL * (r3 * r * r);
-                }
-            }
-        } else {
-            double pml = pstar * L.invp;
-            double sl = uL - L.c * sqrt(k.g2 * pml + k.g1);
-            if (!dneg(sl)) { rho = rhoL; u = uL; pp = pL; }
-            else { rho = rhoL * fdiv(pml + k.g6, pml * k.g6 + 1.); u = ustar; pp = pstar; }
-        }
-        res.flag = -1;
-    } else {
-        if (!nn_le(pstar, pR)) {
-            double pmr = pstar * R.invp;
-            double sr = uR + R.c * sqrt(k.g2 * pmr + k.g1);
-            if (ord_key(sr) <= 0) { rho = rhoR; u = uR; pp = pR; }
-            else { rho = rhoR * fdiv(pmr + k.g6, pmr * k.g6 + 1.); u = ustar; pp = pstar; }
-        } else {
-            double shr = uR + R.c;
-            if (ord_key(shr) <= 0) { rho = rhoR; u = uR; pp = pR; }
-            else {
-                double q = !dneg(qRs) ? qRs : root5(pstar * R.invp);
-                double str = ustar + R.c * q;
-                if (!dneg(str)) { rho = rhoR * (q * q * q); u = ustar; pp = pstar; }
-                else {
-                    double cf = k.g5 * (R.c - k.g7 * uR);
-                    double r = fdiv(cf, R.c), r3 = r * r * r;
-                    u = -cf; rho = rhoR * r3; pp = pR * (r3 * r * r);
-                }
+                const double cf = k.g5 * __fma_rn(k.g7, u_s, c_s);
+                const double r = fdiv(cf, c_s), r3 = r * r * r;
+                u = cf; rho = rho_s * r3; pp = p_s * (r3 * r * r);
             }
         }
-        res.flag = 1;
+    } else {                                      // shock on side s
+        const double pm = pstar * invp_s;
+        const double sl = __fma_rn(-c_s, sqrt(k.g2 * pm + k.g1), u_s);   // shock speed
+        if (!dneg(sl)) { rho = rho_s; u = u_s; pp = p_s; }
+        else { rho = rho_s * fdiv(pm + k.g6, pm * k.g6 + 1.); u = ustar_s; pp = pstar; }
     }
-    res.rho = rho; res.u = u; res.p = pp;
+    res.flag = right ? 1 : -1;
+    res.rho = rho; res.u = flip_if(u, right); res.p = pp;
     return res;
 }
 
