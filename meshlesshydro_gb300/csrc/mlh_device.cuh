@@ -78,12 +78,12 @@ struct Params {
 struct Prim {       // positions, primitive state of this step
     double x, y, z, rho, vx, vy, vz, P;
 };
-struct Grad {       // limited gradients: rho, vx, vy, vz, P (x,y,z each) + pad
+struct Grad {       // limited gradients: rho, vx, vy, vz, P (x,y,z each), div v
     double g[16];
 };
-struct Geo {        // E_i^{-1}, 1/omega_i, omega_i, sound speed
+struct Geo {        // E_i^{-1}, 1/omega_i, omega_i, sound speed, 1/rho_i
     double B[9];
-    double V, omega, c;
+    double V, omega, c, irho;
 };
 struct FaceRef {    // canonical face: owner i, slot index, reverse slot (images)
     int i, slot, rslot, pad;

@@ -509,7 +509,9 @@ __global__ void __launch_bounds__(NNS_WARPS * 32, MLH_NNS_MINB) k_neighbours(
         prim[bi] = pr;
         geo[bi].omega = bomega;
         geo[bi].V = frcp(bomega);
-        geo[bi].c = sqrt(p.gamma * P * frcp(rho));
+        const double irho = frcp(rho);   // also the face kernel's 1/rho_i
+        geo[bi].irho = irho;
+        geo[bi].c = sqrt(p.gamma * P * irho);
     };
     for (int i = gw; i < p.n; i += nw) {
         const int mi = memberOf ? memberOf[i] : 0;
@@ -1026,6 +1028,8 @@ __global__ void __launch_bounds__(256) k_gradients(Params p, const Member *__res
 #pragma unroll
             for (int a = 0; a < D; ++a) go.g[slot * 3 + a] = gr[f][a];
         }
+        // div v of the limited gradients, in the face kernel's order
+        go.g[15] = D == 3 ? (go.g[3] + go.g[7]) + go.g[11] : go.g[3] + go.g[7];
         grad[i] = go;
 #pragma unroll
         for (int k = 0; k < D * D; ++k) geo[i].B[k] = E[k];
@@ -1314,8 +1318,9 @@ __global__ void MLH_FACE_BOUNDS k_faces(Params p, const Member *__restrict__ mem
         for (int a = 0; a < D; ++a) {
             xjxi[a] = xj[a] - xi[a];
             if (p.foqp) {
-                xijxj[a] = .5 * (xi[a] - xj[a]);
-                xijxi[a] = .5 * (xj[a] - xi[a]);
+                // .5 (x_j - x_i), and .5 (x_i - x_j) is its exact negation
+                xijxi[a] = .5 * xjxi[a];
+                xijxj[a] = -xijxi[a];
             } else {
                 double xij = xi[a] + hq / 4. * xjxi[a];
                 xijxi[a] = xij - xi[a];
@@ -1374,11 +1379,11 @@ __global__ void MLH_FACE_BOUNDS k_faces(Params p, const Member *__restrict__ mem
             }
         }
         {
-            double viDiv = Gi[3 + 0] + Gi[6 + 1];
-            double vjDiv = Gj[3 + 0] + Gj[6 + 1];
-            if (D == 3) { viDiv += Gi[9 + 2]; vjDiv += Gj[9 + 2]; }
+            // div v and 1/rho of both particles, stored once per particle
+            // (gradient pad slot, Geo) with the same arithmetic
+            const double viDiv = Gi[15], vjDiv = Gj[15];
             const double hdt = dt / 2.;
-            const double iri = frcp(pi.rho), irj = frcp(pj.rho);
+            const double iri = geo[i].irho, irj = geo[j].irho;
             const double ui0 = vi[0] - vf[0], ui1 = vi[1] - vf[1], uj0 = vj[0] - vf[0], uj1 = vj[1] - vf[1];
             R[0] -= hdt * (pi.rho * viDiv + ui0 * Gi[0] + ui1 * Gi[1]);
             L[0] -= hdt * (pj.rho * vjDiv + uj0 * Gj[0] + uj1 * Gj[1]);
