@@ -316,19 +316,26 @@ __global__ void k_sort_cells(const int *__restrict__ cellTotal, const int *__res
 // Then Particles::compDensity/compOmega (Particles.cpp:1151-1184, 2262-2290)
 // and compPressure (:1272-1288) for the particle.
 //
-// One warp per particle.  Phase 1: the lanes walk the concatenated member
-// lists of the stencil cells and reject candidates with a single-precision
-// distance test against a bound slightly above h^2; the survivors are
-// compacted with a ballot into a per-warp shared list, keeping the stencil
-// order.  Phase 2: the lanes take the survivors 32 at a time and apply the
-// reference's FP64 test exactly (d^2 = (dx*dx + dy*dy) + dz*dz < h*h, no fused
-// multiply-add), compute r and W(r), and append real neighbours (in order) to
-// the slot list and images to a shared list, which is then placed behind the
-// real neighbours sorted by parent index.
+// One warp per cell: the particles of a cell share the candidate sequence
+// (the stencil cells of their cell, in order), so the warp stages it in
+// shared memory once, 128 candidates at a time (index with image bits, and
+// the single-precision position with the image shift applied), and filters
+// every chunk for a batch of up to NNS_PB particles of the cell against the
+// staged copy: a single-precision distance test against a bound slightly
+// above h^2, survivors compacted with a ballot into the particle's shared
+// list in stencil order.  Then, particle by particle, phase 2: the lanes take
+// the survivors 32 at a time and apply the reference's FP64 test exactly (d^2
+// = (dx*dx + dy*dy) + dz*dz < h*h, no fused multiply-add), compute r and
+// W(r), and append real neighbours (in order) to the slot list and images to
+// a shared list, which is then placed behind the real neighbours sorted by
+// parent index.  The single-precision test only decides which candidates
+// phase 2 sees; it passes every neighbour (its error is far below the bound's
+// margin), so the lists are those of the FP64 test alone.
 constexpr int NNS_WARPS = 8;
+constexpr int NNS_PB = 12;    // particles of a cell filtered per staged chunk
+constexpr int NNS_CH = 128;   // candidates per staged chunk
 // blocks of the neighbour search resident per SM: 3 caps it at 80 registers
-// (a 4-byte spill) and gives 24 warps per SM (measured on the Sedov 128^3
-// step: 9.7 ms with 1, 8.6 ms with 3, 12.3 ms with 4)
+// and gives 24 warps per SM
 #ifndef MLH_NNS_MINB
 #define MLH_NNS_MINB 3
 #endif
@@ -340,37 +347,31 @@ struct NnsCells {
 };
 
 // shared memory of k_neighbours: NNS_WARPS NnsCells, then per warp the
-// candidate list (K + 32 uint32), image r and W (K doubles each) and image
-// entries (K uint32), each rounded up to 16 bytes
+// staged chunk (NNS_CH entries and float4 positions), NNS_PB candidate lists
+// (K + 32 uint32 each) and their counts, image r and W (K doubles each) and
+// image entries (K uint32), each rounded up to 16 bytes
 __host__ __device__ constexpr size_t nns_cells_bytes() {
     return (sizeof(NnsCells) * NNS_WARPS + 15) / 16 * 16;
 }
+__host__ __device__ constexpr size_t nns_r16(size_t b) { return (b + 15) / 16 * 16; }
 __host__ __device__ constexpr size_t nns_warp_bytes(int K) {
-    return ((size_t)(K + 32) * 4 + 15) / 16 * 16 + (size_t)K * 16 + ((size_t)K * 4 + 15) / 16 * 16;
+    return (size_t)NNS_CH * 4 + (size_t)NNS_CH * 16 + nns_r16((size_t)NNS_PB * (K + 32) * 4) +
+           nns_r16((size_t)NNS_PB * 4) + (size_t)K * 16 + nns_r16((size_t)K * 4);
 }
 
-// Candidates of particle i, shared by the neighbour search and the
-// smoothing-length solve: the 3^D stencil cells in the reference's order
+// The 3^D stencil cells of local cell ic in the reference's order
 // (Domain::getNeighborCells, demonstrator/src/Domain.cpp:83-118; lane k
-// holds cell k) written to the warp's NnsCells, then every particle of those
-// cells that passes a single-precision distance pre-filter against the
-// search radius (a conservative bound), in stencil order and ascending index
-// within a cell, appended to cand[] (the entry carries the wrapped axes as
-// image bits).  Returns the number of candidates (at most CAP); `overflow`
-// is set when more passed.
+// holds cell k), written to the warp's NnsCells: the offset of each cell's
+// members in the concatenated sequence, the start of its member list, its
+// wrapped axes and image shift.  Returns the length of the sequence.
 template <int D>
-__device__ __forceinline__ int nns_candidates(const Params &p, const GridInfo &g, const Member &mb, int i,
-                                              const int *__restrict__ cell, const int *__restrict__ cellStart,
-                                              const int *__restrict__ cellList, const float4 *__restrict__ posf,
-                                              NnsCells *cs, uint32_t *cand, int CAP, bool &overflow) {
+__device__ __forceinline__ int nns_stencil(const Params &p, const GridInfo &g, int ic,
+                                           const int *__restrict__ cellStart, NnsCells *cs) {
     constexpr int NC = D == 3 ? 27 : 9;
     const int lane = threadIdx.x & 31;
-    const unsigned lt_mask = (1u << lane) - 1u;
-    const int ic = cell[i] - g.cell_base;
     const int ix = ic % g.cells[0];
     const int iy = (ic / g.cells[0]) % g.cells[1];
     const int iz = D == 3 ? ic / (g.cells[0] * g.cells[1]) : 0;
-    // --- stencil cells in the reference's order, lane k holds cell k
     int cnt = 0, start = 0;
     unsigned wrap = 0;
     float sh[3] = {0.f, 0.f, 0.f};
@@ -408,23 +409,47 @@ __device__ __forceinline__ int nns_candidates(const Params &p, const GridInfo &g
         cs->shift[lane][0] = sh[0]; cs->shift[lane][1] = sh[1]; cs->shift[lane][2] = sh[2];
     }
     __syncwarp();
+    return total;
+}
+
+// Stencil cell of position t of the concatenated sequence: the last cell
+// whose range starts at or before t (empty cells share their offset with the
+// next one), by binary search over the non-decreasing offsets.
+template <int D>
+__device__ __forceinline__ int nns_cell_of(const NnsCells *cs, int t) {
+    constexpr int NC = D == 3 ? 27 : 9;
+    int k = 0;
+#pragma unroll
+    for (int step = 16; step > 0; step >>= 1) {
+        const int kk = k + step;
+        if (kk < NC && cs->excl[kk] <= t) k = kk;
+    }
+    return k;
+}
+
+// Candidates of particle i for the smoothing-length solve: the stencil cells
+// of its cell (nns_stencil), then every particle of those cells that passes
+// the single-precision distance pre-filter against the search radius (a
+// conservative bound), in stencil order and ascending index within a cell,
+// appended to cand[] (the entry carries the wrapped axes as image bits).
+// Returns the number of candidates (at most CAP); `overflow` is set when more
+// passed.
+template <int D>
+__device__ __forceinline__ int nns_candidates(const Params &p, const GridInfo &g, const Member &mb, int i,
+                                              const int *__restrict__ cell, const int *__restrict__ cellStart,
+                                              const int *__restrict__ cellList, const float4 *__restrict__ posf,
+                                              NnsCells *cs, uint32_t *cand, int CAP, bool &overflow) {
+    const int lane = threadIdx.x & 31;
+    const unsigned lt_mask = (1u << lane) - 1u;
+    const int total = nns_stencil<D>(p, g, cell[i] - g.cell_base, cellStart, cs);
     const float4 fi = posf[i];
-    // --- phase 1: single-precision pre-filter, ordered compaction
     int ncand = 0;
     for (int t0 = 0; t0 < total; t0 += 32) {
         const int t = t0 + lane;
         bool pass = false;
         uint32_t ent = 0;
         if (t < total) {
-            // the last cell whose range starts at or before t (empty cells
-            // share their offset with the next one): binary search over the
-            // non-decreasing offsets
-            int k = 0;
-#pragma unroll
-            for (int step = 16; step > 0; step >>= 1) {
-                const int kk = k + step;
-                if (kk < NC && cs->excl[kk] <= t) k = kk;
-            }
+            const int k = nns_cell_of<D>(cs, t);
             const int j = cellList[cs->start[k] + (t - cs->excl[k])];
             const unsigned wr = cs->wrap[k];
             if (wr || j != i) {
@@ -458,11 +483,10 @@ __global__ void __launch_bounds__(NNS_WARPS * 32, MLH_NNS_MINB) k_neighbours(
     const GridInfo *__restrict__ grids, const double *__restrict__ x, const double *__restrict__ y,
     const double *__restrict__ z, const float4 *__restrict__ posf, const double *__restrict__ vx,
     const double *__restrict__ vy, const double *__restrict__ vz, const double *__restrict__ m,
-    const double *__restrict__ u, const int *__restrict__ cell, const int *__restrict__ cellStart,
+    const double *__restrict__ u, const int *__restrict__ cellTotal, const int *__restrict__ cellStart,
     const int *__restrict__ cellList, uint32_t *__restrict__ nbr, double *__restrict__ rr,
     double *__restrict__ ww, int *__restrict__ noi, int *__restrict__ noiImg, int *__restrict__ faceCnt,
     Prim *__restrict__ prim, Geo *__restrict__ geo, unsigned *__restrict__ status) {
-    constexpr int NC = D == 3 ? 27 : 9;
     const int K = p.K;
     const int CAP = K + 32;
     extern __shared__ __align__(16) unsigned char nns_smem[];
@@ -471,10 +495,12 @@ __global__ void __launch_bounds__(NNS_WARPS * 32, MLH_NNS_MINB) k_neighbours(
     // per-warp shared areas; every sub-array starts on a 16-byte boundary
     // whatever K is (see nns_warp_bytes)
     NnsCells *cs = reinterpret_cast<NnsCells *>(nns_smem) + warp;
-    const size_t cand_bytes = ((size_t)CAP * 4 + 15) / 16 * 16;
     unsigned char *wbase = nns_smem + nns_cells_bytes() + (size_t)warp * nns_warp_bytes(K);
-    uint32_t *cand = reinterpret_cast<uint32_t *>(wbase);
-    double *imgR = reinterpret_cast<double *>(wbase + cand_bytes);
+    float4 *stP = reinterpret_cast<float4 *>(wbase);                                  // staged positions
+    uint32_t *stE = reinterpret_cast<uint32_t *>(wbase + (size_t)NNS_CH * 16);        // staged entries
+    uint32_t *candq = stE + NNS_CH;                                                   // NNS_PB lists of CAP
+    int *ncq = reinterpret_cast<int *>(wbase + (size_t)NNS_CH * 20 + nns_r16((size_t)NNS_PB * CAP * 4));
+    double *imgR = reinterpret_cast<double *>(reinterpret_cast<unsigned char *>(ncq) + nns_r16((size_t)NNS_PB * 4));
     double *imgW = imgR + K;
     uint32_t *imgE = reinterpret_cast<uint32_t *>(imgW + K);
 
@@ -513,115 +539,182 @@ __global__ void __launch_bounds__(NNS_WARPS * 32, MLH_NNS_MINB) k_neighbours(
         geo[bi].irho = irho;
         geo[bi].c = sqrt(p.gamma * P * irho);
     };
-    for (int i = gw; i < p.n; i += nw) {
-        const int mi = memberOf ? memberOf[i] : 0;
+    const int ncells = *cellTotal;
+    for (int c = gw; c < ncells; c += nw) {
+        const int c0 = cellStart[c], ncell = cellStart[c + 1] - c0;
+        if (ncell <= 0) continue;
+        const int mi = memberOf ? memberOf[cellList[c0]] : 0;   // a cell holds one member's particles
         const GridInfo g = grids[mi];
         const Member mb = members[mi];
-        bool overflow = false;
-        int ncand = nns_candidates<D>(p, g, mb, i, cell, cellStart, cellList, posf, cs, cand, CAP, overflow);
-        // --- phase 2: exact FP64 test, r, W.  With per-particle smoothing
-        // lengths the pair test is r^2 < max(h_i^2, h_j^2) and W uses h_i.
-        int nr = 0, ni = 0, fc = 0;
-        const size_t base = (size_t)i * K;
-        double hsq_i = mb.hsq, ih2_i = mb.ih2, sigma_i = mb.sigma, w0_i = mb.w0;
-        if (p.adaptive_h) {
-            const double hi_ = p.hp[i];
-            const double h2_i = hi_ / 2.;
-            hsq_i = __dmul_rn(hi_, hi_);
-            ih2_i = 1. / h2_i;
-            sigma_i = kernel_sigma<D>(h2_i);
-            w0_i = sigma_i;
-        }
-        double xi[3] = {0., 0., 0.};
-#pragma unroll
-        for (int a = 0; a < D; ++a) xi[a] = X[a][i];
-        for (int t0 = 0; t0 < ncand; t0 += 32) {
-            const int t = t0 + lane;
-            bool pass = false, img = false;
-            uint32_t e = 0;
-            double r = 0., w = 0.;
-            if (t < ncand) {
-                e = cand[t];
-                const int j = (int)(e & IDX_MASK);
-                const unsigned wr = e >> IMG_SHIFT;
-                img = wr != 0;
-                double xj[3];
-                bool ok = true;
-#pragma unroll
-                for (int a = 0; a < D; ++a) {
-                    xj[a] = X[a][j];
-                    if (wr & (1u << a)) {
-                        if (in_band(xj[a], g, a)) xj[a] = image_coord(xj[a], g, a);
-                        else ok = false;
+        const int total = nns_stencil<D>(p, g, c - g.cell_base, cellStart, cs);
+        for (int b0 = 0; b0 < ncell; b0 += NNS_PB) {
+            const int nb = ncell - b0 < NNS_PB ? ncell - b0 : NNS_PB;
+            // --- phase 1 for the batch: particle q of the batch on lane q
+            int myI = -1;
+            float4 myF = make_float4(0.f, 0.f, 0.f, 0.f);
+            if (lane < nb) { myI = cellList[c0 + b0 + lane]; myF = posf[myI]; }
+            if (lane < NNS_PB) ncq[lane] = 0;
+            __syncwarp();
+            for (int ch = 0; ch < total; ch += NNS_CH) {
+                const int cl = total - ch < NNS_CH ? total - ch : NNS_CH;
+                // stage candidates [ch, ch + cl) of the sequence
+                for (int t = lane; t < cl; t += 32) {
+                    const int k = nns_cell_of<D>(cs, ch + t);
+                    const int j = cellList[cs->start[k] + (ch + t - cs->excl[k])];
+                    const unsigned wr = cs->wrap[k];
+                    float4 fj = posf[j];
+                    if (wr) {
+                        fj.x += cs->shift[k][0];
+                        fj.y += cs->shift[k][1];
+                        if (D == 3) fj.z += cs->shift[k][2];
                     }
+                    stP[t] = fj;
+                    stE[t] = (uint32_t)j | (wr << IMG_SHIFT);
                 }
-                if (ok) {
-                    double ex = __dsub_rn(xj[0], xi[0]), ey = __dsub_rn(xj[1], xi[1]);
-                    double d2 = __dadd_rn(__dmul_rn(ex, ex), __dmul_rn(ey, ey));
-                    if (D == 3) { double ez = __dsub_rn(xj[2], xi[2]); d2 = __dadd_rn(d2, __dmul_rn(ez, ez)); }
-                    // d2, h^2 >= 0: compared as bit patterns on the integer pipe
-                    double lim = mb.hsq;
-                    if (p.adaptive_h) {
-                        const double hj = p.hp[j];
-                        const double hsq_j = __dmul_rn(hj, hj);
-                        lim = __double_as_longlong(hsq_i) < __double_as_longlong(hsq_j) ? hsq_j : hsq_i;
+                __syncwarp();
+                for (int q = 0; q < nb; ++q) {
+                    const uint32_t iq = (uint32_t)__shfl_sync(0xffffffffu, myI, q);
+                    const float fx = __shfl_sync(0xffffffffu, myF.x, q);
+                    const float fy = __shfl_sync(0xffffffffu, myF.y, q);
+                    const float fz = __shfl_sync(0xffffffffu, myF.z, q);
+                    uint32_t *cq = candq + (size_t)q * CAP;
+                    int nq = ncq[q];
+                    for (int t0 = 0; t0 < cl; t0 += 32) {
+                        const int t = t0 + lane;
+                        bool pass = false;
+                        uint32_t ent = 0;
+                        if (t < cl) {
+                            ent = stE[t];
+                            if (ent != iq) {   // the particle itself (its images are candidates)
+                                const float4 fj = stP[t];
+                                const float dx = fj.x - fx, dy = fj.y - fy, dz = fj.z - fz;
+                                const float d2f = dx * dx + dy * dy + (D == 3 ? dz * dz : 0.f);
+                                pass = d2f <= mb.hsq_f;
+                            }
+                        }
+                        const unsigned bal = __ballot_sync(0xffffffffu, pass);
+                        if (pass) {
+                            const int pos = nq + __popc(bal & lt_mask);
+                            if (pos < CAP) cq[pos] = ent;
+                        }
+                        nq += __popc(bal);
                     }
-                    pass = __double_as_longlong(d2) < __double_as_longlong(lim);
-                    if (pass) {
-                        r = sqrt(d2);
-                        w = kernelW2(r, ih2_i, sigma_i);
-                    }
+                    __syncwarp();
+                    if (lane == 0) ncq[q] = nq;
+                    __syncwarp();
                 }
             }
-            const unsigned balR = __ballot_sync(0xffffffffu, pass && !img);
-            const unsigned balI = __ballot_sync(0xffffffffu, pass && img);
-            if (pass && !img) {
-                const int pos = nr + __popc(balR & lt_mask);
-                if (pos < K) { nbr[base + pos] = e; rr[base + pos] = r; ww[base + pos] = w; }
-            }
-            if (pass && img) {
-                const int pos = ni + __popc(balI & lt_mask);
-                if (pos < K) { imgE[pos] = e; imgR[pos] = r; imgW[pos] = w; }
-            }
-            nr += __popc(balR);
-            ni += __popc(balI);
-        }
-        if (nr + ni > K || overflow) {
-            overflow = true;
-            if (nr > K) nr = K;
-            if (ni > K - nr) ni = K - nr;
-        }
-        __syncwarp();
-        // --- images behind the real neighbours, ordered by parent index
-        for (int t = lane; t < ni; t += 32) {
-            const uint32_t e = imgE[t];
-            const uint32_t id = e & IDX_MASK;
-            int rank = 0;
-            for (int q = 0; q < ni; ++q) rank += (imgE[q] & IDX_MASK) < id;
-            nbr[base + nr + rank] = e;
-            rr[base + nr + rank] = imgR[t];
-            ww[base + nr + rank] = imgW[t];
-        }
-        __syncwarp();
-        // canonical faces among the stored slots (neighbour or parent > i);
-        // counted from the final list so that it matches k_link exactly
-        for (int t = lane; t < nr + ni; t += 32) fc += (int)(nbr[base + t] & IDX_MASK) > i;
+            for (int q = 0; q < nb; ++q) {
+                const int i = __shfl_sync(0xffffffffu, myI, q);
+                int ncand = ncq[q];
+                bool overflow = ncand > CAP;
+                if (overflow) ncand = CAP;
+                const uint32_t *cand = candq + (size_t)q * CAP;
+                // --- phase 2: exact FP64 test, r, W.  With per-particle smoothing
+                // lengths the pair test is r^2 < max(h_i^2, h_j^2) and W uses h_i.
+                int nr = 0, ni = 0, fc = 0;
+                const size_t base = (size_t)i * K;
+                double hsq_i = mb.hsq, ih2_i = mb.ih2, sigma_i = mb.sigma, w0_i = mb.w0;
+                if (p.adaptive_h) {
+                    const double hi_ = p.hp[i];
+                    const double h2_i = hi_ / 2.;
+                    hsq_i = __dmul_rn(hi_, hi_);
+                    ih2_i = 1. / h2_i;
+                    sigma_i = kernel_sigma<D>(h2_i);
+                    w0_i = sigma_i;
+                }
+                double xi[3] = {0., 0., 0.};
 #pragma unroll
-        for (int o = 16; o > 0; o >>= 1) fc += __shfl_xor_sync(0xffffffffu, fc, o);
-        if (lane == 0) {
-            if (overflow) flag(status, ST_NGB_OVERFLOW);
-            if (nr + ni == 0) flag(status, ST_NO_NEIGHBOUR);
-            noi[i] = nr;
-            noiImg[i] = ni;
-            faceCnt[i] = fc;
-        }
-        // the floating-point tail of every 32 particles of this warp runs
-        // once on all 32 lanes (lane k keeps the k-th particle); the stored
-        // slots are visible to every lane after the __syncwarp above
-        if (lane == (iter & 31)) { bi = i; bnr = nr; bni = ni; bw0 = w0_i; }
-        if ((iter & 31) == 31) { finish(); bi = -1; }
-        ++iter;
-        __syncwarp();
+                for (int a = 0; a < D; ++a) xi[a] = X[a][i];
+                for (int t0 = 0; t0 < ncand; t0 += 32) {
+                    const int t = t0 + lane;
+                    bool pass = false, img = false;
+                    uint32_t e = 0;
+                    double r = 0., w = 0.;
+                    if (t < ncand) {
+                        e = cand[t];
+                        const int j = (int)(e & IDX_MASK);
+                        const unsigned wr = e >> IMG_SHIFT;
+                        img = wr != 0;
+                        double xj[3];
+                        bool ok = true;
+#pragma unroll
+                        for (int a = 0; a < D; ++a) {
+                            xj[a] = X[a][j];
+                            if (wr & (1u << a)) {
+                                if (in_band(xj[a], g, a)) xj[a] = image_coord(xj[a], g, a);
+                                else ok = false;
+                            }
+                        }
+                        if (ok) {
+                            double ex = __dsub_rn(xj[0], xi[0]), ey = __dsub_rn(xj[1], xi[1]);
+                            double d2 = __dadd_rn(__dmul_rn(ex, ex), __dmul_rn(ey, ey));
+                            if (D == 3) { double ez = __dsub_rn(xj[2], xi[2]); d2 = __dadd_rn(d2, __dmul_rn(ez, ez)); }
+                            // d2, h^2 >= 0: compared as bit patterns on the integer pipe
+                            double lim = mb.hsq;
+                            if (p.adaptive_h) {
+                                const double hj = p.hp[j];
+                                const double hsq_j = __dmul_rn(hj, hj);
+                                lim = __double_as_longlong(hsq_i) < __double_as_longlong(hsq_j) ? hsq_j : hsq_i;
+                            }
+                            pass = __double_as_longlong(d2) < __double_as_longlong(lim);
+                            if (pass) {
+                                r = sqrt(d2);
+                                w = kernelW2(r, ih2_i, sigma_i);
+                            }
+                        }
+                    }
+                    const unsigned balR = __ballot_sync(0xffffffffu, pass && !img);
+                    const unsigned balI = __ballot_sync(0xffffffffu, pass && img);
+                    if (pass && !img) {
+                        const int pos = nr + __popc(balR & lt_mask);
+                        if (pos < K) { nbr[base + pos] = e; rr[base + pos] = r; ww[base + pos] = w; }
+                    }
+                    if (pass && img) {
+                        const int pos = ni + __popc(balI & lt_mask);
+                        if (pos < K) { imgE[pos] = e; imgR[pos] = r; imgW[pos] = w; }
+                    }
+                    nr += __popc(balR);
+                    ni += __popc(balI);
+                }
+                if (nr + ni > K || overflow) {
+                    overflow = true;
+                    if (nr > K) nr = K;
+                    if (ni > K - nr) ni = K - nr;
+                }
+                __syncwarp();
+                // --- images behind the real neighbours, ordered by parent index
+                for (int t = lane; t < ni; t += 32) {
+                    const uint32_t e = imgE[t];
+                    const uint32_t id = e & IDX_MASK;
+                    int rank = 0;
+                    for (int q = 0; q < ni; ++q) rank += (imgE[q] & IDX_MASK) < id;
+                    nbr[base + nr + rank] = e;
+                    rr[base + nr + rank] = imgR[t];
+                    ww[base + nr + rank] = imgW[t];
+                }
+                __syncwarp();
+                // canonical faces among the stored slots (neighbour or parent > i);
+                // counted from the final list so that it matches k_link exactly
+                for (int t = lane; t < nr + ni; t += 32) fc += (int)(nbr[base + t] & IDX_MASK) > i;
+#pragma unroll
+                for (int o = 16; o > 0; o >>= 1) fc += __shfl_xor_sync(0xffffffffu, fc, o);
+                if (lane == 0) {
+                    if (overflow) flag(status, ST_NGB_OVERFLOW);
+                    if (nr + ni == 0) flag(status, ST_NO_NEIGHBOUR);
+                    noi[i] = nr;
+                    noiImg[i] = ni;
+                    faceCnt[i] = fc;
+                }
+                // the floating-point tail of every 32 particles of this warp runs
+                // once on all 32 lanes (lane k keeps the k-th particle); the stored
+                // slots are visible to every lane after the __syncwarp above
+                if (lane == (iter & 31)) { bi = i; bnr = nr; bni = ni; bw0 = w0_i; }
+                if ((iter & 31) == 31) { finish(); bi = -1; }
+                ++iter;
+                __syncwarp();
+            }   // particles of the batch
+        }   // batches of the cell
     }
     finish();
 }
@@ -1701,13 +1794,13 @@ void launch_step(StepArgs &a) {
 
     tick(KT_NNS);
     {
-        const int warps_total = a.sm_count * a.tune.nns_warps_per_sm;   // grid-stride, one warp per particle
+        const int warps_total = a.sm_count * a.tune.nns_warps_per_sm;   // grid-stride, one warp per cell
         const int blocks = (warps_total + NNS_WARPS - 1) / NNS_WARPS;
         const size_t smem = nns_smem_bytes(p.K);
         if (smem > 48 * 1024)
             cudaFuncSetAttribute(k_neighbours<D>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
         k_neighbours<D><<<blocks, NNS_WARPS * 32, smem, s>>>(
-            p, a.members, a.memberOf, a.grids, a.x, a.y, a.z, a.posf, a.vx, a.vy, a.vz, a.m, a.u, a.cell,
+            p, a.members, a.memberOf, a.grids, a.x, a.y, a.z, a.posf, a.vx, a.vy, a.vz, a.m, a.u, a.cellTotal,
             a.cellStart, a.cellList, a.nbr, a.rr, a.ww, a.noi, a.noiImg, a.faceCnt, a.prim, a.geo, a.status);
     }
     tock(KT_NNS);
