@@ -45,8 +45,8 @@ LAUNCHES_PER_STEP = 18   # kernels launched by one mlh_step iteration (see csrc/
 # (profiles/sedov64_step_kernels.md): FP64 operations executed per face
 # (2 x DFMA + DADD + DMUL thread instructions / faces) and DRAM bytes
 # (read + write) per face.
-FACE_FP64_FLOPS = {3: 647.0}
-FACE_DRAM_BYTES = {3: 287.0}
+FACE_FP64_FLOPS = {3: 624.0}
+FACE_DRAM_BYTES = {3: 288.0}
 
 
 def make_workload(name: str, seed_offset: int = 0):

@@ -244,6 +244,12 @@ int mlh_probe_fp64_tflops(double seconds, double *tflops);
  * error against exact values.  No counterpart in the reference. */
 int mlh_probe_fast_math(int n, const double *x, const double *y, double *rcp, double *quot, double *rsqrt);
 
+/* Device time (ms, best of three launches) of the FMA chains of
+ * mlh_probe_fp64_tflops run by only the first active_lanes (1..32) lanes of
+ * every warp, iters (1..2^20) steps: how the FP64 pipe charges a partially
+ * active warp instruction.  No counterpart in the reference. */
+int mlh_probe_fp64_lanes(int active_lanes, int iters, double *ms);
+
 /* Learned initial guess for the Riemann star pressure (no counterpart in the
  * reference): a 4-64-64-64-1 SiLU MLP, 8705 float parameters laid out as
  * W1[64][4], b1[64], W2[64][64], b2[64], W3[64][64], b3[64], W4[64], b4,

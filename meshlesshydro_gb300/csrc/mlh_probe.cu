@@ -98,3 +98,59 @@ extern "C" int mlh_probe_fast_math(int n, const double *x, const double *y, doub
     cudaFree(d);
     return e == cudaSuccess ? 0 : MLH_ERR_CUDA;
 }
+
+namespace {
+
+// k_dfma with the chains run only by the first `active` lanes of each warp
+__global__ void __launch_bounds__(256) k_dfma_lanes(double *out, double a, double b, int iters, int active) {
+    double acc[CHAINS];
+#pragma unroll
+    for (int c = 0; c < CHAINS; ++c) acc[c] = (double)(threadIdx.x + c) * 1e-9;
+    if ((int)(threadIdx.x & 31) < active) {
+        for (int it = 0; it < iters; ++it) {
+#pragma unroll
+            for (int c = 0; c < CHAINS; ++c) acc[c] = fma(acc[c], a, b);
+        }
+    }
+    double s = 0.;
+#pragma unroll
+    for (int c = 0; c < CHAINS; ++c) s += acc[c];
+    if (s == 123.456) out[blockIdx.x] = s;   // never true; keeps the chains live
+}
+
+}  // namespace
+
+// Device time of the FMA chains of mlh_probe_fp64_tflops (8 blocks of 256
+// threads per SM, `iters` steps of 8 chains) when only the first
+// `active_lanes` lanes of every warp run them: how the FP64 pipe charges a
+// partially active warp instruction (on GB300 the time does not depend on
+// active_lanes, which is why the kernels keep warps convergent around FP64
+// code).  The best of three launches after a warm-up.
+extern "C" int mlh_probe_fp64_lanes(int active_lanes, int iters, double *ms) {
+    if (!ms || active_lanes < 1 || active_lanes > 32 || iters < 1 || iters > (1 << 20)) return MLH_ERR_INVALID;
+    int dev = 0, sms = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess) return MLH_ERR_NO_DEVICE;
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    const int blocks = sms * 8, threads = 256;
+    double *out = nullptr;
+    if (cudaMalloc(&out, sizeof(double) * (size_t)blocks) != cudaSuccess) return MLH_ERR_CUDA;
+    cudaEvent_t e0, e1;
+    cudaEventCreate(&e0);
+    cudaEventCreate(&e1);
+    float best = -1.f;
+    for (int rep = 0; rep < 4; ++rep) {
+        cudaEventRecord(e0);
+        k_dfma_lanes<<<blocks, threads>>>(out, 0.999999, 1e-7, iters, active_lanes);
+        cudaEventRecord(e1);
+        cudaEventSynchronize(e1);
+        float t = 0.f;
+        cudaEventElapsedTime(&t, e0, e1);
+        if (rep > 0 && (best < 0.f || t < best)) best = t;
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    cudaFree(out);
+    if (cudaGetLastError() != cudaSuccess) return MLH_ERR_CUDA;
+    *ms = best;
+    return 0;
+}

@@ -65,7 +65,7 @@ EXPORTS = ["mlh_abi_version", "mlh_last_error", "mlh_create", "mlh_destroy", "ml
            "mlh_grid_bounds_noalloc", "mlh_ensemble_create", "mlh_member_times", "mlh_set_graph_mode",
            "mlh_autotune", "mlh_set_tuning", "mlh_pstar_infer", "mlh_pstar_grad", "mlh_pstar_train", "mlh_set_pstar_weights",
            "mlh_pstar_harvest", "mlh_smoothing_lengths", "mlh_prepare", "mlh_riemann_fluxes",
-           "mlh_probe_fast_math"]
+           "mlh_probe_fast_math", "mlh_probe_fp64_lanes"]
 
 _lib = None
 
@@ -137,6 +137,8 @@ def load(path: str = LIB_PATH):
     L.mlh_riemann_fluxes.restype = ctypes.c_int
     L.mlh_probe_fast_math.argtypes = [ctypes.c_int] + [dp] * 5
     L.mlh_probe_fast_math.restype = ctypes.c_int
+    L.mlh_probe_fp64_lanes.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.POINTER(ctypes.c_double)]
+    L.mlh_probe_fp64_lanes.restype = ctypes.c_int
     _lib = L
     return L
 
@@ -168,6 +170,17 @@ def probe_fp64_tflops(seconds: float = 0.5) -> float:
     st = L.mlh_probe_fp64_tflops(seconds, ctypes.byref(out))
     if st != 0:
         raise MLHError(st, "mlh_probe_fp64_tflops", L.mlh_last_error().decode())
+    return out.value
+
+
+def probe_fp64_lanes(active_lanes: int, iters: int = 2048) -> float:
+    """Device ms of the FP64 FMA chains run by only `active_lanes` lanes of
+    every warp (mlh_probe_fp64_lanes)."""
+    L = load()
+    out = ctypes.c_double()
+    st = L.mlh_probe_fp64_lanes(active_lanes, iters, ctypes.byref(out))
+    if st != 0:
+        raise MLHError(st, "mlh_probe_fp64_lanes", L.mlh_last_error().decode())
     return out.value
 
 
