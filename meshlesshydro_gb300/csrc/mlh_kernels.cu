@@ -1191,19 +1191,13 @@ __global__ void __launch_bounds__(256) k_link(Params p, const uint32_t *__restri
 
 // ------------------------------------------------------------------ faces
 
-// Particles::pairwiseLimiter, Particles.cpp:1735-1785.
-// `ratio` = |x_ij - x_i| / |x_j - x_i|.
-__device__ __forceinline__ double pairwise_limiter(const Params &p, double phi0, double phi_i, double phi_j,
-                                                   double ratio) {
-    // every comparison on integer keys (ord_key), off the FP64 pipe
-    const long long ki = ord_key(phi_i), kj = ord_key(phi_j);
-    if (ki == kj) return phi_i;   // neither phi_i < phi_j nor phi_i > phi_j
-    const bool i_lt_j = ki < kj;
-    const double d = phi_i - phi_j;              // phi_j - phi_i = -d exactly
-    const double phi_ij = fma(ratio, -d, phi_i);
-    const double ad = ref_abs(d, p.int_abs);
-    const double delta1 = p.psi1 * ad;
-    const double delta2 = p.psi2 * ad;
+// Particles::pairwiseLimiter, Particles.cpp:1735-1785, for one side: phi0
+// the reconstructed value, phi_i this side's particle value, phi_ij the value
+// interpolated to the face, delta1/delta2 = PSI_1/PSI_2 |phi_i - phi_j|, and
+// i_lt_j = phi_i < phi_j (the two values differ).  Every comparison on
+// integer keys (ord_key), off the FP64 pipe.
+__device__ __forceinline__ double pairwise_side(double phi0, double phi_i, double phi_ij, double delta1,
+                                                double delta2, bool i_lt_j, int int_abs) {
     // the bound that is used is phi_minus = phi_min - delta1 when phi_i <
     // phi_j and phi_plus = phi_max + delta1 otherwise, and in both cases the
     // extreme it starts from is phi_i; the reference takes the shift when it
@@ -1211,7 +1205,7 @@ __device__ __forceinline__ double pairwise_limiter(const Params &p, double phi0,
     // phi / (1 + delta1 / |phi|)
     const double shifted = phi_i + (i_lt_j ? -delta1 : delta1);
     const double bound = (ord_key(shifted) >= 0) == (ord_key(phi_i) >= 0)
-                             ? shifted : phi_i / (1. + delta1 / ref_abs(phi_i, p.int_abs));
+                             ? shifted : phi_i / (1. + delta1 / ref_abs(phi_i, int_abs));
     const double t = phi_ij + (i_lt_j ? delta2 : -delta2);
     if (i_lt_j) {
         const double minPhiD2 = dlt(t, phi0) ? t : phi0;
@@ -1219,6 +1213,27 @@ __device__ __forceinline__ double pairwise_limiter(const Params &p, double phi0,
     }
     const double maxPhiD2 = dlt(phi0, t) ? t : phi0;
     return dlt(bound, maxPhiD2) ? bound : maxPhiD2;
+}
+
+// The pairwise limiter on both sides of a face: phi0R/phi0L the
+// reconstructed values (replaced by the limited ones), phiR/phiL the values
+// of particles i and j, rR/rL = |x_ij - x_i| / |x_j - x_i| and
+// |x_ij - x_j| / |x_j - x_i|.  The j side's phi_i - phi_j is the exact
+// negation of the i side's, so |phi_i - phi_j|, delta1 and delta2 are the
+// same doubles on both sides and are computed once; phi_ij on the j side,
+// phi_j + rL (phi_i - phi_j), is fma(rL, d, phi_j) with d = phi_i - phi_j.
+// Equal particle values (neither phi_i < phi_j nor phi_i > phi_j) give the
+// particle values back.
+__device__ __forceinline__ void pairwise_limiter(const Params &p, double &phi0R, double &phi0L, double phiR,
+                                                 double phiL, double rR, double rL) {
+    const long long kR = ord_key(phiR), kL = ord_key(phiL);
+    if (kR == kL) { phi0R = phiR; phi0L = phiL; return; }
+    const bool r_lt_l = kR < kL;
+    const double d = phiR - phiL;
+    const double ad = ref_abs(d, p.int_abs);
+    const double delta1 = p.psi1 * ad, delta2 = p.psi2 * ad;
+    phi0R = pairwise_side(phi0R, phiR, fma(rR, -d, phiR), delta1, delta2, r_lt_l, p.int_abs);
+    phi0L = pairwise_side(phi0L, phiL, fma(rL, d, phiL), delta1, delta2, !r_lt_l, p.int_abs);
 }
 
 // Network inputs of a face from its face-frame states (left = particle i,
@@ -1466,10 +1481,7 @@ __global__ void MLH_FACE_BOUNDS k_faces(Params p, const Member *__restrict__ mem
                 rj = sqrt(xijxj_abs) / xjxi_abs;
             }
 #pragma unroll
-            for (int k = 0; k < NV; ++k) {
-                R[k] = pairwise_limiter(p, R[k], Rb[k], Lb[k], ri);
-                L[k] = pairwise_limiter(p, L[k], Lb[k], Rb[k], rj);
-            }
+            for (int k = 0; k < NV; ++k) pairwise_limiter(p, R[k], L[k], Rb[k], Lb[k], ri, rj);
         }
         {
             // div v and 1/rho of both particles, stored once per particle
