@@ -272,6 +272,36 @@ def learned_section(runtime, make_sim, tuning, args, faces_per_step, st_plain, k
                       "harvest_s": t1 - t0, "train_s": t2 - t1}}
 
 
+def adaptive_section(runtime, cfg, p, tuning, args, ws):
+    """The same workload with per-particle smoothing lengths (adaptive_h):
+    every step solves h_i <= H for an effective neighbour number of 32, H =
+    1.25 kernelSize the search radius, and searches pairs with r < max(h_i,
+    h_j).  Reports its throughput and the share of the h solve."""
+    import torch
+    from dataclasses import replace
+    cfg_a = replace(cfg, adaptive_h=True, n_ngb=32.0, kernel_size=cfg.kernel_size * 1.25)
+    sim = runtime.Simulation(cfg_a, p)
+    if tuning:
+        sim.set_tuning(tuning)
+    sim.step(args.warmup)
+    torch.cuda.synchronize()
+    st = sim.step(args.steps)
+    kt = kernel_breakdown(sim, args.steps)
+    hs = sim.get("h_stats")
+    h = sim.get("h")
+    noi = sim.get("noi")
+    sim.close()
+    per = {k: v[1] / max(v[0], 1) for k, v in kt.items()}
+    return {"value": ws * p.n * st.steps / (st.device_ms / 1e3), "ms_per_step": st.device_ms / st.steps,
+            "n_ngb": 32.0, "search_radius_over_kernel_size": 1.25,
+            "h_over_search_radius_mean": float(np.mean(h) / cfg_a.kernel_size),
+            "neighbours_mean": float(np.mean(noi)),
+            "h_solve_ms_per_step": per.get("smoothing_lengths"),
+            "kernel_ms_per_step": per,
+            "h_stats_last_solve": {"newton_iterations": float(hs[0]), "clamped": float(hs[1])},
+            "status": runtime.status_names(st.status)}
+
+
 def run_mlh(args):
     import torch
     ws, rank, local = dist_env()
@@ -344,6 +374,8 @@ def run_mlh(args):
 
     if not args.no_learned:
         extra["learned"] = learned_section(runtime, make_sim, tuning, args, faces_per_step, st, kt, rho_plain, ws, p.n)
+    if not args.no_adaptive and WORKLOADS[args.workload]["kind"] == "sedov":
+        extra["adaptive_h"] = adaptive_section(runtime, cfg, p, tuning, args, ws)
 
     # end to end through the C ABI with host buffers: H2D of the state,
     # one step, D2H of the state, every step (pinned host memory)
@@ -435,6 +467,7 @@ def main():
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
     ap.add_argument("--no-autotune", action="store_true")
     ap.add_argument("--no-learned", action="store_true", help="skip the learned p* guess comparison")
+    ap.add_argument("--no-adaptive", action="store_true", help="skip the per-particle smoothing-length run")
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference(args)

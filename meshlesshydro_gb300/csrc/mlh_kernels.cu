@@ -1080,19 +1080,20 @@ __global__ void __launch_bounds__(256) k_gradients(Params p, const Member *__res
                 double xj[3], d[3];
                 neighbour_pos<D>(e, pj, g, xj);
                 // face point x_ij = x_i + c (x_j - x_i): c = 1/2 (first-order
-                // quadrature point) or h/4 (the reference's other choice)
+                // quadrature point) or h/4 (the reference's other choice);
+                // f_ij = f_i + grad f . (x_ij - x_i) as one FMA chain from f_i
                 const double cq = p.foqp ? .5 : hq / 4.;
 #pragma unroll
-                for (int a = 0; a < D; ++a) d[a] = xj[a] - xi[a];
+                for (int a = 0; a < D; ++a) d[a] = cq * (xj[a] - xi[a]);
 #pragma unroll
                 for (int f = 0; f < NF; ++f) {
                     const long long kj = ord_key(field_of<D>(pj, f));
                     if (mxN[f] < kj) mxN[f] = kj;
                     if (mnN[f] > kj) mnN[f] = kj;
-                    double gd = gr[f][0] * d[0];
+                    double fij = fma(gr[f][0], d[0], fi[f]);
 #pragma unroll
-                    for (int a = 1; a < D; ++a) gd = fma(gr[f][a], d[a], gd);
-                    const long long kij = ord_key(fma(cq, gd, fi[f]));
+                    for (int a = 1; a < D; ++a) fij = fma(gr[f][a], d[a], fij);
+                    const long long kij = ord_key(fij);
                     if (mxM[f] < kij) mxM[f] = kij;
                     if (mnM[f] > kij) mnM[f] = kij;
                 }
