@@ -427,56 +427,6 @@ __device__ __forceinline__ int nns_cell_of(const NnsCells *cs, int t) {
     return k;
 }
 
-// Candidates of particle i for the smoothing-length solve: the stencil cells
-// of its cell (nns_stencil), then every particle of those cells that passes
-// the single-precision distance pre-filter against the search radius (a
-// conservative bound), in stencil order and ascending index within a cell,
-// appended to cand[] (the entry carries the wrapped axes as image bits).
-// Returns the number of candidates (at most CAP); `overflow` is set when more
-// passed.
-template <int D>
-__device__ __forceinline__ int nns_candidates(const Params &p, const GridInfo &g, const Member &mb, int i,
-                                              const int *__restrict__ cell, const int *__restrict__ cellStart,
-                                              const int *__restrict__ cellList, const float4 *__restrict__ posf,
-                                              NnsCells *cs, uint32_t *cand, int CAP, bool &overflow) {
-    const int lane = threadIdx.x & 31;
-    const unsigned lt_mask = (1u << lane) - 1u;
-    const int total = nns_stencil<D>(p, g, cell[i] - g.cell_base, cellStart, cs);
-    const float4 fi = posf[i];
-    int ncand = 0;
-    for (int t0 = 0; t0 < total; t0 += 32) {
-        const int t = t0 + lane;
-        bool pass = false;
-        uint32_t ent = 0;
-        if (t < total) {
-            const int k = nns_cell_of<D>(cs, t);
-            const int j = cellList[cs->start[k] + (t - cs->excl[k])];
-            const unsigned wr = cs->wrap[k];
-            if (wr || j != i) {
-                float4 fj = posf[j];
-                float dx = fj.x - fi.x, dy = fj.y - fi.y, dz = fj.z - fi.z;
-                if (wr) {
-                    dx += cs->shift[k][0];
-                    dy += cs->shift[k][1];
-                    if (D == 3) dz += cs->shift[k][2];
-                }
-                float d2f = dx * dx + dy * dy + (D == 3 ? dz * dz : 0.f);
-                pass = d2f <= mb.hsq_f;
-                ent = (uint32_t)j | (wr << IMG_SHIFT);
-            }
-        }
-        const unsigned bal = __ballot_sync(0xffffffffu, pass);
-        if (pass) {
-            const int pos = ncand + __popc(bal & lt_mask);
-            if (pos < CAP) cand[pos] = ent;
-        }
-        ncand += __popc(bal);
-    }
-    if (ncand > CAP) { overflow = true; ncand = CAP; }
-    __syncwarp();
-    return ncand;
-}
-
 template <int D>
 __global__ void __launch_bounds__(NNS_WARPS * 32, MLH_NNS_MINB) k_neighbours(
     Params p, const Member *__restrict__ members, const int *__restrict__ memberOf,
@@ -728,26 +678,58 @@ __global__ void __launch_bounds__(NNS_WARPS * 32, MLH_NNS_MINB) k_neighbours(
 // With the cubic spline of support x, N(x) = K_D (1 + S(x)) where
 // S(x) = sum_j f(2 r_ij / x) (f the spline's shape, f(0) = 1; K_D = 32/3 in
 // 3D, 40/7 in 2D); S increases with x and dS/dx = G(x) / x with
-// G = sum_j -f'(q) q.  One warp per particle: the candidates within H (the
+// G = sum_j -f'(q) q.  The candidates within H of each particle (the
 // neighbour search's stencil, pre-filter and exact test, images by the ghost
-// rule) are kept in shared memory in stencil order; every Newton iteration
+// rule) are kept in shared memory in stencil order.  Every Newton iteration
 // sums f and g over them in 32 lane-strided partial sums combined by an xor
-// butterfly, so every lane holds the same bits and the iteration (bracketed,
-// bisection when Newton leaves the bracket) runs in lockstep.  The start is
-// the previous h_i (H at first); a particle with N(H) < n_ngb keeps H and is
-// counted in hstat[1]; hstat[0] counts iterations.  The CPU restatement
-// performs the same operations in the same order and gets the same bits.
+// butterfly, and the iteration is bracketed (bisection when Newton leaves the
+// bracket).  The start is the previous h_i (H at first); a particle with
+// N(H) < n_ngb keeps H and is counted in hstat[1]; hstat[0] counts
+// iterations.  The CPU restatement performs the same operations in the same
+// order and gets the same bits.
+//
+// One warp per cell, as the neighbour search: the cell's candidate sequence
+// is staged in shared memory once and filtered for a batch of up to HS_PB of
+// its particles; the warp then computes their candidate distances and runs
+// their Newton iterations side by side: per iteration, the sums of each
+// unfinished particle of the batch (all lanes, the order above), then the
+// scalar updates of all of them at once, particle q on lane q, so that the
+// divisions and tests of an update are issued once per batch instead of once
+// per particle.
 constexpr int HSOLVE_MAXIT = 50;
+constexpr int HS_PB = 8;
 
+// staged chunk (NNS_CH entries and positions), HS_PB candidate lists (K + 32
+// uint32) and their counts, HS_PB distance lists (K + 32 doubles) and their
+// counts, each rounded up to 16 bytes
 __host__ __device__ constexpr size_t hsolve_warp_bytes(int K) {
-    return ((size_t)(K + 32) * 4 + 15) / 16 * 16 + (size_t)(K + 32) * 8;
+    return (size_t)NNS_CH * 20 + nns_r16((size_t)HS_PB * (K + 32) * 4) + nns_r16((size_t)HS_PB * 4) +
+           (size_t)HS_PB * (K + 32) * 8 + nns_r16((size_t)HS_PB * 4);
+}
+
+// hsolve_shape without branches: both pieces as the same operations with
+// selected operands, rounding as the two-branch form does (f = (t^2/4) t is
+// fma(t^2/4, t, 0), the same rounded product)
+__device__ __forceinline__ void hsolve_shape_sel(double r, double ihh2, double &f, double &g) {
+    const double q = __dmul_rn(r, ihh2);
+    const long long qb = __double_as_longlong(q);   // q >= 0: q <= 1 and q < 2 on the bits
+    const bool inner = qb <= 0x3FF0000000000000ll, in = qb < 0x4000000000000000ll;
+    const double t = __dsub_rn(2., q);
+    const double a = inner ? q : t;
+    const double a2 = __dmul_rn(a, a);
+    const double u = __fma_rn(0.75, q, -1.5);
+    const double v = __fma_rn(-2.25, q, 3.);
+    const double f_ = __fma_rn(inner ? a2 : __dmul_rn(0.25, a2), inner ? u : t, inner ? 1. : 0.);
+    const double g_ = __dmul_rn(inner ? a2 : __dmul_rn(0.75, a2), inner ? v : q);
+    f = in ? f_ : 0.;
+    g = in ? g_ : 0.;
 }
 
 template <int D>
 __global__ void __launch_bounds__(NNS_WARPS * 32) k_hsolve(
     Params p, const Member *__restrict__ members, const int *__restrict__ memberOf,
     const GridInfo *__restrict__ grids, const double *__restrict__ x, const double *__restrict__ y,
-    const double *__restrict__ z, const float4 *__restrict__ posf, const int *__restrict__ cell,
+    const double *__restrict__ z, const float4 *__restrict__ posf, const int *__restrict__ cellTotal,
     const int *__restrict__ cellStart, const int *__restrict__ cellList, double *__restrict__ hp,
     double *__restrict__ neff, unsigned long long *__restrict__ hstat, unsigned *__restrict__ status) {
     const int K = p.K;
@@ -757,106 +739,203 @@ __global__ void __launch_bounds__(NNS_WARPS * 32) k_hsolve(
     const unsigned lt_mask = (1u << lane) - 1u;
     NnsCells *cs = reinterpret_cast<NnsCells *>(hs_smem) + warp;
     unsigned char *wbase = hs_smem + nns_cells_bytes() + (size_t)warp * hsolve_warp_bytes(K);
-    uint32_t *cand = reinterpret_cast<uint32_t *>(wbase);
-    double *rl = reinterpret_cast<double *>(wbase + ((size_t)CAP * 4 + 15) / 16 * 16);
+    float4 *stP = reinterpret_cast<float4 *>(wbase);
+    uint32_t *stE = reinterpret_cast<uint32_t *>(wbase + (size_t)NNS_CH * 16);
+    uint32_t *candq = stE + NNS_CH;                                                   // HS_PB lists of CAP
+    unsigned char *nb0 = wbase + (size_t)NNS_CH * 20 + nns_r16((size_t)HS_PB * CAP * 4);
+    int *ncq = reinterpret_cast<int *>(nb0);
+    double *rlq = reinterpret_cast<double *>(nb0 + nns_r16((size_t)HS_PB * 4));       // HS_PB lists of CAP
+    int *nrq = reinterpret_cast<int *>(reinterpret_cast<unsigned char *>(rlq) + (size_t)HS_PB * CAP * 8);
     constexpr double KD = D == 3 ? 32. / 3. : 40. / 7.;
     const double St = p.sngb_t;
     const double tolS = __dmul_rn(1e-12, St);
     const double *X[3] = {x, y, z};
-    unsigned long long iters = 0, clamped = 0;
+    unsigned long long iters = 0, clamped = 0;   // per lane, for its particles
     bool overflow_any = false;
     const int gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const int nw = (gridDim.x * blockDim.x) >> 5;
-    for (int i = gw; i < p.n; i += nw) {
-        const int mi = memberOf ? memberOf[i] : 0;
+    const int ncells = *cellTotal;
+    for (int c = gw; c < ncells; c += nw) {
+        const int c0 = cellStart[c], ncell = cellStart[c + 1] - c0;
+        if (ncell <= 0) continue;
+        const int mi = memberOf ? memberOf[cellList[c0]] : 0;
         const GridInfo g = grids[mi];
         const Member mb = members[mi];
-        bool overflow = false;
-        const int ncand = nns_candidates<D>(p, g, mb, i, cell, cellStart, cellList, posf, cs, cand, CAP, overflow);
-        if (overflow) {   // the host grows the slots and repeats
-            overflow_any = true;
-            continue;
-        }
-        // exact FP64 distances of the candidates within H, in order
-        double xi[3] = {0., 0., 0.};
-#pragma unroll
-        for (int a = 0; a < D; ++a) xi[a] = X[a][i];
-        int nr = 0;
-        for (int t0 = 0; t0 < ncand; t0 += 32) {
-            const int t = t0 + lane;
-            bool pass = false;
-            double r = 0.;
-            if (t < ncand) {
-                const uint32_t e = cand[t];
-                const int j = (int)(e & IDX_MASK);
-                const unsigned wr = e >> IMG_SHIFT;
-                double xj[3];
-                bool ok = true;
-#pragma unroll
-                for (int a = 0; a < D; ++a) {
-                    xj[a] = X[a][j];
-                    if (wr & (1u << a)) {
-                        if (in_band(xj[a], g, a)) xj[a] = image_coord(xj[a], g, a);
-                        else ok = false;
-                    }
-                }
-                if (ok) {
-                    double ex = __dsub_rn(xj[0], xi[0]), ey = __dsub_rn(xj[1], xi[1]);
-                    double d2 = __dadd_rn(__dmul_rn(ex, ex), __dmul_rn(ey, ey));
-                    if (D == 3) { double ez = __dsub_rn(xj[2], xi[2]); d2 = __dadd_rn(d2, __dmul_rn(ez, ez)); }
-                    pass = d2 < mb.hsq;
-                    if (pass) r = __dsqrt_rn(d2);
-                }
-            }
-            const unsigned bal = __ballot_sync(0xffffffffu, pass);
-            if (pass) rl[nr + __popc(bal & lt_mask)] = r;
-            nr += __popc(bal);
-        }
-        __syncwarp();
-        // bracketed Newton on S(x) = St, in lockstep on all lanes
         const double H = mb.h;
-        double xh = hp[i];
-        if (!(xh > 0. && xh <= H)) xh = H;
-        double lo = 0., hi = H, S = 0.;
-        bool upper = false;
-        for (int it = 0;; ++it) {
-            const double ihh2 = __ddiv_rn(1., __dmul_rn(0.5, xh));
-            double sf = 0., sg = 0.;
-            for (int t = lane; t < nr; t += 32) {
-                double f, gg;
-                hsolve_shape(rl[t], ihh2, f, gg);
-                sf = __dadd_rn(sf, f);
-                sg = __dadd_rn(sg, gg);
+        const int total = nns_stencil<D>(p, g, c - g.cell_base, cellStart, cs);
+        for (int b0 = 0; b0 < ncell; b0 += HS_PB) {
+            const int nb = ncell - b0 < HS_PB ? ncell - b0 : HS_PB;
+            int myI = -1;
+            float4 myF = make_float4(0.f, 0.f, 0.f, 0.f);
+            if (lane < nb) { myI = cellList[c0 + b0 + lane]; myF = posf[myI]; }
+            if (lane < HS_PB) ncq[lane] = 0;
+            __syncwarp();
+            // --- candidates of the batch: staged chunks, single-precision filter
+            for (int ch = 0; ch < total; ch += NNS_CH) {
+                const int cl = total - ch < NNS_CH ? total - ch : NNS_CH;
+                for (int t = lane; t < cl; t += 32) {
+                    const int k = nns_cell_of<D>(cs, ch + t);
+                    const int j = cellList[cs->start[k] + (ch + t - cs->excl[k])];
+                    const unsigned wr = cs->wrap[k];
+                    float4 fj = posf[j];
+                    if (wr) {
+                        fj.x += cs->shift[k][0];
+                        fj.y += cs->shift[k][1];
+                        if (D == 3) fj.z += cs->shift[k][2];
+                    }
+                    stP[t] = fj;
+                    stE[t] = (uint32_t)j | (wr << IMG_SHIFT);
+                }
+                __syncwarp();
+                for (int q = 0; q < nb; ++q) {
+                    const uint32_t iq = (uint32_t)__shfl_sync(0xffffffffu, myI, q);
+                    const float fx = __shfl_sync(0xffffffffu, myF.x, q);
+                    const float fy = __shfl_sync(0xffffffffu, myF.y, q);
+                    const float fz = __shfl_sync(0xffffffffu, myF.z, q);
+                    uint32_t *cq = candq + (size_t)q * CAP;
+                    int nq = ncq[q];
+                    for (int t0 = 0; t0 < cl; t0 += 32) {
+                        const int t = t0 + lane;
+                        bool pass = false;
+                        uint32_t ent = 0;
+                        if (t < cl) {
+                            ent = stE[t];
+                            if (ent != iq) {
+                                const float4 fj = stP[t];
+                                const float dx = fj.x - fx, dy = fj.y - fy, dz = fj.z - fz;
+                                pass = dx * dx + dy * dy + (D == 3 ? dz * dz : 0.f) <= mb.hsq_f;
+                            }
+                        }
+                        const unsigned bal = __ballot_sync(0xffffffffu, pass);
+                        if (pass) {
+                            const int pos = nq + __popc(bal & lt_mask);
+                            if (pos < CAP) cq[pos] = ent;
+                        }
+                        nq += __popc(bal);
+                    }
+                    __syncwarp();
+                    if (lane == 0) ncq[q] = nq;
+                    __syncwarp();
+                }
             }
+            // --- exact FP64 distances of the candidates within H, in order
+            for (int q = 0; q < nb; ++q) {
+                const int i = __shfl_sync(0xffffffffu, myI, q);
+                const int ncand = ncq[q];
+                int nr = 0;
+                if (ncand <= CAP) {
+                    const uint32_t *cand = candq + (size_t)q * CAP;
+                    double *rl = rlq + (size_t)q * CAP;
+                    double xi[3] = {0., 0., 0.};
 #pragma unroll
-            for (int o = 16; o > 0; o >>= 1) {
-                sf = __dadd_rn(sf, __shfl_xor_sync(0xffffffffu, sf, o));
-                sg = __dadd_rn(sg, __shfl_xor_sync(0xffffffffu, sg, o));
+                    for (int a = 0; a < D; ++a) xi[a] = X[a][i];
+                    for (int t0 = 0; t0 < ncand; t0 += 32) {
+                        const int t = t0 + lane;
+                        bool pass = false;
+                        double r = 0.;
+                        if (t < ncand) {
+                            const uint32_t e = cand[t];
+                            const int j = (int)(e & IDX_MASK);
+                            const unsigned wr = e >> IMG_SHIFT;
+                            double xj[3];
+                            bool ok = true;
+#pragma unroll
+                            for (int a = 0; a < D; ++a) {
+                                xj[a] = X[a][j];
+                                if (wr & (1u << a)) {
+                                    if (in_band(xj[a], g, a)) xj[a] = image_coord(xj[a], g, a);
+                                    else ok = false;
+                                }
+                            }
+                            if (ok) {
+                                double ex = __dsub_rn(xj[0], xi[0]), ey = __dsub_rn(xj[1], xi[1]);
+                                double d2 = __dadd_rn(__dmul_rn(ex, ex), __dmul_rn(ey, ey));
+                                if (D == 3) { double ez = __dsub_rn(xj[2], xi[2]); d2 = __dadd_rn(d2, __dmul_rn(ez, ez)); }
+                                pass = __double_as_longlong(d2) < __double_as_longlong(mb.hsq);   // d2 < H^2, both >= 0
+                                if (pass) r = __dsqrt_rn(d2);
+                            }
+                        }
+                        const unsigned bal = __ballot_sync(0xffffffffu, pass);
+                        if (pass) rl[nr + __popc(bal & lt_mask)] = r;
+                        nr += __popc(bal);
+                    }
+                } else {
+                    nr = -1;   // overflow: the host grows the slots and repeats
+                }
+                if (lane == 0) nrq[q] = nr;
+                __syncwarp();
             }
-            S = sf;
-            const double G = sg;
-            ++iters;
-            const double F = __dsub_rn(S, St);
-            if (fabs(F) <= tolS) break;
-            if (F < 0. && xh >= H) { ++clamped; break; }
-            if (it + 1 >= HSOLVE_MAXIT) break;
-            if (F > 0.) { hi = xh; upper = true; }
-            else lo = xh;
-            double xn = G > 0. ? __dsub_rn(xh, __ddiv_rn(__dmul_rn(F, xh), G)) : __dmul_rn(0.5, __dadd_rn(lo, hi));
-            if (!(xn > lo && xn < hi)) xn = (!upper && xn >= hi) ? H : __dmul_rn(0.5, __dadd_rn(lo, hi));
-            if (xn == xh) break;
-            xh = xn;
+            // --- bracketed Newton on S(x) = St, particle q's state on lane q
+            const int mynr = lane < nb ? nrq[lane] : -1;
+            if (lane < nb && mynr < 0) overflow_any = true;
+            bool done = !(lane < nb) || mynr < 0;
+            double xh = H, lo = 0., hi = H, S = 0., sfq = 0., sgq = 0.;
+            bool upper = false;
+            int it = 0;
+            if (!done) {
+                xh = hp[myI];
+                if (!(xh > 0. && xh <= H)) xh = H;
+            }
+            for (;;) {
+                const unsigned act = __ballot_sync(0xffffffffu, !done);
+                if (!act) break;
+                const double ihh2 = __ddiv_rn(1., __dmul_rn(0.5, xh));
+                for (unsigned m = act; m; m &= m - 1) {
+                    const int q = __ffs(m) - 1;
+                    const double ihq = __shfl_sync(0xffffffffu, ihh2, q);
+                    const int nrq_ = __shfl_sync(0xffffffffu, mynr, q);
+                    const double *rl = rlq + (size_t)q * CAP;
+                    double sf = 0., sg = 0.;
+                    for (int t = lane; t < nrq_; t += 32) {
+                        double f, gg;
+                        hsolve_shape_sel(rl[t], ihq, f, gg);
+                        sf = __dadd_rn(sf, f);
+                        sg = __dadd_rn(sg, gg);
+                    }
+#pragma unroll
+                    for (int o = 16; o > 0; o >>= 1) {
+                        sf = __dadd_rn(sf, __shfl_xor_sync(0xffffffffu, sf, o));
+                        sg = __dadd_rn(sg, __shfl_xor_sync(0xffffffffu, sg, o));
+                    }
+                    if (lane == q) { sfq = sf; sgq = sg; }
+                }
+                if (!done) {
+                    S = sfq;
+                    const double G = sgq;
+                    ++iters;
+                    const double F = __dsub_rn(S, St);
+                    if (fabs(F) <= tolS) done = true;
+                    else if (F < 0. && xh >= H) { ++clamped; done = true; }
+                    else if (it + 1 >= HSOLVE_MAXIT) done = true;
+                    else {
+                        if (F > 0.) { hi = xh; upper = true; }
+                        else lo = xh;
+                        double xn = G > 0. ? __dsub_rn(xh, __ddiv_rn(__dmul_rn(F, xh), G))
+                                           : __dmul_rn(0.5, __dadd_rn(lo, hi));
+                        if (!(xn > lo && xn < hi)) xn = (!upper && xn >= hi) ? H : __dmul_rn(0.5, __dadd_rn(lo, hi));
+                        if (xn == xh) done = true;
+                        else xh = xn;
+                    }
+                    ++it;
+                }
+            }
+            if (lane < nb && mynr >= 0) {
+                hp[myI] = xh;
+                if (neff) neff[myI] = __dmul_rn(KD, __dadd_rn(S, 1.));
+            }
+            __syncwarp();
         }
-        if (lane == 0) {
-            hp[i] = xh;
-            if (neff) neff[i] = __dmul_rn(KD, __dadd_rn(S, 1.));
-        }
-        __syncwarp();
     }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        iters += __shfl_xor_sync(0xffffffffu, iters, o);
+        clamped += __shfl_xor_sync(0xffffffffu, clamped, o);
+    }
+    const bool of = __any_sync(0xffffffffu, overflow_any);
     if (lane == 0) {
         if (iters) atomicAdd(hstat, iters);
         if (clamped) atomicAdd(hstat + 1, clamped);
-        if (overflow_any) flag(status, ST_NGB_OVERFLOW);
+        if (of) flag(status, ST_NGB_OVERFLOW);
     }
 }
 
@@ -1782,7 +1861,7 @@ void launch_hsolve(StepArgs &a) {
     const int blocks = (warps_total + NNS_WARPS - 1) / NNS_WARPS;
     const size_t smem = hsolve_smem_bytes(p.K);
     if (smem > 48 * 1024) cudaFuncSetAttribute(k_hsolve<D>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    k_hsolve<D><<<blocks, NNS_WARPS * 32, smem, s>>>(p, a.members, a.memberOf, a.grids, a.x, a.y, a.z, a.posf, a.cell,
+    k_hsolve<D><<<blocks, NNS_WARPS * 32, smem, s>>>(p, a.members, a.memberOf, a.grids, a.x, a.y, a.z, a.posf, a.cellTotal,
                                                      a.cellStart, a.cellList, a.hp, a.neff, a.hstat, a.status);
 }
 
