@@ -38,7 +38,13 @@ WORKLOADS = {
     "kh_ens256": dict(kind="ensemble", members=256),
 }
 METRIC = "particle-updates/s per MFV step on 1 GB300"
-LAUNCHES_PER_STEP = 18   # kernels launched by one mlh_step iteration (see csrc/mlh_kernels.cu)
+# kernels launched by one plain mlh_step iteration (csrc/mlh_kernels.cu,
+# launch_step; the ncu launch list of a step shows the same 20): binning
+# (k_bounds_partial, k_bounds_final, k_assign, 3 scan kernels, k_fill_cells,
+# k_sort_cells), k_neighbours, face links (3 scan kernels, k_link), k_timestep,
+# k_dt_final, k_gradients, k_faces (first pass, second Newton pass), k_update,
+# k_advance_time
+LAUNCHES_PER_STEP = 20
 
 # Per-face cost of the dominant kernel (k_faces, 3D, gamma = 5/3 path),
 # from one ncu --set full capture of the 64^3 periodic Sedov step
