@@ -1605,7 +1605,7 @@ __global__ void MLH_FACE_BOUNDS k_faces(Params p, const Member *__restrict__ mem
         }
         if (MODE == 4) guess = ptr_q;
         // MODE 1 defers faces whose two-rarefaction guess says strong shock
-        const double defer = MODE == 1 ? PSTAR_HARD * fmin(R[1], L[1]) : 0.;
+        const double defer = MODE == 1 ? PSTAR_HARD * (dlt(L[1], R[1]) ? L[1] : R[1]) : 0.;   // min on the keys
         RiemannResult rs = ROOT5 ? riemann_exact5(rc, R[0], unR, R[1], L[0], unL, L[1], guess, defer,
                                                   (MODE == 1 || MODE == 3) ? 1 : 0)
                                  : riemann_exact(rc, R[0], unR, R[1], L[0], unL, L[1], guess, defer);

@@ -317,7 +317,8 @@ __device__ inline RiemannResult riemann_exact5(const RiemannConsts &k, double rh
         double t = fdiv(num, den);
         double t2 = t * t;
         p0 = t2 * t2 * t;
-        if (defer_above > 0. && p0 > defer_above) {   // see riemann_exact
+        // defer_above > 0 and p0 > defer_above, on the keys (see riemann_exact)
+        if (ord_key(defer_above) > 0 && dlt(defer_above, p0)) {
             res.rho = 0.; res.u = 0.; res.p = 0.; res.pstar = p0; res.flag = 2; res.iters = 0;
             return res;
         }
