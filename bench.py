@@ -46,13 +46,14 @@ METRIC = "particle-updates/s per MFV step on 1 GB300"
 # k_advance_time
 LAUNCHES_PER_STEP = 20
 
-# Per-face cost of the dominant kernel (k_faces, 3D, gamma = 5/3 path),
-# from one ncu --set full capture of the 64^3 periodic Sedov step
-# (profiles/sedov64_step_kernels.md): FP64 operations executed per face
-# (2 x DFMA + DADD + DMUL thread instructions / faces) and DRAM bytes
-# (read + write) per face.
-FACE_FP64_FLOPS = {3: 624.0}
-FACE_DRAM_BYTES = {3: 288.0}
+# Per-face cost of the dominant kernel (k_faces, both passes, gamma = 5/3
+# path) from ncu --set full captures: FP64 operations executed per face (2 x
+# DFMA + DADD + DMUL thread instructions / faces) and DRAM bytes (read +
+# write) per face.  3D: the 64^3 periodic Sedov step
+# (profiles/sedov64_step_kernels.md); 2D: 32 members of the Kelvin-Helmholtz
+# ensemble (profiles/kh_ensemble32_step_kernels.md).
+FACE_FP64_FLOPS = {3: 599.0, 2: 483.0}
+FACE_DRAM_BYTES = {3: 288.0, 2: 355.0}
 
 
 def make_workload(name: str, seed_offset: int = 0):
