@@ -630,7 +630,8 @@ int mlh_step(mlh_ctx *c, int nsteps, double dt_max, mlh_step_stats *stats) {
 int mlh_set_tuning(mlh_ctx *c, const mlh_tuning *t) {
     auto threads_ok = [](int v) { return v == 64 || v == 128 || v == 256; };
     if (!c || !t || !threads_ok(t->face_threads) || !threads_ok(t->grad_threads) || t->face_blocks_per_sm < 1 ||
-        t->face_blocks_per_sm > 32 || t->nns_warps_per_sm < 8 || t->nns_warps_per_sm > 256) {
+        t->face_blocks_per_sm > 32 || t->nns_warps_per_sm < 8 || t->nns_warps_per_sm > 256 ||
+        (t->face_split != 0 && t->face_split != 1)) {
         g_last_error = "invalid tuning";
         return MLH_ERR_INVALID;
     }
@@ -639,6 +640,7 @@ int mlh_set_tuning(mlh_ctx *c, const mlh_tuning *t) {
     c->tune.face_blocks_per_sm = t->face_blocks_per_sm;
     c->tune.grad_threads = t->grad_threads;
     c->tune.nns_warps_per_sm = t->nns_warps_per_sm;
+    c->tune.face_split = t->face_split;
     drop_graph(c);
     return 0;
 }
@@ -685,6 +687,15 @@ int mlh_autotune(mlh_ctx *c, int trial_steps, mlh_tuning *out) {
         const int cand_b[] = {2, 4, 8, 16, 32};
         Tuning best = c->tune;
         double best_ms = 1e300;
+        // the second Newton pass pays where few faces need a second step
+        // (Sedov: a fifth) and may not where half do (Kelvin-Helmholtz)
+        for (int split : {1, 0}) {
+            c->tune.face_split = split;
+            double ms;
+            if ((rc = trial(KT_FACES, ms))) goto done;
+            if (ms < best_ms) { best_ms = ms; best.face_split = split; }
+        }
+        c->tune.face_split = best.face_split;
         for (int t : cand_t) {
             c->tune.face_threads = t;
             c->tune.face_blocks_per_sm = best.face_blocks_per_sm;
@@ -733,6 +744,7 @@ done:
         out->face_blocks_per_sm = c->tune.face_blocks_per_sm;
         out->grad_threads = c->tune.grad_threads;
         out->nns_warps_per_sm = c->tune.nns_warps_per_sm;
+        out->face_split = c->tune.face_split;
     }
     return rc;
 }

@@ -1952,7 +1952,7 @@ void launch_step(StepArgs &a) {
         pstar_infer_dev(a.feat, a.queueCount, (int)a.faces_cap, a.mlp_packed, a.yguess, a.sm_count, s);
         if (a.root5) MLH_FACES(true, 2, qa, qb); else MLH_FACES(false, 2, qa, qb);
         if (a.root5 && a.fstate2) MLH_FACES(true, 4, qb, qb);
-    } else if (a.root5 && a.fstate && a.harvest.stride == 0) {
+    } else if (a.root5 && a.fstate && a.harvest.stride == 0 && a.tune.face_split) {
         // unconverged faces after one Newton step go to a second, dense pass
         cudaMemsetAsync(a.queueCount, 0, sizeof(int), s);
         MLH_FACES(true, 3, qa, qb);
