@@ -348,15 +348,16 @@ struct NnsCells {
 
 // shared memory of k_neighbours: NNS_WARPS NnsCells, then per warp the
 // staged chunk (NNS_CH entries and float4 positions), NNS_PB candidate lists
-// (K + 32 uint32 each) and their counts, image r and W (K doubles each) and
-// image entries (K uint32), each rounded up to 16 bytes
+// (K + 32 uint32 each), four NNS_PB int arrays (candidate counts, offsets in
+// the batch's sequence, real and image neighbour counts), image r and W (K
+// doubles each) and image entries (K uint32), each rounded up to 16 bytes
 __host__ __device__ constexpr size_t nns_cells_bytes() {
     return (sizeof(NnsCells) * NNS_WARPS + 15) / 16 * 16;
 }
 __host__ __device__ constexpr size_t nns_r16(size_t b) { return (b + 15) / 16 * 16; }
 __host__ __device__ constexpr size_t nns_warp_bytes(int K) {
     return (size_t)NNS_CH * 4 + (size_t)NNS_CH * 16 + nns_r16((size_t)NNS_PB * (K + 32) * 4) +
-           nns_r16((size_t)NNS_PB * 4) + (size_t)K * 16 + nns_r16((size_t)K * 4);
+           nns_r16((size_t)4 * NNS_PB * 4) + (size_t)K * 16 + nns_r16((size_t)K * 4);
 }
 
 // The 3^D stencil cells of local cell ic in the reference's order
@@ -450,7 +451,8 @@ __global__ void __launch_bounds__(NNS_WARPS * 32, MLH_NNS_MINB) k_neighbours(
     uint32_t *stE = reinterpret_cast<uint32_t *>(wbase + (size_t)NNS_CH * 16);        // staged entries
     uint32_t *candq = stE + NNS_CH;                                                   // NNS_PB lists of CAP
     int *ncq = reinterpret_cast<int *>(wbase + (size_t)NNS_CH * 20 + nns_r16((size_t)NNS_PB * CAP * 4));
-    double *imgR = reinterpret_cast<double *>(reinterpret_cast<unsigned char *>(ncq) + nns_r16((size_t)NNS_PB * 4));
+    int *offq = ncq + NNS_PB, *nrq = offq + NNS_PB, *niq = nrq + NNS_PB;
+    double *imgR = reinterpret_cast<double *>(reinterpret_cast<unsigned char *>(ncq) + nns_r16((size_t)4 * NNS_PB * 4));
     double *imgW = imgR + K;
     uint32_t *imgE = reinterpret_cast<uint32_t *>(imgW + K);
 
@@ -554,35 +556,61 @@ __global__ void __launch_bounds__(NNS_WARPS * 32, MLH_NNS_MINB) k_neighbours(
                     __syncwarp();
                 }
             }
-            for (int q = 0; q < nb; ++q) {
-                const int i = __shfl_sync(0xffffffffu, myI, q);
-                int ncand = ncq[q];
-                bool overflow = ncand > CAP;
-                if (overflow) ncand = CAP;
-                const uint32_t *cand = candq + (size_t)q * CAP;
-                // --- phase 2: exact FP64 test, r, W.  With per-particle smoothing
-                // lengths the pair test is r^2 < max(h_i^2, h_j^2) and W uses h_i.
-                int nr = 0, ni = 0, fc = 0;
-                const size_t base = (size_t)i * K;
-                double hsq_i = mb.hsq, ih2_i = mb.ih2, sigma_i = mb.sigma, w0_i = mb.w0;
-                if (p.adaptive_h) {
-                    const double hi_ = p.hp[i];
-                    const double h2_i = hi_ / 2.;
-                    hsq_i = __dmul_rn(hi_, hi_);
-                    ih2_i = 1. / h2_i;
-                    sigma_i = kernel_sigma<D>(h2_i);
-                    w0_i = sigma_i;
-                }
-                double xi[3] = {0., 0., 0.};
+            // --- phase 2: exact FP64 test, r, W, over the candidate lists of
+            // the batch walked as one sequence, 32 candidates at a time (about
+            // 20 candidates per particle in 2D would leave a third of the lanes
+            // idle per particle).  With per-particle smoothing lengths the pair
+            // test is r^2 < max(h_i^2, h_j^2) and W uses h_i.  Particle q's
+            // position and kernel parameters live on lane q.  Real neighbours
+            // go to the front of the particle's slot row in candidate order,
+            // images to its back (slot K-1-t for the t-th), from where the
+            // per-particle step below sorts them behind the real ones.
+            {
+                const int myN = lane < nb ? (ncq[lane] < CAP ? ncq[lane] : CAP) : 0;
+                int myOff = myN;
 #pragma unroll
-                for (int a = 0; a < D; ++a) xi[a] = X[a][i];
-                for (int t0 = 0; t0 < ncand; t0 += 32) {
-                    const int t = t0 + lane;
+                for (int o = 1; o < 32; o <<= 1) {
+                    const int t = __shfl_up_sync(0xffffffffu, myOff, o);
+                    if (lane >= o) myOff += t;
+                }
+                const int seq = __shfl_sync(0xffffffffu, myOff, 31);
+                myOff -= myN;
+                if (lane < NNS_PB) { offq[lane] = myOff; nrq[lane] = 0; niq[lane] = 0; }
+                double myX[3] = {0., 0., 0.};
+                double myHsq = mb.hsq, myIh2 = mb.ih2, mySig = mb.sigma;
+                if (lane < nb) {
+#pragma unroll
+                    for (int a = 0; a < D; ++a) myX[a] = X[a][myI];
+                    if (p.adaptive_h) {
+                        const double hi_ = p.hp[myI];
+                        const double h2_i = hi_ / 2.;
+                        myHsq = __dmul_rn(hi_, hi_);
+                        myIh2 = 1. / h2_i;
+                        mySig = kernel_sigma<D>(h2_i);
+                    }
+                }
+                __syncwarp();
+                for (int t0 = 0; t0 < seq; t0 += 32) {
+                    const int gi = t0 + lane;
+                    const bool valid = gi < seq;
+                    // the particle of position gi: the last one whose list starts at
+                    // or before it (an empty list shares its offset with the next)
+                    int q = 0;
+#pragma unroll
+                    for (int l = 1; l < NNS_PB; ++l)
+                        if (l < nb && offq[l] <= gi) q = l;
+                    const int i = __shfl_sync(0xffffffffu, myI, q);
+                    double xi[3] = {0., 0., 0.};
+#pragma unroll
+                    for (int a = 0; a < D; ++a) xi[a] = __shfl_sync(0xffffffffu, myX[a], q);
+                    const double hsq_i = __shfl_sync(0xffffffffu, myHsq, q);
+                    const double ih2_i = __shfl_sync(0xffffffffu, myIh2, q);
+                    const double sigma_i = __shfl_sync(0xffffffffu, mySig, q);
                     bool pass = false, img = false;
                     uint32_t e = 0;
                     double r = 0., w = 0.;
-                    if (t < ncand) {
-                        e = cand[t];
+                    if (valid) {
+                        e = candq[(size_t)q * CAP + (gi - offq[q])];
                         const int j = (int)(e & IDX_MASK);
                         const unsigned wr = e >> IMG_SHIFT;
                         img = wr != 0;
@@ -614,23 +642,45 @@ __global__ void __launch_bounds__(NNS_WARPS * 32, MLH_NNS_MINB) k_neighbours(
                             }
                         }
                     }
-                    const unsigned balR = __ballot_sync(0xffffffffu, pass && !img);
-                    const unsigned balI = __ballot_sync(0xffffffffu, pass && img);
+                    // lanes of the same particle, and their ranks among its passes
+                    const unsigned grp = __match_any_sync(0xffffffffu, valid ? q : -1);
+                    const unsigned balR = __ballot_sync(0xffffffffu, pass && !img) & grp;
+                    const unsigned balI = __ballot_sync(0xffffffffu, pass && img) & grp;
+                    const int nr0 = nrq[q], ni0 = niq[q];
+                    const size_t base = (size_t)i * K;
                     if (pass && !img) {
-                        const int pos = nr + __popc(balR & lt_mask);
+                        const int pos = nr0 + __popc(balR & lt_mask);
                         if (pos < K) { nbr[base + pos] = e; rr[base + pos] = r; ww[base + pos] = w; }
                     }
                     if (pass && img) {
-                        const int pos = ni + __popc(balI & lt_mask);
-                        if (pos < K) { imgE[pos] = e; imgR[pos] = r; imgW[pos] = w; }
+                        const int pos = ni0 + __popc(balI & lt_mask);
+                        if (pos < K) { nbr[base + K - 1 - pos] = e; rr[base + K - 1 - pos] = r; ww[base + K - 1 - pos] = w; }
                     }
-                    nr += __popc(balR);
-                    ni += __popc(balI);
+                    __syncwarp();
+                    if (valid && (grp & lt_mask) == 0) {   // first lane of each particle's group
+                        nrq[q] = nr0 + __popc(balR);
+                        niq[q] = ni0 + __popc(balI);
+                    }
+                    __syncwarp();
                 }
+            }
+            for (int q = 0; q < nb; ++q) {
+                const int i = __shfl_sync(0xffffffffu, myI, q);
+                bool overflow = ncq[q] > CAP;
+                int nr = nrq[q], ni = niq[q], fc = 0;
+                const size_t base = (size_t)i * K;
+                double w0_i = mb.w0;
+                if (p.adaptive_h) w0_i = kernel_sigma<D>(p.hp[i] / 2.);
                 if (nr + ni > K || overflow) {
                     overflow = true;
                     if (nr > K) nr = K;
                     if (ni > K - nr) ni = K - nr;
+                }
+                // images from the back of the row, in candidate order
+                for (int t = lane; t < ni; t += 32) {
+                    imgE[t] = nbr[base + K - 1 - t];
+                    imgR[t] = rr[base + K - 1 - t];
+                    imgW[t] = ww[base + K - 1 - t];
                 }
                 __syncwarp();
                 // --- images behind the real neighbours, ordered by parent index
@@ -638,7 +688,7 @@ __global__ void __launch_bounds__(NNS_WARPS * 32, MLH_NNS_MINB) k_neighbours(
                     const uint32_t e = imgE[t];
                     const uint32_t id = e & IDX_MASK;
                     int rank = 0;
-                    for (int q = 0; q < ni; ++q) rank += (imgE[q] & IDX_MASK) < id;
+                    for (int u = 0; u < ni; ++u) rank += (imgE[u] & IDX_MASK) < id;
                     nbr[base + nr + rank] = e;
                     rr[base + nr + rank] = imgR[t];
                     ww[base + nr + rank] = imgW[t];
