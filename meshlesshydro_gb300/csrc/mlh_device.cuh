@@ -141,26 +141,6 @@ __device__ __forceinline__ double kernel_sigma(double h2) {
     return D == 2 ? 10. / (7. * PI * h2 * h2) : 1. / (PI * h2 * h2 * h2);
 }
 
-// Shape of the cubic spline and its scaled derivative for the smoothing-length
-// solve: q = r / (h/2) (given as r times 1 / (h/2)), f(q) with f(0) = 1 and
-// g(q) = -f'(q) q.  Every operation is an explicitly rounded intrinsic so that
-// the CPU restatement, which performs the same operations, gets the same bits.
-__device__ __forceinline__ void hsolve_shape(double r, double ihh2, double &f, double &g) {
-    const double q = __dmul_rn(r, ihh2);
-    if (q <= 1.) {
-        const double q2 = __dmul_rn(q, q);
-        f = __fma_rn(q2, __fma_rn(0.75, q, -1.5), 1.);
-        g = __dmul_rn(q2, __fma_rn(-2.25, q, 3.));
-    } else if (q < 2.) {
-        const double t = __dsub_rn(2., q), t2 = __dmul_rn(t, t);
-        f = __dmul_rn(__dmul_rn(0.25, t2), t);
-        g = __dmul_rn(__dmul_rn(0.75, t2), q);
-    } else {
-        f = 0.;
-        g = 0.;
-    }
-}
-
 // abs() as bound by the reference's limiter code (fabs, or int abs(int) with
 // x86 conversion semantics: NaN / out of range -> INT_MIN, abs(INT_MIN) = INT_MIN).
 __device__ __forceinline__ double ref_abs(double x, int int_abs) {

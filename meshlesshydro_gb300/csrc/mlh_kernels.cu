@@ -757,9 +757,15 @@ __host__ __device__ constexpr size_t hsolve_warp_bytes(int K) {
            (size_t)HS_PB * (K + 32) * 8 + nns_r16((size_t)HS_PB * 4);
 }
 
-// hsolve_shape without branches: both pieces as the same operations with
-// selected operands, rounding as the two-branch form does (f = (t^2/4) t is
-// fma(t^2/4, t, 0), the same rounded product)
+// Shape of the cubic spline and its scaled derivative for the smoothing-length
+// solve: q = r / (h/2) (given as r times 1 / (h/2)), f(q) with f(0) = 1 and
+// g(q) = -f'(q) q; for q <= 1, f = fma(q^2, fma(0.75, q, -1.5), 1) and
+// g = q^2 fma(-2.25, q, 3); for 1 < q < 2, with t = 2 - q, f = (t^2/4) t and
+// g = (3 t^2/4) q; 0 beyond.  Every operation is an explicitly rounded
+// intrinsic so that the CPU restatement, which performs the same operations,
+// gets the same bits.  Both pieces run as the same operations with selected
+// operands (f = (t^2/4) t as fma(t^2/4, t, 0), the same rounded product), so
+// a warp whose candidates fall on both sides of q = 1 issues them once.
 __device__ __forceinline__ void hsolve_shape_sel(double r, double ihh2, double &f, double &g) {
     const double q = __dmul_rn(r, ihh2);
     const long long qb = __double_as_longlong(q);   // q >= 0: q <= 1 and q < 2 on the bits
