@@ -288,8 +288,8 @@ def adaptive_section(runtime, cfg, p, tuning, args, ws):
     from dataclasses import replace
     cfg_a = replace(cfg, adaptive_h=True, n_ngb=32.0, kernel_size=cfg.kernel_size * 1.25)
     sim = runtime.Simulation(cfg_a, p)
-    if tuning:
-        sim.set_tuning(tuning)
+    # its own launch shapes: the wider search radius changes the best ones
+    tuning_a = sim.autotune(1) if tuning else None
     sim.step(args.warmup)
     torch.cuda.synchronize()
     st = sim.step(args.steps)
@@ -306,6 +306,7 @@ def adaptive_section(runtime, cfg, p, tuning, args, ws):
             "h_solve_ms_per_step": per.get("smoothing_lengths"),
             "kernel_ms_per_step": per,
             "h_stats_last_solve": {"newton_iterations": float(hs[0]), "clamped": float(hs[1])},
+            "tuning": tuning_a,
             "status": runtime.status_names(st.status)}
 
 

@@ -28,6 +28,13 @@ int cuda_fail(cudaError_t e, const char *what) {
         if (e_ != cudaSuccess) return cuda_fail(e_, #call); \
     } while (0)
 
+// the smallest float >= x (x finite, positive)
+float float_up(double x) {
+    float f = (float)x;
+    if ((double)f < x) f = std::nextafter(f, INFINITY);
+    return f;
+}
+
 template <class T>
 cudaError_t dalloc(T **p, size_t count) {
     *p = nullptr;
@@ -81,6 +88,7 @@ struct mlh_ctx {
     // per-particle smoothing lengths and the effective neighbour number of
     // the last solve; counters [iterations, clamped]
     double *hp = nullptr, *neff = nullptr;
+    float *hpf = nullptr;
     unsigned long long *hstat = nullptr;
     // scalars
     unsigned *status = nullptr;
@@ -277,8 +285,8 @@ StepArgs make_args(mlh_ctx *c, double dt_max) {
     a.queueFace = c->queueFace; a.queueCount = c->queueCount; a.mlp_packed = c->mlp_packed;
     a.fstate2 = c->fstate2; a.queueFace2 = c->queueFace2; a.queueCount2 = c->queueCount2;
     a.harvest = c->harvest;
-    a.hp = c->hp; a.neff = c->neff; a.hstat = c->hstat;
-    a.p.hp = c->hp;
+    a.hp = c->hp; a.neff = c->neff; a.hstat = c->hstat; a.hpf = c->hpf;
+    a.p.hp = c->hp; a.p.hpf = c->hpf;
     a.timer = c->timing ? timer_cb : nullptr;
     a.timer_ctx = c;
     return a;
@@ -421,7 +429,7 @@ static int create_impl(const mlh_config *cfg, int nmembers, const mlh_member *md
     A(noi, n); A(noiImg, n); A(faceCnt, n); A(faceOff, n + 1);
     A(prim, n); A(geo, n); A(grad, n); A(gradRaw, n); A(fluxSums, n * 5);
     A(status, 1); A(dtbits, nm); A(newtonSum, 3); A(dt, nm); A(simTime, nm); A(stepsDone, 1);
-    A(hp, n); A(neff, n); A(hstat, 2);
+    A(hp, n); A(neff, n); A(hstat, 2); A(hpf, n);
     A(scanTiles, n / 4096 + 1024); A(scanTotal, 1);
 #undef A
     if ((rc = alloc_cell_buffers(c))) return fail(rc);
@@ -449,6 +457,10 @@ static int create_impl(const mlh_config *cfg, int nmembers, const mlh_member *md
             for (int i = mb.first; i < mb.first + mb.count; ++i) h0[i] = mb.h;
         if (cudaMemcpy(c->hp, h0.data(), sizeof(double) * n, cudaMemcpyHostToDevice) != cudaSuccess)
             return fail(cuda_fail(cudaGetLastError(), "hp"));
+        std::vector<float> h0f(n);
+        for (size_t i = 0; i < n; ++i) h0f[i] = float_up(h0[i]);
+        if (cudaMemcpy(c->hpf, h0f.data(), sizeof(float) * n, cudaMemcpyHostToDevice) != cudaSuccess)
+            return fail(cuda_fail(cudaGetLastError(), "hpf"));
     }
     if ((rc = upload(c, init))) return fail(rc);
     if (cudaStreamSynchronize(c->stream) != cudaSuccess) return fail(cuda_fail(cudaGetLastError(), "create sync"));
@@ -496,7 +508,7 @@ void mlh_destroy(mlh_ctx *c) {
     void *ptrs[] = {c->x, c->y, c->z, c->vx, c->vy, c->vz, c->m, c->u, c->posf, c->members, c->memberOf, c->grids,
                     c->cellTotal, c->boundsPart, c->cell, c->cellList, c->noi, c->noiImg, c->faceCnt, c->faceOff,
                     c->prim, c->geo, c->grad, c->gradRaw, c->fluxSums, c->status, c->dtbits, c->newtonSum, c->dt,
-                    c->simTime, c->stepsDone, c->scanTiles, c->scanTotal, c->hp, c->neff, c->hstat};
+                    c->simTime, c->stepsDone, c->scanTiles, c->scanTotal, c->hp, c->neff, c->hstat, c->hpf};
     for (void *q : ptrs) if (q) cudaFree(q);
     free_cell_buffers(c);
     free_neighbour_buffers(c);

@@ -71,6 +71,7 @@ struct Params {
     double cfl;            // CFL (cfl_h = CFL * kernelSize without adaptive_h)
     double sngb_t;         // target of S = sum_j f(2 r_ij / h_i): n_ngb / K_D - 1
     const double *hp;
+    const float *hpf;      // hp rounded up to single precision (pre-filter)
 };
 
 // Per-particle records (array of structures: one particle's values sit in

@@ -347,7 +347,7 @@ struct NnsCells {
 };
 
 // shared memory of k_neighbours: NNS_WARPS NnsCells, then per warp the
-// staged chunk (NNS_CH entries and float4 positions), NNS_PB candidate lists
+// staged chunk (NNS_CH float4 positions and entries), NNS_PB candidate lists
 // (K + 32 uint32 each), four NNS_PB int arrays (candidate counts, offsets in
 // the batch's sequence, real and image neighbour counts), image r and W (K
 // doubles each) and image entries (K uint32), each rounded up to 16 bytes
@@ -355,9 +355,13 @@ __host__ __device__ constexpr size_t nns_cells_bytes() {
     return (sizeof(NnsCells) * NNS_WARPS + 15) / 16 * 16;
 }
 __host__ __device__ constexpr size_t nns_r16(size_t b) { return (b + 15) / 16 * 16; }
-__host__ __device__ constexpr size_t nns_warp_bytes(int K) {
+// (with per-particle smoothing lengths also the staged chunk's h_j, NNS_CH
+// floats, at the end: without them the area of 8 warps stays within a third
+// of the SM's shared memory at K = 64, for 3 blocks per SM)
+__host__ __device__ constexpr size_t nns_warp_bytes(int K, bool adaptive = false) {
     return (size_t)NNS_CH * 4 + (size_t)NNS_CH * 16 + nns_r16((size_t)NNS_PB * (K + 32) * 4) +
-           nns_r16((size_t)4 * NNS_PB * 4) + (size_t)K * 16 + nns_r16((size_t)K * 4);
+           nns_r16((size_t)4 * NNS_PB * 4) + (size_t)K * 16 + nns_r16((size_t)K * 4) +
+           (adaptive ? (size_t)NNS_CH * 4 : 0);
 }
 
 // The 3^D stencil cells of local cell ic in the reference's order
@@ -446,7 +450,7 @@ __global__ void __launch_bounds__(NNS_WARPS * 32, MLH_NNS_MINB) k_neighbours(
     // per-warp shared areas; every sub-array starts on a 16-byte boundary
     // whatever K is (see nns_warp_bytes)
     NnsCells *cs = reinterpret_cast<NnsCells *>(nns_smem) + warp;
-    unsigned char *wbase = nns_smem + nns_cells_bytes() + (size_t)warp * nns_warp_bytes(K);
+    unsigned char *wbase = nns_smem + nns_cells_bytes() + (size_t)warp * nns_warp_bytes(K, p.adaptive_h);
     float4 *stP = reinterpret_cast<float4 *>(wbase);                                  // staged positions
     uint32_t *stE = reinterpret_cast<uint32_t *>(wbase + (size_t)NNS_CH * 16);        // staged entries
     uint32_t *candq = stE + NNS_CH;                                                   // NNS_PB lists of CAP
@@ -455,6 +459,7 @@ __global__ void __launch_bounds__(NNS_WARPS * 32, MLH_NNS_MINB) k_neighbours(
     double *imgR = reinterpret_cast<double *>(reinterpret_cast<unsigned char *>(ncq) + nns_r16((size_t)4 * NNS_PB * 4));
     double *imgW = imgR + K;
     uint32_t *imgE = reinterpret_cast<uint32_t *>(imgW + K);
+    float *stH = reinterpret_cast<float *>(reinterpret_cast<unsigned char *>(imgE) + nns_r16((size_t)K * 4));   // staged h_j
 
     const double *X[3] = {x, y, z};
     const int gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
@@ -504,7 +509,12 @@ __global__ void __launch_bounds__(NNS_WARPS * 32, MLH_NNS_MINB) k_neighbours(
             // --- phase 1 for the batch: particle q of the batch on lane q
             int myI = -1;
             float4 myF = make_float4(0.f, 0.f, 0.f, 0.f);
-            if (lane < nb) { myI = cellList[c0 + b0 + lane]; myF = posf[myI]; }
+            float myHf = 0.f;
+            if (lane < nb) {
+                myI = cellList[c0 + b0 + lane];
+                myF = posf[myI];
+                if (p.adaptive_h) myHf = p.hpf[myI];
+            }
             if (lane < NNS_PB) ncq[lane] = 0;
             __syncwarp();
             for (int ch = 0; ch < total; ch += NNS_CH) {
@@ -522,6 +532,7 @@ __global__ void __launch_bounds__(NNS_WARPS * 32, MLH_NNS_MINB) k_neighbours(
                     }
                     stP[t] = fj;
                     stE[t] = (uint32_t)j | (wr << IMG_SHIFT);
+                    if (p.adaptive_h) stH[t] = p.hpf[j];
                 }
                 __syncwarp();
                 for (int q = 0; q < nb; ++q) {
@@ -529,6 +540,7 @@ __global__ void __launch_bounds__(NNS_WARPS * 32, MLH_NNS_MINB) k_neighbours(
                     const float fx = __shfl_sync(0xffffffffu, myF.x, q);
                     const float fy = __shfl_sync(0xffffffffu, myF.y, q);
                     const float fz = __shfl_sync(0xffffffffu, myF.z, q);
+                    const float hq = __shfl_sync(0xffffffffu, myHf, q);
                     uint32_t *cq = candq + (size_t)q * CAP;
                     int nq = ncq[q];
                     for (int t0 = 0; t0 < cl; t0 += 32) {
@@ -541,7 +553,15 @@ __global__ void __launch_bounds__(NNS_WARPS * 32, MLH_NNS_MINB) k_neighbours(
                                 const float4 fj = stP[t];
                                 const float dx = fj.x - fx, dy = fj.y - fy, dz = fj.z - fz;
                                 const float d2f = dx * dx + dy * dy + (D == 3 ? dz * dz : 0.f);
-                                pass = d2f <= mb.hsq_f;
+                                // with per-particle smoothing lengths the pair needs
+                                // r < max(h_i, h_j): the same bound margin on the
+                                // rounded-up single-precision h
+                                float lim = mb.hsq_f;
+                                if (p.adaptive_h) {
+                                    const float m = fmaxf(hq, stH[t]);
+                                    lim = m * m * 1.001f;
+                                }
+                                pass = d2f <= lim;
                             }
                         }
                         const unsigned bal = __ballot_sync(0xffffffffu, pass);
@@ -787,7 +807,8 @@ __global__ void __launch_bounds__(NNS_WARPS * 32) k_hsolve(
     const GridInfo *__restrict__ grids, const double *__restrict__ x, const double *__restrict__ y,
     const double *__restrict__ z, const float4 *__restrict__ posf, const int *__restrict__ cellTotal,
     const int *__restrict__ cellStart, const int *__restrict__ cellList, double *__restrict__ hp,
-    double *__restrict__ neff, unsigned long long *__restrict__ hstat, unsigned *__restrict__ status) {
+    float *__restrict__ hpf, double *__restrict__ neff, unsigned long long *__restrict__ hstat,
+    unsigned *__restrict__ status) {
     const int K = p.K;
     const int CAP = K + 32;
     extern __shared__ __align__(16) unsigned char hs_smem[];
@@ -977,6 +998,7 @@ __global__ void __launch_bounds__(NNS_WARPS * 32) k_hsolve(
             }
             if (lane < nb && mynr >= 0) {
                 hp[myI] = xh;
+                hpf[myI] = __double2float_ru(xh);
                 if (neff) neff[myI] = __dmul_rn(KD, __dadd_rn(S, 1.));
             }
             __syncwarp();
@@ -999,8 +1021,8 @@ size_t hsolve_smem_bytes(int K) {
     return nns_cells_bytes() + (size_t)NNS_WARPS * hsolve_warp_bytes(K);
 }
 
-size_t nns_smem_bytes(int K) {
-    return nns_cells_bytes() + (size_t)NNS_WARPS * nns_warp_bytes(K);
+size_t nns_smem_bytes(int K, bool adaptive) {
+    return nns_cells_bytes() + (size_t)NNS_WARPS * nns_warp_bytes(K, adaptive);
 }
 
 // ------------------------------------------------------------------ dt
@@ -1918,7 +1940,7 @@ void launch_hsolve(StepArgs &a) {
     const size_t smem = hsolve_smem_bytes(p.K);
     if (smem > 48 * 1024) cudaFuncSetAttribute(k_hsolve<D>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     k_hsolve<D><<<blocks, NNS_WARPS * 32, smem, s>>>(p, a.members, a.memberOf, a.grids, a.x, a.y, a.z, a.posf, a.cellTotal,
-                                                     a.cellStart, a.cellList, a.hp, a.neff, a.hstat, a.status);
+                                                     a.cellStart, a.cellList, a.hp, a.hpf, a.neff, a.hstat, a.status);
 }
 
 template <int D>
@@ -1944,7 +1966,7 @@ void launch_step(StepArgs &a) {
     {
         const int warps_total = a.sm_count * a.tune.nns_warps_per_sm;   // grid-stride, one warp per cell
         const int blocks = (warps_total + NNS_WARPS - 1) / NNS_WARPS;
-        const size_t smem = nns_smem_bytes(p.K);
+        const size_t smem = nns_smem_bytes(p.K, p.adaptive_h);
         if (smem > 48 * 1024)
             cudaFuncSetAttribute(k_neighbours<D>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
         k_neighbours<D><<<blocks, NNS_WARPS * 32, smem, s>>>(

@@ -78,6 +78,7 @@ struct StepArgs {
     // per-particle smoothing lengths: h (also p.hp), effective neighbour
     // number (may be null), counters [iterations, clamped particles]
     double *hp, *neff;
+    float *hpf;   // hp rounded up to single precision, written beside it
     unsigned long long *hstat;
     // end the step after the gradients and the limiter (mlh_prepare)
     int stop_after_gradients;
