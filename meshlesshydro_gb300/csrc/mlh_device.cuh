@@ -219,6 +219,15 @@ __device__ __forceinline__ double dotD(const double *a, const double *b) {
     return r;
 }
 
+// base + a . b as one chain of fused multiply-adds starting from base
+template <int D>
+__device__ __forceinline__ double fma_dotD(const double *a, const double *b, double base) {
+    double r = base;
+#pragma unroll
+    for (int k = 0; k < D; ++k) r = fma(a[k], b[k], r);
+    return r;
+}
+
 __device__ __forceinline__ void flag(unsigned *status, unsigned bits) {
     atomicOr(status, bits);
 }

@@ -1614,11 +1614,12 @@ __global__ void MLH_FACE_BOUNDS k_faces(Params p, const Member *__restrict__ mem
         double Rb[5], Lb[5];
 #pragma unroll
         for (int k = 0; k < NV; ++k) { Rb[k] = R[k]; Lb[k] = L[k]; }
-        R[0] += dotD<D>(Gi + 0, xijxi); L[0] += dotD<D>(Gj + 0, xijxj);
-        R[1] += dotD<D>(Gi + 12, xijxi); L[1] += dotD<D>(Gj + 12, xijxj);
-        R[2] += dotD<D>(Gi + 3, xijxi); L[2] += dotD<D>(Gj + 3, xijxj);
-        R[3] += dotD<D>(Gi + 6, xijxi); L[3] += dotD<D>(Gj + 6, xijxj);
-        if (D == 3) { R[4] += dotD<D>(Gi + 9, xijxi); L[4] += dotD<D>(Gj + 9, xijxj); }
+        // W + grad W . (x_ij - x_side), one FMA chain from W per field
+        R[0] = fma_dotD<D>(Gi + 0, xijxi, R[0]); L[0] = fma_dotD<D>(Gj + 0, xijxj, L[0]);
+        R[1] = fma_dotD<D>(Gi + 12, xijxi, R[1]); L[1] = fma_dotD<D>(Gj + 12, xijxj, L[1]);
+        R[2] = fma_dotD<D>(Gi + 3, xijxi, R[2]); L[2] = fma_dotD<D>(Gj + 3, xijxj, L[2]);
+        R[3] = fma_dotD<D>(Gi + 6, xijxi, R[3]); L[3] = fma_dotD<D>(Gj + 6, xijxj, L[3]);
+        if (D == 3) { R[4] = fma_dotD<D>(Gi + 9, xijxi, R[4]); L[4] = fma_dotD<D>(Gj + 9, xijxj, L[4]); }
         if (p.pairwise && (!img || p.img_pw)) {
             double ri, rj;   // |x_ij - x_i| / |x_j - x_i| and |x_ij - x_j| / |x_j - x_i|
             if (p.foqp) {

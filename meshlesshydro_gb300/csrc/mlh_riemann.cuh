@@ -231,9 +231,15 @@ struct RiemannSide {
 __device__ __forceinline__ RiemannSide make_side(const RiemannConsts &k, double rho, double u, double p) {
     RiemannSide s;
     s.rho = rho; s.u = u; s.p = p;
-    const double irho = frcp(rho);
-    s.c = sqrt(k.gamma * p * irho);
-    s.invp = frcp(p);
+    // one reciprocal square root for c, 1/rho and 1/p: with g = gamma p and
+    // y = 1/sqrt(g rho), c = sqrt(g / rho) = g y, 1/rho = g y^2 and
+    // 1/p = gamma rho y^2 (each within a few ulp)
+    const double gp = k.gamma * p;
+    const double y = frsqrt(gp * rho);
+    const double y2 = y * y;
+    const double irho = gp * y2;
+    s.c = gp * y;
+    s.invp = (k.gamma * rho) * y2;
     s.C = s.c * k.inv_gamma;     // pK / (rhoK cK) = cK / gamma: f' = (p/pK)^g1 C / p
     s.ak = k.g5 * irho;
     s.bk = k.g6 * p;
