@@ -1648,7 +1648,8 @@ __global__ void MLH_FACE_BOUNDS k_faces(Params p, const Member *__restrict__ mem
             const double viDiv = Gi[15], vjDiv = Gj[15];
             const double hdt = dt / 2.;
             const double iri = geo[i].irho, irj = geo[j].irho;
-            const double ui0 = vi[0] - vf[0], ui1 = vi[1] - vf[1], uj0 = vj[0] - vf[0], uj1 = vj[1] - vf[1];
+            // the boosted velocities v - v_frame, saved before the reconstruction
+            const double ui0 = Rb[2], ui1 = Rb[3], uj0 = Lb[2], uj1 = Lb[3];
             R[0] -= hdt * (pi.rho * viDiv + ui0 * Gi[0] + ui1 * Gi[1]);
             L[0] -= hdt * (pj.rho * vjDiv + uj0 * Gj[0] + uj1 * Gj[1]);
             R[1] -= hdt * (gamma * pi.P * viDiv + ui0 * Gi[12] + ui1 * Gi[13]);
@@ -1658,7 +1659,7 @@ __global__ void MLH_FACE_BOUNDS k_faces(Params p, const Member *__restrict__ mem
             R[3] -= hdt * (Gi[13] * iri + ui0 * Gi[6] + ui1 * Gi[7]);
             L[3] -= hdt * (Gj[13] * irj + uj0 * Gj[6] + uj1 * Gj[7]);
             if (D == 3) {
-                const double ui2 = vi[2] - vf[2], uj2 = vj[2] - vf[2];
+                const double ui2 = Rb[4], uj2 = Lb[4];
                 R[0] -= hdt * ui2 * Gi[2];
                 L[0] -= hdt * uj2 * Gj[2];
                 R[1] -= hdt * ui2 * Gi[14];

@@ -14,6 +14,7 @@ namespace mlh {
 
 struct RiemannConsts {
     double gamma, g1, g2, g3, g4, g5, g6, g7, inv_gamma, inv_gm1, tol;
+    double ig5;   // 1 / g5 = (gamma + 1) / 2
     int max_iter;
     // gamma = 5/3: g1 = 1/5, g3 = 5, g4 = 3 and 1/gamma = 3 g1, so every
     // power in the solver is a fifth root or an integer power
@@ -28,6 +29,7 @@ __host__ __device__ inline RiemannConsts make_riemann_consts(double gamma, doubl
     c.g3 = 2. * gamma / (gamma - 1.);
     c.g4 = 2. / (gamma - 1.);
     c.g5 = 2. / (gamma + 1.);
+    c.ig5 = (gamma + 1.) / 2.;
     c.g6 = (gamma - 1.) / (gamma + 1.);
     c.g7 = (gamma - 1.) / 2.;
     c.inv_gamma = 1. / gamma;
@@ -225,23 +227,21 @@ __device__ __forceinline__ double two_rarefaction_guess(const RiemannConsts &k, 
 }
 
 struct RiemannSide {
-    double rho, u, p, c, invp, C, ak, bk, g4c;
+    double rho, u, p, c, invp, C, iak, bk, g4c;   // iak = 1 / A_K = rho / g5
 };
 
 __device__ __forceinline__ RiemannSide make_side(const RiemannConsts &k, double rho, double u, double p) {
     RiemannSide s;
     s.rho = rho; s.u = u; s.p = p;
-    // one reciprocal square root for c, 1/rho and 1/p: with g = gamma p and
-    // y = 1/sqrt(g rho), c = sqrt(g / rho) = g y, 1/rho = g y^2 and
-    // 1/p = gamma rho y^2 (each within a few ulp)
+    // one reciprocal square root for c and 1/p: with g = gamma p and
+    // y = 1/sqrt(g rho), c = sqrt(g / rho) = g y and 1/p = gamma rho y^2
+    // (each within a few ulp)
     const double gp = k.gamma * p;
     const double y = frsqrt(gp * rho);
-    const double y2 = y * y;
-    const double irho = gp * y2;
     s.c = gp * y;
-    s.invp = (k.gamma * rho) * y2;
+    s.invp = (k.gamma * rho) * (y * y);
     s.C = s.c * k.inv_gamma;     // pK / (rhoK cK) = cK / gamma: f' = (p/pK)^g1 C / p
-    s.ak = k.g5 * irho;
+    s.iak = rho * k.ig5;
     s.bk = k.g6 * p;
     s.g4c = k.g4 * s.c;
     return s;
@@ -256,8 +256,11 @@ __device__ __forceinline__ void pressure_fn5(const RiemannSide &s, double p, dou
         fd = q * s.C * invp;
         rare = true;
     } else {
-        double t = frcp(s.bk + p);
-        double qrt = sqrt(s.ak * t);
+        // qrt = sqrt(A_K / (B_K + p)) and t = 1 / (B_K + p) from one
+        // reciprocal square root: qrt = 1/sqrt((B_K + p) / A_K), t = qrt^2 / A_K
+        const double bp = s.bk + p;
+        const double qrt = frsqrt(bp * s.iak);
+        const double t = (qrt * qrt) * s.iak;
         f = (p - s.p) * qrt;
         fd = (1. - .5 * (p - s.p) * t) * qrt;
         q = 0.;
