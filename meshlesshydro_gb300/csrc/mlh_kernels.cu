@@ -1159,19 +1159,21 @@ __global__ void __launch_bounds__(256) k_gradients(Params p, const Member *__res
         const double hq = p.adaptive_h ? p.hp[i] : h;   // quadrature-point radius
         const Prim pi = prim[i];
         const double xi[3] = {pi.x, pi.y, pi.z};
-        const double Vi = geo[i].V;
         const size_t base = (size_t)i * p.K;
         const int tot = noi[i] + noiImg[i];
+        // E_i = V_i E' with E' = sum_j (x_j - x_i)(x_j - x_i)^T W_ij, so that
+        // psi~_j(x_i) = E_i^-1 (x_j - x_i) W_ij V_i = E'^-1 (x_j - x_i) W_ij:
+        // V_i cancels and neither pass multiplies by it
         double E[9] = {0., 0., 0., 0., 0., 0., 0., 0., 0.};
         for (int s = 0; s < tot; ++s) {
             const uint32_t e = nbr[base + s];
             const Prim pj = prim[e & IDX_MASK];
             double xj[3];
             neighbour_pos<D>(e, pj, g, xj);
-            const double psij = ww[base + s] * Vi;
+            const double wij = ww[base + s];
             double d[3], dp[3];
 #pragma unroll
-            for (int a = 0; a < D; ++a) { d[a] = xj[a] - xi[a]; dp[a] = d[a] * psij; }
+            for (int a = 0; a < D; ++a) { d[a] = xj[a] - xi[a]; dp[a] = d[a] * wij; }
 #pragma unroll
             for (int a = 0; a < D; ++a)
 #pragma unroll
@@ -1191,7 +1193,7 @@ __global__ void __launch_bounds__(256) k_gradients(Params p, const Member *__res
             const Prim pj = prim[e & IDX_MASK];
             double xj[3];
             neighbour_pos<D>(e, pj, g, xj);
-            const double psij = ww[base + s] * Vi;
+            const double wij = ww[base + s];
             double d[3], ps[3];
 #pragma unroll
             for (int a = 0; a < D; ++a) d[a] = xj[a] - xi[a];
@@ -1200,7 +1202,7 @@ __global__ void __launch_bounds__(256) k_gradients(Params p, const Member *__res
                 double t = E[D * a] * d[0];
 #pragma unroll
                 for (int b = 1; b < D; ++b) t = fma(E[D * a + b], d[b], t);
-                ps[a] = t * psij;
+                ps[a] = t * wij;
             }
             // psi~_j(x_i) of this slot, reused by the face kernel for A_ij
             double *po = psiOut + (base + s) * 3;
@@ -1231,17 +1233,24 @@ __global__ void __launch_bounds__(256) k_gradients(Params p, const Member *__res
             const long long kmin = ord_key(DBL_MIN_), kmax = ord_key(DBL_MAX_);
 #pragma unroll
             for (int f = 0; f < NF; ++f) { mxN[f] = kmin; mnN[f] = kmax; mxM[f] = kmin; mnM[f] = kmax; }
+            // face point x_ij = x_i + c (x_j - x_i): c = 1/2 (first-order
+            // quadrature point) or h/4 (the reference's other choice);
+            // f_ij = f_i + grad f . (x_ij - x_i) as one FMA chain from f_i, with
+            // the gradients scaled by c for the pass instead of every offset
+            // (for c = 1/2 both the scaling and its undoing are exact)
+            const double cq = p.foqp ? .5 : hq / 4.;
+            const double icq = p.foqp ? 2. : 1. / cq;
+#pragma unroll
+            for (int f = 0; f < NF; ++f)
+#pragma unroll
+                for (int a = 0; a < D; ++a) gr[f][a] *= cq;
             for (int s = 0; s < tot; ++s) {
                 const uint32_t e = nbr[base + s];
                 const Prim pj = prim[e & IDX_MASK];
                 double xj[3], d[3];
                 neighbour_pos<D>(e, pj, g, xj);
-                // face point x_ij = x_i + c (x_j - x_i): c = 1/2 (first-order
-                // quadrature point) or h/4 (the reference's other choice);
-                // f_ij = f_i + grad f . (x_ij - x_i) as one FMA chain from f_i
-                const double cq = p.foqp ? .5 : hq / 4.;
 #pragma unroll
-                for (int a = 0; a < D; ++a) d[a] = cq * (xj[a] - xi[a]);
+                for (int a = 0; a < D; ++a) d[a] = xj[a] - xi[a];
 #pragma unroll
                 for (int f = 0; f < NF; ++f) {
                     const long long kj = ord_key(field_of<D>(pj, f));
@@ -1255,6 +1264,10 @@ __global__ void __launch_bounds__(256) k_gradients(Params p, const Member *__res
                     if (mnM[f] > kij) mnM[f] = kij;
                 }
             }
+#pragma unroll
+            for (int f = 0; f < NF; ++f)
+#pragma unroll
+                for (int a = 0; a < D; ++a) gr[f][a] *= icq;
 #pragma unroll
             for (int f = 0; f < NF; ++f) {
                 const double xN = key_double(mxN[f]), nN = key_double(mnN[f]);
@@ -1282,8 +1295,10 @@ __global__ void __launch_bounds__(256) k_gradients(Params p, const Member *__res
         // div v of the limited gradients, in the face kernel's order
         go.g[15] = D == 3 ? (go.g[3] + go.g[7]) + go.g[11] : go.g[3] + go.g[7];
         grad[i] = go;
+        // B_i = E_i^-1 = E'^-1 / V_i = E'^-1 omega_i (kept for inspection)
+        const double omega_i = geo[i].omega;
 #pragma unroll
-        for (int k = 0; k < D * D; ++k) geo[i].B[k] = E[k];
+        for (int k = 0; k < D * D; ++k) geo[i].B[k] = E[k] * omega_i;
     }
 }
 
