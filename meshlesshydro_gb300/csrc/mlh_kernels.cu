@@ -1056,11 +1056,11 @@ __global__ void __launch_bounds__(256) k_timestep(Params p, const Member *__rest
                 const double cj = geo[j].c;
                 double xij[3] = {pi.x - pj.x, pi.y - pj.y, pi.z - pj.z};
                 double vij[3] = {pi.vx - pj.vx, pi.vy - pj.vy, pi.vz - pj.vz};
-                // min(0, v_ij . x_ij / r): the quotient is needed only when the
-                // dot product is negative (same value and sign as the reference's)
+                // c_i + c_j - min(0, v_ij . x_ij / r) as one fused multiply-add:
+                // 1/r only when the dot product is negative, 0 otherwise
                 const double dv = dotD<D>(vij, xij);
-                const double vijxij = dneg(dv) ? fdiv(dv, rr[base + s]) : 0.;
-                double vs = ci + cj - vijxij;
+                const double ir = dneg(dv) ? frcp(rr[base + s]) : 0.;
+                const double vs = fma(-dv, ir, ci + cj);
                 vSig = dlt(vSig, vs) ? vs : vSig;
             }
             dti = (p.adaptive_h ? p.cfl * p.hp[i] : members[mi].cfl_h) / vSig;
