@@ -1841,18 +1841,40 @@ __global__ void __launch_bounds__(256) k_update(Params p, const int *__restrict_
         const size_t base = (size_t)i * p.K;
         const int tot = noi[i] + noiImg[i];
         double mF = 0., eF = 0., vF[3] = {0., 0., 0.};
-        for (int s = 0; s < tot; ++s) {
-            const int fo = faceOf[base + s];
-            if (fo == 0 || (fo > 0 ? fo : -fo) > p.faces_cap) continue;
-            const double2 *src = reinterpret_cast<const double2 *>(Fface + (size_t)((fo > 0 ? fo : -fo) - 1) * 6);
-            const double2 a = src[0], b = src[1], c = src[2];
-            // the flux with the slot's sign: the sign bit flipped on the
-            // integer pipe for a copied face, so that both kinds of slot
-            // share one set of additions (x + (-f) is the same double as
-            // adding the negated flux)
-            const long long sg = fo > 0 ? 0ll : (long long)0x8000000000000000ull;
-            auto sgn = [sg](double f) { return __longlong_as_double(__double_as_longlong(f) ^ sg); };
-            mF += sgn(a.x); vF[0] += sgn(b.x); vF[1] += sgn(b.y); if (D == 3) vF[2] += sgn(c.x); eF += sgn(a.y);
+        // four slots at a time: their face ids in one 16-byte load (K is a
+        // multiple of 4) and all twelve flux loads issued before the sums,
+        // which still run in slot order
+        const int4 *fo4 = reinterpret_cast<const int4 *>(faceOf + base);
+        for (int s0 = 0; s0 < tot; s0 += 4) {
+            const int4 f4 = fo4[s0 >> 2];
+            const int fos[4] = {f4.x, f4.y, f4.z, f4.w};
+            double2 fa[4], fb[4], fc[4];
+#pragma unroll
+            for (int k = 0; k < 4; ++k) {
+                const int fo = fos[k];
+                const int af = fo > 0 ? fo : -fo;
+                if (s0 + k < tot && fo != 0 && af <= p.faces_cap) {
+                    const double2 *src = reinterpret_cast<const double2 *>(Fface + (size_t)(af - 1) * 6);
+                    fa[k] = src[0]; fb[k] = src[1]; fc[k] = src[2];
+                } else {
+                    fa[k] = fb[k] = fc[k] = make_double2(0., 0.);
+                }
+            }
+#pragma unroll
+            for (int k = 0; k < 4; ++k) {
+                const int fo = fos[k];
+                const int af = fo > 0 ? fo : -fo;
+                if (!(s0 + k < tot && fo != 0 && af <= p.faces_cap)) continue;
+                // the flux with the slot's sign: the sign bit flipped on the
+                // integer pipe for a copied face, so that both kinds of slot
+                // share one set of additions (x + (-f) is the same double as
+                // adding the negated flux)
+                const long long sg = fo > 0 ? 0ll : (long long)0x8000000000000000ull;
+                auto sgn = [sg](double f) { return __longlong_as_double(__double_as_longlong(f) ^ sg); };
+                mF += sgn(fa[k].x); vF[0] += sgn(fb[k].x); vF[1] += sgn(fb[k].y);
+                if (D == 3) vF[2] += sgn(fc[k].x);
+                eF += sgn(fa[k].y);
+            }
         }
         if (fluxSums) {
             fluxSums[(size_t)i * 5 + 0] = mF;
