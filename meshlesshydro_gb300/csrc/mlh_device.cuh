@@ -81,6 +81,10 @@ struct Prim {       // positions, primitive state of this step
 };
 struct Grad {       // limited gradients: rho, vx, vy, vz, P (x,y,z each), div v
     double g[16];
+    // particle part of the half-step prediction of each field, in the order
+    // rho, P, vx, vy, vz: rho div v + v.grad rho, gamma P div v + v.grad P,
+    // (grad P)_a / rho + v.grad v_a (the face subtracts v_frame.grad f)
+    double t[8];
 };
 struct Geo {        // E_i^{-1}, 1/omega_i, omega_i, sound speed, 1/rho_i
     double B[9];

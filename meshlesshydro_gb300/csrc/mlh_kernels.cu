@@ -1218,6 +1218,7 @@ __global__ void __launch_bounds__(256) k_gradients(Params p, const Member *__res
         if (gradRaw) {
             Grad graw;
             for (int k = 0; k < 16; ++k) graw.g[k] = 0.;
+            for (int k = 0; k < 8; ++k) graw.t[k] = 0.;
 #pragma unroll
             for (int f = 0; f < NF; ++f) {
                 int slot = (f == NF - 1) ? 4 : f;
@@ -1294,6 +1295,17 @@ __global__ void __launch_bounds__(256) k_gradients(Params p, const Member *__res
         }
         // div v of the limited gradients, in the face kernel's order
         go.g[15] = D == 3 ? (go.g[3] + go.g[7]) + go.g[11] : go.g[3] + go.g[7];
+        {   // the particle part of the half-step prediction (fma chains)
+            const double *G = go.g;
+            const double div = go.g[15], irho = geo[i].irho;
+            const double v[3] = {pi.vx, pi.vy, pi.vz};
+            const double src[5] = {pi.rho * div, (p.gamma * pi.P) * div, G[12] * irho, G[13] * irho, G[14] * irho};
+            const int blk[5] = {0, 12, 3, 6, 9};
+#pragma unroll
+            for (int f = 0; f < 8; ++f) go.t[f] = 0.;
+#pragma unroll
+            for (int f = 0; f < D + 2; ++f) go.t[f] = fma_dotD<D>(v, G + blk[f], src[f]);
+        }
         grad[i] = go;
         // B_i = E_i^-1 = E'^-1 / V_i = E'^-1 omega_i (kept for inspection)
         const double omega_i = geo[i].omega;
@@ -1660,32 +1672,21 @@ __global__ void MLH_FACE_BOUNDS k_faces(Params p, const Member *__restrict__ mem
         {
             // div v and 1/rho of both particles, stored once per particle
             // (gradient pad slot, Geo) with the same arithmetic
-            const double viDiv = Gi[15], vjDiv = Gj[15];
+            // W -= dt/2 (source + (v - v_frame) . grad W): the particle part,
+            // source + v . grad W, comes with the gradients (Grad::t); the face
+            // subtracts v_frame . grad W (one FMA chain per field and side)
             const double hdt = dt / 2.;
-            const double iri = geo[i].irho, irj = geo[j].irho;
-            // the boosted velocities v - v_frame, saved before the reconstruction
-            const double ui0 = Rb[2], ui1 = Rb[3], uj0 = Lb[2], uj1 = Lb[3];
-            R[0] -= hdt * (pi.rho * viDiv + ui0 * Gi[0] + ui1 * Gi[1]);
-            L[0] -= hdt * (pj.rho * vjDiv + uj0 * Gj[0] + uj1 * Gj[1]);
-            R[1] -= hdt * (gamma * pi.P * viDiv + ui0 * Gi[12] + ui1 * Gi[13]);
-            L[1] -= hdt * (gamma * pj.P * vjDiv + uj0 * Gj[12] + uj1 * Gj[13]);
-            R[2] -= hdt * (Gi[12] * iri + ui0 * Gi[3] + ui1 * Gi[4]);
-            L[2] -= hdt * (Gj[12] * irj + uj0 * Gj[3] + uj1 * Gj[4]);
-            R[3] -= hdt * (Gi[13] * iri + ui0 * Gi[6] + ui1 * Gi[7]);
-            L[3] -= hdt * (Gj[13] * irj + uj0 * Gj[6] + uj1 * Gj[7]);
-            if (D == 3) {
-                const double ui2 = Rb[4], uj2 = Lb[4];
-                R[0] -= hdt * ui2 * Gi[2];
-                L[0] -= hdt * uj2 * Gj[2];
-                R[1] -= hdt * ui2 * Gi[14];
-                L[1] -= hdt * uj2 * Gj[14];
-                // the reference uses vz[i] on the j side here (Particles.cpp:1717,1719)
-                R[2] -= hdt * ui2 * Gi[5];
-                L[2] -= hdt * ui2 * Gj[5];
-                R[3] -= hdt * ui2 * Gi[8];
-                L[3] -= hdt * ui2 * Gj[8];
-                R[4] -= hdt * (Gi[14] * iri + ui0 * Gi[9] + ui1 * Gi[10] + ui2 * Gi[11]);
-                L[4] -= hdt * (Gj[14] * irj + uj0 * Gj[9] + uj1 * Gj[10] + uj2 * Gj[11]);
+            const double *Ti = grad[i].t, *Tj = grad[j].t;
+            const double nvf[3] = {-vf[0], -vf[1], -vf[2]};
+            // the reference uses vz[i] on the j side of the vx and vy terms
+            // (Particles.cpp:1717,1719): (vz_i - vf_z) = (vz_j - (vf_z + vz_j - vz_i))
+            const double nvq[3] = {-vf[0], -vf[1], D == 3 ? -(vf[2] - (vi[2] - vj[2])) : 0.};
+            const int blk[5] = {0, 12, 3, 6, 9};
+#pragma unroll
+            for (int f = 0; f < NV; ++f) {
+                R[f] = fma(-hdt, fma_dotD<D>(nvf, Gi + blk[f], Ti[f]), R[f]);
+                const double *nj = (D == 3 && (f == 2 || f == 3)) ? nvq : nvf;
+                L[f] = fma(-hdt, fma_dotD<D>(nj, Gj + blk[f], Tj[f]), L[f]);
             }
         }
         if (dneg(R[1]) || dneg(L[1])) st_local |= ST_NEG_PRESSURE;
