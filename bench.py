@@ -53,8 +53,8 @@ LAUNCHES_PER_STEP = 20
 # (profiles/sedov64_step_kernels.md); 2D: 32 members of the Kelvin-Helmholtz
 # ensemble with the second Newton pass (profiles/kh_ensemble32_step_kernels.md;
 # the tuned single pass does about the same arithmetic per face).
-FACE_FP64_FLOPS = {3: 552.0, 2: 427.0}
-FACE_DRAM_BYTES = {3: 288.0, 2: 355.0}
+FACE_FP64_FLOPS = {3: 544.0, 2: 417.0}
+FACE_DRAM_BYTES = {3: 298.0, 2: 362.0}
 
 
 def make_workload(name: str, seed_offset: int = 0):
