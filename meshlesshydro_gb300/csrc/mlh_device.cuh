@@ -69,6 +69,7 @@ struct Params {
     // search radius (grid cells, periodic-image band)
     int adaptive_h;
     double cfl;            // CFL (cfl_h = CFL * kernelSize without adaptive_h)
+    int face_split;        // faces unfinished after one Newton step go to a second pass
     double sngb_t;         // target of S = sum_j f(2 r_ij / h_i): n_ngb / K_D - 1
     const double *hp;
     const float *hpf;      // hp rounded up to single precision (pre-filter)

@@ -1703,7 +1703,7 @@ __global__ void MLH_FACE_BOUNDS k_faces(Params p, const Member *__restrict__ mem
         // MODE 1 defers faces whose two-rarefaction guess says strong shock
         const double defer = MODE == 1 ? PSTAR_HARD * (dlt(L[1], R[1]) ? L[1] : R[1]) : 0.;   // min on the keys
         RiemannResult rs = ROOT5 ? riemann_exact5(rc, R[0], unR, R[1], L[0], unL, L[1], guess, defer,
-                                                  (MODE == 1 || MODE == 3) ? 1 : 0)
+                                                  (MODE == 3 || (MODE == 1 && p.face_split)) ? 1 : 0)
                                  : riemann_exact(rc, R[0], unR, R[1], L[0], unL, L[1], guess, defer);
         // deferred faces: strong shocks of MODE 1 (unsolved, iters 0) go to
         // queue A for the network; faces Newton has not finished after one
@@ -2056,10 +2056,12 @@ void launch_step(StepArgs &a) {
 
     tick(KT_FACES);
     const int fT = a.tune.face_threads, fB = a.sm_count * a.tune.face_blocks_per_sm;
+    Params pf = p;   // the face passes see the tuned split
+    pf.face_split = a.tune.face_split;
     const FaceQueue qa{a.fstate, a.queueFace, a.queueCount, a.qcap};
     const FaceQueue qb{a.fstate2, a.queueFace2, a.queueCount2, a.qcap2};
 #define MLH_FACES(R5, MODE, QA, QB)                                                                              \
-    k_faces<D, R5, MODE><<<fB, fT, 0, s>>>(p, a.members, a.memberOf, a.grids, a.prim, a.geo, a.grad, a.nbr, a.psi, \
+    k_faces<D, R5, MODE><<<fB, fT, 0, s>>>(pf, a.members, a.memberOf, a.grids, a.prim, a.geo, a.grad, a.nbr, a.psi, \
                                            a.faceOff + p.n, a.faces, a.dt, a.Fface, a.newtonSum, a.status, QA,   \
                                            QB, a.feat, a.yguess, a.harvest)
     if (a.learned) {
@@ -2069,7 +2071,7 @@ void launch_step(StepArgs &a) {
         if (a.root5) MLH_FACES(true, 1, qa, qb); else MLH_FACES(false, 1, qa, qb);
         pstar_infer_dev(a.feat, a.queueCount, (int)a.faces_cap, a.mlp_packed, a.yguess, a.sm_count, s);
         if (a.root5) MLH_FACES(true, 2, qa, qb); else MLH_FACES(false, 2, qa, qb);
-        if (a.root5 && a.fstate2) MLH_FACES(true, 4, qb, qb);
+        if (a.root5 && a.fstate2 && a.tune.face_split) MLH_FACES(true, 4, qb, qb);
     } else if (a.root5 && a.fstate && a.harvest.stride == 0 && a.tune.face_split) {
         // unconverged faces after one Newton step go to a second, dense pass
         cudaMemsetAsync(a.queueCount, 0, sizeof(int), s);
