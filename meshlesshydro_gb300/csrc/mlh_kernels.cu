@@ -957,25 +957,46 @@ __global__ void __launch_bounds__(NNS_WARPS * 32) k_hsolve(
                 const unsigned act = __ballot_sync(0xffffffffu, !done);
                 if (!act) break;
                 const double ihh2 = __ddiv_rn(1., __dmul_rn(0.5, xh));
-                for (unsigned m = act; m; m &= m - 1) {
-                    const int q = __ffs(m) - 1;
-                    const double ihq = __shfl_sync(0xffffffffu, ihh2, q);
-                    const int nrq_ = __shfl_sync(0xffffffffu, mynr, q);
-                    const double *rl = rlq + (size_t)q * CAP;
-                    double sf = 0., sg = 0.;
-                    for (int t = lane; t < nrq_; t += 32) {
-                        double f, gg;
-                        hsolve_shape_sel(rl[t], ihq, f, gg);
-                        sf = __dadd_rn(sf, f);
-                        sg = __dadd_rn(sg, gg);
-                    }
+                // 32 lane-strided partial sums of f and g per unfinished
+                // particle: v[2q], v[2q + 1]
+                double v[2 * HS_PB];
 #pragma unroll
-                    for (int o = 16; o > 0; o >>= 1) {
-                        sf = __dadd_rn(sf, __shfl_xor_sync(0xffffffffu, sf, o));
-                        sg = __dadd_rn(sg, __shfl_xor_sync(0xffffffffu, sg, o));
+                for (int q = 0; q < HS_PB; ++q) {
+                    v[2 * q] = 0.;
+                    v[2 * q + 1] = 0.;
+                    if (act & (1u << q)) {
+                        const double ihq = __shfl_sync(0xffffffffu, ihh2, q);
+                        const int nrq_ = __shfl_sync(0xffffffffu, mynr, q);
+                        const double *rl = rlq + (size_t)q * CAP;
+                        for (int t = lane; t < nrq_; t += 32) {
+                            double f, gg;
+                            hsolve_shape_sel(rl[t], ihq, f, gg);
+                            v[2 * q] = __dadd_rn(v[2 * q], f);
+                            v[2 * q + 1] = __dadd_rn(v[2 * q + 1], gg);
+                        }
                     }
-                    if (lane == q) { sfq = sf; sgq = sg; }
                 }
+                // reduce-scatter of the 16 partial sums: at distance d = 16,
+                // 8, 4, 2 each lane keeps half of its values and adds its
+                // partner's (own + partner, the pairs of an xor butterfly, so
+                // every sum has the butterfly's tree and bits), then d = 1;
+                // sum k ends on lanes 2k and 2k + 1
+#pragma unroll
+                for (int d = 16, m = HS_PB; d > 1; d >>= 1, m >>= 1) {
+                    const bool upper = (lane & d) != 0;
+#pragma unroll
+                    for (int j = 0; j < 8; ++j) {
+                        if (j < m) {
+                            const double send = upper ? v[j] : v[j + m];
+                            const double keep = upper ? v[j + m] : v[j];
+                            v[j] = __dadd_rn(keep, __shfl_xor_sync(0xffffffffu, send, d));
+                        }
+                    }
+                }
+                v[0] = __dadd_rn(v[0], __shfl_xor_sync(0xffffffffu, v[0], 1));
+                // particle q (lane q) takes sum 2q (lane 4q) and 2q + 1 (lane 4q + 2)
+                sfq = __shfl_sync(0xffffffffu, v[0], (4 * lane) & 31);
+                sgq = __shfl_sync(0xffffffffu, v[0], (4 * lane + 2) & 31);
                 if (!done) {
                     S = sfq;
                     const double G = sgq;
