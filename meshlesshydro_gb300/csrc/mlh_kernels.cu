@@ -768,6 +768,9 @@ __global__ void __launch_bounds__(NNS_WARPS * 32, MLH_NNS_MINB) k_neighbours(
 // per particle.
 constexpr int HSOLVE_MAXIT = 50;
 constexpr int HS_PB = 8;
+// the reduce-scatter of the solve's sums maps the 2 HS_PB = 16 sums onto
+// the 32 lanes (sum k on lanes 2k and 2k + 1)
+static_assert(HS_PB == 8, "k_hsolve reduces exactly 16 sums per batch");
 
 // staged chunk (NNS_CH entries and positions), HS_PB candidate lists (K + 32
 // uint32) and their counts, HS_PB distance lists (K + 32 doubles) and their
