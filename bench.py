@@ -290,7 +290,7 @@ def adaptive_section(runtime, cfg, p, tuning, args, ws):
     cfg_a = replace(cfg, adaptive_h=True, n_ngb=32.0, kernel_size=cfg.kernel_size * 1.25)
     sim = runtime.Simulation(cfg_a, p)
     # its own launch shapes: the wider search radius changes the best ones
-    tuning_a = sim.autotune(1) if tuning else None
+    tuning_a = sim.autotune(2) if tuning else None
     sim.step(args.warmup)
     torch.cuda.synchronize()
     st = sim.step(args.steps)
@@ -330,7 +330,7 @@ def run_mlh(args):
     sim = runtime.Simulation(cfg, members=members) if ensemble else runtime.Simulation(cfg, p)
     if ensemble:
         p = sim.host  # concatenated state: .n
-    tuning = None if args.no_autotune else sim.autotune(1)
+    tuning = None if args.no_autotune else sim.autotune(2)
     sim.step(args.warmup)
     if dist:
         dist.barrier()

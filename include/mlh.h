@@ -141,9 +141,11 @@ typedef struct mlh_tuning {
     int face_blocks_per_sm;  /* blocks per SM of its grid-stride loop */
     int grad_threads;        /* threads per block, gradient/limiter kernel */
     int nns_warps_per_sm;    /* warps per SM of the neighbour search */
-    int face_split;          /* 1: faces Newton has not finished after one step
-                              * go to a second, dense pass; 0: one pass (the
-                              * plain gamma = 5/3 step only) */
+    int face_split;          /* faces Newton has not finished after one step:
+                              * 1 go to a second, dense pass over a queue;
+                              * 2 are continued inside the block by its first
+                              * threads; 0: one pass (the plain gamma = 5/3
+                              * step only) */
 } mlh_tuning;
 
 /* Autotuner: times the face passes with and without the split, then
@@ -154,7 +156,7 @@ typedef struct mlh_tuning {
 int mlh_autotune(mlh_ctx *ctx, int trial_steps, mlh_tuning *out);
 /* Set the launch shapes directly (for example those an autotuned context of
  * the same workload reported).  Threads per block: 64, 128 or 256; blocks
- * per SM 1..32; warps per SM 8..256; face_split 0 or 1.  MLH_ERR_INVALID
+ * per SM 1..32; warps per SM 8..256; face_split 0, 1 or 2.  MLH_ERR_INVALID
  * otherwise. */
 int mlh_set_tuning(mlh_ctx *ctx, const mlh_tuning *tuning);
 

@@ -643,7 +643,7 @@ int mlh_set_tuning(mlh_ctx *c, const mlh_tuning *t) {
     auto threads_ok = [](int v) { return v == 64 || v == 128 || v == 256; };
     if (!c || !t || !threads_ok(t->face_threads) || !threads_ok(t->grad_threads) || t->face_blocks_per_sm < 1 ||
         t->face_blocks_per_sm > 32 || t->nns_warps_per_sm < 8 || t->nns_warps_per_sm > 256 ||
-        (t->face_split != 0 && t->face_split != 1)) {
+        t->face_split < 0 || t->face_split > 2) {
         g_last_error = "invalid tuning";
         return MLH_ERR_INVALID;
     }
@@ -699,24 +699,29 @@ int mlh_autotune(mlh_ctx *c, int trial_steps, mlh_tuning *out) {
         const int cand_b[] = {2, 4, 8, 16, 32};
         Tuning best = c->tune;
         double best_ms = 1e300;
-        // the second Newton pass pays where few faces need a second step
-        // (Sedov: a fifth) and may not where half do (Kelvin-Helmholtz)
-        for (int split : {1, 0}) {
-            c->tune.face_split = split;
-            double ms;
-            if ((rc = trial(KT_FACES, ms))) goto done;
-            if (ms < best_ms) { best_ms = ms; best.face_split = split; }
+        // the face passes: one (0), a second over a queue (1) or the
+        // unfinished faces continued inside the block (2), each over the
+        // candidate grids (the structures favour different grids); which
+        // pays depends on how many faces need a second Newton step
+        for (int split : {1, 2, 0}) {
+            for (int b : cand_b) {
+                c->tune.face_split = split;
+                c->tune.face_blocks_per_sm = b;
+                double ms;
+                if ((rc = trial(KT_FACES, ms))) goto done;
+                if (ms < best_ms) { best_ms = ms; best.face_split = split; best.face_blocks_per_sm = b; }
+            }
         }
         c->tune.face_split = best.face_split;
+        c->tune.face_blocks_per_sm = best.face_blocks_per_sm;
         for (int t : cand_t) {
             c->tune.face_threads = t;
-            c->tune.face_blocks_per_sm = best.face_blocks_per_sm;
             double ms;
             if ((rc = trial(KT_FACES, ms))) goto done;
             if (ms < best_ms) { best_ms = ms; best.face_threads = t; }
         }
         c->tune.face_threads = best.face_threads;
-        for (int b : cand_b) {
+        for (int b : cand_b) {   // the grid again, for the chosen block size
             c->tune.face_blocks_per_sm = b;
             double ms;
             if ((rc = trial(KT_FACES, ms))) goto done;

@@ -1559,6 +1559,147 @@ __device__ __forceinline__ unsigned project_flux(const RiemannResult &rs, const 
 #define MLH_FACE_MAXREG 168
 #endif
 #define MLH_FACE_BOUNDS __maxnreg__(MLH_FACE_MAXREG)
+// The face-frame Riemann problem of canonical face f (i < j): effective face
+// A_ij = psi~_j(x_i)/omega_i - psi~_i(x_j)/omega_j from the psi~ of both
+// slots (compEffectiveFace, Particles.cpp:1290-1311, 2504-2531); boosted,
+// reconstructed, optionally pairwise-limited and half-step-predicted states
+// (compRiemannStatesLR, :1488-1733 / 2533-2683, including the vz[i] of
+// :1717,1719); the face normal and the normal velocity components
+// (face_normal).  R (particle i, the left state) and L: [rho, P, v..] with
+// unrotated velocities.  Returns false for a face without its links (the
+// status bit is set).
+template <int D>
+__device__ __forceinline__ bool face_states(const Params &p, const Member *__restrict__ members,
+                                            const int *__restrict__ memberOf, const GridInfo *__restrict__ grids,
+                                            const Prim *__restrict__ prim, const Geo *__restrict__ geo,
+                                            const Grad *__restrict__ grad, const uint32_t *__restrict__ nbr,
+                                            const double *__restrict__ psi, const FaceRef *__restrict__ faces,
+                                            const double *__restrict__ dtp, int f, unsigned &st_local, double *R,
+                                            double *L, double *A, double *vf, double *hatA, double &unR,
+                                            double &unL) {
+    constexpr int NV = D + 2;
+    const FaceRef fr = faces[f];
+    if (fr.i < 0 || fr.slot < 0) {
+        st_local |= ST_ASYMMETRIC;
+        return false;
+    }
+    const int i = fr.i;
+    const int mi = memberOf ? memberOf[i] : 0;
+    const double dt = dtp[mi];
+    const double h = members[mi].h;
+    const double hq = p.adaptive_h ? p.hp[i] : h;   // quadrature-point radius
+    const size_t si = (size_t)i * p.K + fr.slot;
+    const uint32_t e = nbr[si];
+    const int j = (int)(e & IDX_MASK);
+    const bool img = (e >> IMG_SHIFT) != 0;
+    const Prim pi = prim[i], pj = prim[j];
+    const double Vi = geo[i].V, Vj = geo[j].V;
+    double xi[3] = {pi.x, pi.y, pi.z}, xj[3];
+    if (img) neighbour_pos<D>(e, pj, grids[mi], xj);
+    else { xj[0] = pj.x; xj[1] = pj.y; xj[2] = pj.z; }
+    // --- effective face
+    {
+        const double *ps_i = psi + si * 3;
+        if (fr.rslot >= 0) {
+            const double *ps_j = psi + ((size_t)j * p.K + fr.rslot) * 3;
+#pragma unroll
+            for (int a = 0; a < D; ++a) A[a] = Vi * ps_i[a] - Vj * ps_j[a];
+        } else {
+            st_local |= ST_ASYMMETRIC;
+#pragma unroll
+            for (int a = 0; a < D; ++a) A[a] = Vi * ps_i[a];
+        }
+    }
+    // --- states at the face
+    double xijxi[3], xjxi[3], xijxj[3];
+#pragma unroll
+    for (int a = 0; a < D; ++a) {
+        xjxi[a] = xj[a] - xi[a];
+        if (p.foqp) {
+            // .5 (x_j - x_i), and .5 (x_i - x_j) is its exact negation
+            xijxi[a] = .5 * xjxi[a];
+            xijxj[a] = -xijxi[a];
+        } else {
+            double xij = xi[a] + hq / 4. * xjxi[a];
+            xijxi[a] = xij - xi[a];
+            xijxj[a] = xij - xj[a];
+        }
+    }
+    const double vi[3] = {pi.vx, pi.vy, pi.vz}, vj[3] = {pj.vx, pj.vy, pj.vz};
+    if (p.move) {
+        if (p.foqp) {
+#pragma unroll
+            for (int a = 0; a < D; ++a) vf[a] = (vi[a] + vj[a]) / 2.;
+        } else {
+            double dotProd = dotD<D>(xijxi, xjxi);
+            double dSqr = dotD<D>(xjxi, xjxi);
+#pragma unroll
+            for (int a = 0; a < D; ++a) vf[a] = vi[a] + (vj[a] - vi[a]) * dotProd / dSqr;
+        }
+    }
+    const double *Gi = grad[i].g, *Gj = grad[j].g;
+    // gradient blocks: 0 rho, 3 vx, 6 vy, 9 vz, 12 P
+    R[0] = pi.rho; L[0] = pj.rho;
+    R[1] = pi.P; L[1] = pj.P;
+#pragma unroll
+    for (int a = 0; a < D; ++a) { R[2 + a] = vi[a] - vf[a]; L[2 + a] = vj[a] - vf[a]; }
+    double Rb[5], Lb[5];
+#pragma unroll
+    for (int k = 0; k < NV; ++k) { Rb[k] = R[k]; Lb[k] = L[k]; }
+    // W + grad W . (x_ij - x_side), one FMA chain from W per field
+    R[0] = fma_dotD<D>(Gi + 0, xijxi, R[0]); L[0] = fma_dotD<D>(Gj + 0, xijxj, L[0]);
+    R[1] = fma_dotD<D>(Gi + 12, xijxi, R[1]); L[1] = fma_dotD<D>(Gj + 12, xijxj, L[1]);
+    R[2] = fma_dotD<D>(Gi + 3, xijxi, R[2]); L[2] = fma_dotD<D>(Gj + 3, xijxj, L[2]);
+    R[3] = fma_dotD<D>(Gi + 6, xijxi, R[3]); L[3] = fma_dotD<D>(Gj + 6, xijxj, L[3]);
+    if (D == 3) { R[4] = fma_dotD<D>(Gi + 9, xijxi, R[4]); L[4] = fma_dotD<D>(Gj + 9, xijxj, L[4]); }
+    if (p.pairwise && (!img || p.img_pw)) {
+        double ri, rj;   // |x_ij - x_i| / |x_j - x_i| and |x_ij - x_j| / |x_j - x_i|
+        if (p.foqp) {
+            // x_ij - x_i = (x_j - x_i) / 2 exactly, so both norms are
+            // exactly half of |x_j - x_i| (scaling by 1/2 and 1/4 is exact)
+            // and both quotients are exactly 0.5
+            ri = .5; rj = .5;
+        } else {
+            double xijxi_abs = 0., xijxj_abs = 0., xjxi_abs = 0.;
+#pragma unroll
+            for (int a = 0; a < D; ++a) {
+                xijxi_abs += xijxi[a] * xijxi[a];
+                xijxj_abs += xijxj[a] * xijxj[a];
+                xjxi_abs += xjxi[a] * xjxi[a];
+            }
+            xjxi_abs = sqrt(xjxi_abs);
+            ri = sqrt(xijxi_abs) / xjxi_abs;
+            rj = sqrt(xijxj_abs) / xjxi_abs;
+        }
+#pragma unroll
+        for (int k = 0; k < NV; ++k) pairwise_limiter(p, R[k], L[k], Rb[k], Lb[k], ri, rj);
+    }
+    {
+        // div v and 1/rho of both particles, stored once per particle
+        // (gradient pad slot, Geo) with the same arithmetic
+        // W -= dt/2 (source + (v - v_frame) . grad W): the particle part,
+        // source + v . grad W, comes with the gradients (Grad::t); the face
+        // subtracts v_frame . grad W (one FMA chain per field and side)
+        const double hdt = dt / 2.;
+        const double *Ti = grad[i].t, *Tj = grad[j].t;
+        const double nvf[3] = {-vf[0], -vf[1], -vf[2]};
+        // the reference uses vz[i] on the j side of the vx and vy terms
+        // (Particles.cpp:1717,1719): (vz_i - vf_z) = (vz_j - (vf_z + vz_j - vz_i))
+        const double nvq[3] = {-vf[0], -vf[1], D == 3 ? -(vf[2] - (vi[2] - vj[2])) : 0.};
+        const int blk[5] = {0, 12, 3, 6, 9};
+#pragma unroll
+        for (int f = 0; f < NV; ++f) {
+            R[f] = fma(-hdt, fma_dotD<D>(nvf, Gi + blk[f], Ti[f]), R[f]);
+            const double *nj = (D == 3 && (f == 2 || f == 3)) ? nvq : nvf;
+            L[f] = fma(-hdt, fma_dotD<D>(nj, Gj + blk[f], Tj[f]), L[f]);
+        }
+    }
+    if (dneg(R[1]) || dneg(L[1])) st_local |= ST_NEG_PRESSURE;
+    // --- Riemann problem in the face frame (i left, j right)
+    face_normal<D>(A, R, L, hatA, unR, unL);
+    return true;
+}
+
 template <int D, bool ROOT5, int MODE>
 __global__ void MLH_FACE_BOUNDS k_faces(Params p, const Member *__restrict__ members,
                                                const int *__restrict__ memberOf, const GridInfo *__restrict__ grids,
@@ -1570,7 +1711,6 @@ __global__ void MLH_FACE_BOUNDS k_faces(Params p, const Member *__restrict__ mem
                                                unsigned *__restrict__ status, FaceQueue qa, FaceQueue qb,
                                                float4 *__restrict__ feat, const float *__restrict__ yguess,
                                                Harvest hv) {
-    constexpr int NV = D + 2;
     int nf = *faceTotal < p.faces_cap ? *faceTotal : p.faces_cap;
     constexpr bool QUEUED = MODE == 2 || MODE == 4;   // passes over the queue
     if (QUEUED) {   // the queue holds min(count, capacity) faces; MODE 3 finished the rest itself
@@ -1597,125 +1737,9 @@ __global__ void MLH_FACE_BOUNDS k_faces(Params p, const Member *__restrict__ mem
             unR = dotD<D>(hatA, R + 2);
             unL = dotD<D>(hatA, L + 2);
         } else {
-        const FaceRef fr = faces[f];
-        if (fr.i < 0 || fr.slot < 0) {
-            st_local |= ST_ASYMMETRIC;
+        if (!face_states<D>(p, members, memberOf, grids, prim, geo, grad, nbr, psi, faces, dtp, f, st_local, R, L, A,
+                            vf, hatA, unR, unL))
             continue;
-        }
-        const int i = fr.i;
-        const int mi = memberOf ? memberOf[i] : 0;
-        const double dt = dtp[mi];
-        const double h = members[mi].h;
-        const double hq = p.adaptive_h ? p.hp[i] : h;   // quadrature-point radius
-        const size_t si = (size_t)i * p.K + fr.slot;
-        const uint32_t e = nbr[si];
-        const int j = (int)(e & IDX_MASK);
-        const bool img = (e >> IMG_SHIFT) != 0;
-        const Prim pi = prim[i], pj = prim[j];
-        const double Vi = geo[i].V, Vj = geo[j].V;
-        double xi[3] = {pi.x, pi.y, pi.z}, xj[3];
-        if (img) neighbour_pos<D>(e, pj, grids[mi], xj);
-        else { xj[0] = pj.x; xj[1] = pj.y; xj[2] = pj.z; }
-        // --- effective face
-        {
-            const double *ps_i = psi + si * 3;
-            if (fr.rslot >= 0) {
-                const double *ps_j = psi + ((size_t)j * p.K + fr.rslot) * 3;
-#pragma unroll
-                for (int a = 0; a < D; ++a) A[a] = Vi * ps_i[a] - Vj * ps_j[a];
-            } else {
-                st_local |= ST_ASYMMETRIC;
-#pragma unroll
-                for (int a = 0; a < D; ++a) A[a] = Vi * ps_i[a];
-            }
-        }
-        // --- states at the face
-        double xijxi[3], xjxi[3], xijxj[3];
-#pragma unroll
-        for (int a = 0; a < D; ++a) {
-            xjxi[a] = xj[a] - xi[a];
-            if (p.foqp) {
-                // .5 (x_j - x_i), and .5 (x_i - x_j) is its exact negation
-                xijxi[a] = .5 * xjxi[a];
-                xijxj[a] = -xijxi[a];
-            } else {
-                double xij = xi[a] + hq / 4. * xjxi[a];
-                xijxi[a] = xij - xi[a];
-                xijxj[a] = xij - xj[a];
-            }
-        }
-        const double vi[3] = {pi.vx, pi.vy, pi.vz}, vj[3] = {pj.vx, pj.vy, pj.vz};
-        if (p.move) {
-            if (p.foqp) {
-#pragma unroll
-                for (int a = 0; a < D; ++a) vf[a] = (vi[a] + vj[a]) / 2.;
-            } else {
-                double dotProd = dotD<D>(xijxi, xjxi);
-                double dSqr = dotD<D>(xjxi, xjxi);
-#pragma unroll
-                for (int a = 0; a < D; ++a) vf[a] = vi[a] + (vj[a] - vi[a]) * dotProd / dSqr;
-            }
-        }
-        const double *Gi = grad[i].g, *Gj = grad[j].g;
-        // gradient blocks: 0 rho, 3 vx, 6 vy, 9 vz, 12 P
-        R[0] = pi.rho; L[0] = pj.rho;
-        R[1] = pi.P; L[1] = pj.P;
-#pragma unroll
-        for (int a = 0; a < D; ++a) { R[2 + a] = vi[a] - vf[a]; L[2 + a] = vj[a] - vf[a]; }
-        double Rb[5], Lb[5];
-#pragma unroll
-        for (int k = 0; k < NV; ++k) { Rb[k] = R[k]; Lb[k] = L[k]; }
-        // W + grad W . (x_ij - x_side), one FMA chain from W per field
-        R[0] = fma_dotD<D>(Gi + 0, xijxi, R[0]); L[0] = fma_dotD<D>(Gj + 0, xijxj, L[0]);
-        R[1] = fma_dotD<D>(Gi + 12, xijxi, R[1]); L[1] = fma_dotD<D>(Gj + 12, xijxj, L[1]);
-        R[2] = fma_dotD<D>(Gi + 3, xijxi, R[2]); L[2] = fma_dotD<D>(Gj + 3, xijxj, L[2]);
-        R[3] = fma_dotD<D>(Gi + 6, xijxi, R[3]); L[3] = fma_dotD<D>(Gj + 6, xijxj, L[3]);
-        if (D == 3) { R[4] = fma_dotD<D>(Gi + 9, xijxi, R[4]); L[4] = fma_dotD<D>(Gj + 9, xijxj, L[4]); }
-        if (p.pairwise && (!img || p.img_pw)) {
-            double ri, rj;   // |x_ij - x_i| / |x_j - x_i| and |x_ij - x_j| / |x_j - x_i|
-            if (p.foqp) {
-                // x_ij - x_i = (x_j - x_i) / 2 exactly, so both norms are
-                // exactly half of |x_j - x_i| (scaling by 1/2 and 1/4 is exact)
-                // and both quotients are exactly 0.5
-                ri = .5; rj = .5;
-            } else {
-                double xijxi_abs = 0., xijxj_abs = 0., xjxi_abs = 0.;
-#pragma unroll
-                for (int a = 0; a < D; ++a) {
-                    xijxi_abs += xijxi[a] * xijxi[a];
-                    xijxj_abs += xijxj[a] * xijxj[a];
-                    xjxi_abs += xjxi[a] * xjxi[a];
-                }
-                xjxi_abs = sqrt(xjxi_abs);
-                ri = sqrt(xijxi_abs) / xjxi_abs;
-                rj = sqrt(xijxj_abs) / xjxi_abs;
-            }
-#pragma unroll
-            for (int k = 0; k < NV; ++k) pairwise_limiter(p, R[k], L[k], Rb[k], Lb[k], ri, rj);
-        }
-        {
-            // div v and 1/rho of both particles, stored once per particle
-            // (gradient pad slot, Geo) with the same arithmetic
-            // W -= dt/2 (source + (v - v_frame) . grad W): the particle part,
-            // source + v . grad W, comes with the gradients (Grad::t); the face
-            // subtracts v_frame . grad W (one FMA chain per field and side)
-            const double hdt = dt / 2.;
-            const double *Ti = grad[i].t, *Tj = grad[j].t;
-            const double nvf[3] = {-vf[0], -vf[1], -vf[2]};
-            // the reference uses vz[i] on the j side of the vx and vy terms
-            // (Particles.cpp:1717,1719): (vz_i - vf_z) = (vz_j - (vf_z + vz_j - vz_i))
-            const double nvq[3] = {-vf[0], -vf[1], D == 3 ? -(vf[2] - (vi[2] - vj[2])) : 0.};
-            const int blk[5] = {0, 12, 3, 6, 9};
-#pragma unroll
-            for (int f = 0; f < NV; ++f) {
-                R[f] = fma(-hdt, fma_dotD<D>(nvf, Gi + blk[f], Ti[f]), R[f]);
-                const double *nj = (D == 3 && (f == 2 || f == 3)) ? nvq : nvf;
-                L[f] = fma(-hdt, fma_dotD<D>(nj, Gj + blk[f], Tj[f]), L[f]);
-            }
-        }
-        if (dneg(R[1]) || dneg(L[1])) st_local |= ST_NEG_PRESSURE;
-        // --- Riemann problem in the face frame (i left, j right)
-        face_normal<D>(A, R, L, hatA, unR, unL);
         }   // !QUEUED
         double guess = -1.;
         if (MODE == 2) {
@@ -1790,6 +1814,103 @@ __global__ void MLH_FACE_BOUNDS k_faces(Params p, const Member *__restrict__ mem
         if (iters_local) atomicAdd(newtonSum, iters_local);
         if (fallback_local) atomicAdd(newtonSum + 1, fallback_local);
         if (deferred_local) atomicAdd(newtonSum + 2, deferred_local);
+        if (st_local) flag(status, st_local);
+    }
+}
+
+// Plain gamma = 5/3 face pass with the faces that need more than one Newton
+// step regrouped inside the block (face_split 2).  A warp issues every
+// instruction that any of its lanes needs, so the second Newton step of the
+// few faces that need it would hold the whole warp.  Instead: every face of
+// the block's round sets up its problem and takes the first Newton step
+// from p_TR, and leaves its solver state (sorted sides, iterate) in shared
+// memory; the block's unfinished faces are listed and continued, densely, by
+// its first threads (the iteration riemann_exact5 runs from the iterate as a
+// guess, on the stored sides: the same arithmetic as the two-pass split);
+// then every face samples its solution and projects its flux, with all
+// lanes busy.  The loop runs in block-wide rounds so that every thread
+// reaches the barriers.
+constexpr int FB_T = 128;   // threads per block of k_faces_block
+
+template <int D>
+__global__ void MLH_FACE_BOUNDS k_faces_block(Params p, const Member *__restrict__ members,
+                                              const int *__restrict__ memberOf, const GridInfo *__restrict__ grids,
+                                              const Prim *__restrict__ prim, const Geo *__restrict__ geo,
+                                              const Grad *__restrict__ grad, const uint32_t *__restrict__ nbr,
+                                              const double *__restrict__ psi, const int *__restrict__ faceTotal,
+                                              const FaceRef *__restrict__ faces, const double *__restrict__ dtp,
+                                              double *__restrict__ Fface, unsigned long long *__restrict__ newtonSum,
+                                              unsigned *__restrict__ status) {
+    __shared__ Solve5 sv[FB_T];
+    __shared__ int todo[FB_T];
+    __shared__ int wcount[FB_T / 32];
+    const int nf = *faceTotal < p.faces_cap ? *faceTotal : p.faces_cap;
+    const RiemannConsts rc = make_riemann_consts(p.gamma, p.rtol, p.rmaxit);
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    unsigned long long iters_local = 0;
+    unsigned st_local = 0;
+    for (int t0 = blockIdx.x * FB_T; t0 < nf; t0 += gridDim.x * FB_T) {
+        const int f = t0 + threadIdx.x;
+        double R[5], L[5], A[3] = {0., 0., 0.}, vf[3] = {0., 0., 0.}, hatA[3] = {0., 0., 0.};
+        double unR = 0., unL = 0.;
+        bool valid = f < nf;
+        if (valid)
+            valid = face_states<D>(p, members, memberOf, grids, prim, geo, grad, nbr, psi, faces, dtp, f, st_local, R,
+                                   L, A, vf, hatA, unR, unL);
+        bool unfinished = false;
+        if (valid) {
+            const Solve5 s0 = riemann5_begin(rc, R[0], unR, R[1], L[0], unL, L[1], -1., 0., 1);
+            sv[threadIdx.x] = s0;
+            unfinished = s0.stage == 2;
+        }
+        // --- list the block's unfinished faces
+        const unsigned bal = __ballot_sync(0xffffffffu, unfinished);
+        if (lane == 0) wcount[warp] = __popc(bal);
+        __syncthreads();
+        int before = 0, nu = 0;
+#pragma unroll
+        for (int w = 0; w < FB_T / 32; ++w) {
+            const int c = wcount[w];
+            before += w < warp ? c : 0;
+            nu += c;
+        }
+        if (unfinished) todo[before + __popc(bal & ((1u << lane) - 1u))] = threadIdx.x;
+        __syncthreads();
+        // --- continue them on the first nu threads
+        if ((int)threadIdx.x < nu) {
+            const int slot = todo[threadIdx.x];
+            Solve5 c = sv[slot];
+            riemann5_continue(rc, c);
+            sv[slot] = c;
+        }
+        __syncthreads();
+        // --- sample and project, every face of the round
+        if (valid) {
+            const Solve5 s = sv[threadIdx.x];
+            RiemannResult rs;
+            if (s.stage == 0) {
+                rs.rho = 0.; rs.u = 0.; rs.p = 0.; rs.pstar = 0.; rs.flag = 0; rs.iters = 0;
+            } else {
+                rs = riemann5_finish(rc, s);
+            }
+            if (unfinished) iters_local += 1;   // the first step, counted as the two-pass split counts it
+            if (rs.iters < 0) st_local |= ST_NEWTON;
+            else iters_local += (unsigned long long)rs.iters;
+            double Fo[5];
+            st_local |= project_flux<D>(rs, R, L, unR, unL, hatA, A, vf, rc.inv_gm1, p.mfm, Fo);
+            double2 *dst = reinterpret_cast<double2 *>(Fface + (size_t)f * 6);
+            dst[0] = make_double2(Fo[0], Fo[1]);
+            dst[1] = make_double2(Fo[2], Fo[3]);
+            dst[2] = make_double2(Fo[4], 0.);
+        }
+        __syncthreads();   // the shared state is rewritten in the next round
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+        iters_local += __shfl_xor_sync(0xffffffffu, iters_local, o);
+        st_local |= __shfl_xor_sync(0xffffffffu, st_local, o);
+    }
+    if (lane == 0) {
+        if (iters_local) atomicAdd(newtonSum, iters_local);
         if (st_local) flag(status, st_local);
     }
 }
@@ -2096,6 +2217,10 @@ void launch_step(StepArgs &a) {
         pstar_infer_dev(a.feat, a.queueCount, (int)a.faces_cap, a.mlp_packed, a.yguess, a.sm_count, s);
         if (a.root5) MLH_FACES(true, 2, qa, qb); else MLH_FACES(false, 2, qa, qb);
         if (a.root5 && a.fstate2 && a.tune.face_split) MLH_FACES(true, 4, qb, qb);
+    } else if (a.root5 && a.harvest.stride == 0 && a.tune.face_split == 2) {
+        // unconverged faces after one Newton step continued inside the block
+        k_faces_block<D><<<fB, FB_T, 0, s>>>(pf, a.members, a.memberOf, a.grids, a.prim, a.geo, a.grad, a.nbr, a.psi,
+                                             a.faceOff + p.n, a.faces, a.dt, a.Fface, a.newtonSum, a.status);
     } else if (a.root5 && a.fstate && a.harvest.stride == 0 && a.tune.face_split) {
         // unconverged faces after one Newton step go to a second, dense pass
         cudaMemsetAsync(a.queueCount, 0, sizeof(int), s);

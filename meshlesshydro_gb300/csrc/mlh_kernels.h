@@ -15,7 +15,7 @@ struct Tuning {
     int face_blocks_per_sm = 8;    // grid of the grid-stride face loop
     int grad_threads = 128;        // threads per block of k_gradients
     int nns_warps_per_sm = 64;     // warps (= particles in flight) of k_neighbours
-    int face_split = 1;            // plain gamma = 5/3 step: second Newton pass over a queue
+    int face_split = 1;            // plain gamma = 5/3 step: 1 second Newton pass over a queue, 2 in-block, 0 none
 };
 
 // Device pointers and settings of one step.

@@ -304,36 +304,27 @@ __device__ __forceinline__ double flip_if(double x, bool f) {
 // speed it stands for, and the ties at zero are resolved as the right-side
 // tests resolve them, so the sampled state is the one of the two-sided
 // sampling (Toro section 4.5).
-__device__ inline RiemannResult riemann_exact5(const RiemannConsts &k, double rhoL, double uL, double pL,
-                                               double rhoR, double uR, double pR, double guess = -1.,
-                                               double defer_above = 0., int first_iters = 0) {
-    RiemannResult res;
-    const bool mir = dlt(pR, pL);
-    const RiemannSide A = make_side(k, mir ? rhoR : rhoL, mir ? flip_if(uR, true) : uL, mir ? pR : pL);
-    const RiemannSide B = make_side(k, mir ? rhoL : rhoR, mir ? flip_if(uL, true) : uR, mir ? pL : pR);
-    if (!dlt(B.u - A.u, k.g4 * (A.c + B.c))) {   // g4 (cL + cR) <= uR - uL: vacuum
-        res.rho = 0.; res.u = 0.; res.p = 0.; res.pstar = 0.; res.flag = 0; res.iters = 0;
-        return res;
-    }
-    const double du = B.u - A.u;
-    const double pfloor = 1e-12 * B.p;                   // 1e-12 max(pL, pR)
-    double p0;
-    bool tried_guess = __double_as_longlong(guess) > 0;   // guess > 0 (-1: none)
-    if (tried_guess) p0 = guess;
-    else {
-        double num = A.c + B.c - k.g7 * du;
-        double den = A.c * rroot5<1>(A.p) + B.c * rroot5<1>(B.p);
-        double t = fdiv(num, den);
-        double t2 = t * t;
-        p0 = t2 * t2 * t;
-        // defer_above > 0 and p0 > defer_above, on the keys (see riemann_exact)
-        if (ord_key(defer_above) > 0 && dlt(defer_above, p0)) {
-            res.rho = 0.; res.u = 0.; res.p = 0.; res.pstar = p0; res.flag = 2; res.iters = 0;
-            return res;
-        }
-    }
-    double p, fAs = 0., fBs = 0., qAs = -1., qBs = -1.;
+// State of the gamma = 5/3 solver between its phases: the sorted sides, the
+// Newton iterate and, once converged, f_K(p*) and (p*/p_K)^(1/5).
+struct Solve5 {
+    RiemannSide A, B;
+    double du, pfloor, p, fAs, fBs, qAs, qBs;
+    int iters;   // Newton steps run (a restart from p_TR counts max_iter first); -1: no convergence
+    int stage;   // 0 vacuum; 1 Newton done (finish next); 2 stopped unfinished; 3 strong shock deferred
+    bool mir;
+};
+
+// Newton from p0 (raised to the floor) on the sorted problem; with
+// tried_guess, a start that does not converge is retried from p_TR.
+// first_iters > 0 (not with tried_guess): stop unfinished after that many
+// steps (stage 2, s.p the iterate).
+__device__ __forceinline__ void riemann5_newton(const RiemannConsts &k, Solve5 &s, double p0, bool tried_guess,
+                                                int first_iters) {
+    const RiemannSide &A = s.A, &B = s.B;
+    const double du = s.du, pfloor = s.pfloor;
+    double p = p0;
     int iters = -1, extra = 0;
+    s.fAs = 0.; s.fBs = 0.; s.qAs = -1.; s.qBs = -1.;
     for (int attempt = 0; attempt < 2 && iters < 0; ++attempt) {
         if (attempt == 1) {
             if (!tried_guess) break;
@@ -358,35 +349,105 @@ __device__ inline RiemannResult riemann_exact5(const RiemannConsts &k, double rh
             }
             double dp = pnew - p;
             if (nn_le(2. * fabs(dp), k.tol * (pnew + p))) {
-                fAs = fA + fdA * dp;
-                fBs = fB + fdB * dp;
+                s.fAs = fA + fdA * dp;
+                s.fBs = fB + fdB * dp;
                 double rel = dp * invp;
-                qAs = rA ? qA + qA * (k.g1 * rel) : -1.;
-                qBs = rB ? qB + qB * (k.g1 * rel) : -1.;
+                s.qAs = rA ? qA + qA * (k.g1 * rel) : -1.;
+                s.qBs = rB ? qB + qB * (k.g1 * rel) : -1.;
                 p = pnew;
                 iters = it;
                 break;
             }
             p = pnew;
             if (first_iters > 0 && !tried_guess && it >= first_iters) {
-                res.rho = 0.; res.u = 0.; res.p = 0.; res.pstar = p; res.flag = 2; res.iters = it;
-                return res;
+                s.p = p; s.iters = it; s.stage = 2;
+                return;
             }
         }
     }
+    s.p = p;
+    s.iters = iters < 0 ? -1 : iters + extra;
+    s.stage = 1;
+}
+
+// The sides, the vacuum test, the start (the given guess, or p_TR) and the
+// Newton iteration of riemann_exact5, up to its optional stops.
+__device__ __forceinline__ Solve5 riemann5_begin(const RiemannConsts &k, double rhoL, double uL, double pL,
+                                                 double rhoR, double uR, double pR, double guess,
+                                                 double defer_above, int first_iters) {
+    Solve5 s;
+    s.mir = dlt(pR, pL);
+    const bool mir = s.mir;
+    s.A = make_side(k, mir ? rhoR : rhoL, mir ? flip_if(uR, true) : uL, mir ? pR : pL);
+    s.B = make_side(k, mir ? rhoL : rhoR, mir ? flip_if(uL, true) : uR, mir ? pL : pR);
+    s.fAs = 0.; s.fBs = 0.; s.qAs = -1.; s.qBs = -1.; s.iters = 0; s.p = 0.;
+    if (!dlt(s.B.u - s.A.u, k.g4 * (s.A.c + s.B.c))) {   // g4 (cL + cR) <= uR - uL: vacuum
+        s.stage = 0;
+        return s;
+    }
+    s.du = s.B.u - s.A.u;
+    s.pfloor = 1e-12 * s.B.p;                   // 1e-12 max(pL, pR)
+    double p0;
+    const bool tried_guess = __double_as_longlong(guess) > 0;   // guess > 0 (-1: none)
+    if (tried_guess) p0 = guess;
+    else {
+        double num = s.A.c + s.B.c - k.g7 * s.du;
+        double den = s.A.c * rroot5<1>(s.A.p) + s.B.c * rroot5<1>(s.B.p);
+        double t = fdiv(num, den);
+        double t2 = t * t;
+        p0 = t2 * t2 * t;
+        // defer_above > 0 and p0 > defer_above, on the keys (see riemann_exact)
+        if (ord_key(defer_above) > 0 && dlt(defer_above, p0)) {
+            s.p = p0; s.stage = 3;
+            return s;
+        }
+    }
+    riemann5_newton(k, s, p0, tried_guess, first_iters);
+    return s;
+}
+
+// Continue a solve stopped unfinished (stage 2) from its iterate: the same
+// iteration as restarting riemann_exact5 with the iterate as the guess.
+__device__ __forceinline__ void riemann5_continue(const RiemannConsts &k, Solve5 &s) {
+    riemann5_newton(k, s, s.p, true, 0);
+}
+
+__device__ inline RiemannResult riemann5_finish(const RiemannConsts &k, const Solve5 &s);
+
+__device__ inline RiemannResult riemann_exact5(const RiemannConsts &k, double rhoL, double uL, double pL,
+                                               double rhoR, double uR, double pR, double guess = -1.,
+                                               double defer_above = 0., int first_iters = 0) {
+    const Solve5 s = riemann5_begin(k, rhoL, uL, pL, rhoR, uR, pR, guess, defer_above, first_iters);
+    RiemannResult res;
+    if (s.stage == 0) {
+        res.rho = 0.; res.u = 0.; res.p = 0.; res.pstar = 0.; res.flag = 0; res.iters = 0;
+        return res;
+    }
+    if (s.stage >= 2) {   // unfinished (the iterate) or deferred strong shock (p_TR)
+        res.rho = 0.; res.u = 0.; res.p = 0.; res.pstar = s.p; res.flag = 2; res.iters = s.stage == 2 ? s.iters : 0;
+        return res;
+    }
+    return riemann5_finish(k, s);
+}
+
+// u* and the sampled state of a converged (or given-up) solve.
+__device__ inline RiemannResult riemann5_finish(const RiemannConsts &k, const Solve5 &s) {
+    RiemannResult res;
+    const RiemannSide &A = s.A, &B = s.B;
+    const bool mir = s.mir;
+    double fAs = s.fAs, fBs = s.fBs, qAs = s.qAs, qBs = s.qBs;
+    const double p = s.p;
     const double pstar = p;
     res.pstar = pstar;
-    if (iters < 0) {
+    if (s.iters < 0) {
         double invp = frcp(pstar), fdA, fdB, qA, qB;
         bool rA, rB;
         pressure_fn5(A, pstar, invp, fAs, fdA, qA, rA);
         pressure_fn5(B, pstar, invp, fBs, fdB, qB, rB);
         qAs = rA ? qA : -1.;
         qBs = rB ? qB : -1.;
-        res.iters = -1;
-    } else {
-        res.iters = iters + extra;
     }
+    res.iters = s.iters;
     // u* of the given problem (the sorted one's, negated when mirrored)
     const double ustar = flip_if(.5 * (A.u + B.u) + .5 * (fBs - fAs), mir);
     // --- sampling at S = 0: side s of the contact, as the left side

@@ -133,6 +133,28 @@ def test_deterministic_bitwise():
         assert np.array_equal(sa[k], sb[k]), k
 
 
+@pytest.mark.parametrize("name", ["sedov16_periodic", "kh100"])
+def test_face_pass_structures_bitwise(name):
+    """The three structures of the plain face pass (one pass; a second
+    Newton pass over a queue; the unfinished faces continued inside the
+    block) run the same arithmetic on every face: identical states, bit for
+    bit, over steps where both converged and unfinished faces occur."""
+    p, cfg = CASES[name]
+    states, iters = [], []
+    for split in (0, 1, 2):
+        sim = _sim(cfg, p)
+        sim.set_tuning({"face_threads": 128, "face_blocks_per_sm": 4, "grad_threads": 64,
+                        "nns_warps_per_sm": 32, "face_split": split})
+        st = sim.step(3)
+        states.append(sim.get_state())
+        iters.append(st.newton_iterations)
+        sim.close()
+    for other in states[1:]:
+        for k in states[0]:
+            assert np.array_equal(states[0][k], other[k]), k
+    assert iters[0] == iters[1] == iters[2]
+
+
 def test_neighbour_overflow_retry(oracle_mod):
     """Too few slots: the step detects the overflow, grows the slots and
     repeats (the reference exits, Particles.cpp:348-352)."""
