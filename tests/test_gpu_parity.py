@@ -182,6 +182,18 @@ def test_negative_pressure_reported():
     assert st.status & (1 << 1)
 
 
+def test_nan_reported():
+    """A NaN in the state (an internal energy here) reaches the updated
+    state, and the update reports it in the status word; every loop of the
+    step is bounded, so the step still ends (the reference has no check)."""
+    p, cfg = CASES["kh24"]
+    q = p.copy()
+    q.u[5] = np.nan
+    g = _sim(cfg, q)
+    st = g.step(1, check=False)
+    assert st.status & (1 << 10)
+
+
 @pytest.mark.parametrize("name,nsteps,rtol", [("kh100", 100, 1e-8), ("sedov16_periodic", 30, 1e-8),
                                               ("sedov16_nonperiodic", 40, 1e-8)])
 def test_multistep_density_l1(oracle_mod, name, nsteps, rtol):
