@@ -1829,10 +1829,13 @@ __global__ void MLH_FACE_BOUNDS k_faces(Params p, const Member *__restrict__ mem
 // guess, on the stored sides: the same arithmetic as the two-pass split);
 // then every face samples its solution and projects its flux, with all
 // lanes busy.  The loop runs in block-wide rounds so that every thread
-// reaches the barriers.
+// reaches the barriers.  LEARNED: the first pass of the learned-guess step,
+// which hands strong shocks (p_TR > PSTAR_HARD min(pL, pR)) with their state,
+// p_TR and network inputs to queue A, as k_faces MODE 1 does (solving them
+// here when the queue is full); k_faces MODE 2 solves them afterwards.
 constexpr int FB_T = 128;   // threads per block of k_faces_block
 
-template <int D>
+template <int D, bool LEARNED>
 __global__ void MLH_FACE_BOUNDS k_faces_block(Params p, const Member *__restrict__ members,
                                               const int *__restrict__ memberOf, const GridInfo *__restrict__ grids,
                                               const Prim *__restrict__ prim, const Geo *__restrict__ geo,
@@ -1840,7 +1843,7 @@ __global__ void MLH_FACE_BOUNDS k_faces_block(Params p, const Member *__restrict
                                               const double *__restrict__ psi, const int *__restrict__ faceTotal,
                                               const FaceRef *__restrict__ faces, const double *__restrict__ dtp,
                                               double *__restrict__ Fface, unsigned long long *__restrict__ newtonSum,
-                                              unsigned *__restrict__ status) {
+                                              unsigned *__restrict__ status, FaceQueue qa, float4 *__restrict__ feat) {
     __shared__ Solve5 sv[FB_T];
     __shared__ int todo[FB_T];
     __shared__ int wcount[FB_T / 32];
@@ -1859,9 +1862,29 @@ __global__ void MLH_FACE_BOUNDS k_faces_block(Params p, const Member *__restrict
                                    L, A, vf, hatA, unR, unL);
         bool unfinished = false;
         if (valid) {
-            const Solve5 s0 = riemann5_begin(rc, R[0], unR, R[1], L[0], unL, L[1], -1., 0., 1);
-            sv[threadIdx.x] = s0;
-            unfinished = s0.stage == 2;
+            // strong shocks of the learned step go to the network's queue
+            const double defer = LEARNED ? PSTAR_HARD * (dlt(L[1], R[1]) ? L[1] : R[1]) : 0.;   // min on the keys
+            Solve5 s0 = riemann5_begin(rc, R[0], unR, R[1], L[0], unL, L[1], -1., defer, 1);
+            if (LEARNED && s0.stage == 3) {
+                const int q = atomicAdd(qa.count, 1);
+                if (q < qa.cap) {
+                    FaceState &fs = qa.st[q];
+#pragma unroll
+                    for (int k = 0; k < 5; ++k) { fs.v[k] = R[k]; fs.v[5 + k] = L[k]; }
+#pragma unroll
+                    for (int a = 0; a < 3; ++a) { fs.v[10 + a] = A[a]; fs.v[13 + a] = vf[a]; fs.v[16 + a] = hatA[a]; }
+                    fs.v[19] = s0.p;   // p_TR
+                    qa.face[q] = f;
+                    feat[q] = pstar_features(R, L, unR, unL, p.gamma);
+                    valid = false;   // solved by the pass over the queue
+                } else {
+                    s0 = riemann5_begin(rc, R[0], unR, R[1], L[0], unL, L[1], -1., 0., 1);
+                }
+            }
+            if (valid) {
+                sv[threadIdx.x] = s0;
+                unfinished = s0.stage == 2;
+            }
         }
         // --- list the block's unfinished faces
         const unsigned bal = __ballot_sync(0xffffffffu, unfinished);
@@ -2213,14 +2236,20 @@ void launch_step(StepArgs &a) {
         // strong shocks: network guess (queue A); the rest as the plain step
         cudaMemsetAsync(a.queueCount, 0, sizeof(int), s);
         if (a.queueCount2) cudaMemsetAsync(a.queueCount2, 0, sizeof(int), s);
-        if (a.root5) MLH_FACES(true, 1, qa, qb); else MLH_FACES(false, 1, qa, qb);
+        if (a.root5 && a.tune.face_split == 2)   // unfinished faces continued inside the block
+            k_faces_block<D, true><<<fB, FB_T, 0, s>>>(pf, a.members, a.memberOf, a.grids, a.prim, a.geo, a.grad,
+                                                       a.nbr, a.psi, a.faceOff + p.n, a.faces, a.dt, a.Fface,
+                                                       a.newtonSum, a.status, qa, a.feat);
+        else if (a.root5) MLH_FACES(true, 1, qa, qb);
+        else MLH_FACES(false, 1, qa, qb);
         pstar_infer_dev(a.feat, a.queueCount, (int)a.faces_cap, a.mlp_packed, a.yguess, a.sm_count, s);
         if (a.root5) MLH_FACES(true, 2, qa, qb); else MLH_FACES(false, 2, qa, qb);
-        if (a.root5 && a.fstate2 && a.tune.face_split) MLH_FACES(true, 4, qb, qb);
+        if (a.root5 && a.fstate2 && a.tune.face_split == 1) MLH_FACES(true, 4, qb, qb);
     } else if (a.root5 && a.harvest.stride == 0 && a.tune.face_split == 2) {
         // unconverged faces after one Newton step continued inside the block
-        k_faces_block<D><<<fB, FB_T, 0, s>>>(pf, a.members, a.memberOf, a.grids, a.prim, a.geo, a.grad, a.nbr, a.psi,
-                                             a.faceOff + p.n, a.faces, a.dt, a.Fface, a.newtonSum, a.status);
+        k_faces_block<D, false><<<fB, FB_T, 0, s>>>(pf, a.members, a.memberOf, a.grids, a.prim, a.geo, a.grad, a.nbr,
+                                                    a.psi, a.faceOff + p.n, a.faces, a.dt, a.Fface, a.newtonSum,
+                                                    a.status, qa, a.feat);
     } else if (a.root5 && a.fstate && a.harvest.stride == 0 && a.tune.face_split) {
         // unconverged faces after one Newton step go to a second, dense pass
         cudaMemsetAsync(a.queueCount, 0, sizeof(int), s);

@@ -100,6 +100,29 @@ def test_learned_guess_matches_oracle(trained, oracle_mod, case):
         assert_close(gs[key], v, rtol=LEARNED_RTOL, what=key)
 
 
+@pytest.mark.parametrize("case", [0, 1], ids=["kh40", "sedov12"])
+def test_learned_face_structures_bitwise(trained, case):
+    """With the learned guess, the structures of the first face pass (one
+    pass; unfinished faces in a second pass over a queue; unfinished faces
+    continued inside the block) defer the same strong shocks to the network
+    and run the same arithmetic on every other face: identical states."""
+    w = trained[0]
+    rt = _runtime()
+    cfg, p = _cases()[case]
+    states = []
+    for split in (0, 1, 2):
+        s = rt.Simulation(cfg, p)
+        s.set_tuning({"face_threads": 128, "face_blocks_per_sm": 4, "grad_threads": 64,
+                      "nns_warps_per_sm": 32, "face_split": split})
+        s.set_pstar_weights(w)
+        s.step(3)
+        states.append(s.get_state())
+        s.close()
+    for other in states[1:]:
+        for k in states[0]:
+            assert np.array_equal(states[0][k], other[k]), k
+
+
 def test_bad_guess_falls_back(oracle_mod):
     """A network whose guess is e^20 times p_TR: Newton from there either
     converges or restarts from the two-rarefaction guess; the state stays on
