@@ -249,8 +249,7 @@ void collect_timers(mlh_ctx *c) {
 }
 
 StepArgs make_args(mlh_ctx *c, double dt_max) {
-    StepArgs a;
-    std::memset(&a, 0, sizeof(a));
+    StepArgs a{};   // zeroed pointers and counts, the tuning's defaults
     a.p = c->p;
     a.stream = c->stream;
     a.stream2 = c->stream2;

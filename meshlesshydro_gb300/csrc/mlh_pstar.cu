@@ -158,7 +158,7 @@ __device__ __forceinline__ void input_frags(const float4 x, uint32_t (*a0)[1][4]
 
 // y for the row of this lane, from the C fragments of the last hidden layer
 __device__ __forceinline__ float output_row(const Acc64 &acc3, const float *w4, float b4) {
-    const int lane = threadIdx.x & 31, g = lane >> 2, t = lane & 3;
+    const int lane = threadIdx.x & 31, t = lane & 3;
     float part[2][2] = {{0.f, 0.f}, {0.f, 0.f}};   // [m][row g / g+8]
 #pragma unroll
     for (int m = 0; m < 2; ++m)
@@ -300,7 +300,7 @@ __global__ void __launch_bounds__(TB) k_pstar_train(const float4 *__restrict__ x
     extern __shared__ __align__(16) unsigned char smem_raw[];
     TrainSmem &S = *reinterpret_cast<TrainSmem *>(smem_raw);
     load_packed(&S.w, pk);
-    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, g = lane >> 2, t = lane & 3;
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int row_g = blockIdx.x * TB + warp * 32 + lane;   // sample of this lane
     const bool valid = row_g < nbatch;
     const int src = valid ? (index ? index[row_g] : row_g) : 0;
