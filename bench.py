@@ -46,14 +46,22 @@ METRIC = "particle-updates/s per MFV step on 1 GB300"
 # k_advance_time
 LAUNCHES_PER_STEP = 20
 
-# Per-face cost of the dominant kernel (k_faces, both passes, gamma = 5/3
-# path) from ncu --set full captures: FP64 operations executed per face (2 x
-# DFMA + DADD + DMUL thread instructions / faces) and DRAM bytes (read +
-# write) per face.  3D: the 64^3 periodic Sedov step
-# (profiles/sedov64_step_kernels.md); 2D: 32 members of the Kelvin-Helmholtz
-# ensemble with the second Newton pass (profiles/kh_ensemble32_step_kernels.md;
-# the tuned single pass does about the same arithmetic per face).
-FACE_FP64_FLOPS = {3: 544.0, 2: 417.0}
+# Algorithmic operations per canonical face of the dominant kernel (k_faces:
+# effective face, face states, pairwise limiter, half-step prediction, exact
+# Riemann solve, flux) in the reference's method, counted by the
+# operation-counting build of the oracle (oracle/flops.py; every addition,
+# multiplication, division, square root and pow weighs 1, an FMA 2) over 16
+# steps: 3D on the 32^3 periodic Sedov lattice with the 128^3 workload's h/dx
+# (1.28 Newton iterations per face), 2D on the 100x100 Kelvin-Helmholtz
+# set-up (1.47).  The roofline's `achieved` uses these.
+FACE_ALG_FLOPS = {3: 746.0, 2: 339.8}
+# What k_faces (both passes, gamma = 5/3 path) executes per face, from ncu
+# --set full captures: FP64 operations (2 x DFMA + DADD + DMUL thread
+# instructions / faces) and DRAM bytes (read + write).  3D: the 64^3 periodic
+# Sedov step (profiles/sedov64_step_kernels.md); 2D: 32 members of the
+# Kelvin-Helmholtz ensemble with the second Newton pass
+# (profiles/kh_ensemble32_step_kernels.md).
+FACE_EXEC_FP64_FLOPS = {3: 544.0, 2: 417.0}
 FACE_DRAM_BYTES = {3: 298.0, 2: 362.0}
 
 
@@ -417,10 +425,13 @@ def run_mlh(args):
     dom = max(kt.items(), key=lambda kv: kv[1][1])
     dom_name, (dom_launches, dom_ms) = dom
     dom_avg_s = dom_ms / max(dom_launches, 1) / 1e3
-    flops_per_face = FACE_FP64_FLOPS.get(cfg.dim)
+    flops_per_face = FACE_ALG_FLOPS.get(cfg.dim)
+    exec_per_face = FACE_EXEC_FP64_FLOPS.get(cfg.dim)
     bytes_per_face = FACE_DRAM_BYTES.get(cfg.dim)
     achieved_tf = (flops_per_face * faces_per_step / dom_avg_s / 1e12
                    if (dom_name == "faces_riemann" and flops_per_face) else None)
+    exec_tf = (exec_per_face * faces_per_step / dom_avg_s / 1e12
+               if (dom_name == "faces_riemann" and exec_per_face) else None)
     roofline = {"kernel": "k_faces (faces_riemann)" if dom_name == "faces_riemann" else dom_name,
                 "bound": "fp64", "unit": "TFLOP/s",
                 "achieved": achieved_tf, "peak": fp64_peak,
@@ -428,7 +439,13 @@ def run_mlh(args):
                 "traffic": bytes_per_face * faces_per_step if bytes_per_face else None,
                 "peak_source": "measured: FP64 FMA-chain probe (mlh_probe_fp64_tflops) on this GPU in this run",
                 "units": "canonical faces", "units_per_launch": faces_per_step,
-                "flops_per_unit": flops_per_face, "avg_launch_ms": dom_avg_s * 1e3,
+                "flops_per_unit": flops_per_face,
+                "flops_source": "algorithmic: operations of the reference's method per canonical face, "
+                                "counted by the operation-counting oracle (oracle/flops.py), each 1, an FMA 2",
+                "executed": {"flops_per_unit": exec_per_face, "achieved": exec_tf,
+                             "frac": (exec_tf / fp64_peak) if (exec_tf and fp64_peak) else None,
+                             "source": "FP64 flops k_faces executes per face (ncu, 2 x DFMA + DADD + DMUL)"},
+                "avg_launch_ms": dom_avg_s * 1e3,
                 "hbm_view": {"achieved_gbs": (bytes_per_face * faces_per_step / dom_avg_s / 1e9) if bytes_per_face else None,
                              "peak_gbs": peaks.get("hbm_gbs"), "peak_source": peak_kind}}
     line = {"metric": METRIC, "value": value, "unit": "particle-updates/s", "n_gpus": ws, "steps": st.steps,

@@ -34,6 +34,9 @@
 // implementation that sums the same way gets the same smoothing lengths bit
 // for bit.
 #include "mlh_oracle.h"
+#ifdef ORC_COUNT_FLOPS
+#include "flop_count.hpp"
+#endif
 #include "riemann_exact.hpp"
 
 #include <algorithm>
@@ -47,6 +50,19 @@
 #include <vector>
 
 namespace {
+
+// Arithmetic type of the step: double, or (operation-counting build,
+// -DORC_COUNT_FLOPS) a double that counts the operations done on it.
+#ifdef ORC_COUNT_FLOPS
+using real = orc::Counted;
+#else
+using real = double;
+#endif
+using std::fabs;
+using std::floor;
+using std::fma;
+using std::pow;
+using std::sqrt;
 
 enum Status {
     ST_OK = 0,
@@ -67,40 +83,40 @@ const unsigned IDX_MASK = (1u << IMG_SHIFT) - 1u;
 // unqualified abs(double) at Particles.cpp:1416-1417, 1748-1749, 1754, 1759
 // resolves to int ::abs(int): the double is truncated (x86 cvttsd2si gives
 // INT_MIN for NaN and out-of-range values, and abs(INT_MIN) stays INT_MIN).
-inline double ref_abs(double x, int int_abs) {
-    if (!int_abs) return std::fabs(x);
+inline real ref_abs(real x, int int_abs) {
+    if (!int_abs) return fabs(x);
     int t;
     if (!(x > -2147483649.0 && x < 2147483648.0)) t = INT_MIN;
     else t = (int)x;
-    if (t == INT_MIN) return (double)INT_MIN;
-    return (double)(t < 0 ? -t : t);
+    if (t == INT_MIN) return (real)INT_MIN;
+    return (real)(t < 0 ? -t : t);
 }
 
 template <int D>
 struct Sim {
     orc_config c;
     int N;
-    double h;                          // kernelSize: the support radius, or its maximum with adaptive_h
-    std::vector<double> hp;            // per-particle support radius (h everywhere without adaptive_h)
-    std::vector<double> nEff;          // effective neighbour number of the last h solve
+    double h;                        // kernelSize: the support radius, or its maximum with adaptive_h
+    std::vector<double> hp;          // per-particle support radius (h everywhere without adaptive_h)
+    std::vector<real> nEff;          // effective neighbour number of the last h solve
     long hClamped = 0, hIters = 0;
-    std::vector<double> X[3], V[3], m, u, rho, P, omega;
+    std::vector<real> X[3], V[3], m, u, rho, P, omega;
     // gradients in the reference's call order: rho, vx, vy, (vz), P
-    std::vector<double> G[5];          // [field][i*3+alpha]
-    std::vector<double> Graw[5];       // unlimited copies (for tests)
-    std::vector<double> B;             // inverse of E_i, D*D per particle
+    std::vector<real> G[5];          // [field][i*3+alpha]
+    std::vector<real> Graw[5];       // unlimited copies (for tests)
+    std::vector<real> B;             // inverse of E_i, D*D per particle
     // neighbour lists: real neighbours first (grid stencil order), then
     // periodic images ordered by parent index
     std::vector<int> off, noi, noiImg;
     std::vector<uint32_t> nb;
     std::vector<int> rev;              // slot of i in the neighbour's list
-    std::vector<double> psi, Aij, WL, WR, vFrame, F;
-    std::vector<double> mF, vF, eF;
+    std::vector<real> psi, Aij, WL, WR, vFrame, F;
+    std::vector<real> mF, vF, eF;
     std::vector<int> newtonIters;
     double dt = 0.;
-    double lo[3], hi[3];
+    real lo[3], hi[3];
     int cells[3];
-    double cellSize[3];
+    real cellSize[3];
     std::vector<int> cellOf;
     std::vector<std::vector<int>> grid;
     unsigned status = 0;
@@ -108,18 +124,18 @@ struct Sim {
 
     // --- Kernel::cubicSpline, demonstrator/src/Particles.cpp:7-24, for a
     // support radius hh (the reference's kernelSize)
-    double kernel(double r) const { return kernelH(r, h); }
-    double kernelH(double r, double hh) const {
+    real kernel(real r) const { return kernelH(r, h); }
+    real kernelH(real r, double hh) const {
         double h2 = hh / 2.;
         double sigma = (D == 2) ? 10. / (7. * M_PI * h2 * h2) : 1. / (M_PI * h2 * h2 * h2);
-        double q = r / h2;
+        real q = r / h2;
         if (0. <= q && q <= 1.) return sigma * (1. - 3. / 2. * q * q * (1. - q / 2.));
-        else if (1. < q && q < 2.) return sigma / 4. * std::pow(2. - q, 3.);
+        else if (1. < q && q < 2.) return sigma / 4. * pow(2. - q, 3.);
         return 0.;
     }
 
     // field accessor in gradient order
-    const std::vector<double> &field(int f) const {
+    const std::vector<real> &field(int f) const {
         if (f == 0) return rho;
         if (f == D + 1) return P;
         return V[f - 1];
@@ -128,13 +144,13 @@ struct Sim {
 
     // image coordinate of a particle coordinate along axis a, ghost rule of
     // Particles.cpp:2123-2142 (returns false when the particle has no image)
-    bool image(int a, double xa, double &out) const {
+    bool image(int a, real xa, real &out) const {
         if (xa <= lo[a] + h) { out = hi[a] + (xa - lo[a]); return true; }
         else if (hi[a] - h < xa) { out = lo[a] - (hi[a] - xa); return true; }
         return false;
     }
     // coordinates of neighbour entry e (index + image bits)
-    void coords(uint32_t e, double *xj) const {
+    void coords(uint32_t e, real *xj) const {
         int j = (int)(e & IDX_MASK);
         for (int a = 0; a < D; ++a) {
             xj[a] = X[a][j];
@@ -157,11 +173,11 @@ struct Sim {
     void createGrid() {
         long total = 1;
         for (int a = 0; a < D; ++a) {
-            cells[a] = (int)std::floor((hi[a] - lo[a]) / h);
+            cells[a] = (int)floor((hi[a] - lo[a]) / h);
             if (cells[a] < 1) { status |= ST_GRID; cells[a] = 1; }
             total *= cells[a];
         }
-        for (int a = 0; a < D; ++a) cellSize[a] = (hi[a] - lo[a]) / (double)cells[a];
+        for (int a = 0; a < D; ++a) cellSize[a] = (hi[a] - lo[a]) / (real)cells[a];
         if (c.periodic)
             for (int a = 0; a < D; ++a) if (cells[a] < 3) status |= ST_GRID;
         grid.assign(total, std::vector<int>());
@@ -174,7 +190,7 @@ struct Sim {
         for (int i = 0; i < N; ++i) {
             int fl[3] = {0, 0, 0};
             for (int a = 0; a < D; ++a) {
-                fl[a] = (int)std::floor((X[a][i] - lo[a]) / cellSize[a]);
+                fl[a] = (int)floor((X[a][i] - lo[a]) / cellSize[a]);
                 if (fl[a] == cells[a]) fl[a] -= 1;
                 if (fl[a] < 0 || fl[a] >= cells[a]) { status |= ST_GRID; fl[a] = fl[a] < 0 ? 0 : cells[a] - 1; }
             }
@@ -189,14 +205,14 @@ struct Sim {
     // (Particles::ghostNNS, Particles.cpp:2237-2260) found through wrapped cells.
     // squared search radius of a pair: h^2, or max(h_i^2, h_j^2) with
     // per-particle smoothing lengths (j the parent of an image)
-    double pairSq(int i, int j, double hSqr) const {
+    real pairSq(int i, int j, real hSqr) const {
         if (!c.adaptive_h) return hSqr;
-        double a = hp[i] * hp[i], b = hp[j] * hp[j];
+        real a = hp[i] * hp[i], b = hp[j] * hp[j];
         return a > b ? a : b;
     }
 
     void nns() {
-        const double hSqr = h * h;
+        const real hSqr = h * h;
         off.assign(N + 1, 0);
         noi.assign(N, 0);
         noiImg.assign(N, 0);
@@ -206,7 +222,7 @@ struct Sim {
             int ix = ic % cells[0];
             int iy = (ic / cells[0]) % cells[1];
             int iz = D == 3 ? ic / (cells[0] * cells[1]) : 0;
-            std::vector<uint32_t> real, img;
+            std::vector<uint32_t> own, img;   // real neighbours, periodic images
             for (int k = ix - 1; k <= ix + 1; ++k)
                 for (int l = iy - 1; l <= iy + 1; ++l)
                     for (int mm = (D == 3 ? iz - 1 : 0); mm <= (D == 3 ? iz + 1 : 0); ++mm) {
@@ -225,19 +241,19 @@ struct Sim {
                         for (int j : grid[cell]) {
                             if (!wrap) {
                                 if (j == i) continue;
-                                double dSqr = (X[0][j] - X[0][i]) * (X[0][j] - X[0][i])
+                                real dSqr = (X[0][j] - X[0][i]) * (X[0][j] - X[0][i])
                                             + (X[1][j] - X[1][i]) * (X[1][j] - X[1][i]);
                                 if (D == 3) dSqr += (X[2][j] - X[2][i]) * (X[2][j] - X[2][i]);
-                                if (dSqr < pairSq(i, j, hSqr)) real.push_back((uint32_t)j);
+                                if (dSqr < pairSq(i, j, hSqr)) own.push_back((uint32_t)j);
                             } else {
-                                double xj[3];
+                                real xj[3];
                                 bool ok = true;
                                 for (int a = 0; a < D; ++a) {
                                     xj[a] = X[a][j];
                                     if (wrap & (1u << a)) ok = ok && image(a, X[a][j], xj[a]);
                                 }
                                 if (!ok) continue;
-                                double dSqr = (xj[0] - X[0][i]) * (xj[0] - X[0][i])
+                                real dSqr = (xj[0] - X[0][i]) * (xj[0] - X[0][i])
                                             + (xj[1] - X[1][i]) * (xj[1] - X[1][i]);
                                 if (D == 3) dSqr += (xj[2] - X[2][i]) * (xj[2] - X[2][i]);
                                 if (dSqr < pairSq(i, j, hSqr)) img.push_back((uint32_t)j | (wrap << IMG_SHIFT));
@@ -245,10 +261,10 @@ struct Sim {
                         }
                     }
             std::sort(img.begin(), img.end(), [](uint32_t a, uint32_t b) { return (a & IDX_MASK) < (b & IDX_MASK); });
-            if (real.empty() && img.empty()) status |= ST_NO_NEIGHBOUR;
-            noi[i] = (int)real.size();
+            if (own.empty() && img.empty()) status |= ST_NO_NEIGHBOUR;
+            noi[i] = (int)own.size();
             noiImg[i] = (int)img.size();
-            lists[i] = real;
+            lists[i] = own;
             lists[i].insert(lists[i].end(), img.begin(), img.end());
             off[i + 1] = off[i] + (int)lists[i].size();
         }
@@ -269,12 +285,12 @@ struct Sim {
             }
     }
 
-    double dist(int i, int s) const {
-        double xj[3];
+    real dist(int i, int s) const {
+        real xj[3];
         coords(nb[s], xj);
-        double dSqr = (X[0][i] - xj[0]) * (X[0][i] - xj[0]) + (X[1][i] - xj[1]) * (X[1][i] - xj[1]);
+        real dSqr = (X[0][i] - xj[0]) * (X[0][i] - xj[0]) + (X[1][i] - xj[1]) * (X[1][i] - xj[1]);
         if (D == 3) dSqr += (X[2][i] - xj[2]) * (X[2][i] - xj[2]);
-        return std::sqrt(dSqr);
+        return sqrt(dSqr);
     }
 
     // --- Particles::compDensity/compOmega, Particles.cpp:1151-1184 and the
@@ -282,7 +298,7 @@ struct Sim {
     void density() {
         omega.assign(N, 0.);
         for (int i = 0; i < N; ++i) {
-            double omg = 0.;
+            real omg = 0.;
             for (int s = off[i]; s < off[i] + noi[i]; ++s) omg += kernelH(dist(i, s), hp[i]);
             omega[i] = omg + kernelH(0., hp[i]);
             rho[i] = m[i] * omega[i];
@@ -290,7 +306,7 @@ struct Sim {
         }
         if (c.periodic)
             for (int i = 0; i < N; ++i) {
-                double omg = omega[i];
+                real omg = omega[i];
                 for (int s = off[i] + noi[i]; s < off[i + 1]; ++s) omg += kernelH(dist(i, s), hp[i]);
                 omega[i] = omg;
                 rho[i] = m[i] * omega[i];
@@ -305,49 +321,49 @@ struct Sim {
         }
     }
 
-    static double dot(const double *a, const double *b) {
-        double r = 0.;
+    static real dot(const real *a, const real *b) {
+        real r = 0.;
         for (int k = 0; k < D; ++k) r += a[k] * b[k];
         return r;
     }
 
     // --- Particles::compGlobalTimestep, Particles.cpp:1446-1485 (real
     // neighbours only, v_sig starting at numeric_limits<double>::min())
-    double globalTimestep() {
-        double dt_ = std::numeric_limits<double>::max();
+    real globalTimestep() {
+        real dt_ = std::numeric_limits<double>::max();
         for (int i = 0; i < N; ++i) {
-            double vSig = std::numeric_limits<double>::min();
-            double ci = std::sqrt(c.gamma * P[i] / rho[i]);
+            real vSig = std::numeric_limits<double>::min();
+            real ci = sqrt(c.gamma * P[i] / rho[i]);
             for (int s = off[i]; s < off[i] + noi[i]; ++s) {
                 int j = (int)(nb[s] & IDX_MASK);
-                double cj = std::sqrt(c.gamma * P[j] / rho[j]);
-                double xij[3], vij[3];
+                real cj = sqrt(c.gamma * P[j] / rho[j]);
+                real xij[3], vij[3];
                 for (int a = 0; a < D; ++a) { xij[a] = X[a][i] - X[a][j]; vij[a] = V[a][i] - V[a][j]; }
-                double vijxij = dot(vij, xij) / std::sqrt(dot(xij, xij));
+                real vijxij = dot(vij, xij) / sqrt(dot(xij, xij));
                 vijxij = vijxij < 0. ? vijxij : 0.;
-                double vSig_i = ci + cj - vijxij;
+                real vSig_i = ci + cj - vijxij;
                 vSig = vSig_i > vSig ? vSig_i : vSig;
             }
-            double dti = c.cfl * hp[i] / vSig;
+            real dti = c.cfl * hp[i] / vSig;
             dt_ = dti < dt_ ? dti : dt_;
         }
         return dt_;
     }
 
     // closed-form inverse (replaces Helper::inverseMatrix, Helper.cpp:7-18)
-    static void invert(double *A) {
+    static void invert(real *A) {
         if (D == 2) {
-            double a = A[0], b = A[1], cc = A[2], d = A[3];
-            double det = a * d - b * cc;
-            double id = 1. / det;
+            real a = A[0], b = A[1], cc = A[2], d = A[3];
+            real det = a * d - b * cc;
+            real id = 1. / det;
             A[0] = d * id; A[1] = -b * id; A[2] = -cc * id; A[3] = a * id;
         } else {
-            double a00 = A[0], a01 = A[1], a02 = A[2], a10 = A[3], a11 = A[4], a12 = A[5], a20 = A[6], a21 = A[7], a22 = A[8];
-            double c00 = a11 * a22 - a12 * a21;
-            double c01 = a12 * a20 - a10 * a22;
-            double c02 = a10 * a21 - a11 * a20;
-            double det = a00 * c00 + a01 * c01 + a02 * c02;
-            double id = 1. / det;
+            real a00 = A[0], a01 = A[1], a02 = A[2], a10 = A[3], a11 = A[4], a12 = A[5], a20 = A[6], a21 = A[7], a22 = A[8];
+            real c00 = a11 * a22 - a12 * a21;
+            real c01 = a12 * a20 - a10 * a22;
+            real c02 = a10 * a21 - a11 * a20;
+            real det = a00 * c00 + a01 * c01 + a02 * c02;
+            real id = 1. / det;
             A[0] = c00 * id;
             A[1] = (a02 * a21 - a01 * a22) * id;
             A[2] = (a01 * a12 - a02 * a11) * id;
@@ -365,13 +381,13 @@ struct Sim {
         B.assign((size_t)N * D * D, 0.);
         psi.assign((size_t)off[N] * 3, 0.);
         for (int i = 0; i < N; ++i) {
-            double Bi[9] = {0};
-            double xi[3];
+            real Bi[9] = {0};
+            real xi[3];
             for (int a = 0; a < D; ++a) xi[a] = X[a][i];
             for (int s = off[i]; s < off[i + 1]; ++s) {
-                double r = dist(i, s);
-                double psij_xi = kernelH(r, hp[i]) / omega[i];
-                double xj[3];
+                real r = dist(i, s);
+                real psij_xi = kernelH(r, hp[i]) / omega[i];
+                real xj[3];
                 coords(nb[s], xj);
                 for (int al = 0; al < D; ++al)
                     for (int be = 0; be < D; ++be)
@@ -380,12 +396,12 @@ struct Sim {
             invert(Bi);
             for (int k = 0; k < D * D; ++k) B[(size_t)i * D * D + k] = Bi[k];
             for (int s = off[i]; s < off[i + 1]; ++s) {
-                double r = dist(i, s);
-                double psij_xi = kernelH(r, hp[i]) / omega[i];
-                double xj[3];
+                real r = dist(i, s);
+                real psij_xi = kernelH(r, hp[i]) / omega[i];
+                real xj[3];
                 coords(nb[s], xj);
                 for (int al = 0; al < D; ++al) {
-                    double p = 0.;
+                    real p = 0.;
                     for (int be = 0; be < D; ++be) p += Bi[D * al + be] * (xj[be] - xi[be]) * psij_xi;
                     psi[(size_t)s * 3 + al] = p;
                 }
@@ -396,7 +412,7 @@ struct Sim {
     // --- Particles::gradient, Particles.cpp:1257-1270 / 2457-2502
     void gradients() {
         for (int f = 0; f < nfields(); ++f) {
-            const std::vector<double> &fv = field(f);
+            const std::vector<real> &fv = field(f);
             G[f].assign((size_t)N * 3, 0.);
             for (int i = 0; i < N; ++i)
                 for (int s = off[i]; s < off[i + 1]; ++s) {
@@ -410,16 +426,16 @@ struct Sim {
     // --- Particles::slopeLimiter, Particles.cpp:1313-1444
     void slopeLimiter() {
         for (int f = 0; f < nfields(); ++f) {
-            const std::vector<double> &fv = field(f);
+            const std::vector<real> &fv = field(f);
             for (int i = 0; i < N; ++i) {
-                double psiMaxNgb = std::numeric_limits<double>::min();
-                double psiMinNgb = std::numeric_limits<double>::max();
-                double psiMaxMid = std::numeric_limits<double>::min();
-                double psiMinMid = std::numeric_limits<double>::max();
-                double *g = &G[f][(size_t)i * 3];
+                real psiMaxNgb = std::numeric_limits<double>::min();
+                real psiMinNgb = std::numeric_limits<double>::max();
+                real psiMaxMid = std::numeric_limits<double>::min();
+                real psiMinMid = std::numeric_limits<double>::max();
+                real *g = &G[f][(size_t)i * 3];
                 for (int s = off[i]; s < off[i + 1]; ++s) {
                     int j = (int)(nb[s] & IDX_MASK);
-                    double xj[3], xij[3], xijxi[3];
+                    real xj[3], xij[3], xijxi[3];
                     coords(nb[s], xj);
                     for (int a = 0; a < D; ++a) {
                         if (c.first_order_quad_point) xij[a] = (X[a][i] + xj[a]) / 2.;
@@ -428,12 +444,12 @@ struct Sim {
                     }
                     if (psiMaxNgb < fv[j]) psiMaxNgb = fv[j];
                     if (psiMinNgb > fv[j]) psiMinNgb = fv[j];
-                    double fij = fv[i] + dot(g, xijxi);
+                    real fij = fv[i] + dot(g, xijxi);
                     if (psiMaxMid < fij) psiMaxMid = fij;
                     if (psiMinMid > fij) psiMinMid = fij;
                 }
-                double alphaMax = ref_abs((psiMaxNgb - fv[i]) / (psiMaxMid - fv[i]), c.int_abs);
-                double alphaMin = ref_abs((fv[i] - psiMinNgb) / (fv[i] - psiMinMid), c.int_abs);
+                real alphaMax = ref_abs((psiMaxNgb - fv[i]) / (psiMaxMid - fv[i]), c.int_abs);
+                real alphaMin = ref_abs((fv[i] - psiMinNgb) / (fv[i] - psiMinMid), c.int_abs);
                 if (alphaMin <= alphaMax && c.beta * alphaMin < 1.) {
                     for (int a = 0; a < D; ++a) g[a] *= alphaMin;
                 } else if (alphaMax <= alphaMin && c.beta * alphaMax < 1.) {
@@ -456,24 +472,24 @@ struct Sim {
     }
 
     // --- Particles::pairwiseLimiter, Particles.cpp:1735-1785
-    double pairwiseLimiter(double phi0, double phi_i, double phi_j, double xijxi_abs, double xjxi_abs) const {
-        double phi_ = phi_i;
-        double phi_ij = phi_i + xijxi_abs / xjxi_abs * (phi_j - phi_i);
-        double phiMin, phiMax;
+    real pairwiseLimiter(real phi0, real phi_i, real phi_j, real xijxi_abs, real xjxi_abs) const {
+        real phi_ = phi_i;
+        real phi_ij = phi_i + xijxi_abs / xjxi_abs * (phi_j - phi_i);
+        real phiMin, phiMax;
         if (phi_i < phi_j) { phiMin = phi_i; phiMax = phi_j; }
         else { phiMin = phi_j; phiMax = phi_i; }
-        double delta1 = c.psi1 * ref_abs(phi_i - phi_j, c.int_abs);
-        double delta2 = c.psi2 * ref_abs(phi_i - phi_j, c.int_abs);
-        double phiMinus, phiPlus;
+        real delta1 = c.psi1 * ref_abs(phi_i - phi_j, c.int_abs);
+        real delta2 = c.psi2 * ref_abs(phi_i - phi_j, c.int_abs);
+        real phiMinus, phiPlus;
         if ((phiMax + delta1 >= 0. && phiMax >= 0.) || (phiMax + delta1 < 0. && phiMax < 0.)) phiPlus = phiMax + delta1;
         else phiPlus = phiMax / (1. + delta1 / ref_abs(phiMax, c.int_abs));
         if ((phiMin - delta1 >= 0. && phiMin >= 0.) || (phiMin - delta1 < 0. && phiMin < 0.)) phiMinus = phiMin - delta1;
         else phiMinus = phiMin / (1. + delta1 / ref_abs(phiMin, c.int_abs));
         if (phi_i < phi_j) {
-            double minPhiD2 = (phi_ij + delta2 < phi0) ? phi_ij + delta2 : phi0;
+            real minPhiD2 = (phi_ij + delta2 < phi0) ? phi_ij + delta2 : phi0;
             phi_ = phiMinus > minPhiD2 ? phiMinus : minPhiD2;
         } else if (phi_i > phi_j) {
-            double maxPhiD2 = (phi_ij - delta2 > phi0) ? phi_ij - delta2 : phi0;
+            real maxPhiD2 = (phi_ij - delta2 > phi0) ? phi_ij - delta2 : phi0;
             phi_ = phiPlus < maxPhiD2 ? phiPlus : maxPhiD2;
         }
         return phi_;
@@ -486,13 +502,13 @@ struct Sim {
         WL.assign((size_t)off[N] * NV, 0.);
         WR.assign((size_t)off[N] * NV, 0.);
         vFrame.assign((size_t)off[N] * 3, 0.);
-        const std::vector<double> &rG = G[0], &vxG = G[1], &vyG = G[2], &vzG = G[3], &PG = G[D + 1];
-        const double gamma = c.gamma;
+        const std::vector<real> &rG = G[0], &vxG = G[1], &vyG = G[2], &vzG = G[3], &PG = G[D + 1];
+        const real gamma = c.gamma;
         for (int i = 0; i < N; ++i)
             for (int s = off[i]; s < off[i + 1]; ++s) {
                 int j = (int)(nb[s] & IDX_MASK);
                 bool isImg = (s - off[i]) >= noi[i];
-                double xj[3], xij[3], xijxi[3], xjxi[3], xijxj[3];
+                real xj[3], xij[3], xijxi[3], xjxi[3], xijxj[3];
                 coords(nb[s], xj);
                 for (int a = 0; a < D; ++a) {
                     xjxi[a] = xj[a] - X[a][i];
@@ -506,21 +522,21 @@ struct Sim {
                         xijxj[a] = xij[a] - xj[a];
                     }
                 }
-                double *vf = &vFrame[(size_t)s * 3];
+                real *vf = &vFrame[(size_t)s * 3];
                 if (!c.move_particles) { for (int a = 0; a < D; ++a) vf[a] = 0.; }
                 else if (c.first_order_quad_point) { for (int a = 0; a < D; ++a) vf[a] = (V[a][i] + V[a][j]) / 2.; }
                 else {
-                    double dotProd = dot(xijxi, xjxi);
-                    double dSqr = dot(xjxi, xjxi);
+                    real dotProd = dot(xijxi, xjxi);
+                    real dSqr = dot(xjxi, xjxi);
                     for (int a = 0; a < D; ++a) vf[a] = V[a][i] + (V[a][j] - V[a][i]) * dotProd / dSqr;
                 }
-                double *R = &WR[(size_t)s * NV], *L = &WL[(size_t)s * NV];
+                real *R = &WR[(size_t)s * NV], *L = &WL[(size_t)s * NV];
                 R[0] = rho[i]; L[0] = rho[j];
                 R[1] = P[i]; L[1] = P[j];
                 for (int a = 0; a < D; ++a) { R[2 + a] = V[a][i] - vf[a]; L[2 + a] = V[a][j] - vf[a]; }
-                double Rb[5], Lb[5];
+                real Rb[5], Lb[5];
                 for (int nu = 0; nu < NV; ++nu) { Rb[nu] = R[nu]; Lb[nu] = L[nu]; }
-                const double *gi, *gj;
+                const real *gi, *gj;
                 size_t I = (size_t)i * 3, J = (size_t)j * 3;
                 R[0] += dot(&rG[I], xijxi); L[0] += dot(&rG[J], xijxj);
                 R[1] += dot(&PG[I], xijxi); L[1] += dot(&PG[J], xijxj);
@@ -529,24 +545,24 @@ struct Sim {
                 if (D == 3) { R[4] += dot(&vzG[I], xijxi); L[4] += dot(&vzG[J], xijxj); }
                 (void)gi; (void)gj;
                 if (c.pairwise_limiter && (!isImg || c.image_pairwise_limiter)) {
-                    double xijxi_abs = 0., xijxj_abs = 0., xjxi_abs = 0.;
+                    real xijxi_abs = 0., xijxj_abs = 0., xjxi_abs = 0.;
                     for (int a = 0; a < D; ++a) {
                         xijxi_abs += xijxi[a] * xijxi[a];
                         xijxj_abs += xijxj[a] * xijxj[a];
                         xjxi_abs += xjxi[a] * xjxi[a];
                     }
-                    xijxi_abs = std::sqrt(xijxi_abs);
-                    xijxj_abs = std::sqrt(xijxj_abs);
-                    xjxi_abs = std::sqrt(xjxi_abs);
+                    xijxi_abs = sqrt(xijxi_abs);
+                    xijxj_abs = sqrt(xijxj_abs);
+                    xjxi_abs = sqrt(xjxi_abs);
                     for (int nu = 0; nu < NV; ++nu) {
                         R[nu] = pairwiseLimiter(R[nu], Rb[nu], Lb[nu], xijxi_abs, xjxi_abs);
                         L[nu] = pairwiseLimiter(L[nu], Lb[nu], Rb[nu], xijxj_abs, xjxi_abs);
                     }
                 }
-                double viDiv = vxG[I + 0] + vyG[I + 1];
-                double vjDiv = vxG[J + 0] + vyG[J + 1];
+                real viDiv = vxG[I + 0] + vyG[I + 1];
+                real vjDiv = vxG[J + 0] + vyG[J + 1];
                 if (D == 3) { viDiv += vzG[I + 2]; vjDiv += vzG[J + 2]; }
-                double vxi = V[0][i], vyi = V[1][i], vxj = V[0][j], vyj = V[1][j];
+                real vxi = V[0][i], vyi = V[1][i], vxj = V[0][j], vyj = V[1][j];
                 R[0] -= dt / 2. * (rho[i] * viDiv + (vxi - vf[0]) * rG[I + 0] + (vyi - vf[1]) * rG[I + 1]);
                 L[0] -= dt / 2. * (rho[j] * vjDiv + (vxj - vf[0]) * rG[J + 0] + (vyj - vf[1]) * rG[J + 1]);
                 R[1] -= dt / 2. * (gamma * P[i] * viDiv + (vxi - vf[0]) * PG[I + 0] + (vyi - vf[1]) * PG[I + 1]);
@@ -556,7 +572,7 @@ struct Sim {
                 R[3] -= dt / 2. * (PG[I + 1] / rho[i] + (vxi - vf[0]) * vyG[I + 0] + (vyi - vf[1]) * vyG[I + 1]);
                 L[3] -= dt / 2. * (PG[J + 1] / rho[j] + (vxj - vf[0]) * vyG[J + 0] + (vyj - vf[1]) * vyG[J + 1]);
                 if (D == 3) {
-                    double vzi = V[2][i], vzj = V[2][j];
+                    real vzi = V[2][i], vzj = V[2][j];
                     R[0] -= dt / 2. * (vzi - vf[2]) * rG[I + 2];
                     L[0] -= dt / 2. * (vzj - vf[2]) * rG[J + 2];
                     R[1] -= dt / 2. * (vzi - vf[2]) * PG[I + 2];
@@ -573,19 +589,19 @@ struct Sim {
     }
 
     // --- Helper::rotationMatrix2D/3D, demonstrator/src/Helper.cpp:39-77
-    static void rot2(const double *a, const double *b, double *L) {
+    static void rot2(const real *a, const real *b, real *L) {
         L[0] = a[0] * b[0] + a[1] * b[1];
         L[1] = -(a[0] * b[1] - a[1] * b[0]);
         L[2] = -L[1];
         L[3] = L[0];
     }
-    static void rot3(const double *a, const double *b, double *L) {
-        double v[3];
+    static void rot3(const real *a, const real *b, real *L) {
+        real v[3];
         v[0] = a[1] * b[2] - a[2] * b[1];
         v[1] = a[2] * b[0] - a[0] * b[2];
         v[2] = a[0] * b[1] - a[1] * b[0];
-        double cosAB = dot(a, b);
-        double n = 1. / (1. + cosAB);
+        real cosAB = dot(a, b);
+        real n = 1. / (1. + cosAB);
         L[0] = 1. - n * (v[2] * v[2] + v[1] * v[1]);
         L[1] = -v[2] + n * v[0] * v[1];
         L[2] = v[1] + n * v[0] * v[2];
@@ -601,22 +617,22 @@ struct Sim {
     // demonstrator/src/Riemann.cpp:7-229.  wi = state of the list owner i
     // (the reference's WijR, which the constructor receives as WL), wj = state
     // of neighbour j; i is the LEFT state of the 1D problem.
-    void riemann(double *wi, double *wj, const double *vfr, const double *A, double *Fo, const orc::ExactRiemann &rs) {
-        const double unitX[3] = {1., 0., 0.};
-        double AN = std::sqrt(dot(A, A));
-        double hatA[3];
+    void riemann(real *wi, real *wj, const real *vfr, const real *A, real *Fo, const orc::ExactRiemannT<real> &rs) {
+        const real unitX[3] = {1., 0., 0.};
+        real AN = sqrt(dot(A, A));
+        real hatA[3];
         for (int a = 0; a < D; ++a) hatA[a] = 1. / AN * A[a];
-        double Lam[9];
+        real Lam[9];
         if (D == 2) {
             rot2(hatA, unitX, Lam);
-            double bR[2] = {wj[2], wj[3]}, bL[2] = {wi[2], wi[3]};
+            real bR[2] = {wj[2], wj[3]}, bL[2] = {wi[2], wi[3]};
             wj[2] = Lam[0] * bR[0] + Lam[1] * bR[1];
             wj[3] = Lam[2] * bR[0] + Lam[3] * bR[1];
             wi[2] = Lam[0] * bL[0] + Lam[1] * bL[1];
             wi[3] = Lam[2] * bL[0] + Lam[3] * bL[1];
         } else {
             rot3(hatA, unitX, Lam);
-            double bR[3] = {wj[2], wj[3], wj[4]}, bL[3] = {wi[2], wi[3], wi[4]};
+            real bR[3] = {wj[2], wj[3], wj[4]}, bL[3] = {wi[2], wi[3], wi[4]};
             wj[2] = Lam[0] * bR[0] + Lam[1] * bR[1] + Lam[2] * bR[2];
             wj[3] = Lam[3] * bR[0] + Lam[4] * bR[1] + Lam[5] * bR[2];
             wj[4] = Lam[6] * bR[0] + Lam[7] * bR[1] + Lam[8] * bR[2];
@@ -624,7 +640,7 @@ struct Sim {
             wi[3] = Lam[3] * bL[0] + Lam[4] * bL[1] + Lam[5] * bL[2];
             wi[4] = Lam[6] * bL[0] + Lam[7] * bL[1] + Lam[8] * bL[2];
         }
-        double rhoSol, vSol[3] = {0., 0., 0.}, PSol;
+        real rhoSol, vSol[3] = {0., 0., 0.}, PSol;
         int iters = 0;
         int flag = rs.solve(wi[0], wi[2], wi[1], wj[0], wj[2], wj[1], rhoSol, vSol[0], PSol, &iters);
         ++riemannSolves;
@@ -633,15 +649,15 @@ struct Sim {
         if (flag == 1) { for (int a = 1; a < D; ++a) vSol[a] = wj[2 + a]; }
         else if (flag == -1) { for (int a = 1; a < D; ++a) vSol[a] = wi[2 + a]; }
         else status |= ST_VACUUM;
-        const double gamma = c.gamma;
-        double LI[9];
+        const real gamma = c.gamma;
+        real LI[9];
         if (D == 2) {
             rot2(unitX, hatA, LI);
-            double b[2] = {vSol[0], vSol[1]};
+            real b[2] = {vSol[0], vSol[1]};
             vSol[0] = LI[0] * b[0] + LI[1] * b[1];
             vSol[1] = LI[2] * b[0] + LI[3] * b[1];
             Fo[0] = A[0] * rhoSol * vSol[0] + A[1] * rhoSol * vSol[1];
-            double vLab[2] = {vSol[0] + vfr[0], vSol[1] + vfr[1]};
+            real vLab[2] = {vSol[0] + vfr[0], vSol[1] + vfr[1]};
             if (c.meshless_finite_mass) { vSol[0] = 0.; vSol[1] = 0.; }
             Fo[2] = A[0] * (rhoSol * vLab[0] * vSol[0] + PSol) + A[1] * rhoSol * vLab[0] * vSol[1];
             Fo[3] = A[0] * rhoSol * vLab[1] * vSol[0] + A[1] * (rhoSol * vLab[1] * vSol[1] + PSol);
@@ -649,12 +665,12 @@ struct Sim {
                   + A[1] * (vSol[1] * (PSol / (gamma - 1.) + rhoSol * .5 * dot(vLab, vLab)) + PSol * vLab[1]);
         } else {
             rot3(unitX, hatA, LI);
-            double b[3] = {vSol[0], vSol[1], vSol[2]};
+            real b[3] = {vSol[0], vSol[1], vSol[2]};
             vSol[0] = LI[0] * b[0] + LI[1] * b[1] + LI[2] * b[2];
             vSol[1] = LI[3] * b[0] + LI[4] * b[1] + LI[5] * b[2];
             vSol[2] = LI[6] * b[0] + LI[7] * b[1] + LI[8] * b[2];
             Fo[0] = A[0] * rhoSol * vSol[0] + A[1] * rhoSol * vSol[1] + A[2] * rhoSol * vSol[2];
-            double vLab[3] = {vSol[0] + vfr[0], vSol[1] + vfr[1], vSol[2] + vfr[2]};
+            real vLab[3] = {vSol[0] + vfr[0], vSol[1] + vfr[1], vSol[2] + vfr[2]};
             if (c.meshless_finite_mass) { vSol[0] = 0.; vSol[1] = 0.; vSol[2] = 0.; }
             Fo[2] = A[0] * (rhoSol * vLab[0] * vSol[0] + PSol) + A[1] * rhoSol * vLab[0] * vSol[1] + A[2] * rhoSol * vLab[0] * vSol[2];
             Fo[3] = A[0] * rhoSol * vLab[1] * vSol[0] + A[1] * (rhoSol * vLab[1] * vSol[1] + PSol) + A[2] * rhoSol * vLab[1] * vSol[2];
@@ -672,17 +688,17 @@ struct Sim {
         const int NV = D + 2;
         F.assign((size_t)off[N] * NV, 0.);
         newtonIters.clear();
-        orc::ExactRiemann rs(c.gamma, c.riemann_tol, c.riemann_max_iter);
+        orc::ExactRiemannT<real> rs(c.gamma, c.riemann_tol, c.riemann_max_iter);
         for (int i = 0; i < N; ++i)
             for (int s = off[i]; s < off[i + 1]; ++s) {
                 int j = (int)(nb[s] & IDX_MASK);
-                double *R = &WR[(size_t)s * NV], *L = &WL[(size_t)s * NV];
+                real *R = &WR[(size_t)s * NV], *L = &WL[(size_t)s * NV];
                 if (R[1] < 0. || L[1] < 0.) status |= ST_NEG_PRESSURE;
                 if (j < i) {
                     int t = rev[s];
                     for (int d = 0; d < NV; ++d) F[(size_t)s * NV + d] = -F[(size_t)t * NV + d];
                 } else {
-                    double wi[5], wj[5];
+                    real wi[5], wj[5];
                     for (int d = 0; d < NV; ++d) { wi[d] = R[d]; wj[d] = L[d]; }
                     riemann(wi, wj, &vFrame[(size_t)s * 3], &Aij[(size_t)s * 3], &F[(size_t)s * NV], rs);
                 }
@@ -695,7 +711,7 @@ struct Sim {
         mF.assign(N, 0.); eF.assign(N, 0.); vF.assign((size_t)N * 3, 0.);
         for (int i = 0; i < N; ++i)
             for (int s = off[i]; s < off[i + 1]; ++s) {
-                const double *f = &F[(size_t)s * NV];
+                const real *f = &F[(size_t)s * NV];
                 mF[i] += f[0];
                 vF[(size_t)i * 3 + 0] += f[2];
                 vF[(size_t)i * 3 + 1] += f[3];
@@ -707,8 +723,8 @@ struct Sim {
     // --- Particles::updateStateAndPosition, Particles.cpp:2013-2110
     void update() {
         for (int i = 0; i < N; ++i) {
-            double vxi = V[0][i], vyi = V[1][i], vzi = D == 3 ? V[2][i] : 0.;
-            double Q[4];
+            real vxi = V[0][i], vyi = V[1][i], vzi = D == 3 ? V[2][i] : 0.;
+            real Q[4];
             if (D == 3) Q[0] = m[i] * (u[i] + .5 * (vxi * vxi + vyi * vyi + vzi * vzi));
             else Q[0] = m[i] * (u[i] + .5 * (vxi * vxi + vyi * vyi));
             Q[1] = m[i] * vxi;
@@ -725,7 +741,7 @@ struct Sim {
             else u[i] = Q[0] / m[i] - .5 * (V[0][i] * V[0][i] + V[1][i] * V[1][i]);
             if (u[i] <= 0.) status |= ST_NEG_ENERGY;
             if (c.move_particles) {
-                double vo[3] = {vxi, vyi, vzi};
+                real vo[3] = {vxi, vyi, vzi};
                 for (int a = 0; a < D; ++a) X[a][i] += vo[a] * dt;
                 if (c.periodic)
                     for (int a = 0; a < D; ++a) {
@@ -746,14 +762,14 @@ struct Sim {
     // Newton from the previous h_i (or h); the candidates are the particles
     // of the 3^D cell stencil within h (images by the ghost rule), in stencil
     // order; a particle with N(h) < n_ngb keeps h (counted as clamped).
-    static void shape(double r, double ihh2, double &f, double &g) {
-        double q = r * ihh2;
+    static void shape(real r, real ihh2, real &f, real &g) {
+        real q = r * ihh2;
         if (q <= 1.) {
-            double q2 = q * q;
-            f = std::fma(q2, std::fma(0.75, q, -1.5), 1.);
-            g = q2 * std::fma(-2.25, q, 3.);
+            real q2 = q * q;
+            f = fma(q2, fma(0.75, q, -1.5), 1.);
+            g = q2 * fma(-2.25, q, 3.);
         } else if (q < 2.) {
-            double t = 2. - q, t2 = t * t;
+            real t = 2. - q, t2 = t * t;
             f = 0.25 * t2 * t;
             g = 0.75 * t2 * q;
         } else {
@@ -762,16 +778,16 @@ struct Sim {
         }
     }
 
-    void hsolve(double n_ngb) {
-        const double KD = D == 3 ? 32. / 3. : 40. / 7.;
-        const double St = n_ngb / KD - 1.;
-        const double tolS = 1e-12 * St;
-        const double hSqr = h * h;
+    void hsolve(real n_ngb) {
+        const real KD = D == 3 ? 32. / 3. : 40. / 7.;
+        const real St = n_ngb / KD - 1.;
+        const real tolS = 1e-12 * St;
+        const real hSqr = h * h;
         hp.resize(N, h);
         nEff.assign(N, 0.);
         hClamped = 0;
         hIters = 0;
-        std::vector<double> r;
+        std::vector<real> r;
         for (int i = 0; i < N; ++i) {
             r.clear();
             int ic = cellOf[i];
@@ -794,53 +810,53 @@ struct Sim {
                         int cell = cc[0] + cc[1] * cells[0] + (D == 3 ? cc[2] * cells[0] * cells[1] : 0);
                         for (int j : grid[cell]) {
                             if (!wrap && j == i) continue;
-                            double xj[3];
+                            real xj[3];
                             bool ok = true;
                             for (int a = 0; a < D; ++a) {
                                 xj[a] = X[a][j];
                                 if (wrap & (1u << a)) ok = ok && image(a, X[a][j], xj[a]);
                             }
                             if (!ok) continue;
-                            double dSqr = (xj[0] - X[0][i]) * (xj[0] - X[0][i]) + (xj[1] - X[1][i]) * (xj[1] - X[1][i]);
+                            real dSqr = (xj[0] - X[0][i]) * (xj[0] - X[0][i]) + (xj[1] - X[1][i]) * (xj[1] - X[1][i]);
                             if (D == 3) dSqr += (xj[2] - X[2][i]) * (xj[2] - X[2][i]);
-                            if (dSqr < hSqr) r.push_back(std::sqrt(dSqr));
+                            if (dSqr < hSqr) r.push_back(sqrt(dSqr));
                         }
                     }
-            double x = hp[i];
+            real x = hp[i];
             if (!(x > 0. && x <= h)) x = h;
-            double lo_ = 0., hi_ = h, S = 0.;
+            real lo_ = 0., hi_ = h, S = 0.;
             bool upper = false;
             for (int it = 0;; ++it) {
                 // 32 strided partial sums, then pairwise at distance 16 .. 1
-                double sf[32], sg[32];
+                real sf[32], sg[32];
                 for (int l = 0; l < 32; ++l) { sf[l] = 0.; sg[l] = 0.; }
-                const double ihh2 = 1. / (0.5 * x);
+                const real ihh2 = 1. / (0.5 * x);
                 for (size_t t = 0; t < r.size(); ++t) {
-                    double f, g;
+                    real f, g;
                     shape(r[t], ihh2, f, g);
                     sf[t % 32] += f;
                     sg[t % 32] += g;
                 }
                 for (int o = 16; o > 0; o >>= 1) {
-                    double tf[32], tg[32];
+                    real tf[32], tg[32];
                     for (int l = 0; l < 32; ++l) { tf[l] = sf[l] + sf[l ^ o]; tg[l] = sg[l] + sg[l ^ o]; }
                     for (int l = 0; l < 32; ++l) { sf[l] = tf[l]; sg[l] = tg[l]; }
                 }
                 S = sf[0];
-                const double G = sg[0];
+                const real G = sg[0];
                 ++hIters;
-                const double F = S - St;
-                if (std::fabs(F) <= tolS) break;
+                const real F = S - St;
+                if (fabs(F) <= tolS) break;
                 if (F < 0. && x >= h) { ++hClamped; break; }
                 if (it + 1 >= 50) break;
                 if (F > 0.) { hi_ = x; upper = true; }
                 else lo_ = x;
-                double xn = G > 0. ? x - F * x / G : 0.5 * (lo_ + hi_);
+                real xn = G > 0. ? x - F * x / G : 0.5 * (lo_ + hi_);
                 if (!(xn > lo_ && xn < hi_)) xn = (!upper && xn >= hi_) ? h : 0.5 * (lo_ + hi_);
                 if (xn == x) break;
                 x = xn;
             }
-            hp[i] = x;
+            hp[i] = (double)x;
             nEff[i] = KD * (S + 1.);
         }
     }
@@ -856,24 +872,43 @@ struct Sim {
         assign();
     }
 
+    // operation counts per stage, summed over the steps (counting build)
+#ifdef ORC_COUNT_FLOPS
+    orc::FlopCounts stageFlops[ORC_NSTAGES] = {};
+#endif
+    template <typename F>
+    void stage(int k, F run) {
+#ifdef ORC_COUNT_FLOPS
+        const orc::FlopCounts b = orc::flop_counts();
+        run();
+        const orc::FlopCounts &a = orc::flop_counts();
+        orc::FlopCounts &t = stageFlops[k];
+        t.add += a.add - b.add; t.mul += a.mul - b.mul; t.div += a.div - b.div;
+        t.sqrt += a.sqrt - b.sqrt; t.pow += a.pow - b.pow; t.fma += a.fma - b.fma;
+#else
+        (void)k;
+        run();
+#endif
+    }
+
     // MeshlessScheme::run loop body, MeshlessScheme.cpp:39-253 (no dumps)
     int step() {
         status = 0;
         riemannSolves = 0; newtonTotal = 0;
-        binning();
-        if (c.adaptive_h) hsolve(c.n_ngb);
-        nns();
-        density();
-        pressure();
-        dt = c.adaptive_timestep ? globalTimestep() : c.time_step;
-        psijTilde();
-        gradients();
-        if (c.slope_limiting) slopeLimiter();
-        effectiveFace();
-        riemannStatesLR();
-        solveRiemannProblems();
-        collectFluxes();
-        update();
+        stage(ORC_STAGE_BINNING, [&] { binning(); });
+        if (c.adaptive_h) stage(ORC_STAGE_HSOLVE, [&] { hsolve(c.n_ngb); });
+        stage(ORC_STAGE_NNS, [&] { nns(); });
+        stage(ORC_STAGE_DENSITY, [&] { density(); });
+        stage(ORC_STAGE_PRESSURE, [&] { pressure(); });
+        stage(ORC_STAGE_TIMESTEP, [&] { dt = c.adaptive_timestep ? (double)globalTimestep() : c.time_step; });
+        stage(ORC_STAGE_PSI, [&] { psijTilde(); });
+        stage(ORC_STAGE_GRADIENTS, [&] { gradients(); });
+        if (c.slope_limiting) stage(ORC_STAGE_LIMITER, [&] { slopeLimiter(); });
+        stage(ORC_STAGE_FACE, [&] { effectiveFace(); });
+        stage(ORC_STAGE_STATES, [&] { riemannStatesLR(); });
+        stage(ORC_STAGE_RIEMANN, [&] { solveRiemannProblems(); });
+        stage(ORC_STAGE_COLLECT, [&] { collectFluxes(); });
+        stage(ORC_STAGE_UPDATE, [&] { update(); });
         return (int)status;
     }
 };
@@ -930,7 +965,7 @@ template <int D>
 int getArr(Sim<D> *s, const std::string &nm, void *out) {
     double *o = (double *)out;
     int *oi = (int *)out;
-    auto cp = [&](const std::vector<double> &v) { std::copy(v.begin(), v.end(), o); return 0; };
+    auto cp = [&](const auto &v) { for (size_t k = 0; k < v.size(); ++k) o[k] = (double)v[k]; return 0; };
     auto cpi = [&](const std::vector<int> &v) { std::copy(v.begin(), v.end(), oi); return 0; };
     if (nm == "x") return cp(s->X[0]);
     if (nm == "y") return cp(s->X[1]);
@@ -964,7 +999,11 @@ int getArr(Sim<D> *s, const std::string &nm, void *out) {
     if (nm == "dt") { o[0] = s->dt; return 0; }
     if (nm == "stats") { o[0] = (double)s->riemannSolves; o[1] = (double)s->newtonTotal; return 0; }
     if (nm == "grid") {
-        for (int a = 0; a < 3; ++a) { o[a] = a < D ? s->lo[a] : 0.; o[3 + a] = a < D ? s->hi[a] : 0.; o[6 + a] = a < D ? s->cells[a] : 0; }
+        for (int a = 0; a < 3; ++a) {
+            o[a] = a < D ? (double)s->lo[a] : 0.;
+            o[3 + a] = a < D ? (double)s->hi[a] : 0.;
+            o[6 + a] = a < D ? s->cells[a] : 0;
+        }
         return 0;
     }
     // gradients: "grad_<f>" limited, "gradraw_<f>" unlimited; f in
@@ -985,7 +1024,7 @@ long smoothing(Sim<D> *s, double n_ngb, double *h_out, double *neff_out) {
     s->binning();
     s->hsolve(n_ngb);
     if (h_out) std::copy(s->hp.begin(), s->hp.end(), h_out);
-    if (neff_out) std::copy(s->nEff.begin(), s->nEff.end(), neff_out);
+    if (neff_out) for (int k = 0; k < s->N; ++k) neff_out[k] = (double)s->nEff[k];
     return s->hClamped;
 }
 
@@ -1004,13 +1043,15 @@ int riemannFaces(int n, const double *Wi, const double *Wj, const double *vFrame
     Sim<D> s;
     s.c = cfg;
     s.N = 0;
-    orc::ExactRiemann rs(gamma, cfg.riemann_tol, cfg.riemann_max_iter);
+    orc::ExactRiemannT<real> rs(gamma, cfg.riemann_tol, cfg.riemann_max_iter);
     const int NV = D + 2;
     for (int f = 0; f < n; ++f) {
-        double wi[5], wj[5];
+        real wi[5], wj[5], vf[3], A[3], Fo[5];
         for (int k = 0; k < NV; ++k) { wi[k] = Wi[(size_t)f * NV + k]; wj[k] = Wj[(size_t)f * NV + k]; }
+        for (int k = 0; k < D; ++k) { vf[k] = vFrame[(size_t)f * D + k]; A[k] = Aij[(size_t)f * D + k]; }
         if (wi[1] < 0. || wj[1] < 0.) s.status |= ST_NEG_PRESSURE;
-        s.riemann(wi, wj, vFrame + (size_t)f * D, Aij + (size_t)f * D, F + (size_t)f * NV, rs);
+        s.riemann(wi, wj, vf, A, Fo, rs);
+        for (int k = 0; k < NV; ++k) F[(size_t)f * NV + k] = (double)Fo[k];
         if (iters) iters[f] = s.newtonIters.back();
     }
     return (int)s.status;
@@ -1075,6 +1116,21 @@ int orc_riemann_fluxes(int dim, int n, const double *Wi, const double *Wj, const
                        double gamma, int mfm, double *F, int *iters) {
     if (dim == 2) return riemannFaces<2>(n, Wi, Wj, vFrame, Aij, gamma, mfm, F, iters);
     return riemannFaces<3>(n, Wi, Wj, vFrame, Aij, gamma, mfm, F, iters);
+}
+
+int orc_flop_counts(void *ctx, unsigned long long *out) {
+#ifdef ORC_COUNT_FLOPS
+    Handle *hnd = (Handle *)ctx;
+    const orc::FlopCounts *t = hnd->dim == 2 ? ((Sim<2> *)hnd->sim)->stageFlops : ((Sim<3> *)hnd->sim)->stageFlops;
+    for (int k = 0; k < ORC_NSTAGES; ++k) {
+        const unsigned long long v[6] = {t[k].add, t[k].mul, t[k].div, t[k].sqrt, t[k].pow, t[k].fma};
+        for (int q = 0; q < 6; ++q) out[6 * k + q] = v[q];
+    }
+    return ORC_NSTAGES;
+#else
+    (void)ctx; (void)out;
+    return -1;
+#endif
 }
 
 void orc_destroy(void *ctx) {

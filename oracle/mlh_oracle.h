@@ -66,6 +66,31 @@ int orc_riemann_batch(int n, const double *rhoL, const double *uL, const double 
                       const double *uR, const double *pR, double gamma, const double *guess, double *pstar,
                       int *iters);
 
+/* Stages of one step, in the reference's order (MeshlessScheme.cpp:39-253). */
+enum {
+    ORC_STAGE_BINNING = 0,   /* domain limits, grid, cell assignment */
+    ORC_STAGE_HSOLVE,        /* per-particle smoothing lengths (adaptive_h) */
+    ORC_STAGE_NNS,           /* gridNNS + ghostNNS */
+    ORC_STAGE_DENSITY,       /* compDensity (omega, rho) */
+    ORC_STAGE_PRESSURE,      /* compPressure */
+    ORC_STAGE_TIMESTEP,      /* compGlobalTimestep */
+    ORC_STAGE_PSI,           /* compPsijTilde */
+    ORC_STAGE_GRADIENTS,     /* gradient x (dim + 2) */
+    ORC_STAGE_LIMITER,       /* slopeLimiter */
+    ORC_STAGE_FACE,          /* compEffectiveFace */
+    ORC_STAGE_STATES,        /* compRiemannStatesLR + pairwiseLimiter */
+    ORC_STAGE_RIEMANN,       /* solveRiemannProblems (Riemann::exact) */
+    ORC_STAGE_COLLECT,       /* collectFluxes */
+    ORC_STAGE_UPDATE,        /* updateStateAndPosition */
+    ORC_NSTAGES
+};
+
+/* Operation-counting build only (liborc_count.so, -DORC_COUNT_FLOPS):
+ * operation counts of each stage summed over the steps of this context,
+ * out[6 * stage + k] for k = add, mul, div, sqrt, pow, fma.  Returns
+ * ORC_NSTAGES, or -1 in the plain build. */
+int orc_flop_counts(void *ctx, unsigned long long *out);
+
 #ifdef __cplusplus
 }
 #endif

@@ -16,6 +16,8 @@ import numpy as np
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 LIB = os.path.join(HERE, "libmlh_oracle.so")
+# the same oracle computing in an operation-counting double (flop_count.hpp)
+COUNT_LIB = os.path.join(HERE, "liborc_count.so")
 REF_DIR = os.path.join(HERE, "_ref")
 
 _INT_FIELDS = ["dim", "periodic", "adaptive_timestep", "slope_limiting", "pairwise_limiter",
@@ -34,19 +36,20 @@ class OrcConfig(ctypes.Structure):
 INT_ARRAYS = {"noi", "noi_img", "off", "rev", "newton_iters", "nnl"}
 
 
-def build():
-    subprocess.run(["make", "-s", "-C", HERE], check=True)
+def build(counting: bool = False):
+    subprocess.run(["make", "-s", "-C", HERE] + (["count"] if counting else []), check=True)
 
 
-_lib = None
+_libs = {}
 
 
-def lib():
-    global _lib
-    if _lib is None:
-        if not os.path.exists(LIB):
-            build()
-        L = ctypes.CDLL(LIB)
+def lib(counting: bool = False):
+    """The oracle library (ctypes), or its operation-counting build."""
+    if counting not in _libs:
+        path = COUNT_LIB if counting else LIB
+        if not os.path.exists(path):
+            build(counting)
+        L = ctypes.CDLL(path)
         dp = ctypes.POINTER(ctypes.c_double)
         L.orc_create.restype = ctypes.c_void_p
         L.orc_create.argtypes = [ctypes.POINTER(OrcConfig), ctypes.c_int] + [dp] * 8
@@ -65,8 +68,10 @@ def lib():
         L.orc_riemann_fluxes.restype = ctypes.c_int
         L.orc_smoothing_lengths.restype = ctypes.c_long
         L.orc_smoothing_lengths.argtypes = [ctypes.c_void_p, ctypes.c_double, dp, dp]
-        _lib = L
-    return _lib
+        L.orc_flop_counts.restype = ctypes.c_int
+        L.orc_flop_counts.argtypes = [ctypes.c_void_p, ctypes.POINTER(ctypes.c_ulonglong)]
+        _libs[counting] = L
+    return _libs[counting]
 
 
 def riemann_batch(rhoL, uL, pL, rhoR, uR, pR, gamma=5.0 / 3.0, guess=None):
@@ -112,11 +117,18 @@ def _cfg_struct(cfg) -> OrcConfig:
     return s
 
 
-class Oracle:
-    """One simulation held by the CPU restatement."""
+# stages of one step (ORC_STAGE_* in mlh_oracle.h) and the operation kinds
+STAGES = ["binning", "hsolve", "nns", "density", "pressure", "timestep", "psi", "gradients", "limiter",
+          "face", "states", "riemann", "collect", "update"]
+OPS = ["add", "mul", "div", "sqrt", "pow", "fma"]
 
-    def __init__(self, cfg, pset):
-        self.L = lib()
+
+class Oracle:
+    """One simulation held by the CPU restatement (counting=True: the
+    operation-counting build, same results bit for bit)."""
+
+    def __init__(self, cfg, pset, counting: bool = False):
+        self.L = lib(counting)
         self._arrays = [np.ascontiguousarray(a, dtype=np.float64) for a in pset.arrays()]
         ptrs = [a.ctypes.data_as(ctypes.POINTER(ctypes.c_double)) for a in self._arrays]
         self._cfg = _cfg_struct(cfg)
@@ -147,6 +159,14 @@ class Oracle:
         dp = lambda a: a.ctypes.data_as(ctypes.POINTER(ctypes.c_double))
         clamped = self.L.orc_smoothing_lengths(self.h, float(n_ngb), dp(h), dp(ne))
         return h, ne, int(clamped)
+
+    def flop_counts(self) -> dict:
+        """Operation counts per stage summed over the steps so far
+        ({stage: {op: count}}); counting build only."""
+        out = (ctypes.c_ulonglong * (6 * len(STAGES)))()
+        if self.L.orc_flop_counts(self.h, out) != len(STAGES):
+            raise RuntimeError("not the operation-counting build of the oracle")
+        return {st: {op: int(out[6 * k + q]) for q, op in enumerate(OPS)} for k, st in enumerate(STAGES)}
 
     def state(self) -> dict:
         names = ["x", "y", "vx", "vy", "m", "u"] + (["z", "vz"] if self.dim == 3 else [])

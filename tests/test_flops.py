@@ -1,0 +1,73 @@
+"""The operation-counting build of the oracle (oracle/flop_count.hpp,
+oracle/flops.py): it computes the same step bit for bit, its counts agree
+with hand counts of simple stages, and bench.py's algorithmic flops per face
+are what it counts on the stated samples."""
+import numpy as np
+import pytest
+
+from meshlesshydro_gb300 import ic
+from meshlesshydro_gb300.config import MFVConfig
+
+
+def _pair(oracle_mod, cfg, p, steps):
+    plain = oracle_mod.Oracle(cfg, p)
+    counted = oracle_mod.Oracle(cfg, p, counting=True)
+    for _ in range(steps):
+        assert plain.step() == counted.step()
+    return plain, counted
+
+
+@pytest.mark.parametrize("case", ["sedov12_periodic", "sedov10_nonperiodic", "kh24"])
+def test_counting_build_is_bit_identical(oracle_mod, case):
+    """Computing in the counting double changes no result: every array of the
+    step (neighbour lists, gradients, face states, fluxes, the new state)."""
+    if case == "sedov12_periodic":
+        p = ic.sedov(n_side=12, seed=4, energy=0.05)
+        cfg = MFVConfig.sedov(p, periodic=True)
+    elif case == "sedov10_nonperiodic":
+        p = ic.sedov(n_side=10, seed=6)
+        cfg = MFVConfig.sedov(p, periodic=False)
+    else:
+        p = ic.kelvin_helmholtz(n_side=24, seed=3)
+        cfg = MFVConfig.kelvin_helmholtz(p)
+    a, b = _pair(oracle_mod, cfg, p, 3)
+    names = ["x", "y", "vx", "vy", "m", "u", "rho", "P", "omega", "nnl", "off", "noi", "noi_img", "B", "psi",
+             "Aij", "WL", "WR", "vFrame", "F", "mF", "eF", "vF", "dt", "newton_iters", "stats",
+             "grad_rho", "grad_P", "gradraw_vx"]
+    if cfg.dim == 3:
+        names += ["z", "vz"]
+    for k in names:
+        np.testing.assert_array_equal(a.get(k), b.get(k), err_msg=k)
+    with pytest.raises(RuntimeError):
+        a.flop_counts()   # the plain build has no counts
+
+
+def test_counts_of_simple_stages(oracle_mod):
+    """Hand counts: compPressure is (gamma - 1) rho u, two multiplications per
+    particle (gamma - 1 is a constant); the 3D update is 38 operations per
+    particle while no particle crosses the periodic boundary (kinetic energy
+    8, momenta 3, mass 2, momentum kick 6, velocities 3, energy kick 2,
+    internal energy 8, drift 6)."""
+    import flops
+    p = ic.sedov(n_side=12, seed=4, energy=0.05)
+    cfg = MFVConfig.sedov(p, periodic=True)
+    res = flops.count(cfg, p, 2)
+    assert res["stages_per_particle"]["pressure"] == 2.0
+    assert res["stages_per_particle"]["update"] == 38.0
+    ops = res["ops_per_unit"]["faces_riemann"]
+    assert ops["pow"] > 0 and ops["sqrt"] > 0 and ops["div"] > 0
+
+
+@pytest.mark.parametrize("dim", [3, 2])
+def test_bench_face_flops_are_the_counted_ones(oracle_mod, dim):
+    """bench.py's FACE_ALG_FLOPS: 16 steps of the 32^3 periodic Sedov lattice
+    (3D) and of the 100x100 Kelvin-Helmholtz set-up (2D)."""
+    import bench
+    import flops
+    if dim == 3:
+        cfg, p = flops.workload("sedov", 32, 2)
+    else:
+        cfg, p = flops.workload("kh", 100, 1)
+    res = flops.count(cfg, p, 16)
+    got = res["per_unit"]["faces_riemann"]
+    assert abs(bench.FACE_ALG_FLOPS[dim] - got) <= 0.0005 * got, (bench.FACE_ALG_FLOPS[dim], got)
