@@ -1351,49 +1351,82 @@ __global__ void __launch_bounds__(256) k_link(Params p, const uint32_t *__restri
                                               int *__restrict__ faceOf, FaceRef *__restrict__ faces,
                                               unsigned *__restrict__ status) {
     // faces[] was set to -1: the owner writes (i, slot), the slot on the other
-    // side writes rslot, so each field has exactly one writer
+    // side writes rslot, so each field has exactly one writer.  A slot with
+    // j > i owns face faceOff[i] + (its rank among i's canonical slots); a
+    // slot with j < i searches j's list (real part or image part) for i,
+    // counting on the way j's canonical slots before it (the face's rank in
+    // j's list).  The own list is read four slots per load (K is a multiple
+    // of 4) and the searches of those four slots advance together, one
+    // 4-entry load of each list per round, so that a thread has up to four
+    // loads in flight instead of one chain of dependent loads.
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < p.n; i += gridDim.x * blockDim.x) {
         const size_t base = (size_t)i * p.K;
         const int nr = noi[i], tot = nr + noiImg[i];
+        const uint4 *own = reinterpret_cast<const uint4 *>(nbr + base);
         int rank = 0;
-        for (int s = 0; s < tot; ++s) {
-            const uint32_t e = nbr[base + s];
-            const int j = (int)(e & IDX_MASK);
-            if (j > i) {
-                const int fid = faceOff[i] + rank;
-                ++rank;
-                if (fid >= p.faces_cap) { flag(status, ST_CAPACITY); faceOf[base + s] = 0; continue; }
-                faceOf[base + s] = fid + 1;
-                faces[fid].i = i;
-                faces[fid].slot = s;
-                continue;
+        for (int s0 = 0; s0 < tot; s0 += 4) {
+            const uint4 q = own[s0 >> 2];
+            const uint32_t ev[4] = {q.x, q.y, q.z, q.w};
+            int jj[4], lo[4], hi[4], found[4], crank[4];
+            bool act[4];
+#pragma unroll
+            for (int k = 0; k < 4; ++k) {
+                const int s = s0 + k;
+                const int j = (int)(ev[k] & IDX_MASK);
+                jj[k] = j; lo[k] = 0; hi[k] = 0; found[k] = -1; crank[k] = 0; act[k] = false;
+                if (s >= tot) continue;
+                if (j > i) {
+                    const int fid = faceOff[i] + rank;
+                    ++rank;
+                    if (fid >= p.faces_cap) { flag(status, ST_CAPACITY); faceOf[base + s] = 0; continue; }
+                    faceOf[base + s] = fid + 1;
+                    faces[fid].i = i;
+                    faces[fid].slot = s;
+                    continue;
+                }
+                const int jnr = noi[j];
+                const bool img = s >= nr;
+                lo[k] = img ? jnr : 0;
+                hi[k] = img ? jnr + noiImg[j] : jnr;
+                act[k] = true;
             }
-            // search j's list (real part or image part) for i, counting on
-            // the way j's canonical slots before it (the face's rank); the
-            // list is read 4 entries at a time (K is a multiple of 4)
-            const bool img = s >= nr;
-            const uint4 *lst = reinterpret_cast<const uint4 *>(nbr + (size_t)j * p.K);
-            const int jnr = noi[j];
-            const int b = img ? jnr : 0, en = img ? jnr + noiImg[j] : jnr;
-            int found = -1, crank = 0;
-            for (int t4 = 0; t4 * 4 < en && found < 0; ++t4) {
-                const uint4 q = lst[t4];
-                const uint32_t v[4] = {q.x, q.y, q.z, q.w};
+            for (int t4 = 0;; ++t4) {
+                uint4 r[4];
+                bool any = false;
 #pragma unroll
                 for (int k = 0; k < 4; ++k) {
-                    const int t = t4 * 4 + k;
-                    const int idx = (int)(v[k] & IDX_MASK);
-                    if (found < 0 && t < en) {
-                        if (t >= b && idx == i) found = t;
-                        else crank += idx > j;
+                    if (t4 * 4 >= hi[k]) act[k] = false;   // searched to the end (not found)
+                    r[k] = act[k] ? reinterpret_cast<const uint4 *>(nbr + (size_t)jj[k] * p.K)[t4]
+                                  : make_uint4(0u, 0u, 0u, 0u);
+                    any |= act[k];
+                }
+                if (!any) break;
+#pragma unroll
+                for (int k = 0; k < 4; ++k) {
+                    if (!act[k]) continue;
+                    const uint32_t v[4] = {r[k].x, r[k].y, r[k].z, r[k].w};
+#pragma unroll
+                    for (int m = 0; m < 4; ++m) {
+                        const int t = t4 * 4 + m;
+                        const int idx = (int)(v[m] & IDX_MASK);
+                        if (found[k] < 0 && t < hi[k]) {
+                            if (t >= lo[k] && idx == i) found[k] = t;
+                            else crank[k] += idx > jj[k];
+                        }
                     }
+                    if (found[k] >= 0) act[k] = false;
                 }
             }
-            if (found < 0) { flag(status, ST_ASYMMETRIC); faceOf[base + s] = 0; continue; }
-            const int fid = faceOff[j] + crank;
-            if (fid >= p.faces_cap) { flag(status, ST_CAPACITY); faceOf[base + s] = 0; continue; }
-            faceOf[base + s] = -(fid + 1);
-            faces[fid].rslot = s;
+#pragma unroll
+            for (int k = 0; k < 4; ++k) {
+                const int s = s0 + k;
+                if (s >= tot || jj[k] > i) continue;
+                if (found[k] < 0) { flag(status, ST_ASYMMETRIC); faceOf[base + s] = 0; continue; }
+                const int fid = faceOff[jj[k]] + crank[k];
+                if (fid >= p.faces_cap) { flag(status, ST_CAPACITY); faceOf[base + s] = 0; continue; }
+                faceOf[base + s] = -(fid + 1);
+                faces[fid].rslot = s;
+            }
         }
     }
 }
