@@ -1676,50 +1676,68 @@ __device__ __forceinline__ bool face_states(const Params &p, const Member *__res
     R[1] = pi.P; L[1] = pj.P;
 #pragma unroll
     for (int a = 0; a < D; ++a) { R[2 + a] = vi[a] - vf[a]; L[2 + a] = vj[a] - vf[a]; }
-    double Rb[5], Lb[5];
+    // W -= dt/2 (source + (v - v_frame) . grad W): the particle part,
+    // source + v . grad W, comes with the gradients (Grad::t); the face adds
+    // v_frame . grad W.  The reference uses vz[i] on the j side of the vx and
+    // vy terms in 3D (Particles.cpp:1717,1719): (vz_i - vf_z) = (vz_j - vq_z)
+    // with the shifted frame velocity vq_z = vf_z - (vz_i - vz_j).
+    const double hdt = dt / 2.;
+    const double *Ti = grad[i].t, *Tj = grad[j].t;
+    const int blk[5] = {0, 12, 3, 6, 9};   // gradient blocks: 0 rho, 3 vx, 6 vy, 9 vz, 12 P
+    const double vq2 = D == 3 ? vf[2] - (vi[2] - vj[2]) : 0.;
+    if (D == 2 && !p.pairwise) {
+        // no limiter between reconstruction and prediction: one FMA chain per
+        // field and side, W - dt/2 T + grad W . (x_ij - x_side + dt/2 v_frame)
+        // (a run-wide branch: with the limiter on, image faces that skip it
+        // keep the other form, so that warps do not run both; 3D keeps the
+        // other form, whose registers the 3D face kernels are tuned to)
+        double yi[3], yj[3], yq[3];
 #pragma unroll
-    for (int k = 0; k < NV; ++k) { Rb[k] = R[k]; Lb[k] = L[k]; }
-    // W + grad W . (x_ij - x_side), one FMA chain from W per field
-    R[0] = fma_dotD<D>(Gi + 0, xijxi, R[0]); L[0] = fma_dotD<D>(Gj + 0, xijxj, L[0]);
-    R[1] = fma_dotD<D>(Gi + 12, xijxi, R[1]); L[1] = fma_dotD<D>(Gj + 12, xijxj, L[1]);
-    R[2] = fma_dotD<D>(Gi + 3, xijxi, R[2]); L[2] = fma_dotD<D>(Gj + 3, xijxj, L[2]);
-    R[3] = fma_dotD<D>(Gi + 6, xijxi, R[3]); L[3] = fma_dotD<D>(Gj + 6, xijxj, L[3]);
-    if (D == 3) { R[4] = fma_dotD<D>(Gi + 9, xijxi, R[4]); L[4] = fma_dotD<D>(Gj + 9, xijxj, L[4]); }
-    if (p.pairwise && (!img || p.img_pw)) {
-        double ri, rj;   // |x_ij - x_i| / |x_j - x_i| and |x_ij - x_j| / |x_j - x_i|
-        if (p.foqp) {
-            // x_ij - x_i = (x_j - x_i) / 2 exactly, so both norms are
-            // exactly half of |x_j - x_i| (scaling by 1/2 and 1/4 is exact)
-            // and both quotients are exactly 0.5
-            ri = .5; rj = .5;
-        } else {
-            double xijxi_abs = 0., xijxj_abs = 0., xjxi_abs = 0.;
-#pragma unroll
-            for (int a = 0; a < D; ++a) {
-                xijxi_abs += xijxi[a] * xijxi[a];
-                xijxj_abs += xijxj[a] * xijxj[a];
-                xjxi_abs += xjxi[a] * xjxi[a];
-            }
-            xjxi_abs = sqrt(xjxi_abs);
-            ri = sqrt(xijxi_abs) / xjxi_abs;
-            rj = sqrt(xijxj_abs) / xjxi_abs;
+        for (int a = 0; a < D; ++a) {
+            yi[a] = fma(hdt, vf[a], xijxi[a]);
+            yj[a] = fma(hdt, vf[a], xijxj[a]);
+            yq[a] = (D == 3 && a == 2) ? fma(hdt, vq2, xijxj[a]) : yj[a];
         }
 #pragma unroll
-        for (int k = 0; k < NV; ++k) pairwise_limiter(p, R[k], L[k], Rb[k], Lb[k], ri, rj);
-    }
-    {
-        // div v and 1/rho of both particles, stored once per particle
-        // (gradient pad slot, Geo) with the same arithmetic
-        // W -= dt/2 (source + (v - v_frame) . grad W): the particle part,
-        // source + v . grad W, comes with the gradients (Grad::t); the face
-        // subtracts v_frame . grad W (one FMA chain per field and side)
-        const double hdt = dt / 2.;
-        const double *Ti = grad[i].t, *Tj = grad[j].t;
+        for (int f = 0; f < NV; ++f) {
+            R[f] = fma_dotD<D>(Gi + blk[f], yi, fma(-hdt, Ti[f], R[f]));
+            const double *yy = (D == 3 && (f == 2 || f == 3)) ? yq : yj;
+            L[f] = fma_dotD<D>(Gj + blk[f], yy, fma(-hdt, Tj[f], L[f]));
+        }
+    } else {
+        double Rb[5], Lb[5];
+#pragma unroll
+        for (int k = 0; k < NV; ++k) { Rb[k] = R[k]; Lb[k] = L[k]; }
+        // W + grad W . (x_ij - x_side), one FMA chain from W per field
+#pragma unroll
+        for (int f = 0; f < NV; ++f) {
+            R[f] = fma_dotD<D>(Gi + blk[f], xijxi, R[f]);
+            L[f] = fma_dotD<D>(Gj + blk[f], xijxj, L[f]);
+        }
+        if (p.pairwise && (!img || p.img_pw)) {   // image faces skip it (Particles.cpp:2533-2683)
+            // |x_ij - x_i| / |x_j - x_i| and |x_ij - x_j| / |x_j - x_i|: with the
+            // first-order quadrature point x_ij - x_i = (x_j - x_i) / 2 exactly,
+            // so both norms are exactly half of |x_j - x_i| (scaling by 1/2 and
+            // 1/4 is exact) and both quotients are exactly 0.5
+            double ri = .5, rj = .5;
+            if (!p.foqp) {
+                double xijxi_abs = 0., xijxj_abs = 0., xjxi_abs = 0.;
+#pragma unroll
+                for (int a = 0; a < D; ++a) {
+                    xijxi_abs += xijxi[a] * xijxi[a];
+                    xijxj_abs += xijxj[a] * xijxj[a];
+                    xjxi_abs += xjxi[a] * xjxi[a];
+                }
+                xjxi_abs = sqrt(xjxi_abs);
+                ri = sqrt(xijxi_abs) / xjxi_abs;
+                rj = sqrt(xijxj_abs) / xjxi_abs;
+            }
+#pragma unroll
+            for (int k = 0; k < NV; ++k) pairwise_limiter(p, R[k], L[k], Rb[k], Lb[k], ri, rj);
+        }
+        // the prediction, one FMA chain per field and side from the limited value
         const double nvf[3] = {-vf[0], -vf[1], -vf[2]};
-        // the reference uses vz[i] on the j side of the vx and vy terms
-        // (Particles.cpp:1717,1719): (vz_i - vf_z) = (vz_j - (vf_z + vz_j - vz_i))
-        const double nvq[3] = {-vf[0], -vf[1], D == 3 ? -(vf[2] - (vi[2] - vj[2])) : 0.};
-        const int blk[5] = {0, 12, 3, 6, 9};
+        const double nvq[3] = {-vf[0], -vf[1], -vq2};
 #pragma unroll
         for (int f = 0; f < NV; ++f) {
             R[f] = fma(-hdt, fma_dotD<D>(nvf, Gi + blk[f], Ti[f]), R[f]);
