@@ -1352,13 +1352,18 @@ __global__ void __launch_bounds__(256) k_link(Params p, const uint32_t *__restri
                                               unsigned *__restrict__ status) {
     // faces[] was set to -1: the owner writes (i, slot), the slot on the other
     // side writes rslot, so each field has exactly one writer.  A slot with
-    // j > i owns face faceOff[i] + (its rank among i's canonical slots); a
-    // slot with j < i searches j's list (real part or image part) for i,
-    // counting on the way j's canonical slots before it (the face's rank in
-    // j's list).  The own list is read four slots per load (K is a multiple
-    // of 4) and the searches of those four slots advance together, one
-    // 4-entry load of each list per round, so that a thread has up to four
-    // loads in flight instead of one chain of dependent loads.
+    // j > i owns face faceOff[i] + (its rank among i's canonical slots).  A
+    // slot with j < i finds i in j's list (real part or image part) and the
+    // face's rank in j's list from j's canonical entries (index > j) on one
+    // side of it: searching forward, the rank is the count before i; searching
+    // backward from the end of j's list, it is faceCnt[j] - 1 - the count
+    // after i, faceCnt[j] = faceOff[j + 1] - faceOff[j] being the number of
+    // canonical entries of j's list.  The stencils of i and j mirror each
+    // other, so j early in i's list puts i late in j's list: those searches
+    // and the image searches (images sit at the end of the list) go backward.
+    // The own list is read four slots per load (K is a multiple of 4) and the
+    // searches of those four slots advance together, one 4-entry load of each
+    // list per round, so that a thread has up to four loads in flight.
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < p.n; i += gridDim.x * blockDim.x) {
         const size_t base = (size_t)i * p.K;
         const int nr = noi[i], tot = nr + noiImg[i];
@@ -1367,13 +1372,18 @@ __global__ void __launch_bounds__(256) k_link(Params p, const uint32_t *__restri
         for (int s0 = 0; s0 < tot; s0 += 4) {
             const uint4 q = own[s0 >> 2];
             const uint32_t ev[4] = {q.x, q.y, q.z, q.w};
-            int jj[4], lo[4], hi[4], found[4], crank[4];
-            bool act[4];
+            // per search: j, the length of j's list, the current 4-entry chunk,
+            // the canonical count and flags.  i is sought among j's real
+            // entries (no image bits) or among its images (image bits set), so
+            // an entry's own bits say whether it lies in the searched part.
+            constexpr unsigned ACT = 1u, BWD = 2u, IMG = 4u, FOUND = 8u;
+            int jj[4], jt[4], cur[4], cnt[4];
+            unsigned fl[4];
 #pragma unroll
             for (int k = 0; k < 4; ++k) {
                 const int s = s0 + k;
                 const int j = (int)(ev[k] & IDX_MASK);
-                jj[k] = j; lo[k] = 0; hi[k] = 0; found[k] = -1; crank[k] = 0; act[k] = false;
+                jj[k] = j; jt[k] = 0; cur[k] = 0; cnt[k] = 0; fl[k] = 0u;
                 if (s >= tot) continue;
                 if (j > i) {
                     const int fid = faceOff[i] + rank;
@@ -1384,45 +1394,51 @@ __global__ void __launch_bounds__(256) k_link(Params p, const uint32_t *__restri
                     faces[fid].slot = s;
                     continue;
                 }
-                const int jnr = noi[j];
+                jt[k] = noi[j] + noiImg[j];
                 const bool img = s >= nr;
-                lo[k] = img ? jnr : 0;
-                hi[k] = img ? jnr + noiImg[j] : jnr;
-                act[k] = true;
+                // a particle that is its own image searches forward
+                const bool bwd = (img || 2 * s < nr) && j != i;
+                cur[k] = bwd ? (jt[k] - 1) >> 2 : 0;
+                fl[k] = ACT | (bwd ? BWD : 0u) | (img ? IMG : 0u);
             }
-            for (int t4 = 0;; ++t4) {
+            for (;;) {
                 uint4 r[4];
                 bool any = false;
 #pragma unroll
                 for (int k = 0; k < 4; ++k) {
-                    if (t4 * 4 >= hi[k]) act[k] = false;   // searched to the end (not found)
-                    r[k] = act[k] ? reinterpret_cast<const uint4 *>(nbr + (size_t)jj[k] * p.K)[t4]
-                                  : make_uint4(0u, 0u, 0u, 0u);
-                    any |= act[k];
+                    // past either end of j's list: not found
+                    if ((fl[k] & BWD) ? cur[k] < 0 : cur[k] * 4 >= jt[k]) fl[k] &= ~ACT;
+                    r[k] = (fl[k] & ACT) ? reinterpret_cast<const uint4 *>(nbr + (size_t)jj[k] * p.K)[cur[k]]
+                                         : make_uint4(0u, 0u, 0u, 0u);
+                    any |= (fl[k] & ACT) != 0u;
                 }
                 if (!any) break;
 #pragma unroll
                 for (int k = 0; k < 4; ++k) {
-                    if (!act[k]) continue;
+                    if (!(fl[k] & ACT)) continue;
+                    const bool bwd = (fl[k] & BWD) != 0u, img = (fl[k] & IMG) != 0u;
                     const uint32_t v[4] = {r[k].x, r[k].y, r[k].z, r[k].w};
 #pragma unroll
-                    for (int m = 0; m < 4; ++m) {
-                        const int t = t4 * 4 + m;
-                        const int idx = (int)(v[m] & IDX_MASK);
-                        if (found[k] < 0 && t < hi[k]) {
-                            if (t >= lo[k] && idx == i) found[k] = t;
-                            else crank[k] += idx > jj[k];
+                    for (int mm = 0; mm < 4; ++mm) {
+                        const int m = bwd ? 3 - mm : mm;
+                        const int t = cur[k] * 4 + m;
+                        const uint32_t e = v[m];
+                        const int idx = (int)(e & IDX_MASK);
+                        if (!(fl[k] & FOUND) && t < jt[k]) {
+                            if (idx == i && ((e >> IMG_SHIFT) != 0u) == img) fl[k] |= FOUND;
+                            else cnt[k] += idx > jj[k];
                         }
                     }
-                    if (found[k] >= 0) act[k] = false;
+                    if (fl[k] & FOUND) fl[k] &= ~ACT;
+                    else cur[k] += bwd ? -1 : 1;
                 }
             }
 #pragma unroll
             for (int k = 0; k < 4; ++k) {
                 const int s = s0 + k;
                 if (s >= tot || jj[k] > i) continue;
-                if (found[k] < 0) { flag(status, ST_ASYMMETRIC); faceOf[base + s] = 0; continue; }
-                const int fid = faceOff[jj[k]] + crank[k];
+                if (!(fl[k] & FOUND)) { flag(status, ST_ASYMMETRIC); faceOf[base + s] = 0; continue; }
+                const int fid = (fl[k] & BWD) ? faceOff[jj[k] + 1] - 1 - cnt[k] : faceOff[jj[k]] + cnt[k];
                 if (fid >= p.faces_cap) { flag(status, ST_CAPACITY); faceOf[base + s] = 0; continue; }
                 faceOf[base + s] = -(fid + 1);
                 faces[fid].rslot = s;
