@@ -61,8 +61,8 @@ FACE_ALG_FLOPS = {3: 746.0, 2: 339.8}
 # Sedov step (profiles/sedov64_step_kernels.md); 2D: 32 members of the
 # Kelvin-Helmholtz ensemble with the second Newton pass
 # (profiles/kh_ensemble32_step_kernels.md).
-FACE_EXEC_FP64_FLOPS = {3: 544.0, 2: 417.0}
-FACE_DRAM_BYTES = {3: 298.0, 2: 362.0}
+FACE_EXEC_FP64_FLOPS = {3: 541.0, 2: 391.0}
+FACE_DRAM_BYTES = {3: 298.0, 2: 364.0}
 
 
 def make_workload(name: str, seed_offset: int = 0):
@@ -242,8 +242,10 @@ def kernel_breakdown(sim, steps):
 
 def learned_section(runtime, make_sim, tuning, args, faces_per_step, st_plain, kt_plain, rho_plain, ws, n):
     """The same steps with the learned p* guess: harvest faces of step 1
-    (plain pipeline), train the MLP on 90 % of them, step with the network
-    guess to the same step count and compare with the plain run."""
+    (plain pipeline), train the MLP on 90 % of them, tune the learned
+    pipeline's launch shapes and face-pass structure with the autotuner
+    (which restores the state), step with the network guess to the same step
+    count and compare with the plain run."""
     import torch
     sim2 = make_sim()
     if tuning:
@@ -261,6 +263,7 @@ def learned_section(runtime, make_sim, tuning, args, faces_per_step, st_plain, k
     yv = runtime.pstar_infer(w, x[val])
     rel = np.abs(np.exp(yv.astype(np.float64) - t[val]) - 1.0)
     sim2.set_pstar_weights(w)
+    tuning_l = sim2.autotune(2) if tuning else None
     if args.warmup > 1:
         sim2.step(args.warmup - 1)
     torch.cuda.synchronize()
@@ -278,6 +281,7 @@ def learned_section(runtime, make_sim, tuning, args, faces_per_step, st_plain, k
             "faces_kernel_ms_per_step": kt["faces_riemann"][1] / max(kt["faces_riemann"][0], 1),
             "plain_faces_kernel_ms_per_step": kt_plain["faces_riemann"][1] / max(kt_plain["faces_riemann"][0], 1),
             "density_L1_vs_plain": l1,
+            "tuning": tuning_l,
             "status": runtime.status_names(st.status),
             "guess": "p_TR * exp(y) where |y| > 0.01, else p_TR (two-rarefaction)",
             "train": {"samples": int(tr.size), "val_samples": int(nval), "harvest_stride": stride,
