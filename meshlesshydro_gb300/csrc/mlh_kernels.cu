@@ -1929,10 +1929,16 @@ __global__ void MLH_FACE_BOUNDS k_faces_block(Params p, const Member *__restrict
                                    L, A, vf, hatA, unR, unL);
         bool unfinished = false;
         if (valid) {
-            // strong shocks of the learned step go to the network's queue
-            const double defer = LEARNED ? PSTAR_HARD * (dlt(L[1], R[1]) ? L[1] : R[1]) : 0.;   // min on the keys
-            Solve5 s0 = riemann5_begin(rc, R[0], unR, R[1], L[0], unL, L[1], -1., defer, 1);
-            if (LEARNED && s0.stage == 3) {
+            // strong shocks of the learned step go to the network's queue;
+            // one call site of the solver's start (a second pass without
+            // deferral only when the queue is full), so that the kernel holds
+            // one copy of it
+            double defer = LEARNED ? PSTAR_HARD * (dlt(L[1], R[1]) ? L[1] : R[1]) : 0.;   // min on the keys
+            Solve5 s0;
+#pragma unroll 1
+            for (int pass = 0; pass < 2; ++pass) {
+                s0 = riemann5_begin(rc, R[0], unR, R[1], L[0], unL, L[1], -1., defer, 1);
+                if (!(LEARNED && s0.stage == 3)) break;
                 const int q = atomicAdd(qa.count, 1);
                 if (q < qa.cap) {
                     FaceState &fs = qa.st[q];
@@ -1944,9 +1950,9 @@ __global__ void MLH_FACE_BOUNDS k_faces_block(Params p, const Member *__restrict
                     qa.face[q] = f;
                     feat[q] = pstar_features(R, L, unR, unL, p.gamma);
                     valid = false;   // solved by the pass over the queue
-                } else {
-                    s0 = riemann5_begin(rc, R[0], unR, R[1], L[0], unL, L[1], -1., 0., 1);
+                    break;
                 }
+                defer = 0.;   // queue full: solved here
             }
             if (valid) {
                 sv[threadIdx.x] = s0;
