@@ -15,7 +15,7 @@
 extern "C" {
 #endif
 
-#define MLH_ABI_VERSION 3
+#define MLH_ABI_VERSION 4
 
 /* Status bits.  The reference exits instead (demonstrator/src/Particles.cpp:
  * 348-352 exit(1) neighbour overflow, :2249-2253 exit(3), :1878-1881 exit(6)
@@ -146,18 +146,22 @@ typedef struct mlh_tuning {
                               * 2 are continued inside the block by its first
                               * threads; 0: one pass (the plain gamma = 5/3
                               * step only) */
+    int link_overlap;        /* 1: the face links run on a second stream beside
+                              * the time step and the gradients; 0: in order
+                              * on the step's stream */
 } mlh_tuning;
 
-/* Autotuner: times the face passes with and without the split, then
- * candidate launch shapes of the face, gradient and neighbour kernels, over
+/* Autotuner: times the face-pass structures over candidate grids, then
+ * candidate launch shapes of the face, gradient and neighbour kernels, then
+ * whole steps with and without the overlapped face links, over
  * `trial_steps` steps each (from a saved copy of the
  * state, which is restored afterwards), keeps the fastest in the context and
  * reports them in *out (may be NULL).  Needs one state-sized temporary. */
 int mlh_autotune(mlh_ctx *ctx, int trial_steps, mlh_tuning *out);
 /* Set the launch shapes directly (for example those an autotuned context of
  * the same workload reported).  Threads per block: 64, 128 or 256; blocks
- * per SM 1..32; warps per SM 8..256; face_split 0, 1 or 2.  MLH_ERR_INVALID
- * otherwise. */
+ * per SM 1..32; warps per SM 8..256; face_split 0, 1 or 2; link_overlap 0 or
+ * 1.  MLH_ERR_INVALID otherwise. */
 int mlh_set_tuning(mlh_ctx *ctx, const mlh_tuning *tuning);
 
 /* Per-particle smoothing lengths of the current state (no counterpart in the

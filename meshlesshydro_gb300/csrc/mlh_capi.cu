@@ -642,7 +642,7 @@ int mlh_set_tuning(mlh_ctx *c, const mlh_tuning *t) {
     auto threads_ok = [](int v) { return v == 64 || v == 128 || v == 256; };
     if (!c || !t || !threads_ok(t->face_threads) || !threads_ok(t->grad_threads) || t->face_blocks_per_sm < 1 ||
         t->face_blocks_per_sm > 32 || t->nns_warps_per_sm < 8 || t->nns_warps_per_sm > 256 ||
-        t->face_split < 0 || t->face_split > 2) {
+        t->face_split < 0 || t->face_split > 2 || t->link_overlap < 0 || t->link_overlap > 1) {
         g_last_error = "invalid tuning";
         return MLH_ERR_INVALID;
     }
@@ -652,6 +652,7 @@ int mlh_set_tuning(mlh_ctx *c, const mlh_tuning *t) {
     c->tune.grad_threads = t->grad_threads;
     c->tune.nns_warps_per_sm = t->nns_warps_per_sm;
     c->tune.face_split = t->face_split;
+    c->tune.link_overlap = t->link_overlap;
     drop_graph(c);
     return 0;
 }
@@ -744,6 +745,22 @@ int mlh_autotune(mlh_ctx *c, int trial_steps, mlh_tuning *out) {
             if (ms < best_ms) { best_ms = ms; best.nns_warps_per_sm = w; }
         }
         c->tune.nns_warps_per_sm = best.nns_warps_per_sm;
+        // the face links beside the time step and the gradients, or in order:
+        // whole steps without per-kernel timing (which serialises the
+        // streams), the better of two trials each
+        double best_step = 1e300;
+        for (int ov : {1, 0}) {
+            c->tune.link_overlap = ov;
+            for (int rep = 0; rep < 2; ++rep) {
+                if ((rc = restore())) goto done;
+                mlh_step_stats st;
+                rc = mlh_step(c, trial_steps, 0., &st);
+                if (rc & (MLH_ERR_CUDA | MLH_ERR_INVALID)) goto done;
+                rc = 0;
+                if (st.device_ms < best_step) { best_step = st.device_ms; best.link_overlap = ov; }
+            }
+        }
+        c->tune.link_overlap = best.link_overlap;
     }
 done:
     {
@@ -761,6 +778,7 @@ done:
         out->grad_threads = c->tune.grad_threads;
         out->nns_warps_per_sm = c->tune.nns_warps_per_sm;
         out->face_split = c->tune.face_split;
+        out->link_overlap = c->tune.link_overlap;
     }
     return rc;
 }

@@ -2259,7 +2259,7 @@ void launch_step(StepArgs &a) {
     // the face links (integer work) need only the neighbour lists: without
     // per-kernel timing they run on the second stream while the time step and
     // the gradients keep the FP64 pipe busy
-    const bool overlap = a.stream2 && !a.timer && !a.stop_after_gradients;
+    const bool overlap = a.stream2 && !a.timer && !a.stop_after_gradients && a.tune.link_overlap;
     const int blocksLink = blocksN;
     auto launch_links = [&](cudaStream_t ls) {
         exclusive_scan(a.faceCnt, p.n, a.faceOff, a.scanTiles, a.scanTotal, ls);

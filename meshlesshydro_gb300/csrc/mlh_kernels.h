@@ -16,6 +16,7 @@ struct Tuning {
     int grad_threads = 128;        // threads per block of k_gradients
     int nns_warps_per_sm = 64;     // warps (= particles in flight) of k_neighbours
     int face_split = 1;            // plain gamma = 5/3 step: 1 second Newton pass over a queue, 2 in-block, 0 none
+    int link_overlap = 1;          // face links on the second stream beside the time step and gradients
 };
 
 // Device pointers and settings of one step.

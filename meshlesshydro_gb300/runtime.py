@@ -44,7 +44,8 @@ class Tuning(ctypes.Structure):
     """mlh_tuning: launch shapes chosen by the autotuner."""
     _fields_ = [("face_threads", ctypes.c_int), ("face_blocks_per_sm", ctypes.c_int),
                 ("grad_threads", ctypes.c_int), ("nns_warps_per_sm", ctypes.c_int),
-                ("face_split", ctypes.c_int)]
+                ("face_split", ctypes.c_int),
+                ("link_overlap", ctypes.c_int)]
 
 
 class ParticlesView(ctypes.Structure):
@@ -358,8 +359,10 @@ class Simulation:
         return {k: getattr(t, k) for k, _ in Tuning._fields_}
 
     def set_tuning(self, tuning: dict):
-        """Launch shapes (mlh_set_tuning); face_split defaults to 1."""
-        t = Tuning(**{k: int(tuning.get(k, 1) if k == "face_split" else tuning[k]) for k, _ in Tuning._fields_})
+        """Launch shapes (mlh_set_tuning); face_split and link_overlap
+        default to 1."""
+        t = Tuning(**{k: int(tuning.get(k, 1) if k in ("face_split", "link_overlap") else tuning[k])
+                      for k, _ in Tuning._fields_})
         st = self.L.mlh_set_tuning(self.h, ctypes.byref(t))
         if st != 0:
             raise MLHError(st, "mlh_set_tuning", self.L.mlh_last_error().decode())

@@ -22,7 +22,7 @@ def test_header_and_exports_agree():
     for n in names:
         assert hasattr(L, n), n
     assert set(names) == set(runtime.EXPORTS)
-    assert L.mlh_abi_version() == 3
+    assert L.mlh_abi_version() == 4
     from meshlesshydro_gb300 import io
     io_names = declared_functions("mlh_io.h")
     for n in io_names:

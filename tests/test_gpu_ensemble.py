@@ -122,11 +122,21 @@ def test_set_tuning_validates_and_keeps_bits():
     cfg = MFVConfig.kelvin_helmholtz(members[0])
     a = _sim(cfg, members)
     b = _sim(cfg, members)
+    c = _sim(cfg, members)
     b.set_tuning({"face_threads": 256, "face_blocks_per_sm": 3, "grad_threads": 64, "nns_warps_per_sm": 16})
+    # the face links in order on the step's stream instead of beside the
+    # time step and the gradients
+    c.set_tuning({"face_threads": 128, "face_blocks_per_sm": 8, "grad_threads": 128, "nns_warps_per_sm": 64,
+                  "link_overlap": 0})
     with pytest.raises(runtime.MLHError):
         b.set_tuning({"face_threads": 96, "face_blocks_per_sm": 3, "grad_threads": 64, "nns_warps_per_sm": 16})
+    with pytest.raises(runtime.MLHError):
+        b.set_tuning({"face_threads": 256, "face_blocks_per_sm": 3, "grad_threads": 64, "nns_warps_per_sm": 16,
+                      "link_overlap": 2})
     a.step(2)
     b.step(2)
-    sa, sb = a.get_state(), b.get_state()
+    c.step(2)
+    sa, sb, sc = a.get_state(), b.get_state(), c.get_state()
     for key in sa:
         assert np.array_equal(sa[key], sb[key]), key
+        assert np.array_equal(sa[key], sc[key]), key
