@@ -64,6 +64,53 @@ FACE_ALG_FLOPS = {3: 746.0, 2: 339.8}
 FACE_EXEC_FP64_FLOPS = {3: 541.0, 2: 391.0}
 FACE_DRAM_BYTES = {3: 298.0, 2: 364.0}
 
+# Every kernel of the step, per unit (particle, or canonical face for the
+# face passes): (FP64 flops executed, DRAM bytes read + written) from the
+# same ncu captures (3D: Sedov 64^3; 2D: 32 KH ensemble members), and the
+# algorithmic operations of the reference's method from the
+# operation-counting oracle (3D: 32^3 Sedov lattice; 2D: 100x100 KH set-up).
+# The per-unit figures scale with the units of the measured workload.
+KERNEL_UNITS = {"neighbours_density": "particle", "timestep": "particle", "gradients_limiter": "particle",
+                "face_links": "particle", "faces_riemann": "face", "gather_update": "particle"}
+KERNEL_EXEC = {
+    3: {"neighbours_density": (1030.0, 917.0), "timestep": (607.0, 652.0), "gradients_limiter": (3747.0, 1692.0),
+        "face_links": (0.0, 1010.0), "faces_riemann": (541.0, 298.0), "gather_update": (214.0, 1504.0)},
+    2: {"neighbours_density": (597.0, 733.0), "timestep": (311.0, 748.0), "gradients_limiter": (1382.0, 1962.0),
+        "face_links": (0.0, 781.0), "faces_riemann": (391.0, 364.0), "gather_update": (122.0, 915.0)},
+}
+KERNEL_ALG_OPS = {
+    3: {"neighbours_density": 3618.0, "timestep": 754.0, "gradients_limiter": 7871.0, "face_links": 0.0,
+        "faces_riemann": 746.0, "gather_update": 198.0},
+    2: {"neighbours_density": 700.0, "timestep": 375.0, "gradients_limiter": 2678.0, "face_links": 0.0,
+        "faces_riemann": 339.8, "gather_update": 108.0},
+}
+
+
+def kernel_rooflines(kernel_ms: dict, dim: int, particles: float, faces: float, fp64_peak_tflops, hbm_peak_gbs):
+    """Each kernel of the step against the FP64 and the HBM roofline: its
+    time per step (CUDA events), the FP64 flops it executes and the DRAM
+    bytes it moves per unit (ncu), the rates they give, as fractions of the
+    measured FP64 FMA peak and HBM copy bandwidth, and the rate of the
+    reference's algorithmic operations."""
+    out = {}
+    for k, unit in KERNEL_UNITS.items():
+        ms = kernel_ms.get(k)
+        if not ms or ms <= 0.0 or dim not in KERNEL_EXEC:
+            continue
+        fl, by = KERNEL_EXEC[dim][k]
+        alg = KERNEL_ALG_OPS[dim][k]
+        units = faces if unit == "face" else particles
+        s = ms / 1e3
+        tf = fl * units / s / 1e12
+        gbs = by * units / s / 1e9
+        out[k] = {"ms_per_step": ms, "unit": unit, "units_per_step": units,
+                  "fp64_flops_per_unit": fl, "fp64_tflops": tf,
+                  "fp64_frac": tf / fp64_peak_tflops if fp64_peak_tflops else None,
+                  "dram_bytes_per_unit": by, "hbm_gbs": gbs,
+                  "hbm_frac": gbs / hbm_peak_gbs if hbm_peak_gbs else None,
+                  "algorithmic_ops_per_unit": alg, "algorithmic_tflops": alg * units / s / 1e12}
+    return out
+
 
 def make_workload(name: str, seed_offset: int = 0):
     from meshlesshydro_gb300 import ic
@@ -452,6 +499,14 @@ def run_mlh(args):
                 "avg_launch_ms": dom_avg_s * 1e3,
                 "hbm_view": {"achieved_gbs": (bytes_per_face * faces_per_step / dom_avg_s / 1e9) if bytes_per_face else None,
                              "peak_gbs": peaks.get("hbm_gbs"), "peak_source": peak_kind}}
+    try:   # every kernel against its roofline (arithmetic on the measured times)
+        kernels = kernel_rooflines({k: v[1] / max(v[0], 1) for k, v in kt.items()}, cfg.dim, float(n),
+                                   float(faces_per_step), fp64_peak, peaks.get("hbm_gbs"))
+        kernels["source"] = ("ms: CUDA events; FP64 flops and DRAM bytes per unit: ncu --set full of the same "
+                             "kernels (3D Sedov 64^3, 2D KH ensemble members); algorithmic operations: "
+                             "operation-counting oracle; peaks: FP64 FMA probe, measured HBM copy")
+    except Exception as exc:   # never let the breakdown cost the bench line
+        kernels = {"error": repr(exc)}
     line = {"metric": METRIC, "value": value, "unit": "particle-updates/s", "n_gpus": ws, "steps": st.steps,
             "warmup": args.warmup, "ms_per_step": 1e3 * t_max / st.steps, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
@@ -469,6 +524,7 @@ def run_mlh(args):
             "kernel_ms_source": "up to 3 further steps with per-kernel CUDA events, which serialise the face-link "
                                 "stream that the timed steps overlap with the time step and gradients",
             "roofline": roofline,
+            "kernels": kernels,
             "clocks": ck,
             "tuning": tuning,
             **extra,

@@ -71,3 +71,29 @@ def test_bench_face_flops_are_the_counted_ones(oracle_mod, dim):
     res = flops.count(cfg, p, 16)
     got = res["per_unit"]["faces_riemann"]
     assert abs(bench.FACE_ALG_FLOPS[dim] - got) <= 0.0005 * got, (bench.FACE_ALG_FLOPS[dim], got)
+    # and the other kernels' algorithmic operations of the per-kernel table
+    for k, v in bench.KERNEL_ALG_OPS[dim].items():
+        got = res["per_unit"][k] if k in res["per_unit"] else 0.0
+        assert abs(v - got) <= 0.002 * max(got, 1.0), (k, v, got)
+
+
+def test_kernel_rooflines_arithmetic():
+    """bench.kernel_rooflines: rates and fractions from the per-step times,
+    kernels without a time left out, the face row consistent with the
+    dominant kernel's constants."""
+    import bench
+    for dim in (2, 3):
+        assert bench.KERNEL_EXEC[dim]["faces_riemann"] == (bench.FACE_EXEC_FP64_FLOPS[dim], bench.FACE_DRAM_BYTES[dim])
+        assert bench.KERNEL_ALG_OPS[dim]["faces_riemann"] == bench.FACE_ALG_FLOPS[dim]
+    kt = {"neighbours_density": 2.0, "faces_riemann": 10.0, "face_links": 0.0, "grid_bin": 0.3}
+    r = bench.kernel_rooflines(kt, 3, 1.0e6, 2.0e7, 1.0, 5000.0)
+    assert set(r) == {"neighbours_density", "faces_riemann"}
+    f = r["faces_riemann"]
+    assert f["unit"] == "face" and f["units_per_step"] == 2.0e7
+    assert abs(f["fp64_tflops"] - 541.0 * 2.0e7 / 10.0e-3 / 1e12) < 1e-12
+    assert abs(f["fp64_frac"] - f["fp64_tflops"]) < 1e-12
+    assert abs(f["hbm_gbs"] - 298.0 * 2.0e7 / 10.0e-3 / 1e9) < 1e-9
+    assert abs(f["hbm_frac"] - f["hbm_gbs"] / 5000.0) < 1e-12
+    nb = r["neighbours_density"]
+    assert nb["unit"] == "particle" and abs(nb["algorithmic_tflops"] - 3618.0 * 1.0e6 / 2.0e-3 / 1e12) < 1e-12
+    assert bench.kernel_rooflines(kt, 3, 1.0e6, 2.0e7, None, None)["faces_riemann"]["fp64_frac"] is None
