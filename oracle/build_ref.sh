@@ -42,7 +42,7 @@ PY
 )"
 [ -n "$BLAS" ] || { echo "scipy OpenBLAS not found" >&2; exit 1; }
 
-params() {  # name dim periodic cfl beta pairwise
+params() {  # name dim periodic cfl beta pairwise [first_order_quad_point, default 1]
   local f="$OUT/params_$1.h"
   cat > "$f" <<EOF
 #ifndef DEMONSTRATOR_PARAMETER_H
@@ -62,7 +62,7 @@ params() {  # name dim periodic cfl beta pairwise
 #define ENFORCE_FLUX_SYM 1
 #define MOVE_PARTICLES 1
 #define DEBUG_LVL 0
-#define FIRST_ORDER_QUAD_POINT 1
+#define FIRST_ORDER_QUAD_POINT ${7:-1}
 #define RUNSPH $([ "$2" = 3 ] && echo '(__COUNTER__ < 3)' || echo 0)
 #define ARTVISC 0
 #define VERBOSITY_PARTICLES 10
@@ -95,9 +95,15 @@ KH=$(params kh 2 1 .3 4. 0)
 KHPW=$(params khpw 2 1 .3 4. 1)
 SED=$(params sedov 3 0 .25 1. 1)
 SEDNP=$(params sedovnopw 3 0 .25 1. 0)
+# the face point x_i + kernelSize/4 (x_j - x_i) instead of the midpoint; in 3D
+# this path sets xjxi[2], so the 3D pairwise limiter is well defined there
+KHQ=$(params khq 2 1 .3 4. 1 0)
+SEDQ=$(params sedovq 3 0 .25 1. 1 0)
 build kh_dbl "$KH" dbl
 build kh_int "$KH" int
 build khpw_dbl "$KHPW" dbl
 build sedov_dbl "$SED" dbl
 build sedov_int "$SED" int
 build sedovnopw_dbl "$SEDNP" dbl
+build khq_dbl "$KHQ" dbl
+build sedovq_dbl "$SEDQ" dbl

@@ -6,7 +6,8 @@ seeded inputs and stores inputs and outputs as .npz files.  The reference tree
 is needed only here; the fixtures travel with the repository and pin the CPU
 restatement (oracle/) on any host.
 
-    python tests/golden/make_golden.py      # after: bash oracle/build_ref.sh
+    python tests/golden/make_golden.py [name ...]   # after: bash oracle/build_ref.sh
+                                                    # (no names: every fixture)
 
 Variants (abs binding, see oracle/build_ref.sh):
   kh24_dbl      2D periodic Kelvin-Helmholtz, 24x24, fabs limiters
@@ -16,6 +17,11 @@ Variants (abs binding, see oracle/build_ref.sh):
                 reference's 3D pairwise limiter reads an uninitialised xjxi[2])
   kh100_dbl     the 100x100 Kelvin-Helmholtz set-up: lists and state after
                 one step, state after ten steps
+  kh24q_dbl     kh24pw_dbl with FIRST_ORDER_QUAD_POINT 0 (face point
+                x_i + kernelSize/4 (x_j - x_i))
+  sedov12q_dbl  3D non-periodic Sedov 12^3 with the pairwise limiter and
+                FIRST_ORDER_QUAD_POINT 0, where the reference's 3D pairwise
+                limiter reads only initialised values
 """
 import hashlib
 import os
@@ -84,16 +90,21 @@ def summary(name, variant, p, nsteps):
     print("wrote", name)
 
 
-def main():
-    kh24 = ic.kelvin_helmholtz(n_side=24, seed=3)
-    full("kh24_dbl", "kh_dbl", kh24, 5)
-    full("kh24_int", "kh_int", kh24, 5)
-    full("kh24pw_dbl", "khpw_dbl", kh24, 5)
-    sd12 = ic.sedov(n_side=12, seed=4, energy=0.05)
-    full("sedov12np_dbl", "sedovnopw_dbl", sd12, 1)
-    kh100 = ic.kelvin_helmholtz(n_side=100, seed=1)
-    summary("kh100_dbl", "kh_dbl", kh100, 10)
+def main(names):
+    kh24 = lambda: ic.kelvin_helmholtz(n_side=24, seed=3)
+    sd12 = lambda: ic.sedov(n_side=12, seed=4, energy=0.05)
+    makers = {
+        "kh24_dbl": lambda: full("kh24_dbl", "kh_dbl", kh24(), 5),
+        "kh24_int": lambda: full("kh24_int", "kh_int", kh24(), 5),
+        "kh24pw_dbl": lambda: full("kh24pw_dbl", "khpw_dbl", kh24(), 5),
+        "sedov12np_dbl": lambda: full("sedov12np_dbl", "sedovnopw_dbl", sd12(), 1),
+        "kh100_dbl": lambda: summary("kh100_dbl", "kh_dbl", ic.kelvin_helmholtz(n_side=100, seed=1), 10),
+        "kh24q_dbl": lambda: full("kh24q_dbl", "khq_dbl", kh24(), 5),
+        "sedov12q_dbl": lambda: full("sedov12q_dbl", "sedovq_dbl", sd12(), 1),
+    }
+    for name in names or list(makers):
+        makers[name]()
 
 
 if __name__ == "__main__":
-    main()
+    main(sys.argv[1:])

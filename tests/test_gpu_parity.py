@@ -31,6 +31,9 @@ def cases():
         "kh24": (kh24, MFVConfig.kelvin_helmholtz(kh24)),
         "kh24_int_abs": (kh24, MFVConfig.kelvin_helmholtz(kh24, int_abs=True)),
         "kh24_pairwise": (kh24, MFVConfig.kelvin_helmholtz(kh24, pairwise_limiter=True)),
+        # the face point x_i + kernelSize/4 (x_j - x_i) (FIRST_ORDER_QUAD_POINT 0)
+        "kh24_pairwise_q": (kh24, MFVConfig.kelvin_helmholtz(kh24, pairwise_limiter=True,
+                                                             first_order_quad_point=False)),
         "kh100": (kh100, MFVConfig.kelvin_helmholtz(kh100)),
         "sedov12_nonperiodic_nopw": (sd12, MFVConfig.sedov(sd12, periodic=False, pairwise_limiter=False)),
         "sedov16_nonperiodic": (sd16, MFVConfig.sedov(sd16, periodic=False)),
