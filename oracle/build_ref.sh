@@ -42,7 +42,7 @@ PY
 )"
 [ -n "$BLAS" ] || { echo "scipy OpenBLAS not found" >&2; exit 1; }
 
-params() {  # name dim periodic cfl beta pairwise [first_order_quad_point, default 1]
+params() {  # name dim periodic cfl beta pairwise [first_order_quad_point 1] [finite_mass 0] [move 1]
   local f="$OUT/params_$1.h"
   cat > "$f" <<EOF
 #ifndef DEMONSTRATOR_PARAMETER_H
@@ -58,9 +58,9 @@ params() {  # name dim periodic cfl beta pairwise [first_order_quad_point, defau
 #define PAIRWISE_LIMITER $6
 #define PSI_1 .5
 #define PSI_2 .25
-#define MESHLESS_FINITE_MASS 0
+#define MESHLESS_FINITE_MASS ${8:-0}
 #define ENFORCE_FLUX_SYM 1
-#define MOVE_PARTICLES 1
+#define MOVE_PARTICLES ${9:-1}
 #define DEBUG_LVL 0
 #define FIRST_ORDER_QUAD_POINT ${7:-1}
 #define RUNSPH $([ "$2" = 3 ] && echo '(__COUNTER__ < 3)' || echo 0)
@@ -99,6 +99,9 @@ SEDNP=$(params sedovnopw 3 0 .25 1. 0)
 # this path sets xjxi[2], so the 3D pairwise limiter is well defined there
 KHQ=$(params khq 2 1 .3 4. 1 0)
 SEDQ=$(params sedovq 3 0 .25 1. 1 0)
+# the meshless finite mass scheme, and particles that do not move
+KHMFM=$(params khmfm 2 1 .3 4. 0 1 1)
+KHFIX=$(params khfix 2 1 .3 4. 0 1 0 0)
 build kh_dbl "$KH" dbl
 build kh_int "$KH" int
 build khpw_dbl "$KHPW" dbl
@@ -107,3 +110,5 @@ build sedov_int "$SED" int
 build sedovnopw_dbl "$SEDNP" dbl
 build khq_dbl "$KHQ" dbl
 build sedovq_dbl "$SEDQ" dbl
+build khmfm_dbl "$KHMFM" dbl
+build khfix_dbl "$KHFIX" dbl

@@ -22,6 +22,8 @@ Variants (abs binding, see oracle/build_ref.sh):
   sedov12q_dbl  3D non-periodic Sedov 12^3 with the pairwise limiter and
                 FIRST_ORDER_QUAD_POINT 0, where the reference's 3D pairwise
                 limiter reads only initialised values
+  kh24mfm_dbl   kh24_dbl with MESHLESS_FINITE_MASS 1
+  kh24fix_dbl   kh24_dbl with MOVE_PARTICLES 0
 """
 import hashlib
 import os
@@ -101,6 +103,8 @@ def main(names):
         "kh100_dbl": lambda: summary("kh100_dbl", "kh_dbl", ic.kelvin_helmholtz(n_side=100, seed=1), 10),
         "kh24q_dbl": lambda: full("kh24q_dbl", "khq_dbl", kh24(), 5),
         "sedov12q_dbl": lambda: full("sedov12q_dbl", "sedovq_dbl", sd12(), 1),
+        "kh24mfm_dbl": lambda: full("kh24mfm_dbl", "khmfm_dbl", kh24(), 5),
+        "kh24fix_dbl": lambda: full("kh24fix_dbl", "khfix_dbl", kh24(), 5),
     }
     for name in names or list(makers):
         makers[name]()

@@ -20,6 +20,8 @@ CASES = {
     "kh24pw_dbl": dict(kind="kh", pairwise_limiter=True),
     "sedov12np_dbl": dict(kind="sedov", periodic=False, pairwise_limiter=False),
     "kh24q_dbl": dict(kind="kh", pairwise_limiter=True, first_order_quad_point=False),
+    "kh24mfm_dbl": dict(kind="kh", meshless_finite_mass=True),
+    "kh24fix_dbl": dict(kind="kh", move_particles=False),
 }
 
 
