@@ -42,7 +42,7 @@ PY
 )"
 [ -n "$BLAS" ] || { echo "scipy OpenBLAS not found" >&2; exit 1; }
 
-params() {  # name dim periodic cfl beta pairwise [first_order_quad_point 1] [finite_mass 0] [move 1]
+params() {  # name dim periodic cfl beta pairwise [first_order_quad_point 1] [finite_mass 0] [move 1] [slope 1]
   local f="$OUT/params_$1.h"
   cat > "$f" <<EOF
 #ifndef DEMONSTRATOR_PARAMETER_H
@@ -53,7 +53,7 @@ params() {  # name dim periodic cfl beta pairwise [first_order_quad_point 1] [fi
 #define CFL $4
 #define MAX_NUM_INTERACTIONS 400
 #define MAX_NUM_GHOST_INTERACTIONS 300
-#define SLOPE_LIMITING 1
+#define SLOPE_LIMITING ${10:-1}
 #define BETA $5
 #define PAIRWISE_LIMITER $6
 #define PSI_1 .5
@@ -102,6 +102,8 @@ SEDQ=$(params sedovq 3 0 .25 1. 1 0)
 # the meshless finite mass scheme, and particles that do not move
 KHMFM=$(params khmfm 2 1 .3 4. 0 1 1)
 KHFIX=$(params khfix 2 1 .3 4. 0 1 0 0)
+# no slope limiter
+KHNOLIM=$(params khnolim 2 1 .3 4. 0 1 0 1 0)
 build kh_dbl "$KH" dbl
 build kh_int "$KH" int
 build khpw_dbl "$KHPW" dbl
@@ -112,3 +114,4 @@ build khq_dbl "$KHQ" dbl
 build sedovq_dbl "$SEDQ" dbl
 build khmfm_dbl "$KHMFM" dbl
 build khfix_dbl "$KHFIX" dbl
+build khnolim_dbl "$KHNOLIM" dbl

@@ -24,6 +24,7 @@ Variants (abs binding, see oracle/build_ref.sh):
                 limiter reads only initialised values
   kh24mfm_dbl   kh24_dbl with MESHLESS_FINITE_MASS 1
   kh24fix_dbl   kh24_dbl with MOVE_PARTICLES 0
+  kh24nolim_dbl kh24_dbl with SLOPE_LIMITING 0
 """
 import hashlib
 import os
@@ -105,6 +106,7 @@ def main(names):
         "sedov12q_dbl": lambda: full("sedov12q_dbl", "sedovq_dbl", sd12(), 1),
         "kh24mfm_dbl": lambda: full("kh24mfm_dbl", "khmfm_dbl", kh24(), 5),
         "kh24fix_dbl": lambda: full("kh24fix_dbl", "khfix_dbl", kh24(), 5),
+        "kh24nolim_dbl": lambda: full("kh24nolim_dbl", "khnolim_dbl", kh24(), 5),
     }
     for name in names or list(makers):
         makers[name]()

@@ -22,6 +22,7 @@ CASES = {
     "kh24q_dbl": dict(kind="kh", pairwise_limiter=True, first_order_quad_point=False),
     "kh24mfm_dbl": dict(kind="kh", meshless_finite_mass=True),
     "kh24fix_dbl": dict(kind="kh", move_particles=False),
+    "kh24nolim_dbl": dict(kind="kh", slope_limiting=False),
 }
 
 
