@@ -107,6 +107,7 @@ KHNOLIM=$(params khnolim 2 1 .3 4. 0 1 0 1 0)
 build kh_dbl "$KH" dbl
 build kh_int "$KH" int
 build khpw_dbl "$KHPW" dbl
+build khpw_int "$KHPW" int
 build sedov_dbl "$SED" dbl
 build sedov_int "$SED" int
 build sedovnopw_dbl "$SEDNP" dbl

@@ -25,6 +25,8 @@ Variants (abs binding, see oracle/build_ref.sh):
   kh24mfm_dbl   kh24_dbl with MESHLESS_FINITE_MASS 1
   kh24fix_dbl   kh24_dbl with MOVE_PARTICLES 0
   kh24nolim_dbl kh24_dbl with SLOPE_LIMITING 0
+  kh24pw_int    kh24pw_dbl with the int abs(int) binding (pairwise limiter,
+                Particles.cpp:1748-1759, and slope limiter)
 """
 import hashlib
 import os
@@ -107,6 +109,7 @@ def main(names):
         "kh24mfm_dbl": lambda: full("kh24mfm_dbl", "khmfm_dbl", kh24(), 5),
         "kh24fix_dbl": lambda: full("kh24fix_dbl", "khfix_dbl", kh24(), 5),
         "kh24nolim_dbl": lambda: full("kh24nolim_dbl", "khnolim_dbl", kh24(), 5),
+        "kh24pw_int": lambda: full("kh24pw_int", "khpw_int", kh24(), 5),
     }
     for name in names or list(makers):
         makers[name]()

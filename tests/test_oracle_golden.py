@@ -23,6 +23,7 @@ CASES = {
     "kh24mfm_dbl": dict(kind="kh", meshless_finite_mass=True),
     "kh24fix_dbl": dict(kind="kh", move_particles=False),
     "kh24nolim_dbl": dict(kind="kh", slope_limiting=False),
+    "kh24pw_int": dict(kind="kh", pairwise_limiter=True, int_abs=True),
 }
 
 
