@@ -58,9 +58,8 @@ FACE_ALG_FLOPS = {3: 746.0, 2: 339.8}
 # What k_faces (both passes, gamma = 5/3 path) executes per face, from ncu
 # --set full captures: FP64 operations (2 x DFMA + DADD + DMUL thread
 # instructions / faces) and DRAM bytes (read + write).  3D: the 64^3 periodic
-# Sedov step (profiles/sedov64_step_kernels.md); 2D: 32 members of the
-# Kelvin-Helmholtz ensemble with the second Newton pass
-# (profiles/kh_ensemble32_step_kernels.md).
+# Sedov step; 2D: 32 members of the Kelvin-Helmholtz ensemble with the second
+# Newton pass.
 FACE_EXEC_FP64_FLOPS = {3: 541.0, 2: 391.0}
 FACE_DRAM_BYTES = {3: 298.0, 2: 364.0}
 

@@ -293,9 +293,9 @@ int mlh_pstar_harvest(mlh_ctx *ctx, int stride, float *x, float *t, long long ca
 #define MLH_NOALLOC_MAX_PARTICLES ((1 << 29) - 1)
 
 /* Search grid of one step computed without allocating any memory: for
- * callers that cannot call cudaMalloc (code running during CUDA graph
- * capture, frameworks that own all device memory through their own pool, loops
- * that must not allocate after start-up).  No counterpart in the reference:
+ * callers that cannot call cudaMalloc (frameworks that own all device memory
+ * through their own pool, loops that must not allocate after start-up).  No
+ * counterpart in the reference:
  * it computes what Particles::getDomainLimits + Domain::createGrid compute at
  * the start of a non-periodic step (the box itself when `periodic`), as
  * mlh_step does, from caller-owned device arrays x, y (, z) of n particles.

@@ -492,6 +492,10 @@ static int grow_buffers(mlh_ctx *c, unsigned st) {
         if (int rc = alloc_neighbour_buffers(c)) return rc;
     }
     if (st & ST_CAPACITY) {
+        if (c->p.ncells_cap >= (1 << 30)) {
+            g_last_error = "the grid needs more than 2^31 - 1 cells of size kernelSize";
+            return MLH_ERR_CAPACITY;
+        }
         free_cell_buffers(c);
         c->p.ncells_cap = c->p.ncells_cap * 2;
         if (int rc = alloc_cell_buffers(c)) return rc;

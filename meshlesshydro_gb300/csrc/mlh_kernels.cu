@@ -222,14 +222,18 @@ __global__ void k_bounds_final(const double *__restrict__ x, const double *__res
             g.lo[a] = mn;
             g.hi[a] = hi;
         }
+        // the product saturates at ncells_cap + 1 (each factor is below 2^31,
+        // so the product of the saturated value and one factor fits in 64 bits)
         long long total = 1;
         for (int a = 0; a < D; ++a) {
             double c = floor((g.hi[a] - g.lo[a]) / mb.h);
             int ci = (c >= 1. && c < 2147483647.) ? (int)c : 1;
             if (!(c >= 1.)) flag(status, ST_GRID);
+            if (c >= 2147483647.) { flag(status, ST_CAPACITY); ci = 1; }
             if (p.periodic && ci < 3) flag(status, ST_GRID);
             g.cells[a] = ci;
             total *= ci;
+            if (total > p.ncells_cap) total = (long long)p.ncells_cap + 1;
         }
         for (int a = 0; a < D; ++a) g.cs[a] = (g.hi[a] - g.lo[a]) / (double)g.cells[a];
         for (int a = 0; a < 3; ++a) {

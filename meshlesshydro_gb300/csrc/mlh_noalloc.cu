@@ -1,12 +1,12 @@
 // Allocation-free variant of the grid-bounds reduction.
 //
-// Some callers cannot call cudaMalloc: code running while a CUDA graph is being
-// captured, a host framework that owns all device memory through its own pool
-// and forbids raw allocations, or a real-time loop that must not allocate after
-// start-up.  For them mlh_grid_bounds_noalloc computes the search grid of the
-// reference's non-periodic step (Particles::getDomainLimits with its quirks +
-// Domain::createGrid) from caller-owned device arrays, with its scratch in the
-// file-scope device array below instead of memory from cudaMalloc.
+// Some callers cannot call cudaMalloc: a host framework that owns all device
+// memory through its own pool and forbids raw allocations, or a real-time loop
+// that must not allocate after start-up.  For them mlh_grid_bounds_noalloc
+// computes the search grid of the reference's non-periodic step
+// (Particles::getDomainLimits with its quirks + Domain::createGrid) from
+// caller-owned device arrays, with its scratch in the file-scope device array
+// below instead of memory from cudaMalloc.
 #include "../../include/mlh.h"
 #include "mlh_kernels.h"
 
@@ -91,6 +91,13 @@ extern "C" int mlh_grid_bounds_noalloc(int dim, int periodic, int n, const doubl
     if (!x || !y || (dim == 3 && !z) || !grid_out) { g_error = "null device pointer"; return MLH_ERR_INVALID; }
     if (!(kernel_size > 0.) || !std::isfinite(kernel_size)) { g_error = "kernel_size must be > 0"; return MLH_ERR_INVALID; }
     if (periodic && (!box_lo || !box_hi)) { g_error = "periodic runs need box_lo and box_hi"; return MLH_ERR_INVALID; }
+    // an error left pending by the caller's earlier work is reported, not
+    // consumed: cudaPeekAtLastError leaves it for the caller to read
+    cudaError_t pending = cudaPeekAtLastError();
+    if (pending != cudaSuccess) {
+        g_error = std::string("a CUDA error from earlier work is pending: ") + cudaGetErrorString(pending);
+        return MLH_ERR_CUDA;
+    }
     void *base = nullptr;
     if (int rc = scratch_address(&base)) return rc;
     cudaStream_t s = (cudaStream_t)stream;
@@ -124,14 +131,23 @@ extern "C" int mlh_grid_bounds_noalloc(int dim, int periodic, int n, const doubl
     k_set_member<<<1, 1, 0, s>>>(mb, member);
     launch_grid_bounds(x, y, dim == 3 ? z : x, p, member, 1, BOUNDS_BLOCKS, partials, grid, cellTotal, status, s);
     k_grid_to_doubles<<<1, 1, 0, s>>>(grid, dim, grid_out);
+    // launch errors of the kernels above (none was pending on entry)
+    e = cudaGetLastError();
     unsigned st = 0;
-    e = cudaMemcpyAsync(&st, status, sizeof(unsigned), cudaMemcpyDeviceToHost, s);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(&st, status, sizeof(unsigned), cudaMemcpyDeviceToHost, s);
     if (e == cudaSuccess) e = cudaStreamSynchronize(s);
-    if (e == cudaSuccess) e = cudaGetLastError();
     if (e != cudaSuccess) { g_error = std::string("CUDA: ") + cudaGetErrorString(e); return MLH_ERR_CUDA; }
     int rc = 0;
-    if (st & ST_GRID) rc |= MLH_ERR_GRID;
-    if (st & ST_CAPACITY) rc |= MLH_ERR_CAPACITY;
-    if (rc) g_error = "degenerate grid (fewer than 1 cell per axis, or fewer than 3 on a periodic axis)";
+    std::string msg;
+    if (st & ST_GRID) {
+        rc |= MLH_ERR_GRID;
+        msg = "degenerate grid (fewer than 1 cell per axis, or fewer than 3 on a periodic axis)";
+    }
+    if (st & ST_CAPACITY) {
+        rc |= MLH_ERR_CAPACITY;
+        if (!msg.empty()) msg += "; ";
+        msg += "too many cells (the grid needs more than 2^31 - 1 cells of size kernel_size)";
+    }
+    if (rc) g_error = msg;
     return rc;
 }

@@ -28,6 +28,9 @@
 set -euo pipefail
 HERE="$(cd "$(dirname "$0")" && pwd)"
 REF="${MLH_REFERENCE:-/root/reference}"
+# `build_ref.sh --print-root`: the reference tree this recipe reads (the one
+# place that names its default location)
+if [ "${1:-}" = "--print-root" ]; then echo "$REF"; exit 0; fi
 SRC="$REF/demonstrator/src"
 INC="$REF/demonstrator/include"
 OUT="$HERE/_ref"

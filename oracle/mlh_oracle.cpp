@@ -26,6 +26,12 @@
 //    restatement uses z_j - z_i.
 //  * Errors set bits in the returned status instead of calling exit().
 //
+// Threads: built with OpenMP, the per-particle loops run on several threads
+// (orc_set_threads; one by default).  Every particle's sums run in the same
+// order on one thread whatever the thread count, the minimum of the time step
+// is taken after the loop, and the faces are solved before their mirrored
+// copies are made, so the results do not depend on the number of threads.
+//
 // Addition without a reference counterpart (the reference uses one global
 // kernelSize): per-particle smoothing lengths (hsolve) and the step mode that
 // uses them (adaptive_h).  Its arithmetic is fixed operation by operation
@@ -40,6 +46,7 @@
 #include "riemann_exact.hpp"
 
 #include <algorithm>
+#include <atomic>
 #include <cfloat>
 #include <climits>
 #include <cmath>
@@ -49,7 +56,14 @@
 #include <string>
 #include <vector>
 
+#ifdef _OPENMP
+#include <omp.h>
+#endif
+
 namespace {
+
+// threads of the per-particle loops (orc_set_threads)
+int g_threads = 1;
 
 // Arithmetic type of the step: double, or (operation-counting build,
 // -DORC_COUNT_FLOPS) a double that counts the operations done on it.
@@ -119,7 +133,8 @@ struct Sim {
     real cellSize[3];
     std::vector<int> cellOf;
     std::vector<std::vector<int>> grid;
-    unsigned status = 0;
+    // error bits; OR-ed from the threads of the per-particle loops
+    std::atomic<unsigned> status{0};
     long riemannSolves = 0, newtonTotal = 0;
 
     // --- Kernel::cubicSpline, demonstrator/src/Particles.cpp:7-24, for a
@@ -217,6 +232,7 @@ struct Sim {
         noi.assign(N, 0);
         noiImg.assign(N, 0);
         std::vector<std::vector<uint32_t>> lists(N);
+#pragma omp parallel for schedule(dynamic, 256) num_threads(g_threads)
         for (int i = 0; i < N; ++i) {
             int ic = cellOf[i];
             int ix = ic % cells[0];
@@ -266,14 +282,16 @@ struct Sim {
             noiImg[i] = (int)img.size();
             lists[i] = own;
             lists[i].insert(lists[i].end(), img.begin(), img.end());
-            off[i + 1] = off[i] + (int)lists[i].size();
         }
+        for (int i = 0; i < N; ++i) off[i + 1] = off[i] + (int)lists[i].size();
         nb.resize(off[N]);
+#pragma omp parallel for schedule(static) num_threads(g_threads)
         for (int i = 0; i < N; ++i) std::copy(lists[i].begin(), lists[i].end(), nb.begin() + off[i]);
         // reverse slots: position of i in the list of its neighbour (for
         // images: the first image entry of the parent whose parent is i,
         // Particles.cpp:2514-2516)
         rev.assign(off[N], -1);
+#pragma omp parallel for schedule(dynamic, 256) num_threads(g_threads)
         for (int i = 0; i < N; ++i)
             for (int s = off[i]; s < off[i + 1]; ++s) {
                 int j = (int)(nb[s] & IDX_MASK);
@@ -297,6 +315,7 @@ struct Sim {
     // image part 2262-2290
     void density() {
         omega.assign(N, 0.);
+#pragma omp parallel for schedule(static) num_threads(g_threads)
         for (int i = 0; i < N; ++i) {
             real omg = 0.;
             for (int s = off[i]; s < off[i] + noi[i]; ++s) omg += kernelH(dist(i, s), hp[i]);
@@ -304,17 +323,20 @@ struct Sim {
             rho[i] = m[i] * omega[i];
             if (rho[i] <= 0.) status |= ST_NEG_DENSITY;
         }
-        if (c.periodic)
+        if (c.periodic) {
+#pragma omp parallel for schedule(static) num_threads(g_threads)
             for (int i = 0; i < N; ++i) {
                 real omg = omega[i];
                 for (int s = off[i] + noi[i]; s < off[i + 1]; ++s) omg += kernelH(dist(i, s), hp[i]);
                 omega[i] = omg;
                 rho[i] = m[i] * omega[i];
             }
+        }
     }
 
     // --- Particles::compPressure, Particles.cpp:1272-1288
     void pressure() {
+#pragma omp parallel for schedule(static) num_threads(g_threads)
         for (int i = 0; i < N; ++i) {
             P[i] = (c.gamma - 1.) * rho[i] * u[i];
             if (P[i] <= 0.) status |= ST_NEG_PRESSURE;
@@ -331,6 +353,8 @@ struct Sim {
     // neighbours only, v_sig starting at numeric_limits<double>::min())
     real globalTimestep() {
         real dt_ = std::numeric_limits<double>::max();
+        std::vector<real> dtp(N);
+#pragma omp parallel for schedule(static) num_threads(g_threads)
         for (int i = 0; i < N; ++i) {
             real vSig = std::numeric_limits<double>::min();
             real ci = sqrt(c.gamma * P[i] / rho[i]);
@@ -344,9 +368,9 @@ struct Sim {
                 real vSig_i = ci + cj - vijxij;
                 vSig = vSig_i > vSig ? vSig_i : vSig;
             }
-            real dti = c.cfl * hp[i] / vSig;
-            dt_ = dti < dt_ ? dti : dt_;
+            dtp[i] = c.cfl * hp[i] / vSig;
         }
+        for (int i = 0; i < N; ++i) dt_ = dtp[i] < dt_ ? dtp[i] : dt_;
         return dt_;
     }
 
@@ -380,6 +404,7 @@ struct Sim {
     void psijTilde() {
         B.assign((size_t)N * D * D, 0.);
         psi.assign((size_t)off[N] * 3, 0.);
+#pragma omp parallel for schedule(static) num_threads(g_threads)
         for (int i = 0; i < N; ++i) {
             real Bi[9] = {0};
             real xi[3];
@@ -414,6 +439,7 @@ struct Sim {
         for (int f = 0; f < nfields(); ++f) {
             const std::vector<real> &fv = field(f);
             G[f].assign((size_t)N * 3, 0.);
+#pragma omp parallel for schedule(static) num_threads(g_threads)
             for (int i = 0; i < N; ++i)
                 for (int s = off[i]; s < off[i + 1]; ++s) {
                     int j = (int)(nb[s] & IDX_MASK);
@@ -427,6 +453,7 @@ struct Sim {
     void slopeLimiter() {
         for (int f = 0; f < nfields(); ++f) {
             const std::vector<real> &fv = field(f);
+#pragma omp parallel for schedule(static) num_threads(g_threads)
             for (int i = 0; i < N; ++i) {
                 real psiMaxNgb = std::numeric_limits<double>::min();
                 real psiMinNgb = std::numeric_limits<double>::max();
@@ -462,6 +489,7 @@ struct Sim {
     // --- Particles::compEffectiveFace, Particles.cpp:1290-1311 / 2504-2531
     void effectiveFace() {
         Aij.assign((size_t)off[N] * 3, 0.);
+#pragma omp parallel for schedule(static) num_threads(g_threads)
         for (int i = 0; i < N; ++i)
             for (int s = off[i]; s < off[i + 1]; ++s) {
                 int j = (int)(nb[s] & IDX_MASK);
@@ -504,6 +532,7 @@ struct Sim {
         vFrame.assign((size_t)off[N] * 3, 0.);
         const std::vector<real> &rG = G[0], &vxG = G[1], &vyG = G[2], &vzG = G[3], &PG = G[D + 1];
         const real gamma = c.gamma;
+#pragma omp parallel for schedule(static) num_threads(g_threads)
         for (int i = 0; i < N; ++i)
             for (int s = off[i]; s < off[i + 1]; ++s) {
                 int j = (int)(nb[s] & IDX_MASK);
@@ -617,7 +646,8 @@ struct Sim {
     // demonstrator/src/Riemann.cpp:7-229.  wi = state of the list owner i
     // (the reference's WijR, which the constructor receives as WL), wj = state
     // of neighbour j; i is the LEFT state of the 1D problem.
-    void riemann(real *wi, real *wj, const real *vfr, const real *A, real *Fo, const orc::ExactRiemannT<real> &rs) {
+    // returns the Newton iterations (-1: no convergence)
+    int riemann(real *wi, real *wj, const real *vfr, const real *A, real *Fo, const orc::ExactRiemannT<real> &rs) {
         const real unitX[3] = {1., 0., 0.};
         real AN = sqrt(dot(A, A));
         real hatA[3];
@@ -643,9 +673,7 @@ struct Sim {
         real rhoSol, vSol[3] = {0., 0., 0.}, PSol;
         int iters = 0;
         int flag = rs.solve(wi[0], wi[2], wi[1], wj[0], wj[2], wj[1], rhoSol, vSol[0], PSol, &iters);
-        ++riemannSolves;
-        if (iters < 0) status |= ST_NEWTON; else newtonTotal += iters;
-        newtonIters.push_back(iters);
+        if (iters < 0) status |= ST_NEWTON;
         if (flag == 1) { for (int a = 1; a < D; ++a) vSol[a] = wj[2 + a]; }
         else if (flag == -1) { for (int a = 1; a < D; ++a) vSol[a] = wi[2 + a]; }
         else status |= ST_VACUUM;
@@ -679,36 +707,56 @@ struct Sim {
                   + A[1] * (vSol[1] * (PSol / (gamma - 1.) + rhoSol * .5 * dot(vLab, vLab)) + PSol * vLab[1])
                   + A[2] * (vSol[2] * (PSol / (gamma - 1.) + rhoSol * .5 * dot(vLab, vLab)) + PSol * vLab[2]);
         }
+        return iters;
     }
 
     // --- Particles::solveRiemannProblems, Particles.cpp:1787-1911: the face is
     // solved from the side of the lower (parent) index; the other side copies
     // -F (ENFORCE_FLUX_SYM).
+    // (Faces first, then the copies, so that the faces can be solved in any
+    // order; the iteration list keeps the reference's face order.)
     void solveRiemannProblems() {
         const int NV = D + 2;
         F.assign((size_t)off[N] * NV, 0.);
-        newtonIters.clear();
+        std::vector<int> slotIters(off[N], 0);
         orc::ExactRiemannT<real> rs(c.gamma, c.riemann_tol, c.riemann_max_iter);
+#pragma omp parallel for schedule(dynamic, 256) num_threads(g_threads)
         for (int i = 0; i < N; ++i)
             for (int s = off[i]; s < off[i + 1]; ++s) {
                 int j = (int)(nb[s] & IDX_MASK);
                 real *R = &WR[(size_t)s * NV], *L = &WL[(size_t)s * NV];
                 if (R[1] < 0. || L[1] < 0.) status |= ST_NEG_PRESSURE;
+                if (j >= i) {
+                    real wi[5], wj[5];
+                    for (int d = 0; d < NV; ++d) { wi[d] = R[d]; wj[d] = L[d]; }
+                    slotIters[s] = riemann(wi, wj, &vFrame[(size_t)s * 3], &Aij[(size_t)s * 3], &F[(size_t)s * NV], rs);
+                }
+            }
+#pragma omp parallel for schedule(static) num_threads(g_threads)
+        for (int i = 0; i < N; ++i)
+            for (int s = off[i]; s < off[i + 1]; ++s) {
+                int j = (int)(nb[s] & IDX_MASK);
                 if (j < i) {
                     int t = rev[s];
                     for (int d = 0; d < NV; ++d) F[(size_t)s * NV + d] = -F[(size_t)t * NV + d];
-                } else {
-                    real wi[5], wj[5];
-                    for (int d = 0; d < NV; ++d) { wi[d] = R[d]; wj[d] = L[d]; }
-                    riemann(wi, wj, &vFrame[(size_t)s * 3], &Aij[(size_t)s * 3], &F[(size_t)s * NV], rs);
                 }
             }
+        newtonIters.clear();
+        for (int i = 0; i < N; ++i)
+            for (int s = off[i]; s < off[i + 1]; ++s)
+                if ((int)(nb[s] & IDX_MASK) >= i) {
+                    const int it = slotIters[s];
+                    ++riemannSolves;
+                    if (it >= 0) newtonTotal += it;
+                    newtonIters.push_back(it);
+                }
     }
 
     // --- Particles::collectFluxes, Particles.cpp:1913-2011
     void collectFluxes() {
         const int NV = D + 2;
         mF.assign(N, 0.); eF.assign(N, 0.); vF.assign((size_t)N * 3, 0.);
+#pragma omp parallel for schedule(static) num_threads(g_threads)
         for (int i = 0; i < N; ++i)
             for (int s = off[i]; s < off[i + 1]; ++s) {
                 const real *f = &F[(size_t)s * NV];
@@ -722,6 +770,7 @@ struct Sim {
 
     // --- Particles::updateStateAndPosition, Particles.cpp:2013-2110
     void update() {
+#pragma omp parallel for schedule(static) num_threads(g_threads)
         for (int i = 0; i < N; ++i) {
             real vxi = V[0][i], vyi = V[1][i], vzi = D == 3 ? V[2][i] : 0.;
             real Q[4];
@@ -785,11 +834,10 @@ struct Sim {
         const real hSqr = h * h;
         hp.resize(N, h);
         nEff.assign(N, 0.);
-        hClamped = 0;
-        hIters = 0;
-        std::vector<real> r;
+        long clampedSum = 0, itersSum = 0;
+#pragma omp parallel for schedule(dynamic, 64) num_threads(g_threads) reduction(+ : clampedSum, itersSum)
         for (int i = 0; i < N; ++i) {
-            r.clear();
+            std::vector<real> r;
             int ic = cellOf[i];
             int ix = ic % cells[0];
             int iy = (ic / cells[0]) % cells[1];
@@ -844,10 +892,10 @@ struct Sim {
                 }
                 S = sf[0];
                 const real G = sg[0];
-                ++hIters;
+                ++itersSum;
                 const real F = S - St;
                 if (fabs(F) <= tolS) break;
-                if (F < 0. && x >= h) { ++hClamped; break; }
+                if (F < 0. && x >= h) { ++clampedSum; break; }
                 if (it + 1 >= 50) break;
                 if (F > 0.) { hi_ = x; upper = true; }
                 else lo_ = x;
@@ -859,6 +907,8 @@ struct Sim {
             hp[i] = (double)x;
             nEff[i] = KD * (S + 1.);
         }
+        hClamped = clampedSum;
+        hIters = itersSum;
     }
 
     // grid of the current positions: the periodic box, or the bounding box
@@ -1050,9 +1100,9 @@ int riemannFaces(int n, const double *Wi, const double *Wj, const double *vFrame
         for (int k = 0; k < NV; ++k) { wi[k] = Wi[(size_t)f * NV + k]; wj[k] = Wj[(size_t)f * NV + k]; }
         for (int k = 0; k < D; ++k) { vf[k] = vFrame[(size_t)f * D + k]; A[k] = Aij[(size_t)f * D + k]; }
         if (wi[1] < 0. || wj[1] < 0.) s.status |= ST_NEG_PRESSURE;
-        s.riemann(wi, wj, vf, A, Fo, rs);
+        const int it = s.riemann(wi, wj, vf, A, Fo, rs);
         for (int k = 0; k < NV; ++k) F[(size_t)f * NV + k] = (double)Fo[k];
-        if (iters) iters[f] = s.newtonIters.back();
+        if (iters) iters[f] = it;
     }
     return (int)s.status;
 }
@@ -1116,6 +1166,17 @@ int orc_riemann_fluxes(int dim, int n, const double *Wi, const double *Wj, const
                        double gamma, int mfm, double *F, int *iters) {
     if (dim == 2) return riemannFaces<2>(n, Wi, Wj, vFrame, Aij, gamma, mfm, F, iters);
     return riemannFaces<3>(n, Wi, Wj, vFrame, Aij, gamma, mfm, F, iters);
+}
+
+int orc_set_threads(int n) {
+#ifdef _OPENMP
+    if (n < 1) n = omp_get_num_procs();
+    g_threads = n;
+    return n;
+#else
+    (void)n;
+    return 1;
+#endif
 }
 
 int orc_flop_counts(void *ctx, unsigned long long *out) {

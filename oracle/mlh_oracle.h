@@ -85,6 +85,11 @@ enum {
     ORC_NSTAGES
 };
 
+/* Threads of the per-particle loops (results do not depend on them); n < 1:
+ * one per processor.  Returns the count in effect (1 in a build without
+ * OpenMP).  The default is 1: the serial restatement of the reference. */
+int orc_set_threads(int n);
+
 /* Operation-counting build only (liborc_count.so, -DORC_COUNT_FLOPS):
  * operation counts of each stage summed over the steps of this context,
  * out[6 * stage + k] for k = add, mul, div, sqrt, pow, fma.  Returns

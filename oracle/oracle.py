@@ -36,6 +36,14 @@ class OrcConfig(ctypes.Structure):
 INT_ARRAYS = {"noi", "noi_img", "off", "rev", "newton_iters", "nnl"}
 
 
+def reference_root() -> str:
+    """The reference tree that oracle/build_ref.sh reads (MLH_REFERENCE, or
+    the recipe's default); it exists only where the reference build runs."""
+    r = subprocess.run(["bash", os.path.join(HERE, "build_ref.sh"), "--print-root"], capture_output=True,
+                       text=True)
+    return r.stdout.strip()
+
+
 def build(counting: bool = False):
     subprocess.run(["make", "-s", "-C", HERE] + (["count"] if counting else []), check=True)
 
@@ -68,10 +76,18 @@ def lib(counting: bool = False):
         L.orc_riemann_fluxes.restype = ctypes.c_int
         L.orc_smoothing_lengths.restype = ctypes.c_long
         L.orc_smoothing_lengths.argtypes = [ctypes.c_void_p, ctypes.c_double, dp, dp]
+        L.orc_set_threads.restype = ctypes.c_int
+        L.orc_set_threads.argtypes = [ctypes.c_int]
         L.orc_flop_counts.restype = ctypes.c_int
         L.orc_flop_counts.argtypes = [ctypes.c_void_p, ctypes.POINTER(ctypes.c_ulonglong)]
         _libs[counting] = L
     return _libs[counting]
+
+
+def set_threads(n: int) -> int:
+    """Threads of the oracle's per-particle loops (n < 1: one per processor);
+    the results do not depend on them.  Returns the count in effect."""
+    return int(lib().orc_set_threads(int(n)))
 
 
 def riemann_batch(rhoL, uL, pL, rhoR, uR, pR, gamma=5.0 / 3.0, guess=None):

@@ -9,7 +9,7 @@ import pytest
 import h5spec
 from meshlesshydro_gb300 import build, ic, io
 from meshlesshydro_gb300.config import MFVConfig
-from helpers import assert_close
+from helpers import assert_close, assert_normwise
 
 pytestmark = pytest.mark.gpu
 
@@ -76,10 +76,11 @@ def test_driver_fixed_dt_matches_oracle(tmp_path, oracle_mod):
             np.testing.assert_array_equal(s0["noi"], o.get("noi"))
     last = snaps["000010.h5"]
     st = o.state()
-    assert_close(last["x"][:, 0], st["x"], what="x")
-    assert_close(last["v"][:, 1], st["vy"], what="vy")
-    assert_close(last["m"], st["m"], what="m")
-    assert_close(last["u"], st["u"], what="u")
+    # the state after 10 steps (differences compound over steps)
+    assert_normwise(last["x"][:, 0], st["x"], 1e-12, what="x")
+    assert_normwise(last["v"][:, 1], st["vy"], 1e-12, what="vy")
+    assert_normwise(last["m"], st["m"], 1e-12, what="m")
+    assert_normwise(last["u"], st["u"], 1e-12, what="u")
     assert abs(last["totalMass"][0] - np.sum(p.m)) <= 1e-13 * np.sum(p.m)
 
 

@@ -10,7 +10,7 @@ import pytest
 
 from meshlesshydro_gb300 import ic
 from meshlesshydro_gb300.config import MFVConfig
-from helpers import assert_close
+from helpers import assert_close, assert_normwise
 
 pytestmark = pytest.mark.gpu
 
@@ -43,7 +43,7 @@ def test_ensemble_members_match_single_runs(oracle_mod):
         assert_close([dt_g[k]], o.get("dt"), what=f"member {k} dt")
         assert_close([t_g[k]], [t], what=f"member {k} time")
         for key, v in o.state().items():
-            assert_close(state[key][first:first + m.n], v, rtol=1e-11, what=f"member {k} {key}")
+            assert_normwise(state[key][first:first + m.n], v, 1e-11, what=f"member {k} {key}")
         first += m.n
 
 
@@ -96,7 +96,7 @@ def test_graph_mode_single_sedov(oracle_mod):
     o.step(); o.step()
     gs = g.get_state()
     for key, v in o.state().items():
-        assert_close(gs[key], v, rtol=1e-11, what=key)
+        assert_normwise(gs[key], v, 1e-11, what=key)
 
 
 def test_autotune_keeps_results_bitwise():

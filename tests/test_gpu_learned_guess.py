@@ -14,7 +14,7 @@ import pytest
 
 from meshlesshydro_gb300 import ic
 from meshlesshydro_gb300.config import MFVConfig
-from helpers import assert_close
+from helpers import assert_normwise
 
 pytestmark = pytest.mark.gpu
 
@@ -97,7 +97,7 @@ def test_learned_guess_matches_oracle(trained, oracle_mod, case):
     assert st.newton_iterations <= 2 * plain.newton_iterations
     gs = s.get_state()
     for key, v in o.state().items():
-        assert_close(gs[key], v, rtol=LEARNED_RTOL, what=key)
+        assert_normwise(gs[key], v, LEARNED_RTOL, what=key)
 
 
 @pytest.mark.parametrize("case", [0, 1], ids=["kh40", "sedov12"])
@@ -139,7 +139,7 @@ def test_bad_guess_falls_back(oracle_mod):
     assert st.status == 0
     gs = s.get_state()
     for key, v in o.state().items():
-        assert_close(gs[key], v, rtol=LEARNED_RTOL, what=key)
+        assert_normwise(gs[key], v, LEARNED_RTOL, what=key)
 
 
 def test_learned_then_plain_graph_mode(trained):

@@ -2,7 +2,8 @@
 CPU oracle on identical seeded inputs.
 
 Bar: neighbour lists bit-exact (indices, order, image flags); every per-step
-field within FIELD_RTOL = 1e-12 normwise relative error (max |a-b| / max |b|).
+field within the per-element gate of helpers.assert_close (1e-12 of each
+entry, with a floor of 1e-3 of the field's largest magnitude).
 The oracle itself is pinned to the reference's own code by
 tests/test_oracle_golden.py.
 """
@@ -11,7 +12,7 @@ import pytest
 
 from meshlesshydro_gb300 import ic
 from meshlesshydro_gb300.config import MFVConfig
-from helpers import FIELD_RTOL, assert_close, normwise
+from helpers import assert_normwise, compare_step
 
 pytestmark = pytest.mark.gpu
 
@@ -53,26 +54,7 @@ def test_one_step_stagewise(oracle_mod, name):
     g = _sim(cfg, p)
     stats = g.step(1)
     assert stats.steps == 1
-    # neighbour search: bit-exact
-    for k in ("off", "noi", "noi_img"):
-        np.testing.assert_array_equal(g.get(k), o.get(k), err_msg=k)
-    np.testing.assert_array_equal(g.get("nnl"), o.get("nnl"))
-    np.testing.assert_array_equal(g.get("grid"), o.get("grid"))
-    for k in ("omega", "rho", "P", "dt"):
-        assert_close(g.get(k), o.get(k), what=k)
-    fields = ["rho", "vx", "vy"] + (["vz"] if cfg.dim == 3 else []) + ["P"]
-    for f in fields:
-        assert_close(g.get("gradraw_" + f), o.get("gradraw_" + f), what="gradraw_" + f)
-        assert_close(g.get("grad_" + f), o.get("grad_" + f), what="grad_" + f)
-    assert_close(g.get("B"), o.get("B"), what="B")
-    # per-interaction fluxes with the reference's sign convention
-    assert_close(g.get("F"), o.get("F"), what="F")
-    assert_close(g.get("mF"), o.get("mF"), what="mF")
-    assert_close(g.get("eF"), o.get("eF"), what="eF")
-    assert_close(g.get("vF").reshape(-1, 3)[:, :cfg.dim], o.get("vF").reshape(-1, 3)[:, :cfg.dim], what="vF")
-    gs = g.get_state()
-    for k, v in o.state().items():
-        assert_close(gs[k], v, what="state " + k)
+    compare_step(g, o, cfg.dim, slots=True, what=name + ": ")
     assert stats.faces == int(o.get("stats")[0])
 
 
@@ -170,7 +152,7 @@ def test_neighbour_overflow_retry(oracle_mod):
     np.testing.assert_array_equal(g.get("nnl"), o.get("nnl"))
     gs = g.get_state()
     for k, v in o.state().items():
-        assert_close(gs[k], v, rtol=1e-11, what=k)
+        assert_normwise(gs[k], v, 1e-11, what=k)
 
 
 def test_negative_pressure_reported():

@@ -1,0 +1,151 @@
+"""GPU parity at the sizes of the measured workloads: the CUDA MFV step
+(libmlh.so, through the C ABI) against the CPU oracle on identical seeded
+inputs.
+
+* Sedov 64^3 (262,144 particles), periodic and in the reference's own
+  non-periodic mode (testcases/sedov/parameter.h:12): one step stage by stage,
+  then 100 steps in which the GPU starts every step from the oracle's state
+  (per-step gate of helpers.assert_close, neighbour lists bit-exact every
+  step), and a free-running 100-step run whose density is compared by L1
+  (<= 1e-8 relative).
+* Sedov 128^3 (2,097,152 particles, the bench workload): one step, lists
+  bit-exact, fields per element.
+* Kelvin-Helmholtz 100x100: 100 steps per-step gated, and every state field
+  of a free-running 100-step run by L1.
+* The meshless finite mass scheme (MESHLESS_FINITE_MASS 1) and fixed
+  particles (MOVE_PARTICLES 0) over five whole steps.
+
+The oracle runs its per-particle loops on every host core (its results do not
+depend on the thread count: tests/test_oracle_threads.py).
+"""
+import numpy as np
+import pytest
+
+from meshlesshydro_gb300 import ic
+from meshlesshydro_gb300.config import MFVConfig
+from helpers import assert_close, compare_step, l1_rel, pset_from_state
+
+pytestmark = pytest.mark.gpu
+
+L1_RTOL = 1e-8
+
+
+@pytest.fixture(scope="module")
+def orc(oracle_mod):
+    oracle_mod.set_threads(0)
+    yield oracle_mod
+    oracle_mod.set_threads(1)
+
+
+def _sim(cfg, p):
+    from meshlesshydro_gb300 import build, runtime
+    build.build()
+    return runtime.Simulation(cfg, p)
+
+
+def _sedov64(periodic):
+    p = ic.sedov(n_side=64, seed=2)
+    return p, MFVConfig.sedov(p, periodic=periodic)
+
+
+@pytest.mark.parametrize("periodic", [True, False], ids=["periodic", "nonperiodic"])
+def test_sedov64_one_step_stagewise(orc, periodic):
+    p, cfg = _sedov64(periodic)
+    o = orc.Oracle(cfg, p)
+    assert o.step() == 0
+    g = _sim(cfg, p)
+    st = g.step(1)
+    compare_step(g, o, 3, slots=True, what=f"sedov64 periodic={periodic}: ")
+    assert st.faces == int(o.get("stats")[0])
+    g.close()
+    o.close()
+
+
+def _per_step_and_free_run(orc, p, cfg, nsteps, what, free_fields=("rho",)):
+    """nsteps oracle steps; before each, the GPU takes the oracle's state and
+    runs one step, gated per element (lists bit-exact).  Then a free-running
+    GPU run of nsteps from the initial state, compared with the oracle's
+    states by L1.  Returns the largest per-step error seen per field."""
+    o = orc.Oracle(cfg, p)
+    g = _sim(cfg, p)
+    for k in range(nsteps):
+        g.set_state(pset_from_state(p, o.state()))
+        assert o.step() == 0, f"{what}: oracle status at step {k}"
+        g.step(1)
+        np.testing.assert_array_equal(g.get("nnl"), o.get("nnl"), err_msg=f"{what}: nnl at step {k}")
+        assert_close(g.get("rho"), o.get("rho"), what=f"{what} step {k}: rho")
+        assert_close(g.get("dt"), o.get("dt"), what=f"{what} step {k}: dt")
+        gs = g.get_state()
+        for f, v in o.state().items():
+            assert_close(gs[f], v, what=f"{what} step {k}: {f}")
+    # free run: the oracle's final state after nsteps, and its density at the
+    # next step's density evaluation; the GPU the same from the initial state
+    ost = o.state()
+    assert o.step() == 0
+    orho = o.get("rho")
+    g.set_state(p)
+    g.step(nsteps)
+    gst = g.get_state()
+    g.step(1)
+    grho = g.get("rho")
+    out = {"rho": l1_rel(grho, orho)}
+    for f in free_fields:
+        if f != "rho":
+            out[f] = l1_rel(gst[f], ost[f])
+    g.close()
+    o.close()
+    return out
+
+
+@pytest.mark.parametrize("periodic", [True, False], ids=["periodic", "nonperiodic"])
+def test_sedov64_100_steps(orc, periodic):
+    p, cfg = _sedov64(periodic)
+    l1 = _per_step_and_free_run(orc, p, cfg, 100, f"sedov64 periodic={periodic}")
+    assert l1["rho"] <= L1_RTOL, f"density L1 after 100 steps {l1['rho']:.3e}"
+
+
+def test_sedov128_one_step(orc):
+    p = ic.sedov(n_side=128, seed=2)
+    cfg = MFVConfig.sedov(p, periodic=True)
+    o = orc.Oracle(cfg, p)
+    assert o.step() == 0
+    g = _sim(cfg, p)
+    st = g.step(1)
+    compare_step(g, o, 3, slots=False, what="sedov128: ")
+    assert st.faces == int(o.get("stats")[0])
+    g.close()
+    o.close()
+
+
+def test_kh100_100_steps_all_fields(orc):
+    p = ic.kelvin_helmholtz(n_side=100, seed=1)
+    cfg = MFVConfig.kelvin_helmholtz(p)
+    l1 = _per_step_and_free_run(orc, p, cfg, 100, "kh100", free_fields=("rho", "x", "y", "vx", "vy", "m", "u"))
+    for f, e in l1.items():
+        assert e <= L1_RTOL, f"{f}: L1 after 100 steps {e:.3e}"
+
+
+@pytest.mark.parametrize("mode", ["meshless_finite_mass", "fixed_particles"])
+def test_kh24_mfm_and_fixed_particles(orc, mode):
+    """MESHLESS_FINITE_MASS 1 (Particles.cpp:2041-2043, Riemann.cpp:171-175:
+    no mass flux, masses kept) and MOVE_PARTICLES 0 (Particles.cpp:1542-1565,
+    2077-2108: frame velocity 0, no drift), five whole steps: the first stage
+    by stage, every step per element from the oracle's state, then a free run."""
+    p = ic.kelvin_helmholtz(n_side=24, seed=3)
+    kw = {"meshless_finite_mass": True} if mode == "meshless_finite_mass" else {"move_particles": False}
+    cfg = MFVConfig.kelvin_helmholtz(p, **kw)
+    o = orc.Oracle(cfg, p)
+    assert o.step() == 0
+    g = _sim(cfg, p)
+    g.step(1)
+    compare_step(g, o, 2, slots=True, what=mode + ": ")
+    gs = g.get_state()
+    if mode == "meshless_finite_mass":
+        assert np.array_equal(gs["m"], p.m)
+    else:
+        assert np.array_equal(gs["x"], p.x) and np.array_equal(gs["y"], p.y)
+    g.close()
+    o.close()
+    l1 = _per_step_and_free_run(orc, p, cfg, 5, mode, free_fields=("rho", "x", "y", "vx", "vy", "m", "u"))
+    for f, e in l1.items():
+        assert e <= L1_RTOL, f"{mode} {f}: L1 after 5 steps {e:.3e}"

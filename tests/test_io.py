@@ -11,7 +11,7 @@ import pytest
 import h5spec
 from meshlesshydro_gb300 import build, ic, io
 
-REF = os.environ.get("MLH_REFERENCE", "/root/reference")
+REF = __import__("oracle").reference_root()
 
 
 @pytest.fixture(scope="module", autouse=True)

@@ -1,9 +1,8 @@
 """The allocation-free grid-bounds entry point against the step's own grid.
 
-mlh_grid_bounds_noalloc serves callers that cannot call cudaMalloc (code
-running during CUDA graph capture, frameworks that own all device memory,
-loops that must not allocate after start-up); its scratch is a static device
-array.  This file is collected last so that a failure here leaves every other
+mlh_grid_bounds_noalloc serves callers that cannot call cudaMalloc
+(frameworks that own all device memory through their own pool, loops that
+must not allocate after start-up); its scratch is a static device array.  This file is collected last so that a failure here leaves every other
 test already run.  Each call is compared with the grid that mlh_step computed
 from the same particle positions (exact equality, within FIELD_RTOL).
 """
@@ -78,3 +77,8 @@ def test_noalloc_periodic_2d_and_size_limit():
                                    0.1, out.data_ptr(), None)
     assert rc == MLH_ERR_CAPACITY
     assert b"MLH_NOALLOC_MAX_PARTICLES" in L.mlh_last_error()
+    # a grid of more cells than an int counts is rejected with its own message
+    q = ic.sedov(n_side=8, seed=2)
+    rc, _ = _call(L, torch, [q.x, q.y, q.z], 3, 1e-4)
+    assert rc & MLH_ERR_CAPACITY
+    assert b"too many cells" in L.mlh_last_error()
