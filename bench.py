@@ -8,11 +8,17 @@ full MFV step (binning, neighbour search, density, dt, gradients, limiter,
 faces, exact Riemann solves, flux gather, kick/drift) over all particles.
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl mlh|reference]
-                    [--workload sedov128|sedov64|kh100]
+                    [--workload sedov128|sedov64|kh100|kh_ens256|multi_blast64]
+                    [--no-learned] [--no-adaptive] [--no-ensemble] [--no-cpu-baseline]
 
-Prints one JSON line.  --impl reference times the CPU restatement of the
-reference's serial code (the oracle; the reference itself cannot run on the
-GPU host) on a bounded sample of the same workload.
+Prints one JSON line.  Beside the headline it reports, for the default
+workload: the learned star-pressure guess (trained on faces harvested from the
+64^3 Sedov and 100x100 Kelvin-Helmholtz runs, evaluated on the held-out 128^3
+workload and on a many-blast workload full of strong shocks), per-particle
+smoothing lengths, and the 256-member Kelvin-Helmholtz ensemble batched
+against its members run one after another.  --impl reference times the CPU
+restatement of the reference's serial code (the oracle; the reference itself
+cannot be built on the GPU host) on a bounded sample of the same workload.
 """
 from __future__ import annotations
 
@@ -36,39 +42,25 @@ WORKLOADS = {
     "kh100": dict(kind="kh", n_side=100),
     # 256 independent 2D KH runs, N log-uniform in [2500, 40000], one context
     "kh_ens256": dict(kind="ensemble", members=256),
+    # 64 blasts in the periodic 64^3 cube: strong shocks everywhere
+    "multi_blast64": dict(kind="multi_blast", n_side=64, n_blasts=64),
 }
 METRIC = "particle-updates/s per MFV step on 1 GB300"
 # kernels launched by one plain mlh_step iteration (csrc/mlh_kernels.cu,
-# launch_step; the ncu launch list of a step shows the same 20): binning
-# (k_bounds_partial, k_bounds_final, k_assign, 3 scan kernels, k_fill_cells,
-# k_sort_cells), k_neighbours, face links (3 scan kernels, k_link), k_timestep,
-# k_dt_final, k_gradients, k_faces (first pass, second Newton pass), k_update,
+# launch_step): binning (k_bounds_partial, k_bounds_final, k_assign, 3 scan
+# kernels, k_fill_cells, k_sort_cells), k_neighbours, face links (3 scan
+# kernels, k_link), k_timestep, k_dt_final, k_gradients, the face pass
+# (k_faces_block, or k_faces first pass + second Newton pass), k_update,
 # k_advance_time
 LAUNCHES_PER_STEP = 20
 
-# Algorithmic operations per canonical face of the dominant kernel (k_faces:
-# effective face, face states, pairwise limiter, half-step prediction, exact
-# Riemann solve, flux) in the reference's method, counted by the
-# operation-counting build of the oracle (oracle/flops.py; every addition,
-# multiplication, division, square root and pow weighs 1, an FMA 2) over 16
-# steps: 3D on the 32^3 periodic Sedov lattice with the 128^3 workload's h/dx
-# (1.28 Newton iterations per face), 2D on the 100x100 Kelvin-Helmholtz
-# set-up (1.47).  The roofline's `achieved` uses these.
-FACE_ALG_FLOPS = {3: 746.0, 2: 339.8}
-# What k_faces (both passes, gamma = 5/3 path) executes per face, from ncu
-# --set full captures: FP64 operations (2 x DFMA + DADD + DMUL thread
-# instructions / faces) and DRAM bytes (read + write).  3D: the 64^3 periodic
-# Sedov step; 2D: 32 members of the Kelvin-Helmholtz ensemble with the second
-# Newton pass.
-FACE_EXEC_FP64_FLOPS = {3: 541.0, 2: 391.0}
-FACE_DRAM_BYTES = {3: 298.0, 2: 364.0}
-
-# Every kernel of the step, per unit (particle, or canonical face for the
-# face passes): (FP64 flops executed, DRAM bytes read + written) from the
-# same ncu captures (3D: Sedov 64^3; 2D: 32 KH ensemble members), and the
-# algorithmic operations of the reference's method from the
-# operation-counting oracle (3D: 32^3 Sedov lattice; 2D: 100x100 KH set-up).
-# The per-unit figures scale with the units of the measured workload.
+# What each kernel of the step executes per unit (particle, or canonical
+# face for the face pass), from ncu captures of the same kernels: FP64
+# operations (2 x DFMA + DADD + DMUL thread instructions per unit) and DRAM
+# bytes (read + write per unit); 3D on the 64^3 periodic Sedov step, 2D on 32
+# members of the Kelvin-Helmholtz ensemble.  These are executed, not
+# algorithmic, operations: a kernel cannot execute more than the FP64 pipe
+# issues, so the rates they give are bounded by the pipe's peak.
 KERNEL_UNITS = {"neighbours_density": "particle", "timestep": "particle", "gradients_limiter": "particle",
                 "face_links": "particle", "faces_riemann": "face", "gather_update": "particle"}
 KERNEL_EXEC = {
@@ -77,27 +69,39 @@ KERNEL_EXEC = {
     2: {"neighbours_density": (597.0, 733.0), "timestep": (311.0, 748.0), "gradients_limiter": (1382.0, 1962.0),
         "face_links": (0.0, 781.0), "faces_riemann": (391.0, 364.0), "gather_update": (122.0, 915.0)},
 }
-KERNEL_ALG_OPS = {
+# FP64 pipe active (sm__pipe_fp64_cycles_active over elapsed cycles) of the
+# same captures
+KERNEL_FP64_PIPE = {
+    3: {"neighbours_density": 0.59, "timestep": 0.85, "gradients_limiter": 0.90, "faces_riemann": 0.86,
+        "gather_update": None, "face_links": 0.0},
+}
+# Operations of the reference's method per unit, counted by the
+# operation-counting build of the oracle (oracle/flops.py; every addition,
+# multiplication, division, square root and pow weighs 1, an FMA 2).  This
+# counts the reference implementation's work, including rotation matrices,
+# repeated kernel evaluations and every candidate of the cell stencil, which
+# the kernels here do not execute: it is not a lower bound of the method and
+# is reported for comparison only, never as a roofline.
+KERNEL_REF_OPS = {
     3: {"neighbours_density": 3618.0, "timestep": 754.0, "gradients_limiter": 7871.0, "face_links": 0.0,
         "faces_riemann": 746.0, "gather_update": 198.0},
     2: {"neighbours_density": 700.0, "timestep": 375.0, "gradients_limiter": 2678.0, "face_links": 0.0,
         "faces_riemann": 339.8, "gather_update": 108.0},
 }
+FP64_OPS_PER_SM_CYCLE = 4.0   # two fused multiply-adds per SM and cycle
 
 
 def kernel_rooflines(kernel_ms: dict, dim: int, particles: float, faces: float, fp64_peak_tflops, hbm_peak_gbs):
     """Each kernel of the step against the FP64 and the HBM roofline: its
-    time per step (CUDA events), the FP64 flops it executes and the DRAM
-    bytes it moves per unit (ncu), the rates they give, as fractions of the
-    measured FP64 FMA peak and HBM copy bandwidth, and the rate of the
-    reference's algorithmic operations."""
+    time per step (CUDA events), the FP64 operations it executes and the DRAM
+    bytes it moves per unit (ncu), the rates they give, and their fractions of
+    the measured FP64 FMA peak and HBM copy bandwidth."""
     out = {}
     for k, unit in KERNEL_UNITS.items():
         ms = kernel_ms.get(k)
         if not ms or ms <= 0.0 or dim not in KERNEL_EXEC:
             continue
         fl, by = KERNEL_EXEC[dim][k]
-        alg = KERNEL_ALG_OPS[dim][k]
         units = faces if unit == "face" else particles
         s = ms / 1e3
         tf = fl * units / s / 1e12
@@ -105,10 +109,20 @@ def kernel_rooflines(kernel_ms: dict, dim: int, particles: float, faces: float, 
         out[k] = {"ms_per_step": ms, "unit": unit, "units_per_step": units,
                   "fp64_flops_per_unit": fl, "fp64_tflops": tf,
                   "fp64_frac": tf / fp64_peak_tflops if fp64_peak_tflops else None,
+                  "fp64_pipe_active_ncu": KERNEL_FP64_PIPE.get(dim, {}).get(k),
                   "dram_bytes_per_unit": by, "hbm_gbs": gbs,
                   "hbm_frac": gbs / hbm_peak_gbs if hbm_peak_gbs else None,
-                  "algorithmic_ops_per_unit": alg, "algorithmic_tflops": alg * units / s / 1e12}
+                  "reference_method_ops_per_unit": KERNEL_REF_OPS[dim][k]}
     return out
+
+
+def step_fp64(dim: int, particles: float, faces: float) -> float:
+    """FP64 operations the step's kernels execute per step (ncu per-unit
+    figures times the units)."""
+    tot = 0.0
+    for k, unit in KERNEL_UNITS.items():
+        tot += KERNEL_EXEC[dim][k][0] * (faces if unit == "face" else particles)
+    return tot
 
 
 def make_workload(name: str, seed_offset: int = 0):
@@ -121,6 +135,9 @@ def make_workload(name: str, seed_offset: int = 0):
     if w["kind"] == "sedov":
         p = ic.sedov(n_side=w["n_side"], seed=2 + seed_offset)
         return p, MFVConfig.sedov(p, periodic=w["periodic"])
+    if w["kind"] == "multi_blast":
+        p = ic.multi_blast(n_side=w["n_side"], n_blasts=w["n_blasts"], seed=11 + seed_offset)
+        return p, MFVConfig.sedov(p, periodic=True)
     p = ic.kelvin_helmholtz(n_side=w["n_side"], seed=1 + seed_offset)
     return p, MFVConfig.kelvin_helmholtz(p)
 
@@ -206,57 +223,63 @@ def cpu_model():
     return "unknown"
 
 
-def cpu_baseline_sample(seconds_hint: float = 20.0, kind: str = "sedov"):
-    """The oracle (serial CPU restatement of the reference) on a bounded sample:
-    whole MFV steps of the 32^3 Sedov lattice with the workload's particle
-    density and neighbour count (same per-particle work as 128^3), or of the
-    100x100 Kelvin-Helmholtz set-up for the 2D workloads."""
+def host_cores():
+    return os.cpu_count() or 1
+
+
+def _oracle_sample(kind: str):
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     import oracle
     from meshlesshydro_gb300 import ic
     from meshlesshydro_gb300.config import MFVConfig
     oracle.build()
+    oracle.set_threads(1)
     if kind == "sedov":
         p = ic.sedov(n_side=32, seed=2)
-        cfg = MFVConfig.sedov(p, periodic=True)
-        what = "32^3 periodic Sedov lattice"
-    else:
-        p = ic.kelvin_helmholtz(n_side=100, seed=1)
-        cfg = MFVConfig.kelvin_helmholtz(p)
-        what = "100x100 Kelvin-Helmholtz set-up"
-    o = oracle.Oracle(cfg, p)
+        return oracle, p, MFVConfig.sedov(p, periodic=True), "32^3 periodic Sedov lattice"
+    p = ic.kelvin_helmholtz(n_side=100, seed=1)
+    return oracle, p, MFVConfig.kelvin_helmholtz(p), "100x100 Kelvin-Helmholtz set-up"
+
+
+def _time_oracle(o, seconds_hint, max_steps):
     o.step()  # warm-up
     steps, t0 = 0, time.perf_counter()
     while True:
         o.step()
         steps += 1
         el = time.perf_counter() - t0
-        if el >= seconds_hint or steps >= 50:
-            break
+        if el >= seconds_hint or steps >= max_steps:
+            return steps, el
+
+
+def cpu_baseline_sample(seconds_hint: float = 15.0, kind: str = "sedov"):
+    """The oracle (serial CPU restatement of the reference, -O3 as the
+    reference's own build) on a bounded sample: whole MFV steps of the 32^3
+    Sedov lattice with the workload's particle density and neighbour count
+    (the same per-particle work as 128^3), or of the 100x100 Kelvin-Helmholtz
+    set-up for the 2D workloads; at the reference's DEBUG_LVL 0 (the value)
+    and DEBUG_LVL 1 as its test cases ship it (checkFluxSymmetry every step)."""
+    oracle, p, cfg, what = _oracle_sample(kind)
+    o = oracle.Oracle(cfg, p)
+    steps, el = _time_oracle(o, seconds_hint, 50)
+    o1 = oracle.Oracle(cfg, p)
+    o1.set_debug_level(1)
+    steps1, el1 = _time_oracle(o1, seconds_hint / 3, 20)
     return {"value": p.n * steps / el, "unit": "particle-updates/s", "cores": 1, "kind": "port",
+            "host_cores": host_cores(), "host_cpu": cpu_model(),
+            "debug_lvl1_value": p.n * steps1 / el1,
             "sample": f"{steps} MFV steps of the {what} ({p.n} particles, the workload's h/dx and neighbour "
-                      f"count), serial oracle, {el:.1f} s, host {cpu_model()}"}
+                      f"count), serial oracle built -O3 -ffp-contract=off, {el:.1f} s, 1 of {host_cores()} "
+                      f"cores of {cpu_model()}; debug_lvl1_value: the same with the reference's DEBUG_LVL 1 "
+                      f"flux-symmetry check, {steps1} steps"}
 
 
 def run_reference(args):
     ws, rank, _ = dist_env()
     if rank != 0:
         return 0
-    sys.path.insert(0, os.path.join(ROOT, "oracle"))
-    import oracle
-    from meshlesshydro_gb300 import ic
-    from meshlesshydro_gb300.config import MFVConfig
-    oracle.build()
     w = WORKLOADS[args.workload]
-    # bounded sample: the 32^3 lattice for Sedov workloads, the full KH set-up
-    if w["kind"] == "sedov":
-        p = ic.sedov(n_side=32, seed=2)
-        cfg = MFVConfig.sedov(p, periodic=w["periodic"])
-        sample = f"32^3 periodic Sedov lattice ({p.n} particles; same h/dx as {args.workload}), one MFV step per step"
-    else:
-        p = ic.kelvin_helmholtz(n_side=w["n_side"], seed=1)
-        cfg = MFVConfig.kelvin_helmholtz(p)
-        sample = f"{args.workload} ({p.n} particles), one MFV step per step"
+    oracle, p, cfg, what = _oracle_sample("kh" if w["kind"] in ("kh", "ensemble") else "sedov")
     o = oracle.Oracle(cfg, p)
     for _ in range(args.warmup):
         o.step()
@@ -265,12 +288,15 @@ def run_reference(args):
         o.step()
     el = time.perf_counter() - t0
     val = p.n * args.steps / el
+    sample = (f"{what} ({p.n} particles, the workload's h/dx and neighbour count), one MFV step per step, "
+              f"serial CPU restatement of the reference (the reference is single-threaded), built -O3, "
+              f"DEBUG_LVL 0")
     line = {"metric": METRIC, "value": val, "unit": "particle-updates/s", "n_gpus": ws, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": 1e3 * el / args.steps, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic", "impl": "reference",
             "config": {"workload": args.workload, "sample": sample},
             "cpu_baseline": {"value": val, "unit": "particle-updates/s", "cores": 1, "kind": "port",
-                             "sample": sample + f", host {cpu_model()}"},
+                             "host_cores": host_cores(), "sample": sample + f", host {cpu_model()}"},
             "e2e": {"value": val, "unit": "particle-updates/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
     return 0
@@ -286,79 +312,171 @@ def kernel_breakdown(sim, steps):
     return sim.kernel_times()
 
 
-def learned_section(runtime, make_sim, tuning, args, faces_per_step, st_plain, kt_plain, rho_plain, ws, n):
-    """The same steps with the learned p* guess: harvest faces of step 1
-    (plain pipeline), train the MLP on 90 % of them, tune the learned
-    pipeline's launch shapes and face-pass structure with the autotuner
-    (which restores the state), step with the network guess to the same step
-    count and compare with the plain run."""
+def per_step(kt):
+    return {k: v[1] / max(v[0], 1) for k, v in kt.items()}
+
+
+def timed_steps(sim, warmup, steps):
+    """warmup steps, then `steps` timed steps: (stats, wall seconds)."""
     import torch
-    sim2 = make_sim()
-    if tuning:
-        sim2.set_tuning(tuning)
-    stride = max(1, int(faces_per_step // 2_000_000))
-    t0 = time.perf_counter()
-    x, t = sim2.harvest(stride=stride, capacity=int(faces_per_step // stride) + 64)
-    rng = np.random.default_rng(0)
-    perm = rng.permutation(x.shape[0])
-    nval = x.shape[0] // 10
-    val, tr = perm[:nval], perm[nval:]
-    t1 = time.perf_counter()
-    w, hist = runtime.pstar_train(x[tr], t[tr], epochs=20, batch=4096, lr=2e-3, seed=0)
-    t2 = time.perf_counter()
-    yv = runtime.pstar_infer(w, x[val])
-    rel = np.abs(np.exp(yv.astype(np.float64) - t[val]) - 1.0)
-    sim2.set_pstar_weights(w)
-    tuning_l = sim2.autotune(2) if tuning else None
-    if args.warmup > 1:
-        sim2.step(args.warmup - 1)
+    if warmup:
+        sim.step(warmup)
     torch.cuda.synchronize()
-    st = sim2.step(args.steps)
-    rho = sim2.get("rho")
-    kt = kernel_breakdown(sim2, args.steps)
-    sim2.close()
-    l1 = float(np.sum(np.abs(rho - rho_plain)) / np.sum(np.abs(rho_plain)))
-    return {"value": ws * n * st.steps / (st.device_ms / 1e3),
-            "plain_value": ws * n * st_plain.steps / (st_plain.device_ms / 1e3),
-            "newton_iterations_per_face": st.newton_iterations / max(st.faces, 1),
-            "plain_newton_iterations_per_face": st_plain.newton_iterations / max(st_plain.faces, 1),
-            "fallback_rate": st.newton_fallbacks / max(st.learned_faces, 1),
-            "learned_face_fraction": st.learned_faces / max(st.faces, 1),
-            "faces_kernel_ms_per_step": kt["faces_riemann"][1] / max(kt["faces_riemann"][0], 1),
-            "plain_faces_kernel_ms_per_step": kt_plain["faces_riemann"][1] / max(kt_plain["faces_riemann"][0], 1),
-            "density_L1_vs_plain": l1,
-            "tuning": tuning_l,
-            "status": runtime.status_names(st.status),
-            "guess": "p_TR * exp(y) where |y| > 0.01, else p_TR (two-rarefaction)",
-            "train": {"samples": int(tr.size), "val_samples": int(nval), "harvest_stride": stride,
-                      "harvest_step": 1, "epochs": 20, "batch": 4096, "lr": 2e-3,
-                      "loss_first_epoch": float(hist[0]), "loss_last_epoch": float(hist[-1]),
-                      "val_median_rel_err": float(np.median(rel)) if nval else None,
-                      "val_p90_rel_err": float(np.quantile(rel, 0.9)) if nval else None,
-                      "harvest_s": t1 - t0, "train_s": t2 - t1}}
+    t0 = time.perf_counter()
+    st = sim.step(steps)
+    torch.cuda.synchronize()
+    return st, time.perf_counter() - t0
 
 
-def adaptive_section(runtime, cfg, p, tuning, args, ws):
+def train_learned_guess(runtime, budget_rows: int = 10_000_000, epochs: int = 12):
+    """The network of the learned star-pressure guess, trained on the GPU
+    (mlh_pstar_train) on faces harvested from the plain method's own runs:
+    the 64^3 periodic Sedov blast (100 steps: every face the learned step
+    hands to the network, at every step, and every 4th face at steps 0, 25,
+    50 and 75) and the 100x100 Kelvin-Helmholtz run (100 steps: every face of
+    every 5th step), at most budget_rows rows (a seeded subsample beyond).
+    Seeds differ from the evaluated workloads."""
+    from meshlesshydro_gb300 import ic
+    from meshlesshydro_gb300.config import MFVConfig
+    t0 = time.perf_counter()
+    xs, ts = [], []
+    n_strong = n_sedov = n_kh = 0
+    p = ic.sedov(n_side=64, seed=12)
+    s = runtime.Simulation(MFVConfig.sedov(p, periodic=True), p)
+    for k in range(100):
+        if k % 25 == 0:
+            x, t = s.harvest(stride=4, capacity=1 << 21)
+            n_sedov += x.shape[0]
+        else:
+            x, t, _ = s.harvest(strong=True, capacity=1 << 20)
+            n_strong += x.shape[0]
+        xs.append(x); ts.append(t)
+    s.close()
+    q = ic.kelvin_helmholtz(n_side=100, seed=21)
+    s = runtime.Simulation(MFVConfig.kelvin_helmholtz(q), q)
+    for k in range(100):
+        if k % 5 == 0:
+            x, t = s.harvest(stride=1, capacity=1 << 18)
+            xs.append(x); ts.append(t)
+            n_kh += x.shape[0]
+        else:
+            s.step(1)
+    s.close()
+    x = np.concatenate(xs)
+    t = np.concatenate(ts)
+    rng = np.random.default_rng(0)
+    if x.shape[0] > budget_rows:
+        keep = rng.choice(x.shape[0], budget_rows, replace=False)
+        x, t = x[keep], t[keep]
+    t1 = time.perf_counter()
+    w, hist = runtime.pstar_train(x, t, epochs=epochs, batch=8192, lr=2e-3, seed=0)
+    t2 = time.perf_counter()
+    return w, {"rows": int(x.shape[0]), "rows_sedov64_strong": n_strong, "rows_sedov64_every_4th": n_sedov,
+               "rows_kh100": n_kh, "epochs": epochs, "batch": 8192, "lr": 2e-3,
+               "loss_first_epoch": float(hist[0]), "loss_last_epoch": float(hist[-1]),
+               "harvest_s": t1 - t0, "train_s": t2 - t1}
+
+
+def network_error(runtime, w, sim_factory):
+    """Relative error of the guess p_TR e^y against the converged p* on
+    held-out faces: every strong shock and every 64th face of one step of a
+    fresh simulation of the evaluated workload."""
+    s = sim_factory()
+    xs, ts, n = s.harvest(strong=True, capacity=1 << 21)
+    s.close()
+    s = sim_factory()
+    xa, ta = s.harvest(stride=64, capacity=1 << 21)
+    s.close()
+    out = {}
+    for name, (x, t) in (("strong", (xs, ts)), ("all_every_64th", (xa, ta))):
+        if x.shape[0] == 0:
+            out[name] = {"rows": 0}
+            continue
+        y = runtime.pstar_infer(w, x).astype(np.float64)
+        rel = np.abs(np.exp(y - t) - 1.0)
+        rel_tr = np.abs(np.exp(-t.astype(np.float64)) - 1.0)   # error of p_TR itself
+        out[name] = {"rows": int(x.shape[0]), "median_rel_err": float(np.median(rel)),
+                     "p90_rel_err": float(np.quantile(rel, 0.9)),
+                     "p_TR_median_rel_err": float(np.median(rel_tr))}
+    return out
+
+
+def learned_vs_plain(runtime, make, w, args, tuning_plain=None, st_plain=None, kt_plain=None, rho_plain=None):
+    """The same steps with and without the learned guess, each with the
+    autotuner's launch shapes for its own pipeline (so that the learned step
+    may take another face-pass structure); device time of the timed steps."""
+    out = {}
+    if st_plain is None:
+        sp = make()
+        tuning_plain = sp.autotune(2)
+        st_plain, _ = timed_steps(sp, args.warmup, args.steps)
+        rho_plain = sp.get("rho")
+        kt_plain = kernel_breakdown(sp, args.steps)
+        sp.close()
+    sl = make()
+    sl.set_pstar_weights(w)
+    tuning_l = sl.autotune(2)
+    st, _ = timed_steps(sl, args.warmup, args.steps)
+    rho = sl.get("rho")
+    kt = kernel_breakdown(sl, args.steps)
+    sl.close()
+    npart = rho.size
+    v_l = npart * st.steps / (st.device_ms / 1e3)
+    v_p = npart * st_plain.steps / (st_plain.device_ms / 1e3)
+    saved = st_plain.newton_iterations - st.newton_iterations
+    out.update({
+        "value": v_l, "plain_value": v_p, "learned_over_plain": v_l / v_p,
+        "newton_iterations_per_face": st.newton_iterations / max(st.faces, 1),
+        "plain_newton_iterations_per_face": st_plain.newton_iterations / max(st_plain.faces, 1),
+        "iterations_saved": int(saved),
+        "iterations_saved_per_learned_face": saved / max(st.learned_faces, 1),
+        "learned_faces": int(st.learned_faces), "learned_face_fraction": st.learned_faces / max(st.faces, 1),
+        "fallbacks": int(st.newton_fallbacks),
+        "fallback_rate": st.newton_fallbacks / max(st.learned_faces, 1),
+        "faces_kernel_ms_per_step": per_step(kt).get("faces_riemann"),
+        "plain_faces_kernel_ms_per_step": per_step(kt_plain).get("faces_riemann"),
+        "density_L1_vs_plain": float(np.sum(np.abs(rho - rho_plain)) / np.sum(np.abs(rho_plain))),
+        "tuning": tuning_l, "plain_tuning": tuning_plain,
+        "status": runtime.status_names(st.status)})
+    return out
+
+
+def learned_section(runtime, args, make_main, tuning, st_plain, kt_plain, rho_plain):
+    """Learned guess: training on the Sedov 64^3 + KH harvest, network error
+    on held-out faces, and the learned step against the plain one on the
+    bench workload and on the 64-blast 64^3 workload (strong shocks)."""
+    w, train = train_learned_guess(runtime)
+    out = {"guess": "p_TR * exp(y) for faces with p_TR > 2 min(pL, pR) where |y| > 0.01, else p_TR; Newton to "
+                    "1e-10 relative either way, restarting from p_TR when the network's start does not converge",
+           "train": train}
+    out["network_error_held_out"] = network_error(runtime, w, make_main)
+    out["main_workload"] = learned_vs_plain(runtime, make_main, w, args, tuning, st_plain, kt_plain, rho_plain)
+    pm, cm = make_workload("multi_blast64")
+    mk = lambda: runtime.Simulation(cm, pm)
+    out["multi_blast64"] = learned_vs_plain(runtime, mk, w, args)
+    out["multi_blast64"]["network_error_held_out"] = network_error(runtime, w, mk)
+    out["multi_blast64"]["workload"] = ("64 blasts (energy 0.1 in total) in the periodic 64^3 Sedov cube, "
+                                        "background pressure 1e-2 (ic.multi_blast)")
+    return out, w
+
+
+def adaptive_section(runtime, cfg, p, tuning, args):
     """The same workload with per-particle smoothing lengths (adaptive_h):
     every step solves h_i <= H for an effective neighbour number of 32, H =
     1.25 kernelSize the search radius, and searches pairs with r < max(h_i,
     h_j).  Reports its throughput and the share of the h solve."""
-    import torch
     from dataclasses import replace
     cfg_a = replace(cfg, adaptive_h=True, n_ngb=32.0, kernel_size=cfg.kernel_size * 1.25)
     sim = runtime.Simulation(cfg_a, p)
-    # its own launch shapes: the wider search radius changes the best ones
     tuning_a = sim.autotune(2) if tuning else None
-    sim.step(args.warmup)
-    torch.cuda.synchronize()
-    st = sim.step(args.steps)
+    st, _ = timed_steps(sim, args.warmup, args.steps)
     kt = kernel_breakdown(sim, args.steps)
     hs = sim.get("h_stats")
     h = sim.get("h")
     noi = sim.get("noi")
     sim.close()
-    per = {k: v[1] / max(v[0], 1) for k, v in kt.items()}
-    return {"value": ws * p.n * st.steps / (st.device_ms / 1e3), "ms_per_step": st.device_ms / st.steps,
+    per = per_step(kt)
+    return {"value": p.n * st.steps / (st.device_ms / 1e3), "ms_per_step": st.device_ms / st.steps,
             "n_ngb": 32.0, "search_radius_over_kernel_size": 1.25,
             "h_over_search_radius_mean": float(np.mean(h) / cfg_a.kernel_size),
             "neighbours_mean": float(np.mean(noi)),
@@ -367,6 +485,72 @@ def adaptive_section(runtime, cfg, p, tuning, args, ws):
             "h_stats_last_solve": {"newton_iterations": float(hs[0]), "clamped": float(hs[1])},
             "tuning": tuning_a,
             "status": runtime.status_names(st.status)}
+
+
+def ensemble_section(runtime, args, w_learned):
+    """The 256-member Kelvin-Helmholtz ensemble (N log-uniform in [2500,
+    40000], seeded): all members in one context, one CUDA graph per step,
+    launch shapes and face-pass structure from the autotuner, with and
+    without the learned guess; against the same members run one after
+    another, each in its own context with the plain step.  Both sides are
+    timed on the same clocks: host wall time around all timed steps (one
+    synchronisation at each end), and the summed device time of the step
+    calls (CUDA events)."""
+    from meshlesshydro_gb300 import ic
+    from meshlesshydro_gb300.config import MFVConfig
+    members = ic.kh_ensemble(n_members=256, seed=7)
+    cfg = MFVConfig.kelvin_helmholtz(members[0])
+    npart = sum(m.n for m in members)
+    clocks = ClockSampler(0)
+    clocks.start()
+
+    def batched(weights):
+        sim = runtime.Simulation(cfg, members=members)
+        if weights is not None:
+            sim.set_pstar_weights(weights)
+        tuning = sim.autotune(2)
+        sim.set_graph_mode(True)
+        st, wall = timed_steps(sim, args.warmup, args.steps)
+        sim.close()
+        return tuning, st, wall
+
+    tun_p, st_p, wall_p = batched(None)
+    tun_l, st_l, wall_l = batched(w_learned) if w_learned is not None else (None, None, None)
+    # members one after another: every member's step is a plain mlh_step(1)
+    sims = [runtime.Simulation(MFVConfig.kelvin_helmholtz(m), m) for m in members]
+    for s_ in sims:
+        s_.step(args.warmup)
+    import torch
+    torch.cuda.synchronize()
+    seq_dev = 0.0
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        for s_ in sims:
+            seq_dev += s_.step(1).device_ms
+    torch.cuda.synchronize()
+    seq_wall = time.perf_counter() - t0
+    for s_ in sims:
+        s_.close()
+    ck = clocks.stop()
+    units = npart * args.steps
+    out = {"members": len(members), "particles": npart, "steps": args.steps,
+           "batched_graph_value": units / wall_p,
+           "batched_graph_device_value": units / (st_p.device_ms / 1e3),
+           "sequential_value": units / seq_wall,
+           "sequential_device_value": units / (seq_dev / 1e3),
+           "batched_over_sequential": (units / wall_p) / (units / seq_wall),
+           "batched_over_sequential_device": seq_dev / st_p.device_ms,
+           "clock": "wall: host time around all timed steps, synchronised at both ends, on both sides; device: "
+                    "CUDA-event time of the step calls, summed over calls on the sequential side",
+           "newton_iterations_per_face": st_p.newton_iterations / max(st_p.faces, 1),
+           "tuning": tun_p, "clocks": ck, "status": runtime.status_names(st_p.status)}
+    if st_l is not None:
+        out.update({"learned_value": units / wall_l, "learned_device_value": units / (st_l.device_ms / 1e3),
+                    "learned_over_plain": wall_p / wall_l,
+                    "learned_over_sequential": (units / wall_l) / (units / seq_wall),
+                    "learned_faces": int(st_l.learned_faces),
+                    "learned_tuning": tun_l})
+    return out
 
 
 def run_mlh(args):
@@ -381,7 +565,11 @@ def run_mlh(args):
     from meshlesshydro_gb300 import build, runtime
     from meshlesshydro_gb300.replicas import gather_units, job_rate, job_seconds, replica_seed
     build.build()
-    fp64_peak = runtime.probe_fp64_tflops(0.5)
+    probe_clocks = ClockSampler(local)
+    probe_clocks.start()
+    fp64_peak, probe_mhz = runtime.probe_fp64_clock(1.0)
+    probe_ck = probe_clocks.stop()
+    sm_count = torch.cuda.get_device_properties(local).multi_processor_count
     p, cfg = make_workload(args.workload, seed_offset=replica_seed(0, rank))
     ensemble = WORKLOADS[args.workload]["kind"] == "ensemble"
     members = p if ensemble else None
@@ -403,46 +591,10 @@ def run_mlh(args):
     t_max = job_seconds(st.device_ms / 1e3, dist)
     faces_per_step = st.faces / max(st.steps, 1)
     pairs_per_step = st.pair_interactions / max(st.steps, 1)
-    rho_plain = sim.get("rho")      # density of step warmup + steps (autotune restored its trials)
+    rho_plain = sim.get("rho")
     kt = kernel_breakdown(sim, args.steps)
-    make_sim = ((lambda: runtime.Simulation(cfg, members=members)) if ensemble
-                else (lambda: runtime.Simulation(cfg, p)))
-
-    extra = {}
-    if ensemble:
-        # the same steps in graph mode (one CUDA graph per step), and the
-        # members run one after another as separate plain simulations
-        sim.set_graph_mode(True)
-        sim.step(1)
-        torch.cuda.synchronize()
-        stg = sim.step(args.steps)
-        graph_value = ws * p.n * stg.steps / (stg.device_ms / 1e3)
-        sim.set_graph_mode(False)
-        seq_steps = 2
-        from meshlesshydro_gb300.config import MFVConfig
-        sims = [runtime.Simulation(MFVConfig.kelvin_helmholtz(m), m) for m in members]
-        for s_ in sims:
-            s_.step(1)
-        torch.cuda.synchronize()
-        t0s = time.perf_counter()
-        for _ in range(seq_steps):
-            for s_ in sims:
-                s_.step(1)
-        torch.cuda.synchronize()
-        seq_wall = time.perf_counter() - t0s
-        seq_value = p.n * seq_steps / seq_wall
-        del sims
-        extra = {"ensemble": {"members": len(members), "particles": p.n,
-                              "batched_graph_value": graph_value,
-                              "sequential_value": seq_value,
-                              "sequential": "each member its own context, one mlh_step(1) call per member per step, "
-                                            f"{seq_steps} steps, wall clock",
-                              "batched_over_sequential": graph_value / seq_value}}
-
-    if not args.no_learned:
-        extra["learned"] = learned_section(runtime, make_sim, tuning, args, faces_per_step, st, kt, rho_plain, ws, p.n)
-    if not args.no_adaptive and WORKLOADS[args.workload]["kind"] == "sedov":
-        extra["adaptive_h"] = adaptive_section(runtime, cfg, p, tuning, args, ws)
+    make_main = ((lambda: runtime.Simulation(cfg, members=members)) if ensemble
+                 else (lambda: runtime.Simulation(cfg, p)))
 
     # end to end through the C ABI with host buffers: H2D of the state,
     # one step, D2H of the state, every step (pinned host memory)
@@ -457,6 +609,7 @@ def run_mlh(args):
     L.mlh_get_fields(sim.h, ctypes.byref(view))
     e2e_steps = max(2, min(args.steps, 5))
     used = 8 if cfg.dim == 3 else 6
+    torch.cuda.synchronize()
     t0 = time.perf_counter()
     for _ in range(e2e_steps):
         L.mlh_set_fields(sim.h, ctypes.byref(view))
@@ -464,6 +617,17 @@ def run_mlh(args):
         L.mlh_get_fields(sim.h, ctypes.byref(view))
     e2e_wall = job_seconds(time.perf_counter() - t0, dist)
     units = gather_units(n * st.steps, dist)
+    sim.close()
+
+    extra = {}
+    w_learned = None
+    main_kind = WORKLOADS[args.workload]["kind"]
+    if not args.no_learned and main_kind in ("sedov", "multi_blast"):
+        extra["learned"], w_learned = learned_section(runtime, args, make_main, tuning, st, kt, rho_plain)
+    if not args.no_adaptive and main_kind == "sedov":
+        extra["adaptive_h"] = adaptive_section(runtime, cfg, p, tuning, args)
+    if not args.no_ensemble and rank == 0:
+        extra["ensemble"] = ensemble_section(runtime, args, w_learned)
 
     if rank != 0:
         if dist:
@@ -471,43 +635,47 @@ def run_mlh(args):
         return 0
     value = job_rate(units, t_max)
     peaks, peak_kind = measured_peaks()
-    # dominant kernel and its roofline
-    dom = max(kt.items(), key=lambda kv: kv[1][1])
-    dom_name, (dom_launches, dom_ms) = dom
+    ms_step = 1e3 * t_max / st.steps
+    per = per_step(kt)
+    # dominant kernel and its roofline on executed FP64 operations
+    dom_name = max(per.items(), key=lambda kv: kv[1])[0]
+    dom_launches, dom_ms = kt[dom_name]
     dom_avg_s = dom_ms / max(dom_launches, 1) / 1e3
-    flops_per_face = FACE_ALG_FLOPS.get(cfg.dim)
-    exec_per_face = FACE_EXEC_FP64_FLOPS.get(cfg.dim)
-    bytes_per_face = FACE_DRAM_BYTES.get(cfg.dim)
-    achieved_tf = (flops_per_face * faces_per_step / dom_avg_s / 1e12
-                   if (dom_name == "faces_riemann" and flops_per_face) else None)
-    exec_tf = (exec_per_face * faces_per_step / dom_avg_s / 1e12
-               if (dom_name == "faces_riemann" and exec_per_face) else None)
-    roofline = {"kernel": "k_faces (faces_riemann)" if dom_name == "faces_riemann" else dom_name,
+    dim = cfg.dim
+    unit = KERNEL_UNITS.get(dom_name, "particle")
+    units_launch = faces_per_step if unit == "face" else float(n)
+    fl, by = KERNEL_EXEC.get(dim, {}).get(dom_name, (None, None))
+    achieved = fl * units_launch / dom_avg_s / 1e12 if fl else None
+    step_ops = step_fp64(dim, float(n), faces_per_step) if dim in KERNEL_EXEC else None
+    per_cycle_peak = probe_mhz * 1e6 * sm_count * FP64_OPS_PER_SM_CYCLE / 1e12 if probe_mhz else None
+    roofline = {"kernel": f"{dom_name} (k_faces_block / k_faces)" if dom_name == "faces_riemann" else dom_name,
                 "bound": "fp64", "unit": "TFLOP/s",
-                "achieved": achieved_tf, "peak": fp64_peak,
-                "frac": (achieved_tf / fp64_peak) if (achieved_tf and fp64_peak) else None,
-                "traffic": bytes_per_face * faces_per_step if bytes_per_face else None,
-                "peak_source": "measured: FP64 FMA-chain probe (mlh_probe_fp64_tflops) on this GPU in this run",
-                "units": "canonical faces", "units_per_launch": faces_per_step,
-                "flops_per_unit": flops_per_face,
-                "flops_source": "algorithmic: operations of the reference's method per canonical face, "
-                                "counted by the operation-counting oracle (oracle/flops.py), each 1, an FMA 2",
-                "executed": {"flops_per_unit": exec_per_face, "achieved": exec_tf,
-                             "frac": (exec_tf / fp64_peak) if (exec_tf and fp64_peak) else None,
-                             "source": "FP64 flops k_faces executes per face (ncu, 2 x DFMA + DADD + DMUL)"},
+                "achieved": achieved, "peak": fp64_peak,
+                "frac": (achieved / fp64_peak) if (achieved and fp64_peak) else None,
+                "traffic": by * units_launch if by else None,
+                "units": f"{unit}s", "units_per_launch": units_launch, "fp64_flops_per_unit": fl,
+                "flops_source": "executed: FP64 operations the kernel executes per unit (ncu: 2 x DFMA + DADD + "
+                                "DMUL thread instructions per unit, on the 64^3 Sedov step), not the reference's "
+                                "operation count",
+                "fp64_pipe_active_ncu": KERNEL_FP64_PIPE.get(dim, {}).get(dom_name),
+                "peak_source": "measured: FP64 FMA-chain probe (mlh_probe_fp64_clock) on this GPU in this run",
                 "avg_launch_ms": dom_avg_s * 1e3,
-                "hbm_view": {"achieved_gbs": (bytes_per_face * faces_per_step / dom_avg_s / 1e9) if bytes_per_face else None,
-                             "peak_gbs": peaks.get("hbm_gbs"), "peak_source": peak_kind}}
+                "hbm_view": {"achieved_gbs": (by * units_launch / dom_avg_s / 1e9) if by else None,
+                             "peak_gbs": peaks.get("hbm_gbs"), "peak_source": peak_kind},
+                "step_check": {"fp64_flops_per_step": step_ops,
+                               "tflops": step_ops / (ms_step / 1e3) / 1e12 if step_ops else None,
+                               "frac": (step_ops / (ms_step / 1e3) / 1e12 / fp64_peak) if step_ops else None,
+                               "note": "every kernel's executed FP64 operations per step over ms_per_step; "
+                                       "at most 1 (the kernels overlap only the integer face links)"}}
     try:   # every kernel against its roofline (arithmetic on the measured times)
-        kernels = kernel_rooflines({k: v[1] / max(v[0], 1) for k, v in kt.items()}, cfg.dim, float(n),
-                                   float(faces_per_step), fp64_peak, peaks.get("hbm_gbs"))
-        kernels["source"] = ("ms: CUDA events; FP64 flops and DRAM bytes per unit: ncu --set full of the same "
-                             "kernels (3D Sedov 64^3, 2D KH ensemble members); algorithmic operations: "
-                             "operation-counting oracle; peaks: FP64 FMA probe, measured HBM copy")
+        kernels = kernel_rooflines(per, dim, float(n), float(faces_per_step), fp64_peak, peaks.get("hbm_gbs"))
+        kernels["source"] = ("ms: CUDA events; FP64 operations and DRAM bytes per unit: ncu captures of the same "
+                             "kernels (3D Sedov 64^3, 2D KH ensemble members); peaks: FP64 FMA probe, measured "
+                             "HBM copy")
     except Exception as exc:   # never let the breakdown cost the bench line
         kernels = {"error": repr(exc)}
     line = {"metric": METRIC, "value": value, "unit": "particle-updates/s", "n_gpus": ws, "steps": st.steps,
-            "warmup": args.warmup, "ms_per_step": 1e3 * t_max / st.steps, "higher_is_better": True,
+            "warmup": args.warmup, "ms_per_step": ms_step, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
             "config": {"workload": args.workload, "particles_per_gpu": n, "dim": cfg.dim,
                        "periodic": bool(cfg.periodic), "kernel_size": cfg.kernel_size,
@@ -519,10 +687,16 @@ def run_mlh(args):
             "status": runtime.status_names(st.status),
             "wall_s_timed": wall,
             "gpu_launches": LAUNCHES_PER_STEP * st.steps,
-            "kernel_ms_per_step": {k: v[1] / max(v[0], 1) for k, v in kt.items()},
+            "kernel_ms_per_step": per,
             "kernel_ms_source": "up to 3 further steps with per-kernel CUDA events, which serialise the face-link "
                                 "stream that the timed steps overlap with the time step and gradients",
             "roofline": roofline,
+            "fp64_probe": {"tflops": fp64_peak, "sm_mhz": probe_mhz, "sm_count": sm_count,
+                           "per_cycle_peak_tflops": per_cycle_peak,
+                           "per_cycle_frac": fp64_peak / per_cycle_peak if per_cycle_peak else None,
+                           "tflops_at_max_clock": (fp64_peak * probe_ck["sm_max_mhz"] / probe_mhz
+                                                   if probe_mhz and probe_ck.get("sm_max_mhz") else None),
+                           "clocks": probe_ck},
             "kernels": kernels,
             "clocks": ck,
             "tuning": tuning,
@@ -534,7 +708,7 @@ def run_mlh(args):
             "peaks": {"source": peak_kind, "hbm_gbs": peaks.get("hbm_gbs")}}
     if not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline_sample(args.cpu_seconds,
-                                                   "sedov" if WORKLOADS[args.workload]["kind"] == "sedov" else "kh")
+                                                   "sedov" if main_kind in ("sedov", "multi_blast") else "kh")
     print(json.dumps(line), flush=True)
     if dist:
         dist.barrier()
@@ -553,6 +727,7 @@ def main():
     ap.add_argument("--no-autotune", action="store_true")
     ap.add_argument("--no-learned", action="store_true", help="skip the learned p* guess comparison")
     ap.add_argument("--no-adaptive", action="store_true", help="skip the per-particle smoothing-length run")
+    ap.add_argument("--no-ensemble", action="store_true", help="skip the 256-member KH ensemble comparison")
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference(args)

@@ -248,25 +248,41 @@ void mlh_reset_kernel_times(mlh_ctx *ctx);
  * of the FP64 roofline.  No counterpart in the reference (it has no GPU
  * code); used by bench.py. */
 int mlh_probe_fp64_tflops(double seconds, double *tflops);
+/* The same, also giving the effective SM clock (MHz) of the fastest launch:
+ * SM clock cycles over global-timer time of one thread's loop.  The probe's
+ * TFLOP/s over (sm_mhz * SMs * 4 FP64 operations per cycle, the rate of two
+ * fused multiply-adds per SM and cycle) is the share of the per-cycle FP64
+ * peak it reaches. */
+int mlh_probe_fp64_clock(double seconds, double *tflops, double *sm_mhz);
 
-/* The reciprocal, quotient and reciprocal square root the kernels use in
- * place of IEEE division (Newton-Raphson from the hardware estimates), for n
- * host values: rcp = 1/x, quot = y/x, rsqrt = 1/sqrt(x); for checking their
- * error against exact values.  No counterpart in the reference. */
+/* ---- Test hooks: not part of the step's interface.  They expose device
+ * arithmetic and the FP64 pipe's behaviour to the test suite
+ * (tests/test_gpu_fastmath.py, tests/test_gpu_fp64_lanes.py); no counterpart
+ * in the reference. */
+
+/* TEST HOOK.  The reciprocal, quotient and reciprocal square root the kernels
+ * use in place of IEEE division (Newton-Raphson from the hardware estimates),
+ * for n host values: rcp = 1/x, quot = y/x, rsqrt = 1/sqrt(x); for checking
+ * their error against exact values. */
 int mlh_probe_fast_math(int n, const double *x, const double *y, double *rcp, double *quot, double *rsqrt);
 
-/* Device time (ms, best of three launches) of the FMA chains of
+/* TEST HOOK.  Device time (ms, best of three launches) of the FMA chains of
  * mlh_probe_fp64_tflops run by only the first active_lanes (1..32) lanes of
  * every warp, iters (1..2^20) steps: how the FP64 pipe charges a partially
- * active warp instruction.  No counterpart in the reference. */
+ * active warp instruction. */
 int mlh_probe_fp64_lanes(int active_lanes, int iters, double *ms);
+
+/* ---- End of the test hooks. */
 
 /* Learned initial guess for the Riemann star pressure (no counterpart in the
  * reference): a 4-64-64-64-1 SiLU MLP, 8705 float parameters laid out as
  * W1[64][4], b1[64], W2[64][64], b2[64], W3[64][64], b3[64], W4[64], b4,
  * evaluated on the tensor cores in BF16 with FP32 accumulation.  Input per
- * face (4 floats): log(rhoR/rhoL), (uR-uL)/cL, log(pR/pL), log(cR/cL) of the
- * face-frame states (left = particle i); output y, one float per row.  The
+ * face (4 floats), from the face-frame states sorted by pressure (side A the
+ * lower, B the higher; the mirror image negates both normal velocities, so
+ * du = uB - uA is that of the unsorted problem): log(rhoB/rhoA), du/cA,
+ * log(pB/pA), log(cB/cA), with c = sqrt(gamma p / rho); output y, one float
+ * per row.  The
  * step reads y as log(p* / p_TR), p_TR the two-rarefaction guess of the face
  * (Toro eq. 4.46).  All arrays are host arrays. */
 int mlh_pstar_infer(const float *weights, const float *x, int n, float *y);
@@ -288,6 +304,10 @@ int mlh_set_pstar_weights(mlh_ctx *ctx, const float *weights);
  * floats) and targets log(p* / p_TR) of every `stride`-th face into x, t
  * (host, capacity rows); *count receives the number of rows. */
 int mlh_pstar_harvest(mlh_ctx *ctx, int stride, float *x, float *t, long long capacity, long long *count);
+/* The same, recording every face that the learned step hands to the network
+ * (two-rarefaction guess above 2 min(pL, pR): strong shocks).  *count
+ * receives the number of such faces (rows beyond capacity are dropped). */
+int mlh_pstar_harvest_strong(mlh_ctx *ctx, float *x, float *t, long long capacity, long long *count);
 
 /* Largest particle count mlh_grid_bounds_noalloc accepts (29-bit indices). */
 #define MLH_NOALLOC_MAX_PARTICLES ((1 << 29) - 1)

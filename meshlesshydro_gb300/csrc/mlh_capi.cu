@@ -811,8 +811,23 @@ int mlh_set_pstar_weights(mlh_ctx *c, const float *weights) {
 
 // One step that also records network inputs and targets log(p*/p_TR) of
 // every `stride`-th face (plain face pipeline).
+static int harvest_impl(mlh_ctx *c, int stride, int strong, float *x, float *t, long long capacity,
+                        long long *count);
+
 int mlh_pstar_harvest(mlh_ctx *c, int stride, float *x, float *t, long long capacity, long long *count) {
-    if (!c || stride < 1 || !x || !t || capacity < 1 || capacity > 0x7fffffff) return MLH_ERR_INVALID;
+    return harvest_impl(c, stride, 0, x, t, capacity, count);
+}
+
+int mlh_pstar_harvest_strong(mlh_ctx *c, float *x, float *t, long long capacity, long long *count) {
+    return harvest_impl(c, 1, 1, x, t, capacity, count);
+}
+
+static int harvest_impl(mlh_ctx *c, int stride, int strong, float *x, float *t, long long capacity,
+                        long long *count) {
+    if (!c || stride < 1 || !x || !t || capacity < 1 || capacity > 0x7fffffff) {
+        g_last_error = "invalid argument";
+        return MLH_ERR_INVALID;
+    }
     const bool learned0 = c->learned;
     c->learned = false;
     drop_graph(c);
@@ -824,7 +839,7 @@ int mlh_pstar_harvest(mlh_ctx *c, int stride, float *x, float *t, long long capa
     CK(cudaMalloc(&hc, sizeof(int)));
     CK(cudaMemsetAsync(hc, 0, sizeof(int), c->stream));
     c->harvest.x = hx; c->harvest.t = ht; c->harvest.count = hc;
-    c->harvest.stride = stride; c->harvest.cap = (int)capacity;
+    c->harvest.stride = stride; c->harvest.cap = (int)capacity; c->harvest.strong = strong;
     mlh_step_stats st;
     int rc = mlh_step(c, 1, 0., &st);
     c->harvest = Harvest{};
@@ -972,7 +987,7 @@ int mlh_stage_array(mlh_ctx *c, const char *name, void *out, long long capacity,
         for (int i = 0; i < n; ++i) off[i + 1] = off[i] + noi[i] + noiImg[i];
         return put(off.data(), n + 1, 4);
     }
-    if (nm == "nnl" || nm == "face_of" || nm == "F") {
+    if (nm == "nnl" || nm == "face_of" || nm == "F" || nm == "face_iters") {
         if (int rc = need_lists()) return rc;
         std::vector<uint32_t> nb((size_t)n * K);
         std::vector<int> fo((size_t)n * K);
@@ -989,6 +1004,16 @@ int mlh_stage_array(mlh_ctx *c, const char *name, void *out, long long capacity,
         CK(cudaMemcpy(&ftot, c->faceOff + n, sizeof(int), cudaMemcpyDeviceToHost));
         std::vector<double> F((size_t)ftot * 6 + 6);
         CK(cudaMemcpy(F.data(), c->Fface, sizeof(double) * (size_t)ftot * 6, cudaMemcpyDeviceToHost));
+        if (nm == "face_iters") {   // Newton steps of each slot's face (the record's sixth double)
+            std::vector<int> it;
+            for (int i = 0; i < n; ++i)
+                for (int s = 0; s < noi[i] + noiImg[i]; ++s) {
+                    const int f = fo[(size_t)i * K + s];
+                    const int id = (f > 0 ? f : -f) - 1;
+                    it.push_back(f == 0 ? 0 : (int)F[(size_t)id * 6 + 5]);
+                }
+            return put(it.data(), it.size(), 4);
+        }
         std::vector<double> o;
         const int NV = D + 2;
         for (int i = 0; i < n; ++i)

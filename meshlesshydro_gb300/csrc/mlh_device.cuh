@@ -113,6 +113,7 @@ struct Harvest {
     float *t;
     int *count;
     int stride, cap;
+    int strong;   // record the strong shocks only (compacted), not every stride-th face
 };
 
 // Kernel::cubicSpline, demonstrator/src/Particles.cpp:7-24, for a support

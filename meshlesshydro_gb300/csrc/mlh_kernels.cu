@@ -19,6 +19,7 @@
 #include "mlh_device.cuh"
 #include "mlh_riemann.cuh"
 #include "mlh_kernels.h"
+#include "mlh_mlp.cuh"
 
 #include <cfloat>
 
@@ -1498,11 +1499,14 @@ __device__ __forceinline__ void pairwise_limiter(const Params &p, double &phi0R,
     phi0L = pairwise_side(phi0L, phiL, fma(rL, d, phiL), delta1, delta2, !r_lt_l, p.int_abs);
 }
 
-// Network inputs of a face from its face-frame states (left = particle i,
-// un the velocity components along the face normal):
-// log(rhoR/rhoL), (uR - uL)/cL, log(pR/pL), log(cR/cL).
-// The network predicts y = log(p* / p_TR), p_TR the two-rarefaction guess of
-// the face.  p_TR is exact when both waves are rarefactions and its error grows
+// Network inputs of a face, from its face-frame problem sorted as the
+// gamma = 5/3 solver sorts it (riemann5_begin): side A the one with the lower
+// pressure (particle i on ties), side B the other, the mirror image negating
+// both normal velocities, so that du = uB - uA is the same in both
+// orientations:  log(rhoB/rhoA), du/cA, log(pB/pA) >= 0, log(cB/cA), in single
+// precision (c = sqrt(gamma p / rho)).  The network predicts
+// y = log(p* / p_TR), p_TR the two-rarefaction guess of the face; p* and p_TR
+// are the same for both orientations.  p_TR is exact when both waves are rarefactions and its error grows
 // with the shock strength p_TR / min(pL, pR) - 1 (about 1e-6 at 0.2, 3e-3 at
 // 2-4, 2e-2 beyond 4, measured on random states), so only faces with
 // p_TR > PSTAR_HARD * min(pL, pR) are handed to the network; the others are
@@ -1512,11 +1516,19 @@ __device__ __forceinline__ void pairwise_limiter(const Params &p, double &phi0R,
 constexpr double PSTAR_HARD = 2.0;
 constexpr float PSTAR_GATE = 0.01f;
 
+__device__ __forceinline__ float4 pstar_features_sorted(double rhoA, double pA, double rhoB, double pB, double du,
+                                                       float gamma) {
+    const float ra = (float)rhoA, rb = (float)rhoB, pa = (float)pA, pb = (float)pB;
+    const float ca = sqrtf(gamma * pa / ra), cb = sqrtf(gamma * pb / rb);
+    return make_float4(logf(rb / ra), (float)du / ca, logf(pb / pa), logf(cb / ca));
+}
+
+// the same from the unsorted face-frame states (R = particle i, left; L = j)
 __device__ __forceinline__ float4 pstar_features(const double *R, const double *L, double unR, double unL,
                                                 double gamma) {
-    const float rl = (float)R[0], rr = (float)L[0], pl = (float)R[1], pr = (float)L[1];
-    const float cl = sqrtf((float)gamma * pl / rl), cr = sqrtf((float)gamma * pr / rr);
-    return make_float4(logf(rr / rl), (float)(unL - unR) / cl, logf(pr / pl), logf(cr / cl));
+    const bool mir = dlt(L[1], R[1]);
+    return mir ? pstar_features_sorted(L[0], L[1], R[0], R[1], unL - unR, (float)gamma)
+               : pstar_features_sorted(R[0], R[1], L[0], L[1], unL - unR, (float)gamma);
 }
 
 // One canonical face (i < j): effective face A_ij = psi~_j(x_i)/omega_i -
@@ -1849,13 +1861,26 @@ __global__ void MLH_FACE_BOUNDS k_faces(Params p, const Member *__restrict__ mem
                        : riemann_exact(rc, R[0], unR, R[1], L[0], unL, L[1], -1., 0.);
             if (rs.iters >= 0) rs.iters += done;
         }
-        if (MODE == 0 && hv.stride > 0 && f % hv.stride == 0) {
-            const int slot = f / hv.stride;
+        if (MODE == 0 && hv.stride > 0 && (hv.strong || f % hv.stride == 0)) {
             const double ptr = two_rarefaction_guess<ROOT5>(rc, R[0], unR, R[1], L[0], unL, L[1]);
-            if (slot < hv.cap && rs.iters >= 0 && rs.pstar > 0. && ptr > 0.) {
-                hv.x[slot] = pstar_features(R, L, unR, unL, gamma);
-                hv.t[slot] = (float)log(rs.pstar / ptr);
-                atomicMax(hv.count, slot + 1);
+            if (rs.iters >= 0 && rs.pstar > 0. && ptr > 0.) {
+                if (hv.strong) {
+                    // the faces the learned step hands to the network
+                    if (dlt(PSTAR_HARD * (dlt(L[1], R[1]) ? L[1] : R[1]), ptr)) {
+                        const int slot = atomicAdd(hv.count, 1);
+                        if (slot < hv.cap) {
+                            hv.x[slot] = pstar_features(R, L, unR, unL, gamma);
+                            hv.t[slot] = (float)log(rs.pstar / ptr);
+                        }
+                    }
+                } else {
+                    const int slot = f / hv.stride;
+                    if (slot < hv.cap) {
+                        hv.x[slot] = pstar_features(R, L, unR, unL, gamma);
+                        hv.t[slot] = (float)log(rs.pstar / ptr);
+                        atomicMax(hv.count, slot + 1);
+                    }
+                }
             }
         }
         if (rs.iters < 0) st_local |= ST_NEWTON;
@@ -1869,10 +1894,14 @@ __global__ void MLH_FACE_BOUNDS k_faces(Params p, const Member *__restrict__ mem
         }
         double Fo[5];
         st_local |= project_flux<D>(rs, R, L, unR, unL, hatA, A, vf, rc.inv_gm1, p.mfm, Fo);
+        // the face's Newton steps (the step of the first pass included in
+        // MODE 4; -1: no convergence) in the record's sixth double, for parity
+        // checks
+        const int face_iters = rs.iters < 0 ? -1 : rs.iters + (MODE == 4 ? 1 : 0);
         double2 *dst = reinterpret_cast<double2 *>(Fface + (size_t)f * 6);
         dst[0] = make_double2(Fo[0], Fo[1]);
         dst[1] = make_double2(Fo[2], Fo[3]);
-        dst[2] = make_double2(Fo[4], 0.);
+        dst[2] = make_double2(Fo[4], (double)face_iters);
     }
     // block-level accumulation of the counters
     for (int o = 16; o > 0; o >>= 1) {
@@ -1900,11 +1929,40 @@ __global__ void MLH_FACE_BOUNDS k_faces(Params p, const Member *__restrict__ mem
 // guess, on the stored sides: the same arithmetic as the two-pass split);
 // then every face samples its solution and projects its flux, with all
 // lanes busy.  The loop runs in block-wide rounds so that every thread
-// reaches the barriers.  LEARNED: the first pass of the learned-guess step,
-// which hands strong shocks (p_TR > PSTAR_HARD min(pL, pR)) with their state,
-// p_TR and network inputs to queue A, as k_faces MODE 1 does (solving them
-// here when the queue is full); k_faces MODE 2 solves them afterwards.
+// reaches the barriers.  LEARNED: the learned-guess step.  Strong shocks
+// (p_TR > PSTAR_HARD min(pL, pR)) stop before their first Newton step; the
+// block lists them, evaluates the network for them on the tensor cores (a
+// warp per 16 faces, block_network_guess; a block-uniform branch that a round
+// without strong shocks skips) and continues them from p_TR e^y together with
+// the other unfinished faces.  Nothing leaves the block: the plain and the
+// learned step differ only by that branch.
 constexpr int FB_T = 128;   // threads per block of k_faces_block
+
+// The network's guesses for the ns strong-shock faces of a round listed in
+// slist (their solver states in sv, s.p = p_TR): warp w takes the faces
+// w*16 .. w*16+15, then the next 64, and so on; s.p becomes p_TR e^y where
+// PSTAR_GATE < |y| < 30 (finite), and stays p_TR elsewhere.  Every lane of a
+// warp runs the MMAs (rows beyond ns are zero inputs whose outputs are
+// dropped).  Out of line, so that the rare branch that calls it does not shape
+// the register allocation of the face pass.
+__device__ __noinline__ void block_network_guess(const PackedMlp *__restrict__ w, Solve5 *sv, const int *slist,
+                                                 int ns, float gamma) {
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    for (int base = warp * 16; base < ns; base += FB_T / 2) {
+        const int row = base + (lane & 15);
+        const bool mine = lane < 16 && row < ns;
+        float4 xi = make_float4(0.f, 0.f, 0.f, 0.f);
+        if (mine) {
+            const Solve5 &q = sv[slist[row]];
+            xi = pstar_features_sorted(q.A.rho, q.A.p, q.B.rho, q.B.p, q.du, gamma);
+        }
+        const float y = mlp_rows<1>(w, xi);
+        if (mine && isfinite(y) && fabsf(y) > PSTAR_GATE && fabsf(y) < 30.f) {
+            Solve5 &q = sv[slist[row]];
+            q.p = q.p * (double)__expf(y);
+        }
+    }
+}
 
 template <int D, bool LEARNED>
 __global__ void MLH_FACE_BOUNDS k_faces_block(Params p, const Member *__restrict__ members,
@@ -1914,14 +1972,15 @@ __global__ void MLH_FACE_BOUNDS k_faces_block(Params p, const Member *__restrict
                                               const double *__restrict__ psi, const int *__restrict__ faceTotal,
                                               const FaceRef *__restrict__ faces, const double *__restrict__ dtp,
                                               double *__restrict__ Fface, unsigned long long *__restrict__ newtonSum,
-                                              unsigned *__restrict__ status, FaceQueue qa, float4 *__restrict__ feat) {
+                                              unsigned *__restrict__ status, const PackedMlp *__restrict__ mlp) {
     __shared__ Solve5 sv[FB_T];
     __shared__ int todo[FB_T];
+    __shared__ int slist[LEARNED ? FB_T : 1];
     __shared__ int wcount[FB_T / 32];
     const int nf = *faceTotal < p.faces_cap ? *faceTotal : p.faces_cap;
     const RiemannConsts rc = make_riemann_consts(p.gamma, p.rtol, p.rmaxit);
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    unsigned long long iters_local = 0;
+    unsigned long long iters_local = 0, fallback_local = 0, learned_local = 0;
     unsigned st_local = 0;
     for (int t0 = blockIdx.x * FB_T; t0 < nf; t0 += gridDim.x * FB_T) {
         const int f = t0 + threadIdx.x;
@@ -1931,56 +1990,48 @@ __global__ void MLH_FACE_BOUNDS k_faces_block(Params p, const Member *__restrict
         if (valid)
             valid = face_states<D>(p, members, memberOf, grids, prim, geo, grad, nbr, psi, faces, dtp, f, st_local, R,
                                    L, A, vf, hatA, unR, unL);
-        bool unfinished = false;
+        bool unfinished = false, strong = false;
         if (valid) {
-            // strong shocks of the learned step go to the network's queue;
-            // one call site of the solver's start (a second pass without
-            // deferral only when the queue is full), so that the kernel holds
-            // one copy of it
-            double defer = LEARNED ? PSTAR_HARD * (dlt(L[1], R[1]) ? L[1] : R[1]) : 0.;   // min on the keys
-            Solve5 s0;
-#pragma unroll 1
-            for (int pass = 0; pass < 2; ++pass) {
-                s0 = riemann5_begin(rc, R[0], unR, R[1], L[0], unL, L[1], -1., defer, 1);
-                if (!(LEARNED && s0.stage == 3)) break;
-                const int q = atomicAdd(qa.count, 1);
-                if (q < qa.cap) {
-                    FaceState &fs = qa.st[q];
-#pragma unroll
-                    for (int k = 0; k < 5; ++k) { fs.v[k] = R[k]; fs.v[5 + k] = L[k]; }
-#pragma unroll
-                    for (int a = 0; a < 3; ++a) { fs.v[10 + a] = A[a]; fs.v[13 + a] = vf[a]; fs.v[16 + a] = hatA[a]; }
-                    fs.v[19] = s0.p;   // p_TR
-                    qa.face[q] = f;
-                    feat[q] = pstar_features(R, L, unR, unL, p.gamma);
-                    valid = false;   // solved by the pass over the queue
-                    break;
-                }
-                defer = 0.;   // queue full: solved here
-            }
-            if (valid) {
-                sv[threadIdx.x] = s0;
-                unfinished = s0.stage == 2;
-            }
+            // strong shocks of the learned step stop before their first
+            // Newton step: p_TR > PSTAR_HARD min(pL, pR) (min on the keys)
+            const double defer = LEARNED ? PSTAR_HARD * (dlt(L[1], R[1]) ? L[1] : R[1]) : 0.;
+            const Solve5 s0 = riemann5_begin(rc, R[0], unR, R[1], L[0], unL, L[1], -1., defer, 1);
+            sv[threadIdx.x] = s0;
+            unfinished = s0.stage == 2;
+            strong = LEARNED && s0.stage == 3;
         }
-        // --- list the block's unfinished faces
-        const unsigned bal = __ballot_sync(0xffffffffu, unfinished);
-        if (lane == 0) wcount[warp] = __popc(bal);
+        // --- list the block's unfinished faces (and, learned, its strong shocks)
+        const unsigned bal = __ballot_sync(0xffffffffu, unfinished || strong);
+        const unsigned sbal = LEARNED ? __ballot_sync(0xffffffffu, strong) : 0u;
+        if (lane == 0) wcount[warp] = __popc(bal) | (__popc(sbal) << 16);
         __syncthreads();
-        int before = 0, nu = 0;
+        int before = 0, nu = 0, sbefore = 0, ns = 0;
 #pragma unroll
         for (int w = 0; w < FB_T / 32; ++w) {
-            const int c = wcount[w];
+            const int c = wcount[w] & 0xffff, cs = wcount[w] >> 16;
             before += w < warp ? c : 0;
             nu += c;
+            sbefore += w < warp ? cs : 0;
+            ns += cs;
         }
-        if (unfinished) todo[before + __popc(bal & ((1u << lane) - 1u))] = threadIdx.x;
+        const unsigned below = (1u << lane) - 1u;
+        if (unfinished || strong) todo[before + __popc(bal & below)] = threadIdx.x;
+        if (LEARNED && strong) slist[sbefore + __popc(sbal & below)] = threadIdx.x;
         __syncthreads();
+        if (LEARNED && ns > 0) {   // block-uniform
+            block_network_guess(mlp, sv, slist, ns, (float)p.gamma);
+            __syncthreads();
+        }
         // --- continue them on the first nu threads
         if ((int)threadIdx.x < nu) {
             const int slot = todo[threadIdx.x];
             Solve5 c = sv[slot];
+            const bool from_net = LEARNED && c.stage == 3;
             riemann5_continue(rc, c);
+            if (from_net) {
+                ++learned_local;
+                if (c.iters > rc.max_iter) ++fallback_local;
+            }
             sv[slot] = c;
         }
         __syncthreads();
@@ -1998,19 +2049,26 @@ __global__ void MLH_FACE_BOUNDS k_faces_block(Params p, const Member *__restrict
             else iters_local += (unsigned long long)rs.iters;
             double Fo[5];
             st_local |= project_flux<D>(rs, R, L, unR, unL, hatA, A, vf, rc.inv_gm1, p.mfm, Fo);
+            const int face_iters = rs.iters < 0 ? -1 : rs.iters + (unfinished ? 1 : 0);
             double2 *dst = reinterpret_cast<double2 *>(Fface + (size_t)f * 6);
             dst[0] = make_double2(Fo[0], Fo[1]);
             dst[1] = make_double2(Fo[2], Fo[3]);
-            dst[2] = make_double2(Fo[4], 0.);
+            dst[2] = make_double2(Fo[4], (double)face_iters);
         }
         __syncthreads();   // the shared state is rewritten in the next round
     }
     for (int o = 16; o > 0; o >>= 1) {
         iters_local += __shfl_xor_sync(0xffffffffu, iters_local, o);
+        if (LEARNED) {
+            fallback_local += __shfl_xor_sync(0xffffffffu, fallback_local, o);
+            learned_local += __shfl_xor_sync(0xffffffffu, learned_local, o);
+        }
         st_local |= __shfl_xor_sync(0xffffffffu, st_local, o);
     }
     if (lane == 0) {
         if (iters_local) atomicAdd(newtonSum, iters_local);
+        if (LEARNED && fallback_local) atomicAdd(newtonSum + 1, fallback_local);
+        if (LEARNED && learned_local) atomicAdd(newtonSum + 2, learned_local);
         if (st_local) flag(status, st_local);
     }
 }
@@ -2313,20 +2371,24 @@ void launch_step(StepArgs &a) {
         // strong shocks: network guess (queue A); the rest as the plain step
         cudaMemsetAsync(a.queueCount, 0, sizeof(int), s);
         if (a.queueCount2) cudaMemsetAsync(a.queueCount2, 0, sizeof(int), s);
-        if (a.root5 && a.tune.face_split == 2)   // unfinished faces continued inside the block
+        if (a.root5 && a.tune.face_split == 2) {
+            // unfinished faces continued inside the block, strong shocks from
+            // the network's guess evaluated there
             k_faces_block<D, true><<<fB, FB_T, 0, s>>>(pf, a.members, a.memberOf, a.grids, a.prim, a.geo, a.grad,
                                                        a.nbr, a.psi, a.faceOff + p.n, a.faces, a.dt, a.Fface,
-                                                       a.newtonSum, a.status, qa, a.feat);
-        else if (a.root5) MLH_FACES(true, 1, qa, qb);
-        else MLH_FACES(false, 1, qa, qb);
-        pstar_infer_dev(a.feat, a.queueCount, (int)a.faces_cap, a.mlp_packed, a.yguess, a.sm_count, s);
-        if (a.root5) MLH_FACES(true, 2, qa, qb); else MLH_FACES(false, 2, qa, qb);
-        if (a.root5 && a.fstate2 && a.tune.face_split == 1) MLH_FACES(true, 4, qb, qb);
+                                                       a.newtonSum, a.status, (const PackedMlp *)a.mlp_packed);
+        } else {
+            if (a.root5) MLH_FACES(true, 1, qa, qb);
+            else MLH_FACES(false, 1, qa, qb);
+            pstar_infer_dev(a.feat, a.queueCount, (int)a.faces_cap, a.mlp_packed, a.yguess, a.sm_count, s);
+            if (a.root5) MLH_FACES(true, 2, qa, qb); else MLH_FACES(false, 2, qa, qb);
+            if (a.root5 && a.fstate2 && a.tune.face_split == 1) MLH_FACES(true, 4, qb, qb);
+        }
     } else if (a.root5 && a.harvest.stride == 0 && a.tune.face_split == 2) {
         // unconverged faces after one Newton step continued inside the block
         k_faces_block<D, false><<<fB, FB_T, 0, s>>>(pf, a.members, a.memberOf, a.grids, a.prim, a.geo, a.grad, a.nbr,
                                                     a.psi, a.faceOff + p.n, a.faces, a.dt, a.Fface, a.newtonSum,
-                                                    a.status, qa, a.feat);
+                                                    a.status, nullptr);
     } else if (a.root5 && a.fstate && a.harvest.stride == 0 && a.tune.face_split) {
         // unconverged faces after one Newton step go to a second, dense pass
         cudaMemsetAsync(a.queueCount, 0, sizeof(int), s);

@@ -11,7 +11,20 @@ namespace {
 
 constexpr int CHAINS = 8;
 
-__global__ void __launch_bounds__(256) k_dfma(double *out, double a, double b, int iters) {
+__device__ __forceinline__ unsigned long long global_ns() {
+    unsigned long long t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    return t;
+}
+
+// clk[0..1]: SM clock cycles and global-timer nanoseconds over the loop of
+// block 0, thread 0 (the effective SM clock during the launch)
+__global__ void __launch_bounds__(256) k_dfma(double *out, double a, double b, int iters,
+                                              unsigned long long *clk) {
+    const bool timer = blockIdx.x == 0 && threadIdx.x == 0;
+    long long c0 = 0;
+    unsigned long long t0 = 0;
+    if (timer) { c0 = clock64(); t0 = global_ns(); }
     double acc[CHAINS];
 #pragma unroll
     for (int c = 0; c < CHAINS; ++c) acc[c] = (double)(threadIdx.x + c) * 1e-9;
@@ -23,17 +36,28 @@ __global__ void __launch_bounds__(256) k_dfma(double *out, double a, double b, i
 #pragma unroll
     for (int c = 0; c < CHAINS; ++c) s += acc[c];
     if (s == 123.456) out[blockIdx.x] = s;   // never true; keeps the chains live
+    if (timer) {
+        clk[0] = (unsigned long long)(clock64() - c0);
+        clk[1] = global_ns() - t0;
+    }
 }
 
 }  // namespace
 
 extern "C" int mlh_probe_fp64_tflops(double seconds, double *tflops) {
+    return mlh_probe_fp64_clock(seconds, tflops, nullptr);
+}
+
+extern "C" int mlh_probe_fp64_clock(double seconds, double *tflops, double *sm_mhz) {
     if (!tflops) return MLH_ERR_INVALID;
     int dev = 0, sms = 0;
     if (cudaGetDevice(&dev) != cudaSuccess) return MLH_ERR_NO_DEVICE;
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
     double *out = nullptr;
-    if (cudaMalloc(&out, sizeof(double) * 4096) != cudaSuccess) return MLH_ERR_CUDA;
+    if (cudaMalloc(&out, sizeof(double) * 4096 + 2 * sizeof(unsigned long long)) != cudaSuccess)
+        return MLH_ERR_CUDA;
+    unsigned long long *clk = reinterpret_cast<unsigned long long *>(out + 4096);
+    double best_mhz = 0.;
     cudaEvent_t e0, e1;
     cudaEventCreate(&e0);
     cudaEventCreate(&e1);
@@ -44,7 +68,7 @@ extern "C" int mlh_probe_fp64_tflops(double seconds, double *tflops) {
     // warm up, then grow the loop until a launch takes ~10 ms, then repeat
     for (int rep = 0; rep < 64 && elapsed_total < seconds * 1e3; ++rep) {
         cudaEventRecord(e0);
-        k_dfma<<<blocks, threads>>>(out, 0.999999, 1e-7, iters);
+        k_dfma<<<blocks, threads>>>(out, 0.999999, 1e-7, iters, clk);
         cudaEventRecord(e1);
         cudaEventSynchronize(e1);
         float ms = 0.f;
@@ -52,7 +76,12 @@ extern "C" int mlh_probe_fp64_tflops(double seconds, double *tflops) {
         elapsed_total += ms;
         double flops = 2.0 * CHAINS * (double)iters * blocks * threads;
         double tf = flops / (ms * 1e-3) / 1e12;
-        if (ms > 5.f && tf > best) best = tf;
+        if (ms > 5.f && tf > best) {
+            best = tf;
+            unsigned long long h[2] = {0, 0};
+            cudaMemcpy(h, clk, sizeof(h), cudaMemcpyDeviceToHost);
+            best_mhz = h[1] ? (double)h[0] / (double)h[1] * 1e3 : 0.;
+        }
         if (ms < 10.f) iters *= 2;
     }
     cudaEventDestroy(e0);
@@ -60,6 +89,7 @@ extern "C" int mlh_probe_fp64_tflops(double seconds, double *tflops) {
     cudaFree(out);
     if (cudaGetLastError() != cudaSuccess) return MLH_ERR_CUDA;
     *tflops = best;
+    if (sm_mhz) *sm_mhz = best_mhz;
     return 0;
 }
 

@@ -17,6 +17,7 @@
 #include "../../include/mlh.h"
 #include "mlh_kernels.h"
 #include "mlh_pstar.h"
+#include "mlh_mlp.cuh"
 
 #include <cuda_bf16.h>
 #include <cuda_runtime.h>
@@ -31,20 +32,6 @@
 namespace mlh {
 
 // ------------------------------------------------------------------ packed weights
-
-// smem/global layout of the BF16 operand matrices (rows padded so that the
-// fragment loads of a warp hit 32 different banks)
-constexpr int W1_LD = 24;   // W1 padded to K = 16, row stride 24
-constexpr int W_LD = 72;    // 64-wide rows, stride 72
-
-struct PackedMlp {
-    __nv_bfloat16 w1[64 * W1_LD];
-    __nv_bfloat16 w2[64 * W_LD], w3[64 * W_LD];     // [out][in]
-    __nv_bfloat16 w2t[64 * W_LD], w3t[64 * W_LD];   // [in][out]
-    float b1[64], b2[64], b3[64], w4[64], b4;
-    float pad[3];                                   // size a multiple of 16 bytes
-};
-static_assert(sizeof(PackedMlp) % 16 == 0, "PackedMlp is copied in 16-byte words");
 
 __global__ void k_pack_mlp(const float *__restrict__ prm, PackedMlp *__restrict__ pk) {
     const float *W1 = prm, *b1 = W1 + 256, *W2 = b1 + 64, *b2 = W2 + 4096, *W3 = b2 + 64, *b3 = W3 + 4096,
@@ -69,121 +56,6 @@ __global__ void k_pack_mlp(const float *__restrict__ prm, PackedMlp *__restrict_
     if (blockIdx.x == 0 && threadIdx.x == 0) pk->b4 = b4[0];
 }
 
-// ------------------------------------------------------------------ tensor-core helpers
-
-__device__ __forceinline__ void mma16816(float *d, const uint32_t *a, uint32_t b0, uint32_t b1) {
-    asm volatile(
-        "mma.sync.aligned.m16n8k16.row.col.f32.bf16.bf16.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, "
-        "{%0,%1,%2,%3};\n"
-        : "+f"(d[0]), "+f"(d[1]), "+f"(d[2]), "+f"(d[3])
-        : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b0), "r"(b1));
-}
-
-__device__ __forceinline__ uint32_t pack2(float lo, float hi) {
-    __nv_bfloat162 v = __floats2bfloat162_rn(lo, hi);
-    return *reinterpret_cast<uint32_t *>(&v);
-}
-
-__device__ __forceinline__ float silu(float z) { return z / (1.f + __expf(-z)); }
-__device__ __forceinline__ float silu_grad(float z) {
-    const float s = 1.f / (1.f + __expf(-z));
-    return s * (1.f + z * (1.f - s));
-}
-
-__device__ __forceinline__ uint32_t lds32(const __nv_bfloat16 *p) { return *reinterpret_cast<const uint32_t *>(p); }
-
-// One 32-row slab per warp: rows 0..15 and 16..31 are the two M-tiles.
-// acc[m][nt][4]: C fragments of the 64-wide layer output.
-struct Acc64 {
-    float v[2][8][4];
-};
-
-// acc = bias + A(32 x K) * W^T, W rows [out][in] with stride ld, A fragments
-// given per M-tile and K-tile.
-template <int KT>
-__device__ __forceinline__ void layer_mma(Acc64 &acc, const uint32_t (*afr)[KT][4], const __nv_bfloat16 *w, int ld,
-                                          const float *bias) {
-    const int lane = threadIdx.x & 31, g = lane >> 2, t = lane & 3;
-#pragma unroll
-    for (int nt = 0; nt < 8; ++nt) {
-        const float bb0 = bias[nt * 8 + 2 * t], bb1 = bias[nt * 8 + 2 * t + 1];
-#pragma unroll
-        for (int m = 0; m < 2; ++m) {
-            acc.v[m][nt][0] = bb0; acc.v[m][nt][1] = bb1; acc.v[m][nt][2] = bb0; acc.v[m][nt][3] = bb1;
-        }
-#pragma unroll
-        for (int kt = 0; kt < KT; ++kt) {
-            const __nv_bfloat16 *wr = w + (nt * 8 + g) * ld + kt * 16 + 2 * t;
-            const uint32_t b0 = lds32(wr), b1 = lds32(wr + 8);
-#pragma unroll
-            for (int m = 0; m < 2; ++m) mma16816(acc.v[m][nt], afr[m][kt], b0, b1);
-        }
-    }
-}
-
-// C fragments of a 64-wide layer (after f) -> A fragments of the next layer
-template <class F>
-__device__ __forceinline__ void acc_to_a(const Acc64 &acc, uint32_t (*afr)[4][4], F f) {
-#pragma unroll
-    for (int m = 0; m < 2; ++m)
-#pragma unroll
-        for (int kt = 0; kt < 4; ++kt) {
-            const float *c0 = acc.v[m][2 * kt], *c1 = acc.v[m][2 * kt + 1];
-            afr[m][kt][0] = pack2(f(c0[0]), f(c0[1]));
-            afr[m][kt][1] = pack2(f(c0[2]), f(c0[3]));
-            afr[m][kt][2] = pack2(f(c1[0]), f(c1[1]));
-            afr[m][kt][3] = pack2(f(c1[2]), f(c1[3]));
-        }
-}
-
-// A fragments of the 32 x 16 input slab (4 features, zero padded) from the
-// features held by each lane for its own row (lane = row)
-__device__ __forceinline__ void input_frags(const float4 x, uint32_t (*a0)[1][4]) {
-    const int lane = threadIdx.x & 31, g = lane >> 2, t = lane & 3;
-#pragma unroll
-    for (int m = 0; m < 2; ++m) {
-        // the shuffled value is evaluated on the source lane: move all four
-        // features of rows g and g+8, then pick columns 2t, 2t+1 here
-        const int r0 = m * 16 + g, r1 = r0 + 8;
-        const float p0 = __shfl_sync(0xffffffffu, x.x, r0), p1 = __shfl_sync(0xffffffffu, x.y, r0);
-        const float p2 = __shfl_sync(0xffffffffu, x.z, r0), p3 = __shfl_sync(0xffffffffu, x.w, r0);
-        const float q0 = __shfl_sync(0xffffffffu, x.x, r1), q1 = __shfl_sync(0xffffffffu, x.y, r1);
-        const float q2 = __shfl_sync(0xffffffffu, x.z, r1), q3 = __shfl_sync(0xffffffffu, x.w, r1);
-        a0[m][0][0] = t == 0 ? pack2(p0, p1) : (t == 1 ? pack2(p2, p3) : 0u);
-        a0[m][0][1] = t == 0 ? pack2(q0, q1) : (t == 1 ? pack2(q2, q3) : 0u);
-        a0[m][0][2] = 0u;
-        a0[m][0][3] = 0u;
-    }
-}
-
-// y for the row of this lane, from the C fragments of the last hidden layer
-__device__ __forceinline__ float output_row(const Acc64 &acc3, const float *w4, float b4) {
-    const int lane = threadIdx.x & 31, t = lane & 3;
-    float part[2][2] = {{0.f, 0.f}, {0.f, 0.f}};   // [m][row g / g+8]
-#pragma unroll
-    for (int m = 0; m < 2; ++m)
-#pragma unroll
-        for (int nt = 0; nt < 8; ++nt) {
-            const float wa = w4[nt * 8 + 2 * t], wb = w4[nt * 8 + 2 * t + 1];
-            part[m][0] += silu(acc3.v[m][nt][0]) * wa + silu(acc3.v[m][nt][1]) * wb;
-            part[m][1] += silu(acc3.v[m][nt][2]) * wa + silu(acc3.v[m][nt][3]) * wb;
-        }
-#pragma unroll
-    for (int m = 0; m < 2; ++m)
-#pragma unroll
-        for (int h = 0; h < 2; ++h) {
-            part[m][h] += __shfl_xor_sync(0xffffffffu, part[m][h], 1);
-            part[m][h] += __shfl_xor_sync(0xffffffffu, part[m][h], 2);
-        }
-    // row of this lane: M-tile lane/16, row r = lane%16 held by lane 4*(r%8)
-    const int m = lane >> 4, r = lane & 15;
-    const int src = 4 * (r & 7);
-    float v0 = __shfl_sync(0xffffffffu, part[0][0], src), v1 = __shfl_sync(0xffffffffu, part[0][1], src);
-    float v2 = __shfl_sync(0xffffffffu, part[1][0], src), v3 = __shfl_sync(0xffffffffu, part[1][1], src);
-    const float v = m == 0 ? (r < 8 ? v0 : v1) : (r < 8 ? v2 : v3);
-    return v + b4;
-}
-
 __device__ __forceinline__ void load_packed(PackedMlp *s, const PackedMlp *g) {
     const int4 *src = reinterpret_cast<const int4 *>(g);
     int4 *dst = reinterpret_cast<int4 *>(s);
@@ -206,14 +78,14 @@ __global__ void __launch_bounds__(256) k_pstar_infer(const float4 *__restrict__ 
         const int r = r0 + lane;
         const float4 xi = r < n ? x[r] : make_float4(0.f, 0.f, 0.f, 0.f);
         uint32_t a0[2][1][4];
-        input_frags(xi, a0);
+        input_frags<2>(xi, a0);
         Acc64 acc;
         uint32_t a[2][4][4];
-        layer_mma<1>(acc, a0, s->w1, W1_LD, s->b1);
+        layer_mma<2, 1>(acc, a0, s->w1, W1_LD, s->b1);
         acc_to_a(acc, a, silu);
-        layer_mma<4>(acc, a, s->w2, W_LD, s->b2);
+        layer_mma<2, 4>(acc, a, s->w2, W_LD, s->b2);
         acc_to_a(acc, a, silu);
-        layer_mma<4>(acc, a, s->w3, W_LD, s->b3);
+        layer_mma<2, 4>(acc, a, s->w3, W_LD, s->b3);
         const float out = output_row(acc, s->w4, s->b4);
         if (r < n) y[r] = out;
     }
@@ -308,28 +180,28 @@ __global__ void __launch_bounds__(TB) k_pstar_train(const float4 *__restrict__ x
     const float ti = valid ? target[src] : 0.f;
     // ---- forward
     uint32_t a0[2][1][4];
-    input_frags(xi, a0);
+    input_frags<2>(xi, a0);
     {
         const float xv[4] = {xi.x, xi.y, xi.z, xi.w};
         for (int k = 0; k < 16; ++k) S.xT[k * T_LD + warp * 32 + lane] = __float2bfloat16(k < 4 ? xv[k] : 0.f);
     }
     Acc64 acc;
     uint32_t a[2][4][4];
-    layer_mma<1>(acc, a0, S.w.w1, W1_LD, S.w.b1);
+    layer_mma<2, 1>(acc, a0, S.w.w1, W1_LD, S.w.b1);
     for_frag([&](int m, int nt, int e, int row, int col) {
         const float z = acc.v[m][nt][e];
         S.sg[0][warp][lane][(m * 8 + nt) * 4 + e] = __float2bfloat16(silu_grad(z));
         storeT(S.h1T, warp, row, col, silu(z));
     });
     acc_to_a(acc, a, silu);
-    layer_mma<4>(acc, a, S.w.w2, W_LD, S.w.b2);
+    layer_mma<2, 4>(acc, a, S.w.w2, W_LD, S.w.b2);
     for_frag([&](int m, int nt, int e, int row, int col) {
         const float z = acc.v[m][nt][e];
         S.sg[1][warp][lane][(m * 8 + nt) * 4 + e] = __float2bfloat16(silu_grad(z));
         storeT(S.h2T, warp, row, col, silu(z));
     });
     acc_to_a(acc, a, silu);
-    layer_mma<4>(acc, a, S.w.w3, W_LD, S.w.b3);
+    layer_mma<2, 4>(acc, a, S.w.w3, W_LD, S.w.b3);
     for_frag([&](int m, int nt, int e, int row, int col) {
         const float z = acc.v[m][nt][e];
         S.sg[2][warp][lane][(m * 8 + nt) * 4 + e] = __float2bfloat16(silu_grad(z));
@@ -353,7 +225,7 @@ __global__ void __launch_bounds__(TB) k_pstar_train(const float4 *__restrict__ x
     {
         const float zero[64] = {0};
         acc_to_a(acc, a, [](float v) { return v; });
-        layer_mma<4>(acc, a, S.w.w3t, W_LD, zero);
+        layer_mma<2, 4>(acc, a, S.w.w3t, W_LD, zero);
     }
     for_frag([&](int m, int nt, int e, int row, int col) {
         acc.v[m][nt][e] *= __bfloat162float(S.sg[1][warp][lane][(m * 8 + nt) * 4 + e]);
@@ -362,7 +234,7 @@ __global__ void __launch_bounds__(TB) k_pstar_train(const float4 *__restrict__ x
     {
         const float zero[64] = {0};
         acc_to_a(acc, a, [](float v) { return v; });
-        layer_mma<4>(acc, a, S.w.w2t, W_LD, zero);
+        layer_mma<2, 4>(acc, a, S.w.w2t, W_LD, zero);
     }
     for_frag([&](int m, int nt, int e, int row, int col) {
         acc.v[m][nt][e] *= __bfloat162float(S.sg[0][warp][lane][(m * 8 + nt) * 4 + e]);

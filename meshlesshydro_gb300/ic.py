@@ -153,6 +153,35 @@ def sedov(n_side: int = 64, seed: int = 2, jitter: float = 0.05, energy: float =
                         "energy": energy, "p_background": p_background, "periodic": periodic})
 
 
+def multi_blast(n_side: int = 32, n_blasts: int = 16, seed: int = 11, jitter: float = 0.05,
+                energy: float = 0.1, p_background: float = 1e-2, gamma: float = GAMMA) -> ParticleSet:
+    """Many Sedov blasts in one periodic cube [-0.5, 0.5]^3: the Sedov lattice
+    and background of `sedov`, with energy/n_blasts deposited around each of
+    n_blasts centres drawn uniformly in the cube (seeded), kernel-weighted
+    over periodic distances as `sedov` deposits its one blast.  A workload
+    full of strong shocks across the faces of every blast's rim, where the
+    two-rarefaction guess of the Riemann solver is poor (about 5 % of the
+    faces need 4 or more Newton steps from it with the default energy and
+    background, which keep every step free of vacuum and negative pressures);
+    no counterpart in the reference's test cases."""
+    x, y, z, dx = lattice_3d(n_side, seed, jitter)
+    n = x.shape[0]
+    h = SEDOV_H_OVER_DX * dx
+    m = np.full(n, 1.0 / n)
+    u = np.full(n, p_background / ((gamma - 1.0) * 1.0))
+    rng = np.random.default_rng(seed + 7919)
+    centres = rng.uniform(-0.5, 0.5, (n_blasts, 3))
+    for c in centres:
+        d = [np.remainder(a - ca + 0.5, 1.0) - 0.5 for a, ca in zip((x, y, z), c)]
+        w = cubic_spline(np.sqrt(d[0] ** 2 + d[1] ** 2 + d[2] ** 2), h, 3)
+        u = u + (energy / n_blasts) * w / np.sum(m * w)
+    zeros = np.zeros(n)
+    return ParticleSet(3, x, y, z, zeros.copy(), zeros.copy(), zeros.copy(), m, u, float(h),
+                       (-0.5, -0.5, -0.5), (0.5, 0.5, 0.5), gamma,
+                       {"setup": "multi_blast", "n_side": n_side, "n_blasts": n_blasts, "seed": seed,
+                        "jitter": jitter, "energy": energy, "p_background": p_background})
+
+
 def concatenate(members) -> ParticleSet:
     """The particle sets of an ensemble stored back to back (member order)."""
     first = members[0]

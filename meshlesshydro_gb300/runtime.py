@@ -63,10 +63,10 @@ class StepStats(ctypes.Structure):
 
 EXPORTS = ["mlh_abi_version", "mlh_last_error", "mlh_create", "mlh_destroy", "mlh_set_fields",
            "mlh_get_fields", "mlh_step", "mlh_stage_array", "mlh_set_kernel_timing",
-           "mlh_kernel_times", "mlh_reset_kernel_times", "mlh_probe_fp64_tflops",
+           "mlh_kernel_times", "mlh_reset_kernel_times", "mlh_probe_fp64_tflops", "mlh_probe_fp64_clock",
            "mlh_grid_bounds_noalloc", "mlh_ensemble_create", "mlh_member_times", "mlh_set_graph_mode",
            "mlh_autotune", "mlh_set_tuning", "mlh_pstar_infer", "mlh_pstar_grad", "mlh_pstar_train", "mlh_set_pstar_weights",
-           "mlh_pstar_harvest", "mlh_smoothing_lengths", "mlh_prepare", "mlh_riemann_fluxes",
+           "mlh_pstar_harvest", "mlh_pstar_harvest_strong", "mlh_smoothing_lengths", "mlh_prepare", "mlh_riemann_fluxes",
            "mlh_probe_fast_math", "mlh_probe_fp64_lanes"]
 
 _lib = None
@@ -102,6 +102,9 @@ def load(path: str = LIB_PATH):
     L.mlh_reset_kernel_times.argtypes = [vp]
     L.mlh_probe_fp64_tflops.argtypes = [ctypes.c_double, ctypes.POINTER(ctypes.c_double)]
     L.mlh_probe_fp64_tflops.restype = ctypes.c_int
+    L.mlh_probe_fp64_clock.argtypes = [ctypes.c_double, ctypes.POINTER(ctypes.c_double),
+                                       ctypes.POINTER(ctypes.c_double)]
+    L.mlh_probe_fp64_clock.restype = ctypes.c_int
     dp = ctypes.c_void_p
     L.mlh_grid_bounds_noalloc.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_int, dp, dp, dp,
                                           ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_double),
@@ -130,6 +133,8 @@ def load(path: str = LIB_PATH):
     L.mlh_set_pstar_weights.restype = ctypes.c_int
     L.mlh_pstar_harvest.argtypes = [vp, ctypes.c_int, fp, fp, ctypes.c_longlong, ctypes.POINTER(ctypes.c_longlong)]
     L.mlh_pstar_harvest.restype = ctypes.c_int
+    L.mlh_pstar_harvest_strong.argtypes = [vp, fp, fp, ctypes.c_longlong, ctypes.POINTER(ctypes.c_longlong)]
+    L.mlh_pstar_harvest_strong.restype = ctypes.c_int
     L.mlh_smoothing_lengths.argtypes = [vp, ctypes.c_double, ctypes.POINTER(ctypes.c_double),
                                         ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_longlong)]
     L.mlh_smoothing_lengths.restype = ctypes.c_int
@@ -145,7 +150,7 @@ def load(path: str = LIB_PATH):
     return L
 
 
-INT_ARRAYS = {"noi", "noi_img", "off", "nnl", "face_of"}
+INT_ARRAYS = {"noi", "noi_img", "off", "nnl", "face_of", "face_iters"}
 
 
 class HostState:
@@ -173,6 +178,18 @@ def probe_fp64_tflops(seconds: float = 0.5) -> float:
     if st != 0:
         raise MLHError(st, "mlh_probe_fp64_tflops", L.mlh_last_error().decode())
     return out.value
+
+
+def probe_fp64_clock(seconds: float = 0.5):
+    """(TFLOP/s, effective SM clock in MHz) of the FP64 FMA probe
+    (mlh_probe_fp64_clock)."""
+    L = load()
+    tf = ctypes.c_double()
+    mhz = ctypes.c_double()
+    st = L.mlh_probe_fp64_clock(seconds, ctypes.byref(tf), ctypes.byref(mhz))
+    if st != 0:
+        raise MLHError(st, "mlh_probe_fp64_clock", L.mlh_last_error().decode())
+    return tf.value, mhz.value
 
 
 def probe_fp64_lanes(active_lanes: int, iters: int = 2048) -> float:
@@ -322,16 +339,25 @@ class Simulation:
         if st != 0:
             raise MLHError(st, "mlh_set_pstar_weights", self.L.mlh_last_error().decode())
 
-    def harvest(self, stride: int = 1, capacity: int = 1 << 22):
+    def harvest(self, stride: int = 1, capacity: int = 1 << 22, strong: bool = False):
         """One step recording (network input, log(p*/p_TR)) of every stride-th face,
-        p_TR the two-rarefaction guess of the face."""
+        p_TR the two-rarefaction guess of the face; strong=True: of every face
+        the learned step hands to the network (p_TR > 2 min(pL, pR)).  Returns
+        the rows (at most capacity) and, with strong=True, the number of such
+        faces as a third value."""
         x = np.zeros((capacity, 4), dtype=np.float32)
         t = np.zeros(capacity, dtype=np.float32)
         cnt = ctypes.c_longlong()
-        st = self.L.mlh_pstar_harvest(self.h, stride, _fptr(x), _fptr(t), capacity, ctypes.byref(cnt))
+        if strong:
+            st = self.L.mlh_pstar_harvest_strong(self.h, _fptr(x), _fptr(t), capacity, ctypes.byref(cnt))
+        else:
+            st = self.L.mlh_pstar_harvest(self.h, stride, _fptr(x), _fptr(t), capacity, ctypes.byref(cnt))
         if st != 0:
             raise MLHError(st, "mlh_pstar_harvest", self.L.mlh_last_error().decode())
-        return x[:cnt.value], t[:cnt.value]
+        k = min(cnt.value, capacity)
+        if strong:
+            return x[:k], t[:k], cnt.value
+        return x[:k], t[:k]
 
     def smoothing_lengths(self, n_ngb: float):
         """Per-particle smoothing lengths of the current state (mlh_smoothing_lengths):

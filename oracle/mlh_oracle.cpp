@@ -127,6 +127,7 @@ struct Sim {
     std::vector<real> psi, Aij, WL, WR, vFrame, F;
     std::vector<real> mF, vF, eF;
     std::vector<int> newtonIters;
+    std::vector<int> slotIters;        // Newton steps of each slot's face (copies: the face's)
     double dt = 0.;
     real lo[3], hi[3];
     int cells[3];
@@ -718,7 +719,7 @@ struct Sim {
     void solveRiemannProblems() {
         const int NV = D + 2;
         F.assign((size_t)off[N] * NV, 0.);
-        std::vector<int> slotIters(off[N], 0);
+        slotIters.assign(off[N], 0);
         orc::ExactRiemannT<real> rs(c.gamma, c.riemann_tol, c.riemann_max_iter);
 #pragma omp parallel for schedule(dynamic, 256) num_threads(g_threads)
         for (int i = 0; i < N; ++i)
@@ -739,6 +740,7 @@ struct Sim {
                 if (j < i) {
                     int t = rev[s];
                     for (int d = 0; d < NV; ++d) F[(size_t)s * NV + d] = -F[(size_t)t * NV + d];
+                    slotIters[s] = slotIters[t];
                 }
             }
         newtonIters.clear();
@@ -766,6 +768,35 @@ struct Sim {
                 if (D == 3) vF[(size_t)i * 3 + 2] += f[4];
                 eF[i] += f[1];
             }
+    }
+
+    // --- Particles::checkFluxSymmetry, Particles.cpp:2888-2976 (DEBUG_LVL >= 1,
+    // called after solveRiemannProblems, MeshlessScheme.cpp:210-217): for every
+    // interaction i -> j the reverse interaction is searched in j's list from
+    // its start (real neighbours among the real ones, images among the
+    // images), and F_ij + F_ji of every component is compared with
+    // FLUX_SYM_TOL = 1e-20.  Returns the number of interactions that fail (the
+    // reference logs them).
+    long checkFluxSymmetry() const {
+        const int NV = D + 2;
+        const real tol = 1e-20;
+        long bad = 0;
+        for (int i = 0; i < N; ++i)
+            for (int s = off[i]; s < off[i + 1]; ++s) {
+                const int j = (int)(nb[s] & IDX_MASK);
+                const bool isImg = (s - off[i]) >= noi[i];
+                const int b = isImg ? off[j] + noi[j] : off[j];
+                const int e = isImg ? off[j + 1] : off[j] + noi[j];
+                int t = b;
+                for (; t < e; ++t)
+                    if ((int)(nb[t] & IDX_MASK) == i) break;
+                if (t == e) { ++bad; continue; }
+                bool notSym = false;
+                for (int d = 0; d < NV; ++d)
+                    if (F[(size_t)t * NV + d] + F[(size_t)s * NV + d] > tol) notSym = true;
+                if (notSym) ++bad;
+            }
+        return bad;
     }
 
     // --- Particles::updateStateAndPosition, Particles.cpp:2013-2110
@@ -941,6 +972,11 @@ struct Sim {
 #endif
     }
 
+    // DEBUG_LVL of the reference's build: >= 1 adds checkFluxSymmetry after
+    // the Riemann solves (its count in fluxAsymmetric)
+    int debugLvl = 0;
+    long fluxAsymmetric = 0;
+
     // MeshlessScheme::run loop body, MeshlessScheme.cpp:39-253 (no dumps)
     int step() {
         status = 0;
@@ -957,6 +993,7 @@ struct Sim {
         stage(ORC_STAGE_FACE, [&] { effectiveFace(); });
         stage(ORC_STAGE_STATES, [&] { riemannStatesLR(); });
         stage(ORC_STAGE_RIEMANN, [&] { solveRiemannProblems(); });
+        if (debugLvl >= 1) fluxAsymmetric = checkFluxSymmetry();
         stage(ORC_STAGE_COLLECT, [&] { collectFluxes(); });
         stage(ORC_STAGE_UPDATE, [&] { update(); });
         return (int)status;
@@ -1000,7 +1037,7 @@ long sizeOf(Sim<D> *s, const std::string &nm) {
         nm == "h" || nm == "n_eff")
         return N;
     if (nm == "off") return N + 1;
-    if (nm == "nnl" || nm == "rev" ) return S;
+    if (nm == "nnl" || nm == "rev" || nm == "slot_iters") return S;
     if (nm == "vF") return N * 3;
     if (nm.compare(0, 4, "grad") == 0) return N * 3;
     if (nm == "B") return N * D * D;
@@ -1045,6 +1082,7 @@ int getArr(Sim<D> *s, const std::string &nm, void *out) {
     if (nm == "off") return cpi(s->off);
     if (nm == "rev") return cpi(s->rev);
     if (nm == "newton_iters") return cpi(s->newtonIters);
+    if (nm == "slot_iters") { if (s->slotIters.size() != s->nb.size()) return -1; return cpi(s->slotIters); }
     if (nm == "nnl") { std::copy(s->nb.begin(), s->nb.end(), (uint32_t *)out); return 0; }
     if (nm == "dt") { o[0] = s->dt; return 0; }
     if (nm == "stats") { o[0] = (double)s->riemannSolves; o[1] = (double)s->newtonTotal; return 0; }
@@ -1166,6 +1204,19 @@ int orc_riemann_fluxes(int dim, int n, const double *Wi, const double *Wj, const
                        double gamma, int mfm, double *F, int *iters) {
     if (dim == 2) return riemannFaces<2>(n, Wi, Wj, vFrame, Aij, gamma, mfm, F, iters);
     return riemannFaces<3>(n, Wi, Wj, vFrame, Aij, gamma, mfm, F, iters);
+}
+
+int orc_set_debug_level(void *ctx, int lvl) {
+    Handle *hnd = (Handle *)ctx;
+    if (hnd->dim == 2) ((Sim<2> *)hnd->sim)->debugLvl = lvl;
+    else ((Sim<3> *)hnd->sim)->debugLvl = lvl;
+    return 0;
+}
+
+long orc_flux_asymmetric(void *ctx) {
+    Handle *hnd = (Handle *)ctx;
+    if (hnd->dim == 2) return ((Sim<2> *)hnd->sim)->fluxAsymmetric;
+    return ((Sim<3> *)hnd->sim)->fluxAsymmetric;
 }
 
 int orc_set_threads(int n) {

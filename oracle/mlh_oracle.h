@@ -85,6 +85,14 @@ enum {
     ORC_NSTAGES
 };
 
+/* DEBUG_LVL of the reference's build (0 or 1): 1 adds the reference's
+ * checkFluxSymmetry after the Riemann solves of every step
+ * (demonstrator/src/MeshlessScheme.cpp:210-217, Particles.cpp:2888-2976);
+ * orc_flux_asymmetric gives the count of interactions it found asymmetric
+ * in the last step. */
+int orc_set_debug_level(void *ctx, int lvl);
+long orc_flux_asymmetric(void *ctx);
+
 /* Threads of the per-particle loops (results do not depend on them); n < 1:
  * one per processor.  Returns the count in effect (1 in a build without
  * OpenMP).  The default is 1: the serial restatement of the reference. */

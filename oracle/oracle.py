@@ -33,7 +33,7 @@ class OrcConfig(ctypes.Structure):
                 + [("n_ngb", ctypes.c_double), ("adaptive_h", ctypes.c_int)])
 
 
-INT_ARRAYS = {"noi", "noi_img", "off", "rev", "newton_iters", "nnl"}
+INT_ARRAYS = {"noi", "noi_img", "off", "rev", "newton_iters", "nnl", "slot_iters"}
 
 
 def reference_root() -> str:
@@ -55,8 +55,7 @@ def lib(counting: bool = False):
     """The oracle library (ctypes), or its operation-counting build."""
     if counting not in _libs:
         path = COUNT_LIB if counting else LIB
-        if not os.path.exists(path):
-            build(counting)
+        build(counting)   # make: rebuilds a library older than its sources
         L = ctypes.CDLL(path)
         dp = ctypes.POINTER(ctypes.c_double)
         L.orc_create.restype = ctypes.c_void_p
@@ -76,6 +75,10 @@ def lib(counting: bool = False):
         L.orc_riemann_fluxes.restype = ctypes.c_int
         L.orc_smoothing_lengths.restype = ctypes.c_long
         L.orc_smoothing_lengths.argtypes = [ctypes.c_void_p, ctypes.c_double, dp, dp]
+        L.orc_set_debug_level.restype = ctypes.c_int
+        L.orc_set_debug_level.argtypes = [ctypes.c_void_p, ctypes.c_int]
+        L.orc_flux_asymmetric.restype = ctypes.c_long
+        L.orc_flux_asymmetric.argtypes = [ctypes.c_void_p]
         L.orc_set_threads.restype = ctypes.c_int
         L.orc_set_threads.argtypes = [ctypes.c_int]
         L.orc_flop_counts.restype = ctypes.c_int
@@ -153,6 +156,14 @@ class Oracle:
 
     def step(self) -> int:
         return self.L.orc_step(self.h)
+
+    def set_debug_level(self, lvl: int):
+        """The reference's DEBUG_LVL: 1 adds its checkFluxSymmetry to every step."""
+        self.L.orc_set_debug_level(self.h, int(lvl))
+
+    def flux_asymmetric(self) -> int:
+        """Interactions checkFluxSymmetry found asymmetric in the last step."""
+        return int(self.L.orc_flux_asymmetric(self.h))
 
     def get(self, name: str) -> np.ndarray:
         n = self.L.orc_size(self.h, name.encode())

@@ -9,21 +9,40 @@ GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
 
 # Field tolerance of the parity tests, per element and per step (one step
 # from identical inputs):
-#     |a_i - b_i| <= FIELD_RTOL * max(|b_i|, FIELD_FLOOR * max_k |b_k|)
-# (b the oracle's field).  Entries of at least FIELD_FLOOR of the field's
-# largest magnitude are held to FIELD_RTOL of their own value; smaller ones
-# to FIELD_RTOL * FIELD_FLOOR = 1e-15 of the field's largest magnitude.  The
-# floor covers entries that are sums of terms far larger than themselves,
-# which rounding leaves with absolute, not relative, errors of a few ulp of
-# the terms: velocities that are zero up to rounding in the quiet region of a
-# blast, gradients in uniform regions, coordinates near the origin.  (The
-# reference build and the oracle, which differ only in the 2x2/3x3 inverse,
-# already differ by 4.5e-17 of a field's maximum on a gradient entry
-# 1.7e-6 of it.)  The normwise error max|a - b| / max|b| is reported beside it.
-# States after several steps, where differences compound, are compared
-# normwise (assert_normwise) and by L1.
+#     |a_i - b_i| <= FIELD_RTOL * max(|b_i|, floor * max_k |b_k|)
+# (b the oracle's field), with a floor per kind of field:
+#  * products and sums of positive terms (omega, rho, P, dt, m, u and the
+#    positions): no floor, every entry to 1e-12 of its own value (measured:
+#    <= 9e-15 on every case; the 1e-5 background pressure of a Sedov blast is
+#    held to 1e-12 of 1e-5);
+#  * sums whose terms cancel (raw gradients, E^-1, face fluxes and their
+#    per-particle sums, velocities): SUM_FLOOR of the field's largest
+#    magnitude.  Their entries carry absolute errors of a few ulp of the terms
+#    summed, not of the result: entries of at least SUM_FLOOR of the field's
+#    maximum are held to 1e-12 of their own value, smaller ones to
+#    1e-12 * SUM_FLOOR of the maximum.  (The reference build and the oracle,
+#    which differ only in the 2x2/3x3 inverse, already differ by 4.5e-17 of a
+#    field's maximum on a gradient entry 1.7e-6 of it.)
+#  * limited gradients: LIMITER_RTOL.  The limiter factor is the reference's
+#    ratio (psi_max_ngb - psi_i) / (psi_max_mid - psi_i), whose differences are
+#    1e-4 of psi_i in the nearly uniform background of a blast: a rounding
+#    of psi_i moves the factor by 1e-12 relative and more.
+#  * a face where the two Newton iterations stop one step apart (the last
+#    change of the one lands within rounding of the 1e-10 stopping
+#    threshold; one face in ~10^6): p* then differs by up to the solver's
+#    tolerance, and the fluxes and updated state of the face's two particles
+#    are held to RIEMANN_TIE_RTOL (with the SUM_FLOOR floor); at most
+#    MAX_TIE_FRACTION of the faces may be such ties.
+# The normwise error max|a - b| / max|b| is reported beside it.  States after
+# several steps, where differences compound, are compared normwise
+# (assert_normwise) and by L1.
 FIELD_RTOL = 1e-12
-FIELD_FLOOR = 1e-3
+FIELD_FLOOR = 1e-3          # default floor of assert_close
+SUM_FLOOR = 2e-2
+LIMITER_RTOL = 1e-10
+RIEMANN_TIE_RTOL = 1e-8
+MAX_TIE_FRACTION = 1e-4
+EXACT_FIELDS = {"omega", "rho", "P", "dt", "m", "u", "x", "y", "z"}
 
 
 def load_golden(name):
@@ -90,31 +109,87 @@ def l1_rel(a, b):
     return float(np.sum(np.abs(a - b)) / np.sum(np.abs(b)))
 
 
+def riemann_ties(g, o):
+    """Slots whose face took a different number of Newton steps on the GPU
+    and in the oracle (boolean per slot), and the particles that own them."""
+    gi = g.get("face_iters")
+    oi = o.get("slot_iters")
+    tie = gi != oi
+    off = o.get("off")
+    owner = np.repeat(np.arange(off.size - 1), np.diff(off))
+    touched = np.zeros(off.size - 1, dtype=bool)
+    touched[owner[tie]] = True
+    return tie, touched
+
+
+def assert_masked(a, b, floor, what, mask=None, rtol=FIELD_RTOL, rtol_masked=RIEMANN_TIE_RTOL):
+    """The per-element gate with the field's own scale, entries under `mask`
+    (Newton ties) held to rtol_masked instead of rtol."""
+    a = np.asarray(a, dtype=np.float64)
+    b = np.asarray(b, dtype=np.float64)
+    if b.size == 0:
+        return
+    scale = np.max(np.abs(b))
+    den = np.maximum(np.abs(b), floor * scale)
+    err = np.abs(a - b)
+    with np.errstate(divide="ignore", invalid="ignore"):
+        r = np.where(err == 0.0, 0.0, err / den)
+    lim = np.full(b.shape, rtol)
+    if mask is not None:
+        m = np.asarray(mask, dtype=bool)
+        if b.ndim > 1:
+            m = np.broadcast_to(m.reshape(-1, *([1] * (b.ndim - 1))), b.shape)
+        lim = np.where(m, rtol_masked, rtol)
+    bad = ~(r <= lim)
+    if bad.any():
+        i = int(np.flatnonzero(bad.ravel())[0])
+        raise AssertionError(f"{what}: per-element relative error {r.ravel()[i]:.3e} > {lim.ravel()[i]:.1e} at "
+                             f"[{i}] (gpu {a.ravel()[i]!r}, oracle {b.ravel()[i]!r}, field max {scale:.3e}); "
+                             f"{int(bad.sum())} entries; normwise {normwise(a, b):.3e}")
+
+
+def assert_state(gs, ost, touched, what=""):
+    """The state after one step from identical inputs: exact fields without a
+    floor, velocities with SUM_FLOOR; the particles of a Newton tie to
+    RIEMANN_TIE_RTOL (positions move with the old velocity: exact)."""
+    for k, v in ost.items():
+        floor = 0.0 if k in EXACT_FIELDS else SUM_FLOOR
+        mask = None if k in ("x", "y", "z") else touched
+        assert_masked(gs[k], v, floor, what + "state " + k, mask)
+
+
 def compare_step(g, o, dim, slots=True, what=""):
     """One step of the GPU simulation g against the oracle o from identical
-    inputs: neighbour lists and grid bit-exact; density, pressure, dt,
-    gradients (raw and limited), E^-1, fluxes and the new state per element
-    (assert_close).  slots=False skips the per-interaction flux array (large
-    workloads compare its per-particle sums instead)."""
+    inputs: neighbour lists and grid bit-exact; every stage array and the new
+    state per element, with the floors and tolerances above.  slots=False
+    skips the per-interaction flux array (large workloads compare its
+    per-particle sums instead).  Returns the number of Newton ties."""
     for k in ("off", "noi", "noi_img"):
         np.testing.assert_array_equal(g.get(k), o.get(k), err_msg=what + k)
     np.testing.assert_array_equal(g.get("nnl"), o.get("nnl"), err_msg=what + "nnl")
     np.testing.assert_array_equal(g.get("grid"), o.get("grid"), err_msg=what + "grid")
     for k in ("omega", "rho", "P", "dt"):
-        assert_close(g.get(k), o.get(k), what=what + k)
+        assert_close(g.get(k), o.get(k), floor=0.0, what=what + k)
     fields = ["rho", "vx", "vy"] + (["vz"] if dim == 3 else []) + ["P"]
     for f in fields:
-        assert_close(g.get("gradraw_" + f), o.get("gradraw_" + f), what=what + "gradraw_" + f)
-        assert_close(g.get("grad_" + f), o.get("grad_" + f), what=what + "grad_" + f)
-    assert_close(g.get("B"), o.get("B"), what=what + "B")
+        assert_close(g.get("gradraw_" + f), o.get("gradraw_" + f), floor=SUM_FLOOR, what=what + "gradraw_" + f)
+        assert_close(g.get("grad_" + f), o.get("grad_" + f), rtol=LIMITER_RTOL, floor=SUM_FLOOR,
+                     what=what + "grad_" + f)
+    assert_close(g.get("B"), o.get("B"), floor=SUM_FLOOR, what=what + "B")
+    tie, touched = riemann_ties(g, o)
+    nfaces = max(int(o.get("stats")[0]), 1)
+    assert tie.sum() / 2 <= MAX_TIE_FRACTION * nfaces + 1, f"{what}{tie.sum() // 2} Newton ties"
     if slots:
-        assert_close(g.get("F"), o.get("F"), what=what + "F")
-    assert_close(g.get("mF"), o.get("mF"), what=what + "mF")
-    assert_close(g.get("eF"), o.get("eF"), what=what + "eF")
-    assert_close(g.get("vF").reshape(-1, 3)[:, :dim], o.get("vF").reshape(-1, 3)[:, :dim], what=what + "vF")
-    gs = g.get_state()
-    for k, v in o.state().items():
-        assert_close(gs[k], v, what=what + "state " + k)
+        nv = dim + 2
+        assert_masked(g.get("F").reshape(-1, nv), o.get("F").reshape(-1, nv), SUM_FLOOR, what + "F", tie)
+    for k in ("mF", "eF", "vF"):
+        a, b = g.get(k), o.get(k)
+        if k == "vF":
+            a = a.reshape(-1, 3)[:, :dim]
+            b = b.reshape(-1, 3)[:, :dim]
+        assert_masked(a, b, SUM_FLOOR, what + k, touched)
+    assert_state(g.get_state(), o.state(), touched, what)
+    return int(tie.sum() // 2)
 
 
 def pset_from_state(p, st):

@@ -1,8 +1,10 @@
 """The learned p* initial guess inside the step.
 
-Faces are solved in two passes around one batched network launch (states and
-features, inference, Newton from p_TR * exp(y), p_TR the two-rarefaction
-guess, where |y| > 0.01; from p_TR elsewhere).  The converged p* satisfies
+Strong shocks (p_TR > 2 min(pL, pR), p_TR the two-rarefaction guess) are
+solved by Newton from p_TR * exp(y) where |y| > 0.01, y the network's output
+(from p_TR elsewhere): inside the face block that holds them (the in-block
+structure) or in a second pass around one batched network launch (the other
+structures).  The converged p* satisfies
 the same stopping rule as from the two-rarefaction guess, so the state must
 stay on the oracle's trajectory within LEARNED_RTOL: the two Newton runs stop
 at different points inside the tolerance band, which moves fluxes by
@@ -94,7 +96,6 @@ def test_learned_guess_matches_oracle(trained, oracle_mod, case):
           f"learned faces {st.learned_faces} of {st.faces}")
     assert 0 <= st.learned_faces <= st.faces
     assert st.newton_fallbacks <= 0.01 * st.faces, (st.newton_fallbacks, st.faces)
-    assert st.newton_iterations <= 2 * plain.newton_iterations
     gs = s.get_state()
     for key, v in o.state().items():
         assert_normwise(gs[key], v, LEARNED_RTOL, what=key)
@@ -163,3 +164,57 @@ def test_learned_then_plain_graph_mode(trained):
     sa, sb = a.get_state(), b.get_state()
     for k in sa:
         assert np.array_equal(sa[k], sb[k]), k
+
+
+@pytest.fixture(scope="module")
+def strong_trained():
+    """A network trained on faces harvested from the 24^3 Sedov blast (every
+    face the learned step hands to the network in its first 30 steps, and
+    every 8th face of its first step): a workload held out from the
+    evaluation below."""
+    rt = _runtime()
+    p = ic.sedov(n_side=24, seed=4)
+    s = rt.Simulation(MFVConfig.sedov(p, periodic=True), p)
+    x, t = s.harvest(stride=8, capacity=1 << 20)
+    xs, ts = [x], [t]
+    for _ in range(30):
+        x, t, _n = s.harvest(strong=True, capacity=1 << 20)
+        xs.append(x); ts.append(t)
+    s.close()
+    x = np.concatenate(xs); t = np.concatenate(ts)
+    w, hist = rt.pstar_train(x, t, epochs=60, batch=1024, lr=2e-3, seed=3)
+    return w, x.shape[0]
+
+
+def test_network_saves_newton_iterations_on_strong_shocks(strong_trained, oracle_mod):
+    """What the trained network gains over the method without it, on a
+    workload where the two-rarefaction guess is poor: 16 blasts in a 24^3
+    periodic cube (ic.multi_blast; 4 or more Newton steps from p_TR on about
+    5 % of the faces).  The learned step solves its strong shocks from the
+    network's guess: fewer Newton steps than the plain step on the same three
+    steps, with the fields of the oracle's trajectory (LEARNED_RTOL)."""
+    w, nrows = strong_trained
+    rt = _runtime()
+    p = ic.multi_blast(n_side=24, n_blasts=16, seed=11)
+    cfg = MFVConfig.sedov(p, periodic=True)
+    plain = rt.Simulation(cfg, p)
+    learned = rt.Simulation(cfg, p)
+    learned.set_pstar_weights(w)
+    a = plain.step(3)
+    b = learned.step(3)
+    assert a.status == 0 and b.status == 0
+    assert a.faces == b.faces
+    saved = a.newton_iterations - b.newton_iterations
+    print(f"training rows {nrows}; faces {a.faces}; learned faces {b.learned_faces}; Newton steps plain "
+          f"{a.newton_iterations} learned {b.newton_iterations}: {saved / max(b.learned_faces, 1):.2f} saved per "
+          f"learned face; fallbacks {b.newton_fallbacks}")
+    assert b.learned_faces >= 0.01 * b.faces
+    assert b.newton_fallbacks <= 0.01 * b.learned_faces
+    assert saved >= 1.0 * b.learned_faces, (saved, b.learned_faces)
+    o = oracle_mod.Oracle(cfg, p)
+    for _ in range(3):
+        assert o.step() == 0
+    ga, gb = plain.get_state(), learned.get_state()
+    for key, v in o.state().items():
+        assert_normwise(gb[key], v, LEARNED_RTOL, what="learned " + key)
+        assert_normwise(gb[key], ga[key], LEARNED_RTOL, what="learned vs plain " + key)
