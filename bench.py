@@ -345,10 +345,10 @@ def train_learned_guess(runtime, budget_rows: int = 10_000_000, epochs: int = 12
     s = runtime.Simulation(MFVConfig.sedov(p, periodic=True), p)
     for k in range(100):
         if k % 25 == 0:
-            x, t = s.harvest(stride=4, capacity=1 << 21)
+            x, t = s.harvest(stride=4, capacity=1 << 21, check=False)
             n_sedov += x.shape[0]
         else:
-            x, t, _ = s.harvest(strong=True, capacity=1 << 20)
+            x, t, _ = s.harvest(strong=True, capacity=1 << 20, check=False)
             n_strong += x.shape[0]
         xs.append(x); ts.append(t)
     s.close()
@@ -356,7 +356,7 @@ def train_learned_guess(runtime, budget_rows: int = 10_000_000, epochs: int = 12
     s = runtime.Simulation(MFVConfig.kelvin_helmholtz(q), q)
     for k in range(100):
         if k % 5 == 0:
-            x, t = s.harvest(stride=1, capacity=1 << 18)
+            x, t = s.harvest(stride=1, capacity=1 << 18, check=False)
             xs.append(x); ts.append(t)
             n_kh += x.shape[0]
         else:
@@ -382,10 +382,10 @@ def network_error(runtime, w, sim_factory):
     held-out faces: every strong shock and every 64th face of one step of a
     fresh simulation of the evaluated workload."""
     s = sim_factory()
-    xs, ts, n = s.harvest(strong=True, capacity=1 << 21)
+    xs, ts, n = s.harvest(strong=True, capacity=1 << 21, check=False)
     s.close()
     s = sim_factory()
-    xa, ta = s.harvest(stride=64, capacity=1 << 21)
+    xa, ta = s.harvest(stride=64, capacity=1 << 21, check=False)
     s.close()
     out = {}
     for name, (x, t) in (("strong", (xs, ts)), ("all_every_64th", (xa, ta))):

@@ -149,19 +149,27 @@ typedef struct mlh_tuning {
     int link_overlap;        /* 1: the face links run on a second stream beside
                               * the time step and the gradients; 0: in order
                               * on the step's stream */
+    int persistent_binning;  /* 1: the binning (bounds, grid, cell assignment,
+                              * counts, scan, cell lists) as one persistent
+                              * cooperative kernel whose phases wait on one
+                              * another at bounded grid barriers (a wait that
+                              * runs out sets MLH_ERR_TIMEOUT and the step
+                              * leaves the state untouched); 0: one launch per
+                              * phase */
 } mlh_tuning;
 
 /* Autotuner: times the face-pass structures over candidate grids, then
  * candidate launch shapes of the face, gradient and neighbour kernels, then
- * whole steps with and without the overlapped face links, over
+ * whole steps with and without the overlapped face links and with and
+ * without the persistent binning, over
  * `trial_steps` steps each (from a saved copy of the
  * state, which is restored afterwards), keeps the fastest in the context and
  * reports them in *out (may be NULL).  Needs one state-sized temporary. */
 int mlh_autotune(mlh_ctx *ctx, int trial_steps, mlh_tuning *out);
 /* Set the launch shapes directly (for example those an autotuned context of
  * the same workload reported).  Threads per block: 64, 128 or 256; blocks
- * per SM 1..32; warps per SM 8..256; face_split 0, 1 or 2; link_overlap 0 or
- * 1.  MLH_ERR_INVALID otherwise. */
+ * per SM 1..32; warps per SM 8..256; face_split 0, 1 or 2; link_overlap and
+ * persistent_binning 0 or 1.  MLH_ERR_INVALID otherwise. */
 int mlh_set_tuning(mlh_ctx *ctx, const mlh_tuning *tuning);
 
 /* Per-particle smoothing lengths of the current state (no counterpart in the
@@ -265,6 +273,13 @@ int mlh_probe_fp64_clock(double seconds, double *tflops, double *sm_mhz);
  * for n host values: rcp = 1/x, quot = y/x, rsqrt = 1/sqrt(x); for checking
  * their error against exact values. */
 int mlh_probe_fast_math(int n, const double *x, const double *y, double *rcp, double *quot, double *rsqrt);
+
+/* TEST HOOK.  The grid barriers of the persistent binning wait for
+ * `extra_arrivals` more blocks than the launch holds (nonzero: every wait runs
+ * out, which no correct launch can make happen) and give up after
+ * `spin_limit` polls (0: the default, about half a second).  For testing the
+ * timeout path; 0, 0 restores the defaults. */
+int mlh_test_binning_barrier(mlh_ctx *ctx, unsigned extra_arrivals, unsigned spin_limit);
 
 /* TEST HOOK.  Device time (ms, best of three launches) of the FMA chains of
  * mlh_probe_fp64_tflops run by only the first active_lanes (1..32) lanes of

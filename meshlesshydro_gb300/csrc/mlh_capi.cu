@@ -113,6 +113,11 @@ struct mlh_ctx {
     bool graph_mode = false;
     cudaGraphExec_t graph_exec = nullptr;
     double graph_dt_max = -1.;
+    // persistent binning: grid-barrier words, resident blocks, test-hook
+    // settings of the barriers
+    unsigned *bar = nullptr;
+    int bin_blocks = 0;
+    unsigned bar_extra = 0, bar_spin = 0;
     // kernel timing
     bool timing = false;
     std::vector<cudaEvent_t> tev;   // pairs, in launch order
@@ -180,6 +185,10 @@ int alloc_cell_buffers(mlh_ctx *c) {
     CK(dalloc(&c->cellCount, nc));
     CK(dalloc(&c->cellStart, nc + 1));
     CK(dalloc(&c->cellFill, nc));
+    // tile sums of the scans over the cell counts and over the particles
+    cudaFree(c->scanTiles);
+    const size_t m = nc > (size_t)c->n ? nc : (size_t)c->n;
+    CK(dalloc(&c->scanTiles, m / 4096 + 1024));
     return 0;
 }
 
@@ -284,6 +293,10 @@ StepArgs make_args(mlh_ctx *c, double dt_max) {
     a.queueFace = c->queueFace; a.queueCount = c->queueCount; a.mlp_packed = c->mlp_packed;
     a.fstate2 = c->fstate2; a.queueFace2 = c->queueFace2; a.queueCount2 = c->queueCount2;
     a.harvest = c->harvest;
+    a.bar = c->bar;
+    a.bin_blocks = c->bin_blocks;
+    a.bar_extra = c->bar_extra;
+    a.bar_spin = c->bar_spin ? c->bar_spin : (1u << 21);   // polls of ~0.3 us: about half a second
     a.hp = c->hp; a.neff = c->neff; a.hstat = c->hstat; a.hpf = c->hpf;
     a.p.hp = c->hp; a.p.hpf = c->hpf;
     a.timer = c->timing ? timer_cb : nullptr;
@@ -429,7 +442,8 @@ static int create_impl(const mlh_config *cfg, int nmembers, const mlh_member *md
     A(prim, n); A(geo, n); A(grad, n); A(gradRaw, n); A(fluxSums, n * 5);
     A(status, 1); A(dtbits, nm); A(newtonSum, 3); A(dt, nm); A(simTime, nm); A(stepsDone, 1);
     A(hp, n); A(neff, n); A(hstat, 2); A(hpf, n);
-    A(scanTiles, n / 4096 + 1024); A(scanTotal, 1);
+    A(scanTotal, 1);
+    A(bar, 2);
 #undef A
     if ((rc = alloc_cell_buffers(c))) return fail(rc);
     if ((rc = alloc_neighbour_buffers(c))) return fail(rc);
@@ -449,6 +463,17 @@ static int create_impl(const mlh_config *cfg, int nmembers, const mlh_member *md
     cudaMemsetAsync(c->stepsDone, 0, sizeof(int), c->stream);
     cudaMemsetAsync(c->neff, 0, sizeof(double) * n, c->stream);
     cudaMemsetAsync(c->hstat, 0, 2 * sizeof(unsigned long long), c->stream);
+    // empty lists until the first search (kernels after a binning that gave
+    // up a bounded wait read them)
+    cudaMemsetAsync(c->noi, 0, sizeof(int) * n, c->stream);
+    cudaMemsetAsync(c->noiImg, 0, sizeof(int) * n, c->stream);
+    cudaMemsetAsync(c->faceCnt, 0, sizeof(int) * n, c->stream);
+    // the persistent binning needs its launch's blocks resident at once
+    {
+        int coop = 0;
+        cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, c->device);
+        c->bin_blocks = coop ? binning_blocks(cfg->dim, c->sm_count) : 0;
+    }
     {
         // every particle starts at its simulation's kernelSize
         std::vector<double> h0(n);
@@ -511,7 +536,7 @@ void mlh_destroy(mlh_ctx *c) {
     void *ptrs[] = {c->x, c->y, c->z, c->vx, c->vy, c->vz, c->m, c->u, c->posf, c->members, c->memberOf, c->grids,
                     c->cellTotal, c->boundsPart, c->cell, c->cellList, c->noi, c->noiImg, c->faceCnt, c->faceOff,
                     c->prim, c->geo, c->grad, c->gradRaw, c->fluxSums, c->status, c->dtbits, c->newtonSum, c->dt,
-                    c->simTime, c->stepsDone, c->scanTiles, c->scanTotal, c->hp, c->neff, c->hstat, c->hpf};
+                    c->simTime, c->stepsDone, c->scanTiles, c->scanTotal, c->hp, c->neff, c->hstat, c->hpf, c->bar};
     for (void *q : ptrs) if (q) cudaFree(q);
     free_cell_buffers(c);
     free_neighbour_buffers(c);
@@ -646,7 +671,8 @@ int mlh_set_tuning(mlh_ctx *c, const mlh_tuning *t) {
     auto threads_ok = [](int v) { return v == 64 || v == 128 || v == 256; };
     if (!c || !t || !threads_ok(t->face_threads) || !threads_ok(t->grad_threads) || t->face_blocks_per_sm < 1 ||
         t->face_blocks_per_sm > 32 || t->nns_warps_per_sm < 8 || t->nns_warps_per_sm > 256 ||
-        t->face_split < 0 || t->face_split > 2 || t->link_overlap < 0 || t->link_overlap > 1) {
+        t->face_split < 0 || t->face_split > 2 || t->link_overlap < 0 || t->link_overlap > 1 ||
+        t->persistent_binning < 0 || t->persistent_binning > 1 || (t->persistent_binning && c->bin_blocks < 1)) {
         g_last_error = "invalid tuning";
         return MLH_ERR_INVALID;
     }
@@ -657,6 +683,16 @@ int mlh_set_tuning(mlh_ctx *c, const mlh_tuning *t) {
     c->tune.nns_warps_per_sm = t->nns_warps_per_sm;
     c->tune.face_split = t->face_split;
     c->tune.link_overlap = t->link_overlap;
+    c->tune.persistent_binning = t->persistent_binning;
+    drop_graph(c);
+    return 0;
+}
+
+int mlh_test_binning_barrier(mlh_ctx *c, unsigned extra_arrivals, unsigned spin_limit) {
+    if (!c) { g_last_error = "null context"; return MLH_ERR_INVALID; }
+    CK(cudaStreamSynchronize(c->stream));
+    c->bar_extra = extra_arrivals;
+    c->bar_spin = spin_limit;
     drop_graph(c);
     return 0;
 }
@@ -765,6 +801,21 @@ int mlh_autotune(mlh_ctx *c, int trial_steps, mlh_tuning *out) {
             }
         }
         c->tune.link_overlap = best.link_overlap;
+        // the binning as one persistent kernel or one launch per phase
+        best_step = 1e300;
+        for (int pb : {0, 1}) {
+            if (pb && c->bin_blocks < 1) continue;
+            c->tune.persistent_binning = pb;
+            for (int rep = 0; rep < 2; ++rep) {
+                if ((rc = restore())) goto done;
+                mlh_step_stats st;
+                rc = mlh_step(c, trial_steps, 0., &st);
+                if (rc & (MLH_ERR_CUDA | MLH_ERR_INVALID | MLH_ERR_TIMEOUT)) goto done;
+                rc = 0;
+                if (st.device_ms < best_step) { best_step = st.device_ms; best.persistent_binning = pb; }
+            }
+        }
+        c->tune.persistent_binning = best.persistent_binning;
     }
 done:
     {
@@ -783,6 +834,7 @@ done:
         out->nns_warps_per_sm = c->tune.nns_warps_per_sm;
         out->face_split = c->tune.face_split;
         out->link_overlap = c->tune.link_overlap;
+        out->persistent_binning = c->tune.persistent_binning;
     }
     return rc;
 }

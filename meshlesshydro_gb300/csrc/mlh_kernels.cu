@@ -146,12 +146,15 @@ void exclusive_scan(const int *in, int n, int *out, int *tile_buf, int *total, c
 // other particle (the only case where the two differ).
 constexpr int BOUNDS_T = 256;
 
+// the partial minima and maxima of virtual block vb (block vb % bpm of member
+// vb / bpm), for a block of BOUNDS_T threads
 template <int D>
-__global__ void k_bounds_partial(const double *__restrict__ x, const double *__restrict__ y,
-                                 const double *__restrict__ z, Params p, const Member *__restrict__ members,
-                                 int bpm, double *__restrict__ part) {
+__device__ __forceinline__ void bounds_partial_block(int vb, const double *__restrict__ x,
+                                                     const double *__restrict__ y, const double *__restrict__ z,
+                                                     const Params &p, const Member *__restrict__ members, int bpm,
+                                                     double *__restrict__ part) {
     __shared__ double smin[3][BOUNDS_T / 32], smax[3][BOUNDS_T / 32];
-    const int mi = blockIdx.x / bpm, sub = blockIdx.x % bpm;
+    const int mi = vb / bpm, sub = vb % bpm;
     const Member mb = members[mi];
     const double *X[3] = {x, y, z};
     double mn[3], mx[3];
@@ -180,20 +183,29 @@ __global__ void k_bounds_partial(const double *__restrict__ x, const double *__r
         for (int a = 0; a < D; ++a) {
             double a0 = DBL_MAX_, a1 = -DBL_MAX_;
             for (int w = 0; w < BOUNDS_T / 32; ++w) { a0 = fmin(a0, smin[a][w]); a1 = fmax(a1, smax[a][w]); }
-            part[(blockIdx.x * 3 + a) * 2 + 0] = a0;
-            part[(blockIdx.x * 3 + a) * 2 + 1] = a1;
+            part[(vb * 3 + a) * 2 + 0] = a0;
+            part[(vb * 3 + a) * 2 + 1] = a1;
         }
     }
+    __syncthreads();   // the shared partials are reused by the next virtual block
+}
+
+template <int D>
+__global__ void k_bounds_partial(const double *__restrict__ x, const double *__restrict__ y,
+                                 const double *__restrict__ z, Params p, const Member *__restrict__ members,
+                                 int bpm, double *__restrict__ part) {
+    bounds_partial_block<D>(blockIdx.x, x, y, z, p, members, bpm, part);
 }
 
 // Final pass + Domain::createGrid (Domain.cpp:9-54) for every simulation,
 // then the cell numbering of the concatenated grids.  For periodic runs the
 // bounds are the configured box.
 template <int D>
-__global__ void k_bounds_final(const double *__restrict__ x, const double *__restrict__ y,
-                               const double *__restrict__ z, const double *__restrict__ part, int bpm, Params p,
-                               const Member *__restrict__ members, int nmembers, GridInfo *__restrict__ grids,
-                               int *__restrict__ cellTotal, unsigned *__restrict__ status) {
+__device__ __forceinline__ void bounds_final_block(const double *__restrict__ x, const double *__restrict__ y,
+                                                   const double *__restrict__ z, const double *__restrict__ part,
+                                                   int bpm, const Params &p, const Member *__restrict__ members,
+                                                   int nmembers, GridInfo *__restrict__ grids,
+                                                   int *__restrict__ cellTotal, unsigned *__restrict__ status) {
     const double *X[3] = {x, y, z};
     for (int mi = threadIdx.x; mi < nmembers; mi += blockDim.x) {
         const Member mb = members[mi];
@@ -260,13 +272,22 @@ __global__ void k_bounds_final(const double *__restrict__ x, const double *__res
     }
 }
 
+template <int D>
+__global__ void k_bounds_final(const double *__restrict__ x, const double *__restrict__ y,
+                               const double *__restrict__ z, const double *__restrict__ part, int bpm, Params p,
+                               const Member *__restrict__ members, int nmembers, GridInfo *__restrict__ grids,
+                               int *__restrict__ cellTotal, unsigned *__restrict__ status) {
+    bounds_final_block<D>(x, y, z, part, bpm, p, members, nmembers, grids, cellTotal, status);
+}
+
 // Particles::assignParticlesAndCells (Particles.cpp:270-322).
 template <int D>
-__global__ void k_assign(const double *__restrict__ x, const double *__restrict__ y, const double *__restrict__ z,
-                         int n, const int *__restrict__ memberOf, const GridInfo *__restrict__ grids,
-                         int *__restrict__ cell, int *__restrict__ cellCount, unsigned *__restrict__ status) {
+__device__ __forceinline__ void assign_one(int i, const double *__restrict__ x, const double *__restrict__ y,
+                                           const double *__restrict__ z, const int *__restrict__ memberOf,
+                                           const GridInfo *__restrict__ grids, int *__restrict__ cell,
+                                           int *__restrict__ cellCount, unsigned *__restrict__ status) {
     const double *X[3] = {x, y, z};
-    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    {
         const GridInfo g = grids[memberOf ? memberOf[i] : 0];
         int fl[3] = {0, 0, 0};
         bool bad = false;
@@ -287,6 +308,14 @@ __global__ void k_assign(const double *__restrict__ x, const double *__restrict_
     }
 }
 
+template <int D>
+__global__ void k_assign(const double *__restrict__ x, const double *__restrict__ y, const double *__restrict__ z,
+                         int n, const int *__restrict__ memberOf, const GridInfo *__restrict__ grids,
+                         int *__restrict__ cell, int *__restrict__ cellCount, unsigned *__restrict__ status) {
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+        assign_one<D>(i, x, y, z, memberOf, grids, cell, cellCount, status);
+}
+
 __global__ void k_fill_cells(const int *__restrict__ cell, int n, const int *__restrict__ cellStart,
                              int *__restrict__ cellFill, int *__restrict__ cellList) {
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
@@ -298,18 +327,160 @@ __global__ void k_fill_cells(const int *__restrict__ cell, int n, const int *__r
 
 // Members of a cell in ascending particle index: the order in which
 // assignParticlesAndCells pushes them (Particles.cpp:319).
+__device__ __forceinline__ void sort_cell(int c, const int *__restrict__ cellStart, int *__restrict__ cellList) {
+    int b = cellStart[c], e = cellStart[c + 1];
+    for (int k = b + 1; k < e; ++k) {
+        int v = cellList[k];
+        int t = k - 1;
+        while (t >= b && cellList[t] > v) { cellList[t + 1] = cellList[t]; --t; }
+        cellList[t + 1] = v;
+    }
+}
+
 __global__ void k_sort_cells(const int *__restrict__ cellTotal, const int *__restrict__ cellStart,
                              int *__restrict__ cellList) {
     const int nc = *cellTotal;
-    for (int c = blockIdx.x * blockDim.x + threadIdx.x; c < nc; c += gridDim.x * blockDim.x) {
-        int b = cellStart[c], e = cellStart[c + 1];
-        for (int k = b + 1; k < e; ++k) {
-            int v = cellList[k];
-            int t = k - 1;
-            while (t >= b && cellList[t] > v) { cellList[t + 1] = cellList[t]; --t; }
-            cellList[t + 1] = v;
+    for (int c = blockIdx.x * blockDim.x + threadIdx.x; c < nc; c += gridDim.x * blockDim.x)
+        sort_cell(c, cellStart, cellList);
+}
+
+// ------------------------------------------------------------------ persistent binning
+
+// The binning of a step (bounds, grid, assignment, cell counts, their scan,
+// cell lists, in-cell order) as one persistent kernel: a cooperative launch of
+// at most the blocks the GPU holds at once, its phases separated by grid
+// barriers.  Results are those of the launch-per-phase sequence (integer and
+// min/max work, the cell lists sorted).
+//
+// Grid barrier: arrivals counted in bar.count, phases in bar.gen; the last
+// block to arrive resets the count and opens the next phase.  Every wait is
+// bounded: after bar.spin_limit polls (each followed by a short sleep) the
+// block sets ST_TIMEOUT and leaves the kernel, and so does every other block
+// (a block that left does not arrive again, so the others run out too).  The
+// step's later kernels that read the binning skip their work when ST_TIMEOUT
+// is set, so that a step which timed out leaves the state untouched.
+struct GridBar {
+    unsigned *count;
+    unsigned *gen;
+    unsigned expected;     // blocks that arrive at each barrier
+    unsigned spin_limit;   // polls before giving up
+};
+
+__device__ __forceinline__ bool grid_sync(const GridBar &b, unsigned *status) {
+    __shared__ int ok;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        int good = 1;
+        __threadfence();
+        const unsigned g = *(volatile unsigned *)b.gen;
+        const unsigned prev = atomicAdd(b.count, 1u);
+        if (prev + 1 == b.expected) {
+            atomicExch(b.count, 0u);
+            __threadfence();
+            atomicAdd(b.gen, 1u);
+        } else {
+            unsigned polls = 0;
+            while (*(volatile unsigned *)b.gen == g) {
+                if (++polls > b.spin_limit) {
+                    good = 0;
+                    flag(status, ST_TIMEOUT);
+                    break;
+                }
+                __nanosleep(256);
+            }
+        }
+        __threadfence();
+        ok = good;
+    }
+    __syncthreads();
+    return ok != 0;
+}
+
+// true when an earlier kernel of the step gave up a bounded wait (ST_TIMEOUT);
+// the value is the same for every thread of a launch
+__device__ __forceinline__ bool step_timed_out(const unsigned *status) {
+    return (*(volatile const unsigned *)status & ST_TIMEOUT) != 0u;
+}
+
+constexpr int PB_T = 256;                    // threads per block of k_binning
+constexpr int PB_ITEMS = SCAN_TILE / PB_T;   // scan items per thread (a tile of SCAN_TILE counts)
+
+template <int D>
+__global__ void __launch_bounds__(PB_T) k_binning(const double *__restrict__ x, const double *__restrict__ y,
+                                                  const double *__restrict__ z, Params p,
+                                                  const Member *__restrict__ members, const int *__restrict__ memberOf,
+                                                  int nmembers, int bpm, double *__restrict__ part,
+                                                  GridInfo *__restrict__ grids, int *__restrict__ cellTotal,
+                                                  int *__restrict__ cell, int *__restrict__ cellCount,
+                                                  int *__restrict__ cellStart, int *__restrict__ cellFill,
+                                                  int *__restrict__ cellList, int *__restrict__ tileSums,
+                                                  int *__restrict__ scanTotal, unsigned *__restrict__ status,
+                                                  GridBar bar) {
+    __shared__ int smem[32];
+    const int tid = blockIdx.x * blockDim.x + threadIdx.x, nthr = gridDim.x * blockDim.x;
+    const int ncap = p.ncells_cap;
+    const int ntiles = (ncap + SCAN_TILE - 1) / SCAN_TILE;
+    // 1: partial bounds of every member; clear the cell counters
+    for (int vb = blockIdx.x; vb < nmembers * bpm; vb += gridDim.x)
+        bounds_partial_block<D>(vb, x, y, z, p, members, bpm, part);
+    for (int k = tid; k <= ncap; k += nthr) { cellCount[k] = 0; cellFill[k] = 0; }
+    if (!grid_sync(bar, status)) return;
+    // 2: final bounds and Domain::createGrid (one block)
+    if (blockIdx.x == 0) bounds_final_block<D>(x, y, z, part, bpm, p, members, nmembers, grids, cellTotal, status);
+    if (!grid_sync(bar, status)) return;
+    // 3: Particles::assignParticlesAndCells and the cell counts
+    for (int i = tid; i < p.n; i += nthr) assign_one<D>(i, x, y, z, memberOf, grids, cell, cellCount, status);
+    if (!grid_sync(bar, status)) return;
+    // 4: exclusive scan of the counts: tile sums, their scan, the tiles
+    for (int t = blockIdx.x; t < ntiles; t += gridDim.x) {
+        const long long b0 = (long long)t * SCAN_TILE + (long long)threadIdx.x * PB_ITEMS;
+        int sum = 0;
+#pragma unroll 4
+        for (int k = 0; k < PB_ITEMS; ++k) sum += b0 + k < ncap ? cellCount[b0 + k] : 0;
+        int tot;
+        (void)block_exclusive_scan(sum, smem, tot);
+        if (threadIdx.x == 0) tileSums[t] = tot;
+    }
+    if (!grid_sync(bar, status)) return;
+    if (blockIdx.x == 0) {
+        int carry = 0;
+        for (int b = 0; b < ntiles; b += PB_T) {
+            const int idx = b + threadIdx.x;
+            const int v = idx < ntiles ? tileSums[idx] : 0;
+            int tot;
+            const int ex = block_exclusive_scan(v, smem, tot);
+            if (idx < ntiles) tileSums[idx] = carry + ex;
+            carry += tot;
+        }
+        if (threadIdx.x == 0) { *scanTotal = carry; cellStart[ncap] = carry; }
+    }
+    if (!grid_sync(bar, status)) return;
+    for (int t = blockIdx.x; t < ntiles; t += gridDim.x) {
+        const long long b0 = (long long)t * SCAN_TILE + (long long)threadIdx.x * PB_ITEMS;
+        int sum = 0;
+#pragma unroll 4
+        for (int k = 0; k < PB_ITEMS; ++k) sum += b0 + k < ncap ? cellCount[b0 + k] : 0;
+        int tot;
+        int ex = block_exclusive_scan(sum, smem, tot) + tileSums[t];
+#pragma unroll 4
+        for (int k = 0; k < PB_ITEMS; ++k) {
+            if (b0 + k < ncap) {
+                const int v = cellCount[b0 + k];
+                cellStart[b0 + k] = ex;
+                ex += v;
+            }
         }
     }
+    if (!grid_sync(bar, status)) return;
+    // 5: cell lists, then the reference's in-cell order
+    for (int i = tid; i < p.n; i += nthr) {
+        const int c = cell[i];
+        const int pos = atomicAdd(&cellFill[c], 1);
+        cellList[cellStart[c] + pos] = i;
+    }
+    if (!grid_sync(bar, status)) return;
+    const int nc = *cellTotal;
+    for (int c = tid; c < nc; c += nthr) sort_cell(c, cellStart, cellList);
 }
 
 // ------------------------------------------------------------------ neighbour search
@@ -467,6 +638,8 @@ __global__ void __launch_bounds__(NNS_WARPS * 32, MLH_NNS_MINB) k_neighbours(
     float *stH = reinterpret_cast<float *>(reinterpret_cast<unsigned char *>(imgE) + nns_r16((size_t)K * 4));   // staged h_j
 
     const double *X[3] = {x, y, z};
+    // a binning that gave up a bounded wait left no valid cells
+    if (step_timed_out(status)) return;
     const int gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const int nw = (gridDim.x * blockDim.x) >> 5;
     // omega, density, pressure, 1/omega and sound speed of particle bi (per
@@ -835,6 +1008,7 @@ __global__ void __launch_bounds__(NNS_WARPS * 32) k_hsolve(
     const double St = p.sngb_t;
     const double tolS = __dmul_rn(1e-12, St);
     const double *X[3] = {x, y, z};
+    if (step_timed_out(status)) return;   // no valid cells
     unsigned long long iters = 0, clamped = 0;   // per lane, for its particles
     bool overflow_any = false;
     const int gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
@@ -1172,24 +1346,43 @@ __device__ __forceinline__ double field_of(const Prim &q, int f) {
     return q.P;
 }
 
+//
+// With dtbits (adaptive time step), the first pass over the neighbours also
+// runs Particles::compGlobalTimestep (Particles.cpp:1446-1485) for the
+// particle, as k_timestep does (real neighbours only, v_sig from
+// numeric_limits<double>::min(), the same expressions), on the positions and
+// velocities that pass loads anyway; the per-particle dt goes into the
+// per-member minimum (warp reduction, then one atomicMin on its bit pattern).
 template <int D>
 __global__ void __launch_bounds__(256) k_gradients(Params p, const Member *__restrict__ members,
                                                    const int *__restrict__ memberOf, const GridInfo *__restrict__ grids,
                                                    const Prim *__restrict__ prim, Geo *__restrict__ geo,
                                                    const uint32_t *__restrict__ nbr, const double *__restrict__ ww,
+                                                   const double *__restrict__ rr,
                                                    const int *__restrict__ noi, const int *__restrict__ noiImg,
                                                    Grad *__restrict__ grad, Grad *__restrict__ gradRaw,
-                                                   double *__restrict__ psiOut) {
+                                                   double *__restrict__ psiOut,
+                                                   unsigned long long *__restrict__ dtbits) {
     constexpr int NF = D + 2;
-    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < p.n; i += gridDim.x * blockDim.x) {
-        const int mi = memberOf ? memberOf[i] : 0;
+    const int lane = threadIdx.x & 31;
+    // warp-uniform loop: every lane takes part in the time-step reduction
+    for (int i0 = (blockIdx.x * blockDim.x + threadIdx.x) & ~31; i0 < p.n; i0 += gridDim.x * blockDim.x) {
+      const int i = i0 + lane;
+      int mi = -1;
+      double dti = DBL_MAX_;
+      if (i < p.n) {
+        mi = memberOf ? memberOf[i] : 0;
         const GridInfo g = grids[mi];
         const double h = members[mi].h;
         const double hq = p.adaptive_h ? p.hp[i] : h;   // quadrature-point radius
         const Prim pi = prim[i];
         const double xi[3] = {pi.x, pi.y, pi.z};
         const size_t base = (size_t)i * p.K;
-        const int tot = noi[i] + noiImg[i];
+        const int nr = noi[i];
+        const int tot = nr + noiImg[i];
+        const bool want_dt = dtbits != nullptr;
+        const double ci = want_dt ? geo[i].c : 0.;
+        double vSig = DBL_MIN_;
         // E_i = V_i E' with E' = sum_j (x_j - x_i)(x_j - x_i)^T W_ij, so that
         // psi~_j(x_i) = E_i^-1 (x_j - x_i) W_ij V_i = E'^-1 (x_j - x_i) W_ij:
         // V_i cancels and neither pass multiplies by it
@@ -1207,7 +1400,20 @@ __global__ void __launch_bounds__(256) k_gradients(Params p, const Member *__res
             for (int a = 0; a < D; ++a)
 #pragma unroll
                 for (int b = a; b < D; ++b) E[D * a + b] = fma(d[a], dp[b], E[D * a + b]);
+            if (want_dt && s < nr) {
+                // v_sig = c_i + c_j - min(0, v_ij . x_ij / r) as one fused
+                // multiply-add (1/r only when the dot product is negative);
+                // x_ij = x_i - x_j is the exact negation of d
+                const double cj = geo[e & IDX_MASK].c;
+                const double xij[3] = {-d[0], -d[1], D == 3 ? -d[2] : 0.};
+                const double vij[3] = {pi.vx - pj.vx, pi.vy - pj.vy, pi.vz - pj.vz};
+                const double dv = dotD<D>(vij, xij);
+                const double ir = dneg(dv) ? frcp(rr[base + s]) : 0.;
+                const double vs = fma(-dv, ir, ci + cj);
+                vSig = dlt(vSig, vs) ? vs : vSig;
+            }
         }
+        if (want_dt) dti = (p.adaptive_h ? p.cfl * p.hp[i] : members[mi].cfl_h) / vSig;
 #pragma unroll
         for (int a = 0; a < D; ++a)
 #pragma unroll
@@ -1340,6 +1546,21 @@ __global__ void __launch_bounds__(256) k_gradients(Params p, const Member *__res
         const double omega_i = geo[i].omega;
 #pragma unroll
         for (int k = 0; k < D * D; ++k) geo[i].B[k] = E[k] * omega_i;
+      }   // i < p.n
+      if (dtbits) {
+        // the minimum over particles does not depend on the order of the
+        // atomicMin calls: a warp inside one simulation reduces first and
+        // issues one atomic; a warp that straddles two issues one per lane
+        const int m0 = __shfl_sync(0xffffffffu, mi, 0);
+        if (__all_sync(0xffffffffu, mi == m0)) {
+            double best = dti;
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) best = fmin(best, __shfl_xor_sync(0xffffffffu, best, o));
+            if (lane == 0 && m0 >= 0 && best < DBL_MAX_) atomic_min_pos_double(dtbits + m0, best);
+        } else if (mi >= 0 && dti < DBL_MAX_) {
+            atomic_min_pos_double(dtbits + mi, dti);
+        }
+      }
     }
 }
 
@@ -2135,7 +2356,7 @@ __global__ void __launch_bounds__(256) k_update(Params p, const int *__restrict_
                                                 double *__restrict__ m, double *__restrict__ u, float4 *__restrict__ posf,
                                                 double *__restrict__ fluxSums, unsigned *__restrict__ status) {
     const unsigned st0 = *status;
-    if (st0 & (ST_NGB_OVERFLOW | ST_CAPACITY)) return;
+    if (st0 & (ST_NGB_OVERFLOW | ST_CAPACITY | ST_TIMEOUT)) return;
     double *X[3] = {x, y, z};
     double *Vv[3] = {vx, vy, vz};
     unsigned st_local = 0;
@@ -2237,7 +2458,7 @@ __global__ void __launch_bounds__(256) k_update(Params p, const int *__restrict_
 // like the update, when the step is to be repeated with more capacity).
 __global__ void k_advance_time(int nmembers, const double *__restrict__ dt, double *__restrict__ simTime,
                                int *__restrict__ stepsDone, const unsigned *__restrict__ status) {
-    if (*status & (ST_NGB_OVERFLOW | ST_CAPACITY)) return;
+    if (*status & (ST_NGB_OVERFLOW | ST_CAPACITY | ST_TIMEOUT)) return;
     for (int mi = blockIdx.x * blockDim.x + threadIdx.x; mi < nmembers; mi += gridDim.x * blockDim.x)
         simTime[mi] += dt[mi];
     if (blockIdx.x == 0 && threadIdx.x == 0) *stepsDone += 1;
@@ -2261,6 +2482,26 @@ void launch_binning(StepArgs &a) {
     cudaStream_t s = a.stream;
     const int T = 128;
     const int blocksN = (p.n + T - 1) / T;
+    if (a.tune.persistent_binning && a.bar && a.bin_blocks > 0) {
+        // one cooperative launch of at most the blocks resident at once
+        cudaMemsetAsync(a.bar, 0, 2 * sizeof(unsigned), s);
+        GridBar bar{a.bar, a.bar + 1, (unsigned)a.bin_blocks + a.bar_extra, a.bar_spin};
+        cudaLaunchConfig_t cfg = {};
+        cfg.gridDim = dim3(a.bin_blocks);
+        cfg.blockDim = dim3(PB_T);
+        cfg.dynamicSmemBytes = 0;
+        cfg.stream = s;
+        cudaLaunchAttribute attr[1];
+        attr[0].id = cudaLaunchAttributeCooperative;
+        attr[0].val.cooperative = 1;
+        cfg.attrs = attr;
+        cfg.numAttrs = 1;
+        cudaLaunchKernelEx(&cfg, k_binning<D>, (const double *)a.x, (const double *)a.y, (const double *)a.z, p,
+                           (const Member *)a.members, a.memberOf, a.nmembers, a.bpm, a.boundsPart, a.grids,
+                           a.cellTotal, a.cell, a.cellCount, a.cellStart, a.cellFill, a.cellList, a.scanTiles,
+                           a.scanTotal, a.status, bar);
+        return;
+    }
     k_bounds_partial<D><<<a.nmembers * a.bpm, BOUNDS_T, 0, s>>>(a.x, a.y, a.z, p, a.members, a.bpm, a.boundsPart);
     k_bounds_final<D><<<1, 256, 0, s>>>(a.x, a.y, a.z, a.boundsPart, a.bpm, p, a.members, a.nmembers, a.grids,
                                         a.cellTotal, a.status);
@@ -2335,17 +2576,22 @@ void launch_step(StepArgs &a) {
         cudaEventRecord(a.ev_join, a.stream2);
     }
 
-    tick(KT_DT);
-    cudaMemsetAsync(a.dtbits, 0xff, sizeof(unsigned long long) * (size_t)a.nmembers, s);
-    k_timestep<D><<<(p.n + 255) / 256, 256, 0, s>>>(p, a.members, a.memberOf, a.prim, a.geo, a.nbr, a.rr, a.noi,
-                                                    a.dtbits);
-    k_dt_final<<<(a.nmembers + 127) / 128, 128, 0, s>>>(p, a.nmembers, a.dtbits, a.dt_max, a.dt);
-    tock(KT_DT);
-
-    tick(KT_GRAD);
+    // the time step runs inside the gradients' first neighbour pass
+    // (k_gradients with dtbits; k_timestep, the separate kernel of the same
+    // arithmetic, is the fallback when the time step is timed on its own)
     const int gT = a.tune.grad_threads;
-    k_gradients<D><<<(p.n + gT - 1) / gT, gT, 0, s>>>(p, a.members, a.memberOf, a.grids, a.prim, a.geo, a.nbr, a.ww, a.noi,
-                                         a.noiImg, a.grad, a.gradRaw, a.psi);
+    cudaMemsetAsync(a.dtbits, 0xff, sizeof(unsigned long long) * (size_t)a.nmembers, s);
+    if (a.separate_dt) {
+        tick(KT_DT);
+        k_timestep<D><<<(p.n + 255) / 256, 256, 0, s>>>(p, a.members, a.memberOf, a.prim, a.geo, a.nbr, a.rr,
+                                                        a.noi, a.dtbits);
+        tock(KT_DT);
+    }
+    tick(KT_GRAD);
+    k_gradients<D><<<(p.n + gT - 1) / gT, gT, 0, s>>>(p, a.members, a.memberOf, a.grids, a.prim, a.geo, a.nbr, a.ww,
+                                                      a.rr, a.noi, a.noiImg, a.grad, a.gradRaw, a.psi,
+                                                      (p.adaptive && !a.separate_dt) ? a.dtbits : nullptr);
+    k_dt_final<<<(a.nmembers + 127) / 128, 128, 0, s>>>(p, a.nmembers, a.dtbits, a.dt_max, a.dt);
     tock(KT_GRAD);
     if (a.stop_after_gradients) return;
 
@@ -2418,6 +2664,14 @@ void launch_grid_bounds(const double *x, const double *y, const double *z, const
         k_bounds_partial<3><<<blocks, BOUNDS_T, 0, s>>>(x, y, z, p, members, bpm, partials);
         k_bounds_final<3><<<1, 256, 0, s>>>(x, y, z, partials, bpm, p, members, nmembers, grids, cellTotal, status);
     }
+}
+
+int binning_blocks(int dim, int sm_count) {
+    int per_sm = 0;
+    cudaError_t e = dim == 3 ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_binning<3>, PB_T, 0)
+                             : cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_binning<2>, PB_T, 0);
+    if (e != cudaSuccess || per_sm < 1) return 0;
+    return per_sm * sm_count;
 }
 
 void step(StepArgs &a) {

@@ -17,6 +17,7 @@ struct Tuning {
     int nns_warps_per_sm = 64;     // warps (= particles in flight) of k_neighbours
     int face_split = 1;            // plain gamma = 5/3 step: 1 second Newton pass over a queue, 2 in-block, 0 none
     int link_overlap = 1;          // face links on the second stream beside the time step and gradients
+    int persistent_binning = 0;    // the binning as one persistent cooperative kernel (k_binning)
 };
 
 // Device pointers and settings of one step.
@@ -83,6 +84,16 @@ struct StepArgs {
     unsigned long long *hstat;
     // end the step after the gradients and the limiter (mlh_prepare)
     int stop_after_gradients;
+    // the time step as its own kernel (k_timestep) instead of inside the
+    // gradients' first neighbour pass
+    int separate_dt;
+    // persistent binning: its grid-barrier words (2 unsigned), its block
+    // count (resident blocks, 0: unavailable), extra arrivals the barriers
+    // wait for (a test hook: nonzero makes every wait run out) and the polls
+    // before a wait gives up
+    unsigned *bar;
+    int bin_blocks;
+    unsigned bar_extra, bar_spin;
     // optional per-kernel timer callback (phase 0 = before, 1 = after)
     void (*timer)(void *, int, int);
     void *timer_ctx;
@@ -93,6 +104,8 @@ struct StepArgs {
 constexpr int BOUNDS_BLOCKS = 304;
 
 void step(StepArgs &a);
+// blocks of the persistent binning kernel resident at once (0: none)
+int binning_blocks(int dim, int sm_count);
 // binning and the smoothing-length solve alone, on the current positions
 void smoothing_lengths(StepArgs &a);
 // Particles::getDomainLimits + Domain::createGrid alone: per-block partial

@@ -45,7 +45,7 @@ class Tuning(ctypes.Structure):
     _fields_ = [("face_threads", ctypes.c_int), ("face_blocks_per_sm", ctypes.c_int),
                 ("grad_threads", ctypes.c_int), ("nns_warps_per_sm", ctypes.c_int),
                 ("face_split", ctypes.c_int),
-                ("link_overlap", ctypes.c_int)]
+                ("link_overlap", ctypes.c_int), ("persistent_binning", ctypes.c_int)]
 
 
 class ParticlesView(ctypes.Structure):
@@ -67,7 +67,7 @@ EXPORTS = ["mlh_abi_version", "mlh_last_error", "mlh_create", "mlh_destroy", "ml
            "mlh_grid_bounds_noalloc", "mlh_ensemble_create", "mlh_member_times", "mlh_set_graph_mode",
            "mlh_autotune", "mlh_set_tuning", "mlh_pstar_infer", "mlh_pstar_grad", "mlh_pstar_train", "mlh_set_pstar_weights",
            "mlh_pstar_harvest", "mlh_pstar_harvest_strong", "mlh_smoothing_lengths", "mlh_prepare", "mlh_riemann_fluxes",
-           "mlh_probe_fast_math", "mlh_probe_fp64_lanes"]
+           "mlh_probe_fast_math", "mlh_probe_fp64_lanes", "mlh_test_binning_barrier"]
 
 _lib = None
 
@@ -104,6 +104,8 @@ def load(path: str = LIB_PATH):
     L.mlh_probe_fp64_tflops.restype = ctypes.c_int
     L.mlh_probe_fp64_clock.argtypes = [ctypes.c_double, ctypes.POINTER(ctypes.c_double),
                                        ctypes.POINTER(ctypes.c_double)]
+    L.mlh_test_binning_barrier.argtypes = [ctypes.c_void_p, ctypes.c_uint, ctypes.c_uint]
+    L.mlh_test_binning_barrier.restype = ctypes.c_int
     L.mlh_probe_fp64_clock.restype = ctypes.c_int
     dp = ctypes.c_void_p
     L.mlh_grid_bounds_noalloc.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_int, dp, dp, dp,
@@ -339,12 +341,14 @@ class Simulation:
         if st != 0:
             raise MLHError(st, "mlh_set_pstar_weights", self.L.mlh_last_error().decode())
 
-    def harvest(self, stride: int = 1, capacity: int = 1 << 22, strong: bool = False):
+    def harvest(self, stride: int = 1, capacity: int = 1 << 22, strong: bool = False, check: bool = True):
         """One step recording (network input, log(p*/p_TR)) of every stride-th face,
         p_TR the two-rarefaction guess of the face; strong=True: of every face
         the learned step hands to the network (p_TR > 2 min(pL, pR)).  Returns
         the rows (at most capacity) and, with strong=True, the number of such
-        faces as a third value."""
+        faces as a third value.  check=False: the physics status bits of the
+        step (non-physical values, which the reference only warns about) do
+        not raise; argument, CUDA and capacity errors still do."""
         x = np.zeros((capacity, 4), dtype=np.float32)
         t = np.zeros(capacity, dtype=np.float32)
         cnt = ctypes.c_longlong()
@@ -352,7 +356,8 @@ class Simulation:
             st = self.L.mlh_pstar_harvest_strong(self.h, _fptr(x), _fptr(t), capacity, ctypes.byref(cnt))
         else:
             st = self.L.mlh_pstar_harvest(self.h, stride, _fptr(x), _fptr(t), capacity, ctypes.byref(cnt))
-        if st != 0:
+        hard = (1 << 20) | (1 << 21) | (1 << 22) | (1 << 23) | (1 << 11)
+        if st != 0 and (check or (st & hard)):
             raise MLHError(st, "mlh_pstar_harvest", self.L.mlh_last_error().decode())
         k = min(cnt.value, capacity)
         if strong:
@@ -386,9 +391,9 @@ class Simulation:
 
     def set_tuning(self, tuning: dict):
         """Launch shapes (mlh_set_tuning); face_split and link_overlap
-        default to 1."""
-        t = Tuning(**{k: int(tuning.get(k, 1) if k in ("face_split", "link_overlap") else tuning[k])
-                      for k, _ in Tuning._fields_})
+        default to 1, persistent_binning to 0."""
+        dflt = {"face_split": 1, "link_overlap": 1, "persistent_binning": 0}
+        t = Tuning(**{k: int(tuning.get(k, dflt[k]) if k in dflt else tuning[k]) for k, _ in Tuning._fields_})
         st = self.L.mlh_set_tuning(self.h, ctypes.byref(t))
         if st != 0:
             raise MLHError(st, "mlh_set_tuning", self.L.mlh_last_error().decode())

@@ -75,12 +75,13 @@ def test_adaptive_step_stagewise(oracle_mod, name):
     for step in range(3):
         # every step from the oracle's state (and both solves start from the
         # smoothing lengths of the previous step, equal bit for bit)
-        g.set_state(pset_from_state(p, o.state()))
+        pre = o.state()
+        g.set_state(pset_from_state(p, pre))
         assert o.step() == 0
         st = g.step(1)
         assert st.steps == 1
         np.testing.assert_array_equal(g.get("h"), o.get("h"), err_msg=f"h, step {step}")
-        compare_step(g, o, cfg.dim, slots=True, what=f"{name} step {step}: ")
+        compare_step(g, o, cfg.dim, slots=True, what=f"{name} step {step}: ", pre=pre)
     h = g.get("h")
     assert h.min() > 0 and h.max() <= cfg.kernel_size and h.std() > 0
     hs = g.get("h_stats")

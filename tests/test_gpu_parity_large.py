@@ -23,8 +23,8 @@ import pytest
 
 from meshlesshydro_gb300 import ic
 from meshlesshydro_gb300.config import MFVConfig
-from helpers import (MAX_TIE_FRACTION, assert_close, assert_state, compare_step, l1_rel, pset_from_state,
-                     riemann_ties)
+from helpers import (MAX_TIE_FRACTION, assert_close, assert_state, compare_step, flux_terms, l1_rel,
+                     pset_from_state, riemann_ties, state_of, state_terms)
 
 pytestmark = pytest.mark.gpu
 
@@ -56,7 +56,7 @@ def test_sedov64_one_step_stagewise(orc, periodic):
     assert o.step() == 0
     g = _sim(cfg, p)
     st = g.step(1)
-    compare_step(g, o, 3, slots=True, what=f"sedov64 periodic={periodic}: ")
+    compare_step(g, o, 3, slots=True, what=f"sedov64 periodic={periodic}: ", pre=state_of(p))
     assert st.faces == int(o.get("stats")[0])
     g.close()
     o.close()
@@ -71,7 +71,8 @@ def _per_step_and_free_run(orc, p, cfg, nsteps, what, free_fields=("rho",)):
     g = _sim(cfg, p)
     ties = 0
     for k in range(nsteps):
-        g.set_state(pset_from_state(p, o.state()))
+        pre = o.state()
+        g.set_state(pset_from_state(p, pre))
         assert o.step() == 0, f"{what}: oracle status at step {k}"
         g.step(1)
         np.testing.assert_array_equal(g.get("nnl"), o.get("nnl"), err_msg=f"{what}: nnl at step {k}")
@@ -79,7 +80,9 @@ def _per_step_and_free_run(orc, p, cfg, nsteps, what, free_fields=("rho",)):
         assert_close(g.get("dt"), o.get("dt"), floor=0.0, what=f"{what} step {k}: dt")
         tie, touched = riemann_ties(g, o)
         ties += int(tie.sum() // 2)
-        assert_state(g.get_state(), o.state(), touched, what=f"{what} step {k}: ")
+        ost = o.state()
+        terms = state_terms(pre, ost, flux_terms(o.get("F"), o.get("off"), cfg.dim), float(o.get("dt")[0]), cfg.dim)
+        assert_state(g.get_state(), ost, touched, what=f"{what} step {k}: ", terms=terms)
     faces = max(int(o.get("stats")[0]), 1)
     assert ties <= MAX_TIE_FRACTION * faces * nsteps + 1, f"{what}: {ties} Newton ties in {nsteps} steps"
     # free run: the oracle's final state after nsteps, and its density at the
@@ -115,7 +118,7 @@ def test_sedov128_one_step(orc):
     assert o.step() == 0
     g = _sim(cfg, p)
     st = g.step(1)
-    compare_step(g, o, 3, slots=False, what="sedov128: ")
+    compare_step(g, o, 3, slots=False, what="sedov128: ", pre=state_of(p))
     assert st.faces == int(o.get("stats")[0])
     g.close()
     o.close()
@@ -142,7 +145,7 @@ def test_kh24_mfm_and_fixed_particles(orc, mode):
     assert o.step() == 0
     g = _sim(cfg, p)
     g.step(1)
-    compare_step(g, o, 2, slots=True, what=mode + ": ")
+    compare_step(g, o, 2, slots=True, what=mode + ": ", pre=state_of(p))
     gs = g.get_state()
     if mode == "meshless_finite_mass":
         assert np.array_equal(gs["m"], p.m)
