@@ -223,6 +223,14 @@ def cpu_model():
     return "unknown"
 
 
+_T0 = time.perf_counter()
+
+
+def progress(msg: str):
+    """A progress line on stderr (the JSON line alone goes to stdout)."""
+    print(f"[bench {time.perf_counter() - _T0:8.1f} s] {msg}", file=sys.stderr, flush=True)
+
+
 def host_cores():
     return os.cpu_count() or 1
 
@@ -445,12 +453,16 @@ def learned_section(runtime, args, make_main, tuning, st_plain, kt_plain, rho_pl
     """Learned guess: training on the Sedov 64^3 + KH harvest, network error
     on held-out faces, and the learned step against the plain one on the
     bench workload and on the 64-blast 64^3 workload (strong shocks)."""
+    progress("learned: harvest and training")
     w, train = train_learned_guess(runtime)
+    progress("learned: network error on held-out faces")
     out = {"guess": "p_TR * exp(y) for faces with p_TR > 2 min(pL, pR) where |y| > 0.01, else p_TR; Newton to "
                     "1e-10 relative either way, restarting from p_TR when the network's start does not converge",
            "train": train}
     out["network_error_held_out"] = network_error(runtime, w, make_main)
+    progress("learned: main workload")
     out["main_workload"] = learned_vs_plain(runtime, make_main, w, args, tuning, st_plain, kt_plain, rho_plain)
+    progress("learned: multi-blast workload")
     pm, cm = make_workload("multi_blast64")
     mk = lambda: runtime.Simulation(cm, pm)
     out["multi_blast64"] = learned_vs_plain(runtime, mk, w, args)
@@ -514,8 +526,11 @@ def ensemble_section(runtime, args, w_learned):
         sim.close()
         return tuning, st, wall
 
+    progress("ensemble: batched, plain")
     tun_p, st_p, wall_p = batched(None)
+    progress("ensemble: batched, learned")
     tun_l, st_l, wall_l = batched(w_learned) if w_learned is not None else (None, None, None)
+    progress("ensemble: members one after another")
     # members one after another: every member's step is a plain mlh_step(1)
     sims = [runtime.Simulation(MFVConfig.kelvin_helmholtz(m), m) for m in members]
     for s_ in sims:
@@ -567,7 +582,9 @@ def run_mlh(args):
     build.build()
     probe_clocks = ClockSampler(local)
     probe_clocks.start()
+    progress("FP64 probe")
     fp64_peak, probe_mhz = runtime.probe_fp64_clock(1.0)
+    progress("main workload: set-up and autotune")
     probe_ck = probe_clocks.stop()
     sm_count = torch.cuda.get_device_properties(local).multi_processor_count
     p, cfg = make_workload(args.workload, seed_offset=replica_seed(0, rank))
@@ -576,7 +593,12 @@ def run_mlh(args):
     sim = runtime.Simulation(cfg, members=members) if ensemble else runtime.Simulation(cfg, p)
     if ensemble:
         p = sim.host  # concatenated state: .n
-    tuning = None if args.no_autotune else sim.autotune(2)
+    if args.tuning:
+        sim.set_tuning(json.loads(args.tuning))
+        tuning = json.loads(args.tuning)
+    else:
+        tuning = None if args.no_autotune else sim.autotune(2)
+    progress(f"main workload: tuning {tuning}")
     sim.step(args.warmup)
     if dist:
         dist.barrier()
@@ -625,6 +647,7 @@ def run_mlh(args):
     if not args.no_learned and main_kind in ("sedov", "multi_blast"):
         extra["learned"], w_learned = learned_section(runtime, args, make_main, tuning, st, kt, rho_plain)
     if not args.no_adaptive and main_kind == "sedov":
+        progress("adaptive smoothing lengths")
         extra["adaptive_h"] = adaptive_section(runtime, cfg, p, tuning, args)
     if not args.no_ensemble and rank == 0:
         extra["ensemble"] = ensemble_section(runtime, args, w_learned)
@@ -707,6 +730,7 @@ def run_mlh(args):
                     "steps": e2e_steps},
             "peaks": {"source": peak_kind, "hbm_gbs": peaks.get("hbm_gbs")}}
     if not args.no_cpu_baseline:
+        progress("CPU baseline")
         line["cpu_baseline"] = cpu_baseline_sample(args.cpu_seconds,
                                                    "sedov" if main_kind in ("sedov", "multi_blast") else "kh")
     print(json.dumps(line), flush=True)
@@ -725,6 +749,8 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
     ap.add_argument("--no-autotune", action="store_true")
+    ap.add_argument("--tuning", default="", help="launch shapes as JSON (mlh_tuning fields) instead of the "
+                                                 "autotuner's, e.g. for profiling")
     ap.add_argument("--no-learned", action="store_true", help="skip the learned p* guess comparison")
     ap.add_argument("--no-adaptive", action="store_true", help="skip the per-particle smoothing-length run")
     ap.add_argument("--no-ensemble", action="store_true", help="skip the 256-member KH ensemble comparison")

@@ -1687,9 +1687,16 @@ __device__ __forceinline__ double pairwise_side(double phi0, double phi_i, doubl
     // extreme it starts from is phi_i; the reference takes the shift when it
     // keeps the sign, (a >= 0 && b >= 0) || (a < 0 && b < 0), else
     // phi / (1 + delta1 / |phi|)
+    // (phi / (1 + delta1 / |phi|) evaluated as phi |phi| / (|phi| + delta1),
+    // one division by the Newton-Raphson reciprocal, and only where the
+    // shift would change the sign; the same value to a few ulp, also for
+    // |phi| = 0 and the int abs binding)
     const double shifted = phi_i + (i_lt_j ? -delta1 : delta1);
-    const double bound = (ord_key(shifted) >= 0) == (ord_key(phi_i) >= 0)
-                             ? shifted : phi_i / (1. + delta1 / ref_abs(phi_i, int_abs));
+    double bound = shifted;
+    if ((ord_key(shifted) >= 0) != (ord_key(phi_i) >= 0)) {
+        const double ra = ref_abs(phi_i, int_abs);
+        bound = fdiv(phi_i * ra, ra + delta1);
+    }
     const double t = phi_ij + (i_lt_j ? delta2 : -delta2);
     if (i_lt_j) {
         const double minPhiD2 = dlt(t, phi0) ? t : phi0;
