@@ -343,32 +343,43 @@ def train_learned_guess(runtime, budget_rows: int = 10_000_000, epochs: int = 12
     hands to the network, at every step, and every 4th face at steps 0, 25,
     50 and 75) and the 100x100 Kelvin-Helmholtz run (100 steps: every face of
     every 5th step), at most budget_rows rows (a seeded subsample beyond).
-    Seeds differ from the evaluated workloads."""
+    A run is harvested up to its first step with non-physical values (which
+    the reference only warns about).  Seeds differ from the evaluated
+    workloads."""
     from meshlesshydro_gb300 import ic
     from meshlesshydro_gb300.config import MFVConfig
     t0 = time.perf_counter()
     xs, ts = [], []
     n_strong = n_sedov = n_kh = 0
+    stopped = {}
     p = ic.sedov(n_side=64, seed=12)
     s = runtime.Simulation(MFVConfig.sedov(p, periodic=True), p)
     for k in range(100):
-        if k % 25 == 0:
-            x, t = s.harvest(stride=4, capacity=1 << 21, check=False)
-            n_sedov += x.shape[0]
-        else:
-            x, t, _ = s.harvest(strong=True, capacity=1 << 20, check=False)
-            n_strong += x.shape[0]
+        try:   # a run that reports non-physical values is not harvested further
+            if k % 25 == 0:
+                x, t = s.harvest(stride=4, capacity=1 << 21)
+                n_sedov += x.shape[0]
+            else:
+                x, t, _ = s.harvest(strong=True, capacity=1 << 20)
+                n_strong += x.shape[0]
+        except runtime.MLHError as exc:
+            stopped["sedov64"] = {"step": k, "status": runtime.status_names(exc.status)}
+            break
         xs.append(x); ts.append(t)
     s.close()
     q = ic.kelvin_helmholtz(n_side=100, seed=21)
     s = runtime.Simulation(MFVConfig.kelvin_helmholtz(q), q)
     for k in range(100):
-        if k % 5 == 0:
-            x, t = s.harvest(stride=1, capacity=1 << 18, check=False)
-            xs.append(x); ts.append(t)
-            n_kh += x.shape[0]
-        else:
-            s.step(1)
+        try:
+            if k % 5 == 0:
+                x, t = s.harvest(stride=1, capacity=1 << 18)
+                xs.append(x); ts.append(t)
+                n_kh += x.shape[0]
+            else:
+                s.step(1)
+        except runtime.MLHError as exc:
+            stopped["kh100"] = {"step": k, "status": runtime.status_names(exc.status)}
+            break
     s.close()
     x = np.concatenate(xs)
     t = np.concatenate(ts)
@@ -380,7 +391,7 @@ def train_learned_guess(runtime, budget_rows: int = 10_000_000, epochs: int = 12
     w, hist = runtime.pstar_train(x, t, epochs=epochs, batch=8192, lr=2e-3, seed=0)
     t2 = time.perf_counter()
     return w, {"rows": int(x.shape[0]), "rows_sedov64_strong": n_strong, "rows_sedov64_every_4th": n_sedov,
-               "rows_kh100": n_kh, "epochs": epochs, "batch": 8192, "lr": 2e-3,
+               "rows_kh100": n_kh, "harvest_stopped": stopped, "epochs": epochs, "batch": 8192, "lr": 2e-3,
                "loss_first_epoch": float(hist[0]), "loss_last_epoch": float(hist[-1]),
                "harvest_s": t1 - t0, "train_s": t2 - t1}
 

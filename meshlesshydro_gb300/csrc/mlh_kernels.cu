@@ -316,8 +316,23 @@ __global__ void k_assign(const double *__restrict__ x, const double *__restrict_
         assign_one<D>(i, x, y, z, memberOf, grids, cell, cellCount, status);
 }
 
+// True when the binning of this step is not valid: a bounded wait gave up
+// (ST_TIMEOUT), a particle fell outside the grid (ST_GRID: outside the box,
+// a NaN coordinate, or fewer than 3 cells on a periodic axis) or the cells
+// exceed their buffers (ST_CAPACITY, the step is repeated with more).  The
+// kernels that read the binning then skip their work: the step completes
+// nothing and reports the bits, and a NaN particle, which the grid clamps
+// into one cell, cannot make a cell of every particle whose sort and search
+// are quadratic in its size.  The value is the same for every thread of a
+// launch (the bits are set by earlier kernels or before a grid barrier).
+__device__ __forceinline__ bool step_aborted(const unsigned *status) {
+    return (*(volatile const unsigned *)status & (ST_TIMEOUT | ST_GRID | ST_CAPACITY)) != 0u;
+}
+
 __global__ void k_fill_cells(const int *__restrict__ cell, int n, const int *__restrict__ cellStart,
-                             int *__restrict__ cellFill, int *__restrict__ cellList) {
+                             int *__restrict__ cellFill, int *__restrict__ cellList,
+                             const unsigned *__restrict__ status) {
+    if (step_aborted(status)) return;
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
         int c = cell[i];
         int pos = atomicAdd(&cellFill[c], 1);
@@ -338,7 +353,8 @@ __device__ __forceinline__ void sort_cell(int c, const int *__restrict__ cellSta
 }
 
 __global__ void k_sort_cells(const int *__restrict__ cellTotal, const int *__restrict__ cellStart,
-                             int *__restrict__ cellList) {
+                             int *__restrict__ cellList, const unsigned *__restrict__ status) {
+    if (step_aborted(status)) return;
     const int nc = *cellTotal;
     for (int c = blockIdx.x * blockDim.x + threadIdx.x; c < nc; c += gridDim.x * blockDim.x)
         sort_cell(c, cellStart, cellList);
@@ -396,12 +412,6 @@ __device__ __forceinline__ bool grid_sync(const GridBar &b, unsigned *status) {
     return ok != 0;
 }
 
-// true when an earlier kernel of the step gave up a bounded wait (ST_TIMEOUT);
-// the value is the same for every thread of a launch
-__device__ __forceinline__ bool step_timed_out(const unsigned *status) {
-    return (*(volatile const unsigned *)status & ST_TIMEOUT) != 0u;
-}
-
 constexpr int PB_T = 256;                    // threads per block of k_binning
 constexpr int PB_ITEMS = SCAN_TILE / PB_T;   // scan items per thread (a tile of SCAN_TILE counts)
 
@@ -431,6 +441,8 @@ __global__ void __launch_bounds__(PB_T) k_binning(const double *__restrict__ x, 
     // 3: Particles::assignParticlesAndCells and the cell counts
     for (int i = tid; i < p.n; i += nthr) assign_one<D>(i, x, y, z, memberOf, grids, cell, cellCount, status);
     if (!grid_sync(bar, status)) return;
+    // the same decision in every block: the bits were set before the barrier
+    if (step_aborted(status)) return;
     // 4: exclusive scan of the counts: tile sums, their scan, the tiles
     for (int t = blockIdx.x; t < ntiles; t += gridDim.x) {
         const long long b0 = (long long)t * SCAN_TILE + (long long)threadIdx.x * PB_ITEMS;
@@ -639,7 +651,7 @@ __global__ void __launch_bounds__(NNS_WARPS * 32, MLH_NNS_MINB) k_neighbours(
 
     const double *X[3] = {x, y, z};
     // a binning that gave up a bounded wait left no valid cells
-    if (step_timed_out(status)) return;
+    if (step_aborted(status)) return;
     const int gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const int nw = (gridDim.x * blockDim.x) >> 5;
     // omega, density, pressure, 1/omega and sound speed of particle bi (per
@@ -1008,7 +1020,7 @@ __global__ void __launch_bounds__(NNS_WARPS * 32) k_hsolve(
     const double St = p.sngb_t;
     const double tolS = __dmul_rn(1e-12, St);
     const double *X[3] = {x, y, z};
-    if (step_timed_out(status)) return;   // no valid cells
+    if (step_aborted(status)) return;   // no valid cells
     unsigned long long iters = 0, clamped = 0;   // per lane, for its particles
     bool overflow_any = false;
     const int gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
@@ -2363,7 +2375,7 @@ __global__ void __launch_bounds__(256) k_update(Params p, const int *__restrict_
                                                 double *__restrict__ m, double *__restrict__ u, float4 *__restrict__ posf,
                                                 double *__restrict__ fluxSums, unsigned *__restrict__ status) {
     const unsigned st0 = *status;
-    if (st0 & (ST_NGB_OVERFLOW | ST_CAPACITY | ST_TIMEOUT)) return;
+    if (st0 & (ST_NGB_OVERFLOW | ST_CAPACITY | ST_TIMEOUT | ST_GRID)) return;
     double *X[3] = {x, y, z};
     double *Vv[3] = {vx, vy, vz};
     unsigned st_local = 0;
@@ -2465,7 +2477,7 @@ __global__ void __launch_bounds__(256) k_update(Params p, const int *__restrict_
 // like the update, when the step is to be repeated with more capacity).
 __global__ void k_advance_time(int nmembers, const double *__restrict__ dt, double *__restrict__ simTime,
                                int *__restrict__ stepsDone, const unsigned *__restrict__ status) {
-    if (*status & (ST_NGB_OVERFLOW | ST_CAPACITY | ST_TIMEOUT)) return;
+    if (*status & (ST_NGB_OVERFLOW | ST_CAPACITY | ST_TIMEOUT | ST_GRID)) return;
     for (int mi = blockIdx.x * blockDim.x + threadIdx.x; mi < nmembers; mi += gridDim.x * blockDim.x)
         simTime[mi] += dt[mi];
     if (blockIdx.x == 0 && threadIdx.x == 0) *stepsDone += 1;
@@ -2516,8 +2528,8 @@ void launch_binning(StepArgs &a) {
     cudaMemsetAsync(a.cellFill, 0, sizeof(int) * (size_t)(p.ncells_cap + 1), s);
     k_assign<D><<<blocksN, T, 0, s>>>(a.x, a.y, a.z, p.n, a.memberOf, a.grids, a.cell, a.cellCount, a.status);
     exclusive_scan(a.cellCount, p.ncells_cap, a.cellStart, a.scanTiles, a.scanTotal, s);
-    k_fill_cells<<<blocksN, T, 0, s>>>(a.cell, p.n, a.cellStart, a.cellFill, a.cellList);
-    k_sort_cells<<<(p.ncells_cap + T - 1) / T, T, 0, s>>>(a.cellTotal, a.cellStart, a.cellList);
+    k_fill_cells<<<blocksN, T, 0, s>>>(a.cell, p.n, a.cellStart, a.cellFill, a.cellList, a.status);
+    k_sort_cells<<<(p.ncells_cap + T - 1) / T, T, 0, s>>>(a.cellTotal, a.cellStart, a.cellList, a.status);
 }
 
 // Smoothing lengths of every particle on the current grid (k_hsolve).

@@ -16,19 +16,24 @@ GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
 #    fluxes): scale 0, every entry to 1e-12 of its own value (measured
 #    <= 9e-15 on every case; the 1e-5 background pressure of a Sedov blast is
 #    held to 1e-12 of 1e-5);
-#  * per-particle flux sums mF, eF, vF: sum_j |F_ij| of the component (the
-#    oracle's per-interaction fluxes); the new state: m, v, u from the
-#    update's terms (|m v| + dt sum_j |F_p,ij|) / m_new and the like, x with
-#    |v| dt.  A blast's pressure fluxes nearly cancel on every particle, so
-#    |vF| is a small fraction of sum |F|: 1e-14 of the terms is 1e-12 of the
-#    sum and more;
+#  * per-particle flux sums mF, eF, vF: sum_j max(|F_ij|, SUM_FLOOR max|F|)
+#    of the component (the oracle's per-interaction fluxes, each with the
+#    floor of the per-interaction gate below, so that a sum is held to what
+#    its terms are held to); the new state: m, v, u from the update's terms
+#    (|m v| + dt sum_j |F_p,ij|) / m_new and the like, x with |v| dt.  A
+#    blast's pressure fluxes nearly cancel on every particle, so |vF| is a
+#    small fraction of sum |F|: 1e-14 of the terms is 1e-12 of the sum and
+#    more; in quiet regions the mass flux rho* (A . v*) is small against the
+#    terms of u* = (uL + uR)/2 + (fR - fL)/2, which cancel;
 #  * raw gradients, E^-1 and the per-interaction fluxes: SUM_FLOOR of the
 #    field's largest magnitude (sums over neighbours whose terms cancel in
 #    uniform regions);
 #  * limited gradients: LIMITER_RTOL.  The limiter factor is the reference's
 #    ratio (psi_max_ngb - psi_i) / (psi_max_mid - psi_i), whose differences are
 #    1e-4 of psi_i in the nearly uniform background of a blast: a rounding of
-#    psi_i moves the factor by 1e-12 relative and more;
+#    psi_i moves the factor by 1e-12 relative and more.  The face states,
+#    fluxes and new state of a particle whose limited gradient needs it, and
+#    of its neighbours (the faces it shares), inherit it: LIMITER_RTOL there;
 #  * Newton ties: faces whose iterations stop one step apart on the two sides
 #    (the GPU seeds Newton with a two-rarefaction guess accurate to ~1e-13, so
 #    where the first step's change lies within that of the 1e-10 stopping
@@ -125,10 +130,13 @@ def riemann_ties(g, o):
     return tie, touched
 
 
-def assert_masked(a, b, floor, what, mask=None, rtol=FIELD_RTOL, rtol_masked=RIEMANN_TIE_RTOL, terms=None):
+def assert_masked(a, b, floor, what, mask=None, rtol=FIELD_RTOL, rtol_masked=RIEMANN_TIE_RTOL, terms=None,
+                  limits=None):
     """The per-element gate: |a - b| <= rtol * max(|b|, floor * max|b|,
     terms) (terms: the per-entry magnitude of the terms b is computed from,
-    or None), entries under `mask` (Newton ties) held to rtol_masked."""
+    or None), entries under `mask` (Newton ties) held to rtol_masked; or,
+    with `limits` (one tolerance per particle or slot, first axis), to
+    those."""
     a = np.asarray(a, dtype=np.float64)
     b = np.asarray(b, dtype=np.float64)
     if b.size == 0:
@@ -141,7 +149,12 @@ def assert_masked(a, b, floor, what, mask=None, rtol=FIELD_RTOL, rtol_masked=RIE
     with np.errstate(divide="ignore", invalid="ignore"):
         r = np.where(err == 0.0, 0.0, err / den)
     lim = np.full(b.shape, rtol)
-    if mask is not None:
+    if limits is not None:
+        L = np.asarray(limits, dtype=np.float64)
+        if b.ndim > 1:
+            L = np.broadcast_to(L.reshape(-1, *([1] * (b.ndim - 1))), b.shape)
+        lim = np.array(L, dtype=np.float64)
+    elif mask is not None:
         m = np.asarray(mask, dtype=bool)
         if b.ndim > 1:
             m = np.broadcast_to(m.reshape(-1, *([1] * (b.ndim - 1))), b.shape)
@@ -155,10 +168,14 @@ def assert_masked(a, b, floor, what, mask=None, rtol=FIELD_RTOL, rtol_masked=RIE
 
 
 def flux_terms(F, off, dim):
-    """sum over each particle's interactions of |F_ij| per flux component
-    (N x (dim + 2)): the magnitude of the terms of its flux sums."""
+    """sum over each particle's interactions of max(|F_ij|, SUM_FLOOR
+    max_kl |F_kl|) per flux component (N x (dim + 2)): the magnitude of the
+    terms of its flux sums, each at least the floor the per-interaction gate
+    allows it."""
     nv = dim + 2
     A = np.abs(np.asarray(F, dtype=np.float64).reshape(-1, nv))
+    if A.size:
+        A = np.maximum(A, SUM_FLOOR * A.max(axis=0, keepdims=True))
     cs = np.zeros((A.shape[0] + 1, nv))
     np.cumsum(A, axis=0, out=cs[1:])
     off = np.asarray(off, dtype=np.int64)
@@ -186,16 +203,48 @@ def state_terms(pre, post, S, dt, dim):
     return out
 
 
-def assert_state(gs, ost, touched, what="", terms=None):
+def assert_state(gs, ost, limits, what="", terms=None):
     """The state after one step from identical inputs, each entry relative to
     the magnitude of its update's terms (state_terms; without them a
-    SUM_FLOOR floor for velocities); the particles of a Newton tie to
-    RIEMANN_TIE_RTOL."""
+    SUM_FLOOR floor for velocities), held to the particle's tolerance
+    (step_limits; positions, which move with the old velocity, to
+    FIELD_RTOL)."""
     for k, v in ost.items():
         t = None if terms is None else terms.get(k)
         floor = 0.0 if (t is not None or k in ("m", "u", "x", "y", "z")) else SUM_FLOOR
-        mask = None if k in ("x", "y", "z") else touched
-        assert_masked(gs[k], v, floor, what + "state " + k, mask, terms=t)
+        lim = None if k in ("x", "y", "z") else limits
+        assert_masked(gs[k], v, floor, what + "state " + k, terms=t, limits=lim)
+
+
+def step_limits(g, o, dim):
+    """Per-particle and per-slot tolerances of the entries downstream of the
+    limiter and the face solve: FIELD_RTOL; LIMITER_RTOL for a particle whose
+    limited gradient needs more than FIELD_RTOL (an ill-conditioned limiter
+    factor) and for its neighbours; RIEMANN_TIE_RTOL for the particles of a
+    Newton tie.  Returns (per-particle limits, per-slot limits, ties)."""
+    off = np.asarray(o.get("off"), dtype=np.int64)
+    n = off.size - 1
+    nnl = np.asarray(o.get("nnl")).astype(np.int64) & ((1 << 29) - 1)
+    owner = np.repeat(np.arange(n), np.diff(off))
+    sens = np.zeros(n, dtype=bool)
+    for f in ["rho", "vx", "vy"] + (["vz"] if dim == 3 else []) + ["P"]:
+        a = np.asarray(g.get("grad_" + f), dtype=np.float64)
+        b = np.asarray(o.get("grad_" + f), dtype=np.float64)
+        den = np.maximum(np.abs(b), SUM_FLOOR * np.max(np.abs(b)))
+        err = np.abs(a - b)
+        with np.errstate(divide="ignore", invalid="ignore"):
+            r = np.where(err == 0.0, 0.0, err / den)
+        sens |= (r.reshape(n, 3) > FIELD_RTOL).any(axis=1)
+    ring = sens.copy()
+    ring[nnl[sens[owner]]] = True
+    ring[owner[sens[nnl]]] = True
+    tie, touched = riemann_ties(g, o)
+    lim = np.full(n, FIELD_RTOL)
+    lim[ring] = LIMITER_RTOL
+    lim[touched] = RIEMANN_TIE_RTOL
+    slot = np.maximum(lim[owner], lim[nnl])
+    slot[tie] = RIEMANN_TIE_RTOL
+    return lim, slot, tie
 
 
 def compare_step(g, o, dim, slots=True, what="", pre=None):
@@ -217,13 +266,13 @@ def compare_step(g, o, dim, slots=True, what="", pre=None):
         assert_close(g.get("grad_" + f), o.get("grad_" + f), rtol=LIMITER_RTOL, floor=SUM_FLOOR,
                      what=what + "grad_" + f)
     assert_close(g.get("B"), o.get("B"), floor=SUM_FLOOR, what=what + "B")
-    tie, touched = riemann_ties(g, o)
+    lim, slot_lim, tie = step_limits(g, o, dim)
     nfaces = max(int(o.get("stats")[0]), 1)
     assert tie.sum() / 2 <= MAX_TIE_FRACTION * nfaces + 1, f"{what}{tie.sum() // 2} Newton ties"
     nv = dim + 2
     Fo = o.get("F")
     if slots:
-        assert_masked(g.get("F").reshape(-1, nv), Fo.reshape(-1, nv), SUM_FLOOR, what + "F", tie)
+        assert_masked(g.get("F").reshape(-1, nv), Fo.reshape(-1, nv), SUM_FLOOR, what + "F", limits=slot_lim)
     S = flux_terms(Fo, o.get("off"), dim)
     del Fo
     for k, cols in (("mF", [0]), ("eF", [1]), ("vF", list(range(2, nv)))):
@@ -232,10 +281,10 @@ def compare_step(g, o, dim, slots=True, what="", pre=None):
             a = a.reshape(-1, 3)[:, :dim]
             b = b.reshape(-1, 3)[:, :dim]
         t = S[:, cols] if k == "vF" else S[:, cols[0]]
-        assert_masked(a, b, 0.0, what + k, touched, terms=t)
+        assert_masked(a, b, 0.0, what + k, terms=t, limits=lim)
     ost = o.state()
     terms = state_terms(pre, ost, S, float(o.get("dt")[0]), dim) if pre is not None else None
-    assert_state(g.get_state(), ost, touched, what, terms)
+    assert_state(g.get_state(), ost, lim, what, terms)
     return int(tie.sum() // 2)
 
 

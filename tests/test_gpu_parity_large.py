@@ -24,7 +24,7 @@ import pytest
 from meshlesshydro_gb300 import ic
 from meshlesshydro_gb300.config import MFVConfig
 from helpers import (MAX_TIE_FRACTION, assert_close, assert_state, compare_step, flux_terms, l1_rel,
-                     pset_from_state, riemann_ties, state_of, state_terms)
+                     pset_from_state, state_of, state_terms, step_limits)
 
 pytestmark = pytest.mark.gpu
 
@@ -78,11 +78,11 @@ def _per_step_and_free_run(orc, p, cfg, nsteps, what, free_fields=("rho",)):
         np.testing.assert_array_equal(g.get("nnl"), o.get("nnl"), err_msg=f"{what}: nnl at step {k}")
         assert_close(g.get("rho"), o.get("rho"), floor=0.0, what=f"{what} step {k}: rho")
         assert_close(g.get("dt"), o.get("dt"), floor=0.0, what=f"{what} step {k}: dt")
-        tie, touched = riemann_ties(g, o)
+        lim, _, tie = step_limits(g, o, cfg.dim)
         ties += int(tie.sum() // 2)
         ost = o.state()
         terms = state_terms(pre, ost, flux_terms(o.get("F"), o.get("off"), cfg.dim), float(o.get("dt")[0]), cfg.dim)
-        assert_state(g.get_state(), ost, touched, what=f"{what} step {k}: ", terms=terms)
+        assert_state(g.get_state(), ost, lim, what=f"{what} step {k}: ", terms=terms)
     faces = max(int(o.get("stats")[0]), 1)
     assert ties <= MAX_TIE_FRACTION * faces * nsteps + 1, f"{what}: {ties} Newton ties in {nsteps} steps"
     # free run: the oracle's final state after nsteps, and its density at the
