@@ -42,8 +42,10 @@ WORKLOADS = {
     "kh100": dict(kind="kh", n_side=100),
     # 256 independent 2D KH runs, N log-uniform in [2500, 40000], one context
     "kh_ens256": dict(kind="ensemble", members=256),
-    # 64 blasts in the periodic 64^3 cube: strong shocks everywhere
-    "multi_blast64": dict(kind="multi_blast", n_side=64, n_blasts=64),
+    # 64 blasts in the periodic 64^3 cube: strong shocks everywhere (energy
+    # 0.02 in all: the blast-to-background pressure ratio of 16 blasts of
+    # energy 0.1 in all on 24^3)
+    "multi_blast64": dict(kind="multi_blast", n_side=64, n_blasts=64, energy=0.02),
 }
 METRIC = "particle-updates/s per MFV step on 1 GB300"
 # kernels launched by one plain mlh_step iteration (csrc/mlh_kernels.cu,
@@ -57,23 +59,32 @@ LAUNCHES_PER_STEP = 20
 # What each kernel of the step executes per unit (particle, or canonical
 # face for the face pass), from ncu captures of the same kernels: FP64
 # operations (2 x DFMA + DADD + DMUL thread instructions per unit) and DRAM
-# bytes (read + write per unit); 3D on the 64^3 periodic Sedov step, 2D on 32
-# members of the Kelvin-Helmholtz ensemble.  These are executed, not
+# bytes (read + write per unit); 3D on the 64^3 periodic Sedov step (the time
+# step inside the gradients' first pass, the face pass as its first pass and
+# the second Newton pass over the queue), 2D on 32 members of the
+# Kelvin-Helmholtz ensemble (captured with the time step as its own kernel:
+# the gradients' row is the sum of the two).  These are executed, not
 # algorithmic, operations: a kernel cannot execute more than the FP64 pipe
 # issues, so the rates they give are bounded by the pipe's peak.
 KERNEL_UNITS = {"neighbours_density": "particle", "timestep": "particle", "gradients_limiter": "particle",
                 "face_links": "particle", "faces_riemann": "face", "gather_update": "particle"}
 KERNEL_EXEC = {
-    3: {"neighbours_density": (1030.0, 917.0), "timestep": (607.0, 652.0), "gradients_limiter": (3747.0, 1692.0),
-        "face_links": (0.0, 1010.0), "faces_riemann": (541.0, 298.0), "gather_update": (214.0, 1504.0)},
-    2: {"neighbours_density": (597.0, 733.0), "timestep": (311.0, 748.0), "gradients_limiter": (1382.0, 1962.0),
+    3: {"neighbours_density": (1030.1, 850.3), "timestep": (0.0, 0.0), "gradients_limiter": (4260.5, 1978.9),
+        "face_links": (0.0, 1010.9), "faces_riemann": (557.8, 301.4), "gather_update": (214.0, 1507.8)},
+    2: {"neighbours_density": (597.0, 733.0), "timestep": (0.0, 0.0), "gradients_limiter": (1693.0, 2710.0),
         "face_links": (0.0, 781.0), "faces_riemann": (391.0, 364.0), "gather_update": (122.0, 915.0)},
 }
+# FP64 thread instructions (DFMA + DADD + DMUL) per unit of the same 3D
+# captures: what the FP64 pipe issues, each instruction one lane-slot
+KERNEL_FP64_INSTR = {
+    3: {"neighbours_density": 793.1, "timestep": 0.0, "gradients_limiter": 2619.0, "face_links": 0.0,
+        "faces_riemann": 384.6, "gather_update": 196.0},
+}
 # FP64 pipe active (sm__pipe_fp64_cycles_active over elapsed cycles) of the
-# same captures
+# same 3D captures
 KERNEL_FP64_PIPE = {
-    3: {"neighbours_density": 0.59, "timestep": 0.85, "gradients_limiter": 0.90, "faces_riemann": 0.86,
-        "gather_update": None, "face_links": 0.0},
+    3: {"neighbours_density": 0.587, "timestep": None, "gradients_limiter": 0.891, "faces_riemann": 0.870,
+        "gather_update": 0.760, "face_links": 0.0},
 }
 # Operations of the reference's method per unit, counted by the
 # operation-counting build of the oracle (oracle/flops.py; every addition,
@@ -106,9 +117,14 @@ def kernel_rooflines(kernel_ms: dict, dim: int, particles: float, faces: float, 
         s = ms / 1e3
         tf = fl * units / s / 1e12
         gbs = by * units / s / 1e9
+        ins = KERNEL_FP64_INSTR.get(dim, {}).get(k)
+        ins_rate = ins * units / s if ins is not None else None
         out[k] = {"ms_per_step": ms, "unit": unit, "units_per_step": units,
                   "fp64_flops_per_unit": fl, "fp64_tflops": tf,
                   "fp64_frac": tf / fp64_peak_tflops if fp64_peak_tflops else None,
+                  "fp64_instr_per_unit": ins,
+                  "fp64_instr_frac": (ins_rate / (fp64_peak_tflops * 1e12 / 2.0))
+                  if (ins_rate is not None and fp64_peak_tflops) else None,
                   "fp64_pipe_active_ncu": KERNEL_FP64_PIPE.get(dim, {}).get(k),
                   "dram_bytes_per_unit": by, "hbm_gbs": gbs,
                   "hbm_frac": gbs / hbm_peak_gbs if hbm_peak_gbs else None,
@@ -136,7 +152,7 @@ def make_workload(name: str, seed_offset: int = 0):
         p = ic.sedov(n_side=w["n_side"], seed=2 + seed_offset)
         return p, MFVConfig.sedov(p, periodic=w["periodic"])
     if w["kind"] == "multi_blast":
-        p = ic.multi_blast(n_side=w["n_side"], n_blasts=w["n_blasts"], seed=11 + seed_offset)
+        p = ic.multi_blast(n_side=w["n_side"], n_blasts=w["n_blasts"], seed=11 + seed_offset, energy=w["energy"])
         return p, MFVConfig.sedov(p, periodic=True)
     p = ic.kelvin_helmholtz(n_side=w["n_side"], seed=1 + seed_offset)
     return p, MFVConfig.kelvin_helmholtz(p)
@@ -324,14 +340,16 @@ def per_step(kt):
     return {k: v[1] / max(v[0], 1) for k, v in kt.items()}
 
 
-def timed_steps(sim, warmup, steps):
-    """warmup steps, then `steps` timed steps: (stats, wall seconds)."""
+def timed_steps(sim, warmup, steps, check=True):
+    """warmup steps, then `steps` timed steps: (stats, wall seconds).
+    check=False: non-physical values (which the reference only warns about)
+    are reported in the status instead of raised."""
     import torch
     if warmup:
-        sim.step(warmup)
+        sim.step(warmup, check=check)
     torch.cuda.synchronize()
     t0 = time.perf_counter()
-    st = sim.step(steps)
+    st = sim.step(steps, check=check)
     torch.cuda.synchronize()
     return st, time.perf_counter() - t0
 
@@ -344,15 +362,15 @@ def train_learned_guess(runtime, budget_rows: int = 10_000_000, epochs: int = 12
     50 and 75) and the 100x100 Kelvin-Helmholtz run (100 steps: every face of
     every 5th step), at most budget_rows rows (a seeded subsample beyond).
     A run is harvested up to its first step with non-physical values (which
-    the reference only warns about).  Seeds differ from the evaluated
-    workloads."""
+    the reference only warns about).  The evaluated workloads are other sizes
+    and set-ups (the 128^3 Sedov lattice, the 64-blast 64^3 cube)."""
     from meshlesshydro_gb300 import ic
     from meshlesshydro_gb300.config import MFVConfig
     t0 = time.perf_counter()
     xs, ts = [], []
     n_strong = n_sedov = n_kh = 0
     stopped = {}
-    p = ic.sedov(n_side=64, seed=12)
+    p = ic.sedov(n_side=64, seed=2)
     s = runtime.Simulation(MFVConfig.sedov(p, periodic=True), p)
     for k in range(100):
         try:   # a run that reports non-physical values is not harvested further
@@ -428,14 +446,14 @@ def learned_vs_plain(runtime, make, w, args, tuning_plain=None, st_plain=None, k
     if st_plain is None:
         sp = make()
         tuning_plain = sp.autotune(2)
-        st_plain, _ = timed_steps(sp, args.warmup, args.steps)
+        st_plain, _ = timed_steps(sp, args.warmup, args.steps, check=False)
         rho_plain = sp.get("rho")
         kt_plain = kernel_breakdown(sp, args.steps)
         sp.close()
     sl = make()
     sl.set_pstar_weights(w)
     tuning_l = sl.autotune(2)
-    st, _ = timed_steps(sl, args.warmup, args.steps)
+    st, _ = timed_steps(sl, args.warmup, args.steps, check=False)
     rho = sl.get("rho")
     kt = kernel_breakdown(sl, args.steps)
     sl.close()
@@ -456,7 +474,7 @@ def learned_vs_plain(runtime, make, w, args, tuning_plain=None, st_plain=None, k
         "plain_faces_kernel_ms_per_step": per_step(kt_plain).get("faces_riemann"),
         "density_L1_vs_plain": float(np.sum(np.abs(rho - rho_plain)) / np.sum(np.abs(rho_plain))),
         "tuning": tuning_l, "plain_tuning": tuning_plain,
-        "status": runtime.status_names(st.status)})
+        "status": runtime.status_names(st.status), "plain_status": runtime.status_names(st_plain.status)})
     return out
 
 
@@ -478,7 +496,7 @@ def learned_section(runtime, args, make_main, tuning, st_plain, kt_plain, rho_pl
     mk = lambda: runtime.Simulation(cm, pm)
     out["multi_blast64"] = learned_vs_plain(runtime, mk, w, args)
     out["multi_blast64"]["network_error_held_out"] = network_error(runtime, w, mk)
-    out["multi_blast64"]["workload"] = ("64 blasts (energy 0.1 in total) in the periodic 64^3 Sedov cube, "
+    out["multi_blast64"]["workload"] = ("64 blasts (energy 0.02 in total) in the periodic 64^3 Sedov cube, "
                                         "background pressure 1e-2 (ic.multi_blast)")
     return out, w
 
@@ -692,6 +710,11 @@ def run_mlh(args):
                                 "DMUL thread instructions per unit, on the 64^3 Sedov step), not the reference's "
                                 "operation count",
                 "fp64_pipe_active_ncu": KERNEL_FP64_PIPE.get(dim, {}).get(dom_name),
+                "fp64_instr_frac": ((KERNEL_FP64_INSTR[dim][dom_name] * units_launch / dom_avg_s) /
+                                    (fp64_peak * 1e12 / 2.0)) if (dim in KERNEL_FP64_INSTR and fp64_peak) else None,
+                "fp64_instr_frac_note": "FP64 thread instructions (DFMA + DADD + DMUL) per second over the probe's "
+                                        "(its TFLOP/s / 2, all FMAs): the pipe's issue rate, where frac counts an "
+                                        "FMA twice and an add or multiply once",
                 "peak_source": "measured: FP64 FMA-chain probe (mlh_probe_fp64_clock) on this GPU in this run",
                 "avg_launch_ms": dom_avg_s * 1e3,
                 "hbm_view": {"achieved_gbs": (by * units_launch / dom_avg_s / 1e9) if by else None,

@@ -95,14 +95,14 @@ def test_kernel_rooflines_arithmetic():
 def test_executed_rates_stay_below_the_fp64_peak():
     """The roofline unit passes the step-level check: on a measured Sedov
     128^3 step (2,097,152 particles, 33,556,373 faces, 41.74 ms; kernel times
-    per step: face passes 24.0, gradients 8.7, neighbours 4.4, time step 1.9,
-    gather and update 0.83 ms; FP64 FMA probe 1.058 TFLOP/s), every kernel's
+    per step: face passes 24.0, gradients with the time step 10.6, neighbours
+    4.4, gather and update 0.83 ms; FP64 FMA probe 1.058 TFLOP/s), every kernel's
     executed FP64 rate and the whole step's (the executed operations of all
     kernels over ms_per_step) stay at or below the peak.  The reference
     method's operation count would not (kept for comparison only)."""
     import bench
     n, faces, peak = 2097152.0, 33556373.0, 1.058
-    kt = {"faces_riemann": 24.0, "gradients_limiter": 8.7, "neighbours_density": 4.4, "timestep": 1.9,
+    kt = {"faces_riemann": 24.0, "gradients_limiter": 10.6, "neighbours_density": 4.4,
           "gather_update": 0.83}
     r = bench.kernel_rooflines(kt, 3, n, faces, peak, 6788.3)
     for k, v in r.items():
