@@ -61,9 +61,9 @@ LAUNCHES_PER_STEP = 20
 # operations (2 x DFMA + DADD + DMUL thread instructions per unit) and DRAM
 # bytes (read + write per unit); 3D on the 64^3 periodic Sedov step (the time
 # step inside the gradients' first pass, the face pass as its first pass and
-# the second Newton pass over the queue), 2D on 32 members of the
-# Kelvin-Helmholtz ensemble (captured with the time step as its own kernel:
-# the gradients' row is the sum of the two).  These are executed, not
+# the second Newton pass over the queue), 2D on the 256-member
+# Kelvin-Helmholtz ensemble (the face pass with the unfinished faces
+# continued inside the block).  These are executed, not
 # algorithmic, operations: a kernel cannot execute more than the FP64 pipe
 # issues, so the rates they give are bounded by the pipe's peak.
 KERNEL_UNITS = {"neighbours_density": "particle", "timestep": "particle", "gradients_limiter": "particle",
@@ -71,20 +71,24 @@ KERNEL_UNITS = {"neighbours_density": "particle", "timestep": "particle", "gradi
 KERNEL_EXEC = {
     3: {"neighbours_density": (1030.1, 850.3), "timestep": (0.0, 0.0), "gradients_limiter": (4260.5, 1978.9),
         "face_links": (0.0, 1010.9), "faces_riemann": (557.8, 301.4), "gather_update": (214.0, 1507.8)},
-    2: {"neighbours_density": (597.0, 733.0), "timestep": (0.0, 0.0), "gradients_limiter": (1693.0, 2710.0),
-        "face_links": (0.0, 781.0), "faces_riemann": (391.0, 364.0), "gather_update": (122.0, 915.0)},
+    2: {"neighbours_density": (596.7, 863.5), "timestep": (0.0, 0.0), "gradients_limiter": (1653.4, 2337.8),
+        "face_links": (0.0, 874.9), "faces_riemann": (367.4, 179.2), "gather_update": (122.0, 977.7)},
 }
-# FP64 thread instructions (DFMA + DADD + DMUL) per unit of the same 3D
+# FP64 thread instructions (DFMA + DADD + DMUL) per unit of the same
 # captures: what the FP64 pipe issues, each instruction one lane-slot
 KERNEL_FP64_INSTR = {
     3: {"neighbours_density": 793.1, "timestep": 0.0, "gradients_limiter": 2619.0, "face_links": 0.0,
         "faces_riemann": 384.6, "gather_update": 196.0},
+    2: {"neighbours_density": 443.7, "timestep": 0.0, "gradients_limiter": 1052.9, "face_links": 0.0,
+        "faces_riemann": 259.3, "gather_update": 108.0},
 }
 # FP64 pipe active (sm__pipe_fp64_cycles_active over elapsed cycles) of the
-# same 3D captures
+# same captures
 KERNEL_FP64_PIPE = {
     3: {"neighbours_density": 0.587, "timestep": None, "gradients_limiter": 0.891, "faces_riemann": 0.870,
         "gather_update": 0.760, "face_links": 0.0},
+    2: {"neighbours_density": 0.715, "timestep": None, "gradients_limiter": 0.895, "faces_riemann": 0.850,
+        "gather_update": 0.840, "face_links": 0.0},
 }
 # Operations of the reference's method per unit, counted by the
 # operation-counting build of the oracle (oracle/flops.py; every addition,

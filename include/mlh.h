@@ -147,8 +147,10 @@ typedef struct mlh_tuning {
                               * threads; 0: one pass (the plain gamma = 5/3
                               * step only) */
     int link_overlap;        /* 1: the face links run on a second stream beside
-                              * the time step and the gradients; 0: in order
-                              * on the step's stream */
+                              * the time step and the gradients; 2: inside the
+                              * gradients kernel, each particle's links before
+                              * its neighbour passes; 0: in order on the
+                              * step's stream */
     int persistent_binning;  /* 1: the binning (bounds, grid, cell assignment,
                               * counts, scan, cell lists) as one persistent
                               * cooperative kernel whose phases wait on one
@@ -160,15 +162,16 @@ typedef struct mlh_tuning {
 
 /* Autotuner: times the face-pass structures over candidate grids, then
  * candidate launch shapes of the face, gradient and neighbour kernels, then
- * whole steps with and without the overlapped face links and with and
- * without the persistent binning, over
+ * whole steps with the face links in order, overlapped on a second stream
+ * or inside the gradients kernel, and with and without the persistent
+ * binning, over
  * `trial_steps` steps each (from a saved copy of the
  * state, which is restored afterwards), keeps the fastest in the context and
  * reports them in *out (may be NULL).  Needs one state-sized temporary. */
 int mlh_autotune(mlh_ctx *ctx, int trial_steps, mlh_tuning *out);
 /* Set the launch shapes directly (for example those an autotuned context of
  * the same workload reported).  Threads per block: 64, 128 or 256; blocks
- * per SM 1..32; warps per SM 8..256; face_split 0, 1 or 2; link_overlap and
+ * per SM 1..32; warps per SM 8..256; face_split and link_overlap 0, 1 or 2;
  * persistent_binning 0 or 1.  MLH_ERR_INVALID otherwise. */
 int mlh_set_tuning(mlh_ctx *ctx, const mlh_tuning *tuning);
 

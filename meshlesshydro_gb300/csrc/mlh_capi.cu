@@ -671,7 +671,7 @@ int mlh_set_tuning(mlh_ctx *c, const mlh_tuning *t) {
     auto threads_ok = [](int v) { return v == 64 || v == 128 || v == 256; };
     if (!c || !t || !threads_ok(t->face_threads) || !threads_ok(t->grad_threads) || t->face_blocks_per_sm < 1 ||
         t->face_blocks_per_sm > 32 || t->nns_warps_per_sm < 8 || t->nns_warps_per_sm > 256 ||
-        t->face_split < 0 || t->face_split > 2 || t->link_overlap < 0 || t->link_overlap > 1 ||
+        t->face_split < 0 || t->face_split > 2 || t->link_overlap < 0 || t->link_overlap > 2 ||
         t->persistent_binning < 0 || t->persistent_binning > 1 || (t->persistent_binning && c->bin_blocks < 1)) {
         g_last_error = "invalid tuning";
         return MLH_ERR_INVALID;
@@ -789,7 +789,7 @@ int mlh_autotune(mlh_ctx *c, int trial_steps, mlh_tuning *out) {
         // whole steps without per-kernel timing (which serialises the
         // streams), the better of two trials each
         double best_step = 1e300;
-        for (int ov : {1, 0}) {
+        for (int ov : {1, 0, 2}) {
             c->tune.link_overlap = ov;
             for (int rep = 0; rep < 2; ++rep) {
                 if ((rc = restore())) goto done;

@@ -1305,6 +1305,122 @@ __global__ void k_dt_final(Params p, int nmembers, const unsigned long long *__r
     }
 }
 
+// ------------------------------------------------------------------ face links
+
+// Canonical faces: slot s of particle i with neighbour (or image parent)
+// j > i, the side on which Particles::solveRiemannProblems computes the flux
+// (Particles.cpp:1838-1858, 1886-1897).  Slot -> face id (+1 canonical, -1
+// copied with the opposite sign), face -> (i, slot, reverse slot).  The
+// reverse slot of a non-canonical slot is the first entry of j's list (real
+// part or image part) that refers to i, as in the reference's searches.
+// The face links of particle i (see k_link).
+__device__ __forceinline__ void link_particle(int i, const Params &p, const uint32_t *__restrict__ nbr,
+                                              const int *__restrict__ noi, const int *__restrict__ noiImg,
+                                              const int *__restrict__ faceOff, int *__restrict__ faceOf,
+                                              FaceRef *__restrict__ faces, unsigned *__restrict__ status) {
+    const size_t base = (size_t)i * p.K;
+    const int nr = noi[i], tot = nr + noiImg[i];
+    const uint4 *own = reinterpret_cast<const uint4 *>(nbr + base);
+    int rank = 0;
+    for (int s0 = 0; s0 < tot; s0 += 4) {
+        const uint4 q = own[s0 >> 2];
+        const uint32_t ev[4] = {q.x, q.y, q.z, q.w};
+        // per search: j, the length of j's list, the current 4-entry chunk,
+        // the canonical count and flags.  i is sought among j's real
+        // entries (no image bits) or among its images (image bits set), so
+        // an entry's own bits say whether it lies in the searched part.
+        constexpr unsigned ACT = 1u, BWD = 2u, IMG = 4u, FOUND = 8u;
+        int jj[4], jt[4], cur[4], cnt[4];
+        unsigned fl[4];
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+            const int s = s0 + k;
+            const int j = (int)(ev[k] & IDX_MASK);
+            jj[k] = j; jt[k] = 0; cur[k] = 0; cnt[k] = 0; fl[k] = 0u;
+            if (s >= tot) continue;
+            if (j > i) {
+                const int fid = faceOff[i] + rank;
+                ++rank;
+                if (fid >= p.faces_cap) { flag(status, ST_CAPACITY); faceOf[base + s] = 0; continue; }
+                faceOf[base + s] = fid + 1;
+                faces[fid].i = i;
+                faces[fid].slot = s;
+                continue;
+            }
+            jt[k] = noi[j] + noiImg[j];
+            const bool img = s >= nr;
+            // a particle that is its own image searches forward
+            const bool bwd = (img || 2 * s < nr) && j != i;
+            cur[k] = bwd ? (jt[k] - 1) >> 2 : 0;
+            fl[k] = ACT | (bwd ? BWD : 0u) | (img ? IMG : 0u);
+        }
+        for (;;) {
+            uint4 r[4];
+            bool any = false;
+#pragma unroll
+            for (int k = 0; k < 4; ++k) {
+                // past either end of j's list: not found
+                if ((fl[k] & BWD) ? cur[k] < 0 : cur[k] * 4 >= jt[k]) fl[k] &= ~ACT;
+                r[k] = (fl[k] & ACT) ? reinterpret_cast<const uint4 *>(nbr + (size_t)jj[k] * p.K)[cur[k]]
+                                     : make_uint4(0u, 0u, 0u, 0u);
+                any |= (fl[k] & ACT) != 0u;
+            }
+            if (!any) break;
+#pragma unroll
+            for (int k = 0; k < 4; ++k) {
+                if (!(fl[k] & ACT)) continue;
+                const bool bwd = (fl[k] & BWD) != 0u, img = (fl[k] & IMG) != 0u;
+                const uint32_t v[4] = {r[k].x, r[k].y, r[k].z, r[k].w};
+#pragma unroll
+                for (int mm = 0; mm < 4; ++mm) {
+                    const int m = bwd ? 3 - mm : mm;
+                    const int t = cur[k] * 4 + m;
+                    const uint32_t e = v[m];
+                    const int idx = (int)(e & IDX_MASK);
+                    if (!(fl[k] & FOUND) && t < jt[k]) {
+                        if (idx == i && ((e >> IMG_SHIFT) != 0u) == img) fl[k] |= FOUND;
+                        else cnt[k] += idx > jj[k];
+                    }
+                }
+                if (fl[k] & FOUND) fl[k] &= ~ACT;
+                else cur[k] += bwd ? -1 : 1;
+            }
+        }
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+            const int s = s0 + k;
+            if (s >= tot || jj[k] > i) continue;
+            if (!(fl[k] & FOUND)) { flag(status, ST_ASYMMETRIC); faceOf[base + s] = 0; continue; }
+            const int fid = (fl[k] & BWD) ? faceOff[jj[k] + 1] - 1 - cnt[k] : faceOff[jj[k]] + cnt[k];
+            if (fid >= p.faces_cap) { flag(status, ST_CAPACITY); faceOf[base + s] = 0; continue; }
+            faceOf[base + s] = -(fid + 1);
+            faces[fid].rslot = s;
+        }
+    }
+}
+
+__global__ void __launch_bounds__(256) k_link(Params p, const uint32_t *__restrict__ nbr, const int *__restrict__ noi,
+                                              const int *__restrict__ noiImg, const int *__restrict__ faceOff,
+                                              int *__restrict__ faceOf, FaceRef *__restrict__ faces,
+                                              unsigned *__restrict__ status) {
+    // faces[] was set to -1: the owner writes (i, slot), the slot on the other
+    // side writes rslot, so each field has exactly one writer.  A slot with
+    // j > i owns face faceOff[i] + (its rank among i's canonical slots).  A
+    // slot with j < i finds i in j's list (real part or image part) and the
+    // face's rank in j's list from j's canonical entries (index > j) on one
+    // side of it: searching forward, the rank is the count before i; searching
+    // backward from the end of j's list, it is faceCnt[j] - 1 - the count
+    // after i, faceCnt[j] = faceOff[j + 1] - faceOff[j] being the number of
+    // canonical entries of j's list.  The stencils of i and j mirror each
+    // other, so j early in i's list puts i late in j's list: those searches
+    // and the image searches (images sit at the end of the list) go backward.
+    // The own list is read four slots per load (K is a multiple of 4) and the
+    // searches of those four slots advance together, one 4-entry load of each
+    // list per round, so that a thread has up to four loads in flight.
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < p.n; i += gridDim.x * blockDim.x)
+        link_particle(i, p, nbr, noi, noiImg, faceOff, faceOf, faces, status);
+}
+
 // ------------------------------------------------------------------ gradients
 
 // Particles::compPsijTilde (Particles.cpp:1186-1254, 2292-2455): E_i =
@@ -1374,7 +1490,9 @@ __global__ void __launch_bounds__(256) k_gradients(Params p, const Member *__res
                                                    const int *__restrict__ noi, const int *__restrict__ noiImg,
                                                    Grad *__restrict__ grad, Grad *__restrict__ gradRaw,
                                                    double *__restrict__ psiOut,
-                                                   unsigned long long *__restrict__ dtbits) {
+                                                   unsigned long long *__restrict__ dtbits,
+                                                   const int *__restrict__ faceOff, int *__restrict__ faceOf,
+                                                   FaceRef *__restrict__ faces, unsigned *__restrict__ status) {
     constexpr int NF = D + 2;
     const int lane = threadIdx.x & 31;
     // warp-uniform loop: every lane takes part in the time-step reduction
@@ -1383,6 +1501,10 @@ __global__ void __launch_bounds__(256) k_gradients(Params p, const Member *__res
       int mi = -1;
       double dti = DBL_MAX_;
       if (i < p.n) {
+        // with faceOff, the particle's face links first (link_particle):
+        // integer searches whose load latency the other warps' FP64 work
+        // hides, and whose registers are free again before the passes below
+        if (faceOff) link_particle(i, p, nbr, noi, noiImg, faceOff, faceOf, faces, status);
         mi = memberOf ? memberOf[i] : 0;
         const GridInfo g = grids[mi];
         const double h = members[mi].h;
@@ -1573,115 +1695,6 @@ __global__ void __launch_bounds__(256) k_gradients(Params p, const Member *__res
             atomic_min_pos_double(dtbits + mi, dti);
         }
       }
-    }
-}
-
-// ------------------------------------------------------------------ face links
-
-// Canonical faces: slot s of particle i with neighbour (or image parent)
-// j > i, the side on which Particles::solveRiemannProblems computes the flux
-// (Particles.cpp:1838-1858, 1886-1897).  Slot -> face id (+1 canonical, -1
-// copied with the opposite sign), face -> (i, slot, reverse slot).  The
-// reverse slot of a non-canonical slot is the first entry of j's list (real
-// part or image part) that refers to i, as in the reference's searches.
-__global__ void __launch_bounds__(256) k_link(Params p, const uint32_t *__restrict__ nbr, const int *__restrict__ noi,
-                                              const int *__restrict__ noiImg, const int *__restrict__ faceOff,
-                                              int *__restrict__ faceOf, FaceRef *__restrict__ faces,
-                                              unsigned *__restrict__ status) {
-    // faces[] was set to -1: the owner writes (i, slot), the slot on the other
-    // side writes rslot, so each field has exactly one writer.  A slot with
-    // j > i owns face faceOff[i] + (its rank among i's canonical slots).  A
-    // slot with j < i finds i in j's list (real part or image part) and the
-    // face's rank in j's list from j's canonical entries (index > j) on one
-    // side of it: searching forward, the rank is the count before i; searching
-    // backward from the end of j's list, it is faceCnt[j] - 1 - the count
-    // after i, faceCnt[j] = faceOff[j + 1] - faceOff[j] being the number of
-    // canonical entries of j's list.  The stencils of i and j mirror each
-    // other, so j early in i's list puts i late in j's list: those searches
-    // and the image searches (images sit at the end of the list) go backward.
-    // The own list is read four slots per load (K is a multiple of 4) and the
-    // searches of those four slots advance together, one 4-entry load of each
-    // list per round, so that a thread has up to four loads in flight.
-    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < p.n; i += gridDim.x * blockDim.x) {
-        const size_t base = (size_t)i * p.K;
-        const int nr = noi[i], tot = nr + noiImg[i];
-        const uint4 *own = reinterpret_cast<const uint4 *>(nbr + base);
-        int rank = 0;
-        for (int s0 = 0; s0 < tot; s0 += 4) {
-            const uint4 q = own[s0 >> 2];
-            const uint32_t ev[4] = {q.x, q.y, q.z, q.w};
-            // per search: j, the length of j's list, the current 4-entry chunk,
-            // the canonical count and flags.  i is sought among j's real
-            // entries (no image bits) or among its images (image bits set), so
-            // an entry's own bits say whether it lies in the searched part.
-            constexpr unsigned ACT = 1u, BWD = 2u, IMG = 4u, FOUND = 8u;
-            int jj[4], jt[4], cur[4], cnt[4];
-            unsigned fl[4];
-#pragma unroll
-            for (int k = 0; k < 4; ++k) {
-                const int s = s0 + k;
-                const int j = (int)(ev[k] & IDX_MASK);
-                jj[k] = j; jt[k] = 0; cur[k] = 0; cnt[k] = 0; fl[k] = 0u;
-                if (s >= tot) continue;
-                if (j > i) {
-                    const int fid = faceOff[i] + rank;
-                    ++rank;
-                    if (fid >= p.faces_cap) { flag(status, ST_CAPACITY); faceOf[base + s] = 0; continue; }
-                    faceOf[base + s] = fid + 1;
-                    faces[fid].i = i;
-                    faces[fid].slot = s;
-                    continue;
-                }
-                jt[k] = noi[j] + noiImg[j];
-                const bool img = s >= nr;
-                // a particle that is its own image searches forward
-                const bool bwd = (img || 2 * s < nr) && j != i;
-                cur[k] = bwd ? (jt[k] - 1) >> 2 : 0;
-                fl[k] = ACT | (bwd ? BWD : 0u) | (img ? IMG : 0u);
-            }
-            for (;;) {
-                uint4 r[4];
-                bool any = false;
-#pragma unroll
-                for (int k = 0; k < 4; ++k) {
-                    // past either end of j's list: not found
-                    if ((fl[k] & BWD) ? cur[k] < 0 : cur[k] * 4 >= jt[k]) fl[k] &= ~ACT;
-                    r[k] = (fl[k] & ACT) ? reinterpret_cast<const uint4 *>(nbr + (size_t)jj[k] * p.K)[cur[k]]
-                                         : make_uint4(0u, 0u, 0u, 0u);
-                    any |= (fl[k] & ACT) != 0u;
-                }
-                if (!any) break;
-#pragma unroll
-                for (int k = 0; k < 4; ++k) {
-                    if (!(fl[k] & ACT)) continue;
-                    const bool bwd = (fl[k] & BWD) != 0u, img = (fl[k] & IMG) != 0u;
-                    const uint32_t v[4] = {r[k].x, r[k].y, r[k].z, r[k].w};
-#pragma unroll
-                    for (int mm = 0; mm < 4; ++mm) {
-                        const int m = bwd ? 3 - mm : mm;
-                        const int t = cur[k] * 4 + m;
-                        const uint32_t e = v[m];
-                        const int idx = (int)(e & IDX_MASK);
-                        if (!(fl[k] & FOUND) && t < jt[k]) {
-                            if (idx == i && ((e >> IMG_SHIFT) != 0u) == img) fl[k] |= FOUND;
-                            else cnt[k] += idx > jj[k];
-                        }
-                    }
-                    if (fl[k] & FOUND) fl[k] &= ~ACT;
-                    else cur[k] += bwd ? -1 : 1;
-                }
-            }
-#pragma unroll
-            for (int k = 0; k < 4; ++k) {
-                const int s = s0 + k;
-                if (s >= tot || jj[k] > i) continue;
-                if (!(fl[k] & FOUND)) { flag(status, ST_ASYMMETRIC); faceOf[base + s] = 0; continue; }
-                const int fid = (fl[k] & BWD) ? faceOff[jj[k] + 1] - 1 - cnt[k] : faceOff[jj[k]] + cnt[k];
-                if (fid >= p.faces_cap) { flag(status, ST_CAPACITY); faceOf[base + s] = 0; continue; }
-                faceOf[base + s] = -(fid + 1);
-                faces[fid].rslot = s;
-            }
-        }
     }
 }
 
@@ -2581,7 +2594,11 @@ void launch_step(StepArgs &a) {
     // the face links (integer work) need only the neighbour lists: without
     // per-kernel timing they run on the second stream while the time step and
     // the gradients keep the FP64 pipe busy
-    const bool overlap = a.stream2 && !a.timer && !a.stop_after_gradients && a.tune.link_overlap;
+    // link_overlap 2: the links inside the gradients kernel (after the scan of
+    // the canonical counts); 1: on the second stream beside the gradients;
+    // 0: in order
+    const bool fused = a.tune.link_overlap == 2 && !a.stop_after_gradients;
+    const bool overlap = !fused && a.stream2 && !a.timer && !a.stop_after_gradients && a.tune.link_overlap == 1;
     const int blocksLink = blocksN;
     auto launch_links = [&](cudaStream_t ls) {
         exclusive_scan(a.faceCnt, p.n, a.faceOff, a.scanTiles, a.scanTotal, ls);
@@ -2607,16 +2624,21 @@ void launch_step(StepArgs &a) {
         tock(KT_DT);
     }
     tick(KT_GRAD);
+    if (fused) {
+        exclusive_scan(a.faceCnt, p.n, a.faceOff, a.scanTiles, a.scanTotal, s);
+        cudaMemsetAsync(a.faces, 0xff, sizeof(FaceRef) * a.faces_cap, s);
+    }
     k_gradients<D><<<(p.n + gT - 1) / gT, gT, 0, s>>>(p, a.members, a.memberOf, a.grids, a.prim, a.geo, a.nbr, a.ww,
                                                       a.rr, a.noi, a.noiImg, a.grad, a.gradRaw, a.psi,
-                                                      (p.adaptive && !a.separate_dt) ? a.dtbits : nullptr);
+                                                      (p.adaptive && !a.separate_dt) ? a.dtbits : nullptr,
+                                                      fused ? a.faceOff : nullptr, a.faceOf, a.faces, a.status);
     k_dt_final<<<(a.nmembers + 127) / 128, 128, 0, s>>>(p, a.nmembers, a.dtbits, a.dt_max, a.dt);
     tock(KT_GRAD);
     if (a.stop_after_gradients) return;
 
     if (overlap) {
         cudaStreamWaitEvent(s, a.ev_join, 0);
-    } else {
+    } else if (!fused) {
         tick(KT_LINK);
         launch_links(s);
         tock(KT_LINK);

@@ -58,6 +58,7 @@ LIMITER_RTOL = 1e-10
 RIEMANN_TIE_RTOL = 1e-8
 MAX_TIE_FRACTION = 1e-3
 COND_EPS = 1e-15
+COND_CAP = 1e-6             # the largest tolerance a condition number can give
 EXACT_FIELDS = {"omega", "rho", "P", "dt"}
 
 
@@ -252,11 +253,11 @@ def step_limits(g, o, dim):
     # cond(E_i) of the oracle's E_i^-1, spread to the particles that share a face
     B = np.asarray(o.get("B"), dtype=np.float64).reshape(n, dim, dim)
     cond = np.linalg.cond(B)
-    cl = np.where(np.isfinite(cond), COND_EPS * cond, RIEMANN_TIE_RTOL)
+    cl = np.where(np.isfinite(cond), COND_EPS * cond, COND_CAP)
     slot_c = np.maximum(cl[owner], cl[nnl])
     cspread = cl.copy()
     np.maximum.at(cspread, owner, slot_c)
-    lim = np.maximum(lim, np.minimum(cspread, RIEMANN_TIE_RTOL))
+    lim = np.maximum(lim, np.minimum(cspread, COND_CAP))
     lim[touched] = np.maximum(lim[touched], RIEMANN_TIE_RTOL)
     slot = np.maximum(lim[owner], lim[nnl])
     slot[tie] = RIEMANN_TIE_RTOL

@@ -198,3 +198,25 @@ def test_multistep_density_l1(oracle_mod, name, nsteps, rtol):
     ro, rg = o.get("rho"), g.get("rho")
     l1 = np.sum(np.abs(rg - ro)) / np.sum(np.abs(ro))
     assert l1 <= rtol, f"L1 {l1:.3e}"
+
+
+@pytest.mark.parametrize("name", ["sedov16_periodic", "kh24"])
+def test_link_modes_bitwise(name):
+    """The face links in order, on a second stream beside the gradients, or
+    inside the gradients kernel (link_overlap 0, 1, 2): the same face table
+    and the same steps, bit for bit."""
+    p, cfg = CASES[name]
+    states, faces = [], []
+    for lo in (0, 1, 2):
+        sim = _sim(cfg, p)
+        sim.set_tuning({"face_threads": 128, "face_blocks_per_sm": 4, "grad_threads": 64,
+                        "nns_warps_per_sm": 32, "face_split": 1, "link_overlap": lo})
+        st = sim.step(3)
+        assert st.status == 0
+        states.append(sim.get_state())
+        faces.append(sim.get("face_of"))
+        sim.close()
+    for k in range(1, 3):
+        assert np.array_equal(faces[0], faces[k])
+        for key in states[0]:
+            assert np.array_equal(states[0][key], states[k][key]), key
