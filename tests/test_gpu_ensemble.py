@@ -132,7 +132,7 @@ def test_set_tuning_validates_and_keeps_bits():
         b.set_tuning({"face_threads": 96, "face_blocks_per_sm": 3, "grad_threads": 64, "nns_warps_per_sm": 16})
     with pytest.raises(runtime.MLHError):
         b.set_tuning({"face_threads": 256, "face_blocks_per_sm": 3, "grad_threads": 64, "nns_warps_per_sm": 16,
-                      "link_overlap": 2})
+                      "link_overlap": 3})
     a.step(2)
     b.step(2)
     c.step(2)

@@ -4,10 +4,12 @@ inputs.
 
 * Sedov 64^3 (262,144 particles), periodic and in the reference's own
   non-periodic mode (testcases/sedov/parameter.h:12): one step stage by stage,
-  then 100 steps in which the GPU starts every step from the oracle's state
-  (the per-step gate of tests/helpers.py, neighbour lists bit-exact every
-  step), and a free-running 100-step run whose density is compared by L1
-  (<= 1e-8 relative).
+  then up to 100 steps in which the GPU starts every step from the oracle's
+  state (the per-step gate of tests/helpers.py, neighbour lists bit-exact
+  every step), and a free-running run over the same steps whose density is
+  compared by L1 (<= 1e-8 relative).  The reference's scheme gives negative
+  internal energy at the blast's evacuated centre at step 64: both codes
+  report it at that step, which ends the comparison.
 * Sedov 128^3 (2,097,152 particles, the bench workload): one step, lists
   bit-exact, fields per element.
 * Kelvin-Helmholtz 100x100: 100 steps per-step gated, and every state field
@@ -64,36 +66,50 @@ def test_sedov64_one_step_stagewise(orc, periodic):
 
 def _per_step_and_free_run(orc, p, cfg, nsteps, what, free_fields=("rho",)):
     """nsteps oracle steps; before each, the GPU takes the oracle's state and
-    runs one step, gated per element (lists bit-exact).  Then a free-running
-    GPU run of nsteps from the initial state, compared with the oracle's
-    states by L1.  Returns the largest per-step error seen per field."""
+    runs one step, gated per element (lists bit-exact).  A step at which the
+    reference's own scheme gives non-physical values (the oracle's status)
+    ends the comparison: the GPU must report the same bits at the same step.
+    Then a free-running GPU run over the steps before it, from the initial
+    state, compared with the oracle's states by L1.  Returns the L1 errors
+    and the number of steps compared."""
     o = orc.Oracle(cfg, p)
     g = _sim(cfg, p)
     ties = 0
+    done = nsteps
+    ost = orho = None
     for k in range(nsteps):
         pre = o.state()
         g.set_state(pset_from_state(p, pre))
-        assert o.step() == 0, f"{what}: oracle status at step {k}"
-        g.step(1)
+        so = o.step()
+        sg = g.step(1, check=False).status
+        if so != 0:
+            assert sg & so == so, f"{what}: the oracle reports {so:#x} at step {k}, the GPU {sg:#x}"
+            done, ost, orho = k, pre, o.get("rho")
+            break
+        assert sg == 0, f"{what}: GPU status {sg:#x} at step {k}"
         np.testing.assert_array_equal(g.get("nnl"), o.get("nnl"), err_msg=f"{what}: nnl at step {k}")
         assert_close(g.get("rho"), o.get("rho"), floor=0.0, what=f"{what} step {k}: rho")
         assert_close(g.get("dt"), o.get("dt"), floor=0.0, what=f"{what} step {k}: dt")
         lim, _, tie = step_limits(g, o, cfg.dim)
         ties += int(tie.sum() // 2)
-        ost = o.state()
-        terms = state_terms(pre, ost, flux_terms(o.get("F"), o.get("off"), cfg.dim), float(o.get("dt")[0]), cfg.dim)
-        assert_state(g.get_state(), ost, lim, what=f"{what} step {k}: ", terms=terms)
+        ost_k = o.state()
+        terms = state_terms(pre, ost_k, flux_terms(o.get("F"), o.get("off"), cfg.dim), float(o.get("dt")[0]),
+                            cfg.dim)
+        assert_state(g.get_state(), ost_k, lim, what=f"{what} step {k}: ", terms=terms)
     faces = max(int(o.get("stats")[0]), 1)
-    assert ties <= MAX_TIE_FRACTION * faces * nsteps + 1, f"{what}: {ties} Newton ties in {nsteps} steps"
-    # free run: the oracle's final state after nsteps, and its density at the
-    # next step's density evaluation; the GPU the same from the initial state
-    ost = o.state()
-    assert o.step() == 0
-    orho = o.get("rho")
+    assert ties <= MAX_TIE_FRACTION * faces * max(done, 1) + 1, f"{what}: {ties} Newton ties in {done} steps"
+    if ost is None:
+        # the oracle's state after nsteps, and its density at the next step's
+        # density evaluation
+        ost = o.state()
+        o.step()
+        orho = o.get("rho")
+    # the free run: the GPU the same from the initial state
     g.set_state(p)
-    g.step(nsteps)
+    if done:
+        g.step(done)
     gst = g.get_state()
-    g.step(1)
+    g.step(1, check=False)
     grho = g.get("rho")
     out = {"rho": l1_rel(grho, orho)}
     for f in free_fields:
@@ -101,14 +117,21 @@ def _per_step_and_free_run(orc, p, cfg, nsteps, what, free_fields=("rho",)):
             out[f] = l1_rel(gst[f], ost[f])
     g.close()
     o.close()
-    return out
+    return out, done
 
 
 @pytest.mark.parametrize("periodic", [True, False], ids=["periodic", "nonperiodic"])
 def test_sedov64_100_steps(orc, periodic):
+    """100 steps, or up to the step at which the reference's scheme itself
+    gives non-physical values: at step 64 the blast's evacuated centre holds
+    particles with 3 neighbours and the oracle (the reference's arithmetic)
+    reports negative internal energy (and, non-periodic, negative mass); both
+    codes report it at that step, and every step before it is compared."""
     p, cfg = _sedov64(periodic)
-    l1 = _per_step_and_free_run(orc, p, cfg, 100, f"sedov64 periodic={periodic}")
-    assert l1["rho"] <= L1_RTOL, f"density L1 after 100 steps {l1['rho']:.3e}"
+    l1, done = _per_step_and_free_run(orc, p, cfg, 100, f"sedov64 periodic={periodic}")
+    print(f"sedov64 periodic={periodic}: {done} steps compared, density L1 {l1['rho']:.3e}")
+    assert done >= 60
+    assert l1["rho"] <= L1_RTOL, f"density L1 after {done} steps {l1['rho']:.3e}"
 
 
 def test_sedov128_one_step(orc):
@@ -127,7 +150,8 @@ def test_sedov128_one_step(orc):
 def test_kh100_100_steps_all_fields(orc):
     p = ic.kelvin_helmholtz(n_side=100, seed=1)
     cfg = MFVConfig.kelvin_helmholtz(p)
-    l1 = _per_step_and_free_run(orc, p, cfg, 100, "kh100", free_fields=("rho", "x", "y", "vx", "vy", "m", "u"))
+    l1, done = _per_step_and_free_run(orc, p, cfg, 100, "kh100", free_fields=("rho", "x", "y", "vx", "vy", "m", "u"))
+    assert done == 100
     for f, e in l1.items():
         assert e <= L1_RTOL, f"{f}: L1 after 100 steps {e:.3e}"
 
@@ -153,6 +177,7 @@ def test_kh24_mfm_and_fixed_particles(orc, mode):
         assert np.array_equal(gs["x"], p.x) and np.array_equal(gs["y"], p.y)
     g.close()
     o.close()
-    l1 = _per_step_and_free_run(orc, p, cfg, 5, mode, free_fields=("rho", "x", "y", "vx", "vy", "m", "u"))
+    l1, done = _per_step_and_free_run(orc, p, cfg, 5, mode, free_fields=("rho", "x", "y", "vx", "vy", "m", "u"))
+    assert done == 5
     for f, e in l1.items():
         assert e <= L1_RTOL, f"{mode} {f}: L1 after 5 steps {e:.3e}"
