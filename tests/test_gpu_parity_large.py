@@ -8,8 +8,8 @@ inputs.
   state (the per-step gate of tests/helpers.py, neighbour lists bit-exact
   every step), and a free-running run over the same steps whose density is
   compared by L1 (<= 1e-8 relative).  The reference's scheme gives negative
-  internal energy at the blast's evacuated centre at step 64: both codes
-  report it at that step, which ends the comparison.
+  internal energy at the blast's evacuated centre at step 64, which ends the
+  comparison.
 * Sedov 128^3 (2,097,152 particles, the bench workload): one step, lists
   bit-exact, fields per element.
 * Kelvin-Helmholtz 100x100: 100 steps per-step gated, and every state field
@@ -67,8 +67,8 @@ def test_sedov64_one_step_stagewise(orc, periodic):
 def _per_step_and_free_run(orc, p, cfg, nsteps, what, free_fields=("rho",)):
     """nsteps oracle steps; before each, the GPU takes the oracle's state and
     runs one step, gated per element (lists bit-exact).  A step at which the
-    reference's own scheme gives non-physical values (the oracle's status)
-    ends the comparison: the GPU must report the same bits at the same step.
+    reference's own scheme gives non-physical values (the oracle's status) is
+    gated too and ends the comparison.
     Then a free-running GPU run over the steps before it, from the initial
     state, compared with the oracle's states by L1.  Returns the L1 errors
     and the number of steps compared."""
@@ -82,11 +82,7 @@ def _per_step_and_free_run(orc, p, cfg, nsteps, what, free_fields=("rho",)):
         g.set_state(pset_from_state(p, pre))
         so = o.step()
         sg = g.step(1, check=False).status
-        if so != 0:
-            assert sg & so == so, f"{what}: the oracle reports {so:#x} at step {k}, the GPU {sg:#x}"
-            done, ost, orho = k, pre, o.get("rho")
-            break
-        assert sg == 0, f"{what}: GPU status {sg:#x} at step {k}"
+        assert so != 0 or sg == 0, f"{what}: GPU status {sg:#x} at step {k}"
         np.testing.assert_array_equal(g.get("nnl"), o.get("nnl"), err_msg=f"{what}: nnl at step {k}")
         assert_close(g.get("rho"), o.get("rho"), floor=0.0, what=f"{what} step {k}: rho")
         assert_close(g.get("dt"), o.get("dt"), floor=0.0, what=f"{what} step {k}: dt")
@@ -96,6 +92,14 @@ def _per_step_and_free_run(orc, p, cfg, nsteps, what, free_fields=("rho",)):
         terms = state_terms(pre, ost_k, flux_terms(o.get("F"), o.get("off"), cfg.dim), float(o.get("dt")[0]),
                             cfg.dim)
         assert_state(g.get_state(), ost_k, lim, what=f"{what} step {k}: ", terms=terms)
+        if so != 0:
+            # the reference's scheme gives non-physical values at this step
+            # (the state, gated above like every step, agrees; the sign of a
+            # value that crosses zero within its tolerance may differ, so the
+            # GPU's status is not required to match): no step after it is
+            # compared
+            done, ost, orho = k, pre, o.get("rho")
+            break
     faces = max(int(o.get("stats")[0]), 1)
     assert ties <= MAX_TIE_FRACTION * faces * max(done, 1) + 1, f"{what}: {ties} Newton ties in {done} steps"
     if ost is None:
@@ -125,8 +129,11 @@ def test_sedov64_100_steps(orc, periodic):
     """100 steps, or up to the step at which the reference's scheme itself
     gives non-physical values: at step 64 the blast's evacuated centre holds
     particles with 3 neighbours and the oracle (the reference's arithmetic)
-    reports negative internal energy (and, non-periodic, negative mass); both
-    codes report it at that step, and every step before it is compared."""
+    reports negative internal energy (and, non-periodic, negative mass).
+    Every step up to it is compared; there the value that crosses zero is a
+    cancellation (u = Q/m - |v|^2/2 on a particle with an ill-conditioned
+    E_i) and the GPU's lies on the other side of zero within its tolerance.
+    The free run compares the steps before it."""
     p, cfg = _sedov64(periodic)
     l1, done = _per_step_and_free_run(orc, p, cfg, 100, f"sedov64 periodic={periodic}")
     print(f"sedov64 periodic={periodic}: {done} steps compared, density L1 {l1['rho']:.3e}")
