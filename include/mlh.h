@@ -158,6 +158,16 @@ typedef struct mlh_tuning {
                               * runs out sets MLH_ERR_TIMEOUT and the step
                               * leaves the state untouched); 0: one launch per
                               * phase */
+    int fp32_filters;        /* single-precision filters that decide where the
+                              * FP64 arithmetic runs, with the same bits as
+                              * without them; bit 0 (1): the slope limiter
+                              * (Particles::slopeLimiter) evaluates the
+                              * face-point values f_ij only at the neighbours
+                              * where a bounded estimate can reach an extremum;
+                              * bit 1 (2): the time step (compGlobalTimestep)
+                              * evaluates v_sig only for the particles whose
+                              * bounded dt can be the minimum; 0: FP64 at every
+                              * neighbour */
 } mlh_tuning;
 
 /* Autotuner: times the face-pass structures over candidate grids, then
@@ -172,7 +182,7 @@ int mlh_autotune(mlh_ctx *ctx, int trial_steps, mlh_tuning *out);
 /* Set the launch shapes directly (for example those an autotuned context of
  * the same workload reported).  Threads per block: 64, 128 or 256; blocks
  * per SM 1..32; warps per SM 8..256; face_split and link_overlap 0, 1 or 2;
- * persistent_binning 0 or 1.  MLH_ERR_INVALID otherwise. */
+ * persistent_binning 0 or 1; fp32_filters 0..3.  MLH_ERR_INVALID otherwise. */
 int mlh_set_tuning(mlh_ctx *ctx, const mlh_tuning *tuning);
 
 /* Per-particle smoothing lengths of the current state (no counterpart in the
@@ -276,6 +286,11 @@ int mlh_probe_fp64_clock(double seconds, double *tflops, double *sm_mhz);
  * for n host values: rcp = 1/x, quot = y/x, rsqrt = 1/sqrt(x); for checking
  * their error against exact values. */
 int mlh_probe_fast_math(int n, const double *x, const double *y, double *rcp, double *quot, double *rsqrt);
+
+/* TEST HOOK.  The kernels' exact scalings by powers of two on the integer
+ * pipe, for n host values: half = x/2, quarter = x/4, twice = 2x; for checking
+ * them bit for bit against IEEE products (subnormal results included). */
+int mlh_probe_scale2(int n, const double *x, double *half, double *quarter, double *twice);
 
 /* TEST HOOK.  The grid barriers of the persistent binning wait for
  * `extra_arrivals` more blocks than the launch holds (nonzero: every wait runs

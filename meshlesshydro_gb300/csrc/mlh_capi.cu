@@ -62,6 +62,9 @@ struct mlh_ctx {
     // state
     double *x = nullptr, *y = nullptr, *z = nullptr, *vx = nullptr, *vy = nullptr, *vz = nullptr, *m = nullptr, *u = nullptr;
     float4 *posf = nullptr;
+    float4 *velf = nullptr;       // velocity and sound speed in single precision
+    float *dtlo = nullptr;        // time-step filter: lower bound on each particle's dt
+    unsigned *dtcap = nullptr;    // and the least upper bound of each simulation
     // simulations held by the context (1, or an ensemble stored back to back)
     int nmembers = 1;
     int bpm = 1;
@@ -275,6 +278,7 @@ StepArgs make_args(mlh_ctx *c, double dt_max) {
     a.dt_max = dt_max;
     a.x = c->x; a.y = c->y; a.z = c->z; a.vx = c->vx; a.vy = c->vy; a.vz = c->vz; a.m = c->m; a.u = c->u;
     a.posf = c->posf;
+    a.velf = c->velf; a.dtlo = c->dtlo; a.dtcap = c->dtcap;
     a.nmembers = c->nmembers; a.bpm = c->bpm;
     a.members = c->members; a.memberOf = c->memberOf;
     a.grids = c->grids; a.cellTotal = c->cellTotal; a.boundsPart = c->boundsPart;
@@ -434,7 +438,7 @@ static int create_impl(const mlh_config *cfg, int nmembers, const mlh_member *md
     size_t n = (size_t)c->n, nm = (size_t)nmembers;
 #define A(ptr, cnt) if (dalloc(&c->ptr, cnt) != cudaSuccess) return fail(cuda_fail(cudaGetLastError(), "cudaMalloc " #ptr))
     A(x, n); A(y, n); A(z, n); A(vx, n); A(vy, n); A(vz, n); A(m, n); A(u, n);
-    A(posf, n);
+    A(posf, n); A(velf, n); A(dtlo, n); A(dtcap, nm);
     A(members, nm); A(grids, nm); A(cellTotal, 1); A(boundsPart, nm * (size_t)c->bpm * 6);
     if (nmembers > 1) A(memberOf, n);
     A(cell, n); A(cellList, n);
@@ -536,7 +540,8 @@ void mlh_destroy(mlh_ctx *c) {
     void *ptrs[] = {c->x, c->y, c->z, c->vx, c->vy, c->vz, c->m, c->u, c->posf, c->members, c->memberOf, c->grids,
                     c->cellTotal, c->boundsPart, c->cell, c->cellList, c->noi, c->noiImg, c->faceCnt, c->faceOff,
                     c->prim, c->geo, c->grad, c->gradRaw, c->fluxSums, c->status, c->dtbits, c->newtonSum, c->dt,
-                    c->simTime, c->stepsDone, c->scanTiles, c->scanTotal, c->hp, c->neff, c->hstat, c->hpf, c->bar};
+                    c->simTime, c->stepsDone, c->scanTiles, c->scanTotal, c->hp, c->neff, c->hstat, c->hpf, c->bar,
+                    c->velf, c->dtlo, c->dtcap};
     for (void *q : ptrs) if (q) cudaFree(q);
     free_cell_buffers(c);
     free_neighbour_buffers(c);
@@ -672,7 +677,8 @@ int mlh_set_tuning(mlh_ctx *c, const mlh_tuning *t) {
     if (!c || !t || !threads_ok(t->face_threads) || !threads_ok(t->grad_threads) || t->face_blocks_per_sm < 1 ||
         t->face_blocks_per_sm > 32 || t->nns_warps_per_sm < 8 || t->nns_warps_per_sm > 256 ||
         t->face_split < 0 || t->face_split > 2 || t->link_overlap < 0 || t->link_overlap > 2 ||
-        t->persistent_binning < 0 || t->persistent_binning > 1 || (t->persistent_binning && c->bin_blocks < 1)) {
+        t->persistent_binning < 0 || t->persistent_binning > 1 || (t->persistent_binning && c->bin_blocks < 1) ||
+        t->fp32_filters < 0 || t->fp32_filters > 3) {
         g_last_error = "invalid tuning";
         return MLH_ERR_INVALID;
     }
@@ -684,6 +690,7 @@ int mlh_set_tuning(mlh_ctx *c, const mlh_tuning *t) {
     c->tune.face_split = t->face_split;
     c->tune.link_overlap = t->link_overlap;
     c->tune.persistent_binning = t->persistent_binning;
+    c->tune.fp32_filters = t->fp32_filters;
     drop_graph(c);
     return 0;
 }
@@ -835,6 +842,7 @@ done:
         out->face_split = c->tune.face_split;
         out->link_overlap = c->tune.link_overlap;
         out->persistent_binning = c->tune.persistent_binning;
+        out->fp32_filters = c->tune.fp32_filters;
     }
     return rc;
 }

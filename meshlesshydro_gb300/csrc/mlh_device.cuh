@@ -13,6 +13,8 @@ constexpr unsigned IMG_SHIFT = 29;
 constexpr unsigned IDX_MASK = (1u << IMG_SHIFT) - 1u;
 constexpr double DBL_MIN_ = 2.2250738585072014e-308;   // numeric_limits<double>::min()
 constexpr double DBL_MAX_ = 1.7976931348623157e+308;   // numeric_limits<double>::max()
+constexpr float FLT_MAX_ = 3.40282347e+38f;
+constexpr float FLT_INF_ = __builtin_huge_valf();
 
 // status bits (mirror MLH_ERR_* of include/mlh.h)
 enum : unsigned {
@@ -172,6 +174,43 @@ __device__ __forceinline__ double key_double(long long k) {
     return __longlong_as_double(k >= 0 ? k : (long long)(0x8000000000000000ull - (unsigned long long)k));
 }
 __device__ __forceinline__ bool dlt(double a, double b) { return ord_key(a) < ord_key(b); }
+
+// x * 2^-K (K = 1, 2) on the integer pipe, the IEEE product bit for bit: a
+// normal result takes K off the exponent; a subnormal one is the significand
+// (with its implicit bit) shifted right and rounded to nearest even; zero,
+// infinity and NaN stay as they are.  (A DMUL by 0.5 occupies the scarce FP64
+// pipe like an FMA.)  Straight-line selects, no branches: a branch would
+// split the caller's basic blocks and with them the compiler's fusing of
+// neighbouring multiplies and adds, which then could differ between the
+// kernels that inline the same code.
+template <int K>
+__device__ __forceinline__ double scale_down(double x) {
+    static_assert(K == 1 || K == 2, "scale_down: K = 1 or 2");
+    const unsigned long long b = (unsigned long long)__double_as_longlong(x);
+    const unsigned long long sign = b & 0x8000000000000000ull, mag = b ^ sign;
+    const unsigned long long E = mag >> 52;
+    const unsigned long long rn = mag - ((unsigned long long)K << 52);   // normal result (E > K)
+    // subnormal result (E <= K): shift 1..K, kept in range on the other paths
+    const unsigned long long sig = E ? ((mag & 0x000FFFFFFFFFFFFFull) | 0x0010000000000000ull) : mag;
+    const unsigned sh0 = (unsigned)K - (E ? (unsigned)E - 1u : 0u);
+    const unsigned sh = E <= (unsigned long long)K ? sh0 : 1u;
+    const unsigned long long q = sig >> sh, rem = sig & ((1ull << sh) - 1ull), hv = 1ull << (sh - 1u);
+    const unsigned long long rs = q + (unsigned long long)((rem > hv) | ((rem == hv) & ((q & 1ull) != 0)));
+    unsigned long long r = E > (unsigned long long)K ? rn : rs;
+    r = E == 0x7FFull ? mag : r;
+    return __longlong_as_double((long long)(r | sign));
+}
+__device__ __forceinline__ double half_of(double x) { return scale_down<1>(x); }
+// 2 x on the integer pipe, the IEEE product bit for bit (overflow to
+// infinity); straight-line selects as in scale_down
+__device__ __forceinline__ double twice(double x) {
+    const unsigned long long b = (unsigned long long)__double_as_longlong(x);
+    const unsigned long long sign = b & 0x8000000000000000ull, mag = b ^ sign;
+    unsigned long long r = mag < 0x0010000000000000ull ? mag << 1 : mag + 0x0010000000000000ull;
+    r = mag >= 0x7FE0000000000000ull ? 0x7FF0000000000000ull : r;   // overflow
+    r = mag >= 0x7FF0000000000000ull ? mag : r;                      // infinity, NaN
+    return __longlong_as_double((long long)(r | sign));
+}
 __device__ __forceinline__ bool dneg(double x) { return ord_key(x) < 0; }   // x < 0
 
 // Ghost image coordinate, Particles.cpp:2123-2142: a coordinate in the
@@ -212,7 +251,7 @@ __device__ __forceinline__ double frsqrt(double x) {
 #pragma unroll
     for (int k = 0; k < 2; ++k) {
         const double e = fma(-(x * y), y, 1.);
-        y = fma(0.5 * y, e, y);
+        y = fma(half_of(y), e, y);
     }
     return y;
 }

@@ -629,7 +629,7 @@ __global__ void __launch_bounds__(NNS_WARPS * 32, MLH_NNS_MINB) k_neighbours(
     const double *__restrict__ u, const int *__restrict__ cellTotal, const int *__restrict__ cellStart,
     const int *__restrict__ cellList, uint32_t *__restrict__ nbr, double *__restrict__ rr,
     double *__restrict__ ww, int *__restrict__ noi, int *__restrict__ noiImg, int *__restrict__ faceCnt,
-    Prim *__restrict__ prim, Geo *__restrict__ geo, unsigned *__restrict__ status) {
+    Prim *__restrict__ prim, Geo *__restrict__ geo, float4 *__restrict__ velf, unsigned *__restrict__ status) {
     const int K = p.K;
     const int CAP = K + 32;
     extern __shared__ __align__(16) unsigned char nns_smem[];
@@ -684,7 +684,12 @@ __global__ void __launch_bounds__(NNS_WARPS * 32, MLH_NNS_MINB) k_neighbours(
         geo[bi].V = frcp(bomega);
         const double irho = frcp(rho);   // also the face kernel's 1/rho_i
         geo[bi].irho = irho;
-        geo[bi].c = sqrt(p.gamma * P * irho);
+        const double cs = sqrt(p.gamma * P * irho);
+        geo[bi].c = cs;
+        // velocity and sound speed in single precision, for the time step's
+        // filter (k_gradients)
+        velf[bi] = make_float4(__double2float_rn(pr.vx), __double2float_rn(pr.vy), __double2float_rn(pr.vz),
+                               __double2float_rn(cs));
     };
     const int ncells = *cellTotal;
     for (int c = gw; c < ncells; c += nw) {
@@ -1251,14 +1256,24 @@ __global__ void __launch_bounds__(256) k_timestep(Params p, const Member *__rest
                                                   const int *__restrict__ memberOf, const Prim *__restrict__ prim,
                                                   const Geo *__restrict__ geo, const uint32_t *__restrict__ nbr,
                                                   const double *__restrict__ rr, const int *__restrict__ noi,
-                                                  unsigned long long *__restrict__ dtbits) {
+                                                  unsigned long long *__restrict__ dtbits,
+                                                  const float *__restrict__ dtlo, const unsigned *__restrict__ dtcap) {
     const int lane = threadIdx.x & 31;
     // warp-uniform loop: every lane takes part in the reductions below
     for (int i0 = (blockIdx.x * blockDim.x + threadIdx.x) & ~31; i0 < p.n; i0 += gridDim.x * blockDim.x) {
         const int i = i0 + lane;
         int mi = -1;
         double dti = DBL_MAX_;
-        if (i < p.n) {
+        // with dtlo (the single-precision filter of k_gradients): only the
+        // particles whose lower bound on dt reaches their simulation's least
+        // upper bound can hold the minimum (the others leave dti at DBL_MAX;
+        // every lane stays in the loop for the warp's reduction)
+        bool cand = i < p.n;
+        if (cand && dtlo) {
+            const int m = memberOf ? memberOf[i] : 0;
+            cand = dtlo[i] <= __uint_as_float(dtcap[m]);
+        }
+        if (cand) {
             mi = memberOf ? memberOf[i] : 0;
             const Prim pi = prim[i];
             const double ci = geo[i].c;
@@ -1481,8 +1496,18 @@ __device__ __forceinline__ double field_of(const Prim &q, int f) {
 // numeric_limits<double>::min(), the same expressions), on the positions and
 // velocities that pass loads anyway; the per-particle dt goes into the
 // per-member minimum (warp reduction, then one atomicMin on its bit pattern).
+// Register cap of the gradients kernel.  It waits on dependent gathers as
+// much as on the FP64 pipe (Sedov 64^3: FP64 pipe 73 % active, 17 % of the
+// warp slots occupied at 146 registers), so warps per SM matter: 128
+// registers (16 warps per SM, a small spill) took the Sedov 128^3 gradients
+// from 11.1-11.4 to 10.1 ms; 112 spill more and gave 10.4 ms.  Blocks of up
+// to 256 threads.
+#ifndef MLH_GRAD_MAXREG
+#define MLH_GRAD_MAXREG 128
+#endif
+#define MLH_GRAD_BOUNDS __maxnreg__(MLH_GRAD_MAXREG)
 template <int D>
-__global__ void __launch_bounds__(256) k_gradients(Params p, const Member *__restrict__ members,
+__global__ void MLH_GRAD_BOUNDS k_gradients(Params p, const Member *__restrict__ members,
                                                    const int *__restrict__ memberOf, const GridInfo *__restrict__ grids,
                                                    const Prim *__restrict__ prim, Geo *__restrict__ geo,
                                                    const uint32_t *__restrict__ nbr, const double *__restrict__ ww,
@@ -1492,7 +1517,10 @@ __global__ void __launch_bounds__(256) k_gradients(Params p, const Member *__res
                                                    double *__restrict__ psiOut,
                                                    unsigned long long *__restrict__ dtbits,
                                                    const int *__restrict__ faceOff, int *__restrict__ faceOf,
-                                                   FaceRef *__restrict__ faces, unsigned *__restrict__ status) {
+                                                   FaceRef *__restrict__ faces, unsigned *__restrict__ status,
+                                                   const float4 *__restrict__ posf, int fp32_filters,
+                                                   const float4 *__restrict__ velf, float *__restrict__ dtlo,
+                                                   unsigned *__restrict__ dtcap) {
     constexpr int NF = D + 2;
     const int lane = threadIdx.x & 31;
     // warp-uniform loop: every lane takes part in the time-step reduction
@@ -1500,6 +1528,7 @@ __global__ void __launch_bounds__(256) k_gradients(Params p, const Member *__res
       const int i = i0 + lane;
       int mi = -1;
       double dti = DBL_MAX_;
+      float dthi = FLT_INF_;   // with dtlo: upper bound on the particle's dt
       if (i < p.n) {
         // with faceOff, the particle's face links first (link_particle):
         // integer searches whose load latency the other warps' FP64 work
@@ -1517,6 +1546,21 @@ __global__ void __launch_bounds__(256) k_gradients(Params p, const Member *__res
         const bool want_dt = dtbits != nullptr;
         const double ci = want_dt ? geo[i].c : 0.;
         double vSig = DBL_MIN_;
+        // the time step's single-precision filter (dtlo): bounds on v_sig
+        // = max_j (c_i + c_j - min(0, v_ij . x_ij / r_ij)) over the real
+        // neighbours from the packed positions, velocities and sound speeds
+        const bool want_dtf = dtlo != nullptr;
+        float4 vif = make_float4(0.f, 0.f, 0.f, 0.f), xif4 = make_float4(0.f, 0.f, 0.f, 0.f);
+        float vlo = 0.f, vhi = 0.f, xbf = 0.f;
+        bool dt_exact = false;   // no usable bound: the particle is always a candidate
+        if (want_dtf) {
+            vif = velf[i];
+            xif4 = posf[i];
+            double xb = 0.;
+#pragma unroll
+            for (int a = 0; a < D; ++a) xb = fmax(xb, fmax(fabs(g.lo[a]), fabs(g.hi[a])));
+            xbf = __double2float_ru(xb);
+        }
         // E_i = V_i E' with E' = sum_j (x_j - x_i)(x_j - x_i)^T W_ij, so that
         // psi~_j(x_i) = E_i^-1 (x_j - x_i) W_ij V_i = E'^-1 (x_j - x_i) W_ij:
         // V_i cancels and neither pass multiplies by it
@@ -1546,8 +1590,47 @@ __global__ void __launch_bounds__(256) k_gradients(Params p, const Member *__res
                 const double vs = fma(-dv, ir, ci + cj);
                 vSig = dlt(vSig, vs) ? vs : vSig;
             }
+            if (want_dtf && s < nr) {
+                // |vs - vs64| <= B: the inputs' roundings (eps |c|, eps |v|,
+                // 3 eps X on each coordinate difference), the estimate's own
+                // and the FP64 expression's, at most eps (2 (c_i + c_j) +
+                // 2 vs + V (7 X / r + 8)) with V = |v_i|_1 + |v_j|_1; B is
+                // twice that
+                const int j = (int)(e & IDX_MASK);
+                const float4 vj = velf[j], xj4 = posf[j];
+                const float dx = __fsub_rn(xj4.x, xif4.x), dy = __fsub_rn(xj4.y, xif4.y),
+                            dz = D == 3 ? __fsub_rn(xj4.z, xif4.z) : 0.f;
+                const float wx = __fsub_rn(vif.x, vj.x), wy = __fsub_rn(vif.y, vj.y),
+                            wz = D == 3 ? __fsub_rn(vif.z, vj.z) : 0.f;
+                const float dvd = __fmaf_rn(wz, dz, __fmaf_rn(wy, dy, __fmul_rn(wx, dx)));   // v_ij . (x_j - x_i)
+                const float r = __fsqrt_rn(__fmaf_rn(dz, dz, __fmaf_rn(dy, dy, __fmul_rn(dx, dx))));
+                // -min(0, v_ij . x_ij / r) with x_ij = -(x_j - x_i)
+                const float T = dvd > 0.f ? __fdiv_rn(dvd, r) : 0.f;
+                const float vs = __fadd_rn(__fadd_rn(vif.w, vj.w), T);
+                const float V = fabsf(vif.x) + fabsf(vif.y) + fabsf(vif.z) + fabsf(vj.x) + fabsf(vj.y) + fabsf(vj.z);
+                constexpr float EPS32 = 5.9604645e-8f;
+                const float B = 2.f * EPS32 * (2.f * (vif.w + vj.w) + 2.f * vs + V * (7.f * __fdiv_ru(xbf, r) + 8.f));
+                dt_exact = dt_exact || !(r > 0.f) || !(B < 1e30f);
+                vlo = fmaxf(vlo, vs - B);
+                vhi = fmaxf(vhi, vs + B);
+            }
         }
         if (want_dt) dti = (p.adaptive_h ? p.cfl * p.hp[i] : members[mi].cfl_h) / vSig;
+        if (want_dtf) {
+            // dt = cfl_h / v_sig bounded below by the largest v_sig and above by
+            // the smallest (rounded outward, with the FP64 quotient's and the
+            // conversion's roundings); v_sig >= DBL_MIN when nothing is found
+            const float ch = __double2float_rn(p.adaptive_h ? p.cfl * p.hp[i] : members[mi].cfl_h);
+            constexpr float EPS32 = 5.9604645e-8f;
+            float lo = 0.f;
+            if (!dt_exact && nr > 0 && vhi > 0.f && vhi < FLT_INF_)
+                lo = __fmul_rd(__fdiv_rd(ch, vhi), 1.f - 4.f * EPS32);
+            if (!(lo < 1e38f)) lo = 0.f;   // below any cap
+            if (!dt_exact && nr > 0 && vlo > 0.f)
+                dthi = __fmul_ru(__fdiv_ru(ch, vlo), 1.f + 4.f * EPS32);
+            dtlo[i] = dt_exact ? 0.f : lo;
+            if (dt_exact) dthi = FLT_INF_;
+        }
 #pragma unroll
         for (int a = 0; a < D; ++a)
 #pragma unroll
@@ -1596,6 +1679,13 @@ __global__ void __launch_bounds__(256) k_gradients(Params p, const Member *__res
             }
             gradRaw[i] = graw;
         }
+        // B_i = E_i^-1 = E'^-1 / V_i = E'^-1 omega_i (kept for inspection; E
+        // is not needed after the gradient pass)
+        {
+            const double omega_i = geo[i].omega;
+#pragma unroll
+            for (int k = 0; k < D * D; ++k) geo[i].B[k] = E[k] * omega_i;
+        }
         if (p.slope) {
             // running extrema as integer keys (ord_key): the comparisons of
             // the reference's if (max < f) max = f stay off the FP64 pipe
@@ -1610,11 +1700,19 @@ __global__ void __launch_bounds__(256) k_gradients(Params p, const Member *__res
             // (for c = 1/2 both the scaling and its undoing are exact)
             const double cq = p.foqp ? .5 : hq / 4.;
             const double icq = p.foqp ? 2. : 1. / cq;
+            if (p.foqp) {   // the halving and doubling on the integer pipe
 #pragma unroll
-            for (int f = 0; f < NF; ++f)
+                for (int f = 0; f < NF; ++f)
 #pragma unroll
-                for (int a = 0; a < D; ++a) gr[f][a] *= cq;
-            for (int s = 0; s < tot; ++s) {
+                    for (int a = 0; a < D; ++a) gr[f][a] = half_of(gr[f][a]);
+            } else {
+#pragma unroll
+                for (int f = 0; f < NF; ++f)
+#pragma unroll
+                    for (int a = 0; a < D; ++a) gr[f][a] *= cq;
+            }
+            // one neighbour's f_ij of every field, into the extrema
+            auto exact_slot = [&](int s) {
                 const uint32_t e = nbr[base + s];
                 const Prim pj = prim[e & IDX_MASK];
                 double xj[3], d[3];
@@ -1623,9 +1721,6 @@ __global__ void __launch_bounds__(256) k_gradients(Params p, const Member *__res
                 for (int a = 0; a < D; ++a) d[a] = xj[a] - xi[a];
 #pragma unroll
                 for (int f = 0; f < NF; ++f) {
-                    const long long kj = ord_key(field_of<D>(pj, f));
-                    if (mxN[f] < kj) mxN[f] = kj;
-                    if (mnN[f] > kj) mnN[f] = kj;
                     double fij = fma(gr[f][0], d[0], fi[f]);
 #pragma unroll
                     for (int a = 1; a < D; ++a) fij = fma(gr[f][a], d[a], fij);
@@ -1633,11 +1728,157 @@ __global__ void __launch_bounds__(256) k_gradients(Params p, const Member *__res
                     if (mxM[f] < kij) mxM[f] = kij;
                     if (mnM[f] > kij) mnM[f] = kij;
                 }
+            };
+            if (!(fp32_filters & MLH_FILTER_SLOPE)) {
+                for (int s = 0; s < tot; ++s) {
+                    const Prim pj = prim[nbr[base + s] & IDX_MASK];
+#pragma unroll
+                    for (int f = 0; f < NF; ++f) {
+                        const long long kj = ord_key(field_of<D>(pj, f));
+                        if (mxN[f] < kj) mxN[f] = kj;
+                        if (mnN[f] > kj) mnN[f] = kj;
+                    }
+                    exact_slot(s);
+                }
+            } else {
+                // Single-precision filter (the FP64 pipe is the step's
+                // bound; the FP32 pipe is 64 times wider).  The increment
+                // q_j = (c grad f) . (x_j - x_i) is estimated in single
+                // precision from the packed positions; |f_ij - (f_i + q_j)|
+                // <= B_f for every neighbour, B_f bounding the estimate's
+                // rounding (positions, gradients, the chain) and the FP64
+                // chain's own.  The neighbour with the largest f_ij then has
+                // q_j >= max_k q_k - 2 B_f (and the smallest q_j <= min_k q_k
+                // + 2 B_f), so the FP64 chain runs only over the neighbours
+                // inside those windows (a handful; every lane of a warp walks
+                // its own list): the same extrema, bit for bit.  A field whose
+                // gradient is zero has f_ij = f_i at every neighbour.
+                float gf[NF][3], xif[3];
+#pragma unroll
+                for (int f = 0; f < NF; ++f)
+#pragma unroll
+                    for (int a = 0; a < 3; ++a) gf[f][a] = a < D ? __double2float_rn(gr[f][a]) : 0.f;
+#pragma unroll
+                for (int a = 0; a < 3; ++a) xif[a] = a < D ? __double2float_rn(xi[a]) : 0.f;
+                // bound on |coordinate| of any neighbour or image: the box (the
+                // grid spans every particle) and one box length for images
+                double xb = 0.;
+#pragma unroll
+                for (int a = 0; a < D; ++a) {
+                    const double ext = fmax(fabs(g.lo[a]), fabs(g.hi[a])) + (p.periodic ? g.hi[a] - g.lo[a] : 0.);
+                    xb = fmax(xb, ext);
+                }
+                // x_j - x_i in single precision: the packed position, or the
+                // image coordinate (double) rounded once
+                auto offset_f = [&](uint32_t e, const Prim *pjp, float *d) {
+                    const int j = (int)(e & IDX_MASK);
+                    float xj[3];
+                    if (e >> IMG_SHIFT) {
+                        const Prim pj = pjp ? *pjp : prim[j];
+                        double xd[3];
+                        neighbour_pos<D>(e, pj, g, xd);
+#pragma unroll
+                        for (int a = 0; a < 3; ++a) xj[a] = a < D ? __double2float_rn(xd[a]) : 0.f;
+                    } else {
+                        const float4 q = posf[j];
+                        xj[0] = q.x; xj[1] = q.y; xj[2] = q.z;
+                    }
+#pragma unroll
+                    for (int a = 0; a < 3; ++a) d[a] = a < D ? __fsub_rn(xj[a], xif[a]) : 0.f;
+                };
+                auto incr = [&](int f, const float *d) {
+                    float q = __fmul_rn(gf[f][0], d[0]);
+#pragma unroll
+                    for (int a = 1; a < D; ++a) q = __fmaf_rn(gf[f][a], d[a], q);
+                    return q;
+                };
+                float hiQ[NF], loQ[NF], dmax = 0.f;
+#pragma unroll
+                for (int f = 0; f < NF; ++f) { hiQ[f] = -FLT_MAX_; loQ[f] = FLT_MAX_; }
+                for (int s = 0; s < tot; ++s) {
+                    const uint32_t e = nbr[base + s];
+                    const Prim pj = prim[e & IDX_MASK];
+#pragma unroll
+                    for (int f = 0; f < NF; ++f) {
+                        const long long kj = ord_key(field_of<D>(pj, f));
+                        if (mxN[f] < kj) mxN[f] = kj;
+                        if (mnN[f] > kj) mnN[f] = kj;
+                    }
+                    float d[3];
+                    offset_f(e, &pj, d);
+#pragma unroll
+                    for (int a = 0; a < D; ++a) dmax = fmaxf(dmax, fabsf(d[a]));
+#pragma unroll
+                    for (int f = 0; f < NF; ++f) {
+                        const float q = incr(f, d);
+                        hiQ[f] = fmaxf(hiQ[f], q);
+                        loQ[f] = fminf(loQ[f], q);
+                    }
+                }
+                // B_f = 12 eps32 S R + 12 u64 (|f_i| + S R) with S = sum |c grad f|
+                // and R = max|x| + max|x_j - x_i|: twice the sum of the
+                // single-precision error, at most (6 |x|max + 5 |d|max) eps32 S,
+                // and the FP64 chain's, at most 4 u64 (|f_i| + S (|d|max + eps |x|max))
+                constexpr float EPS32 = 5.9604645e-8f, U64 = 1.1102230e-16f;
+                const float R = __double2float_ru(xb) + dmax;
+                float thHi[NF], thLo[NF];
+                bool ok = true, flat[NF];
+#pragma unroll
+                for (int f = 0; f < NF; ++f) {
+                    bool z = true;
+                    float S = 0.f;
+#pragma unroll
+                    for (int a = 0; a < D; ++a) {
+                        z = z && (__double_as_longlong(gr[f][a]) & 0x7FFFFFFFFFFFFFFFll) == 0;
+                        S += fabsf(gf[f][a]);
+                    }
+                    flat[f] = z;
+                    const float fa = fabsf(__double2float_rn(fi[f]));
+                    const float SR = S * R;
+                    ok = ok && SR < 1e36f && fa < 1e36f;   // false for NaN and infinity
+                    const float B = 12.f * EPS32 * SR + 12.f * U64 * (fa + SR) + 1e-36f;
+                    thHi[f] = z ? FLT_INF_ : hiQ[f] - 2.f * B;
+                    thLo[f] = z ? -FLT_INF_ : loQ[f] + 2.f * B;
+                }
+                const int t64 = tot < 64 ? tot : 64;
+                unsigned long long cand = t64 == 64 ? ~0ull : ((1ull << t64) - 1ull);
+                if (ok) {
+                    cand = 0ull;
+                    for (int s = 0; s < t64; ++s) {
+                        float d[3];
+                        offset_f(nbr[base + s], nullptr, d);
+                        bool c = false;
+#pragma unroll
+                        for (int f = 0; f < NF; ++f) {
+                            const float q = incr(f, d);
+                            c = c || q >= thHi[f] || q <= thLo[f];
+                        }
+                        cand |= (unsigned long long)c << s;
+                    }
+                }
+                while (cand) {
+                    const int s = __ffsll((long long)cand) - 1;
+                    cand &= cand - 1ull;
+                    exact_slot(s);
+                }
+                for (int s = 64; s < tot; ++s) exact_slot(s);
+                if (tot > 0) {
+#pragma unroll
+                    for (int f = 0; f < NF; ++f)
+                        if (flat[f]) mxM[f] = mnM[f] = ord_key(fi[f]);
+                }
             }
+            if (p.foqp) {
 #pragma unroll
-            for (int f = 0; f < NF; ++f)
+                for (int f = 0; f < NF; ++f)
 #pragma unroll
-                for (int a = 0; a < D; ++a) gr[f][a] *= icq;
+                    for (int a = 0; a < D; ++a) gr[f][a] = twice(gr[f][a]);
+            } else {
+#pragma unroll
+                for (int f = 0; f < NF; ++f)
+#pragma unroll
+                    for (int a = 0; a < D; ++a) gr[f][a] *= icq;
+            }
 #pragma unroll
             for (int f = 0; f < NF; ++f) {
                 const double xN = key_double(mxN[f]), nN = key_double(mnN[f]);
@@ -1676,11 +1917,20 @@ __global__ void __launch_bounds__(256) k_gradients(Params p, const Member *__res
             for (int f = 0; f < D + 2; ++f) go.t[f] = fma_dotD<D>(v, G + blk[f], src[f]);
         }
         grad[i] = go;
-        // B_i = E_i^-1 = E'^-1 / V_i = E'^-1 omega_i (kept for inspection)
-        const double omega_i = geo[i].omega;
-#pragma unroll
-        for (int k = 0; k < D * D; ++k) geo[i].B[k] = E[k] * omega_i;
       }   // i < p.n
+      if (dtlo) {
+        // the least upper bound on dt of each simulation (positive floats
+        // order as their bit patterns)
+        const int m0 = __shfl_sync(0xffffffffu, mi, 0);
+        if (__all_sync(0xffffffffu, mi == m0)) {
+            float best = dthi;
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) best = fminf(best, __shfl_xor_sync(0xffffffffu, best, o));
+            if (lane == 0 && m0 >= 0 && best < FLT_INF_) atomicMin(dtcap + m0, __float_as_uint(best));
+        } else if (mi >= 0 && dthi < FLT_INF_) {
+            atomicMin(dtcap + mi, __float_as_uint(dthi));
+        }
+      }
       if (dtbits) {
         // the minimum over particles does not depend on the order of the
         // atomicMin calls: a warp inside one simulation reduces first and
@@ -1702,11 +1952,15 @@ __global__ void __launch_bounds__(256) k_gradients(Params p, const Member *__res
 
 // Particles::pairwiseLimiter, Particles.cpp:1735-1785, for one side: phi0
 // the reconstructed value, phi_i this side's particle value, phi_ij the value
-// interpolated to the face, delta1/delta2 = PSI_1/PSI_2 |phi_i - phi_j|, and
-// i_lt_j = phi_i < phi_j (the two values differ).  Every comparison on
-// integer keys (ord_key), off the FP64 pipe.
-__device__ __forceinline__ double pairwise_side(double phi0, double phi_i, double phi_ij, double delta1,
-                                                double delta2, bool i_lt_j, int int_abs) {
+// interpolated to the face, ad = |phi_i - phi_j|, delta1/delta2 = PSI_1/PSI_2
+// ad, and i_lt_j = phi_i < phi_j (the two values differ).  Every comparison
+// on integer keys (ord_key), off the FP64 pipe.  The shifts phi +- delta are
+// fused multiply-adds fma(+-PSI, ad, phi): for the reference's PSI_1 = 0.5
+// and PSI_2 = 0.25 the product is exact, so this is the reference's product
+// then sum bit for bit, one FP64 instruction instead of two (other PSI: one
+// rounding fewer).
+__device__ __forceinline__ double pairwise_side(double phi0, double phi_i, double phi_ij, double ad, double psi1,
+                                                double psi2, bool i_lt_j, int int_abs) {
     // the bound that is used is phi_minus = phi_min - delta1 when phi_i <
     // phi_j and phi_plus = phi_max + delta1 otherwise, and in both cases the
     // extreme it starts from is phi_i; the reference takes the shift when it
@@ -1716,13 +1970,13 @@ __device__ __forceinline__ double pairwise_side(double phi0, double phi_i, doubl
     // one division by the Newton-Raphson reciprocal, and only where the
     // shift would change the sign; the same value to a few ulp, also for
     // |phi| = 0 and the int abs binding)
-    const double shifted = phi_i + (i_lt_j ? -delta1 : delta1);
+    const double shifted = fma(i_lt_j ? -psi1 : psi1, ad, phi_i);
     double bound = shifted;
     if ((ord_key(shifted) >= 0) != (ord_key(phi_i) >= 0)) {
         const double ra = ref_abs(phi_i, int_abs);
-        bound = fdiv(phi_i * ra, ra + delta1);
+        bound = fdiv(phi_i * ra, fma(psi1, ad, ra));
     }
-    const double t = phi_ij + (i_lt_j ? delta2 : -delta2);
+    const double t = fma(i_lt_j ? psi2 : -psi2, ad, phi_ij);
     if (i_lt_j) {
         const double minPhiD2 = dlt(t, phi0) ? t : phi0;
         return dlt(minPhiD2, bound) ? bound : minPhiD2;
@@ -1735,11 +1989,10 @@ __device__ __forceinline__ double pairwise_side(double phi0, double phi_i, doubl
 // reconstructed values (replaced by the limited ones), phiR/phiL the values
 // of particles i and j, rR/rL = |x_ij - x_i| / |x_j - x_i| and
 // |x_ij - x_j| / |x_j - x_i|.  The j side's phi_i - phi_j is the exact
-// negation of the i side's, so |phi_i - phi_j|, delta1 and delta2 are the
-// same doubles on both sides and are computed once; phi_ij on the j side,
-// phi_j + rL (phi_i - phi_j), is fma(rL, d, phi_j) with d = phi_i - phi_j.
-// Equal particle values (neither phi_i < phi_j nor phi_i > phi_j) give the
-// particle values back.
+// negation of the i side's, so |phi_i - phi_j| is the same double on both
+// sides and is computed once; phi_ij on the j side, phi_j + rL (phi_i -
+// phi_j), is fma(rL, d, phi_j) with d = phi_i - phi_j.  Equal particle values
+// (neither phi_i < phi_j nor phi_i > phi_j) give the particle values back.
 __device__ __forceinline__ void pairwise_limiter(const Params &p, double &phi0R, double &phi0L, double phiR,
                                                  double phiL, double rR, double rL) {
     const long long kR = ord_key(phiR), kL = ord_key(phiL);
@@ -1747,9 +2000,8 @@ __device__ __forceinline__ void pairwise_limiter(const Params &p, double &phi0R,
     const bool r_lt_l = kR < kL;
     const double d = phiR - phiL;
     const double ad = ref_abs(d, p.int_abs);
-    const double delta1 = p.psi1 * ad, delta2 = p.psi2 * ad;
-    phi0R = pairwise_side(phi0R, phiR, fma(rR, -d, phiR), delta1, delta2, r_lt_l, p.int_abs);
-    phi0L = pairwise_side(phi0L, phiL, fma(rL, d, phiL), delta1, delta2, !r_lt_l, p.int_abs);
+    phi0R = pairwise_side(phi0R, phiR, fma(rR, -d, phiR), ad, p.psi1, p.psi2, r_lt_l, p.int_abs);
+    phi0L = pairwise_side(phi0L, phiL, fma(rL, d, phiL), ad, p.psi1, p.psi2, !r_lt_l, p.int_abs);
 }
 
 // Network inputs of a face, from its face-frame problem sorted as the
@@ -1864,8 +2116,8 @@ __device__ __forceinline__ unsigned project_flux(const RiemannResult &rs, const 
 #pragma unroll
     for (int a = 0; a < D; ++a) Fo[2 + a] = fma(mflux, vLab[a], PSol * A[a]);
     if (D == 2) Fo[4] = 0.;
-    const double ek = rhoSol * .5 * dotD<D>(vLab, vLab);
-    Fo[1] = fma(Avm, pe + ek, PSol * dotD<D>(A, vLab));
+    // pe + rho*/2 |v_lab|^2 as one fused multiply-add
+    Fo[1] = fma(Avm, fma(half_of(rhoSol), dotD<D>(vLab, vLab), pe), PSol * dotD<D>(A, vLab));
     return st;
 }
 
@@ -1934,8 +2186,9 @@ __device__ __forceinline__ bool face_states(const Params &p, const Member *__res
     for (int a = 0; a < D; ++a) {
         xjxi[a] = xj[a] - xi[a];
         if (p.foqp) {
-            // .5 (x_j - x_i), and .5 (x_i - x_j) is its exact negation
-            xijxi[a] = .5 * xjxi[a];
+            // .5 (x_j - x_i) (on the integer pipe), and .5 (x_i - x_j) is its
+            // exact negation
+            xijxi[a] = half_of(xjxi[a]);
             xijxj[a] = -xijxi[a];
         } else {
             double xij = xi[a] + hq / 4. * xjxi[a];
@@ -1947,7 +2200,7 @@ __device__ __forceinline__ bool face_states(const Params &p, const Member *__res
     if (p.move) {
         if (p.foqp) {
 #pragma unroll
-            for (int a = 0; a < D; ++a) vf[a] = (vi[a] + vj[a]) / 2.;
+            for (int a = 0; a < D; ++a) vf[a] = half_of(vi[a] + vj[a]);
         } else {
             double dotProd = dotD<D>(xijxi, xjxi);
             double dSqr = dotD<D>(xjxi, xjxi);
@@ -1966,7 +2219,7 @@ __device__ __forceinline__ bool face_states(const Params &p, const Member *__res
     // v_frame . grad W.  The reference uses vz[i] on the j side of the vx and
     // vy terms in 3D (Particles.cpp:1717,1719): (vz_i - vf_z) = (vz_j - vq_z)
     // with the shifted frame velocity vq_z = vf_z - (vz_i - vz_j).
-    const double hdt = dt / 2.;
+    const double hdt = half_of(dt);
     const double *Ti = grad[i].t, *Tj = grad[j].t;
     const int blk[5] = {0, 12, 3, 6, 9};   // gradient blocks: 0 rho, 3 vx, 6 vy, 9 vz, 12 P
     const double vq2 = D == 3 ? vf[2] - (vi[2] - vj[2]) : 0.;
@@ -2587,7 +2840,7 @@ void launch_step(StepArgs &a) {
             cudaFuncSetAttribute(k_neighbours<D>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
         k_neighbours<D><<<blocks, NNS_WARPS * 32, smem, s>>>(
             p, a.members, a.memberOf, a.grids, a.x, a.y, a.z, a.posf, a.vx, a.vy, a.vz, a.m, a.u, a.cellTotal,
-            a.cellStart, a.cellList, a.nbr, a.rr, a.ww, a.noi, a.noiImg, a.faceCnt, a.prim, a.geo, a.status);
+            a.cellStart, a.cellList, a.nbr, a.rr, a.ww, a.noi, a.noiImg, a.faceCnt, a.prim, a.geo, a.velf, a.status);
     }
     tock(KT_NNS);
 
@@ -2617,10 +2870,17 @@ void launch_step(StepArgs &a) {
     // arithmetic, is the fallback when the time step is timed on its own)
     const int gT = a.tune.grad_threads;
     cudaMemsetAsync(a.dtbits, 0xff, sizeof(unsigned long long) * (size_t)a.nmembers, s);
+    // with the single-precision filters the gradients kernel bounds every
+    // particle's dt (dtlo, and the least upper bound per simulation in dtcap,
+    // 0x7F7F7F7F = 3.4e38 to start) and k_timestep evaluates v_sig in FP64
+    // for the particles whose bound reaches it
+    const bool dt_filter = p.adaptive && !a.separate_dt && (a.tune.fp32_filters & MLH_FILTER_TIMESTEP) && a.velf &&
+                           a.dtlo && a.dtcap;
+    if (dt_filter) cudaMemsetAsync(a.dtcap, 0x7f, sizeof(unsigned) * (size_t)a.nmembers, s);
     if (a.separate_dt) {
         tick(KT_DT);
         k_timestep<D><<<(p.n + 255) / 256, 256, 0, s>>>(p, a.members, a.memberOf, a.prim, a.geo, a.nbr, a.rr,
-                                                        a.noi, a.dtbits);
+                                                        a.noi, a.dtbits, nullptr, nullptr);
         tock(KT_DT);
     }
     tick(KT_GRAD);
@@ -2630,8 +2890,13 @@ void launch_step(StepArgs &a) {
     }
     k_gradients<D><<<(p.n + gT - 1) / gT, gT, 0, s>>>(p, a.members, a.memberOf, a.grids, a.prim, a.geo, a.nbr, a.ww,
                                                       a.rr, a.noi, a.noiImg, a.grad, a.gradRaw, a.psi,
-                                                      (p.adaptive && !a.separate_dt) ? a.dtbits : nullptr,
-                                                      fused ? a.faceOff : nullptr, a.faceOf, a.faces, a.status);
+                                                      (p.adaptive && !a.separate_dt && !dt_filter) ? a.dtbits : nullptr,
+                                                      fused ? a.faceOff : nullptr, a.faceOf, a.faces, a.status,
+                                                      a.posf, a.tune.fp32_filters, a.velf, dt_filter ? a.dtlo : nullptr,
+                                                      a.dtcap);
+    if (dt_filter)
+        k_timestep<D><<<(p.n + 255) / 256, 256, 0, s>>>(p, a.members, a.memberOf, a.prim, a.geo, a.nbr, a.rr,
+                                                        a.noi, a.dtbits, a.dtlo, a.dtcap);
     k_dt_final<<<(a.nmembers + 127) / 128, 128, 0, s>>>(p, a.nmembers, a.dtbits, a.dt_max, a.dt);
     tock(KT_GRAD);
     if (a.stop_after_gradients) return;

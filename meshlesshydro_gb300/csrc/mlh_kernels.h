@@ -18,7 +18,11 @@ struct Tuning {
     int face_split = 1;            // plain gamma = 5/3 step: 1 second Newton pass over a queue, 2 in-block, 0 none
     int link_overlap = 1;          // face links on the second stream beside the time step and gradients
     int persistent_binning = 0;    // the binning as one persistent cooperative kernel (k_binning)
+    int fp32_filters = 3;          // bits: 1 slope-limiter extrema, 2 time step (FP64 only where a single-precision bound reaches the result)
 };
+
+// bits of Tuning::fp32_filters
+constexpr int MLH_FILTER_SLOPE = 1, MLH_FILTER_TIMESTEP = 2;
 
 // Device pointers and settings of one step.
 struct StepArgs {
@@ -37,6 +41,12 @@ struct StepArgs {
     // state (structure of arrays)
     double *x, *y, *z, *vx, *vy, *vz, *m, *u;
     float4 *posf;
+    // velocity and sound speed in single precision (written with the
+    // density); the time step's bounds: per particle a lower bound on dt,
+    // per simulation the least upper bound (float bits)
+    float4 *velf;
+    float *dtlo;
+    unsigned *dtcap;
     // simulations (members) of the context
     int nmembers;
     int bpm;                   // bounding-box blocks per member

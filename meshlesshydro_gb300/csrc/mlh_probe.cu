@@ -104,7 +104,36 @@ __global__ void k_fast_math(int n, const double *__restrict__ x, const double *_
     }
 }
 
+__global__ void k_scale2(int n, const double *__restrict__ x, double *__restrict__ half, double *__restrict__ quarter,
+                         double *__restrict__ twice) {
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        half[i] = mlh::scale_down<1>(x[i]);
+        quarter[i] = mlh::scale_down<2>(x[i]);
+        twice[i] = mlh::twice(x[i]);
+    }
+}
+
 }  // namespace
+
+// The integer-pipe scalings by 1/2, 1/4 and 2 (mlh_device.cuh: scale_down,
+// twice) of host values, for checking them against IEEE products.
+extern "C" int mlh_probe_scale2(int n, const double *x, double *half, double *quarter, double *twice) {
+    if (n < 0 || (n > 0 && (!x || !half || !quarter || !twice))) return MLH_ERR_INVALID;
+    if (n == 0) return 0;
+    double *d = nullptr;
+    if (cudaMalloc(&d, sizeof(double) * 4 * (size_t)n) != cudaSuccess) return MLH_ERR_CUDA;
+    const size_t b = sizeof(double) * (size_t)n;
+    cudaError_t e = cudaMemcpy(d, x, b, cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) {
+        k_scale2<<<(n + 255) / 256, 256>>>(n, d, d + n, d + 2 * (size_t)n, d + 3 * (size_t)n);
+        e = cudaGetLastError();
+    }
+    if (e == cudaSuccess) e = cudaMemcpy(half, d + n, b, cudaMemcpyDeviceToHost);
+    if (e == cudaSuccess) e = cudaMemcpy(quarter, d + 2 * (size_t)n, b, cudaMemcpyDeviceToHost);
+    if (e == cudaSuccess) e = cudaMemcpy(twice, d + 3 * (size_t)n, b, cudaMemcpyDeviceToHost);
+    cudaFree(d);
+    return e == cudaSuccess ? 0 : MLH_ERR_CUDA;
+}
 
 // The library's reciprocal, quotient and reciprocal square root
 // (mlh_device.cuh: frcp, fdiv, frsqrt) of host arrays, for checking them

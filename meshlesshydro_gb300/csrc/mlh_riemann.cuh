@@ -177,12 +177,14 @@ __device__ inline RiemannResult riemann_exact(const RiemannConsts &c, double rho
 // are ordered as the values.
 __device__ __forceinline__ bool nn_le(double a, double b) { return __double_as_longlong(a) <= __double_as_longlong(b); }
 
-// x^(-1/5): single-precision seed (relative error ~1e-7) refined by `steps`
-// Newton steps y <- y + y (1 - x y^5) / 5, whose error contracts as 3 e^2:
-// two steps give a result within a few ulp of the correctly rounded value,
-// one step ~1e-13 relative (enough for an initial guess).  Values outside the
-// float range go through pow.
-template <int STEPS = 2>
+// x^(-1/5) to a few ulp: a single-precision seed y (relative error e below
+// 3e-7) refined by one third-order step.  With r = 1 - x y^5,
+// x^(-1/5) = y (1 - r)^(-1/5) = y (1 + r/5 + 3 r^2/25 + O(r^3)), and
+// |r| ~ 5 e, so dropping the O(r^3) term (0.088 r^3 < 1e-18) leaves the
+// roundings of y^5, r and the last two operations: within a few ulp of the
+// correctly rounded value, in seven FP64 operations (two Newton steps, whose
+// error contracts as 3 e^2, took twelve).  Values outside the float range go
+// through pow.
 __device__ __forceinline__ double rroot5(double x) {
     // 1e-30 < x < 1e30 on the bit patterns (the test is false for NaN and x <= 0)
     const long long b = __double_as_longlong(x);
@@ -192,15 +194,10 @@ __device__ __forceinline__ double rroot5(double x) {
     // the seed are positive and normal in both formats in this range
     const float xf = __int_as_float((int)((b >> 29) - (896ll << 23)));
     const float yf = exp2f(-0.2f * __log2f(xf));
-    double y = __longlong_as_double(((long long)__float_as_int(yf) + (896ll << 23)) << 29);
-#pragma unroll
-    for (int k = 0; k < STEPS; ++k) {
-        double y2 = y * y;
-        double y5 = y2 * y2 * y;
-        double r = fma(-x, y5, 1.);
-        y = fma(y * 0.2, r, y);
-    }
-    return y;
+    const double y = __longlong_as_double(((long long)__float_as_int(yf) + (896ll << 23)) << 29);
+    const double y2 = y * y;
+    const double r = fma(-x, y2 * y2 * y, 1.);
+    return fma(y, r * fma(0.12, r, 0.2), y);
 }
 // x^(1/5) = x * (x^(-1/5))^4
 __device__ __forceinline__ double root5(double x) {
@@ -219,7 +216,7 @@ __device__ __forceinline__ double two_rarefaction_guess(const RiemannConsts &k, 
     const double num = cL + cR - k.g7 * (uR - uL);
     if (!(num > 0.)) return -1.;
     if (ROOT5) {
-        const double t = fdiv(num, cL * rroot5<1>(pL) + cR * rroot5<1>(pR));
+        const double t = fdiv(num, cL * rroot5(pL) + cR * rroot5(pR));
         const double t2 = t * t;
         return t2 * t2 * t;
     }
@@ -262,7 +259,7 @@ __device__ __forceinline__ void pressure_fn5(const RiemannSide &s, double p, dou
         const double qrt = frsqrt(bp * s.iak);
         const double t = (qrt * qrt) * s.iak;
         f = (p - s.p) * qrt;
-        fd = (1. - .5 * (p - s.p) * t) * qrt;
+        fd = __dmul_rn(fma(-half_of(p - s.p), t, 1.), qrt);
         q = 0.;
         rare = false;
     }
@@ -278,8 +275,8 @@ __device__ __forceinline__ double flip_if(double x, bool f) {
 // reciprocals by Newton-Raphson (frcp), f_K(p*) from the last Newton
 // evaluation plus its derivative times the final (<= tol relative) step,
 // which differs from re-evaluating f at p* by O(tol^2) relative, and sign
-// and order tests on the integer pipe.  The two-rarefaction guess takes its
-// fifth roots to ~1e-13: it only seeds Newton, whose result is the same.
+// and order tests on the integer pipe; halvings and doublings on the
+// integer pipe too (half_of, twice).
 // first_iters > 0: when Newton from the two-rarefaction guess has not
 // converged after that many steps, return unsolved (flag 2, pstar = the
 // current iterate, iters = steps run); solving again with that iterate as
@@ -330,7 +327,7 @@ __device__ __forceinline__ void riemann5_newton(const RiemannConsts &k, Solve5 &
             if (!tried_guess) break;
             extra = k.max_iter;
             double num = A.c + B.c - k.g7 * du;
-            double den = A.c * rroot5<1>(A.p) + B.c * rroot5<1>(B.p);
+            double den = A.c * rroot5(A.p) + B.c * rroot5(B.p);
             double t = fdiv(num, den);
             double t2 = t * t;
             p0 = t2 * t2 * t;
@@ -348,7 +345,7 @@ __device__ __forceinline__ void riemann5_newton(const RiemannConsts &k, Solve5 &
                 if (pb <= 0 || pb > 0x7FF0000000000000ll) pnew = pfloor;
             }
             double dp = pnew - p;
-            if (nn_le(2. * fabs(dp), k.tol * (pnew + p))) {
+            if (nn_le(twice(fabs(dp)), k.tol * (pnew + p))) {
                 s.fAs = fA + fdA * dp;
                 s.fBs = fB + fdB * dp;
                 double rel = dp * invp;
@@ -392,7 +389,7 @@ __device__ __forceinline__ Solve5 riemann5_begin(const RiemannConsts &k, double 
     if (tried_guess) p0 = guess;
     else {
         double num = s.A.c + s.B.c - k.g7 * s.du;
-        double den = s.A.c * rroot5<1>(s.A.p) + s.B.c * rroot5<1>(s.B.p);
+        double den = s.A.c * rroot5(s.A.p) + s.B.c * rroot5(s.B.p);
         double t = fdiv(num, den);
         double t2 = t * t;
         p0 = t2 * t2 * t;
@@ -449,7 +446,9 @@ __device__ inline RiemannResult riemann5_finish(const RiemannConsts &k, const So
     }
     res.iters = s.iters;
     // u* of the given problem (the sorted one's, negated when mirrored)
-    const double ustar = flip_if(.5 * (A.u + B.u) + .5 * (fBs - fAs), mir);
+    // .5 (uA + uB) + .5 (fB - fA) = .5 ((uA + uB) + (fB - fA)): halving is
+    // exact, so one rounding of the sum, halved on the integer pipe
+    const double ustar = flip_if(half_of((A.u + B.u) + (fBs - fAs)), mir);
     // --- sampling at S = 0: side s of the contact, as the left side
     const bool right = dneg(ustar);               // u* < 0: the right state
     const bool useB = right != mir;               // where side s sits in the sorted problem

@@ -45,7 +45,8 @@ class Tuning(ctypes.Structure):
     _fields_ = [("face_threads", ctypes.c_int), ("face_blocks_per_sm", ctypes.c_int),
                 ("grad_threads", ctypes.c_int), ("nns_warps_per_sm", ctypes.c_int),
                 ("face_split", ctypes.c_int),
-                ("link_overlap", ctypes.c_int), ("persistent_binning", ctypes.c_int)]
+                ("link_overlap", ctypes.c_int), ("persistent_binning", ctypes.c_int),
+                ("fp32_filters", ctypes.c_int)]
 
 
 class ParticlesView(ctypes.Structure):
@@ -67,7 +68,7 @@ EXPORTS = ["mlh_abi_version", "mlh_last_error", "mlh_create", "mlh_destroy", "ml
            "mlh_grid_bounds_noalloc", "mlh_ensemble_create", "mlh_member_times", "mlh_set_graph_mode",
            "mlh_autotune", "mlh_set_tuning", "mlh_pstar_infer", "mlh_pstar_grad", "mlh_pstar_train", "mlh_set_pstar_weights",
            "mlh_pstar_harvest", "mlh_pstar_harvest_strong", "mlh_smoothing_lengths", "mlh_prepare", "mlh_riemann_fluxes",
-           "mlh_probe_fast_math", "mlh_probe_fp64_lanes", "mlh_test_binning_barrier"]
+           "mlh_probe_fast_math", "mlh_probe_scale2", "mlh_probe_fp64_lanes", "mlh_test_binning_barrier"]
 
 _lib = None
 
@@ -146,6 +147,8 @@ def load(path: str = LIB_PATH):
     L.mlh_riemann_fluxes.restype = ctypes.c_int
     L.mlh_probe_fast_math.argtypes = [ctypes.c_int] + [dp] * 5
     L.mlh_probe_fast_math.restype = ctypes.c_int
+    L.mlh_probe_scale2.argtypes = [ctypes.c_int] + [dp] * 4
+    L.mlh_probe_scale2.restype = ctypes.c_int
     L.mlh_probe_fp64_lanes.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.POINTER(ctypes.c_double)]
     L.mlh_probe_fp64_lanes.restype = ctypes.c_int
     _lib = L
@@ -391,8 +394,8 @@ class Simulation:
 
     def set_tuning(self, tuning: dict):
         """Launch shapes (mlh_set_tuning); face_split and link_overlap
-        default to 1, persistent_binning to 0."""
-        dflt = {"face_split": 1, "link_overlap": 1, "persistent_binning": 0}
+        default to 1, persistent_binning to 0, fp32_filters to 3 (both)."""
+        dflt = {"face_split": 1, "link_overlap": 1, "persistent_binning": 0, "fp32_filters": 3}
         t = Tuning(**{k: int(tuning.get(k, dflt[k]) if k in dflt else tuning[k]) for k, _ in Tuning._fields_})
         st = self.L.mlh_set_tuning(self.h, ctypes.byref(t))
         if st != 0:

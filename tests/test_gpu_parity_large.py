@@ -8,8 +8,8 @@ inputs.
   state (the per-step gate of tests/helpers.py, neighbour lists bit-exact
   every step), and a free-running run over the same steps whose density is
   compared by L1 (<= 1e-8 relative).  The reference's scheme gives negative
-  internal energy at the blast's evacuated centre at step 64, which ends the
-  comparison.
+  internal energy at the blast's evacuated centre at its 65th step (index
+  64), which ends the comparison.
 * Sedov 128^3 (2,097,152 particles, the bench workload): one step, lists
   bit-exact, fields per element.
 * Kelvin-Helmholtz 100x100: 100 steps per-step gated, and every state field
@@ -25,8 +25,8 @@ import pytest
 
 from meshlesshydro_gb300 import ic
 from meshlesshydro_gb300.config import MFVConfig
-from helpers import (MAX_TIE_FRACTION, assert_close, assert_state, compare_step, flux_terms, l1_rel,
-                     pset_from_state, state_of, state_terms, step_limits)
+from helpers import (MAX_TIE_FRACTION, assert_close, assert_state, compare_step, flux_terms, l1_rel, pset_from_state,
+                     rank_deficient, state_of, state_terms, step_limits)
 
 pytestmark = pytest.mark.gpu
 
@@ -88,14 +88,16 @@ def _per_step_and_free_run(orc, p, cfg, nsteps, what, free_fields=("rho",)):
         assert_close(g.get("dt"), o.get("dt"), floor=0.0, what=f"{what} step {k}: dt")
         lim, _, tie = step_limits(g, o, cfg.dim)
         ties += int(tie.sum() // 2)
+        nrd = int(rank_deficient(o, cfg.dim).sum())
+        assert nrd <= 1e-4 * p.n, f"{what}: {nrd} particles with fewer than {cfg.dim} neighbours at step {k}"
         ost_k = o.state()
         terms = state_terms(pre, ost_k, flux_terms(o.get("F"), o.get("off"), cfg.dim), float(o.get("dt")[0]),
                             cfg.dim)
         assert_state(g.get_state(), ost_k, lim, what=f"{what} step {k}: ", terms=terms)
         if so != 0:
             # the reference's scheme gives non-physical values at this step
-            # (the state, gated above like every step, agrees; the sign of a
-            # value that crosses zero within its tolerance may differ, so the
+            # (its cause, a particle with a singular E_i, is out of the gate
+            # above and its outcome is rounding noise in both codes, so the
             # GPU's status is not required to match): no step after it is
             # compared
             done, ost, orho = k, pre, o.get("rho")
@@ -127,13 +129,14 @@ def _per_step_and_free_run(orc, p, cfg, nsteps, what, free_fields=("rho",)):
 @pytest.mark.parametrize("periodic", [True, False], ids=["periodic", "nonperiodic"])
 def test_sedov64_100_steps(orc, periodic):
     """100 steps, or up to the step at which the reference's scheme itself
-    gives non-physical values: at step 64 the blast's evacuated centre holds
-    particles with 3 neighbours and the oracle (the reference's arithmetic)
-    reports negative internal energy (and, non-periodic, negative mass).
-    Every step up to it is compared; there the value that crosses zero is a
-    cancellation (u = Q/m - |v|^2/2 on a particle with an ill-conditioned
-    E_i) and the GPU's lies on the other side of zero within its tolerance.
-    The free run compares the steps before it."""
+    gives non-physical values.  The particle at the blast's evacuated centre
+    keeps 3 neighbours up to step index 63 (cond(E_i) = 1.2e8, gated with
+    the condition-number tolerance) and has one at index 64, where E_i is
+    singular, the reference inverts rounding noise and the oracle reports
+    negative internal energy (and, non-periodic, negative mass).  That step
+    is gated with the particle and its neighbour out of the gate
+    (tests/helpers.py), the GPU need not report the same status, and the
+    comparison ends there.  The free run compares the steps before it."""
     p, cfg = _sedov64(periodic)
     l1, done = _per_step_and_free_run(orc, p, cfg, 100, f"sedov64 periodic={periodic}")
     print(f"sedov64 periodic={periodic}: {done} steps compared, density L1 {l1['rho']:.3e}")
