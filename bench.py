@@ -60,8 +60,9 @@ LAUNCHES_PER_STEP = 20
 # face for the face pass), from ncu captures of the same kernels: FP64
 # operations (2 x DFMA + DADD + DMUL thread instructions per unit) and DRAM
 # bytes (read + write per unit); 3D on the 64^3 periodic Sedov step (the time
-# step inside the gradients' first pass, the face pass as its first pass and
-# the second Newton pass over the queue), 2D on the 256-member
+# step's single-precision bounds inside the gradients' first pass and its FP64
+# v_sig for the few candidate particles in k_timestep, the face pass as its
+# first pass and the second Newton pass over the queue), 2D on the 256-member
 # Kelvin-Helmholtz ensemble (the face pass with the unfinished faces
 # continued inside the block).  These are executed, not
 # algorithmic, operations: a kernel cannot execute more than the FP64 pipe
@@ -69,25 +70,25 @@ LAUNCHES_PER_STEP = 20
 KERNEL_UNITS = {"neighbours_density": "particle", "timestep": "particle", "gradients_limiter": "particle",
                 "face_links": "particle", "faces_riemann": "face", "gather_update": "particle"}
 KERNEL_EXEC = {
-    3: {"neighbours_density": (1030.1, 850.3), "timestep": (0.0, 0.0), "gradients_limiter": (4260.5, 1978.9),
-        "face_links": (0.0, 1010.9), "faces_riemann": (557.8, 301.4), "gather_update": (214.0, 1507.8)},
-    2: {"neighbours_density": (596.7, 863.5), "timestep": (0.0, 0.0), "gradients_limiter": (1653.4, 2337.8),
-        "face_links": (0.0, 874.9), "faces_riemann": (367.4, 179.2), "gather_update": (122.0, 977.7)},
+    3: {"neighbours_density": (1030.1, 871.6), "timestep": (0.0, 4.1), "gradients_limiter": (2906.7, 1802.5),
+        "face_links": (0.0, 1004.5), "faces_riemann": (569.1, 301.7), "gather_update": (214.0, 1551.0)},
+    2: {"neighbours_density": (596.7, 888.2), "timestep": (0.0, 8.5), "gradients_limiter": (1126.9, 2072.3),
+        "face_links": (0.0, 876.0), "faces_riemann": (362.6, 188.7), "gather_update": (122.0, 980.5)},
 }
 # FP64 thread instructions (DFMA + DADD + DMUL) per unit of the same
 # captures: what the FP64 pipe issues, each instruction one lane-slot
 KERNEL_FP64_INSTR = {
-    3: {"neighbours_density": 793.1, "timestep": 0.0, "gradients_limiter": 2619.0, "face_links": 0.0,
-        "faces_riemann": 384.6, "gather_update": 196.0},
-    2: {"neighbours_density": 443.7, "timestep": 0.0, "gradients_limiter": 1052.9, "face_links": 0.0,
-        "faces_riemann": 259.3, "gather_update": 108.0},
+    3: {"neighbours_density": 793.1, "timestep": 0.0, "gradients_limiter": 1845.3, "face_links": 0.0,
+        "faces_riemann": 372.0, "gather_update": 196.0},
+    2: {"neighbours_density": 443.7, "timestep": 0.0, "gradients_limiter": 747.7, "face_links": 0.0,
+        "faces_riemann": 254.6, "gather_update": 108.0},
 }
 # FP64 pipe active (sm__pipe_fp64_cycles_active over elapsed cycles) of the
 # same captures
 KERNEL_FP64_PIPE = {
-    3: {"neighbours_density": 0.587, "timestep": None, "gradients_limiter": 0.891, "faces_riemann": 0.870,
-        "gather_update": 0.760, "face_links": 0.0},
-    2: {"neighbours_density": 0.715, "timestep": None, "gradients_limiter": 0.895, "faces_riemann": 0.850,
+    3: {"neighbours_density": 0.594, "timestep": 0.552, "gradients_limiter": 0.840, "faces_riemann": 0.877,
+        "gather_update": 0.762, "face_links": 0.0},
+    2: {"neighbours_density": 0.722, "timestep": 0.655, "gradients_limiter": 0.766, "faces_riemann": 0.834,
         "gather_update": 0.840, "face_links": 0.0},
 }
 # Operations of the reference's method per unit, counted by the
@@ -715,7 +716,8 @@ def run_mlh(args):
                                 "operation count",
                 "fp64_pipe_active_ncu": KERNEL_FP64_PIPE.get(dim, {}).get(dom_name),
                 "fp64_instr_frac": ((KERNEL_FP64_INSTR[dim][dom_name] * units_launch / dom_avg_s) /
-                                    (fp64_peak * 1e12 / 2.0)) if (dim in KERNEL_FP64_INSTR and fp64_peak) else None,
+                                    (fp64_peak * 1e12 / 2.0))
+                if (dom_name in KERNEL_FP64_INSTR.get(dim, {}) and fp64_peak) else None,
                 "fp64_instr_frac_note": "FP64 thread instructions (DFMA + DADD + DMUL) per second over the probe's "
                                         "(its TFLOP/s / 2, all FMAs): the pipe's issue rate, where frac counts an "
                                         "FMA twice and an add or multiply once",

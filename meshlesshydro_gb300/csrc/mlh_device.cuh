@@ -201,6 +201,13 @@ __device__ __forceinline__ double scale_down(double x) {
     return __longlong_as_double((long long)(r | sign));
 }
 __device__ __forceinline__ double half_of(double x) { return scale_down<1>(x); }
+// y / 2 for a normal y with a biased exponent of at least 2 (|y| >=
+// 2^-1021): one integer subtraction on the high word, exact.  For the
+// iterates of the reciprocal square root, which stay normal for the normal,
+// finite, nonzero operands it is defined for.
+__device__ __forceinline__ double half_normal(double y) {
+    return __hiloint2double(__double2hiint(y) - 0x00100000, __double2loint(y));
+}
 // 2 x on the integer pipe, the IEEE product bit for bit (overflow to
 // infinity); straight-line selects as in scale_down
 __device__ __forceinline__ double twice(double x) {
@@ -251,7 +258,7 @@ __device__ __forceinline__ double frsqrt(double x) {
 #pragma unroll
     for (int k = 0; k < 2; ++k) {
         const double e = fma(-(x * y), y, 1.);
-        y = fma(half_of(y), e, y);
+        y = fma(half_normal(y), e, y);
     }
     return y;
 }

@@ -14,6 +14,7 @@ namespace mlh {
 
 struct RiemannConsts {
     double gamma, g1, g2, g3, g4, g5, g6, g7, inv_gamma, inv_gm1, tol;
+    double tol_half;   // tol / 2 (exact): 2 |dp| <= tol s  <=>  |dp| <= (tol / 2) s
     double ig5;   // 1 / g5 = (gamma + 1) / 2
     int max_iter;
     // gamma = 5/3: g1 = 1/5, g3 = 5, g4 = 3 and 1/gamma = 3 g1, so every
@@ -35,6 +36,7 @@ __host__ __device__ inline RiemannConsts make_riemann_consts(double gamma, doubl
     c.inv_gamma = 1. / gamma;
     c.inv_gm1 = 1. / (gamma - 1.);
     c.tol = tol;
+    c.tol_half = tol / 2.;
     c.max_iter = max_iter;
     c.root5 = (fabs(1. / c.g1 - 5.) < 1e-12 && fabs(c.g4 - 3.) < 1e-12) ? 1 : 0;
     return c;
@@ -257,9 +259,11 @@ __device__ __forceinline__ void pressure_fn5(const RiemannSide &s, double p, dou
         // reciprocal square root: qrt = 1/sqrt((B_K + p) / A_K), t = qrt^2 / A_K
         const double bp = s.bk + p;
         const double qrt = frsqrt(bp * s.iak);
-        const double t = (qrt * qrt) * s.iak;
+        // t / 2 = qrt^2 A_K^-1 / 2, halved through the operand (exact), so
+        // that nothing on the iteration's dependency chain waits on it
+        const double t2 = (qrt * qrt) * half_of(s.iak);
         f = (p - s.p) * qrt;
-        fd = __dmul_rn(fma(-half_of(p - s.p), t, 1.), qrt);
+        fd = __dmul_rn(fma(-(p - s.p), t2, 1.), qrt);
         q = 0.;
         rare = false;
     }
@@ -345,7 +349,7 @@ __device__ __forceinline__ void riemann5_newton(const RiemannConsts &k, Solve5 &
                 if (pb <= 0 || pb > 0x7FF0000000000000ll) pnew = pfloor;
             }
             double dp = pnew - p;
-            if (nn_le(twice(fabs(dp)), k.tol * (pnew + p))) {
+            if (nn_le(fabs(dp), k.tol_half * (pnew + p))) {
                 s.fAs = fA + fdA * dp;
                 s.fBs = fB + fdB * dp;
                 double rel = dp * invp;
