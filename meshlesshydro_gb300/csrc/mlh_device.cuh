@@ -201,13 +201,6 @@ __device__ __forceinline__ double scale_down(double x) {
     return __longlong_as_double((long long)(r | sign));
 }
 __device__ __forceinline__ double half_of(double x) { return scale_down<1>(x); }
-// y / 2 for a normal y with a biased exponent of at least 2 (|y| >=
-// 2^-1021): one integer subtraction on the high word, exact.  For the
-// iterates of the reciprocal square root, which stay normal for the normal,
-// finite, nonzero operands it is defined for.
-__device__ __forceinline__ double half_normal(double y) {
-    return __hiloint2double(__double2hiint(y) - 0x00100000, __double2loint(y));
-}
 // 2 x on the integer pipe, the IEEE product bit for bit (overflow to
 // infinity); straight-line selects as in scale_down
 __device__ __forceinline__ double twice(double x) {
@@ -236,31 +229,32 @@ __device__ __forceinline__ double image_coord(double xa, const GridInfo &g, int 
     return __dadd_rn(low ? g.hi[a] : g.lo[a], __dsub_rn(xa, low ? g.lo[a] : g.hi[a]));
 }
 
-// Reciprocal and reciprocal square root by Newton-Raphson iteration from the
-// hardware estimates of PTX rcp.approx.ftz.f64 / rsqrt.approx.ftz.f64: each
-// step r <- r + r (1 - x r), respectively y <- y + (y/2) (1 - x y^2), squares
-// the relative error, and two steps give a result within about an ulp of the
-// correctly rounded one (the probe mlh_probe_fast_math measures it against
-// exact values).  Cheaper on the FP64 pipe than IEEE division, which also
-// guards subnormal, zero and infinite operands: these are for normal,
-// finite, nonzero operands only.
+// Reciprocal and reciprocal square root from the hardware estimates of PTX
+// rcp.approx.ftz.f64 / rsqrt.approx.ftz.f64 (relative error e of the estimate
+// a few times 2^-23), each refined by one third-order step:
+//   1/x       = r (1 - e)^-1   = r (1 + e + e^2 + ...),         e = 1 - x r
+//   1/sqrt(x) = y (1 - e)^-1/2 = y (1 + e/2 + 3 e^2/8 + ...),   e = 1 - x y^2
+// whose dropped terms (e^3, 5 e^3 / 16) are below 2^-60: the result is within
+// about an ulp of the correctly rounded one (the probe mlh_probe_fast_math
+// measures it against exact values).  Three and five FP64 operations in a
+// dependent chain of the same length, against four and six for two
+// Newton-Raphson steps: these sit on the Riemann iteration's dependency
+// chain, and the face pass waits on that chain as well as on the pipe.
+// Cheaper on the FP64 pipe than IEEE division, which also guards subnormal,
+// zero and infinite operands: these are for normal, finite, nonzero operands
+// only.
 __device__ __forceinline__ double frcp(double x) {
     double r;
     asm("rcp.approx.ftz.f64 %0, %1;" : "=d"(r) : "d"(x));
-    r = fma(r, fma(-x, r, 1.), r);
-    r = fma(r, fma(-x, r, 1.), r);
-    return r;
+    const double e = fma(-x, r, 1.);
+    return fma(r, fma(e, e, e), r);
 }
 __device__ __forceinline__ double fdiv(double a, double b) { return a * frcp(b); }
 __device__ __forceinline__ double frsqrt(double x) {
     double y;
     asm("rsqrt.approx.ftz.f64 %0, %1;" : "=d"(y) : "d"(x));
-#pragma unroll
-    for (int k = 0; k < 2; ++k) {
-        const double e = fma(-(x * y), y, 1.);
-        y = fma(half_normal(y), e, y);
-    }
-    return y;
+    const double e = fma(-(x * y), y, 1.);
+    return fma(y, e * fma(0.375, e, 0.5), y);
 }
 
 template <int D>

@@ -1,4 +1,4 @@
-"""The kernels' reciprocal, quotient and reciprocal square root (Newton-Raphson
+"""The kernels' reciprocal, quotient and reciprocal square root (one third-order step
 from the hardware estimates, mlh_device.cuh frcp / fdiv / frsqrt) against
 exact values: the error bound is 2 ulp (reciprocal, reciprocal square root)
 and 3 ulp (quotient), over the decades the MFV step meets."""
