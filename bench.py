@@ -70,25 +70,25 @@ LAUNCHES_PER_STEP = 20
 KERNEL_UNITS = {"neighbours_density": "particle", "timestep": "particle", "gradients_limiter": "particle",
                 "face_links": "particle", "faces_riemann": "face", "gather_update": "particle"}
 KERNEL_EXEC = {
-    3: {"neighbours_density": (1030.1, 871.6), "timestep": (0.0, 4.1), "gradients_limiter": (2906.7, 1802.5),
-        "face_links": (0.0, 1004.5), "faces_riemann": (569.1, 301.7), "gather_update": (214.0, 1551.0)},
-    2: {"neighbours_density": (596.7, 888.2), "timestep": (0.0, 8.5), "gradients_limiter": (1126.9, 2072.3),
-        "face_links": (0.0, 876.0), "faces_riemann": (362.6, 188.7), "gather_update": (122.0, 980.5)},
+    3: {"neighbours_density": (1026.1, 870.9), "timestep": (0.0, 4.1), "gradients_limiter": (2906.7, 1803.9),
+        "face_links": (0.0, 1007.7), "faces_riemann": (537.7, 300.9), "gather_update": (212.0, 1534.5)},
+    2: {"neighbours_density": (592.7, 887.2), "timestep": (0.0, 8.5), "gradients_limiter": (1126.9, 2074.6),
+        "face_links": (0.0, 876.0), "faces_riemann": (344.3, 180.8), "gather_update": (120.0, 975.6)},
 }
 # FP64 thread instructions (DFMA + DADD + DMUL) per unit of the same
 # captures: what the FP64 pipe issues, each instruction one lane-slot
 KERNEL_FP64_INSTR = {
-    3: {"neighbours_density": 793.1, "timestep": 0.0, "gradients_limiter": 1845.3, "face_links": 0.0,
-        "faces_riemann": 372.0, "gather_update": 196.0},
-    2: {"neighbours_density": 443.7, "timestep": 0.0, "gradients_limiter": 747.7, "face_links": 0.0,
-        "faces_riemann": 254.6, "gather_update": 108.0},
+    3: {"neighbours_density": 791.1, "timestep": 0.0, "gradients_limiter": 1845.3, "face_links": 0.0,
+        "faces_riemann": 353.5, "gather_update": 195.0},
+    2: {"neighbours_density": 441.7, "timestep": 0.0, "gradients_limiter": 747.7, "face_links": 0.0,
+        "faces_riemann": 244.4, "gather_update": 107.0},
 }
 # FP64 pipe active (sm__pipe_fp64_cycles_active over elapsed cycles) of the
 # same captures
 KERNEL_FP64_PIPE = {
-    3: {"neighbours_density": 0.594, "timestep": 0.552, "gradients_limiter": 0.840, "faces_riemann": 0.877,
-        "gather_update": 0.762, "face_links": 0.0},
-    2: {"neighbours_density": 0.722, "timestep": 0.655, "gradients_limiter": 0.766, "faces_riemann": 0.834,
+    3: {"neighbours_density": 0.588, "timestep": 0.546, "gradients_limiter": 0.840, "faces_riemann": 0.878,
+        "gather_update": 0.764, "face_links": 0.0},
+    2: {"neighbours_density": 0.716, "timestep": 0.656, "gradients_limiter": 0.766, "faces_riemann": 0.858,
         "gather_update": 0.840, "face_links": 0.0},
 }
 # Operations of the reference's method per unit, counted by the

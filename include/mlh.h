@@ -321,7 +321,8 @@ int mlh_probe_fp64_lanes(int active_lanes, int iters, double *ms);
 int mlh_pstar_infer(const float *weights, const float *x, int n, float *y);
 /* Mean squared error over n samples and its gradient (8705 floats). */
 int mlh_pstar_grad(const float *weights, const float *x, const float *t, int n, float *loss, float *grad);
-/* Adam training on the GPU (epochs over shuffled mini-batches), in place on
+/* Adam training on the GPU (epochs over shuffled mini-batches, the learning
+ * rate decayed from lr to lr / 100 along a half cosine), in place on
  * `weights`; loss_history (epochs floats, may be NULL) gets the mean batch loss. */
 int mlh_pstar_train(const float *x, const float *t, long long n, int epochs, int batch, float lr, unsigned seed,
                     float *weights, float *loss_history);

@@ -2121,14 +2121,20 @@ __device__ __forceinline__ unsigned project_flux(const RiemannResult &rs, const 
     return st;
 }
 
-// Register cap of the face kernel: 168 registers (a small spill) let 12
-// warps per SM instead of 8 hide the FP64 pipe's dependency latency
-// (measured: face pass 3.7 % faster on the Sedov 128^3 step; 128 registers
-// spill too much).  Blocks of up to 256 threads.
-#ifndef MLH_FACE_MAXREG
-#define MLH_FACE_MAXREG 168
+// Register caps of the face kernels, per dimension: more warps per SM hide
+// more of the Riemann iteration's dependency latency, fewer registers spill
+// more.  Measured on the face passes: 3D (Sedov 128^3) 168 registers (12
+// warps per SM, a small spill) 21.60 ms, against 21.74 / 21.81 / 22.29 /
+// 21.80 ms at 152 / 144 / 136 / 128; 2D (the 256-member KH ensemble) 128
+// registers (16 warps) 19.34 ms, against 20.95 ms at 168 and 21.6-21.9 ms
+// at 136-152.  Blocks of up to 256 threads.
+#ifndef MLH_FACE_MAXREG_3D
+#define MLH_FACE_MAXREG_3D 168
 #endif
-#define MLH_FACE_BOUNDS __maxnreg__(MLH_FACE_MAXREG)
+#ifndef MLH_FACE_MAXREG_2D
+#define MLH_FACE_MAXREG_2D 128
+#endif
+#define MLH_FACE_BOUNDS __maxnreg__(D == 3 ? MLH_FACE_MAXREG_3D : MLH_FACE_MAXREG_2D)
 // The face-frame Riemann problem of canonical face f (i < j): effective face
 // A_ij = psi~_j(x_i)/omega_i - psi~_i(x_j)/omega_j from the psi~ of both
 // slots (compEffectiveFace, Particles.cpp:1290-1311, 2504-2531); boosted,

@@ -417,7 +417,11 @@ extern "C" int mlh_pstar_grad(const float *weights, const float *x, const float 
 }
 
 // Adam on the GPU over `epochs` passes of shuffled mini-batches of `batch`
-// samples; weights are read from and written back to `weights` (host);
+// samples, the learning rate decayed from lr to lr / 100 along a half cosine
+// over the run (Adam moves every parameter by about the learning rate per
+// step whatever its gradient, so at a constant rate the final weights, and
+// with them the output's offset, land anywhere in a band of a few lr);
+// weights are read from and written back to `weights` (host);
 // loss_history[e] receives the mean mini-batch loss of epoch e.
 extern "C" int mlh_pstar_train(const float *x, const float *t, long long n, int epochs, int batch, float lr,
                                unsigned seed, float *weights, float *loss_history) {
@@ -444,6 +448,7 @@ extern "C" int mlh_pstar_train(const float *x, const float *t, long long n, int 
     for (long long i = 0; i < n; ++i) perm[i] = (int)i;
     std::mt19937_64 rng(seed);
     const long long per_epoch = n / batch;
+    const double total = (double)epochs * (double)per_epoch;
     int step = 0;
     for (int e = 0; e < epochs; ++e) {
         std::shuffle(perm.begin(), perm.end(), rng);
@@ -452,7 +457,9 @@ extern "C" int mlh_pstar_train(const float *x, const float *t, long long n, int 
             pstar_pack(w.as<float>(), pk.p, 0);
             pstar_train_batch(dx.as<float4>(), dt.as<float>(), idx.as<int>() + b * batch, batch, pk.p,
                               part.as<float>(), g.as<float>(), l.as<float>() + (size_t)e * per_epoch + b, 0);
-            pstar_adam(w.as<float>(), g.as<float>(), m1.as<float>(), m2.as<float>(), lr, ++step, 0);
+            const double frac = total > 1. ? (double)step / (total - 1.) : 1.;
+            const float lr_t = (float)(lr * (0.01 + 0.99 * 0.5 * (1. + cos(3.14159265358979323846 * frac))));
+            pstar_adam(w.as<float>(), g.as<float>(), m1.as<float>(), m2.as<float>(), lr_t, ++step, 0);
         }
     }
     PCK(cudaGetLastError());
