@@ -173,8 +173,8 @@ typedef struct mlh_tuning {
 /* Autotuner: times the face-pass structures over candidate grids, then
  * candidate launch shapes of the face, gradient and neighbour kernels, then
  * whole steps with the face links in order, overlapped on a second stream
- * or inside the gradients kernel, and with and without the persistent
- * binning, over
+ * or inside the gradients kernel, with and without the persistent binning,
+ * and with and without the slope limiter's single-precision filter, over
  * `trial_steps` steps each (from a saved copy of the
  * state, which is restored afterwards), keeps the fastest in the context and
  * reports them in *out (may be NULL).  Needs one state-sized temporary. */

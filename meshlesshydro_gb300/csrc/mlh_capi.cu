@@ -823,6 +823,23 @@ int mlh_autotune(mlh_ctx *c, int trial_steps, mlh_tuning *out) {
             }
         }
         c->tune.persistent_binning = best.persistent_binning;
+        // the slope limiter's single-precision filter on or off (the same
+        // bits either way; it trades FP64 work for two single-precision
+        // passes, which pays or not with the gradients' occupancy)
+        best_step = 1e300;
+        const int keep = c->tune.fp32_filters & MLH_FILTER_TIMESTEP;
+        for (int sf : {keep | MLH_FILTER_SLOPE, keep}) {
+            c->tune.fp32_filters = sf;
+            for (int rep = 0; rep < 2; ++rep) {
+                if ((rc = restore())) goto done;
+                mlh_step_stats st;
+                rc = mlh_step(c, trial_steps, 0., &st);
+                if (rc & (MLH_ERR_CUDA | MLH_ERR_INVALID | MLH_ERR_TIMEOUT)) goto done;
+                rc = 0;
+                if (st.device_ms < best_step) { best_step = st.device_ms; best.fp32_filters = sf; }
+            }
+        }
+        c->tune.fp32_filters = best.fp32_filters;
     }
 done:
     {
