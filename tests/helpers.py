@@ -51,10 +51,11 @@ GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
 #    of the gate (limit infinity), counted, and the field scales are taken
 #    over the others;
 #  * Newton ties: faces whose iterations stop one step apart on the two sides
-#    (the GPU seeds Newton with a two-rarefaction guess accurate to ~1e-13, so
-#    where the first step's change lies within that of the 1e-10 stopping
-#    threshold, one side takes one more step; in that quadratic regime the
-#    extra step moves p* by ~tol^2).  They are counted (at most
+#    (the GPU's two-rarefaction guess and pressure functions use fifth roots,
+#    reciprocals and reciprocal square roots a few ulp from the oracle's pow,
+#    division and sqrt, so where the first step's change lies within that of
+#    the 1e-10 stopping threshold, one side takes one more step; in that
+#    quadratic regime the extra step moves p* by ~tol^2).  They are counted (at most
 #    MAX_TIE_FRACTION of the faces) and the entries of their particles are
 #    held to RIEMANN_TIE_RTOL.
 # The normwise error max|a - b| / max|b| is reported beside it.  States after
