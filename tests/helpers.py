@@ -66,7 +66,7 @@ FIELD_FLOOR = 1e-3          # default floor of assert_close
 SUM_FLOOR = 2e-2
 LIMITER_RTOL = 1e-10
 RIEMANN_TIE_RTOL = 1e-8
-MAX_TIE_FRACTION = 1e-3
+MAX_TIE_FRACTION = 1e-4
 COND_EPS = 1e-15
 COND_CAP = 1e-6             # the largest tolerance a condition number can give
 EXACT_FIELDS = {"omega", "rho", "P", "dt"}
