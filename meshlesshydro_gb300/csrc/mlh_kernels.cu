@@ -1496,16 +1496,21 @@ __device__ __forceinline__ double field_of(const Prim &q, int f) {
 // numeric_limits<double>::min(), the same expressions), on the positions and
 // velocities that pass loads anyway; the per-particle dt goes into the
 // per-member minimum (warp reduction, then one atomicMin on its bit pattern).
-// Register cap of the gradients kernel.  It waits on dependent gathers as
-// much as on the FP64 pipe (Sedov 64^3: FP64 pipe 73 % active, 17 % of the
-// warp slots occupied at 146 registers), so warps per SM matter: 128
-// registers (16 warps per SM, a small spill) took the Sedov 128^3 gradients
-// from 11.1-11.4 to 10.1 ms; 112 spill more and gave 10.4 ms.  Blocks of up
-// to 256 threads.
+// Register caps of the gradients kernel, per dimension.  It waits on
+// dependent gathers as much as on the FP64 pipe (Sedov 64^3: FP64 pipe 73 %
+// active, 17 % of the warp slots occupied at 146 registers), so warps per SM
+// matter: in 3D 128 registers (16 warps per SM, a small spill) took the Sedov
+// 128^3 gradients from 11.1-11.4 to 10.1 ms (112: 10.4, 120: +0.2 ms, 136:
+// +0.5 ms); in 2D (the KH ensemble, 110 registers uncapped) 96 registers
+// gave 7.19 ms against 7.45 at 104 and 7.59 at 128.  Blocks of up to 256
+// threads.
 #ifndef MLH_GRAD_MAXREG
 #define MLH_GRAD_MAXREG 128
 #endif
-#define MLH_GRAD_BOUNDS __maxnreg__(MLH_GRAD_MAXREG)
+#ifndef MLH_GRAD_MAXREG_2D
+#define MLH_GRAD_MAXREG_2D 96
+#endif
+#define MLH_GRAD_BOUNDS __maxnreg__(D == 3 ? MLH_GRAD_MAXREG : MLH_GRAD_MAXREG_2D)
 template <int D>
 __global__ void MLH_GRAD_BOUNDS k_gradients(Params p, const Member *__restrict__ members,
                                                    const int *__restrict__ memberOf, const GridInfo *__restrict__ grids,
