@@ -446,7 +446,12 @@ def network_error(runtime, w, sim_factory):
 def learned_vs_plain(runtime, make, w, args, tuning_plain=None, st_plain=None, kt_plain=None, rho_plain=None):
     """The same steps with and without the learned guess, each with the
     autotuner's launch shapes for its own pipeline (so that the learned step
-    may take another face-pass structure); device time of the timed steps."""
+    may take another face-pass structure, and the plain face pipeline where
+    the network does not pay: `learned_guess` 0); device time of the timed
+    steps.  `learned_over_plain` is the learned context as the autotuner
+    configures it; the network pipeline itself (learned_guess 1, the
+    autotuner's other shapes) is timed beside it, with its Newton-step
+    savings."""
     out = {}
     if st_plain is None:
         sp = make()
@@ -458,16 +463,25 @@ def learned_vs_plain(runtime, make, w, args, tuning_plain=None, st_plain=None, k
     sl = make()
     sl.set_pstar_weights(w)
     tuning_l = sl.autotune(2)
+    st_a, _ = timed_steps(sl, args.warmup, args.steps, check=False)
+    sl.close()
+    # the network pipeline with the same shapes
+    sl = make()
+    sl.set_pstar_weights(w)
+    sl.set_tuning(dict(tuning_l, learned_guess=1))
     st, _ = timed_steps(sl, args.warmup, args.steps, check=False)
     rho = sl.get("rho")
     kt = kernel_breakdown(sl, args.steps)
     sl.close()
     npart = rho.size
+    v_a = npart * st_a.steps / (st_a.device_ms / 1e3)
     v_l = npart * st.steps / (st.device_ms / 1e3)
     v_p = npart * st_plain.steps / (st_plain.device_ms / 1e3)
     saved = st_plain.newton_iterations - st.newton_iterations
     out.update({
-        "value": v_l, "plain_value": v_p, "learned_over_plain": v_l / v_p,
+        "value": v_a, "plain_value": v_p, "learned_over_plain": v_a / v_p,
+        "learned_guess_chosen": int(tuning_l.get("learned_guess", 1)),
+        "network_pipeline_value": v_l, "network_pipeline_over_plain": v_l / v_p,
         "newton_iterations_per_face": st.newton_iterations / max(st.faces, 1),
         "plain_newton_iterations_per_face": st_plain.newton_iterations / max(st_plain.faces, 1),
         "iterations_saved": int(saved),

@@ -168,21 +168,29 @@ typedef struct mlh_tuning {
                               * evaluates v_sig only for the particles whose
                               * bounded dt can be the minimum; 0: FP64 at every
                               * neighbour */
+    int learned_guess;       /* with star-pressure weights set
+                              * (mlh_set_pstar_weights): 1 runs the learned face
+                              * pipeline, 0 the plain one (the weights stay
+                              * set); the autotuner keeps the faster, so that
+                              * the network runs only where it pays */
 } mlh_tuning;
 
 /* Autotuner: times the face-pass structures over candidate grids, then
  * candidate launch shapes of the face, gradient and neighbour kernels, then
  * whole steps with the face links in order, overlapped on a second stream
- * or inside the gradients kernel, with and without the persistent binning,
+ * or inside the gradients kernel, with and without the persistent binning
  * and with and without the slope limiter's single-precision filter, over
- * `trial_steps` steps each (from a saved copy of the
- * state, which is restored afterwards), keeps the fastest in the context and
- * reports them in *out (may be NULL).  Needs one state-sized temporary. */
+ * `trial_steps` steps each (from a saved copy of the state, which is
+ * restored afterwards), keeps the fastest in the context and reports them in
+ * *out (may be NULL).  With star-pressure weights set it runs that search
+ * for the learned face pipeline and for the plain one (`learned_guess`) and
+ * keeps the faster.  Needs one state-sized temporary. */
 int mlh_autotune(mlh_ctx *ctx, int trial_steps, mlh_tuning *out);
 /* Set the launch shapes directly (for example those an autotuned context of
  * the same workload reported).  Threads per block: 64, 128 or 256; blocks
  * per SM 1..32; warps per SM 8..256; face_split and link_overlap 0, 1 or 2;
- * persistent_binning 0 or 1; fp32_filters 0..3.  MLH_ERR_INVALID otherwise. */
+ * persistent_binning and learned_guess 0 or 1; fp32_filters 0..3.
+ * MLH_ERR_INVALID otherwise. */
 int mlh_set_tuning(mlh_ctx *ctx, const mlh_tuning *tuning);
 
 /* Per-particle smoothing lengths of the current state (no counterpart in the

@@ -292,7 +292,7 @@ StepArgs make_args(mlh_ctx *c, double dt_max) {
     a.status = c->status; a.dtbits = c->dtbits; a.newtonSum = c->newtonSum;
     a.dt = c->dt; a.simTime = c->simTime; a.stepsDone = c->stepsDone;
     a.scanTiles = c->scanTiles; a.scanTotal = c->scanTotal;
-    a.learned = c->learned ? 1 : 0;
+    a.learned = (c->learned && c->tune.learned_guess) ? 1 : 0;
     a.fstate = c->fstate; a.feat = c->feat; a.yguess = c->yguess;
     a.queueFace = c->queueFace; a.queueCount = c->queueCount; a.mlp_packed = c->mlp_packed;
     a.fstate2 = c->fstate2; a.queueFace2 = c->queueFace2; a.queueCount2 = c->queueCount2;
@@ -678,7 +678,7 @@ int mlh_set_tuning(mlh_ctx *c, const mlh_tuning *t) {
         t->face_blocks_per_sm > 32 || t->nns_warps_per_sm < 8 || t->nns_warps_per_sm > 256 ||
         t->face_split < 0 || t->face_split > 2 || t->link_overlap < 0 || t->link_overlap > 2 ||
         t->persistent_binning < 0 || t->persistent_binning > 1 || (t->persistent_binning && c->bin_blocks < 1) ||
-        t->fp32_filters < 0 || t->fp32_filters > 3) {
+        t->fp32_filters < 0 || t->fp32_filters > 3 || t->learned_guess < 0 || t->learned_guess > 1) {
         g_last_error = "invalid tuning";
         return MLH_ERR_INVALID;
     }
@@ -691,6 +691,7 @@ int mlh_set_tuning(mlh_ctx *c, const mlh_tuning *t) {
     c->tune.link_overlap = t->link_overlap;
     c->tune.persistent_binning = t->persistent_binning;
     c->tune.fp32_filters = t->fp32_filters;
+    c->tune.learned_guess = t->learned_guess;
     drop_graph(c);
     return 0;
 }
@@ -742,104 +743,130 @@ int mlh_autotune(mlh_ctx *c, int trial_steps, mlh_tuning *out) {
         if ((rc = trial(KT_FACES, dummy))) goto done;
     }
     {
-        const int cand_t[] = {64, 128, 256};
-        const int cand_b[] = {2, 4, 8, 16, 32};
-        Tuning best = c->tune;
-        double best_ms = 1e300;
-        // the face passes: one (0), a second over a queue (1) or the
-        // unfinished faces continued inside the block (2), each over the
-        // candidate grids (the structures favour different grids); which
-        // pays depends on how many faces need a second Newton step
-        for (int split : {1, 2, 0}) {
-            for (int b : cand_b) {
-                c->tune.face_split = split;
-                c->tune.face_blocks_per_sm = b;
-                double ms;
-                if ((rc = trial(KT_FACES, ms))) goto done;
-                if (ms < best_ms) { best_ms = ms; best.face_split = split; best.face_blocks_per_sm = b; }
+        // with star-pressure weights set, the whole search once per face
+        // pipeline (learned, then plain: `learned_guess`), each tuned for
+        // itself, and the faster kept: the network pays only where strong
+        // shocks are frequent enough to outweigh its evaluation and passes
+        const Tuning init = c->tune;
+        Tuning chosen = c->tune;
+        double chosen_ms = 1e300;
+        const int npipes = c->learned ? 2 : 1;
+        for (int pipe = 0; pipe < npipes; ++pipe) {
+            c->tune = init;
+            if (c->learned) c->tune.learned_guess = pipe == 0 ? 1 : 0;
+            {
+                const int cand_t[] = {64, 128, 256};
+                const int cand_b[] = {2, 4, 8, 16, 32};
+                Tuning best = c->tune;
+                double best_ms = 1e300;
+                // the face passes: one (0), a second over a queue (1) or the
+                // unfinished faces continued inside the block (2), each over the
+                // candidate grids (the structures favour different grids); which
+                // pays depends on how many faces need a second Newton step
+                for (int split : {1, 2, 0}) {
+                    for (int b : cand_b) {
+                        c->tune.face_split = split;
+                        c->tune.face_blocks_per_sm = b;
+                        double ms;
+                        if ((rc = trial(KT_FACES, ms))) goto done;
+                        if (ms < best_ms) { best_ms = ms; best.face_split = split; best.face_blocks_per_sm = b; }
+                    }
+                }
+                c->tune.face_split = best.face_split;
+                c->tune.face_blocks_per_sm = best.face_blocks_per_sm;
+                for (int t : cand_t) {
+                    c->tune.face_threads = t;
+                    double ms;
+                    if ((rc = trial(KT_FACES, ms))) goto done;
+                    if (ms < best_ms) { best_ms = ms; best.face_threads = t; }
+                }
+                c->tune.face_threads = best.face_threads;
+                for (int b : cand_b) {   // the grid again, for the chosen block size
+                    c->tune.face_blocks_per_sm = b;
+                    double ms;
+                    if ((rc = trial(KT_FACES, ms))) goto done;
+                    if (ms < best_ms) { best_ms = ms; best.face_blocks_per_sm = b; }
+                }
+                c->tune.face_blocks_per_sm = best.face_blocks_per_sm;
+                best_ms = 1e300;
+                for (int t : cand_t) {
+                    c->tune.grad_threads = t;
+                    double ms;
+                    if ((rc = trial(KT_GRAD, ms))) goto done;
+                    if (ms < best_ms) { best_ms = ms; best.grad_threads = t; }
+                }
+                c->tune.grad_threads = best.grad_threads;
+                best_ms = 1e300;
+                const int cand_w[] = {16, 32, 64, 128};
+                for (int w : cand_w) {
+                    c->tune.nns_warps_per_sm = w;
+                    double ms;
+                    if ((rc = trial(KT_NNS, ms))) goto done;
+                    if (ms < best_ms) { best_ms = ms; best.nns_warps_per_sm = w; }
+                }
+                c->tune.nns_warps_per_sm = best.nns_warps_per_sm;
+                // the face links beside the time step and the gradients, or in order:
+                // whole steps without per-kernel timing (which serialises the
+                // streams), the better of two trials each
+                double best_step = 1e300;
+                for (int ov : {1, 0, 2}) {
+                    c->tune.link_overlap = ov;
+                    for (int rep = 0; rep < 2; ++rep) {
+                        if ((rc = restore())) goto done;
+                        mlh_step_stats st;
+                        rc = mlh_step(c, trial_steps, 0., &st);
+                        if (rc & (MLH_ERR_CUDA | MLH_ERR_INVALID)) goto done;
+                        rc = 0;
+                        if (st.device_ms < best_step) { best_step = st.device_ms; best.link_overlap = ov; }
+                    }
+                }
+                c->tune.link_overlap = best.link_overlap;
+                // the binning as one persistent kernel or one launch per phase
+                best_step = 1e300;
+                for (int pb : {0, 1}) {
+                    if (pb && c->bin_blocks < 1) continue;
+                    c->tune.persistent_binning = pb;
+                    for (int rep = 0; rep < 2; ++rep) {
+                        if ((rc = restore())) goto done;
+                        mlh_step_stats st;
+                        rc = mlh_step(c, trial_steps, 0., &st);
+                        if (rc & (MLH_ERR_CUDA | MLH_ERR_INVALID | MLH_ERR_TIMEOUT)) goto done;
+                        rc = 0;
+                        if (st.device_ms < best_step) { best_step = st.device_ms; best.persistent_binning = pb; }
+                    }
+                }
+                c->tune.persistent_binning = best.persistent_binning;
+                // the slope limiter's single-precision filter on or off (the same
+                // bits either way; it trades FP64 work for two single-precision
+                // passes, which pays or not with the gradients' occupancy)
+                best_step = 1e300;
+                const int keep = c->tune.fp32_filters & MLH_FILTER_TIMESTEP;
+                for (int sf : {keep | MLH_FILTER_SLOPE, keep}) {
+                    c->tune.fp32_filters = sf;
+                    for (int rep = 0; rep < 2; ++rep) {
+                        if ((rc = restore())) goto done;
+                        mlh_step_stats st;
+                        rc = mlh_step(c, trial_steps, 0., &st);
+                        if (rc & (MLH_ERR_CUDA | MLH_ERR_INVALID | MLH_ERR_TIMEOUT)) goto done;
+                        rc = 0;
+                        if (st.device_ms < best_step) { best_step = st.device_ms; best.fp32_filters = sf; }
+                    }
+                }
+                c->tune.fp32_filters = best.fp32_filters;
             }
-        }
-        c->tune.face_split = best.face_split;
-        c->tune.face_blocks_per_sm = best.face_blocks_per_sm;
-        for (int t : cand_t) {
-            c->tune.face_threads = t;
-            double ms;
-            if ((rc = trial(KT_FACES, ms))) goto done;
-            if (ms < best_ms) { best_ms = ms; best.face_threads = t; }
-        }
-        c->tune.face_threads = best.face_threads;
-        for (int b : cand_b) {   // the grid again, for the chosen block size
-            c->tune.face_blocks_per_sm = b;
-            double ms;
-            if ((rc = trial(KT_FACES, ms))) goto done;
-            if (ms < best_ms) { best_ms = ms; best.face_blocks_per_sm = b; }
-        }
-        c->tune.face_blocks_per_sm = best.face_blocks_per_sm;
-        best_ms = 1e300;
-        for (int t : cand_t) {
-            c->tune.grad_threads = t;
-            double ms;
-            if ((rc = trial(KT_GRAD, ms))) goto done;
-            if (ms < best_ms) { best_ms = ms; best.grad_threads = t; }
-        }
-        c->tune.grad_threads = best.grad_threads;
-        best_ms = 1e300;
-        const int cand_w[] = {16, 32, 64, 128};
-        for (int w : cand_w) {
-            c->tune.nns_warps_per_sm = w;
-            double ms;
-            if ((rc = trial(KT_NNS, ms))) goto done;
-            if (ms < best_ms) { best_ms = ms; best.nns_warps_per_sm = w; }
-        }
-        c->tune.nns_warps_per_sm = best.nns_warps_per_sm;
-        // the face links beside the time step and the gradients, or in order:
-        // whole steps without per-kernel timing (which serialises the
-        // streams), the better of two trials each
-        double best_step = 1e300;
-        for (int ov : {1, 0, 2}) {
-            c->tune.link_overlap = ov;
-            for (int rep = 0; rep < 2; ++rep) {
-                if ((rc = restore())) goto done;
-                mlh_step_stats st;
-                rc = mlh_step(c, trial_steps, 0., &st);
-                if (rc & (MLH_ERR_CUDA | MLH_ERR_INVALID)) goto done;
-                rc = 0;
-                if (st.device_ms < best_step) { best_step = st.device_ms; best.link_overlap = ov; }
-            }
-        }
-        c->tune.link_overlap = best.link_overlap;
-        // the binning as one persistent kernel or one launch per phase
-        best_step = 1e300;
-        for (int pb : {0, 1}) {
-            if (pb && c->bin_blocks < 1) continue;
-            c->tune.persistent_binning = pb;
+            // the pipeline's whole step with its shapes
+            double pipe_ms = 1e300;
             for (int rep = 0; rep < 2; ++rep) {
                 if ((rc = restore())) goto done;
                 mlh_step_stats st;
                 rc = mlh_step(c, trial_steps, 0., &st);
                 if (rc & (MLH_ERR_CUDA | MLH_ERR_INVALID | MLH_ERR_TIMEOUT)) goto done;
                 rc = 0;
-                if (st.device_ms < best_step) { best_step = st.device_ms; best.persistent_binning = pb; }
+                if (st.device_ms < pipe_ms) pipe_ms = st.device_ms;
             }
+            if (pipe_ms < chosen_ms) { chosen_ms = pipe_ms; chosen = c->tune; }
         }
-        c->tune.persistent_binning = best.persistent_binning;
-        // the slope limiter's single-precision filter on or off (the same
-        // bits either way; it trades FP64 work for two single-precision
-        // passes, which pays or not with the gradients' occupancy)
-        best_step = 1e300;
-        const int keep = c->tune.fp32_filters & MLH_FILTER_TIMESTEP;
-        for (int sf : {keep | MLH_FILTER_SLOPE, keep}) {
-            c->tune.fp32_filters = sf;
-            for (int rep = 0; rep < 2; ++rep) {
-                if ((rc = restore())) goto done;
-                mlh_step_stats st;
-                rc = mlh_step(c, trial_steps, 0., &st);
-                if (rc & (MLH_ERR_CUDA | MLH_ERR_INVALID | MLH_ERR_TIMEOUT)) goto done;
-                rc = 0;
-                if (st.device_ms < best_step) { best_step = st.device_ms; best.fp32_filters = sf; }
-            }
-        }
-        c->tune.fp32_filters = best.fp32_filters;
+        c->tune = chosen;
     }
 done:
     {
@@ -860,6 +887,7 @@ done:
         out->link_overlap = c->tune.link_overlap;
         out->persistent_binning = c->tune.persistent_binning;
         out->fp32_filters = c->tune.fp32_filters;
+        out->learned_guess = c->tune.learned_guess;
     }
     return rc;
 }

@@ -19,6 +19,7 @@ struct Tuning {
     int link_overlap = 1;          // face links on the second stream beside the time step and gradients
     int persistent_binning = 0;    // the binning as one persistent cooperative kernel (k_binning)
     int fp32_filters = 3;          // bits: 1 slope-limiter extrema, 2 time step (FP64 only where a single-precision bound reaches the result)
+    int learned_guess = 1;         // with weights set: 1 the learned face pipeline, 0 the plain one
 };
 
 // bits of Tuning::fp32_filters

@@ -46,7 +46,7 @@ class Tuning(ctypes.Structure):
                 ("grad_threads", ctypes.c_int), ("nns_warps_per_sm", ctypes.c_int),
                 ("face_split", ctypes.c_int),
                 ("link_overlap", ctypes.c_int), ("persistent_binning", ctypes.c_int),
-                ("fp32_filters", ctypes.c_int)]
+                ("fp32_filters", ctypes.c_int), ("learned_guess", ctypes.c_int)]
 
 
 class ParticlesView(ctypes.Structure):
@@ -393,9 +393,10 @@ class Simulation:
         return {k: getattr(t, k) for k, _ in Tuning._fields_}
 
     def set_tuning(self, tuning: dict):
-        """Launch shapes (mlh_set_tuning); face_split and link_overlap
-        default to 1, persistent_binning to 0, fp32_filters to 3 (both)."""
-        dflt = {"face_split": 1, "link_overlap": 1, "persistent_binning": 0, "fp32_filters": 3}
+        """Launch shapes (mlh_set_tuning); face_split, link_overlap and
+        learned_guess default to 1, persistent_binning to 0, fp32_filters to
+        3 (both)."""
+        dflt = {"face_split": 1, "link_overlap": 1, "persistent_binning": 0, "fp32_filters": 3, "learned_guess": 1}
         t = Tuning(**{k: int(tuning.get(k, dflt[k]) if k in dflt else tuning[k]) for k, _ in Tuning._fields_})
         st = self.L.mlh_set_tuning(self.h, ctypes.byref(t))
         if st != 0:

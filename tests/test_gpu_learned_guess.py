@@ -219,3 +219,33 @@ def test_network_saves_newton_iterations_on_strong_shocks(strong_trained, oracle
     for key, v in o.state().items():
         assert_normwise(gb[key], v, LEARNED_RTOL, what="learned " + key)
         assert_normwise(gb[key], ga[key], LEARNED_RTOL, what="learned vs plain " + key)
+
+
+def test_learned_guess_off_runs_the_plain_pipeline():
+    """With weights set and mlh_tuning.learned_guess 0 (what the autotuner
+    keeps where the network does not pay), the step is the plain step bit
+    for bit and no face takes the network's guess; with 1 the network
+    pipeline runs again."""
+    rt = _runtime()
+    cfg, p = _cases()[1]
+    w = rt.pstar_init(7)
+    base = {"face_threads": 128, "face_blocks_per_sm": 4, "grad_threads": 64, "nns_warps_per_sm": 32,
+            "face_split": 1}
+    plain = rt.Simulation(cfg, p)
+    plain.set_tuning(base)
+    st_p = plain.step(3)
+    want = plain.get_state()
+    plain.close()
+    s = rt.Simulation(cfg, p)
+    s.set_pstar_weights(w)
+    s.set_tuning(dict(base, learned_guess=0))
+    st = s.step(3)
+    got = s.get_state()
+    assert st.learned_faces == 0
+    assert st.newton_iterations == st_p.newton_iterations
+    for k in want:
+        assert np.array_equal(got[k], want[k]), k
+    s.set_tuning(dict(base, learned_guess=1))
+    st = s.step(1)
+    assert st.status == 0
+    s.close()
