@@ -133,6 +133,10 @@ def test_set_tuning_validates_and_keeps_bits():
     with pytest.raises(runtime.MLHError):
         b.set_tuning({"face_threads": 256, "face_blocks_per_sm": 3, "grad_threads": 64, "nns_warps_per_sm": 16,
                       "link_overlap": 3})
+    for bad in ({"fp32_filters": 4}, {"fp32_filters": -1}, {"learned_guess": 2}, {"persistent_binning": 2}):
+        with pytest.raises(runtime.MLHError):
+            b.set_tuning(dict({"face_threads": 256, "face_blocks_per_sm": 3, "grad_threads": 64,
+                               "nns_warps_per_sm": 16}, **bad))
     a.step(2)
     b.step(2)
     c.step(2)
