@@ -1,5 +1,5 @@
 // FP64 pipe throughput probe: the denominator of the FP64 roofline of the
-// MFV kernels (the machine's measured peaks cover HBM copy and BF16 GEMM only).
+// MFV kernels (measured HBM-copy and BF16-GEMM peaks give no FP64 figure).
 // Independent fused multiply-add chains keep the FP64 pipe busy; one FMA
 // counts as two floating-point operations.
 #include "../../include/mlh.h"
