@@ -1,5 +1,5 @@
 // TEST INFRASTRUCTURE (oracle).  Not part of the product: only tests/, the
-// smoke check and bench.py's CPU baseline load this library, as the checker.
+// smoke check and bench.py's CPU baseline load this library, to compare against.
 //
 // A plain, serial CPU restatement of one MFV (meshless finite volume) step of
 // the reference demonstrator, jammartin/meshlessHydro.  Every stage follows the

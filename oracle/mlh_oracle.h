@@ -3,7 +3,7 @@
  * C interface of the CPU restatement of the reference's MFV timestep
  * (jammartin/meshlessHydro, demonstrator/src/MeshlessScheme.cpp:39-253 and the
  * Particles stage methods it calls).  Only tests/, the smoke check and
- * bench.py's CPU baseline load this library, as the checker.
+ * bench.py's CPU baseline load this library, to compare against.
  */
 #ifndef MLH_ORACLE_H
 #define MLH_ORACLE_H

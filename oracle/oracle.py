@@ -1,8 +1,8 @@
 """TEST INFRASTRUCTURE (oracle): ctypes access to the CPU restatement
 (oracle/libmlh_oracle.so) and to the reference build (oracle/_ref/ref_*).
 
-Only tests/, the smoke check and bench.py's CPU baseline use this module, as
-the checker; the product never imports it.
+Only tests/, the smoke check and bench.py's CPU baseline use this module, to
+compare against; the product never imports it.
 """
 from __future__ import annotations
 
