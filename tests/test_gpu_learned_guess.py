@@ -249,3 +249,33 @@ def test_learned_guess_off_runs_the_plain_pipeline():
     st = s.step(1)
     assert st.status == 0
     s.close()
+
+
+def test_autotune_with_weights_picks_a_pipeline_and_restores_the_state():
+    """With weights set the autotuner searches both face pipelines
+    (learned_guess 1 and 0), reports the one it keeps, and leaves the state
+    as it found it: the next steps are those of a context set to the
+    reported tuning directly."""
+    rt = _runtime()
+    cfg, p = _cases()[1]
+    w = rt.pstar_init(3)
+    s = rt.Simulation(cfg, p)
+    s.set_pstar_weights(w)
+    before = s.get_state()
+    tun = s.autotune(1)
+    assert tun["learned_guess"] in (0, 1)
+    after = s.get_state()
+    for k in before:
+        assert np.array_equal(before[k], after[k]), k
+    st = s.step(2)
+    assert st.status == 0
+    got = s.get_state()
+    s.close()
+    ref = rt.Simulation(cfg, p)
+    ref.set_pstar_weights(w)
+    ref.set_tuning(tun)
+    ref.step(2)
+    want = ref.get_state()
+    ref.close()
+    for k in want:
+        assert np.array_equal(got[k], want[k]), k
