@@ -127,8 +127,9 @@ struct Harvest {
 //   q <= 1:     sigma   * fma(-(1.5 q) q, t, 1),  t = fma(-0.5, q, 1) = 1 - q/2
 //   1 < q < 2:  sigma/4 * fma((t t) t, 1, 0),     t = fma(-1, q, 2) = 2 - q
 // (fma(z, 1, 0) = z for z >= 0, and sigma/4 is exact), each the value of the
-// reference's expression for its piece.
-__device__ __forceinline__ double kernelW2(double r, double ih2, double sigma) {
+// reference's expression for its piece.  sigma4 = sigma / 4 is passed in
+// (computed once per particle, not per neighbour).
+__device__ __forceinline__ double kernelW2(double r, double ih2, double sigma, double sigma4) {
     // r >= 0, so q >= 0 and the range tests compare bit patterns (integer
     // pipe): q <= 1 and q < 2
     const double q = __dmul_rn(r, ih2);
@@ -139,10 +140,9 @@ __device__ __forceinline__ double kernelW2(double r, double ih2, double sigma) {
     const double z = __dmul_rn(y, inner ? q : t);
     const double zs = __longlong_as_double(__double_as_longlong(z) ^ (inner ? (long long)0x8000000000000000ull : 0ll));
     const double w = __fma_rn(zs, inner ? t : 1., inner ? 1. : 0.);
-    const double W = __dmul_rn(inner ? sigma : 0.25 * sigma, w);
+    const double W = __dmul_rn(inner ? sigma : sigma4, w);
     return qb < 0x4000000000000000ll ? W : 0.;
 }
-__device__ __forceinline__ double kernelW(double r, const Member &mb) { return kernelW2(r, mb.ih2, mb.sigma); }
 // Particles.cpp:10-15 (the value of the kernel at r = 0 is sigma)
 template <int D>
 __device__ __forceinline__ double kernel_sigma(double h2) {

@@ -792,7 +792,7 @@ __global__ void __launch_bounds__(NNS_WARPS * 32, MLH_NNS_MINB) k_neighbours(
                 myOff -= myN;
                 if (lane < NNS_PB) { offq[lane] = myOff; nrq[lane] = 0; niq[lane] = 0; }
                 double myX[3] = {0., 0., 0.};
-                double myHsq = mb.hsq, myIh2 = mb.ih2, mySig = mb.sigma;
+                double myHsq = mb.hsq, myIh2 = mb.ih2, mySig = mb.sigma, mySig4 = 0.;
                 if (lane < nb) {
 #pragma unroll
                     for (int a = 0; a < D; ++a) myX[a] = X[a][myI];
@@ -804,6 +804,7 @@ __global__ void __launch_bounds__(NNS_WARPS * 32, MLH_NNS_MINB) k_neighbours(
                         mySig = kernel_sigma<D>(h2_i);
                     }
                 }
+                mySig4 = 0.25 * mySig;   // the outer piece's factor, once per particle (exact)
                 __syncwarp();
                 for (int t0 = 0; t0 < seq; t0 += 32) {
                     const int gi = t0 + lane;
@@ -821,6 +822,7 @@ __global__ void __launch_bounds__(NNS_WARPS * 32, MLH_NNS_MINB) k_neighbours(
                     const double hsq_i = __shfl_sync(0xffffffffu, myHsq, q);
                     const double ih2_i = __shfl_sync(0xffffffffu, myIh2, q);
                     const double sigma_i = __shfl_sync(0xffffffffu, mySig, q);
+                    const double sigma4_i = __shfl_sync(0xffffffffu, mySig4, q);
                     bool pass = false, img = false;
                     uint32_t e = 0;
                     double r = 0., w = 0.;
@@ -853,7 +855,7 @@ __global__ void __launch_bounds__(NNS_WARPS * 32, MLH_NNS_MINB) k_neighbours(
                             pass = __double_as_longlong(d2) < __double_as_longlong(lim);
                             if (pass) {
                                 r = sqrt(d2);
-                                w = kernelW2(r, ih2_i, sigma_i);
+                                w = kernelW2(r, ih2_i, sigma_i, sigma4_i);
                             }
                         }
                     }
@@ -993,7 +995,8 @@ __device__ __forceinline__ void hsolve_shape_sel(double r, double ihh2, double &
     const double a2 = __dmul_rn(a, a);
     const double u = __fma_rn(0.75, q, -1.5);
     const double v = __fma_rn(-2.25, q, 3.);
-    const double f_ = __fma_rn(inner ? a2 : __dmul_rn(0.25, a2), inner ? u : t, inner ? 1. : 0.);
+    // a2 / 4 (exact) on the integer pipe
+    const double f_ = __fma_rn(inner ? a2 : scale_down<2>(a2), inner ? u : t, inner ? 1. : 0.);
     const double g_ = __dmul_rn(inner ? a2 : __dmul_rn(0.75, a2), inner ? v : q);
     f = in ? f_ : 0.;
     g = in ? g_ : 0.;
