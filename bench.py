@@ -281,6 +281,20 @@ def _time_oracle(o, seconds_hint, max_steps):
             return steps, el
 
 
+def _time_oracle_all_threads(oracle, p, cfg, seconds_hint, max_steps):
+    """The same restatement with its per-particle loops on every host core
+    (OpenMP; the results are the same bits for any thread count): steps per
+    second and the thread count.  The reference itself is single-threaded;
+    this is reported beside the serial figure, not instead of it."""
+    n = oracle.set_threads(0)
+    try:
+        o = oracle.Oracle(cfg, p)
+        steps, el = _time_oracle(o, seconds_hint, max_steps)
+    finally:
+        oracle.set_threads(1)
+    return p.n * steps / el, n
+
+
 def cpu_baseline_sample(seconds_hint: float = 15.0, kind: str = "sedov"):
     """The oracle (serial CPU restatement of the reference, -O3 as the
     reference's own build) on a bounded sample: whole MFV steps of the 32^3
@@ -294,13 +308,16 @@ def cpu_baseline_sample(seconds_hint: float = 15.0, kind: str = "sedov"):
     o1 = oracle.Oracle(cfg, p)
     o1.set_debug_level(1)
     steps1, el1 = _time_oracle(o1, seconds_hint / 3, 20)
+    v_all, n_all = _time_oracle_all_threads(oracle, p, cfg, seconds_hint / 3, 50)
     return {"value": p.n * steps / el, "unit": "particle-updates/s", "cores": 1, "kind": "port",
             "host_cores": host_cores(), "host_cpu": cpu_model(),
             "debug_lvl1_value": p.n * steps1 / el1,
+            "all_threads_value": v_all, "all_threads": n_all,
             "sample": f"{steps} MFV steps of the {what} ({p.n} particles, the workload's h/dx and neighbour "
                       f"count), serial oracle built -O3 -ffp-contract=off, {el:.1f} s, 1 of {host_cores()} "
                       f"cores of {cpu_model()}; debug_lvl1_value: the same with the reference's DEBUG_LVL 1 "
-                      f"flux-symmetry check, {steps1} steps"}
+                      f"flux-symmetry check, {steps1} steps; all_threads_value: the restatement's per-particle "
+                      f"loops on {n_all} threads (the reference itself is single-threaded)"}
 
 
 def run_reference(args):
@@ -317,15 +334,17 @@ def run_reference(args):
         o.step()
     el = time.perf_counter() - t0
     val = p.n * args.steps / el
+    v_all, n_all = _time_oracle_all_threads(oracle, p, cfg, 5.0, max(args.steps, 2))
     sample = (f"{what} ({p.n} particles, the workload's h/dx and neighbour count), one MFV step per step, "
               f"serial CPU restatement of the reference (the reference is single-threaded), built -O3, "
-              f"DEBUG_LVL 0")
+              f"DEBUG_LVL 0; all_threads_value: its per-particle loops on {n_all} threads")
     line = {"metric": METRIC, "value": val, "unit": "particle-updates/s", "n_gpus": ws, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": 1e3 * el / args.steps, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic", "impl": "reference",
             "config": {"workload": args.workload, "sample": sample},
             "cpu_baseline": {"value": val, "unit": "particle-updates/s", "cores": 1, "kind": "port",
-                             "host_cores": host_cores(), "sample": sample + f", host {cpu_model()}"},
+                             "host_cores": host_cores(), "all_threads_value": v_all, "all_threads": n_all,
+                             "sample": sample + f", host {cpu_model()}"},
             "e2e": {"value": val, "unit": "particle-updates/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
     return 0
