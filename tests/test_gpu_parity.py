@@ -28,6 +28,9 @@ def cases():
     kh100 = ic.kelvin_helmholtz(n_side=100, seed=1)
     sd12 = ic.sedov(n_side=12, seed=4, energy=0.05)
     sd16 = ic.sedov(n_side=16, seed=5)
+    # gamma = 1.4: the general-gamma Riemann path (pow instead of fifth roots)
+    kh24g = ic.kelvin_helmholtz(n_side=24, seed=3, gamma=1.4)
+    sd12g = ic.sedov(n_side=12, seed=4, energy=0.05, gamma=1.4)
     return {
         "kh24": (kh24, MFVConfig.kelvin_helmholtz(kh24)),
         "kh24_int_abs": (kh24, MFVConfig.kelvin_helmholtz(kh24, int_abs=True)),
@@ -35,8 +38,14 @@ def cases():
         # the face point x_i + kernelSize/4 (x_j - x_i) (FIRST_ORDER_QUAD_POINT 0)
         "kh24_pairwise_q": (kh24, MFVConfig.kelvin_helmholtz(kh24, pairwise_limiter=True,
                                                              first_order_quad_point=False)),
+        "kh24_gamma14": (kh24g, MFVConfig.kelvin_helmholtz(kh24g)),
+        # SLOPE_LIMITING 0 (MeshlessScheme.cpp:124-130, 140-144 skip slopeLimiter)
+        "kh24_no_slope_limiter": (kh24, MFVConfig.kelvin_helmholtz(kh24, slope_limiting=False)),
+        # ADAPTIVE_TIMESTEP 0: the configured timeStep (MeshlessScheme.cpp:91-105)
+        "kh24_fixed_dt": (kh24, MFVConfig.kelvin_helmholtz(kh24, adaptive_timestep=False, time_step=1e-3)),
         "kh100": (kh100, MFVConfig.kelvin_helmholtz(kh100)),
         "sedov12_nonperiodic_nopw": (sd12, MFVConfig.sedov(sd12, periodic=False, pairwise_limiter=False)),
+        "sedov12_gamma14_nonperiodic": (sd12g, MFVConfig.sedov(sd12g, periodic=False)),
         "sedov16_nonperiodic": (sd16, MFVConfig.sedov(sd16, periodic=False)),
         "sedov16_periodic": (sd16, MFVConfig.sedov(sd16, periodic=True)),
         "sedov16_periodic_int_abs": (sd16, MFVConfig.sedov(sd16, periodic=True, int_abs=True)),
@@ -179,7 +188,8 @@ def test_nan_reported():
     assert st.status & (1 << 10)
 
 
-@pytest.mark.parametrize("name,nsteps,rtol", [("kh100", 100, 1e-8), ("sedov16_periodic", 30, 1e-8),
+@pytest.mark.parametrize("name,nsteps,rtol", [("kh100", 100, 1e-8), ("kh24_gamma14", 50, 1e-8),
+                                              ("sedov16_periodic", 30, 1e-8),
                                               ("sedov16_nonperiodic", 40, 1e-8)])
 def test_multistep_density_l1(oracle_mod, name, nsteps, rtol):
     """Density after many steps: L1 relative difference to the oracle.  The
