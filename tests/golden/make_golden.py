@@ -27,6 +27,8 @@ Variants (abs binding, see oracle/build_ref.sh):
   kh24nolim_dbl kh24_dbl with SLOPE_LIMITING 0
   kh24pw_int    kh24pw_dbl with the int abs(int) binding (pairwise limiter,
                 Particles.cpp:1748-1759, and slope limiter)
+  kh24g14_dbl   kh24_dbl at gamma = 1.4 (set-up and configuration)
+  sedov12g14_dbl sedov12np_dbl at gamma = 1.4
 """
 import hashlib
 import os
@@ -110,6 +112,9 @@ def main(names):
         "kh24fix_dbl": lambda: full("kh24fix_dbl", "khfix_dbl", kh24(), 5),
         "kh24nolim_dbl": lambda: full("kh24nolim_dbl", "khnolim_dbl", kh24(), 5),
         "kh24pw_int": lambda: full("kh24pw_int", "khpw_int", kh24(), 5),
+        "kh24g14_dbl": lambda: full("kh24g14_dbl", "kh_dbl", ic.kelvin_helmholtz(n_side=24, seed=3, gamma=1.4), 5),
+        "sedov12g14_dbl": lambda: full("sedov12g14_dbl", "sedovnopw_dbl",
+                                       ic.sedov(n_side=12, seed=4, energy=0.05, gamma=1.4), 1),
     }
     for name in names or list(makers):
         makers[name]()

@@ -24,6 +24,9 @@ CASES = {
     "kh24fix_dbl": dict(kind="kh", move_particles=False),
     "kh24nolim_dbl": dict(kind="kh", slope_limiting=False),
     "kh24pw_int": dict(kind="kh", pairwise_limiter=True, int_abs=True),
+    # gamma = 1.4 (the fixture's own gamma): the general-gamma arithmetic
+    "kh24g14_dbl": dict(kind="kh"),
+    "sedov12g14_dbl": dict(kind="sedov", periodic=False, pairwise_limiter=False),
 }
 
 
