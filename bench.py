@@ -321,29 +321,47 @@ def cpu_baseline_sample(seconds_hint: float = 15.0, kind: str = "sedov"):
 
 
 def run_reference(args):
+    """The reference arm: the CPU restatement of the reference's step (the
+    reference's own sources are not on the GPU host) on every host core, on
+    the workload itself (for the ensemble, on one 100x100 KH member-sized
+    set-up), W untimed and K timed steps.  The reference is single-threaded;
+    the restatement's per-particle loops run on all cores with the same bits
+    (OpenMP), and its serial rate on a small sample is reported beside."""
     ws, rank, _ = dist_env()
     if rank != 0:
         return 0
     w = WORKLOADS[args.workload]
-    oracle, p, cfg, what = _oracle_sample("kh" if w["kind"] in ("kh", "ensemble") else "sedov")
-    o = oracle.Oracle(cfg, p)
-    for _ in range(args.warmup):
-        o.step()
-    t0 = time.perf_counter()
-    for _ in range(args.steps):
-        o.step()
-    el = time.perf_counter() - t0
+    oracle, ps, cfgs, what_s = _oracle_sample("kh" if w["kind"] in ("kh", "ensemble") else "sedov")
+    if w["kind"] == "ensemble":
+        p, cfg, what = ps, cfgs, what_s + " (one member-sized set-up)"
+    else:
+        p, cfg = make_workload(args.workload)
+        what = f"the {args.workload} workload itself"
+    n_threads = oracle.set_threads(0)
+    try:
+        o = oracle.Oracle(cfg, p)
+        for _ in range(args.warmup):
+            o.step()
+        t0 = time.perf_counter()
+        for _ in range(args.steps):
+            o.step()
+        el = time.perf_counter() - t0
+        o.close()
+    finally:
+        oracle.set_threads(1)
     val = p.n * args.steps / el
-    v_all, n_all = _time_oracle_all_threads(oracle, p, cfg, 5.0, max(args.steps, 2))
-    sample = (f"{what} ({p.n} particles, the workload's h/dx and neighbour count), one MFV step per step, "
-              f"serial CPU restatement of the reference (the reference is single-threaded), built -O3, "
-              f"DEBUG_LVL 0; all_threads_value: its per-particle loops on {n_all} threads")
+    serial_steps, serial_el = _time_oracle(oracle.Oracle(cfgs, ps), 5.0, max(args.steps, 2))
+    serial = ps.n * serial_steps / serial_el
+    sample = (f"{what} ({p.n} particles), one MFV step per step, CPU restatement of the reference built -O3, "
+              f"DEBUG_LVL 0, its per-particle loops on {n_threads} threads (the same bits as serial; the "
+              f"reference itself is single-threaded); serial_value: 1 thread on the {what_s} "
+              f"({ps.n} particles)")
     line = {"metric": METRIC, "value": val, "unit": "particle-updates/s", "n_gpus": ws, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": 1e3 * el / args.steps, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic", "impl": "reference",
             "config": {"workload": args.workload, "sample": sample},
-            "cpu_baseline": {"value": val, "unit": "particle-updates/s", "cores": 1, "kind": "port",
-                             "host_cores": host_cores(), "all_threads_value": v_all, "all_threads": n_all,
+            "cpu_baseline": {"value": val, "unit": "particle-updates/s", "cores": n_threads, "kind": "port",
+                             "host_cores": host_cores(), "serial_value": serial,
                              "sample": sample + f", host {cpu_model()}"},
             "e2e": {"value": val, "unit": "particle-updates/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
