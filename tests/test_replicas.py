@@ -65,7 +65,8 @@ def test_single_process_needs_no_collective():
 
 def test_reference_arm_prints_from_rank_zero_only():
     """bench.py --impl reference under torchrun with two ranks: rank 0 times
-    the serial CPU arm and prints one JSON line; rank 1 exits 0 without work."""
+    the CPU arm (the restatement on the host's threads, its serial rate
+    beside) and prints one JSON line; rank 1 exits 0 without work."""
     port = free_port()
     env = dict(os.environ, OMP_NUM_THREADS="1")
     r = subprocess.run([sys.executable, "-m", "torch.distributed.run", "--nnodes=1", "--nproc-per-node", "2",
@@ -79,4 +80,5 @@ def test_reference_arm_prints_from_rank_zero_only():
     line = lines[0]
     assert line["impl"] == "reference" and line["n_gpus"] == 2
     assert line["value"] > 0 and line["e2e"]["value"] == line["value"]
-    assert line["cpu_baseline"]["cores"] == 1 and line["cpu_baseline"]["kind"] == "port"
+    assert line["cpu_baseline"]["cores"] >= 1 and line["cpu_baseline"]["kind"] == "port"
+    assert line["cpu_baseline"]["serial_value"] > 0
