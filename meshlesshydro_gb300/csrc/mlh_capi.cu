@@ -144,9 +144,18 @@ void free_neighbour_buffers(mlh_ctx *c) {
     c->Fface = nullptr; c->fstate = nullptr; c->feat = nullptr; c->yguess = nullptr;
 }
 
+// Face ids and face offsets are 32-bit: the face table may hold at most
+// 2^31 - 1 faces (half the neighbour slots, plus one per particle).
+size_t face_capacity(long long n, int K) { return (size_t)n * (size_t)K / 2 + (size_t)n + 16; }
+constexpr size_t MAX_FACES = 0x7fffffff;
+
 int alloc_neighbour_buffers(mlh_ctx *c) {
     size_t slots = (size_t)c->n * c->p.K;
-    size_t faces = slots / 2 + (size_t)c->n + 16;
+    size_t faces = face_capacity(c->n, c->p.K);
+    if (faces > MAX_FACES) {
+        g_last_error = "too many faces for 32-bit face ids (particles x neighbour slots / 2 above 2^31 - 1)";
+        return MLH_ERR_CAPACITY;
+    }
     CK(dalloc(&c->nbr, slots));
     CK(dalloc(&c->rr, slots));
     CK(dalloc(&c->ww, slots));
@@ -391,6 +400,11 @@ static int create_impl(const mlh_config *cfg, int nmembers, const mlh_member *md
         return MLH_ERR_INVALID;
     }
     if (init->n > (int)IDX_MASK) { g_last_error = "too many particles"; return MLH_ERR_CAPACITY; }
+    if (face_capacity(init->n, round_slots(cfg->max_neighbours > 0 ? cfg->max_neighbours : (cfg->dim == 2 ? 40 : 64))) >
+        MAX_FACES) {
+        g_last_error = "too many faces for 32-bit face ids (particles x neighbour slots / 2 above 2^31 - 1)";
+        return MLH_ERR_CAPACITY;
+    }
     if (cfg->adaptive_h && !(sngb_target(cfg->dim, cfg->n_ngb) > 0.)) {
         g_last_error = "adaptive_h needs n_ngb above the particle's own count (32/3 in 3D, 40/7 in 2D)";
         return MLH_ERR_INVALID;

@@ -91,6 +91,11 @@ def test_create_rejects_empty_ragged_and_oversized_inputs():
     hs.view.n = (1 << 29)
     assert create(hs.view) == CAPACITY
     assert b"too many particles" in L.mlh_last_error()
+    # face ids are 32-bit: particles x neighbour slots / 2 + particles must
+    # stay below 2^31 (40 slots in 2D by default: 103 M particles is over)
+    hs.view.n = 103_000_000
+    assert create(hs.view) == CAPACITY
+    assert b"too many faces" in L.mlh_last_error()
 
     def ensemble(sizes, ks):
         descs = (runtime.MemberDesc * max(len(sizes), 1))()
