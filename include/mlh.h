@@ -120,7 +120,10 @@ const char *mlh_last_error(void);
 
 /* Particles(N) + InitialDistribution::getAllParticles + MeshlessScheme ctor
  * (demonstrator/src/MeshlessScheme.cpp:8-19): copies the initial state to the
- * device and allocates all per-particle and per-interaction buffers. */
+ * device and allocates all per-particle and per-interaction buffers.
+ * MLH_ERR_INVALID for an empty or incomplete view; MLH_ERR_CAPACITY for more
+ * than 2^29 - 1 particles (29-bit neighbour indices) or a face table above
+ * 2^31 - 1 faces (n x neighbour slots / 2 + n: 32-bit face ids). */
 int mlh_create(const mlh_config *cfg, const mlh_particles_view *init, mlh_ctx **out);
 void mlh_destroy(mlh_ctx *ctx);
 
