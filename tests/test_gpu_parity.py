@@ -97,12 +97,14 @@ def _totals(st, dim):
     import math
     return {"mass": math.fsum(m), "energy": math.fsum(E),
             **{f"p{a}": math.fsum(m * c) for a, c in zip("xyz", v)},
-            "pscale": math.fsum(m * np.sqrt(sum(c * c for c in v)))}
+            **{f"s{a}": math.fsum(np.abs(m * c)) for a, c in zip("xyz", v)}}
 
 
 @pytest.mark.parametrize("name", ["kh100", "sedov16_periodic"])
 def test_conservation(name):
-    """Mass and energy to 1e-13 relative per step; momentum relative to sum m|v|."""
+    """Mass and energy to 1e-13 relative per step; each momentum component
+    to 1e-13 of sum |m v_a| (the total itself is near zero: a symmetric blast,
+    counter-flowing KH layers), plus 1e-18 for a state at rest."""
     p, cfg = CASES[name]
     g = _sim(cfg, p)
     t0 = _totals(g.get_state(), cfg.dim)
@@ -112,7 +114,7 @@ def test_conservation(name):
         assert abs(t1["mass"] - t0["mass"]) <= 1e-13 * abs(t0["mass"])
         assert abs(t1["energy"] - t0["energy"]) <= 1e-13 * abs(t0["energy"])
         for a in "xyz"[:cfg.dim]:
-            assert abs(t1["p" + a] - t0["p" + a]) <= 1e-13 * max(t0["pscale"], 1e-300) + 1e-18
+            assert abs(t1["p" + a] - t0["p" + a]) <= 1e-13 * t0["s" + a] + 1e-18, a
         t0 = t1
 
 
