@@ -18,7 +18,9 @@ workload and on a many-blast workload full of strong shocks), per-particle
 smoothing lengths, and the 256-member Kelvin-Helmholtz ensemble batched
 against its members run one after another.  --impl reference times the CPU
 restatement of the reference's serial code (the oracle; the reference itself
-cannot be built on the GPU host) on a bounded sample of the same workload.
+cannot be built on the GPU host) on every host core, over the workload itself
+(a 100x100 KH member-sized set-up for the ensemble), with its serial rate on
+a small sample beside.
 """
 from __future__ import annotations
 
