@@ -293,6 +293,8 @@ class Simulation:
     """
 
     def __init__(self, cfg: MFVConfig, pset=None, members=None):
+        if pset is None and not members:
+            raise ValueError("Simulation needs a particle set or a list of members")
         self.L = load()
         self.cfg = cfg
         self._cfg = to_struct(cfg)
@@ -417,10 +419,14 @@ class Simulation:
         return {k: self.host.arrays[k].copy() for k in keys}
 
     def set_state(self, pset):
-        self.host = HostState(pset)
-        st = self.L.mlh_set_fields(self.h, ctypes.byref(self.host.view))
+        """Replace the state (mlh_set_fields); a particle count other than the
+        context's raises and leaves the context and its host buffers as they
+        were."""
+        host = HostState(pset)
+        st = self.L.mlh_set_fields(self.h, ctypes.byref(host.view))
         if st != 0:
             raise MLHError(st, "mlh_set_fields", self.L.mlh_last_error().decode())
+        self.host = host
 
     def get(self, name: str) -> np.ndarray:
         cnt = ctypes.c_longlong()

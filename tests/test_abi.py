@@ -115,3 +115,14 @@ def test_create_rejects_empty_ragged_and_oversized_inputs():
     assert ensemble([n // 2, n // 2 - 1], [0.1, 0.1]) == INVALID   # one particle left over
     assert b"add up" in L.mlh_last_error()
     assert ensemble([n // 2, n - n // 2 + 1], [0.1, 0.1]) == INVALID
+
+
+def test_simulation_needs_particles():
+    import pytest
+    from meshlesshydro_gb300.config import MFVConfig
+    from meshlesshydro_gb300 import ic
+    p = ic.kelvin_helmholtz(n_side=8, seed=1)
+    with pytest.raises(ValueError):
+        runtime.Simulation(MFVConfig.kelvin_helmholtz(p))
+    with pytest.raises(ValueError):
+        runtime.Simulation(MFVConfig.kelvin_helmholtz(p), members=[])
