@@ -89,3 +89,54 @@ def test_cli_help():
     assert r.returncode == 2 and "incompatible" in r.stderr
     r = subprocess.run([exe, "-c", "/nonexistent/config.info"], capture_output=True, text=True)
     assert r.returncode == 1 and "cannot open" in r.stderr
+
+
+C_PROGRAM = r"""
+#include <stdio.h>
+#include <string.h>
+#include "mlh.h"
+
+int main(void) {
+    double x[4] = {0.1, 0.2, 0.3, 0.4}, v[4] = {0., 0., 0., 0.}, m[4] = {1., 1., 1., 1.};
+    mlh_config cfg;
+    mlh_particles_view view;
+    mlh_ctx *ctx = NULL;
+    int st;
+    memset(&cfg, 0, sizeof cfg);
+    memset(&view, 0, sizeof view);
+    cfg.dim = 2;
+    cfg.periodic = 1;
+    cfg.kernel_size = 0.3;
+    cfg.gamma = 5. / 3.;
+    cfg.box_hi[0] = cfg.box_hi[1] = 1.;
+    view.n = 0;                          /* empty: rejected before the device */
+    view.x = view.y = x;
+    view.vx = view.vy = v;
+    view.m = view.u = m;
+    st = mlh_create(&cfg, &view, &ctx);
+    printf("%d %d %d %s\n", mlh_abi_version(), st == MLH_ERR_INVALID, ctx == NULL, mlh_last_error());
+    view.n = 4;
+    view.u = NULL;                       /* incomplete view */
+    st = mlh_create(&cfg, &view, &ctx);
+    printf("%d\n", st == MLH_ERR_INVALID);
+    return 0;
+}
+"""
+
+
+def test_c99_caller(tmp_path):
+    """A plain C99 program against include/mlh.h and libmlh.so (the binding
+    an FFI user writes): the ABI version and argument errors, no device."""
+    build.build()
+    cc = shutil.which("gcc")
+    if not cc:
+        pytest.skip("no C compiler")
+    src = tmp_path / "t.c"
+    src.write_text(C_PROGRAM)
+    exe = tmp_path / "t"
+    lib_dir = os.path.join(ROOT, "meshlesshydro_gb300")
+    subprocess.run([cc, "-std=c99", "-Wall", "-Wextra", "-pedantic", "-Werror", "-I", os.path.join(ROOT, "include"),
+                    str(src), "-o", str(exe), "-L", lib_dir, "-lmlh", "-Wl,-rpath," + lib_dir], check=True)
+    out = subprocess.run([str(exe)], check=True, capture_output=True, text=True).stdout.split("\n")
+    assert out[0].startswith("4 1 1 invalid configuration")
+    assert out[1] == "1"
